@@ -1,0 +1,1838 @@
+/*
+ * mks_oracle.c — serial CPU restatement of the MulSKIPS KMC program.
+ *
+ * TEST INFRASTRUCTURE ONLY (see mks_oracle.h).  This file restates the
+ * reference Fortran, routine by routine, on the same dense int32 bit-field
+ * grid.  Every routine cites the reference file:line it follows.  Paths are
+ * relative to the MulSKIPS project root; MS/ = mulskips-source/.
+ *
+ * Bit-exactness notes (all mirror the compiled reference):
+ *  - ran3 `fac` is the single-precision quotient 1./1e9 widened to double
+ *    (MS/mcevent/random.f:24,29).
+ *  - the test-mode uniforms are single-precision literals widened to double
+ *    (MS/mcevent/PickTreeEvent.f:77-1076); they are loaded from a fixture.
+ *  - the dummy rate of unsupported coor-1 sites is the single-precision
+ *    literal 1.e-8 (MS/mcevent/Get_Prob.f:183); Pi in FIND_NN is the
+ *    single-precision literal widened (MS/lattice/FIND_NN.f:27); the
+ *    arm-chair shift 8.6602254037 is single precision (FIND_SN.f:67).
+ *  - sum-tree parents are left+right recomputed bottom-up
+ *    (MS/mcevent/UpdateTree.f:49-65).
+ * Out-of-range reads that the Fortran performs silently (z<0 neighbours of a
+ * z=0 bulk layer, list index 0) read zero-filled guard storage here.
+ */
+#include "mks_oracle.h"
+
+#include <math.h>
+#include <setjmp.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <ctype.h>
+
+/* ---- bit layout, MS/modules/defsystem.f:87-91 ---- */
+#define POS_INDEX 0
+#define LEN_INDEX 8
+#define POS_T 9
+#define LEN_T 13
+#define POS_OCC 23
+#define LEN_OCC 1
+#define POS_COOR 24
+#define LEN_COOR 3
+#define POS_SIC 27
+#define LEN_SIC 3
+#define POS_SI 27
+#define POS_C 28
+#define WALL 113
+
+#define NCRYSTAL_MAX 3
+#define NCOV_MAX 3
+#define ZGUARD 8          /* zero planes below z=0 and above z=LenZ */
+
+typedef struct {
+    int xyz[3];
+    int nn[4][3];
+    int ind_event;
+    double prob;
+} mcp_t;                  /* MCParticle, MS/modules/defdertype.f:32-37 */
+
+typedef struct {
+    int xyz[3];
+    int nn[4][3];
+} blk_t;                  /* BulkParticle / Vacancy, defdertype.f:25-45 */
+
+typedef struct {
+    int xyz[3];
+    int ind_atype;
+} atbuf_t;                /* AtBuffer, defdertype.f:47-50 */
+
+/* ran3 (MS/mcevent/random.f:22-69) */
+typedef struct {
+    int ma[56];
+    int inext, inextp, iff;
+} ran3_t;
+
+struct ora {
+    int lx, ly, lz;
+    int32_t *latt_base, *latt;     /* LattCoo(0:lx-1,0:ly-1,0:lz) */
+    int32_t *lind_base, *lind;     /* LattInd */
+    /* lists (1-based, element 0 is a zero guard) */
+    mcp_t *mc; int num_mc, mc_max;          /* ListAdAtom, NumMcMax */
+    blk_t *bulk; int64_t num_bulk, bulk_cap, bulk_max;   /* ListAtom */
+    blk_t *voids; int num_void, void_max;   /* ListVoid */
+    atbuf_t *atbuf; int atbuf_cap;
+    double *tree; int levels, size_tree;
+    /* model */
+    int ncrystal, ncov;
+    int list_crystal[NCRYSTAL_MAX], list_cov[NCOV_MAX];
+    int count_crystal[NCRYSTAL_MAX], count_crystal_old[NCRYSTAL_MAX];
+    int count_cov[NCOV_MAX];
+    double ptransE[NCRYSTAL_MAX][4][4][4][4][4][4];
+    double ptransD[NCRYSTAL_MAX][3];
+    double ptransAbs[NCOV_MAX][4], ptransDes[NCOV_MAX][4];
+    double ptrans_zig;
+    double sf;
+    double alloyfraction;
+    /* LA law parameters (MS/modules/definitions.f:30) */
+    double Tm, P0, sigma, Tflex;
+    char init_st[3], run_type[3], exit_strategy[5];
+    char save_final[3], save_coo[3];
+    char restartfile[2048], coofile[2048];
+    int len1, len2, len3, len4;
+    int64_t max_iter, out_molmol;
+    double max_time, out_time;
+    int idum;
+    ran3_t rng;
+    int counter;                    /* test-mode list counter */
+    double numbers[1000];
+    int have_numbers;
+    /* loop state (MS/main.f:31-54) */
+    int64_t iter, iter_out, framecounter;
+    double time;
+    int started;
+    /* Evaporation's NBuff: a local of Evaporation.f:33 that is read even
+     * when not assigned in the same call; kept across calls here. */
+    int nbuff[3];
+    /* trace */
+    int trace_on;
+    ora_event_t *trace; int64_t trace_len, trace_cap;
+    int cur_arm;
+    /* log */
+    FILE *log;
+    jmp_buf jb;
+    char err[512];
+};
+
+static char g_err[512];
+const char *ora_last_error(void) { return g_err; }
+
+static void ora_fail(ora_t *o, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(o->err, sizeof o->err, fmt, ap);
+    va_end(ap);
+    snprintf(g_err, sizeof g_err, "%s", o->err);
+    longjmp(o->jb, 1);
+}
+
+static void lg(ora_t *o, const char *fmt, ...)
+{
+    if (!o->log) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vfprintf(o->log, fmt, ap);
+    va_end(ap);
+}
+
+/* ---- bit helpers: IBITS / MVBITS ---- */
+static inline int ibits(int32_t v, int pos, int len)
+{
+    return (int)(((uint32_t)v >> pos) & ((1u << len) - 1u));
+}
+static inline void mvbits(int from, int len, int32_t *to, int pos)
+{
+    uint32_t m = ((1u << len) - 1u) << pos;
+    *to = (int32_t)(((uint32_t)*to & ~m) | (((uint32_t)from << pos) & m));
+}
+
+static inline int64_t lidx(const ora_t *o, int x, int y, int z)
+{
+    return (int64_t)x + (int64_t)o->lx * ((int64_t)y + (int64_t)o->ly * (int64_t)z);
+}
+static inline int32_t *LC(ora_t *o, const int s[3]) { return &o->latt[lidx(o, s[0], s[1], s[2])]; }
+static inline int32_t *LI(ora_t *o, const int s[3]) { return &o->lind[lidx(o, s[0], s[1], s[2])]; }
+static inline int same3(const int a[3], const int b[3]) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
+static inline void cp3(int d[3], const int s[3]) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
+
+/* JumpDia, MS/modules/defsystem.f:104-105 (bond vectors of the two fcc
+ * sublattices; columns 1-4 for (x1+y1+z1) mod 4 == 0 sites, 5-8 for == 3). */
+static const int JUMPDIA[8][3] = {
+    {3, 3, 3}, {3, -3, -3}, {-3, -3, 3}, {-3, 3, -3},
+    {3, 3, -3}, {3, -3, 3}, {-3, -3, -3}, {-3, 3, 3}};
+
+/* ================= RNG: ran3, MS/mcevent/random.f:22-69 ================= */
+#define MBIG 1000000000
+#define MSEED 161803398
+#define MZ 0
+static double ran3_fac(void)
+{
+    volatile float f = 1.0f / (float)MBIG;   /* fac=1./Mbig, default real */
+    return (double)f;
+}
+static double ran3(ran3_t *r, int *idum)
+{
+    int mj, mk, i, ii, k;
+    if (*idum < 0 || r->iff == 0) {
+        r->iff = 1;
+        mj = MSEED - abs(*idum);
+        mj = mj % MBIG;
+        r->ma[55] = mj;
+        mk = 1;
+        for (i = 1; i <= 54; i++) {
+            ii = (21 * i) % 55;
+            r->ma[ii] = mk;
+            mk = mj - mk;
+            if (mk < MZ) mk += MBIG;
+            mj = r->ma[ii];
+        }
+        for (k = 1; k <= 4; k++)
+            for (i = 1; i <= 55; i++) {
+                r->ma[i] = r->ma[i] - r->ma[1 + (i + 30) % 55];
+                if (r->ma[i] < MZ) r->ma[i] += MBIG;
+            }
+        r->inext = 0;
+        r->inextp = 31;
+        *idum = 1;
+    }
+    r->inext++;
+    if (r->inext == 56) r->inext = 1;
+    r->inextp++;
+    if (r->inextp == 56) r->inextp = 1;
+    mj = r->ma[r->inext] - r->ma[r->inextp];
+    if (mj < MZ) mj += MBIG;
+    r->ma[r->inext] = mj;
+    return (double)mj * ran3_fac();
+}
+static double rnd(ora_t *o) { return ran3(&o->rng, &o->idum); }
+
+void ora_ran3_sequence(int idum, int n, double *out)
+{
+    ran3_t r;
+    memset(&r, 0, sizeof r);
+    for (int i = 0; i < n; i++) out[i] = ran3(&r, &idum);
+}
+
+/* ============ sum-tree: MS/mcevent/UpdateTree.f:25-66 ============ */
+static void update_tree(ora_t *o, int index, double patom)
+{
+    if (patom == 0.0 && index < o->num_mc)
+        ora_fail(o, "error stabilizzato da dentro Update! %d", index);
+    else if (index > o->num_mc)
+        ora_fail(o, "Index > NumAdAtom %d %d", index, o->num_mc);
+    int pos = index + (1 << (o->levels - 1)) - 1;
+    o->tree[pos] = patom;
+    for (int parent = o->levels - 1; parent >= 1; parent--) {
+        int neigh = (pos & 1) ? pos - 1 : pos + 1;
+        int np = pos >> 1;
+        o->tree[np] = o->tree[pos] + o->tree[neigh];
+        pos = np;
+    }
+}
+
+/* AllocateArrays, MS/mcevent/AllocateArrays.f:24-45 */
+static void allocate_arrays(ora_t *o)
+{
+    int lev = 0;
+    for (int ind = 0; ind <= 31; ind++)
+        if ((o->mc_max >> ind) & 1) lev = ind;
+    if (o->mc_max > (1 << lev)) lev += 2; else lev += 1;
+    o->levels = lev;
+    o->size_tree = (1 << lev) - 1;
+    free(o->tree);
+    o->tree = (double *)calloc((size_t)o->size_tree + 2, sizeof(double));
+    if (!o->tree) ora_fail(o, "tree allocation failed");
+    lg(o, " numParticelle= %d Levels = %d , SizeTree = %d\n", o->mc_max, o->levels, o->size_tree);
+}
+
+/* PickTreeEvent, MS/mcevent/PickTreeEvent.f:25-70 */
+static int pick_tree_event(ora_t *o, double *patom)
+{
+    int index = 1;
+    for (int parent = 1; parent <= o->levels - 1; parent++) {
+        double u;
+        if (o->run_type[0] == 'T') {
+            o->counter++;
+            u = o->numbers[(o->counter - 1) % 1000];
+        } else {
+            u = rnd(o);
+        }
+        *patom = u * o->tree[index];
+        index <<= 1;
+        if (o->tree[index] < *patom) index++;
+    }
+    *patom = o->tree[index];
+    if (index - (1 << (o->levels - 1)) + 1 > o->num_mc)
+        ora_fail(o, "write Index> NumAdAtom");
+    return index - (1 << (o->levels - 1)) + 1;
+}
+
+/* ============ lists: MS/mcevent/Add.f, Erase.f ============ */
+static void add_mc(ora_t *o, const int site[3], int nextn[4][3], int ind_event, double prob)
+{   /* Add.f:24-52 */
+    if (prob == 0.0) ora_fail(o, "provo ad aggiungere prob nulla");
+    o->num_mc++;
+    if (o->num_mc >= o->mc_max) ora_fail(o, "troppe particelle cinetiche %d", o->num_mc);
+    *LI(o, site) = o->num_mc;
+    mcp_t *p = &o->mc[o->num_mc];
+    cp3(p->xyz, site);
+    memcpy(p->nn, nextn, sizeof p->nn);
+    p->ind_event = ind_event;
+    p->prob = prob;
+    update_tree(o, o->num_mc, prob);
+}
+
+static void add_bulk(ora_t *o, const int site[3], int nextn[4][3])
+{   /* Add.f:57-76 */
+    o->num_bulk++;
+    if (o->num_bulk >= o->bulk_max) ora_fail(o, "troppe particelle bulk");
+    if (o->num_bulk >= o->bulk_cap) {
+        int64_t nc = o->bulk_cap * 2;
+        blk_t *nb = (blk_t *)realloc(o->bulk, (size_t)nc * sizeof(blk_t));
+        if (!nb) ora_fail(o, "bulk list allocation failed");
+        memset(nb + o->bulk_cap, 0, (size_t)(nc - o->bulk_cap) * sizeof(blk_t));
+        o->bulk = nb;
+        o->bulk_cap = nc;
+    }
+    *LI(o, site) = (int32_t)o->num_bulk;
+    cp3(o->bulk[o->num_bulk].xyz, site);
+    memcpy(o->bulk[o->num_bulk].nn, nextn, sizeof(int) * 12);
+}
+
+static void add_void(ora_t *o, const int site[3], int nextn[4][3])
+{   /* Add.f:82-101 */
+    o->num_void++;
+    if (o->num_void >= o->void_max) ora_fail(o, "troppe vacanze");
+    *LI(o, site) = o->num_void;
+    cp3(o->voids[o->num_void].xyz, site);
+    memcpy(o->voids[o->num_void].nn, nextn, sizeof(int) * 12);
+}
+
+static void erase_mc(ora_t *o, const int site[3])
+{   /* Erase.f:24-76 */
+    if (site[2] == -1) ora_fail(o, "accesso a latt fuori bond");
+    int ind = *LI(o, site);
+    if (ind > o->mc_max || ind == 0) ora_fail(o, "err: EraseMC %d %d %d %d", ind, site[0], site[1], site[2]);
+    if (ind >= o->num_mc) {
+        memset(&o->mc[ind], 0, sizeof(mcp_t));
+        *LI(o, site) = 0;
+        update_tree(o, ind, 0.0);
+        o->num_mc--;
+    } else {
+        o->mc[ind] = o->mc[o->num_mc];
+        int leaf = o->num_mc + (1 << (o->levels - 1)) - 1;
+        update_tree(o, ind, o->tree[leaf]);
+        update_tree(o, o->num_mc, 0.0);
+        int st[3];
+        cp3(st, o->mc[o->num_mc].xyz);
+        *LI(o, st) = ind;
+        memset(&o->mc[o->num_mc], 0, sizeof(mcp_t));
+        *LI(o, site) = 0;
+        o->num_mc--;
+    }
+}
+
+static void erase_bulk(ora_t *o, const int site[3])
+{   /* Erase.f:82-127 */
+    if (site[2] == -1) ora_fail(o, "accesso a latt fuori bond");
+    int64_t ind = *LI(o, site);
+    if (ind > o->bulk_max || ind == 0) ora_fail(o, "err: EraseBulk");
+    if (ind == o->num_bulk) {
+        memset(&o->bulk[o->num_bulk], 0, sizeof(blk_t));
+        *LI(o, site) = 0;
+        o->num_bulk--;
+    } else {
+        o->bulk[ind] = o->bulk[o->num_bulk];
+        int st[3];
+        cp3(st, o->bulk[o->num_bulk].xyz);
+        *LI(o, st) = (int32_t)ind;
+        memset(&o->bulk[o->num_bulk], 0, sizeof(blk_t));
+        *LI(o, site) = 0;
+        o->num_bulk--;
+    }
+}
+
+static void erase_void(ora_t *o, const int site[3])
+{   /* Erase.f:134-179 */
+    if (site[2] == -1) ora_fail(o, "accesso a latt fuori bond");
+    int ind = *LI(o, site);
+    if (ind > o->void_max || ind == 0) ora_fail(o, "err: EraseVoid");
+    if (ind == o->num_void) {
+        memset(&o->voids[o->num_void], 0, sizeof(blk_t));
+        *LI(o, site) = 0;
+        o->num_void--;
+    } else {
+        o->voids[ind] = o->voids[o->num_void];
+        int st[3];
+        cp3(st, o->voids[o->num_void].xyz);
+        *LI(o, st) = ind;
+        memset(&o->voids[o->num_void], 0, sizeof(blk_t));
+        *LI(o, site) = 0;
+        o->num_void--;
+    }
+}
+
+/* ============ rate tables ============ */
+static const double KB = 0.00008617330350;   /* Get_Prob.f:70 */
+
+/* PE(...) entry; the LA law of Get_Prob.f:127-149 is evaluated per element,
+ * which equals recomputing the whole table and reading one entry. */
+static double pe_entry(ora_t *o, int s, int i1, int i2, int i3, int i4, int i5, int i6, int temperature)
+{
+    double v = o->ptransE[s - 1][i1][i2][i3][i4][i5][i6];
+    if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
+        double e = o->P0 * exp(-v / (KB * (double)temperature));
+        return e * (v != 0.0 ? 1.0 : 0.0);
+    }
+    return v;
+}
+static double pd_entry(ora_t *o, int s, int coor, int temperature)
+{
+    double v = o->ptransD[s - 1][coor - 1];
+    if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
+        double e = 0.5 * o->P0 * exp(-v / (KB * o->Tm)) *
+                   (1.0 + erf(((double)temperature - o->Tflex) / o->sigma));
+        return e * (v != 0.0 ? 1.0 : 0.0);
+    }
+    return v;
+}
+
+/* IndexEvent_Abs, MS/mcevent/Get_Prob.f:22-52 */
+static int index_event_abs(ora_t *o, int coor, double ptmp, double pdepo)
+{
+    int res = 0;
+    if (o->ncov == 1) return 6;
+    for (int i = 1; i <= o->ncov; i++) {
+        double pmin, pmax, s = 0.0;
+        if (i == 1) {
+            pmin = pdepo;
+            pmax = pdepo + o->ptransAbs[0][coor];
+        } else {
+            for (int k = 0; k < i - 1; k++) s += o->ptransAbs[k][coor];
+            pmin = pdepo + s;
+            s = 0.0;
+            for (int k = 0; k < i; k++) s += o->ptransAbs[k][coor];
+            pmax = pdepo + s;
+        }
+        if (ptmp > pmin && ptmp <= pmax) res = 5 + i;
+    }
+    return res;
+}
+
+static double sum_abs(ora_t *o, int coor)
+{   /* SUM(PtransAbs(:,Coor)) over NCovMax entries */
+    double s = 0.0;
+    for (int k = 0; k < NCOV_MAX; k++) s += o->ptransAbs[k][coor];
+    return s;
+}
+
+static void get_nn_list(ora_t *o, int ind, int which, int out[4][3])
+{
+    if (which == 1) memcpy(out, o->mc[ind].nn, sizeof(int) * 12);
+    else memcpy(out, o->bulk[ind].nn, sizeof(int) * 12);
+}
+
+static int in_list(int nn[4][3], const int site[3])
+{
+    int r = 0;
+    for (int j = 0; j < 4; j++)
+        if (same3(nn[j], site)) r = 1;
+    return r;
+}
+
+/* Get_Prob, MS/mcevent/Get_Prob.f:54-331 */
+static void get_prob(ora_t *o, int occ, int nsic, int covind, int coor,
+                     const int site[3], int nextn[4][3], int *index_event, double *prob_event)
+{
+    int temperature = 0;
+    int la = (o->init_st[0] == 'L' && o->init_st[1] == 'A');
+    if (la) {
+        temperature = ibits(*LC(o, site), POS_T, LEN_T);
+        if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob()");
+    }
+    if (covind > 0 && covind < WALL) {            /* desorption, :91-119 */
+        if (occ != 0) ora_fail(o, "ERROR Covind!=0 with Occ!=0 in get_prob");
+        if (coor <= 3) {
+            *index_event = 5;
+            int icov = 0;
+            for (int j = 1; j <= o->ncov; j++)
+                if (o->list_cov[j - 1] == covind) { icov = j; break; }
+            if (icov == 0) ora_fail(o, "ERROR: could not find CovInd=%d inside ListCov", covind);
+            *prob_event = o->ptransDes[icov - 1][coor];
+        } else {
+            *index_event = 0;
+            *prob_event = 0.0;
+            if (coor > 4) lg(o, " anomalous coordination in desorption\n");
+        }
+    } else if (occ == 0) {                       /* :154-214 */
+        if (coor == 1) {
+            int coornn = ibits(*LC(o, nextn[0]), POS_COOR, LEN_COOR);
+            if (coornn >= 2) {
+                double pd1 = pd_entry(o, 1, coor, temperature);
+                double pd2 = pd_entry(o, 2, coor, temperature);
+                double pd3 = pd_entry(o, 3, coor, temperature);
+                double pdep = pd1 + pd2 + pd3;
+                double pabs = sum_abs(o, coor);
+                double ptot = pdep + pabs;
+                double pcurr = rnd(o) * ptot;
+                if (pcurr <= pdep) {
+                    if (pcurr <= pd1) *index_event = 1;
+                    else if (pcurr > pd1 + pd2) *index_event = 3;
+                    else *index_event = 2;
+                } else {
+                    *index_event = index_event_abs(o, coor, pcurr, pdep);
+                }
+                *prob_event = ptot;
+            } else {
+                *index_event = 1;
+                *prob_event = (double)1.e-8f;
+            }
+        } else if (coor == 2 || coor == 3) {
+            double pd1 = pd_entry(o, 1, coor, temperature);
+            double pd2 = pd_entry(o, 2, coor, temperature);
+            double pd3 = pd_entry(o, 3, coor, temperature);
+            double pdep = pd1 + pd2 + pd3;
+            double pabs = sum_abs(o, coor);
+            double ptot = pdep + pabs;
+            double pcurr = rnd(o) * ptot;
+            if (pcurr <= pdep) {
+                if (pcurr <= pd1) *index_event = 1;
+                else if (pcurr > pd1 + pd2) *index_event = 3;
+                else *index_event = 2;
+            } else {
+                *index_event = index_event_abs(o, coor, pcurr, pdep);
+            }
+            *prob_event = ptot;
+        } else if (coor >= 4) {
+            *index_event = 0;
+            *prob_event = 0.0;
+            if (coor > 4) lg(o, " anomalous coordination\n");
+        } else {
+            lg(o, " anomalous coordination %d\n", coor);
+        }
+    } else {                                      /* occupied, :215-323 */
+        int n_si = 0, n_c = 0, n_b = 0, n_wall = 0;
+        int covnn[NCOV_MAX] = {0, 0, 0};
+        for (int i = 0; i < 4; i++) {
+            int32_t v = *LC(o, nextn[i]);
+            int occn = ibits(v, POS_OCC, LEN_OCC);
+            int covindn = ibits(v, POS_INDEX, LEN_INDEX);
+            int coornn = ibits(v, POS_COOR, LEN_COOR);
+            if (occn != 0) {
+                if (covindn != WALL) {
+                    int indnn = *LI(o, nextn[i]);
+                    int nnn[4][3];
+                    get_nn_list(o, indnn, (coornn >= 1 && coornn <= 3) ? 1 : 2, nnn);
+                    if (in_list(nnn, site)) {
+                        int sioc = ibits(v, POS_SIC, LEN_SIC);
+                        if (sioc == 1) n_si++;
+                        if (sioc == 2) n_c++;
+                        if (sioc == 3) n_b++;
+                    }
+                } else {
+                    n_wall++;
+                }
+            } else if (covindn != 0) {
+                int indnn = *LI(o, nextn[i]);
+                int nnn[4][3];
+                get_nn_list(o, indnn, 1, nnn);
+                if (in_list(nnn, site)) {
+                    int icov = 0;
+                    for (int j = 1; j <= o->ncov; j++)
+                        if (o->list_cov[j - 1] == covindn) { icov = j; break; }
+                    if (icov == 0) ora_fail(o, "ERROR: could not find CovIndN=%d inside ListCov", covindn);
+                    covnn[icov - 1]++;
+                }
+            }
+        }
+        int tot = n_si + n_c + n_b + n_wall;
+        if (tot != coor)
+            ora_fail(o, "Get Prob Error N_Si+N_C+N_B+N_wall.NE.Coor at %d %d %d (coor %d, census %d)",
+                     site[0], site[1], site[2], coor, tot);
+        if (tot > 3) {
+            *index_event = 0;
+            *prob_event = 0.0;
+        } else if (tot == 0) {
+            *index_event = 4;
+            *prob_event = 100000.0 * o->tree[1];
+        } else {
+            *index_event = 4;
+            int c1 = 0, c2 = 0, c3 = 0;
+            if (o->ncov >= 1) c1 = covnn[0];
+            if (o->ncov >= 2) c2 = covnn[1];
+            if (o->ncov >= 3) c3 = covnn[2];
+            *prob_event = pe_entry(o, nsic, n_si + n_wall, n_c, n_b, c1, c2, c3, temperature);
+        }
+    }
+    if (*index_event != 0 && *prob_event < (double)1e-12f)
+        lg(o, " %d %.17g %d\n", *index_event, *prob_event, coor);
+}
+
+/* ============ geometry: MS/lattice/FIND_SN.f, FIND_NN.f ============ */
+static int isign_f(int a, int b) { int m = abs(a); return b >= 0 ? m : -m; }
+
+/* FIND_SN, MS/lattice/FIND_SN.f:26-84 */
+static void find_sn(const int site[3], const int sitec_in[3], int sn_in[4][3],
+                    int zig[3][3], int arm[3][3], int lx, int ly)
+{
+    int sn[3][3], sitec[3];
+    for (int i = 0; i < 3; i++) cp3(sn[i], sn_in[i]);
+    cp3(sitec, sitec_in);
+    if (abs(site[0] - sitec[0]) > lx / 2) sitec[0] += isign_f(lx, site[0] - sitec[0]);
+    if (abs(site[1] - sitec[1]) > ly / 2) sitec[1] += isign_f(ly, site[1] - sitec[1]);
+    for (int i = 0; i < 3; i++) {
+        if (abs(site[0] - sn[i][0]) > lx / 2) sn[i][0] += isign_f(lx, site[0] - sn[i][0]);
+        if (abs(site[1] - sn[i][1]) > ly / 2) sn[i][1] += isign_f(ly, site[1] - sn[i][1]);
+    }
+    double cent[3], ax[3];
+    for (int k = 0; k < 3; k++) {
+        cent[k] = 0.5 * ((double)sitec[k] + (double)(float)site[k]);
+        ax[k] = (double)site[k] - (double)sitec[k];
+    }
+    double snorm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    for (int k = 0; k < 3; k++) ax[k] = ax[k] / snorm;
+    const double shift = (double)8.6602254037f;
+    for (int i = 0; i < 3; i++) {
+        for (int k = 0; k < 3; k++) {
+            double rz = 2.0 * cent[k] - (double)sn[i][k];
+            double ra = (double)sn[i][k] + shift * ax[k];
+            zig[i][k] = (int)lround(rz);
+            arm[i][k] = (int)lround(ra);
+        }
+        if (zig[i][0] >= lx) zig[i][0] -= lx;
+        if (zig[i][0] < 0) zig[i][0] += lx;
+        if (zig[i][1] >= ly) zig[i][1] -= ly;
+        if (zig[i][1] < 0) zig[i][1] += ly;
+        if (arm[i][0] >= lx) arm[i][0] -= lx;
+        if (arm[i][0] < 0) arm[i][0] += lx;
+        if (arm[i][1] >= ly) arm[i][1] -= ly;
+        if (arm[i][1] < 0) arm[i][1] += ly;
+    }
+}
+
+/* FIND_NN, MS/lattice/FIND_NN.f:25-77 */
+static void find_nn(const int site1[3], const int site2[3], const int sitec[3],
+                    int newsite[2][3], int lx, int ly)
+{
+    const double pi = (double)3.14159265358979323f;
+    int s11[3], s22[3];
+    cp3(s11, site1);
+    cp3(s22, site2);
+    if (abs(sitec[0] - s11[0]) > lx / 2) s11[0] += isign_f(lx, sitec[0] - s11[0]);
+    if (abs(sitec[1] - s11[1]) > ly / 2) s11[1] += isign_f(ly, sitec[1] - s11[1]);
+    if (abs(sitec[0] - s22[0]) > lx / 2) s22[0] += isign_f(lx, sitec[0] - s22[0]);
+    if (abs(sitec[1] - s22[1]) > ly / 2) s22[1] += isign_f(ly, sitec[1] - s22[1]);
+    double ax[3];
+    for (int k = 0; k < 3; k++) ax[k] = (double)sitec[k] - (double)s11[k];
+    double snorm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    for (int k = 0; k < 3; k++) ax[k] = ax[k] / snorm;
+    for (int irot = 1; irot <= 2; irot++) {
+        double cth = cos((double)(2 * irot) * pi / 3.0);
+        double sth = sin((double)(2 * irot) * pi / 3.0);
+        double rot[3][3];   /* rot[i][j] = Rot(i+1,j+1) */
+        for (int i = 0; i < 3; i++) rot[i][i] = ax[i] * ax[i] * (1.0 - cth) + cth;
+        rot[1][0] = ax[0] * ax[1] * (1.0 - cth) - ax[2] * sth;
+        rot[0][1] = ax[0] * ax[1] * (1.0 - cth) + ax[2] * sth;
+        rot[2][0] = ax[0] * ax[2] * (1.0 - cth) + ax[1] * sth;
+        rot[0][2] = ax[0] * ax[2] * (1.0 - cth) - ax[1] * sth;
+        rot[2][1] = ax[1] * ax[2] * (1.0 - cth) - ax[0] * sth;
+        rot[1][2] = ax[1] * ax[2] * (1.0 - cth) + ax[0] * sth;
+        for (int k = 0; k < 3; k++) {
+            double r = 0.0;
+            for (int l = 0; l < 3; l++)
+                r = r + rot[l][k] * ((double)s22[l] - (double)sitec[l]);
+            newsite[irot - 1][k] = (int)lround(r) + sitec[k];
+        }
+        int *ns = newsite[irot - 1];
+        if (ns[0] >= lx) ns[0] -= lx;
+        if (ns[0] < 0) ns[0] += lx;
+        if (ns[1] >= ly) ns[1] -= ly;
+        if (ns[1] < 0) ns[1] += ly;
+    }
+}
+
+/* IF_Arm_Choice, MS/mcevent/IF_Arm_Choice.f:21-56 */
+static int if_arm_choice(ora_t *o, int zig[3][3], int arm[3][3])
+{
+    int ca = 0, cz = 0;
+    for (int i = 0; i < 3; i++) {
+        ca += ibits(*LC(o, arm[i]), POS_COOR, LEN_COOR);
+        cz += ibits(*LC(o, zig[i]), POS_COOR, LEN_COOR);
+    }
+    if (cz > ca) return 0;
+    if (cz == ca) return (rnd(o) <= o->ptrans_zig) ? 0 : 1;
+    return 1;
+}
+
+/* ============ events ============ */
+/* Deposition, MS/mcevent/deposition.f:24-251 */
+static void deposition(ora_t *o, int indvoid, int iatom)
+{
+    int site[3], nextn[4][3], nextnn[4][3], nextnnn[4][3];
+    int index_event;
+    double prob;
+    cp3(site, o->mc[indvoid].xyz);
+    int32_t *ls = LC(o, site);
+    int coor = ibits(*ls, POS_COOR, LEN_COOR);
+    int coor_old = coor;
+    mvbits(1, LEN_OCC, ls, POS_OCC);
+    mvbits(iatom, LEN_SIC, ls, POS_SIC);
+    o->cur_arm = 0;
+    if (coor == 1) {                              /* :49-74 */
+        int sitec[3];
+        cp3(sitec, o->mc[indvoid].nn[0]);
+        int indnn = *LI(o, sitec);
+        int snsite[4][3];
+        memset(snsite, 0, sizeof snsite);
+        int j = 0;
+        for (int i = 0; i < 4; i++) {
+            if (!same3(o->mc[indnn].nn[i], site)) {
+                if (j < 4) cp3(snsite[j], o->mc[indnn].nn[i]);
+                j++;
+            }
+        }
+        int zig[3][3], arm[3][3];
+        find_sn(site, sitec, snsite, zig, arm, o->lx, o->ly);
+        int if_arm = if_arm_choice(o, zig, arm);
+        o->cur_arm = if_arm;
+        for (int i = 0; i < 3; i++) cp3(o->mc[indvoid].nn[i + 1], if_arm ? arm[i] : zig[i]);
+    }
+    memcpy(nextn, o->mc[indvoid].nn, sizeof nextn);
+    for (int i = 0; i < 4; i++) {                 /* :78-235 */
+        int32_t *ln = LC(o, nextn[i]);
+        int occ = ibits(*ln, POS_OCC, LEN_OCC);
+        int indnn = *LI(o, nextn[i]);
+        int coornn = ibits(*ln, POS_COOR, LEN_COOR);
+        int covind = ibits(*ln, POS_INDEX, LEN_INDEX);
+        memset(nextnn, 0, sizeof nextnn);
+        if (occ == 0) {
+            if (coornn == 0) {
+                coornn = 1;
+                mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                cp3(nextnn[0], site);
+                get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                if (index_event != 0) add_mc(o, nextn[i], nextnn, index_event, prob);
+            } else if (coornn == 1) {
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                int dx = abs(nextnn[0][0] - site[0]);
+                if (o->lx - dx < dx) dx = o->lx - dx;
+                int dy = abs(nextnn[0][1] - site[1]);
+                if (o->ly - dy < dy) dy = o->ly - dy;
+                int dz = nextnn[0][2] - site[2];
+                int dis = dx * dx + dy * dy + dz * dz;
+                if (dis == 72) {
+                    coornn = 2;
+                    cp3(nextnn[1], site);
+                    int newsite[2][3];
+                    find_nn(nextnn[0], nextnn[1], nextn[i], newsite, o->lx, o->ly);
+                    for (int j = 2; j < 4; j++) {
+                        cp3(nextnn[j], newsite[j - 2]);
+                        int32_t v = *LC(o, nextnn[j]);
+                        int occn = ibits(v, POS_OCC, LEN_OCC);
+                        if (occn != 0) {
+                            int coornnn = ibits(v, POS_COOR, LEN_COOR);
+                            int covindnnn = ibits(v, POS_INDEX, LEN_INDEX);
+                            if (coornnn <= 3 && covindnnn != WALL) {
+                                int indnnn = *LI(o, nextnn[j]);
+                                memcpy(nextnnn, o->mc[indnnn].nn, sizeof nextnnn);
+                                if (in_list(nextnnn, nextn[i])) coornn++;
+                            }
+                        }
+                    }
+                    mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                    memcpy(o->mc[indnn].nn, nextnn, sizeof nextnn);
+                    get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                    if (index_event == 0) {
+                        erase_mc(o, nextn[i]);
+                        add_void(o, nextn[i], nextnn);
+                    } else {
+                        o->mc[indnn].ind_event = index_event;
+                        o->mc[indnn].prob = prob;
+                        update_tree(o, indnn, prob);
+                    }
+                }
+            } else if (coornn == 2 || coornn == 3) {
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    coornn++;
+                    mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                    get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                    if (index_event == 0) {
+                        erase_mc(o, nextn[i]);
+                        add_void(o, nextn[i], nextnn);
+                    } else {
+                        o->mc[indnn].ind_event = index_event;
+                        o->mc[indnn].prob = prob;
+                        update_tree(o, indnn, prob);
+                    }
+                }
+            }
+        } else {
+            if (covind != WALL) {
+                if (covind != 0) ora_fail(o, "ERROR in deposition: Site can only have NN with CovInd=0 or 113 when its Occ=1");
+                if (coornn <= 3) {
+                    memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                    if (in_list(nextnn, site)) {
+                        coornn++;
+                        mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                        int sioc = ibits(*ln, POS_SIC, LEN_SIC);
+                        get_prob(o, 1, sioc, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                        if (index_event == 0) {
+                            erase_mc(o, nextn[i]);
+                            add_bulk(o, nextn[i], nextnn);
+                        } else {
+                            o->mc[indnn].ind_event = index_event;
+                            o->mc[indnn].prob = prob;
+                            update_tree(o, indnn, prob);
+                        }
+                        if (coor_old == 1 && i >= 1) coor++;
+                    }
+                }
+            } else {
+                coor++;
+            }
+        }
+    }
+    indvoid = *LI(o, site);                       /* :236-250 */
+    if (coor != coor_old) mvbits(coor, LEN_COOR, ls, POS_COOR);
+    get_prob(o, 1, iatom, 0, coor, site, nextn, &index_event, &prob);
+    if (index_event == 0) {
+        erase_mc(o, site);
+        add_bulk(o, site, nextn);
+    } else {
+        o->mc[indvoid].ind_event = index_event;
+        o->mc[indvoid].prob = prob;
+        update_tree(o, indvoid, prob);
+    }
+}
+
+/* Evaporation, MS/mcevent/Evaporation.f:25-262 */
+static void evaporation(ora_t *o, int indatom)
+{
+    int site[3], nextn[4][3], nextnn[4][3], nextnnn[4][3];
+    int index_event;
+    double prob;
+    int la_or_st = (o->init_st[0] == 'L' && o->init_st[1] == 'A') ||
+                   (o->init_st[0] == 'S' && o->init_st[1] == 'T');
+    cp3(site, o->mc[indatom].xyz);
+    int32_t *ls = LC(o, site);
+    int iatom = ibits(*ls, POS_SIC, LEN_SIC);
+    if (iatom >= 1 && iatom <= NCRYSTAL_MAX) o->count_crystal[iatom - 1]--;
+    int coor = ibits(*ls, POS_COOR, LEN_COOR);
+    mvbits(0, LEN_OCC, ls, POS_OCC);
+    mvbits(0, LEN_SIC, ls, POS_SIC);
+    memcpy(nextn, o->mc[indatom].nn, sizeof nextn);
+    for (int i = 0; i < 4; i++) {
+        int32_t *ln = LC(o, nextn[i]);
+        int occ = ibits(*ln, POS_OCC, LEN_OCC);
+        int coornn = ibits(*ln, POS_COOR, LEN_COOR);
+        int indnn = *LI(o, nextn[i]);
+        int covind = ibits(*ln, POS_INDEX, LEN_INDEX);
+        memset(nextnn, 0, sizeof nextnn);
+        if (occ == 0) {
+            if (coornn == 1) {                    /* :51-68 */
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    erase_mc(o, nextn[i]);
+                    if (la_or_st) {
+                        int t = ibits(*ln, POS_T, LEN_T);
+                        *ln = 0;
+                        mvbits(t, LEN_T, ln, POS_T);
+                    } else {
+                        *ln = 0;
+                    }
+                }
+            } else if (coornn == 2) {             /* :69-123 */
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    coornn = 1;
+                    mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                    for (int j = 0; j < 4; j++) {
+                        int32_t v = *LC(o, nextnn[j]);
+                        int occn = ibits(v, POS_OCC, LEN_OCC);
+                        if (occn == 0) {
+                            memset(o->mc[indnn].nn[j], 0, sizeof(int) * 3);
+                        } else {
+                            int coornnn = ibits(v, POS_COOR, LEN_COOR);
+                            int covindnn = ibits(v, POS_INDEX, LEN_INDEX);
+                            if (coornnn <= 3 && covindnn != WALL) {
+                                int indnnn = *LI(o, nextnn[j]);
+                                memcpy(nextnnn, o->mc[indnnn].nn, sizeof nextnnn);
+                                if (in_list(nextnnn, nextn[i]))
+                                    cp3(o->nbuff, o->mc[indnn].nn[j]);
+                            }
+                            memset(o->mc[indnn].nn[j], 0, sizeof(int) * 3);
+                        }
+                    }
+                    cp3(o->mc[indnn].nn[0], o->nbuff);
+                    get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                    o->mc[indnn].ind_event = index_event;
+                    o->mc[indnn].prob = prob;
+                    update_tree(o, indnn, prob);
+                }
+            } else if (coornn == 3) {             /* :124-141 */
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    coornn = 2;
+                    mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                    get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                    o->mc[indnn].ind_event = index_event;
+                    o->mc[indnn].prob = prob;
+                    update_tree(o, indnn, prob);
+                }
+            } else if (coornn == 4) {             /* :142-164 */
+                memcpy(nextnn, o->voids[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    coornn = 3;
+                    mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                    get_prob(o, 0, 0, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                    erase_void(o, nextn[i]);
+                    add_mc(o, nextn[i], nextnn, index_event, prob);
+                }
+            }
+        } else {
+            if (covind != WALL) {                 /* :166-210 */
+                if (covind != 0) ora_fail(o, "ERROR in evaporation: NN with CovInd not 0/113 and Occ=1");
+                if (coornn == 4) {
+                    memcpy(nextnn, o->bulk[indnn].nn, sizeof nextnn);
+                    if (in_list(nextnn, site)) {
+                        coornn = 3;
+                        mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                        int sioc = ibits(*ln, POS_SIC, LEN_SIC);
+                        get_prob(o, 1, sioc, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                        erase_bulk(o, nextn[i]);
+                        add_mc(o, nextn[i], nextnn, index_event, prob);
+                    }
+                } else {
+                    memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                    if (in_list(nextnn, site)) {
+                        coornn--;
+                        mvbits(coornn, LEN_COOR, ln, POS_COOR);
+                        int sioc = ibits(*ln, POS_SIC, LEN_SIC);
+                        get_prob(o, 1, sioc, covind, coornn, nextn[i], nextnn, &index_event, &prob);
+                        o->mc[indnn].ind_event = index_event;
+                        o->mc[indnn].prob = prob;
+                        update_tree(o, indnn, prob);
+                    }
+                }
+            } else {
+                coor--;
+            }
+        }
+    }
+    indatom = *LI(o, site);                       /* :216-261 */
+    mvbits(coor, LEN_COOR, ls, POS_COOR);
+    if (coor == 0) {
+        erase_mc(o, site);
+    } else {
+        get_prob(o, 0, 0, 0, coor, site, nextn, &index_event, &prob);
+        o->mc[indatom].ind_event = index_event;
+        o->mc[indatom].prob = prob;
+        if (coor == 1) {
+            memcpy(nextn, o->mc[indatom].nn, sizeof nextn);
+            for (int i = 0; i < 4; i++) {
+                int32_t v = *LC(o, nextn[i]);
+                int occn = ibits(v, POS_OCC, LEN_OCC);
+                if (occn == 0) {
+                    memset(o->mc[indatom].nn[i], 0, sizeof(int) * 3);
+                } else {
+                    int coornn = ibits(v, POS_COOR, LEN_COOR);
+                    int covindnn = ibits(v, POS_INDEX, LEN_INDEX);
+                    if (coornn <= 3 && covindnn != WALL) {
+                        int indnn = *LI(o, nextn[i]);
+                        memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                        if (in_list(nextnn, site)) cp3(o->nbuff, o->mc[indatom].nn[i]);
+                    }
+                    memset(o->mc[indatom].nn[i], 0, sizeof(int) * 3);
+                }
+            }
+            cp3(o->mc[indatom].nn[0], o->nbuff);
+        }
+        update_tree(o, indatom, prob);
+    }
+}
+
+/* absorption, MS/mcevent/absorption.f:25-78 */
+static void absorption(ora_t *o, int indvoid, int covind)
+{
+    int site[3], nextn[4][3], nextnn[4][3], index_event;
+    double prob;
+    cp3(site, o->mc[indvoid].xyz);
+    int32_t *ls = LC(o, site);
+    int coor = ibits(*ls, POS_COOR, LEN_COOR);
+    mvbits(covind, LEN_INDEX, ls, POS_INDEX);
+    memcpy(nextn, o->mc[indvoid].nn, sizeof nextn);
+    for (int i = 0; i < 4; i++) {
+        int32_t v = *LC(o, nextn[i]);
+        int occn = ibits(v, POS_OCC, LEN_OCC);
+        int indnn = *LI(o, nextn[i]);
+        int coorn = ibits(v, POS_COOR, LEN_COOR);
+        if (occn != 0) {
+            int covindn = ibits(v, POS_INDEX, LEN_INDEX);
+            if (covindn != WALL && coorn <= 3) {
+                memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+                if (in_list(nextnn, site)) {
+                    int sioc = ibits(v, POS_SIC, LEN_SIC);
+                    get_prob(o, 1, sioc, covindn, coorn, nextn[i], nextnn, &index_event, &prob);
+                    o->mc[indnn].ind_event = index_event;
+                    o->mc[indnn].prob = prob;
+                    update_tree(o, indnn, prob);
+                }
+            }
+        }
+    }
+    get_prob(o, 0, 0, covind, coor, site, nextn, &index_event, &prob);
+    o->mc[indvoid].ind_event = index_event;
+    o->mc[indvoid].prob = prob;
+    update_tree(o, indvoid, prob);
+}
+
+/* desorption, MS/mcevent/desorption.f:25-117 */
+static void desorption_nn(ora_t *o, const int site[3], const int nn[3])
+{
+    int nextnn[4][3], index_event;
+    double prob;
+    int32_t v = *LC(o, nn);
+    int occn = ibits(v, POS_OCC, LEN_OCC);
+    int indnn = *LI(o, nn);
+    int coorn = ibits(v, POS_COOR, LEN_COOR);
+    if (occn != 0) {
+        int covindn = ibits(v, POS_INDEX, LEN_INDEX);
+        if (covindn != WALL) {
+            memcpy(nextnn, o->mc[indnn].nn, sizeof nextnn);
+            if (in_list(nextnn, site)) {
+                int sioc = ibits(v, POS_SIC, LEN_SIC);
+                get_prob(o, 1, sioc, covindn, coorn, nn, nextnn, &index_event, &prob);
+                o->mc[indnn].ind_event = index_event;
+                o->mc[indnn].prob = prob;
+                update_tree(o, indnn, prob);
+            }
+        }
+    }
+}
+
+static void desorption(ora_t *o, int indatom)
+{
+    int site[3], nextn[4][3], index_event;
+    double prob;
+    cp3(site, o->mc[indatom].xyz);
+    int32_t *ls = LC(o, site);
+    int covind = ibits(*ls, POS_INDEX, LEN_INDEX);
+    if (covind == o->list_cov[0]) o->count_cov[0]--;
+    else if (covind == o->list_cov[1]) o->count_cov[1]--;
+    else if (covind == o->list_cov[2]) o->count_cov[2]--;
+    int coor = ibits(*ls, POS_COOR, LEN_COOR);
+    mvbits(0, LEN_INDEX, ls, POS_INDEX);
+    memcpy(nextn, o->mc[indatom].nn, sizeof nextn);
+    if (coor == 1) {
+        desorption_nn(o, site, nextn[0]);
+    } else {
+        for (int i = 0; i < 4; i++) desorption_nn(o, site, nextn[i]);
+    }
+    get_prob(o, 0, 0, 0, coor, site, nextn, &index_event, &prob);
+    o->mc[indatom].ind_event = index_event;
+    o->mc[indatom].prob = prob;
+    update_tree(o, indatom, prob);
+}
+
+/* ============ initial structures ============ */
+static void std_neighbours(ora_t *o, const int site[3], int first, int nextn[4][3])
+{
+    for (int i = 0; i < 4; i++) {
+        for (int k = 0; k < 3; k++) nextn[i][k] = site[k] + JUMPDIA[first + i][k];
+        if (nextn[i][0] >= o->lx) nextn[i][0] -= o->lx;
+        if (nextn[i][0] < 0) nextn[i][0] += o->lx;
+        if (nextn[i][1] >= o->ly) nextn[i][1] -= o->ly;
+        if (nextn[i][1] < 0) nextn[i][1] += o->ly;
+    }
+}
+
+/* diamond site test used by every initializer (e.g. SetSi.f:52-57):
+ * returns 0 (not a site), 1 ((x1+y1+z1) mod 4 == 0), 2 (== 3) */
+static int dia_kind(int x, int y, int z)
+{
+    if (x % 3 || y % 3 || z % 3) return 0;
+    int x1 = x / 3, y1 = y / 3, z1 = z / 3;
+    if ((x1 % 2) != (y1 % 2) || (x1 % 2) != (z1 % 2)) return 0;
+    int m = (x1 + y1 + z1) % 4;
+    if (m == 0) return 1;
+    if (m == 3) return 2;
+    return 0;
+}
+
+static void set_walls(ora_t *o, int z0, int z1)
+{
+    for (int z = z0; z <= z1; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
+                mvbits(WALL, LEN_INDEX, v, POS_INDEX);
+            }
+}
+
+/* SetSi (InitSt 'FS'), MS/initial/SetSi.f:25-221; SetSiC3C (InitSt 'F'),
+ * MS/initial/SetSiC3C.f:25-199.  They differ in the walls (SetSi only),
+ * the bulk start (z=6 vs z=0) and the species of the second sublattice
+ * (Si vs C) and of the surface layer's rate (PtransE(1|2,2,...)). */
+static void set_flat(ora_t *o, int len, int sic)
+{
+    int site[3], nextn[4][3], index_event;
+    double prob;
+    if (!sic) set_walls(o, 0, 5);
+    int zb = sic ? 0 : 6;
+    for (int z = zb; z <= len - 4; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                int sp = (k == 2 && sic) ? POS_C : POS_SI;
+                *v = (int32_t)((uint32_t)*v | (1u << sp) | (1u << POS_OCC));
+                mvbits(4, LEN_COOR, v, POS_COOR);
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                add_bulk(o, site, nextn);
+            }
+    for (int z = len - 3; z <= len - 1; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                int sp = (k == 2 && sic) ? POS_C : POS_SI;
+                *v = (int32_t)((uint32_t)*v | (1u << sp) | (1u << POS_OCC));
+                mvbits(2, LEN_COOR, v, POS_COOR);
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                prob = o->ptransE[(k == 2 && sic) ? 1 : 0][2][0][0][0][0][0];
+                add_mc(o, site, nextn, 4, prob);
+            }
+    for (int y = 0; y < o->ly; y++)
+        for (int x = 0; x < o->lx; x++) {
+            int z = len;
+            int k = dia_kind(x, y, z);
+            if (!k) continue;
+            int32_t *v = &o->latt[lidx(o, x, y, z)];
+            mvbits(2, LEN_COOR, v, POS_COOR);
+            site[0] = x; site[1] = y; site[2] = z;
+            std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+            get_prob(o, 0, 0, 0, 2, site, nextn, &index_event, &prob);
+            add_mc(o, site, nextn, index_event, prob);
+        }
+    if (!sic) set_walls(o, o->lz - 6, o->lz - 1);
+}
+
+/* ============ start.dat parsing (MS/main.f:80-212, SetProbability.f) ============ */
+typedef struct {
+    FILE *f;
+    char line[4096];
+    char *tok;       /* cursor into line for list-directed continuation */
+} rd_t;
+
+static int rd_line(rd_t *r)
+{
+    if (!fgets(r->line, sizeof r->line, r->f)) return 0;
+    size_t n = strlen(r->line);
+    while (n && (r->line[n - 1] == '\n' || r->line[n - 1] == '\r')) r->line[--n] = 0;
+    r->tok = r->line;
+    return 1;
+}
+
+/* list-directed READ of `n` items: starts a new record, continues to the next
+ * record when the current one runs out of values. */
+static int rd_items(ora_t *o, rd_t *r, int n, char out[][256])
+{
+    if (!rd_line(r)) ora_fail(o, "start.dat: unexpected end of file");
+    for (int k = 0; k < n; k++) {
+        for (;;) {
+            while (*r->tok && (isspace((unsigned char)*r->tok) || *r->tok == ',')) r->tok++;
+            if (*r->tok) break;
+            if (!rd_line(r)) ora_fail(o, "start.dat: unexpected end of file");
+        }
+        int m = 0;
+        while (*r->tok && !isspace((unsigned char)*r->tok) && *r->tok != ',' && m < 255) out[k][m++] = *r->tok++;
+        out[k][m] = 0;
+    }
+    return n;
+}
+
+static double to_real(const char *s)
+{
+    char b[256];
+    snprintf(b, sizeof b, "%s", s);
+    for (char *p = b; *p; p++)
+        if (*p == 'd' || *p == 'D') *p = 'e';
+    return strtod(b, NULL);
+}
+
+static void set_probability(ora_t *o, rd_t *r)
+{   /* SetProbability, MS/mcevent/SetProbability.f:21-143 */
+    static const int maxe[4][4] = {   /* [ncov][ncrystal] */
+        {0, 3, 18, 57}, {0, 9, 50, 150}, {0, 19, 100, 288}, {0, 34, 172, 480}};
+    memset(o->ptransE, 0, sizeof o->ptransE);
+    if (o->ncrystal < 1 || o->ncrystal > 3 || o->ncov < 0 || o->ncov > 3)
+        ora_fail(o, "ERROR NOT IMPLEMENTED: NCrystal and NCov must be <= 3 3");
+    int maxlines = maxe[o->ncov][o->ncrystal];
+    lg(o, " maxElines %d\n", maxlines);
+    char it[3][256];
+    for (int i = 0; i < maxlines; i++) {
+        rd_items(o, r, 3, it);
+        int indsp = atoi(it[0]);
+        long elind = atol(it[1]);
+        double val = to_real(it[2]);
+        if (indsp > o->ncrystal || indsp < 1) ora_fail(o, "ERROR: 1st index in evap prob must be <= NCrystal");
+        int ind[6] = {0, 0, 0, 0, 0, 0};
+        long p10;
+        for (int j = 1; j <= o->ncrystal; j++) {
+            p10 = 1;
+            for (int q = 0; q < o->ncrystal + o->ncov - j; q++) p10 *= 10;
+            ind[j - 1] = (int)((elind / p10) % 10);
+        }
+        for (int j = o->ncrystal + 1; j <= o->ncrystal + o->ncov; j++) {
+            p10 = 1;
+            for (int q = 0; q < o->ncrystal + o->ncov - j; q++) p10 *= 10;
+            ind[NCRYSTAL_MAX + j - o->ncrystal - 1] = (int)((elind / p10) % 10);
+        }
+        for (int j = 0; j < 6; j++)
+            if (ind[j] > 3) ora_fail(o, "evaporation index digit > 3");
+        o->ptransE[indsp - 1][ind[0]][ind[1]][ind[2]][ind[3]][ind[4]][ind[5]] = val;
+    }
+    for (int j = 0; j < o->ncrystal * 3; j++) {
+        rd_items(o, r, 3, it);
+        int indsp = atoi(it[0]), el = atoi(it[1]);
+        if (indsp > o->ncrystal || indsp < 1 || el < 1 || el > 3) ora_fail(o, "ERROR: 1st index in depo prob block must be <= NCrystal");
+        o->ptransD[indsp - 1][el - 1] = to_real(it[2]);
+    }
+    for (int j = 0; j < o->ncov * 3; j++) {
+        rd_items(o, r, 3, it);
+        int indsp = atoi(it[0]), el = atoi(it[1]);
+        if (indsp <= o->ncrystal || indsp > o->ncrystal + o->ncov || el < 0 || el > 3) ora_fail(o, "ERROR: absorption index");
+        o->ptransAbs[indsp - o->ncrystal - 1][el] = to_real(it[2]);
+    }
+    for (int j = 0; j < o->ncov * 3; j++) {
+        rd_items(o, r, 3, it);
+        int indsp = atoi(it[0]), el = atoi(it[1]);
+        if (indsp <= o->ncrystal || indsp > o->ncrystal + o->ncov || el < 0 || el > 3) ora_fail(o, "ERROR: desorption index");
+        o->ptransDes[indsp - o->ncrystal - 1][el] = to_real(it[2]);
+    }
+}
+
+static void parse_startdat(ora_t *o, const char *path)
+{   /* MS/main.f:80-212 */
+    rd_t r;
+    memset(&r, 0, sizeof r);
+    r.f = fopen(path, "r");
+    if (!r.f) ora_fail(o, "cannot open %s", path);
+    char it[8][256];
+    rd_items(o, &r, 2, it);
+    o->ncrystal = atoi(it[0]);
+    o->ncov = atoi(it[1]);
+    if (o->ncrystal > NCRYSTAL_MAX || o->ncrystal < 1) { fclose(r.f); ora_fail(o, "ERR NOT IMPLEMENTED: NCrystal must be <= 3"); }
+    rd_items(o, &r, o->ncrystal, it);
+    for (int i = 0; i < o->ncrystal; i++) o->list_crystal[i] = atoi(it[i]);
+    if (o->ncov > 0 && o->ncov <= NCOV_MAX) {
+        rd_items(o, &r, o->ncov, it);
+        for (int i = 0; i < o->ncov; i++) o->list_cov[i] = atoi(it[i]);
+    } else if (o->ncov != 0) {
+        fclose(r.f);
+        ora_fail(o, "ERR NOT IMPLEMENTED: NCov must be <= 3");
+    }
+    rd_items(o, &r, 1, it);
+    snprintf(o->init_st, sizeof o->init_st, "%.2s", it[0]);
+    if (!strcmp(o->init_st, "FF")) {
+        rd_items(o, &r, 4, it);
+        o->len1 = atoi(it[0]); o->len2 = atoi(it[1]); o->len3 = atoi(it[2]); o->len4 = atoi(it[3]);
+    } else if (!strcmp(o->init_st, "IN") || !strcmp(o->init_st, "SH") || !strcmp(o->init_st, "LA") ||
+               !strcmp(o->init_st, "ST")) {
+        fclose(r.f);
+        ora_fail(o, "InitSt %s is not restated by the oracle", o->init_st);
+    } else {
+        rd_items(o, &r, 3, it);
+        o->len1 = atoi(it[0]); o->len2 = atoi(it[1]); o->len3 = atoi(it[2]);
+    }
+    int sige = (o->ncrystal >= 2 && o->list_crystal[0] == 14 && o->list_crystal[1] == 32 &&
+                (o->ncrystal == 2 || o->list_crystal[2] == 5));
+    if (sige) {
+        rd_items(o, &r, 1, it);
+        o->alloyfraction = to_real(it[0]);
+    }
+    rd_items(o, &r, 1, it);
+    o->ptrans_zig = to_real(it[0]);
+    rd_items(o, &r, 1, it);
+    o->sf = to_real(it[0]);
+    rd_items(o, &r, 1, it);
+    snprintf(o->exit_strategy, sizeof o->exit_strategy, "%.4s", it[0]);
+    if (!strcmp(o->exit_strategy, "Iter")) {
+        rd_items(o, &r, 1, it); o->max_iter = atoll(it[0]);
+        rd_items(o, &r, 1, it); o->out_molmol = atoll(it[0]);
+    } else if (!strcmp(o->exit_strategy, "Time")) {
+        rd_items(o, &r, 1, it); o->max_time = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->out_time = to_real(it[0]);
+    }
+    rd_items(o, &r, 1, it);
+    snprintf(o->run_type, sizeof o->run_type, "%.2s", it[0]);
+    rd_items(o, &r, 1, it);
+    o->idum = atoi(it[0]);
+    rd_items(o, &r, 1, it);
+    snprintf(o->save_final, sizeof o->save_final, "%.2s", it[0]);
+    if (!strcmp(o->save_final, "T")) {
+        if (!rd_line(&r)) ora_fail(o, "start.dat: missing restart file name");
+        snprintf(o->restartfile, sizeof o->restartfile, "%s", r.line);
+    }
+    rd_items(o, &r, 1, it);
+    snprintf(o->save_coo, sizeof o->save_coo, "%.2s", it[0]);
+    if (!strcmp(o->save_coo, "T")) {
+        if (!rd_line(&r)) ora_fail(o, "start.dat: missing coo file name");
+        snprintf(o->coofile, sizeof o->coofile, "%s", r.line);
+    }
+    set_probability(o, &r);
+    fclose(r.f);
+}
+
+/* ============ output: MS/inpout/ ============ */
+/* Fortran Ew.d (0.ddddE+xx) */
+static void fmt_e(char *out, double v, int w, int d)
+{
+    char m[64], b[64];
+    if (v == 0.0) {
+        snprintf(b, sizeof b, "0.%0*dE+00", d, 0);
+    } else {
+        snprintf(m, sizeof m, "%.*e", d - 1, fabs(v));
+        /* m = "D.DDDDe+XX" */
+        char digits[64];
+        int nd = 0;
+        char *p = m;
+        digits[nd++] = *p++;
+        if (*p == '.') p++;
+        while (*p && *p != 'e') digits[nd++] = *p++;
+        digits[nd] = 0;
+        int ex = atoi(p + 1) + 1;
+        snprintf(b, sizeof b, "%s0.%sE%c%02d", v < 0 ? "-" : "", digits, ex < 0 ? '-' : '+', abs(ex));
+    }
+    snprintf(out, 64, "%*s", w, b);
+}
+
+static void fmt_header(char *out, size_t n, int count, double time, int64_t iter)
+{   /* FORMAT (1x,i8,1x,a,1x,a,1x,e15.8,1x,a,1x,i12), WriteMolMolXYZFile.f:166 */
+    char e[64];
+    fmt_e(e, time, 15, 8);
+    snprintf(out, n, " %8d angstroem KMC-time: %s Iter: %12lld\n", count, e, (long long)iter);
+}
+
+static void fmt_periodic(char *out, size_t n, ora_t *o)
+{   /* FORMAT (1x,a,3(1x,e15.8)), WriteMolMolXYZFile.f:169 */
+    char a[64], b[64], c[64];
+    fmt_e(a, o->sf * (double)o->lx, 15, 8);
+    fmt_e(b, o->sf * (double)o->ly, 15, 8);
+    fmt_e(c, o->sf * (double)o->lz, 15, 8);
+    snprintf(out, n, " periodic %s %s %s\n", a, b, c);
+}
+
+static void wr_atom(FILE *f, const char *sym, ora_t *o, int x, int y, int z)
+{   /* FORMAT('Si ',F10.5,' ',F10.5,' ',F10.5,'  ',F6.2) with 3 items */
+    fprintf(f, "%s %10.5f %10.5f %10.5f  \n", sym, o->sf * (double)x, o->sf * (double)y, o->sf * (double)z);
+}
+
+static const char *species_sym(ora_t *o, int iat)
+{
+    if (iat == 1) return "Si";
+    int z = o->list_crystal[iat - 1];
+    if (z == 6) return "C";
+    if (z == 32) return "Ge";
+    if (z == 5) return "B";
+    return NULL;
+}
+
+/* WriteMolMolXYZFile, MS/inpout/WriteMolMolXYZFile.f:22-406.  f_xyz is the
+ * main frame, f_d the non-epitaxial bulk list, f_v the vacancies, f_w the
+ * SiC wrong-bond list (may be NULL). */
+static void write_xyz_files(ora_t *o, FILE *f_xyz, FILE *f_d, FILE *f_v, FILE *f_w, double time, int64_t iter)
+{
+    char hdr[256], per[256];
+    int num_at = 0, num_cov = 0, noepi_bulk = 0;
+    for (int z = 1; z <= o->lz - 1; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                int covind = ibits(v, POS_INDEX, LEN_INDEX);
+                if (covind != WALL) {
+                    int occ = ibits(v, POS_OCC, LEN_OCC), coo = ibits(v, POS_COOR, LEN_COOR);
+                    if (occ == 1 && coo <= 3) num_at++;
+                    else if (occ == 0 && covind != 0) num_cov++;
+                }
+            }
+    for (int z = 0; z <= o->lz - 1; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (ibits(v, POS_OCC, LEN_OCC) == 1 && ibits(v, POS_COOR, LEN_COOR) == 4 && !dia_kind(x, y, z))
+                    noepi_bulk++;
+            }
+    lg(o, " %d\n", noepi_bulk);
+    fmt_periodic(per, sizeof per, o);
+    if (f_d) {
+        fmt_header(hdr, sizeof hdr, noepi_bulk, time, iter);
+        fputs(hdr, f_d);
+        fputs(per, f_d);
+        for (int z = 0; z <= o->lz - 1; z++)
+            for (int y = 0; y < o->ly; y++)
+                for (int x = 0; x < o->lx; x++) {
+                    int32_t v = o->latt[lidx(o, x, y, z)];
+                    if (ibits(v, POS_OCC, LEN_OCC) == 1 && ibits(v, POS_COOR, LEN_COOR) == 4 && !dia_kind(x, y, z)) {
+                        int iat = ibits(v, POS_SIC, LEN_SIC);
+                        if (iat == 1) wr_atom(f_d, "Ge", o, x, y, z);
+                        if (iat == 2) wr_atom(f_d, "B", o, x, y, z);
+                        if (iat == 3) wr_atom(f_d, "Cl", o, x, y, z);
+                    }
+                }
+    }
+    if (f_xyz) {
+        fmt_header(hdr, sizeof hdr, num_at + o->num_void + num_cov, time, iter);
+        fputs(hdr, f_xyz);
+        fputs(per, f_xyz);
+        for (int z = 0; z <= o->lz - 1; z++)
+            for (int y = 0; y < o->ly; y++)
+                for (int x = 0; x < o->lx; x++) {
+                    int32_t v = o->latt[lidx(o, x, y, z)];
+                    int iat = ibits(v, POS_SIC, LEN_SIC);
+                    int coo = ibits(v, POS_COOR, LEN_COOR);
+                    int covind = ibits(v, POS_INDEX, LEN_INDEX);
+                    if (covind == 1) wr_atom(f_xyz, "H", o, x, y, z);
+                    if (covind == 17) wr_atom(f_xyz, "Cl", o, x, y, z);
+                    if (iat >= 1 && iat <= 3 && coo <= 3) {
+                        if (iat > o->ncrystal) ora_fail(o, "ERR: IAt=%d should not happen", iat);
+                        const char *sym = species_sym(o, iat);
+                        if (!sym) ora_fail(o, "ERROR: 2nd crystal specie can only be C/Ge/B");
+                        wr_atom(f_xyz, sym, o, x, y, z);
+                    }
+                }
+        for (int i = 1; i <= o->num_void; i++)
+            wr_atom(f_xyz, "O", o, o->voids[i].xyz[0], o->voids[i].xyz[1], o->voids[i].xyz[2]);
+    }
+    if (f_v) {
+        fprintf(f_v, " %8d angstroem\n", o->num_void);
+        fputs(per, f_v);
+        for (int i = 1; i <= o->num_void; i++) {
+            int x = o->voids[i].xyz[0], y = o->voids[i].xyz[1], z = o->voids[i].xyz[2];
+            if (o->ncov == 0 && o->ncrystal == 2 && o->list_crystal[1] == 6) {
+                int iat = 0;
+                for (int j = 0; j < 4; j++) iat += ibits(*LC(o, o->voids[i].nn[j]), POS_SIC, LEN_SIC);
+                const char *lbl = NULL;
+                if (iat == 4) lbl = "Mg %10.5f %10.5f %10.5f # CV (C vacancy)\n";
+                else if (iat == 8) lbl = "He %10.5f %10.5f %10.5f # SV (Si vacancy)\n";
+                else if (iat == 7) lbl = "Ne %10.5f %10.5f %10.5f # SAV (Si antisite vac)\n";
+                else if (iat == 5) lbl = "Be %10.5f %10.5f %10.5f # CAV (C antisite vac)\n";
+                else if (iat == 6) lbl = "Ar %10.5f %10.5f %10.5f # XV (near 2C and 2Si)\n";
+                else ora_fail(o, "ERROR: Weird Defect type was formed...ABORTING");
+                fprintf(f_v, lbl, o->sf * x, o->sf * y, o->sf * z);
+            } else {
+                wr_atom(f_v, "O", o, x, y, z);
+            }
+        }
+    }
+    /* SiC "wrong" sites, :264-398 (mutates and then restores LattCoo with
+     * the type of the LAST buffered site, as the reference does). */
+    int sic = 0;
+    if (o->ncrystal == 2)
+        for (int k = 0; k < NCRYSTAL_MAX; k++)
+            if (o->list_crystal[k] == 6) sic = 1;
+    if (sic) {
+        int num_is_wrong = 0;
+        for (int z = 1; z <= o->lz - 1; z++)
+            for (int y = 0; y < o->ly; y++)
+                for (int x = 0; x < o->lx; x++) {
+                    int32_t *v = &o->latt[lidx(o, x, y, z)];
+                    if (ibits(*v, POS_INDEX, LEN_INDEX) == WALL) continue;
+                    if (ibits(*v, POS_OCC, LEN_OCC) == 1 && ibits(*v, POS_COOR, LEN_COOR) == 4) {
+                        int ind = o->lind[lidx(o, x, y, z)];
+                        int iat = ibits(*v, POS_SIC, LEN_SIC);
+                        int nc = 0;
+                        for (int i = 0; i < 4; i++) {
+                            int32_t w = *LC(o, o->bulk[ind].nn[i]);
+                            if (iat == 1) nc += ibits(w, POS_C, 1);
+                            else if (iat == 2) nc += ibits(w, POS_SI, 1);
+                        }
+                        if (nc == 0) {
+                            num_is_wrong++;
+                            if (num_is_wrong >= o->atbuf_cap) {
+                                int nc2 = o->atbuf_cap * 2 + 64;
+                                o->atbuf = (atbuf_t *)realloc(o->atbuf, (size_t)nc2 * sizeof(atbuf_t));
+                                o->atbuf_cap = nc2;
+                            }
+                            atbuf_t *b = &o->atbuf[num_is_wrong];
+                            b->xyz[0] = x; b->xyz[1] = y; b->xyz[2] = z;
+                            if (iat == 1) {
+                                *v = (int32_t)(((uint32_t)*v & ~(1u << POS_SI)) | (1u << POS_C));
+                                b->ind_atype = 1;
+                            } else {
+                                *v = (int32_t)(((uint32_t)*v & ~(1u << POS_C)) | (1u << POS_SI));
+                                b->ind_atype = 2;
+                            }
+                        }
+                    }
+                }
+        int num_at_wrong = 0;
+        for (int pass = 0; pass < 2; pass++) {
+            if (pass == 1 && f_w) {
+                fprintf(f_w, " %8d angstroem\n", num_at_wrong);
+                fputs(per, f_w);
+            }
+            for (int z = 1; z <= o->lz - 1; z++)
+                for (int y = 0; y < o->ly; y++)
+                    for (int x = 0; x < o->lx; x++) {
+                        int32_t v = o->latt[lidx(o, x, y, z)];
+                        if (ibits(v, POS_OCC, LEN_OCC) == 1 && ibits(v, POS_COOR, LEN_COOR) == 4) {
+                            int ind = o->lind[lidx(o, x, y, z)];
+                            int iat = ibits(v, POS_SIC, LEN_SIC);
+                            int nc = 0;
+                            for (int i = 0; i < 4; i++) {
+                                int32_t w = *LC(o, o->bulk[ind].nn[i]);
+                                if (iat == 1) nc += ibits(w, POS_C, 1);
+                                else if (iat == 2) nc += ibits(w, POS_SI, 1);
+                            }
+                            if (nc == 3) {
+                                if (pass == 0) num_at_wrong++;
+                                else if (f_w) {
+                                    if (iat == 1) wr_atom(f_w, "Si", o, x, y, z);
+                                    if (iat == 2) wr_atom(f_w, "C", o, x, y, z);
+                                }
+                            }
+                        }
+                    }
+            if (pass == 0) lg(o, " NumAtWrong: %d\n", num_at_wrong);
+        }
+        for (int i = 1; i <= num_is_wrong; i++) {
+            atbuf_t *b = &o->atbuf[i];
+            int32_t *v = &o->latt[lidx(o, b->xyz[0], b->xyz[1], b->xyz[2])];
+            if (o->atbuf[num_is_wrong].ind_atype == 1)
+                *v = (int32_t)(((uint32_t)*v & ~(1u << POS_C)) | (1u << POS_SI));
+            else
+                *v = (int32_t)(((uint32_t)*v & ~(1u << POS_SI)) | (1u << POS_C));
+        }
+    }
+}
+
+/* GetOutputFileName, MS/inpout/GetOutputFileName.f:22-81: 'I' followed by
+ * the first 8 of the 9 digits of Iout*10 (CHARACTER(Len=9) truncation). */
+static void output_name(ora_t *o, int64_t iout, char base[16])
+{
+    int64_t t = iout * 10;
+    if (t >= 1000000000LL) ora_fail(o, "GetOutputFileName:: Iter can not be represented");
+    char d[32];
+    snprintf(d, sizeof d, "%09lld", (long long)t);
+    base[0] = 'I';
+    memcpy(base + 1, d, 8);
+    base[9] = 0;
+}
+
+/* WriteMolMolSource, MS/inpout/WriteMolMolSource.f:22-112 */
+static void write_molmol_source(ora_t *o, const char *outdir, double time, int64_t iter, int64_t iout)
+{
+    char base[16], path[4096];
+    output_name(o, iout, base);
+    lg(o, " %s\n", base);
+    if (!outdir) return;
+    FILE *fx, *fd, *fv, *fw = NULL, *fs;
+    snprintf(path, sizeof path, "%s/%s.xyz", outdir, base);
+    fx = fopen(path, "w");
+    snprintf(path, sizeof path, "%s/%s_d.xyz", outdir, base);
+    fd = fopen(path, "w");
+    snprintf(path, sizeof path, "%s/%s_v.xyz", outdir, base);
+    fv = fopen(path, "w");
+    int sic = 0;
+    if (o->ncrystal == 2)
+        for (int k = 0; k < NCRYSTAL_MAX; k++)
+            if (o->list_crystal[k] == 6) sic = 1;
+    if (sic) {
+        snprintf(path, sizeof path, "%s/%s_w.xyz", outdir, base);
+        fw = fopen(path, "w");
+    }
+    if (!fx || !fd || !fv) ora_fail(o, "cannot open output files in %s", outdir);
+    write_xyz_files(o, fx, fd, fv, fw, time, iter);
+    fclose(fx);
+    fclose(fd);
+    fclose(fv);
+    if (fw) fclose(fw);
+    snprintf(path, sizeof path, "%s/%s.src", outdir, base);
+    fs = fopen(path, "w");
+    if (fs) {
+        fprintf(fs, " load xyz %s.xyz\n color temperature\n set background white\n set boundbox true\n"
+                    " zoom 140\n rotate x 41\n rotate y 4\n spacefill 2\n color axes black\n wireframe 2\n"
+                    " color atom green\n wireframe 12\n color atom purple\n set bondmode and\n", base);
+        fclose(fs);
+    }
+    snprintf(path, sizeof path, "%s/movie.mos", outdir);
+    fs = fopen(path, "a");
+    if (fs) {
+        fprintf(fs, " source    %s.src\n write gif %s.gif\n zap\n", base, base);
+        fclose(fs);
+    }
+}
+
+/* ============ public API ============ */
+ora_t *ora_create(const char *startdat_path, const char *numbers_path, int lenx, int leny, int lenz, int num_mc_max)
+{
+    ora_t *o = (ora_t *)calloc(1, sizeof(ora_t));
+    if (!o) return NULL;
+    o->lx = lenx; o->ly = leny; o->lz = lenz;
+    o->mc_max = num_mc_max > 0 ? num_mc_max : 500000;
+    o->bulk_max = 100000000;
+    o->void_max = 100000;
+    o->iter = 1;
+    o->log = NULL;
+    if (setjmp(o->jb)) {
+        ora_destroy(o);
+        return NULL;
+    }
+    if (lenx <= 0 || leny <= 0 || lenz <= 0) ora_fail(o, "bad box");
+    int64_t plane = (int64_t)lenx * leny;
+    int64_t n = plane * ((int64_t)lenz + 1 + 2 * ZGUARD);
+    o->latt_base = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    o->lind_base = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    if (!o->latt_base || !o->lind_base) ora_fail(o, "lattice allocation failed");
+    o->latt = o->latt_base + plane * ZGUARD;
+    o->lind = o->lind_base + plane * ZGUARD;
+    o->mc = (mcp_t *)calloc((size_t)o->mc_max + 2, sizeof(mcp_t));
+    o->bulk_cap = 1 << 16;
+    o->bulk = (blk_t *)calloc((size_t)o->bulk_cap, sizeof(blk_t));
+    o->voids = (blk_t *)calloc((size_t)o->void_max + 2, sizeof(blk_t));
+    o->atbuf_cap = 1024;
+    o->atbuf = (atbuf_t *)calloc((size_t)o->atbuf_cap, sizeof(atbuf_t));
+    if (!o->mc || !o->bulk || !o->voids || !o->atbuf) ora_fail(o, "list allocation failed");
+    if (numbers_path) {
+        FILE *f = fopen(numbers_path, "r");
+        if (!f) ora_fail(o, "cannot open %s", numbers_path);
+        for (int i = 0; i < 1000; i++) {
+            float v;
+            if (fscanf(f, "%f", &v) != 1) { fclose(f); ora_fail(o, "bad numbers file"); }
+            o->numbers[i] = (double)v;
+        }
+        fclose(f);
+        o->have_numbers = 1;
+    }
+    parse_startdat(o, startdat_path);
+    if (o->run_type[0] == 'T' && !o->have_numbers) ora_fail(o, "RunType T needs the test-mode number list");
+    allocate_arrays(o);
+    return o;
+}
+
+void ora_destroy(ora_t *o)
+{
+    if (!o) return;
+    free(o->latt_base);
+    free(o->lind_base);
+    free(o->mc);
+    free(o->bulk);
+    free(o->voids);
+    free(o->atbuf);
+    free(o->tree);
+    free(o->trace);
+    free(o);
+}
+
+int ora_init(ora_t *o)
+{
+    if (setjmp(o->jb)) return -1;
+    /* MS/main.f:224-295 */
+    if (!strcmp(o->init_st, "FS")) {
+        o->len1 -= o->len1 % 24;
+        set_flat(o, o->len1, 0);
+    } else if (!strcmp(o->init_st, "F")) {
+        o->len1 -= o->len1 % 24;
+        set_flat(o, o->len1, 1);
+    } else {
+        ora_fail(o, "initialization not_implemented in the oracle: %s", o->init_st);
+    }
+    lg(o, " Atoms,Voids,AdAtoms %lld %d %d\n", (long long)o->num_bulk, o->num_void, o->num_mc);
+    memcpy(o->count_crystal_old, o->count_crystal, sizeof o->count_crystal);
+    return 0;
+}
+
+static void trace_push(ora_t *o, const int site[3], int itrans, int arm)
+{
+    if (!o->trace_on) return;
+    if (o->trace_len >= o->trace_cap) {
+        int64_t nc = o->trace_cap ? o->trace_cap * 2 : (1 << 16);
+        ora_event_t *t = (ora_event_t *)realloc(o->trace, (size_t)nc * sizeof(ora_event_t));
+        if (!t) ora_fail(o, "trace allocation failed");
+        o->trace = t;
+        o->trace_cap = nc;
+    }
+    ora_event_t *e = &o->trace[o->trace_len++];
+    e->x = site[0]; e->y = site[1]; e->z = site[2];
+    e->itrans = (int8_t)itrans;
+    e->arm = (int8_t)arm;
+    e->pad = 0;
+}
+
+/* One iteration of the KMC loop, MS/main.f:304-369.  Returns 1 to exit. */
+static int kmc_step(ora_t *o, const char *outdir)
+{
+    o->iter_out = o->iter;
+    if (o->num_mc <= 20) {
+        lg(o, " few MC particles: stop MC %lld %d\n", (long long)o->iter, o->num_mc);
+        return 1;
+    }
+    double patom;
+    int ind = pick_tree_event(o, &patom);
+    o->time = o->time + 1.0 / o->tree[1];
+    int itrans = o->mc[ind].ind_event;
+    if (!strcmp(o->exit_strategy, "Iter")) {
+        if (o->out_molmol > 0 && o->iter % o->out_molmol == 0) {
+            o->framecounter = o->iter_out / o->out_molmol;
+            write_molmol_source(o, outdir, o->time, o->iter_out, o->framecounter);
+            int *s = o->mc[ind].xyz;
+            lg(o, " Iter, Time, Site %lld %.17g %d %d %d\n", (long long)o->iter, o->time, s[0], s[1], s[2]);
+            lg(o, " NatNvoidNad %lld %d %d\n", (long long)o->num_bulk, o->num_void, o->num_mc);
+        }
+    } else if (!strcmp(o->exit_strategy, "Time")) {
+        if (o->time >= (double)(o->framecounter + 1) * o->out_time) {
+            write_molmol_source(o, outdir, o->time, o->iter_out, o->framecounter + 1);
+            int *s = o->mc[ind].xyz;
+            lg(o, " Iter, Time, Site %lld %.17g %d %d %d\n", (long long)o->iter, o->time, s[0], s[1], s[2]);
+            lg(o, " NatNvoidNad %lld %d %d\n", (long long)o->num_bulk, o->num_void, o->num_mc);
+            o->framecounter++;
+        }
+    }
+    int site[3];
+    cp3(site, o->mc[ind].xyz);
+    if (itrans <= 3) {
+        deposition(o, ind, itrans);
+        if (itrans >= 1) o->count_crystal[itrans - 1]++;
+        trace_push(o, site, itrans, o->cur_arm);
+    } else if (itrans == 4) {
+        evaporation(o, ind);
+        trace_push(o, site, 4, 0);
+    } else if (itrans == 5) {
+        desorption(o, ind);
+        trace_push(o, site, 5, 0);
+    } else {
+        int covind = o->list_cov[itrans - 6];
+        absorption(o, ind, covind);
+        o->count_cov[itrans - 6]++;
+        trace_push(o, site, itrans, 0);
+    }
+    o->iter++;
+    if (!strcmp(o->exit_strategy, "Iter")) {
+        if (o->iter > o->max_iter) return 2;
+    } else if (!strcmp(o->exit_strategy, "Time")) {
+        if (o->time > o->max_time) return 2;
+    }
+    return 0;
+}
+
+int ora_run(ora_t *o, int64_t n, const char *outdir)
+{
+    if (setjmp(o->jb)) return -1;
+    if (!o->started) {
+        write_molmol_source(o, outdir, o->time, 0, 0);
+        o->started = 1;
+    }
+    for (int64_t k = 0; k < n; k++) {
+        int r = kmc_step(o, outdir);
+        if (r) return r;
+    }
+    return 0;
+}
+
+int ora_main(ora_t *o, const char *outdir)
+{
+    o->log = stdout;
+    if (ora_init(o)) return -1;
+    if (setjmp(o->jb)) return -1;
+    write_molmol_source(o, outdir, o->time, 0, 0);
+    o->started = 1;
+    for (;;) {
+        int r = kmc_step(o, outdir);
+        if (r < 0) return -1;
+        if (r) break;
+    }
+    if (!strcmp(o->exit_strategy, "Iter"))
+        write_molmol_source(o, outdir, o->time, o->iter_out, o->out_molmol > 0 ? o->iter_out / o->out_molmol : 0);
+    else
+        write_molmol_source(o, outdir, o->time, o->iter_out, o->framecounter);
+    return 0;
+}
+
+void ora_trace_enable(ora_t *o, int on) { o->trace_on = on; }
+int64_t ora_trace_len(const ora_t *o) { return o->trace_len; }
+const ora_event_t *ora_trace(const ora_t *o) { return o->trace; }
+void ora_trace_clear(ora_t *o) { o->trace_len = 0; }
+int64_t ora_iter(const ora_t *o) { return o->iter; }
+double ora_time(const ora_t *o) { return o->time; }
+double ora_total_rate(const ora_t *o) { return o->tree[1]; }
+int ora_counts(const ora_t *o, int32_t out[3])
+{
+    out[0] = (int32_t)o->num_bulk;
+    out[1] = o->num_void;
+    out[2] = o->num_mc;
+    return 0;
+}
+void ora_dims(const ora_t *o, int32_t out[3])
+{
+    out[0] = o->lx; out[1] = o->ly; out[2] = o->lz;
+}
+void ora_get_lattcoo(const ora_t *o, int32_t *out)
+{
+    memcpy(out, o->latt, sizeof(int32_t) * (size_t)o->lx * o->ly * ((size_t)o->lz + 1));
+}
+int ora_site_info(const ora_t *o, int x, int y, int z, int32_t nn[12], int32_t *ind_event, double *prob)
+{
+    int64_t i = lidx(o, x, y, z);
+    int32_t v = o->latt[i];
+    int ind = o->lind[i];
+    int occ = ibits(v, POS_OCC, LEN_OCC), coo = ibits(v, POS_COOR, LEN_COOR);
+    int which = 0;
+    if (ind == 0) which = 0;
+    else if (occ == 1 && coo == 4) which = 2;
+    else if (occ == 0 && coo == 4) which = 3;
+    else which = 1;
+    *ind_event = 0;
+    *prob = 0.0;
+    if (which == 1) {
+        memcpy(nn, o->mc[ind].nn, sizeof(int32_t) * 12);
+        *ind_event = o->mc[ind].ind_event;
+        *prob = o->mc[ind].prob;
+    } else if (which == 2) {
+        memcpy(nn, o->bulk[ind].nn, sizeof(int32_t) * 12);
+    } else if (which == 3) {
+        memcpy(nn, o->voids[ind].nn, sizeof(int32_t) * 12);
+    } else {
+        memset(nn, 0, sizeof(int32_t) * 12);
+    }
+    return which;
+}
+int ora_write_xyz(ora_t *o, const char *path)
+{
+    if (setjmp(o->jb)) return -1;
+    FILE *f = fopen(path, "w");
+    if (!f) return -1;
+    write_xyz_files(o, f, NULL, NULL, NULL, o->time, o->iter_out);
+    fclose(f);
+    return 0;
+}
+void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9])
+{
+    int k = 0;
+    for (int s = 0; s < 3; s++)
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++)
+                for (int c = 0; c < 4; c++)
+                    for (int d = 0; d < 4; d++)
+                        for (int e = 0; e < 4; e++)
+                            for (int f = 0; f < 4; f++) ptransE[k++] = o->ptransE[s][a][b][c][d][e][f];
+    for (int s = 0; s < 3; s++)
+        for (int c = 0; c < 3; c++) ptransD[s * 3 + c] = o->ptransD[s][c];
+}

@@ -1,0 +1,85 @@
+/*
+ * mks_oracle.h — serial CPU restatement of the MulSKIPS KMC event loop.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the parity oracle for the GPU engine in
+ * mulskips_gb300/.  Only tests/, __graft_entry__.smoke() and the cpu_baseline
+ * leg of bench.py may load it.  The product never calls it.
+ *
+ * It restates, function by function, the reference Fortran program
+ * (mulskips-source/main.f and mulskips-source/mcevent/, lattice/, initial/,
+ * inpout/) on the same dense super-lattice grid (LattCoo/LattInd int32 bit
+ * fields), with the same ran3 generator, the same 1000-value test-mode list,
+ * the same binary sum-tree and the same list bookkeeping, so that a given
+ * start.dat produces the same event sequence and the same output frames.
+ * Parity is pinned against the reference's own regression fixtures
+ * (regression-tests/input-and-references-files, cases Si-SL and surface).
+ */
+#ifndef MKS_ORACLE_H
+#define MKS_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ora ora_t;
+
+/* One applied KMC event, as the GPU replay consumes it. */
+typedef struct {
+    int32_t x, y, z;   /* super-lattice grid coordinates of the event site   */
+    int8_t  itrans;    /* 1..3 deposition of that species, 4 evaporation,
+                          5 desorption, >=6 absorption                      */
+    int8_t  arm;       /* 1 if a coor-1 deposition chose arm-chair stacking  */
+    int16_t pad;
+} ora_event_t;
+
+/* Create an oracle from a start.dat file (reference format).  `numbers_path`
+ * is the 1000-value test-mode uniform list (needed for RunType 'T'); may be
+ * NULL otherwise.  `num_mc_max` <= 0 keeps the reference's 500000.
+ * Returns NULL on error (message in ora_last_error()).                     */
+ora_t *ora_create(const char *startdat_path, const char *numbers_path,
+                  int lenx, int leny, int lenz, int num_mc_max);
+void ora_destroy(ora_t *o);
+const char *ora_last_error(void);
+
+/* Run the initializer named by InitSt (FS, F supported).  0 on success. */
+int ora_init(ora_t *o);
+
+/* Advance up to n events (stops early on the reference's exit conditions).
+ * Returns 0 ok, 1 "few MC particles" stop, 2 exit condition reached,
+ * <0 error.  Writes output frames into `outdir` when non-NULL.             */
+int ora_run(ora_t *o, int64_t n, const char *outdir);
+
+/* Run the whole program like mulskips.e in directory `outdir`. */
+int ora_main(ora_t *o, const char *outdir);
+
+/* Trace recording. */
+void ora_trace_enable(ora_t *o, int on);
+int64_t ora_trace_len(const ora_t *o);
+const ora_event_t *ora_trace(const ora_t *o);
+void ora_trace_clear(ora_t *o);
+
+/* State access. */
+int64_t ora_iter(const ora_t *o);          /* Iter (next event number) */
+double ora_time(const ora_t *o);
+double ora_total_rate(const ora_t *o);     /* Tree(1)                  */
+int ora_counts(const ora_t *o, int32_t out[3]);   /* NumAtoms, NumVoids, NumAdAtom */
+void ora_dims(const ora_t *o, int32_t out[3]);
+/* Copy LattCoo(0:LenX-1,0:LenY-1,0:LenZ) (x fastest) into out. */
+void ora_get_lattcoo(const ora_t *o, int32_t *out);
+/* Per-site list data of the site at (x,y,z): which list (0 none, 1 MC,
+ * 2 bulk, 3 void), the 4 listed neighbours (12 ints), Ind_Event and rate.  */
+int ora_site_info(const ora_t *o, int x, int y, int z, int32_t nn[12],
+                  int32_t *ind_event, double *prob);
+/* Write the xyz frame exactly as WriteMolMolXYZFile would. */
+int ora_write_xyz(ora_t *o, const char *path);
+
+/* Export the rate tables parsed from start.dat. */
+void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);
+/* Raw ran3 for testing: seed then draw n values. */
+void ora_ran3_sequence(int idum, int n, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

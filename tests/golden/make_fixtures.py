@@ -1,0 +1,49 @@
+"""Generate the golden fixtures under tests/golden/ from the MulSKIPS reference.
+
+Run once in a container that has the reference checkout (default path
+/root/reference, override with MULSKIPS_REF).  The outputs are committed; the
+tests read only the committed files, never the reference itself.
+
+Fixtures written:
+  numberslist.txt        the 1000 test-mode uniforms of
+                         mulskips-source/mcevent/PickTreeEvent.f:77-1076
+                         (RunType 'T'), one literal per line, as written
+  <case>/start.dat       regression-tests/input-and-references-files/start-<case>.dat
+  <case>/I00000000.xyz.gz, I00000001.xyz.gz, log.txt
+                         the reference's own regression outputs for that case
+"""
+import gzip
+import os
+import re
+import shutil
+
+REF = os.environ.get("MULSKIPS_REF", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+RT = os.path.join(REF, "regression-tests", "input-and-references-files")
+CASES = ["Si-SL", "surface"]
+
+
+def numbers_list():
+    src = open(os.path.join(REF, "mulskips-source", "mcevent", "PickTreeEvent.f")).read()
+    body = src[src.index("numbers = (/"):src.index("/)", src.index("numbers = (/"))]
+    vals = re.findall(r"[-+]?\d+\.\d+E[-+]\d+", body)
+    assert len(vals) == 1000, len(vals)
+    with open(os.path.join(HERE, "numberslist.txt"), "w") as f:
+        f.write("\n".join(vals) + "\n")
+
+
+def cases():
+    for case in CASES:
+        d = os.path.join(HERE, case)
+        os.makedirs(d, exist_ok=True)
+        shutil.copyfile(os.path.join(RT, f"start-{case}.dat"), os.path.join(d, "start.dat"))
+        shutil.copyfile(os.path.join(RT, f"log-{case}.txt"), os.path.join(d, "log.txt"))
+        for fr in ("I00000000", "I00000001"):
+            with open(os.path.join(RT, f"{fr}-{case}.xyz"), "rb") as fi, \
+                    gzip.open(os.path.join(d, f"{fr}.xyz.gz"), "wb", compresslevel=9) as fo:
+                fo.write(fi.read())
+
+
+if __name__ == "__main__":
+    numbers_list()
+    cases()
