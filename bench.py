@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark: accepted KMC events/s of the plain Si(001) model on one GB300.
+
+Workload (one step = one pass of the KMC hot path over one lattice):
+  plain Si(001), 256 conventional cells per side (3072^3 super-lattice grid,
+  134M diamond sites), substrate filling the box (Len1 = 3000 grid units),
+  walls as SetSi, PtransE(1,n) = 1e13 exp(-0.6 n eV / kT), PtransD(1,n) = 0.5,
+  T cycling over {1000, 1100, 1200} K by step, one sublattice window of
+  tau = 1e-4 s.  Inputs: the lattice is initialised on the device before each
+  step (untimed for `value`).  The lattice (268 MB) is larger than L2.
+
+`value`: events / device time of the KMC kernels (CUDA events on the
+engine's stream), inputs resident.  `e2e`: the same through the C ABI with
+host buffers: compact lattice upload from pinned memory, the window, the
+lattice download and the observables, timed on the host.
+`--impl reference`: the reference CPU path (the oracle restatement; the
+Fortran reference has no compiler here) on all host cores.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TEMPS = (1000.0, 1100.0, 1200.0)
+BOX = 3072
+LEN1 = 3000
+TAU = 1e-4
+ALGO_BYTES_PER_EVENT = 28   # uint8 reads of site+4NN+12NNN occupancy, 5 coordinations; 6 writes
+METRIC = "accepted KMC events/s (plain Si(001) 256^3 cells, tau=1e-4 s)"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except OSError:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(r[1]) for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": float(rows[0][2]), "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU side
+def _oracle_sample(args):
+    """One bounded sample of the same model on the CPU oracle: a 480^3 box with
+    a Len1=360 Si(001) slab at temperature T, run until the slab is gone."""
+    T, seed = args
+    from oracle import ora
+    from mulskips_gb300.startdat import write_plain_si_startdat
+    d = tempfile.mkdtemp()
+    p = os.path.join(d, "start.dat")
+    write_plain_si_startdat(p, T=T, len1=360, max_iter=100000000, seed=seed)
+    o = ora.Oracle(p, 480, 480, 480, numbers=None)
+    o.init()
+    t0 = time.perf_counter()
+    o.run(100000000)
+    dt = time.perf_counter() - t0
+    n = o.iter - 1
+    o.close()
+    shutil.rmtree(d, ignore_errors=True)
+    return n, dt
+
+
+def cpu_baseline(seconds=10.0, cores=1):
+    from oracle import ora
+    ora.build()
+    ctx = mp.get_context("spawn")
+    ev = 0
+    busy = 0.0
+    k = 0
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        while time.perf_counter() - t0 < seconds:
+            jobs = [(TEMPS[(k + i) % 3], 1000 + k + i) for i in range(cores)]
+            k += cores
+            res = pool.map(_oracle_sample, jobs)
+            ev += sum(r[0] for r in res)
+            busy += max(r[1] for r in res)
+    return ev / busy, ev, k
+
+
+# ---------------------------------------------------------------- GPU side
+def gb300(args, rank, world):
+    import numpy as np
+    import torch
+    from mulskips_gb300 import Lattice, arrhenius_tables
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    tables = [arrhenius_tables(T) for T in TEMPS]
+    lat = Lattice(BOX, BOX, BOX, sf=5.43 / 12, seed=1 + rank)
+
+    def step(k):
+        pE, pD = tables[k % 3]
+        lat.set_rates(pE, pD)
+        lat.init_flat("S", LEN1)
+        ev, _ = lat.run(TAU, 1)
+        st = lat.run_stats()
+        return ev, st
+
+    for k in range(args.warmup):
+        step(k)
+    barrier()
+    events = 0
+    dev_ms = 0.0
+    launches = 0
+    phases = 0
+    with Clocks(dev) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev, st = step(args.warmup + k)
+            events += ev
+            dev_ms += st["kernel_ms"]
+            launches += st["kernel_launches"] + 1      # + the lattice init kernel
+            phases += st["phase_launches"]
+        barrier()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    # max over ranks of the device time, sum of events
+    if dist:
+        t = torch.tensor([dev_ms, float(events)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        dev_ms_max, events_all = mx[0].item(), sm[1].item()
+    else:
+        dev_ms_max, events_all = dev_ms, float(events)
+    value = events_all / (dev_ms_max / 1e3)
+
+    # end to end through the C ABI with pinned host buffers
+    pE, pD = tables[0]
+    lat.set_rates(pE, pD)
+    lat.init_flat("S", LEN1)
+    n = lat.state().size
+    host_in = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    host_out = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    host_in.numpy()[:] = lat.state().reshape(-1)
+    e2e_events = 0
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        pE, pD = tables[k % 3]
+        lat.set_rates(pE, pD)
+        lat.set_state_ptr(host_in.data_ptr(), n)
+        ev, _ = lat.run(TAU, 1)
+        lat.get_state_ptr(host_out.data_ptr(), n)
+        obs = lat.observables()
+        e2e_events += ev
+    barrier()
+    e2e_wall = time.perf_counter() - t0
+    lat.close()
+    if dist:
+        t = torch.tensor([e2e_wall, float(e2e_events)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        e2e_wall, e2e_events = mx[0].item(), sm[1].item()
+    e2e = e2e_events / e2e_wall
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    # dominant kernel: the sublattice phase kernel; per-launch averages
+    per_launch_events = events / max(phases, 1)
+    per_launch_s = (dev_ms / 1e3) / max(phases, 1)
+    achieved = per_launch_events * ALGO_BYTES_PER_EVENT / per_launch_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "sl_phase_traffic.json")
+    if os.path.exists(tp):
+        try:
+            tj = json.load(open(tp))
+            traffic = tj.get("dram_bytes_per_event", None)
+            if traffic is not None:
+                traffic = traffic * per_launch_events
+        except Exception:
+            traffic = None
+    base_v, base_ev, base_runs = cpu_baseline(seconds=args.cpu_seconds, cores=1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "plain Si(001) KMC, 256^3 cells (3072^3 grid, 134M sites), Len1=3000 slab, "
+                               "T cycling 1000/1100/1200 K, F=0.5 ML/s, E=0.6 eV/bond, nu=1e13, one tau=1e-4 s "
+                               "sublattice window per step",
+                   "box_grid": BOX, "len1": LEN1, "tau_s": TAU, "temperatures_K": list(TEMPS),
+                   "events_per_step": events / args.steps, "l2": "lattice 268 MB > 129 MB L2, no flush",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single replica"},
+        "e2e": {"value": e2e, "unit": "events/s", "h2d_bytes_per_step": n + 2 * 8 * 4096 * 3,
+                "d2h_bytes_per_step": n + 3 * 8 * 64},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": f"28 B/event algorithmic x events per k_sl_phase launch / mean launch time; "
+                             f"peak {peak_kind}"},
+        "cpu_baseline": {"value": base_v, "unit": "events/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle (serial C restatement) on {base_runs} runs of the same model in a "
+                                   f"480^3 box, Len1=360 slab etched to the walls, T cycling 1000/1100/1200 K, "
+                                   f"{base_ev} events"},
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    samples = []
+    for _ in range(args.warmup):
+        pass
+    total_ev = 0
+    total_t = 0.0
+    for k in range(args.steps):
+        v, ev, runs = cpu_baseline(seconds=args.cpu_seconds, cores=cores)
+        samples.append(v)
+        total_ev += ev
+        total_t += ev / v
+    value = total_ev / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "plain Si(001) KMC, same rates; bounded CPU sample: 480^3 box, Len1=360 slab "
+                               "etched to the walls, T cycling 1000/1100/1200 K, one oracle process per core"},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": "port",
+                         "sample": "serial C restatement of the reference (no Fortran compiler for the "
+                                   "reference itself), one independent seed per core"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    if args.impl == "reference":
+        reference(args, rank, world)
+    else:
+        gb300(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

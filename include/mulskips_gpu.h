@@ -1,0 +1,150 @@
+/*
+ * mulskips_gpu.h — C ABI of the GB300 KMC engine (libmulskips_gpu.so).
+ *
+ * The reference MulSKIPS program is one serial Fortran executable whose KMC
+ * state lives in module globals (mulskips-source/modules/defsystem.f) and whose
+ * hot loop is mulskips-source/main.f:304-371.  It has no library interface;
+ * the only precedent for a C ABI in the project is the ISO_C_BINDING socket
+ * layer (mulskips-source-LaserAnnealing/sockets/fsockets.f:45-62).  The entry
+ * points below replace the reference's internal calls one to one, so that a
+ * Fortran or C++ host (mulskips.e) or the Python wrapper can drive the GPU:
+ *
+ *   mks_create / mks_destroy     module state + AllocateArrays
+ *                                (defsystem.f:49-68, AllocateArrays.f:24-45)
+ *   mks_set_rates                SetProbability (SetProbability.f:21-143)
+ *   mks_init_flat                SetSi / SetSiC3C (SetSi.f:25-221,
+ *                                SetSiC3C.f:25-199), main.f:237-239,224-226
+ *   mks_load_lattice             continuation / CAD load of LattCoo
+ *                                (SetCAD.f:54-79,301-418)
+ *   mks_get_lattice              LattCoo dump (main.f:385-403)
+ *   mks_run                      the KMC loop main.f:304-371 (PickTreeEvent,
+ *                                Deposition, Evaporation, Get_Prob, UpdateTree)
+ *   mks_replay                   Deposition.f / Evaporation.f applied to a
+ *                                given event sequence (no selection)
+ *   mks_class_histogram          the per-class view of the rate tree Tree(:)
+ *   mks_get_observables          the scans of WriteMolMolXYZFile.f:77-119 and
+ *                                pymulskips/analyze.py:124-207
+ *
+ * All pointers are host memory owned by the caller; data is copied in/out.
+ * Every function returns 0 on success or one of the MKS_ERR_* codes; the
+ * reference STOPs the process on the same conditions (UpdateTree.f:38-48,
+ * Add.f:37-45, Erase.f:41-50, Get_Prob.f:293-298).  mks_last_error() gives
+ * the message of the last failure on the calling thread.
+ *
+ * One handle holds a batch of independent replicas (1 for a plain run) on one
+ * GPU, with one CUDA stream.  Handles are not thread-safe; several handles
+ * may live in one process.
+ */
+#ifndef MULSKIPS_GPU_H
+#define MULSKIPS_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MKS_OK 0
+#define MKS_ERR_ARG 1          /* bad argument or unsupported box size        */
+#define MKS_ERR_CUDA 2         /* CUDA runtime failure / no device            */
+#define MKS_ERR_INVARIANT 3    /* lattice state contradicts the model         */
+#define MKS_ERR_CAPACITY 4     /* a tile held more surface sites than fit     */
+#define MKS_ERR_UNSUPPORTED 5  /* feature outside the engine (e.g. PtransZig<1) */
+#define MKS_ERR_TIMEOUT 6      /* a bounded device wait gave up               */
+
+#define MKS_NCLASS 63          /* rate classes, see mks_class_histogram       */
+
+typedef struct mks_handle mks_handle;
+
+/* One replica's setup (the scalar part of start.dat, main.f:83-212). */
+typedef struct {
+    int32_t lenx, leny, lenz;      /* LenX, LenY, LenZ; LenX, LenY multiples of 12, LenZ of 3 */
+    int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (must be 0)          */
+    int32_t list_crystal[3];       /* atomic numbers (ListCrystal)               */
+    double ptrans_zig;             /* PtransZig; the engine requires 1.0         */
+    double sf;                     /* super-lattice parameter in Angstrom        */
+    uint64_t seed;                 /* IDUM / replica seed                        */
+} mks_config;
+
+/* One applied event (the trace format of the oracle and of mks_replay). */
+typedef struct {
+    int32_t x, y, z;               /* grid coordinates of the event site         */
+    int8_t itrans;                 /* 1..3 deposition of that species, 4 evaporation */
+    int8_t arm;                    /* arm-chair stacking choice (must be 0)      */
+    int16_t pad;
+} mks_event;
+
+typedef struct {
+    int64_t events;                /* accepted events since creation             */
+    double time;                   /* simulated time (FP64 clock)                */
+    int64_t atoms;                 /* occupied non-wall sites                    */
+    int64_t undercoord;            /* atoms with coordination <= 3 (xyz count)   */
+    int64_t mc_sites;              /* sites with an event (NumAdAtom)            */
+    int64_t voids;                 /* empty sites with coordination 4            */
+    int64_t species[3];            /* atoms per species                          */
+    double mean_height;            /* mean top-atom height, grid units           */
+    double rms_roughness;          /* RMS of the column heights, grid units      */
+    double total_rate;             /* sum of all event rates (FP64)              */
+    int64_t nonepitaxial;          /* off-lattice bulk atoms (stacking faults)   */
+} mks_observables;
+
+typedef struct {
+    int32_t error;                 /* last device error code (0 = none)          */
+    int32_t pending_tiles;         /* tiles left unfinished by a window          */
+    int64_t fallback_tiles;        /* tiles run from global memory               */
+    int64_t windows;               /* sublattice windows completed               */
+    int32_t active;                /* 1 while the replica still runs             */
+    int32_t stop_reason;           /* 0 running, 1 few MC sites, 2 max events, 3 max time */
+} mks_status;
+
+/* ---- plain (single-replica) interface ---- */
+int mks_create(const mks_config *cfg, mks_handle **out);
+void mks_destroy(mks_handle *h);
+const char *mks_version(void);
+int mks_last_error(char *buf, int32_t len);
+
+/* ptransE: 3*4^6 doubles indexed [s][n1][n2][n3][c1][c2][c3] (the PTransE
+ * array of defsystem.f:63-64); ptransD: 3x3 doubles [s][coor-1].          */
+int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
+/* kind 'S' = SetSi (InitSt FS), 'C' = SetSiC3C (InitSt F); len1 is the slab
+ * height, rounded down to a multiple of 24 as main.f:226,238 does.         */
+int mks_init_flat(mks_handle *h, char kind, int32_t len1);
+/* LattCoo(0:LenX-1,0:LenY-1,0:LenZ), x fastest (Fortran order).           */
+int mks_load_lattice(mks_handle *h, const int32_t *lattcoo);
+int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
+/* Compact state bytes (layer-major, see DESIGN); n >= mks_state_size(). */
+int64_t mks_state_size(mks_handle *h);
+int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
+/* Upload compact state bytes (same layout); the per-tile bands are rebuilt. */
+int mks_set_state(mks_handle *h, const uint8_t *st, int64_t n);
+int mks_replay(mks_handle *h, const mks_event *trace, int64_t n);
+/* Synchronous-sublattice KMC: windows of length tau (s); stops after
+ * max_windows windows, or once max_events / max_time is reached (checked per
+ * window), or when fewer than 21 surface sites remain (main.f:307-310).    */
+int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events,
+            double max_time, int64_t *events_done, double *time_out);
+int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
+int mks_get_observables(mks_handle *h, mks_observables *obs);
+int mks_get_status(mks_handle *h, mks_status *st);
+
+/* ---- batched replicas ---- */
+/* n replicas of uneven boxes, each with its own rates and seed, advanced
+ * together; tau per replica.  Replica i uses rates ptransE + i*3*4096 and
+ * ptransD + i*9.                                                           */
+int mks_batch_create(const mks_config *cfgs, int32_t n, mks_handle **out);
+int mks_batch_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
+int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1);
+int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
+                  int64_t max_events_each, double max_time_each, int64_t *events_total);
+int mks_batch_observables(mks_handle *h, mks_observables *obs /* n entries */);
+int32_t mks_batch_size(mks_handle *h);
+
+/* Launch statistics of the last mks_run / mks_batch_run: kernel launches,
+ * graph launches, and the device time (ms) of the sublattice kernels
+ * measured with CUDA events on the engine's stream.                        */
+int mks_last_run_stats(mks_handle *h, int64_t *kernel_launches, int64_t *graph_launches,
+                       double *kernel_ms, int64_t *phase_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

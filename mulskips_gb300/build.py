@@ -1,0 +1,69 @@
+"""Build the in-tree native libraries of mulskips_gb300 for GB300 (sm_103a).
+
+`build_all()` compiles
+  _lib/libmulskips_gpu.so   the CUDA engine + C ABI (include/mulskips_gpu.h)
+  _lib/mulskips.e           the drop-in host program (reads ./start.dat)
+with nvcc for sm_103a only.  No CPU build of the engine exists.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB = os.path.join(PKG, "_lib")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the GB300 engine must be compiled with the CUDA toolkit")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout)
+        raise RuntimeError("build failed: " + " ".join(cmd))
+    return r.stdout
+
+
+def engine_cmd(out):
+    src = os.path.join(PKG, "csrc", "engine.cu")
+    return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+            "-I", os.path.join(ROOT, "include"), src, "-o", out]
+
+
+def host_cmd(out, lib):
+    src = os.path.join(PKG, "host", "mulskips_main.cpp")
+    return [nvcc(), *ARCH, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", out,
+            "-L", os.path.dirname(lib), "-lmulskips_gpu", "-Xlinker", "-rpath=$ORIGIN"]
+
+
+def build_all(verbose=False):
+    os.makedirs(LIB, exist_ok=True)
+    lib = os.path.join(LIB, "libmulskips_gpu.so")
+    out = _run(engine_cmd(lib))
+    if verbose:
+        print(out)
+    host_src = os.path.join(PKG, "host", "mulskips_main.cpp")
+    if os.path.exists(host_src):
+        _run(host_cmd(os.path.join(LIB, "mulskips.e"), lib))
+    return lib
+
+
+def build_oracle():
+    """Compile the test oracle (oracle/Makefile).  Test infrastructure only."""
+    return _run(["make", "-C", os.path.join(ROOT, "oracle")])
+
+
+if __name__ == "__main__":
+    with ThreadPoolExecutor(2) as ex:
+        f1 = ex.submit(build_all, True)
+        f2 = ex.submit(build_oracle)
+        f1.result()
+        f2.result()

@@ -1,0 +1,1376 @@
+// engine.cu — GB300 (sm_103a) synchronous-sublattice KMC engine for the
+// MulSKIPS event loop, and the C ABI declared in include/mulskips_gpu.h.
+//
+// Data layout in HBM (per replica): one byte per diamond site (lattice.cuh),
+// layer-major st[z1][b][a] with rows padded to 16 bytes.  Each replica's
+// (a,b) plane is cut into an even number of tiles per side; the four tile
+// colours (tile index parity in a and b) form the four sublattices of the
+// synchronous-sublattice method (Shim & Amar, Phys. Rev. B 71, 125432).  In
+// one window of length tau every colour in turn advances all of its tiles
+// from T0 to T0+tau; tiles of one colour are two tiles apart, so their event
+// neighbourhoods (read range two bonds = 2 columns, write range one bond)
+// never meet.  One warp runs one tile: it stages the tile plus a two-column
+// halo and the surface band of layers in shared memory, builds the tile's
+// list of event sites with per-class counts (warp ballot / popc), and then
+// selects events rejection-free: class by cumulative rate (warp scan), member
+// by a ballot scan of the class.  Rates are an FP32 table per class; the tile
+// clock is FP64.  The reference's serial loop is mulskips-source/main.f:304-371.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "lattice.cuh"
+#include "rng.cuh"
+#include "../../include/mulskips_gpu.h"
+
+using namespace mks;
+
+namespace {
+
+// ---------------------------------------------------------------- limits
+constexpr int QMAX = 12;                 // max tile width (sites) in a or b
+constexpr int HALO = 2;                  // read range of an event, in columns
+constexpr int WX = QMAX + 2 * HALO;      // 16: window row stride
+constexpr int WMAX = 24;                 // max staged layers
+constexpr int MCCAP = 768;               // max event sites per tile
+constexpr int ZMARGIN = 5;               // extra staged layers beyond the band
+constexpr int NRELOAD = 512;             // bounded re-staging per tile and phase
+constexpr uint16_t NOPOS = 0xFFFF;
+
+// device error codes (status word)
+constexpr int DERR_INVARIANT = MKS_ERR_INVARIANT;
+constexpr int DERR_CAPACITY = MKS_ERR_CAPACITY;
+constexpr int DERR_TIMEOUT = MKS_ERR_TIMEOUT;
+
+struct RepDev {
+    int64_t st_off;
+    int NA, NB, NZ, pitch;
+    int nqa, nqb, quad_base, pad0;
+    double tau, T0, t_max;
+    long long ev_max;
+    unsigned long long seed;
+    unsigned long long events;
+    long long mc_count;
+    unsigned int window;
+    int active, stop_reason, pad1;
+    float rate[64];          // per class; CLS_ISO is computed per event
+    float spcum[3][2];       // cumulative species fractions per deposition coordination
+};
+
+struct QuadDev {
+    int rep, a0, a1, b0, b1;
+    int zlo, zhi, mc;
+};
+
+struct DevStatus {
+    int error;
+    int err_quad;
+    unsigned long long fallback;
+    unsigned long long reloads;
+};
+
+__device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+struct GLat {
+    uint8_t *st;
+    int NA, NB, NZ, pitch;
+    __device__ __forceinline__ uint8_t get(int a, int b, int z) const
+    {
+        if (z < 0 || z >= NZ) return 0;
+        return st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)];
+    }
+    __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
+    {
+        if (z < 0 || z >= NZ) return;
+        st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)] = v;
+    }
+};
+
+struct SLat {
+    uint8_t *w;
+    int ax0, bx0, zw0, NZ;
+    __device__ __forceinline__ uint8_t get(int a, int b, int z) const
+    {
+        if (z < 0 || z >= NZ) return 0;
+        return w[((z - zw0) * WX + (b - bx0)) * WX + (a - ax0)];
+    }
+    __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
+    {
+        if (z < 0 || z >= NZ) return;
+        w[((z - zw0) * WX + (b - bx0)) * WX + (a - ax0)] = v;
+    }
+};
+
+__device__ void set_error(DevStatus *s, int code, int quad)
+{
+    if (atomicCAS(&s->error, 0, code) == 0) s->err_quad = quad;
+}
+
+// --------------------------------------------------------------- kernels
+__global__ void k_init_flat(uint8_t *st, int NA, int NB, int NZ, int pitch, int lz, int len1, int sic)
+{
+    int64_t n = (int64_t)NZ * NB * pitch;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int a = (int)(i % pitch);
+        int64_t r = i / pitch;
+        int b = (int)(r % NB);
+        int z = (int)(r / NB);
+        uint8_t v = 0;
+        if (a < NA && ((a + b + (z >> 1)) & 1) == 0) v = flat_init_state(z, lz, len1, sic != 0);
+        st[i] = v;
+    }
+}
+
+// Per-tile z range and count of event sites (and invariant check of the
+// coordination bytes against the occupancy).
+__global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint8_t *st_all, DevStatus *status)
+{
+    int q = blockIdx.x;
+    if (q >= nquads) return;
+    QuadDev Q = quads[q];
+    const RepDev &R = reps[Q.rep];
+    GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
+    int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
+    int ncol = wa * wb;
+    int zlo = 1 << 30, zhi = -1, cnt = 0;
+    for (int i = threadIdx.x; i < ncol * R.NZ; i += blockDim.x) {
+        int col = i % ncol, z = i / ncol;
+        int a = Q.a0 + col % wa, b = Q.b0 + col / wa;
+        if ((a + b + (z >> 1)) & 1) continue;
+        if (site_class(L, a, b, z) != CLS_NONE) {
+            cnt++;
+            zlo = min(zlo, z);
+            zhi = max(zhi, z);
+        }
+    }
+    __shared__ int s_lo, s_hi, s_cnt;
+    if (threadIdx.x == 0) { s_lo = 1 << 30; s_hi = -1; s_cnt = 0; }
+    __syncthreads();
+    atomicMin(&s_lo, zlo);
+    atomicMax(&s_hi, zhi);
+    atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        quads[q].zlo = s_lo;
+        quads[q].zhi = s_hi;
+        quads[q].mc = s_cnt;
+    }
+}
+
+// Class histogram of one replica (int64 counts per class) and FP64 total rate.
+__global__ void k_class_hist(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *hist)
+{
+    const RepDev &R = reps[rep];
+    GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
+    __shared__ unsigned int sh[NCLASS];
+    for (int i = threadIdx.x; i < NCLASS; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int a = (int)(i % R.NA);
+        int64_t r = i / R.NA;
+        int b = (int)(r % R.NB);
+        int z = (int)(r / R.NB);
+        if ((a + b + (z >> 1)) & 1) continue;
+        int c = site_class(L, a, b, z);
+        if (c == CLS_NONE) continue;
+        // warp-aggregated increment of the same class
+        unsigned m = __match_any_sync(__activemask(), c);
+        int leader = __ffs(m) - 1;
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&sh[c], __popc(m));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NCLASS; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+// Observables of one replica: column heights, atom counts.
+__global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *cnt, double *hsum)
+{
+    const RepDev &R = reps[rep];
+    const uint8_t *st = st_all + R.st_off;
+    int ncol = R.NA * R.NB;
+    unsigned long long atoms = 0, under = 0, voids = 0, sp1 = 0, sp2 = 0, sp3 = 0;
+    double h1 = 0.0, h2 = 0.0;
+    int cols = 0;
+    for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol; col += gridDim.x * blockDim.x) {
+        int a = col % R.NA, b = col / R.NA;
+        int top = -1;
+        for (int z = 0; z < R.NZ; z++) {
+            if ((a + b + (z >> 1)) & 1) continue;
+            uint8_t s = st[((int64_t)z * R.NB + b) * R.pitch + a];
+            if (s == 0 || s == WALL) continue;
+            int sp = sp_of(s), co = co_of(s);
+            if (sp) {
+                atoms++;
+                if (co <= 3) under++;
+                if (sp == 1) sp1++;
+                if (sp == 2) sp2++;
+                if (sp == 3) sp3++;
+                top = z;
+            } else if (co == 4) {
+                voids++;
+            }
+        }
+        if (top >= 0) {
+            double h = 3.0 * top;
+            h1 += h;
+            h2 += h * h;
+            cols++;
+        }
+    }
+    atomicAdd(&cnt[0], atoms);
+    atomicAdd(&cnt[1], under);
+    atomicAdd(&cnt[2], voids);
+    atomicAdd(&cnt[3], sp1);
+    atomicAdd(&cnt[4], sp2);
+    atomicAdd(&cnt[5], sp3);
+    atomicAdd(&cnt[6], (unsigned long long)cols);
+    atomicAdd(&hsum[0], h1);
+    atomicAdd(&hsum[1], h2);
+}
+
+// Apply a given event sequence in order (one thread; the sequence is serial by
+// definition).  Deposition.f / Evaporation.f restated in lattice.cuh.
+__global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *ev, int64_t n, DevStatus *status,
+                         long long *done)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const RepDev &R = reps[0];
+    GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
+    for (int64_t i = 0; i < n; i++) {
+        mks_event e = ev[i];
+        int x1 = e.x / 3, y1 = e.y / 3, z1 = e.z / 3;
+        int a = x1 >> 1, b = y1 >> 1;
+        bool ok = (e.x % 3 == 0) && (e.y % 3 == 0) && (e.z % 3 == 0) && ((x1 & 1) == (z1 & 1)) &&
+                  ((y1 & 1) == (z1 & 1)) && z1 >= 0 && z1 < R.NZ && a < R.NA && b < R.NB && e.arm == 0;
+        int c = ok ? site_class(L, a, b, z1) : CLS_NONE;
+        Touched tc;
+        int err = 1;
+        if (ok && c != CLS_NONE) {
+            if (e.itrans >= 1 && e.itrans <= 3 && c >= CLS_C1 && c <= CLS_C3)
+                err = apply_deposition(L, a, b, z1, e.itrans, tc);
+            else if (e.itrans == 4 && c >= CLS_ISO)
+                err = apply_evaporation(L, a, b, z1, tc);
+        }
+        if (err) {
+            set_error(status, DERR_INVARIANT, (int)i);
+            *done = i;
+            return;
+        }
+    }
+    *done = n;
+}
+
+// ------------------------------------------------ the sublattice kernel
+struct TileShared {
+    uint8_t win[WX * WX * WMAX];
+    uint32_t list[MCCAP];
+    uint16_t pos[QMAX * QMAX * WMAX];
+    int cnt[64];
+    float rate[64];
+    float spcum[3][2];
+    int tc_a[5], tc_b[5], tc_z[5], tc_n;
+    int nlist;
+    int abort_code;
+};
+
+__device__ __forceinline__ int key_of(int ia, int ib, int z) { return (z << 10) | (ib << 5) | ia; }
+
+// Scan the tile interior (staged in `L`), build the event-site list and class
+// counts.  ia/ib are window coordinates (HALO-based).
+template <class Lat>
+__device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh, bool use_pos,
+                           int zw0)
+{
+    int lane = threadIdx.x & 31;
+    for (int c = lane; c < 64; c += 32) S.cnt[c] = 0;
+    if (lane == 0) S.nlist = 0;
+    __syncwarp();
+    int ncol = wa * wb;
+    int total = ncol * (zh - zl + 1);
+    bool overflow = false;
+    if (use_pos) {
+        uint32_t *p32 = reinterpret_cast<uint32_t *>(S.pos);
+        for (int i = lane; i < QMAX * QMAX * WMAX / 2; i += 32) p32[i] = 0xFFFFFFFFu;
+        __syncwarp();
+    }
+    for (int base = 0; base < total; base += 32) {
+        int i = base + lane;
+        int cls = CLS_NONE, key = 0;
+        if (i < total) {
+            int col = i % ncol, z = zl + i / ncol;
+            int ia = col % wa, ib = col / wa;
+            int a = a0 + ia, b = b0 + ib;
+            if (((a + b + (z >> 1)) & 1) == 0) cls = site_class(L, a, b, z);
+            key = key_of(ia + HALO, ib + HALO, z);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, cls != CLS_NONE);
+        int before = __popc(m & ((1u << lane) - 1u));
+        int nl = S.nlist;
+        if (cls != CLS_NONE) {
+            int slot = nl + before;
+            if (slot < MCCAP) {
+                S.list[slot] = ((uint32_t)key << 8) | (uint32_t)cls;
+                if (use_pos) {
+                    int ia = (key & 31) - HALO, ib = ((key >> 5) & 31) - HALO, z = key >> 10;
+                    S.pos[((z - zw0) * QMAX + ib) * QMAX + ia] = (uint16_t)slot;
+                }
+                atomicAdd(&S.cnt[cls], 1);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) S.nlist = nl + __popc(m);
+        __syncwarp();
+        if (S.nlist > MCCAP) overflow = true;
+    }
+    __syncwarp();
+    return !overflow;
+}
+
+__device__ __forceinline__ int find_slot(TileShared &S, uint32_t key, bool use_pos, int zw0)
+{
+    if (use_pos) {
+        int ia = (key & 31) - HALO, ib = ((key >> 5) & 31) - HALO, z = key >> 10;
+        uint16_t p = S.pos[((z - zw0) * QMAX + ib) * QMAX + ia];
+        return p == NOPOS ? -1 : (int)p;
+    }
+    int lane = threadIdx.x & 31;
+    for (int base = 0; base < S.nlist; base += 32) {
+        int i = base + lane;
+        bool hit = i < S.nlist && (S.list[i] >> 8) == key;
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) return base + __ffs(m) - 1;
+    }
+    return -1;
+}
+
+// Run events of one tile on accessor L until the tile clock reaches t_end,
+// the tile has no events, or an event would read outside the staged layers.
+// Returns 0 done, 1 needs re-staging, <0 error.
+template <class Lat>
+__device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev &Q, int qid, double &t, double t_end,
+                          unsigned int &evc, int zw0, int zw1, bool use_pos, int &hz_lo, int &hz_hi,
+                          unsigned long long &nev, uint32_t k0, uint32_t k1, uint32_t phase_tag)
+{
+    int lane = threadIdx.x & 31;
+    int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
+    for (;;) {
+        // cumulative class weights: lane l owns classes 2l and 2l+1 (ISO apart)
+        int c0 = 2 * lane, c1 = 2 * lane + 1;
+        float w0 = (c0 < NCLASS && c0 != CLS_ISO) ? (float)S.cnt[c0] * S.rate[c0] : 0.f;
+        float w1 = (c1 < NCLASS && c1 != CLS_ISO) ? (float)S.cnt[c1] * S.rate[c1] : 0.f;
+        float s = w0 + w1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            float v = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += v;
+        }
+        float r_rest = __shfl_sync(0xffffffffu, s, 31);
+        int n_iso = S.cnt[CLS_ISO];
+        float r_iso = n_iso ? (float)n_iso * 1.0e5f * fmaxf(r_rest, 1.0e-30f) : 0.f;
+        float rtot = r_rest + r_iso;
+        if (!(rtot > 0.f)) return 0;
+        U4 rnd;
+        if (lane == 0) {
+            U4 ctr{evc, (uint32_t)qid, R.window, phase_tag};
+            rnd = philox4x32_10(ctr, k0, k1);
+        }
+        rnd.x = __shfl_sync(0xffffffffu, rnd.x, 0);
+        rnd.y = __shfl_sync(0xffffffffu, rnd.y, 0);
+        rnd.z = __shfl_sync(0xffffffffu, rnd.z, 0);
+        rnd.w = __shfl_sync(0xffffffffu, rnd.w, 0);
+        evc++;
+        float dt = -__logf(u01(rnd.z)) / rtot;
+        if (t + (double)dt > t_end) {
+            t = t_end;
+            return 0;
+        }
+        // class selection
+        float target = u01(rnd.x) * rtot;
+        int cls;
+        if (target >= r_rest && n_iso > 0) {
+            cls = CLS_ISO;
+        } else {
+            unsigned m = __ballot_sync(0xffffffffu, s > target);
+            cls = -1;
+            if (m) {
+                int l = __ffs(m) - 1;
+                float sl = __shfl_sync(0xffffffffu, s, l);
+                float w0l = __shfl_sync(0xffffffffu, w0, l);
+                float w1l = __shfl_sync(0xffffffffu, w1, l);
+                float el = sl - w0l - w1l;
+                cls = (target < el + w0l) ? 2 * l : 2 * l + 1;
+                if (cls == 2 * l && !(w0l > 0.f)) cls = 2 * l + 1;
+                if (cls == 2 * l + 1 && !(w1l > 0.f)) cls = (w0l > 0.f) ? 2 * l : -1;
+            }
+            if (cls < 0 || cls >= NCLASS || S.cnt[cls] == 0) {
+                // rounding at the top end: take the last class with weight
+                cls = -1;
+                for (int c = NCLASS - 1; c >= 0; c--)
+                    if (c != CLS_ISO && S.cnt[c] > 0 && S.rate[c] > 0.f) { cls = c; break; }
+                if (cls < 0) return 0;
+            }
+        }
+        // member selection: the k-th list entry of class cls (ballot scan)
+        int k = min((int)(u01(rnd.y) * (float)S.cnt[cls]), S.cnt[cls] - 1);
+        int slot = -1;
+        for (int base = 0; base < S.nlist; base += 32) {
+            int i = base + lane;
+            bool hit = i < S.nlist && (int)(S.list[i] & 0xFF) == cls;
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            int nh = __popc(m);
+            if (k < nh) {
+                slot = base + __fns(m, 0, k + 1);
+                break;
+            }
+            k -= nh;
+        }
+        if (slot < 0) return -DERR_INVARIANT;
+        uint32_t key = S.list[slot] >> 8;
+        int z = key >> 10;
+        int a = Q.a0 + (int)(key & 31) - HALO, b = Q.b0 + (int)((key >> 5) & 31) - HALO;
+        if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < R.NZ)) return 1;   // needs re-staging
+        t += (double)dt;
+        if (lane == 0) {
+            Touched tc;
+            int err;
+            if (cls >= CLS_C1 && cls <= CLS_C3) {
+                int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
+                float u = u01(rnd.w);
+                int sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
+                err = apply_deposition(L, a, b, z, sp, tc);
+            } else {
+                err = apply_evaporation(L, a, b, z, tc);
+            }
+            S.abort_code = err;
+            S.tc_n = tc.n;
+            for (int i = 0; i < tc.n; i++) {
+                S.tc_a[i] = tc.a[i];
+                S.tc_b[i] = tc.b[i];
+                S.tc_z[i] = tc.z[i];
+            }
+        }
+        __syncwarp();
+        if (S.abort_code) return -DERR_INVARIANT;
+        // re-classify the touched sites and update the list
+        int ntc = S.tc_n;
+        for (int i = 0; i < ntc; i++) {
+            int ta = S.tc_a[i], tb = S.tc_b[i], tz = S.tc_z[i];
+            int ia = ta - Q.a0, ib = tb - Q.b0;
+            if (ia < 0 || ia >= wa || ib < 0 || ib >= wb) {
+                hz_lo = min(hz_lo, tz);
+                hz_hi = max(hz_hi, tz);
+                continue;
+            }
+            if (tz < 0 || tz >= R.NZ) continue;
+            int ncls = site_class(L, ta, tb, tz);
+            uint32_t tkey = (uint32_t)key_of(ia + HALO, ib + HALO, tz);
+            int ts = find_slot(S, tkey, use_pos, zw0);
+            if (lane == 0) {
+                if (ts >= 0) {
+                    int oc = S.list[ts] & 0xFF;
+                    if (ncls == CLS_NONE) {
+                        S.cnt[oc]--;
+                        int last = S.nlist - 1;
+                        uint32_t le = S.list[last];
+                        S.list[ts] = le;
+                        if (use_pos) {
+                            uint32_t lk = le >> 8;
+                            int la = (lk & 31) - HALO, lb = ((lk >> 5) & 31) - HALO, lz = lk >> 10;
+                            S.pos[((lz - zw0) * QMAX + lb) * QMAX + la] = (uint16_t)ts;
+                            S.pos[((tz - zw0) * QMAX + ib) * QMAX + ia] = NOPOS;
+                        }
+                        S.nlist = last;
+                    } else if (ncls != oc) {
+                        S.cnt[oc]--;
+                        S.cnt[ncls]++;
+                        S.list[ts] = (tkey << 8) | (uint32_t)ncls;
+                    }
+                } else if (ncls != CLS_NONE) {
+                    if (S.nlist >= MCCAP) {
+                        S.abort_code = DERR_CAPACITY;
+                    } else {
+                        int ns = S.nlist++;
+                        S.list[ns] = (tkey << 8) | (uint32_t)ncls;
+                        if (use_pos) S.pos[((tz - zw0) * QMAX + ib) * QMAX + ia] = (uint16_t)ns;
+                        S.cnt[ncls]++;
+                    }
+                }
+            }
+            __syncwarp();
+            if (S.abort_code) return -S.abort_code;
+        }
+        nev++;
+    }
+}
+
+__global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
+                                                 uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
+{
+    __shared__ TileShared S;
+    int lane = threadIdx.x & 31;
+    int qi = blockIdx.x;
+    if (qi >= nq) return;
+    int qid = qlist[qi];
+    QuadDev Q = quads[qid];
+    RepDev &R = reps[Q.rep];
+    if (!R.active) return;
+    if (Q.zhi < Q.zlo) return;   // no event sites in this tile
+    for (int c = lane; c < 64; c += 32) S.rate[c] = R.rate[c];
+    if (lane < 6) S.spcum[lane >> 1][lane & 1] = R.spcum[lane >> 1][lane & 1];
+    if (lane == 0) S.abort_code = 0;
+    __syncwarp();
+    uint8_t *st = st_all + R.st_off;
+    GLat G{st, R.NA, R.NB, R.NZ, R.pitch};
+    const double t_end = R.T0 + R.tau;
+    double t = R.T0;
+    unsigned int evc = 0;
+    unsigned long long nev = 0;
+    int hz_lo = 1 << 30, hz_hi = -1;
+    int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
+    uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32) ^ (0x9E3779B9u * (uint32_t)(Q.rep + 1));
+    int zlo = Q.zlo, zhi = Q.zhi;
+    int rc = 0;
+    for (int reload = 0;; reload++) {
+        if (reload >= NRELOAD) {
+            if (lane == 0) set_error(status, DERR_TIMEOUT, qid);
+            break;
+        }
+        int need = zhi - zlo + 5;
+        if (need <= WMAX) {
+            // stage tile + halo and the layer band in shared memory
+            int spare = WMAX - need;
+            int zw0 = max(0, zlo - 2 - min(ZMARGIN, spare / 2));
+            int zw1 = min(R.NZ, zw0 + WMAX);
+            if (zw1 - zw0 < WMAX) zw0 = max(0, zw1 - WMAX);
+            int ax0 = Q.a0 - HALO, bx0 = Q.b0 - HALO;
+            int WA = wa + 2 * HALO, WB = wb + 2 * HALO, WZ = zw1 - zw0;
+            int tot = WA * WB * WZ;
+            for (int i = lane; i < tot; i += 32) {
+                int ia = i % WA;
+                int r = i / WA;
+                int ib = r % WB, iz = r / WB;
+                S.win[(iz * WX + ib) * WX + ia] = G.get(ax0 + ia, bx0 + ib, zw0 + iz);
+            }
+            __syncwarp();
+            SLat L{S.win, ax0, bx0, zw0, R.NZ};
+            if (!build_list(S, L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0)) {
+                if (lane == 0) set_error(status, DERR_CAPACITY, qid);
+                return;
+            }
+            rc = run_events(S, L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag);
+            // write back the tile and the one-column ring its events can change
+            int wa1 = wa + 2, wb1 = wb + 2;
+            int tot1 = wa1 * wb1 * WZ;
+            for (int i = lane; i < tot1; i += 32) {
+                int ia = i % wa1;
+                int r = i / wa1;
+                int ib = r % wb1, iz = r / wb1;
+                G.put(Q.a0 - 1 + ia, Q.b0 - 1 + ib, zw0 + iz, S.win[(iz * WX + ib + 1) * WX + ia + 1]);
+            }
+            if (rc > 0 && lane == 0) atomicAdd(&status->reloads, 1ull);
+        } else {
+            // band taller than the staging buffer: run from global memory
+            if (lane == 0) atomicAdd(&status->fallback, 1ull);
+            if (!build_list(S, G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0)) {
+                if (lane == 0) set_error(status, DERR_CAPACITY, qid);
+                return;
+            }
+            GLat G2 = G;
+            rc = run_events(S, G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag);
+        }
+        __syncwarp();
+        // z band of the remaining event sites
+        int lo = 1 << 30, hi = -1;
+        for (int i = lane; i < S.nlist; i += 32) {
+            int z = (int)(S.list[i] >> 18);
+            lo = min(lo, z);
+            hi = max(hi, z);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        zlo = lo;
+        zhi = hi;
+        if (rc < 0) {
+            if (lane == 0) set_error(status, -rc, qid);
+            break;
+        }
+        if (rc == 0 || zhi < zlo) break;
+        __syncwarp();
+    }
+    __syncwarp();
+    if (lane == 0) {
+        quads[qid].zlo = zlo;
+        quads[qid].zhi = zhi;
+        quads[qid].mc = S.nlist;
+        if (nev) atomicAdd(&R.events, nev);
+        if (hz_hi >= 0) {
+            // widen the z bands of the neighbouring tiles whose sites changed
+            int qa = (Q.a0 * R.nqa) / R.NA, qb = (Q.b0 * R.nqb) / R.NB;
+            // recover exact tile indices (tiles are [floor(i*NA/nqa), floor((i+1)*NA/nqa)))
+            while (qa > 0 && (qa * R.NA) / R.nqa > Q.a0) qa--;
+            while (qa + 1 < R.nqa && ((qa + 1) * R.NA) / R.nqa <= Q.a0) qa++;
+            while (qb > 0 && (qb * R.NB) / R.nqb > Q.b0) qb--;
+            while (qb + 1 < R.nqb && ((qb + 1) * R.NB) / R.nqb <= Q.b0) qb++;
+            for (int db = -1; db <= 1; db++)
+                for (int da = -1; da <= 1; da++) {
+                    if (!da && !db) continue;
+                    int na = (qa + da + R.nqa) % R.nqa, nb = (qb + db + R.nqb) % R.nqb;
+                    QuadDev *N = &quads[R.quad_base + nb * R.nqa + na];
+                    atomicMin(&N->zlo, hz_lo);
+                    atomicMax(&N->zhi, hz_hi);
+                }
+        }
+    }
+}
+
+// End of a window: advance the replica clock, apply the exit conditions.
+__global__ void k_window_end(RepDev *reps, QuadDev *quads)
+{
+    RepDev &R = reps[blockIdx.x];
+    long long s = 0;
+    int nqt = R.nqa * R.nqb;
+    for (int i = threadIdx.x; i < nqt; i += blockDim.x) s += quads[R.quad_base + i].mc;
+    __shared__ long long sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        R.mc_count = sh[0];
+        if (!R.active) return;
+        R.T0 += R.tau;
+        R.window++;
+        if (R.mc_count <= 20) {
+            R.active = 0;
+            R.stop_reason = 1;
+        } else if ((long long)R.events >= R.ev_max) {
+            R.active = 0;
+            R.stop_reason = 2;
+        } else if (R.T0 >= R.t_max) {
+            R.active = 0;
+            R.stop_reason = 3;
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return fail(MKS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+struct RepHost {
+    mks_config cfg;
+    int NA, NB, NZ, pitch;
+    int nqa, nqb, quad_base;
+    int64_t st_off;
+    double ptransE[3 * 4096];
+    double ptransD[9];
+    bool rates_set = false;
+};
+
+}  // namespace
+
+struct mks_handle {
+    std::vector<RepHost> reps;
+    std::vector<QuadDev> quads_h;
+    std::vector<int> color_list_h[4];
+    int64_t st_bytes = 0;
+    uint8_t *d_st = nullptr;
+    RepDev *d_reps = nullptr;
+    QuadDev *d_quads = nullptr;
+    int *d_clist[4] = {nullptr, nullptr, nullptr, nullptr};
+    DevStatus *d_status = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_windows = 0;
+    uint32_t phase_counter = 0;
+    int64_t last_kernels = 0, last_graphs = 0, last_phase_launches = 0;
+    double last_ms = 0.0;
+    double time_acc = 0.0;
+};
+
+namespace {
+
+void rate_tables(const RepHost &r, RepDev &d)
+{
+    for (int c = 0; c < 64; c++) d.rate[c] = 0.f;
+    const double *pD = r.ptransD;
+    for (int co = 1; co <= 3; co++) {
+        double p1 = pD[co - 1], p2 = pD[3 + co - 1], p3 = pD[6 + co - 1];
+        double tot = p1 + p2 + p3;
+        int cls = co == 1 ? CLS_C1 : (co == 2 ? CLS_C2 : CLS_C3);
+        d.rate[cls] = (float)tot;
+        d.spcum[co - 1][0] = tot > 0 ? (float)(p1 / tot) : 1.f;
+        d.spcum[co - 1][1] = tot > 0 ? (float)((p1 + p2) / tot) : 1.f;
+    }
+    d.rate[CLS_C1D] = 1.e-8f;   // Get_Prob.f:183
+    d.rate[CLS_ISO] = 0.f;      // dynamic: 1e5 x tile rate (Get_Prob.f:305)
+    for (int sp = 1; sp <= 3; sp++)
+        for (int n1 = 0; n1 <= 3; n1++)
+            for (int n2 = 0; n2 <= 3; n2++)
+                for (int n3 = 0; n3 <= 3; n3++) {
+                    int t = n1 + n2 + n3;
+                    if (t < 1 || t > 3) continue;
+                    double v = r.ptransE[(sp - 1) * 4096 + n1 * 1024 + n2 * 256 + n3 * 64];
+                    d.rate[CLS_OCC0 + (sp - 1) * NCENSUS + census_index(n1, n2, n3)] = (float)v;
+                }
+}
+
+int check_config(const mks_config &c)
+{
+    if (c.lenx <= 0 || c.leny <= 0 || c.lenz <= 0 || c.lenx % 12 || c.leny % 12 || c.lenz % 3)
+        return fail(MKS_ERR_ARG, "box %dx%dx%d: LenX, LenY must be multiples of 12 and LenZ of 3", c.lenx, c.leny,
+                    c.lenz);
+    if (c.lenx / 6 < 16 || c.leny / 6 < 16)
+        return fail(MKS_ERR_ARG, "box side %d/%d too small (needs >= 96 grid units)", c.lenx, c.leny);
+    if (c.ncrystal < 1 || c.ncrystal > 3) return fail(MKS_ERR_ARG, "NCrystal must be 1..3");
+    if (c.ncov != 0) return fail(MKS_ERR_UNSUPPORTED, "coverage species (NCov>0) are not in the GPU engine");
+    if (c.ptrans_zig != 1.0)
+        return fail(MKS_ERR_UNSUPPORTED, "PtransZig=%g: arm-chair stacking is not in the compact GPU lattice", c.ptrans_zig);
+    return 0;
+}
+
+// even number of tiles per side, widths within [8, QMAX]
+int tiles_for(int n)
+{
+    int t = 2 * (n / 16);
+    if (t < 2) t = 2;
+    while ((n + t - 1) / t > QMAX) t += 2;
+    return t;
+}
+
+int upload_reps(mks_handle *h, const std::vector<RepDev> &d)
+{
+    CK(cudaMemcpyAsync(h->d_reps, d.data(), sizeof(RepDev) * d.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int download_reps(mks_handle *h, std::vector<RepDev> &d)
+{
+    d.resize(h->reps.size());
+    CK(cudaMemcpyAsync(d.data(), h->d_reps, sizeof(RepDev) * d.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int read_status(mks_handle *h, DevStatus &s)
+{
+    CK(cudaMemcpyAsync(&s, h->d_status, sizeof s, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int rescan(mks_handle *h)
+{
+    k_quad_scan<<<(int)h->quads_h.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, (int)h->quads_h.size(), h->d_st,
+                                                               h->d_status);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int create_impl(const mks_config *cfgs, int n, mks_handle **out)
+{
+    if (!cfgs || n <= 0 || !out) return fail(MKS_ERR_ARG, "bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(MKS_ERR_CUDA, "no CUDA device: the GB300 engine has no CPU path");
+    mks_handle *h = new mks_handle();
+    int64_t off = 0;
+    for (int i = 0; i < n; i++) {
+        int rc = check_config(cfgs[i]);
+        if (rc) {
+            delete h;
+            return rc;
+        }
+        RepHost r;
+        r.cfg = cfgs[i];
+        r.NA = cfgs[i].lenx / 6;
+        r.NB = cfgs[i].leny / 6;
+        r.NZ = cfgs[i].lenz / 3 + 1;
+        r.pitch = (r.NA + 15) & ~15;
+        r.nqa = tiles_for(r.NA);
+        r.nqb = tiles_for(r.NB);
+        r.quad_base = (int)h->quads_h.size();
+        r.st_off = off;
+        off += (int64_t)r.NZ * r.NB * r.pitch;
+        off = (off + 255) & ~(int64_t)255;
+        memset(r.ptransE, 0, sizeof r.ptransE);
+        memset(r.ptransD, 0, sizeof r.ptransD);
+        for (int qb = 0; qb < r.nqb; qb++)
+            for (int qa = 0; qa < r.nqa; qa++) {
+                QuadDev q;
+                q.rep = i;
+                q.a0 = (qa * r.NA) / r.nqa;
+                q.a1 = ((qa + 1) * r.NA) / r.nqa;
+                q.b0 = (qb * r.NB) / r.nqb;
+                q.b1 = ((qb + 1) * r.NB) / r.nqb;
+                q.zlo = 1 << 30;
+                q.zhi = -1;
+                q.mc = 0;
+                h->color_list_h[(qa & 1) + 2 * (qb & 1)].push_back((int)h->quads_h.size());
+                h->quads_h.push_back(q);
+            }
+        h->reps.push_back(r);
+    }
+    h->st_bytes = off;
+    auto cleanup_fail = [&](const char *what, cudaError_t e) {
+        fail(MKS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+        mks_destroy(h);
+        return MKS_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return cleanup_fail("stream", e);
+    if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return cleanup_fail("event", e);
+    if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return cleanup_fail("event", e);
+    if ((e = cudaMalloc(&h->d_st, (size_t)h->st_bytes)) != cudaSuccess) return cleanup_fail("lattice allocation", e);
+    if ((e = cudaMemsetAsync(h->d_st, 0, (size_t)h->st_bytes, h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
+    if ((e = cudaMalloc(&h->d_reps, sizeof(RepDev) * n)) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMalloc(&h->d_quads, sizeof(QuadDev) * h->quads_h.size())) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMalloc(&h->d_status, sizeof(DevStatus))) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
+    for (int c = 0; c < 4; c++) {
+        size_t nb = sizeof(int) * std::max<size_t>(1, h->color_list_h[c].size());
+        if ((e = cudaMalloc(&h->d_clist[c], nb)) != cudaSuccess) return cleanup_fail("alloc", e);
+        if (!h->color_list_h[c].empty() &&
+            (e = cudaMemcpyAsync(h->d_clist[c], h->color_list_h[c].data(), sizeof(int) * h->color_list_h[c].size(),
+                                 cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+            return cleanup_fail("copy", e);
+    }
+    if ((e = cudaMemcpyAsync(h->d_quads, h->quads_h.data(), sizeof(QuadDev) * h->quads_h.size(),
+                             cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+        return cleanup_fail("copy", e);
+    std::vector<RepDev> d(n);
+    for (int i = 0; i < n; i++) {
+        memset(&d[i], 0, sizeof(RepDev));
+        const RepHost &r = h->reps[i];
+        d[i].st_off = r.st_off;
+        d[i].NA = r.NA;
+        d[i].NB = r.NB;
+        d[i].NZ = r.NZ;
+        d[i].pitch = r.pitch;
+        d[i].nqa = r.nqa;
+        d[i].nqb = r.nqb;
+        d[i].quad_base = r.quad_base;
+        d[i].tau = 1e-6;
+        d[i].T0 = 0.0;
+        d[i].t_max = 1e300;
+        d[i].ev_max = (long long)9e18;
+        d[i].seed = r.cfg.seed;
+        d[i].active = 1;
+        rate_tables(r, d[i]);
+    }
+    int rc = upload_reps(h, d);
+    if (rc) {
+        mks_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return 0;
+}
+
+// one window = 4 colour phases + window end
+int launch_window(mks_handle *h)
+{
+    for (int c = 0; c < 4; c++) {
+        int nq = (int)h->color_list_h[c].size();
+        if (!nq) continue;
+        k_sl_phase<<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st, h->d_status,
+                                             (uint32_t)c);
+        h->last_kernels++;
+        h->last_phase_launches++;
+    }
+    k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads);
+    h->last_kernels++;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_events, double max_time)
+{
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    for (size_t i = 0; i < d.size(); i++) {
+        if (!(tau[i] > 0.0)) return fail(MKS_ERR_ARG, "tau must be > 0");
+        d[i].tau = tau[i];
+        d[i].ev_max = max_events > 0 ? (long long)(d[i].events + (unsigned long long)max_events) : (long long)9e18;
+        d[i].t_max = max_time > 0 ? max_time : 1e300;
+        d[i].active = d[i].stop_reason == 1 ? 0 : 1;
+        if (d[i].active) d[i].stop_reason = 0;
+    }
+    rc = upload_reps(h, d);
+    if (rc) return rc;
+    rc = rescan(h);
+    if (rc) return rc;
+    h->last_kernels = 1;
+    h->last_graphs = 0;
+    h->last_phase_launches = 0;
+    // capture a block of windows once, replay it
+    const int WPG = (int)std::max<int64_t>(1, std::min<int64_t>(8, max_windows));
+    if (!h->graph_exec || h->graph_windows != WPG) {
+        if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int64_t k0 = h->last_kernels, p0 = h->last_phase_launches;
+        for (int w = 0; w < WPG; w++) {
+            int r2 = launch_window(h);
+            if (r2) {
+                cudaStreamEndCapture(h->stream, &g);
+                return r2;
+            }
+        }
+        h->last_kernels = k0;
+        h->last_phase_launches = p0;
+        CK(cudaStreamEndCapture(h->stream, &g));
+        CK(cudaGraphInstantiate(&h->graph_exec, g, 0));
+        cudaGraphDestroy(g);
+        h->graph_windows = WPG;
+    }
+    int64_t kernels_per_graph = 0, phases_per_graph = 0;
+    for (int c = 0; c < 4; c++)
+        if (!h->color_list_h[c].empty()) phases_per_graph++;
+    kernels_per_graph = (phases_per_graph + 1) * WPG;
+    phases_per_graph *= WPG;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    int64_t done = 0;
+    while (done < max_windows) {
+        CK(cudaGraphLaunch(h->graph_exec, h->stream));
+        h->last_graphs++;
+        h->last_kernels += kernels_per_graph;
+        h->last_phase_launches += phases_per_graph;
+        done += WPG;
+        // poll the replica state every few blocks of windows
+        if ((h->last_graphs & 7) == 0 || done >= max_windows) {
+            DevStatus s;
+            rc = read_status(h, s);
+            if (rc) return rc;
+            if (s.error) return fail(s.error, "device error %d in tile %d", s.error, s.err_quad);
+            rc = download_reps(h, d);
+            if (rc) return rc;
+            bool any = false;
+            for (auto &x : d) any |= x.active != 0;
+            if (!any) break;
+        }
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->last_ms = ms;
+    DevStatus s;
+    rc = read_status(h, s);
+    if (rc) return rc;
+    if (s.error) return fail(s.error, "device error %d in tile %d", s.error, s.err_quad);
+    return 0;
+}
+
+int obs_impl(mks_handle *h, int rep, mks_observables *o)
+{
+    memset(o, 0, sizeof *o);
+    unsigned long long *d_cnt = nullptr, *d_hist = nullptr;
+    double *d_h = nullptr;
+    CK(cudaMallocAsync(&d_cnt, sizeof(unsigned long long) * 8, h->stream));
+    CK(cudaMallocAsync(&d_h, sizeof(double) * 2, h->stream));
+    CK(cudaMallocAsync(&d_hist, sizeof(unsigned long long) * NCLASS, h->stream));
+    CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 8, h->stream));
+    CK(cudaMemsetAsync(d_h, 0, sizeof(double) * 2, h->stream));
+    CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
+    const RepHost &r = h->reps[rep];
+    int ncol = r.NA * r.NB;
+    k_observables<<<std::min(1024, (ncol + 255) / 256), 256, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_cnt, d_h);
+    k_class_hist<<<1024, 256, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_hist);
+    CK(cudaGetLastError());
+    unsigned long long cnt[8], hist[NCLASS];
+    double hs[2];
+    CK(cudaMemcpyAsync(cnt, d_cnt, sizeof cnt, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hs, d_h, sizeof hs, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hist, d_hist, sizeof hist, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_cnt, h->stream);
+    cudaFreeAsync(d_h, h->stream);
+    cudaFreeAsync(d_hist, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    o->events = (int64_t)d[rep].events;
+    o->time = d[rep].T0;
+    o->atoms = (int64_t)cnt[0];
+    o->undercoord = (int64_t)cnt[1];
+    o->voids = (int64_t)cnt[2];
+    o->species[0] = (int64_t)cnt[3];
+    o->species[1] = (int64_t)cnt[4];
+    o->species[2] = (int64_t)cnt[5];
+    double ncols = (double)cnt[6];
+    if (ncols > 0) {
+        o->mean_height = hs[0] / ncols;
+        double var = hs[1] / ncols - o->mean_height * o->mean_height;
+        o->rms_roughness = var > 0 ? sqrt(var) : 0.0;
+    }
+    double rt = 0.0;
+    int64_t mc = 0;
+    for (int c = 1; c < NCLASS; c++) {
+        mc += (int64_t)hist[c];
+        if (c != CLS_ISO) rt += (double)hist[c] * (double)d[rep].rate[c];
+    }
+    rt += (double)hist[CLS_ISO] * 1.0e5 * rt;
+    o->mc_sites = mc;
+    o->total_rate = rt;
+    o->nonepitaxial = 0;
+    return 0;
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+const char *mks_version(void) { return "mulskips_gb300 0.1 (sm_103a)"; }
+
+int mks_last_error(char *buf, int32_t len)
+{
+    if (!buf || len <= 0) return MKS_ERR_ARG;
+    snprintf(buf, (size_t)len, "%s", g_err.c_str());
+    return 0;
+}
+
+int mks_create(const mks_config *cfg, mks_handle **out) { return create_impl(cfg, 1, out); }
+int mks_batch_create(const mks_config *cfgs, int32_t n, mks_handle **out) { return create_impl(cfgs, n, out); }
+int32_t mks_batch_size(mks_handle *h) { return h ? (int32_t)h->reps.size() : 0; }
+
+void mks_destroy(mks_handle *h)
+{
+    if (!h) return;
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_st);
+    cudaFree(h->d_reps);
+    cudaFree(h->d_quads);
+    cudaFree(h->d_status);
+    for (int c = 0; c < 4; c++) cudaFree(h->d_clist[c]);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int mks_batch_set_rates(mks_handle *h, const double *ptransE, const double *ptransD)
+{
+    if (!h || !ptransE || !ptransD) return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        memcpy(h->reps[i].ptransE, ptransE + i * 3 * 4096, sizeof(double) * 3 * 4096);
+        memcpy(h->reps[i].ptransD, ptransD + i * 9, sizeof(double) * 9);
+        h->reps[i].rates_set = true;
+        rate_tables(h->reps[i], d[i]);
+    }
+    return upload_reps(h, d);
+}
+
+int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD)
+{
+    if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_set_rates needs a single-replica handle");
+    return mks_batch_set_rates(h, ptransE, ptransD);
+}
+
+int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1)
+{
+    if (!h || !len1 || (kind != 'S' && kind != 'C')) return fail(MKS_ERR_ARG, "bad arguments");
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        const RepHost &r = h->reps[i];
+        int l1 = len1[i] - len1[i] % 24;
+        if (l1 < 24 || l1 + 3 > r.cfg.lenz - 7) return fail(MKS_ERR_ARG, "Len1 %d outside the box", len1[i]);
+        if (kind == 'C' && r.cfg.ncrystal < 2) return fail(MKS_ERR_ARG, "SiC needs NCrystal=2");
+        int64_t n = (int64_t)r.NZ * r.NB * r.pitch;
+        int blocks = (int)std::min<int64_t>(4096, (n + 255) / 256);
+        k_init_flat<<<blocks, 256, 0, h->stream>>>(h->d_st + r.st_off, r.NA, r.NB, r.NZ, r.pitch, r.cfg.lenz, l1,
+                                                   kind == 'C');
+    }
+    CK(cudaGetLastError());
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    for (auto &x : d) {
+        x.T0 = 0.0;
+        x.events = 0;
+        x.window = 0;
+        x.active = 1;
+        x.stop_reason = 0;
+    }
+    rc = upload_reps(h, d);
+    if (rc) return rc;
+    return rescan(h);
+}
+
+int mks_init_flat(mks_handle *h, char kind, int32_t len1) { return mks_batch_init_flat(h, kind, &len1); }
+
+int64_t mks_state_size(mks_handle *h)
+{
+    if (!h || h->reps.empty()) return 0;
+    const RepHost &r = h->reps[0];
+    return (int64_t)r.NZ * r.NB * r.NA;
+}
+
+int mks_get_state(mks_handle *h, uint8_t *out, int64_t n)
+{
+    if (!h || !out || n < mks_state_size(h)) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    CK(cudaMemcpy2DAsync(out, r.NA, h->d_st + r.st_off, r.pitch, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyDeviceToHost,
+                         h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int mks_set_state(mks_handle *h, const uint8_t *in, int64_t n)
+{
+    if (!h || !in || n < mks_state_size(h) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    CK(cudaMemcpy2DAsync(h->d_st + r.st_off, r.pitch, in, r.NA, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyHostToDevice,
+                         h->stream));
+    return rescan(h);
+}
+
+int mks_get_lattice(mks_handle *h, int32_t *lc)
+{
+    if (!h || !lc) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    std::vector<uint8_t> st((size_t)mks_state_size(h));
+    int rc = mks_get_state(h, st.data(), (int64_t)st.size());
+    if (rc) return rc;
+    int lx = r.cfg.lenx, ly = r.cfg.leny, lz = r.cfg.lenz;
+    memset(lc, 0, sizeof(int32_t) * (size_t)lx * ly * (lz + 1));
+    // wall planes of SetSi cover every grid point (SetSi.f:38-46,212-220):
+    // a wall layer z1 stands for grid planes 3*z1 .. 3*z1+2
+    for (int z1 = 0; z1 < r.NZ; z1++) {
+        if (st[(size_t)z1 * r.NB * r.NA + (size_t)((z1 >> 1) & 1)] != WALL) continue;
+        for (int zz = 3 * z1; zz < 3 * z1 + 3 && zz <= lz; zz++)
+            for (size_t k = 0; k < (size_t)lx * ly; k++) lc[(size_t)lx * ly * zz + k] = (1 << 23) | 113;
+    }
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            for (int a = 0; a < r.NA; a++) {
+                uint8_t s = st[((size_t)z1 * r.NB + b) * r.NA + a];
+                if (((a + b + (z1 >> 1)) & 1) || s == 0) continue;
+                int x = 3 * (2 * a + (z1 & 1)), y = 3 * (2 * b + (z1 & 1)), z = 3 * z1;
+                if (z > lz) continue;
+                int32_t v;
+                if (s == WALL) continue;
+                int sp = sp_of(s), co = co_of(s);
+                v = (co << 24) | (sp ? (1 << 23) : 0) | (sp << 27);
+                lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] = v;
+            }
+    return 0;
+}
+
+int mks_load_lattice(mks_handle *h, const int32_t *lc)
+{
+    if (!h || !lc || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    int lx = r.cfg.lenx, ly = r.cfg.leny;
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    auto at = [&](int a, int b, int z) -> uint8_t & {
+        a = (a % r.NA + r.NA) % r.NA;
+        b = (b % r.NB + r.NB) % r.NB;
+        return st[((size_t)z * r.NB + b) * r.pitch + a];
+    };
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            for (int a = 0; a < r.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                int x = 3 * (2 * a + (z1 & 1)), y = 3 * (2 * b + (z1 & 1)), z = 3 * z1;
+                int32_t v = lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)];
+                if ((v & 255) == 113) {
+                    at(a, b, z1) = WALL;
+                    continue;
+                }
+                if ((v & 255) != 0) return fail(MKS_ERR_UNSUPPORTED, "coverage species in LattCoo");
+                int occ = (v >> 23) & 1, co = (v >> 24) & 7, sp = (v >> 27) & 7;
+                if (sp > 3 || (occ && !sp) || (!occ && sp)) return fail(MKS_ERR_INVARIANT, "bad LattCoo word %d", v);
+                at(a, b, z1) = mk(sp, co, 0, 0);
+            }
+    // the first list entry of a coor-1 empty site is its one occupied
+    // neighbour; its dummy flag follows that neighbour's coordination
+    // (Get_Prob.f:156-184), as a rebuild from LattCoo gives (SetCAD.f:301-418)
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            for (int a = 0; a < r.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                uint8_t s = at(a, b, z1);
+                if (s == WALL || sp_of(s) || co_of(s) != 1) continue;
+                int found = -1;
+                uint8_t ns = 0;
+                for (int d = 0; d < 4; d++) {
+                    int da, db, dz;
+                    nb_off(z1 & 1, d, da, db, dz);
+                    if (z1 + dz < 0 || z1 + dz >= r.NZ) continue;
+                    uint8_t t = at(a + da, b + db, z1 + dz);
+                    if (t != WALL && sp_of(t)) {
+                        found = d;
+                        ns = t;
+                    }
+                }
+                if (found < 0) return fail(MKS_ERR_INVARIANT, "coor-1 site without neighbour");
+                at(a, b, z1) = mk(0, 1, found, co_of(ns) < 2 ? 1 : 0);
+            }
+    CK(cudaMemcpyAsync(h->d_st + r.st_off, st.data(), st.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return rescan(h);
+}
+
+int mks_replay(mks_handle *h, const mks_event *trace, int64_t n)
+{
+    if (!h || (n > 0 && !trace) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    if (n == 0) return 0;
+    mks_event *d_ev = nullptr;
+    long long *d_done = nullptr;
+    CK(cudaMallocAsync(&d_ev, sizeof(mks_event) * (size_t)n, h->stream));
+    CK(cudaMallocAsync(&d_done, sizeof(long long), h->stream));
+    CK(cudaMemcpyAsync(d_ev, trace, sizeof(mks_event) * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+    k_replay<<<1, 32, 0, h->stream>>>(h->d_reps, h->d_st, d_ev, n, h->d_status, d_done);
+    CK(cudaGetLastError());
+    long long done = 0;
+    CK(cudaMemcpyAsync(&done, d_done, sizeof done, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_ev, h->stream);
+    cudaFreeAsync(d_done, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    DevStatus s;
+    int rc = read_status(h, s);
+    if (rc) return rc;
+    if (s.error) {
+        CK(cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream));
+        return fail(s.error, "replay: event %lld is not applicable to the lattice state", done);
+    }
+    return rescan(h);
+}
+
+int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events, double max_time,
+            int64_t *events_done, double *time_out)
+{
+    if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_run needs a single-replica handle");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    unsigned long long e0 = d[0].events;
+    rc = run_impl(h, &tau, max_windows, max_events, max_time);
+    if (rc) return rc;
+    rc = download_reps(h, d);
+    if (rc) return rc;
+    if (events_done) *events_done = (int64_t)(d[0].events - e0);
+    if (time_out) *time_out = d[0].T0;
+    return 0;
+}
+
+int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_events_each,
+                  double max_time_each, int64_t *events_total)
+{
+    if (!h || !tau) return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    unsigned long long e0 = 0;
+    for (auto &x : d) e0 += x.events;
+    rc = run_impl(h, tau, max_windows, max_events_each, max_time_each);
+    if (rc) return rc;
+    rc = download_reps(h, d);
+    if (rc) return rc;
+    unsigned long long e1 = 0;
+    for (auto &x : d) e1 += x.events;
+    if (events_total) *events_total = (int64_t)(e1 - e0);
+    return 0;
+}
+
+int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
+{
+    if (!h || !hist || nclass < NCLASS) return fail(MKS_ERR_ARG, "bad arguments");
+    unsigned long long *d_hist = nullptr;
+    CK(cudaMallocAsync(&d_hist, sizeof(unsigned long long) * NCLASS, h->stream));
+    CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
+    k_class_hist<<<1024, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, d_hist);
+    CK(cudaGetLastError());
+    unsigned long long tmp[NCLASS];
+    CK(cudaMemcpyAsync(tmp, d_hist, sizeof tmp, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_hist, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < nclass; i++) hist[i] = i < NCLASS ? (int64_t)tmp[i] : 0;
+    return 0;
+}
+
+int mks_get_observables(mks_handle *h, mks_observables *obs)
+{
+    if (!h || !obs) return fail(MKS_ERR_ARG, "bad arguments");
+    return obs_impl(h, 0, obs);
+}
+
+int mks_batch_observables(mks_handle *h, mks_observables *obs)
+{
+    if (!h || !obs) return fail(MKS_ERR_ARG, "bad arguments");
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        int rc = obs_impl(h, (int)i, &obs[i]);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+int mks_get_status(mks_handle *h, mks_status *st)
+{
+    if (!h || !st) return fail(MKS_ERR_ARG, "bad arguments");
+    DevStatus s;
+    int rc = read_status(h, s);
+    if (rc) return rc;
+    std::vector<RepDev> d;
+    rc = download_reps(h, d);
+    if (rc) return rc;
+    memset(st, 0, sizeof *st);
+    st->error = s.error;
+    st->fallback_tiles = (int64_t)s.fallback;
+    st->windows = d[0].window;
+    st->active = d[0].active;
+    st->stop_reason = d[0].stop_reason;
+    return 0;
+}
+
+int mks_last_run_stats(mks_handle *h, int64_t *kernel_launches, int64_t *graph_launches, double *kernel_ms,
+                       int64_t *phase_launches)
+{
+    if (!h) return fail(MKS_ERR_ARG, "bad arguments");
+    if (kernel_launches) *kernel_launches = h->last_kernels;
+    if (graph_launches) *graph_launches = h->last_graphs;
+    if (kernel_ms) *kernel_ms = h->last_ms;
+    if (phase_launches) *phase_launches = h->last_phase_launches;
+    return 0;
+}
+
+}  // extern "C"

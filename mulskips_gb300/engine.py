@@ -1,0 +1,193 @@
+"""Python face of the GB300 KMC engine (a thin layer over the C ABI).
+
+`Lattice` is one KMC system (the plain path, `mks_*`); `Batch` holds many
+independent replicas advanced together (`mks_batch_*`).  Both keep their
+state on the GPU; the methods copy in and out through host buffers.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _native as N
+
+KB_EV = 0.00008617330350  # Boltzmann constant in eV/K, mulskips-source/mcevent/Get_Prob.f:70
+
+
+def arrhenius_tables(T, e_bond=0.6, nu=1e13, flux=0.5, ncrystal=1):
+    """PTransE / PTransD arrays of the plain Si(001) model: evaporation rate
+    nu*exp(-n*e_bond/kT) for an atom with n bonded neighbours (n = 1..3) and a
+    deposition rate `flux` on every empty site with >= 1 bonded neighbour."""
+    pE = np.zeros((3, 4, 4, 4, 4, 4, 4), dtype=np.float64)
+    pD = np.zeros((3, 3), dtype=np.float64)
+    for n in (1, 2, 3):
+        pE[0, n, 0, 0, 0, 0, 0] = nu * math.exp(-n * e_bond / (KB_EV * T))
+        pD[0, n - 1] = flux
+    return pE, pD
+
+
+def _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed):
+    c = N.MksConfig()
+    c.lenx, c.leny, c.lenz = int(lenx), int(leny), int(lenz)
+    c.ncrystal, c.ncov = int(ncrystal), 0
+    lc = list(list_crystal) + [0] * (3 - len(list_crystal))
+    for i in range(3):
+        c.list_crystal[i] = int(lc[i])
+    c.ptrans_zig = float(ptrans_zig)
+    c.sf = float(sf)
+    c.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    return c
+
+
+class Lattice:
+    """One KMC system on the GPU."""
+
+    def __init__(self, lenx, leny, lenz, ncrystal=1, list_crystal=(14,), ptrans_zig=1.0, sf=5.43 / 12,
+                 seed=1):
+        self.dims = (int(lenx), int(leny), int(lenz))
+        self.na, self.nb, self.nz = lenx // 6, leny // 6, lenz // 3 + 1
+        h = C.c_void_p()
+        N.check(N.lib().mks_create(C.byref(_cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf,
+                                                 seed)), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            N.lib().mks_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_rates(self, ptransE, ptransD):
+        e = np.ascontiguousarray(ptransE, dtype=np.float64).reshape(-1)
+        d = np.ascontiguousarray(ptransD, dtype=np.float64).reshape(-1)
+        assert e.size == 3 * 4096 and d.size == 9
+        N.check(N.lib().mks_set_rates(self._h, N.ptr(e), N.ptr(d)))
+
+    def init_flat(self, kind="S", len1=120):
+        N.check(N.lib().mks_init_flat(self._h, kind.encode()[:1], int(len1)))
+
+    def replay(self, events):
+        ev = np.ascontiguousarray(events, dtype=N.EVENT_DTYPE)
+        N.check(N.lib().mks_replay(self._h, N.ptr(ev), int(ev.size)))
+
+    def run(self, tau, max_windows, max_events=0, max_time=0.0):
+        ne = C.c_int64()
+        t = C.c_double()
+        N.check(N.lib().mks_run(self._h, float(tau), int(max_windows), int(max_events), float(max_time),
+                                C.byref(ne), C.byref(t)))
+        return ne.value, t.value
+
+    def state(self):
+        n = N.lib().mks_state_size(self._h)
+        a = np.empty(n, dtype=np.uint8)
+        N.check(N.lib().mks_get_state(self._h, N.ptr(a), n))
+        return a.reshape(self.nz, self.nb, self.na)
+
+    def set_state(self, st):
+        a = np.ascontiguousarray(st, dtype=np.uint8).reshape(-1)
+        N.check(N.lib().mks_set_state(self._h, N.ptr(a), a.size))
+
+    def set_state_ptr(self, addr, n):
+        """Upload from a raw host address (e.g. a pinned buffer)."""
+        N.check(N.lib().mks_set_state(self._h, C.c_void_p(addr), int(n)))
+
+    def get_state_ptr(self, addr, n):
+        N.check(N.lib().mks_get_state(self._h, C.c_void_p(addr), int(n)))
+
+    def class_histogram(self):
+        h = np.zeros(N.MKS_NCLASS, dtype=np.int64)
+        N.check(N.lib().mks_class_histogram(self._h, N.ptr(h), N.MKS_NCLASS))
+        return h
+
+    def observables(self):
+        o = N.MksObservables()
+        N.check(N.lib().mks_get_observables(self._h, C.byref(o)))
+        return o.as_dict()
+
+    def status(self):
+        s = N.MksStatus()
+        N.check(N.lib().mks_get_status(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def lattcoo(self):
+        lx, ly, lz = self.dims
+        a = np.empty((lz + 1, ly, lx), dtype=np.int32)
+        N.check(N.lib().mks_get_lattice(self._h, N.ptr(a)))
+        return a
+
+    def load_lattcoo(self, arr):
+        a = np.ascontiguousarray(arr, dtype=np.int32)
+        lx, ly, lz = self.dims
+        assert a.size == lx * ly * (lz + 1)
+        N.check(N.lib().mks_load_lattice(self._h, N.ptr(a)))
+
+    def run_stats(self):
+        k, g, p = C.c_int64(), C.c_int64(), C.c_int64()
+        ms = C.c_double()
+        N.check(N.lib().mks_last_run_stats(self._h, C.byref(k), C.byref(g), C.byref(ms), C.byref(p)))
+        return {"kernel_launches": k.value, "graph_launches": g.value, "kernel_ms": ms.value,
+                "phase_launches": p.value}
+
+
+class Batch:
+    """Independent replicas of uneven boxes advanced together."""
+
+    def __init__(self, boxes, seeds, ncrystal=1, list_crystal=(14,), sf=5.43 / 12):
+        cfgs = (N.MksConfig * len(boxes))()
+        for i, (b, s) in enumerate(zip(boxes, seeds)):
+            cfgs[i] = _cfg(b[0], b[1], b[2], ncrystal, list_crystal, 1.0, sf, s)
+        h = C.c_void_p()
+        N.check(N.lib().mks_batch_create(cfgs, len(boxes), C.byref(h)))
+        self._h = h
+        self.n = len(boxes)
+
+    def close(self):
+        if self._h:
+            N.lib().mks_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_rates(self, ptransE, ptransD):
+        e = np.ascontiguousarray(ptransE, dtype=np.float64).reshape(-1)
+        d = np.ascontiguousarray(ptransD, dtype=np.float64).reshape(-1)
+        assert e.size == self.n * 3 * 4096 and d.size == self.n * 9
+        N.check(N.lib().mks_batch_set_rates(self._h, N.ptr(e), N.ptr(d)))
+
+    def init_flat(self, kind, len1):
+        l1 = np.ascontiguousarray(len1, dtype=np.int32)
+        N.check(N.lib().mks_batch_init_flat(self._h, kind.encode()[:1], N.ptr(l1)))
+
+    def run(self, tau, max_windows, max_events_each=0, max_time_each=0.0):
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(tau, dtype=np.float64), (self.n,)))
+        ne = C.c_int64()
+        N.check(N.lib().mks_batch_run(self._h, N.ptr(t), int(max_windows), int(max_events_each),
+                                      float(max_time_each), C.byref(ne)))
+        return ne.value
+
+    def observables(self):
+        o = (N.MksObservables * self.n)()
+        N.check(N.lib().mks_batch_observables(self._h, o))
+        return [x.as_dict() for x in o]
+
+    def run_stats(self):
+        k, g, p = C.c_int64(), C.c_int64(), C.c_int64()
+        ms = C.c_double()
+        N.check(N.lib().mks_last_run_stats(self._h, C.byref(k), C.byref(g), C.byref(ms), C.byref(p)))
+        return {"kernel_launches": k.value, "graph_launches": g.value, "kernel_ms": ms.value,
+                "phase_launches": p.value}

@@ -1836,3 +1836,102 @@ void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9])
     for (int s = 0; s < 3; s++)
         for (int c = 0; c < 3; c++) ptransD[s * 3 + c] = o->ptransD[s][c];
 }
+
+/* Conversion to the one-byte-per-site layout of the GPU engine (used by the
+ * parity tests to compare states). */
+int64_t ora_compact_state(const ora_t *o, uint8_t *out)
+{
+    static const int OFF[2][4][3] = {{{0, 0, 1}, {0, -1, -1}, {-1, -1, 1}, {-1, 0, -1}},
+                                     {{1, 1, -1}, {1, 0, 1}, {0, 0, -1}, {0, 1, 1}}};
+    int na = o->lx / 6, nb = o->ly / 6, nz = o->lz / 3 + 1;
+    int64_t offgrid = 0;
+    for (int z = 0; z <= o->lz; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (v && ibits(v, POS_INDEX, LEN_INDEX) != WALL && !dia_kind(x, y, z)) offgrid++;
+            }
+    for (int z1 = 0; z1 < nz; z1++)
+        for (int b = 0; b < nb; b++)
+            for (int a = 0; a < na; a++) {
+                uint8_t *d = &out[((size_t)z1 * nb + b) * na + a];
+                *d = 0;
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                int x = 3 * (2 * a + (z1 & 1)), y = 3 * (2 * b + (z1 & 1)), z = 3 * z1;
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (ibits(v, POS_INDEX, LEN_INDEX) == WALL) { *d = 0x80; continue; }
+                if (!v) continue;
+                int occ = ibits(v, POS_OCC, LEN_OCC), co = ibits(v, POS_COOR, LEN_COOR), sp = ibits(v, POS_SIC, LEN_SIC);
+                int32_t nn[12], ie;
+                double pr;
+                int which = ora_site_info(o, x, y, z, nn, &ie, &pr);
+                int fd = 0;
+                if (which) {
+                    fd = -1;
+                    for (int dd = 0; dd < 4; dd++) {
+                        int aa = ((a + OFF[z1 & 1][dd][0]) % na + na) % na;
+                        int bb = ((b + OFF[z1 & 1][dd][1]) % nb + nb) % nb;
+                        int kk = z1 + OFF[z1 & 1][dd][2];
+                        if (3 * (2 * aa + (kk & 1)) == nn[0] && 3 * (2 * bb + (kk & 1)) == nn[1] && 3 * kk == nn[2]) fd = dd;
+                    }
+                    if (fd < 0) return -1;
+                }
+                int dm = (!occ && co == 1 && which == 1 && pr == (double)1.e-8f) ? 1 : 0;
+                *d = (uint8_t)((sp & 3) | ((co & 7) << 2) | (fd << 5) | (dm << 7));
+            }
+    return offgrid;
+}
+
+/* census enumeration shared with the GPU engine: (n1,n2,n3) with
+ * 1 <= n1+n2+n3 <= 3, by total, then n1 descending, then n2 descending */
+static int census_idx(int n1, int n2, int n3)
+{
+    int k = 0;
+    for (int t = 1; t <= 3; t++)
+        for (int a = t; a >= 0; a--)
+            for (int b = t - a; b >= 0; b--) {
+                int c = t - a - b;
+                if (a == n1 && b == n2 && c == n3) return k;
+                k++;
+            }
+    return -1;
+}
+
+int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
+{
+    ora_t *o = (ora_t *)o_;
+    for (int i = 1; i <= o->num_mc && i <= n; i++) {
+        mcp_t *p = &o->mc[i];
+        int32_t v = *LC(o, p->xyz);
+        int occ = ibits(v, POS_OCC, LEN_OCC), co = ibits(v, POS_COOR, LEN_COOR);
+        int sp = ibits(v, POS_SIC, LEN_SIC);
+        int c = 0;
+        if (!occ) {
+            if (co == 1) c = (p->prob == (double)1.e-8f) ? 2 : 1;
+            else if (co == 2) c = 3;
+            else if (co == 3) c = 4;
+        } else {
+            int n_si = 0, n_c = 0, n_b = 0, n_w = 0;
+            for (int k = 0; k < 4; k++) {
+                int32_t w = *LC(o, p->nn[k]);
+                if (!ibits(w, POS_OCC, LEN_OCC)) continue;
+                if (ibits(w, POS_INDEX, LEN_INDEX) == WALL) { n_w++; continue; }
+                int cn = ibits(w, POS_COOR, LEN_COOR);
+                int ind = *LI(o, p->nn[k]);
+                int nnn[4][3];
+                get_nn_list(o, ind, (cn >= 1 && cn <= 3) ? 1 : 2, nnn);
+                if (!in_list(nnn, p->xyz)) continue;
+                int s2 = ibits(w, POS_SIC, LEN_SIC);
+                if (s2 == 1) n_si++;
+                if (s2 == 2) n_c++;
+                if (s2 == 3) n_b++;
+            }
+            int t = n_si + n_c + n_b + n_w;
+            if (t == 0) c = 5;
+            else if (t <= 3) c = 6 + (sp - 1) * 19 + census_idx(n_si + n_w, n_c, n_b);
+        }
+        cls[i - 1] = c;
+        rate[i - 1] = p->prob;
+    }
+    return o->num_mc;
+}

@@ -74,6 +74,20 @@ int ora_site_info(const ora_t *o, int x, int y, int z, int32_t nn[12],
 /* Write the xyz frame exactly as WriteMolMolXYZFile would. */
 int ora_write_xyz(ora_t *o, const char *path);
 
+/* The state as one byte per diamond site, in the GPU engine's layout
+ * (mulskips_gb300/csrc/lattice.cuh): out[(z1*LenY/6 + b)*LenX/6 + a] =
+ * species | coor<<2 | first-list-entry direction<<5 | dummy<<7, 0x80 wall.
+ * Returns the number of non-wall points off the diamond sub-grid (arm-chair
+ * sites, which that layout cannot hold), or -1 if a list entry is not a bond. */
+int64_t ora_compact_state(const ora_t *o, uint8_t *out);
+
+/* Rate class of every listed MC particle, in the GPU engine's enumeration
+ * (0 none, 1 empty coor-1, 2 empty coor-1 with the dummy rate, 3 coor-2,
+ * 4 coor-3, 5 isolated atom, 6 + (species-1)*19 + census index for atoms),
+ * derived from the oracle's own lists and reciprocity checks.  Writes up to
+ * n (class, rate) pairs and returns NumAdAtom.                              */
+int64_t ora_mc_classes(const ora_t *o, int32_t *cls, double *rate, int64_t n);
+
 /* Export the rate tables parsed from start.dat. */
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);
 /* Raw ran3 for testing: seed then draw n values. */

@@ -1,0 +1,177 @@
+"""ctypes wrapper of the oracle library (oracle/_build/libmks_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py, as the checker.  The product never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libmks_oracle.so")
+NUMBERS = os.path.join(os.path.dirname(HERE), "tests", "golden", "numberslist.txt")
+
+EVENT_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("itrans", "i1"), ("arm", "i1"),
+                        ("pad", "<i2")])
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.ora_create.restype = C.c_void_p
+        L.ora_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.ora_destroy.argtypes = [C.c_void_p]
+        L.ora_last_error.restype = C.c_char_p
+        L.ora_init.argtypes = [C.c_void_p]
+        L.ora_run.argtypes = [C.c_void_p, C.c_int64, C.c_char_p]
+        L.ora_main.argtypes = [C.c_void_p, C.c_char_p]
+        L.ora_trace_enable.argtypes = [C.c_void_p, C.c_int]
+        L.ora_trace_len.restype = C.c_int64
+        L.ora_trace_len.argtypes = [C.c_void_p]
+        L.ora_trace.restype = C.c_void_p
+        L.ora_trace.argtypes = [C.c_void_p]
+        L.ora_trace_clear.argtypes = [C.c_void_p]
+        L.ora_iter.restype = C.c_int64
+        L.ora_iter.argtypes = [C.c_void_p]
+        L.ora_time.restype = C.c_double
+        L.ora_time.argtypes = [C.c_void_p]
+        L.ora_total_rate.restype = C.c_double
+        L.ora_total_rate.argtypes = [C.c_void_p]
+        L.ora_counts.argtypes = [C.c_void_p, C.c_void_p]
+        L.ora_get_lattcoo.argtypes = [C.c_void_p, C.c_void_p]
+        L.ora_site_info.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ora_write_xyz.argtypes = [C.c_void_p, C.c_char_p]
+        L.ora_get_rates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ora_ran3_sequence.argtypes = [C.c_int, C.c_int, C.c_void_p]
+        L.ora_mc_classes.restype = C.c_int64
+        L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L.ora_compact_state.restype = C.c_int64
+        L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    def __init__(self, startdat, lenx, leny, lenz, numbers=NUMBERS, num_mc_max=0):
+        self.dims = (lenx, leny, lenz)
+        h = lib().ora_create(startdat.encode(), numbers.encode() if numbers else None, lenx, leny, lenz,
+                             num_mc_max)
+        if not h:
+            raise RuntimeError(lib().ora_last_error().decode())
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().ora_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def init(self):
+        if lib().ora_init(self._h):
+            raise RuntimeError(lib().ora_last_error().decode())
+
+    def run(self, n, outdir=None):
+        r = lib().ora_run(self._h, int(n), outdir.encode() if outdir else None)
+        if r < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return r
+
+    def trace_enable(self, on=True):
+        lib().ora_trace_enable(self._h, 1 if on else 0)
+
+    def trace(self, clear=True):
+        n = lib().ora_trace_len(self._h)
+        p = lib().ora_trace(self._h)
+        if n == 0:
+            out = np.zeros(0, dtype=EVENT_DTYPE)
+        else:
+            buf = (C.c_char * (n * EVENT_DTYPE.itemsize)).from_address(p)
+            out = np.frombuffer(bytes(buf), dtype=EVENT_DTYPE).copy()
+        if clear:
+            lib().ora_trace_clear(self._h)
+        return out
+
+    @property
+    def time(self):
+        return lib().ora_time(self._h)
+
+    @property
+    def iter(self):
+        return lib().ora_iter(self._h)
+
+    @property
+    def total_rate(self):
+        return lib().ora_total_rate(self._h)
+
+    def counts(self):
+        a = np.zeros(3, dtype=np.int32)
+        lib().ora_counts(self._h, a.ctypes.data_as(C.c_void_p))
+        return {"bulk": int(a[0]), "voids": int(a[1]), "mc": int(a[2])}
+
+    def lattcoo(self):
+        lx, ly, lz = self.dims
+        a = np.empty((lz + 1, ly, lx), dtype=np.int32)
+        lib().ora_get_lattcoo(self._h, a.ctypes.data_as(C.c_void_p))
+        return a
+
+    def site_info(self, x, y, z):
+        nn = np.zeros(12, dtype=np.int32)
+        ie = C.c_int32()
+        pr = C.c_double()
+        which = lib().ora_site_info(self._h, x, y, z, nn.ctypes.data_as(C.c_void_p), C.byref(ie), C.byref(pr))
+        return which, nn.reshape(4, 3), ie.value, pr.value
+
+    def write_xyz(self, path):
+        if lib().ora_write_xyz(self._h, path.encode()):
+            raise RuntimeError(lib().ora_last_error().decode())
+
+    def rates(self):
+        e = np.zeros(3 * 4096)
+        d = np.zeros(9)
+        lib().ora_get_rates(self._h, e.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p))
+        return e.reshape(3, 4, 4, 4, 4, 4, 4), d.reshape(3, 3)
+
+
+def ran3_sequence(idum, n):
+    out = np.zeros(n)
+    lib().ora_ran3_sequence(int(idum), int(n), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def compact_state(o):
+    """The oracle state as one byte per diamond site, in the GPU engine's
+    layout (mulskips_gb300/csrc/lattice.cuh).  Returns (state, offgrid)."""
+    lx, ly, lz = o.dims
+    out = np.zeros((lz // 3 + 1, ly // 6, lx // 6), dtype=np.uint8)
+    r = lib().ora_compact_state(o._h, out.ctypes.data_as(C.c_void_p))
+    if r < 0:
+        raise AssertionError("a list entry of the oracle is not a bond direction")
+    return out, int(r)
+
+
+def mc_classes(o):
+    """(class, rate) of every MC particle of the oracle, GPU class enumeration."""
+    n = o.counts()["mc"]
+    cls = np.zeros(max(n, 1), dtype=np.int32)
+    rate = np.zeros(max(n, 1), dtype=np.float64)
+    m = lib().ora_mc_classes(o._h, cls.ctypes.data_as(C.c_void_p), rate.ctypes.data_as(C.c_void_p), n)
+    return cls[:m], rate[:m]
+
+
+def rate_of_site(o, x, y, z):
+    """(list kind, Ind_Event, rate) of the site, from the oracle's lists."""
+    which, _, ie, pr = o.site_info(x, y, z)
+    return which, ie, pr

@@ -1,0 +1,104 @@
+"""Synchronous-sublattice KMC on the GPU: lattice invariants after runs
+(coordination bytes equal the bonded-neighbour count of the occupancy, class
+histogram consistent), clock and event accounting, batching."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NB_OFF = [[(0, 0, 1), (0, -1, -1), (-1, -1, 1), (-1, 0, -1)],
+          [(1, 1, -1), (1, 0, 1), (0, 0, -1), (0, 1, 1)]]
+
+
+def check_invariants(st):
+    """Coordination of atoms = occupied neighbours incl. walls; of tracked
+    empty sites = occupied non-wall neighbours (the reference's bookkeeping,
+    deposition.f / Evaporation.f)."""
+    nz, nb, na = st.shape
+    wall = st == 0x80
+    occ = ((st & 3) != 0) & ~wall
+    co = (st >> 2) & 7
+    z = np.arange(nz)[:, None, None]
+    n_occ = np.zeros(st.shape, np.int32)
+    n_wall = np.zeros(st.shape, np.int32)
+    for par in (0, 1):
+        for (da, db, dz) in NB_OFF[par]:
+            o2 = np.zeros_like(occ)
+            w2 = np.zeros_like(wall)
+            src = np.roll(np.roll(occ, -da, axis=2), -db, axis=1)
+            srcw = np.roll(np.roll(wall, -da, axis=2), -db, axis=1)
+            if dz > 0:
+                o2[:-dz] = src[dz:]
+                w2[:-dz] = srcw[dz:]
+            else:
+                o2[-dz:] = src[:dz]
+                w2[-dz:] = srcw[:dz]
+            m = (z % 2 == par)
+            n_occ += np.where(m, o2, 0)
+            n_wall += np.where(m, w2, 0)
+    valid = ((np.arange(na)[None, None, :] + np.arange(nb)[None, :, None] + (z >> 1)) & 1) == 0
+    atoms = occ & valid
+    assert np.array_equal(co[atoms], (n_occ + n_wall)[atoms]), "atom coordination inconsistent"
+    tracked = (~occ) & (~wall) & (st != 0) & valid
+    assert np.array_equal(co[tracked], n_occ[tracked]), "empty-site coordination inconsistent"
+    # every empty site touching an atom is tracked
+    untracked = (st == 0) & valid & (n_occ > 0)
+    assert not untracked.any(), "empty site next to an atom is not tracked"
+    return int(atoms.sum())
+
+
+def test_sublattice_run_invariants():
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    with Lattice(480, 480, 480, seed=7) as lat:
+        lat.set_rates(pE, pD)
+        lat.init_flat("S", 240)
+        n0 = check_invariants(lat.state())
+        tau = 2e-8
+        ev, t = lat.run(tau, 16)
+        assert ev > 0
+        assert abs(t - 16 * tau) < 1e-15
+        n1 = check_invariants(lat.state())
+        assert n1 < n0          # T = 1100 K etches
+        obs = lat.observables()
+        assert obs["events"] == ev and obs["atoms"] == n1
+        h = lat.class_histogram()
+        assert h[1:].sum() == obs["mc_sites"]
+        st = lat.status()
+        assert st["error"] == 0
+
+
+def test_growth_regime_invariants():
+    """Low temperature: deposition wins and the film grows."""
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    pE, pD = arrhenius_tables(400.0, flux=5.0)
+    with Lattice(480, 480, 480, seed=3) as lat:
+        lat.set_rates(pE, pD)
+        lat.init_flat("S", 120)
+        n0 = check_invariants(lat.state())
+        ev, t = lat.run(0.01, 40)
+        n1 = check_invariants(lat.state())
+        assert ev > 1000 and n1 > n0
+
+
+def test_batch_uneven_replicas():
+    from mulskips_gb300 import Batch, arrhenius_tables
+    sides = [16, 24, 40]
+    boxes = [(12 * s, 12 * s, 12 * s) for s in sides]
+    b = Batch(boxes, seeds=[11, 12, 13])
+    pEs, pDs = zip(*[arrhenius_tables(T) for T in (1000.0, 1100.0, 1200.0)])
+    b.set_rates(np.stack(pEs), np.stack(pDs))
+    b.init_flat("S", [12 * s // 2 for s in sides])
+    ev = b.run(1e-8, 8)
+    obs = b.observables()
+    assert ev == sum(o["events"] for o in obs) and all(o["events"] > 0 for o in obs)
+    b.close()
+
+
+def test_unsupported_config_is_rejected():
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300._native import MksError
+    with pytest.raises(MksError):
+        Lattice(480, 480, 480, ptrans_zig=0.8)
+    with pytest.raises(MksError):
+        Lattice(100, 480, 480)

@@ -1,0 +1,86 @@
+"""Replay parity: the reference's event sequence (from the pinned oracle),
+applied by the GPU engine through the C ABI, gives bit-identical lattice
+occupancy, coordination, neighbour-list head and dummy flags, and the same
+rate-class histogram as the oracle's own lists."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_hist(ora, o):
+    cls, _ = ora.mc_classes(o)
+    return np.bincount(cls, minlength=63)[:63]
+
+
+def replay_case(ora, startdat, len1, kind, total, chunk, lenxyz=480):
+    from mulskips_gb300 import Lattice
+    o = ora.Oracle(startdat, lenxyz, lenxyz, lenxyz)
+    o.init()
+    d = __import__("mulskips_gb300.startdat", fromlist=["x"]).parse_startdat(startdat)
+    pE, pD = o.rates()
+    lat = Lattice(lenxyz, lenxyz, lenxyz, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"])
+    try:
+        lat.set_rates(pE, pD)
+        lat.init_flat(kind, len1)
+        st0, off = ora.compact_state(o)
+        assert off == 0
+        assert np.array_equal(lat.state(), st0), "initial lattice differs"
+        o.trace_enable()
+        done = 0
+        while done < total:
+            r = o.run(chunk)
+            tr = o.trace()
+            lat.replay(tr)
+            done += len(tr)
+            st, off = ora.compact_state(o)
+            assert off == 0
+            g = lat.state()
+            bad = np.argwhere(g != st)
+            assert bad.size == 0, f"after {done} events: {len(bad)} sites differ, first {bad[:3]}"
+            h = lat.class_histogram()
+            ho = oracle_hist(ora, o)
+            assert np.array_equal(h[1:], ho[1:]), f"class histogram differs after {done} events"
+            if r:
+                break
+        return done
+    finally:
+        lat.close()
+        o.close()
+
+
+def test_replay_si001(oracle_lib):
+    n = replay_case(oracle_lib, os.path.join(GOLDEN, "Si-SL", "start.dat"), 360, "S", 400000, 100000)
+    assert n == 400000
+
+
+def test_replay_sic001(oracle_lib):
+    n = replay_case(oracle_lib, os.path.join(GOLDEN, "surface", "start.dat"), 120, "C", 200000, 100000)
+    assert n == 200000
+
+
+def test_replay_etch_to_walls(oracle_lib, tmp_path):
+    """T=1100 K plain Si(001) (the benchmark model): etches through to the
+    walls and stops on the few-MC-particles rule; replay stays exact."""
+    from mulskips_gb300.startdat import write_plain_si_startdat
+    p = tmp_path / "start.dat"
+    write_plain_si_startdat(str(p), T=1100.0, len1=120, max_iter=1000000, seed=1)
+    n = replay_case(oracle_lib, str(p), 120, "S", 1000000, 40000)
+    assert 100000 < n < 1000000
+
+
+def test_replay_rejects_inapplicable_event(oracle_lib):
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    from mulskips_gb300._native import EVENT_DTYPE, MksError
+    pE, pD = arrhenius_tables(1100.0)
+    with Lattice(480, 480, 480) as lat:
+        lat.set_rates(pE, pD)
+        lat.init_flat("S", 120)
+        ev = np.zeros(1, dtype=EVENT_DTYPE)
+        ev[0] = (0, 0, 300, 1, 0, 0)      # empty, untracked site far above the surface
+        with pytest.raises(MksError):
+            lat.replay(ev)

@@ -1,0 +1,60 @@
+"""The oracle (serial C restatement of the reference) reproduces the
+reference's own regression outputs byte for byte
+(regression-tests/input-and-references-files: Si-SL and surface, 10^7 events
+each, RunType T, IDUM 9117116, 480^3 box)."""
+import gzip
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+ORACLE_EXE = os.path.join(ROOT, "oracle", "_build", "mks_oracle")
+
+
+def run_case(case, tmp_path):
+    d = tmp_path / case
+    d.mkdir()
+    shutil.copy(os.path.join(GOLDEN, case, "start.dat"), d / "start.dat")
+    r = subprocess.run([ORACLE_EXE, "480", "480", "480", os.path.join(GOLDEN, "numberslist.txt")], cwd=d,
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    return d, r.stdout
+
+
+def golden_log_numbers(case):
+    txt = open(os.path.join(GOLDEN, case, "log.txt")).read()
+    m = re.search(r"Iter, Time, Site\s+(\d+)\s+([0-9.Ee+-]+)\s+(\d+)\s+(\d+)\s+(\d+)", txt)
+    n = re.search(r"NatNvoidNad\s+(\d+)\s+(\d+)\s+(\d+)", txt)
+    return m.groups(), n.groups()
+
+
+@pytest.mark.parametrize("case", ["Si-SL", "surface"])
+def test_regression_frames_identical(case, oracle_lib, tmp_path):
+    d, out = run_case(case, tmp_path)
+    for fr in ("I00000000", "I00000001"):
+        with gzip.open(os.path.join(GOLDEN, case, fr + ".xyz.gz"), "rb") as f:
+            gold = f.read()
+        mine = (d / (fr + ".xyz")).read_bytes()
+        assert mine == gold, f"{case} {fr}.xyz differs from the reference"
+    (it, t, x, y, z), (nat, nvoid, nad) = golden_log_numbers(case)
+    m = re.search(r"Iter, Time, Site\s+(\d+)\s+([0-9.Ee+-]+)\s+(\d+)\s+(\d+)\s+(\d+)", out)
+    assert m.group(1) == it and (m.group(3), m.group(4), m.group(5)) == (x, y, z)
+    assert abs(float(m.group(2)) - float(t)) <= 1e-10 * abs(float(t))
+    n = re.search(r"NatNvoidNad\s+(\d+)\s+(\d+)\s+(\d+)", out)
+    assert n.groups() == (nat, nvoid, nad)
+
+
+def test_ran3_is_deterministic_and_in_range(oracle_lib):
+    a = oracle_lib.ran3_sequence(9117116, 1000)
+    b = oracle_lib.ran3_sequence(9117116, 1000)
+    assert (a == b).all() and (a >= 0).all() and (a < 1).all()
+    assert not (a == oracle_lib.ran3_sequence(1, 1000)).all()
+
+
+def test_numbers_list_fixture():
+    vals = [float(v) for v in open(os.path.join(GOLDEN, "numberslist.txt")).read().split()]
+    assert len(vals) == 1000 and all(0 < v < 1 for v in vals)
