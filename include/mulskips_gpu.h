@@ -117,6 +117,19 @@ int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
 /* Upload compact state bytes (same layout); the per-tile bands are rebuilt. */
 int mks_set_state(mks_handle *h, const uint8_t *st, int64_t n);
 int mks_replay(mks_handle *h, const mks_event *trace, int64_t n);
+/* mks_replay without any device allocation: no counterpart in the reference
+ * (the Fortran program has no device memory at all).  For callers that may
+ * not call cudaMalloc -- e.g. a host that has handed its whole memory budget
+ * to the lattice, or that runs this step under a stream-ordered memory pool it
+ * must not grow.  The trace is staged in one fixed 1 MiB + 256 B device array
+ * owned by the library, so n may be at most MKS_REPLAY_NOALLOC_MAX events per
+ * call (longer traces are rejected with MKS_ERR_ARG; split them).  The array
+ * is shared by every call and every handle on a device: calls that overlap on
+ * the GPU (several handles or threads at once) race and must be serialized.
+ * The first call on a device looks up the array's device address, so make
+ * that first call before any CUDA stream capture.                         */
+#define MKS_REPLAY_NOALLOC_MAX 65536
+int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n);
 /* Synchronous-sublattice KMC: windows of length tau (s); stops after
  * max_windows windows, or once max_events / max_time is reached (checked per
  * window), or when fewer than 21 surface sites remain (main.f:307-310).    */

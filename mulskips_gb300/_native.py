@@ -61,6 +61,7 @@ SIGNATURES = {
     "mks_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_replay": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "mks_replay_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_int64, C.c_double,
                           C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "mks_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),

@@ -25,6 +25,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "lattice.cuh"
 #include "rng.cuh"
@@ -1271,6 +1272,72 @@ int mks_replay(mks_handle *h, const mks_event *trace, int64_t n)
     if (rc) return rc;
     if (s.error) {
         CK(cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream));
+        return fail(s.error, "replay: event %lld is not applicable to the lattice state", done);
+    }
+    return rescan(h);
+}
+
+// ---- mks_replay_noalloc: the replay kernel fed from a library-owned array ----
+// Layout of the array: bytes [0, 8) the kernel's progress counter, bytes
+// [256, 256 + 16 * MKS_REPLAY_NOALLOC_MAX) the staged events.  Every GPU that
+// loads this library holds the array until the process exits.
+static __device__ __align__(256) unsigned char g_replay_scratch[256 + sizeof(mks_event) * MKS_REPLAY_NOALLOC_MAX];
+
+namespace {
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_replay_scratch on `dev`, looked up once per device with
+// that device current.  In host code the symbol itself is only a stand-in for
+// the device array, never a device address.
+int noalloc_scratch(int dev, unsigned char **out)
+{
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(MKS_ERR_ARG, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        int prev = -1;
+        CK(cudaGetDevice(&prev));
+        if (prev != dev) CK(cudaSetDevice(dev));
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_replay_scratch);
+        if (prev != dev) cudaSetDevice(prev);
+        if (e != cudaSuccess) return fail(MKS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return 0;
+}
+}  // namespace
+
+int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n)
+{
+    if (!h || (n > 0 && !trace) || n < 0 || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    if (n > MKS_REPLAY_NOALLOC_MAX)
+        return fail(MKS_ERR_ARG, "mks_replay_noalloc: %lld events exceed the per-call limit of %d; split the trace",
+                    (long long)n, MKS_REPLAY_NOALLOC_MAX);
+    if (n == 0) return 0;
+    int dev = -1;
+    CK(cudaStreamGetDevice(h->stream, &dev));
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(dev, &scratch);
+    if (rc) return rc;
+    long long *d_done = reinterpret_cast<long long *>(scratch);
+    mks_event *d_ev = reinterpret_cast<mks_event *>(scratch + 256);
+    // the array keeps the previous call's contents: reset the progress counter
+    CK(cudaMemsetAsync(d_done, 0, sizeof(long long), h->stream));
+    CK(cudaMemcpyAsync(d_ev, trace, sizeof(mks_event) * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+    k_replay<<<1, 32, 0, h->stream>>>(h->d_reps, h->d_st, d_ev, n, h->d_status, d_done);
+    CK(cudaGetLastError());
+    long long done = 0;
+    CK(cudaMemcpyAsync(&done, d_done, sizeof done, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    DevStatus s;
+    rc = read_status(h, s);
+    if (rc) return rc;
+    if (s.error) {
+        CK(cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream));
+        CK(cudaStreamSynchronize(h->stream));
         return fail(s.error, "replay: event %lld is not applicable to the lattice state", done);
     }
     return rescan(h);
