@@ -233,9 +233,7 @@ def gb300(args, rank, world):
     if os.path.exists(tp):
         try:
             tj = json.load(open(tp))
-            traffic = tj.get("dram_bytes_per_event", None)
-            if traffic is not None:
-                traffic = traffic * per_launch_events
+            traffic = tj.get("dram_bytes_per_launch", None)
         except Exception:
             traffic = None
     base_v, base_ev, base_runs = cpu_baseline(seconds=args.cpu_seconds, cores=1)

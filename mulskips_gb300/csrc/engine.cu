@@ -41,7 +41,7 @@ constexpr int HALO = 2;                  // read range of an event, in columns
 constexpr int WX = QMAX + 2 * HALO;      // 16: window row stride
 constexpr int WMAX = 24;                 // max staged layers
 constexpr int MCCAP = 768;               // max event sites per tile
-constexpr int ZMARGIN = 5;               // extra staged layers beyond the band
+constexpr int ZMARGIN = 2;               // extra staged layers beyond the band on each side
 constexpr int NRELOAD = 512;             // bounded re-staging per tile and phase
 constexpr uint16_t NOPOS = 0xFFFF;
 
@@ -96,6 +96,7 @@ struct GLat {
 
 struct SLat {
     uint8_t *w;
+    uint32_t *dirty;     // one bit per staged row (b, z)
     int ax0, bx0, zw0, NZ;
     __device__ __forceinline__ uint8_t get(int a, int b, int z) const
     {
@@ -105,7 +106,9 @@ struct SLat {
     __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
     {
         if (z < 0 || z >= NZ) return;
-        w[((z - zw0) * WX + (b - bx0)) * WX + (a - ax0)] = v;
+        int row = (z - zw0) * WX + (b - bx0);
+        w[row * WX + (a - ax0)] = v;
+        atomicOr(&dirty[row >> 5], 1u << (row & 31));   // lanes may mark rows concurrently
     }
 };
 
@@ -273,12 +276,13 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
 // ------------------------------------------------ the sublattice kernel
 struct TileShared {
     uint8_t win[WX * WX * WMAX];
+    uint32_t dirty[(WX * WMAX + 31) / 32];
     uint32_t list[MCCAP];
     uint16_t pos[QMAX * QMAX * WMAX];
     int cnt[64];
     float rate[64];
     float spcum[3][2];
-    int tc_a[5], tc_b[5], tc_z[5], tc_n;
+    EvCtx ev;
     int nlist;
     int abort_code;
 };
@@ -289,7 +293,7 @@ __device__ __forceinline__ int key_of(int ia, int ib, int z) { return (z << 10) 
 // counts.  ia/ib are window coordinates (HALO-based).
 template <class Lat>
 __device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh, bool use_pos,
-                           int zw0)
+                           int zw0, int wz)
 {
     int lane = threadIdx.x & 31;
     for (int c = lane; c < 64; c += 32) S.cnt[c] = 0;
@@ -299,8 +303,10 @@ __device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, 
     int total = ncol * (zh - zl + 1);
     bool overflow = false;
     if (use_pos) {
+        // every staged layer: events may create sites anywhere in the band
         uint32_t *p32 = reinterpret_cast<uint32_t *>(S.pos);
-        for (int i = lane; i < QMAX * QMAX * WMAX / 2; i += 32) p32[i] = 0xFFFFFFFFu;
+        int nw = QMAX * QMAX * wz / 2;
+        for (int i = lane; i < nw; i += 32) p32[i] = 0xFFFFFFFFu;
         __syncwarp();
     }
     for (int base = 0; base < total; base += 32) {
@@ -355,14 +361,22 @@ __device__ __forceinline__ int find_slot(TileShared &S, uint32_t key, bool use_p
 
 // Run events of one tile on accessor L until the tile clock reaches t_end,
 // the tile has no events, or an event would read outside the staged layers.
-// Returns 0 done, 1 needs re-staging, <0 error.
+// Returns 0 done, 1 needs re-staging, <0 error.  hz_lo/hz_hi (per lane) collect
+// the layers of changed sites outside the tile.
 template <class Lat>
 __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev &Q, int qid, double &t, double t_end,
                           unsigned int &evc, int zw0, int zw1, bool use_pos, int &hz_lo, int &hz_hi,
                           unsigned long long &nev, uint32_t k0, uint32_t k1, uint32_t phase_tag)
 {
+    const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
+    const unsigned int window = R.window;
+    const int NZ = R.NZ;
+    // Philox draws of 32 consecutive events, one event per lane
+    unsigned int pre_base = evc;
+    U4 pre = philox4x32_10(U4{pre_base + (unsigned)lane, (uint32_t)qid, window, phase_tag}, k0, k1);
+    int used = 0;
     for (;;) {
         // cumulative class weights: lane l owns classes 2l and 2l+1 (ISO apart)
         int c0 = 2 * lane, c1 = 2 * lane + 1;
@@ -371,23 +385,25 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         float s = w0 + w1;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            float v = __shfl_up_sync(0xffffffffu, s, o);
+            float v = __shfl_up_sync(FULL, s, o);
             if (lane >= o) s += v;
         }
-        float r_rest = __shfl_sync(0xffffffffu, s, 31);
+        float r_rest = __shfl_sync(FULL, s, 31);
         int n_iso = S.cnt[CLS_ISO];
         float r_iso = n_iso ? (float)n_iso * 1.0e5f * fmaxf(r_rest, 1.0e-30f) : 0.f;
         float rtot = r_rest + r_iso;
         if (!(rtot > 0.f)) return 0;
-        U4 rnd;
-        if (lane == 0) {
-            U4 ctr{evc, (uint32_t)qid, R.window, phase_tag};
-            rnd = philox4x32_10(ctr, k0, k1);
+        if (used == 32) {
+            pre_base += 32;
+            pre = philox4x32_10(U4{pre_base + (unsigned)lane, (uint32_t)qid, window, phase_tag}, k0, k1);
+            used = 0;
         }
-        rnd.x = __shfl_sync(0xffffffffu, rnd.x, 0);
-        rnd.y = __shfl_sync(0xffffffffu, rnd.y, 0);
-        rnd.z = __shfl_sync(0xffffffffu, rnd.z, 0);
-        rnd.w = __shfl_sync(0xffffffffu, rnd.w, 0);
+        U4 rnd;
+        rnd.x = __shfl_sync(FULL, pre.x, used);
+        rnd.y = __shfl_sync(FULL, pre.y, used);
+        rnd.z = __shfl_sync(FULL, pre.z, used);
+        rnd.w = __shfl_sync(FULL, pre.w, used);
+        used++;
         evc++;
         float dt = -__logf(u01(rnd.z)) / rtot;
         if (t + (double)dt > t_end) {
@@ -400,13 +416,13 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         if (target >= r_rest && n_iso > 0) {
             cls = CLS_ISO;
         } else {
-            unsigned m = __ballot_sync(0xffffffffu, s > target);
+            unsigned m = __ballot_sync(FULL, s > target);
             cls = -1;
             if (m) {
                 int l = __ffs(m) - 1;
-                float sl = __shfl_sync(0xffffffffu, s, l);
-                float w0l = __shfl_sync(0xffffffffu, w0, l);
-                float w1l = __shfl_sync(0xffffffffu, w1, l);
+                float sl = __shfl_sync(FULL, s, l);
+                float w0l = __shfl_sync(FULL, w0, l);
+                float w1l = __shfl_sync(FULL, w1, l);
                 float el = sl - w0l - w1l;
                 cls = (target < el + w0l) ? 2 * l : 2 * l + 1;
                 if (cls == 2 * l && !(w0l > 0.f)) cls = 2 * l + 1;
@@ -426,7 +442,7 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         for (int base = 0; base < S.nlist; base += 32) {
             int i = base + lane;
             bool hit = i < S.nlist && (int)(S.list[i] & 0xFF) == cls;
-            unsigned m = __ballot_sync(0xffffffffu, hit);
+            unsigned m = __ballot_sync(FULL, hit);
             int nh = __popc(m);
             if (k < nh) {
                 slot = base + __fns(m, 0, k + 1);
@@ -438,47 +454,59 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         uint32_t key = S.list[slot] >> 8;
         int z = key >> 10;
         int a = Q.a0 + (int)(key & 31) - HALO, b = Q.b0 + (int)((key >> 5) & 31) - HALO;
-        if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < R.NZ)) return 1;   // needs re-staging
+        if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return 1;   // needs re-staging
         t += (double)dt;
+        // stage 1 (one lane): the event site
         if (lane == 0) {
-            Touched tc;
-            int err;
+            int sp = 0;
             if (cls >= CLS_C1 && cls <= CLS_C3) {
                 int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
                 float u = u01(rnd.w);
-                int sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
-                err = apply_deposition(L, a, b, z, sp, tc);
-            } else {
-                err = apply_evaporation(L, a, b, z, tc);
+                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
             }
-            S.abort_code = err;
-            S.tc_n = tc.n;
-            for (int i = 0; i < tc.n; i++) {
-                S.tc_a[i] = tc.a[i];
-                S.tc_b[i] = tc.b[i];
-                S.tc_z[i] = tc.z[i];
-            }
+            S.abort_code = ev_begin(L, a, b, z, sp, S.ev);
         }
         __syncwarp();
         if (S.abort_code) return -DERR_INVARIANT;
-        // re-classify the touched sites and update the list
-        int ntc = S.tc_n;
-        for (int i = 0; i < ntc; i++) {
-            int ta = S.tc_a[i], tb = S.tc_b[i], tz = S.tc_z[i];
-            int ia = ta - Q.a0, ib = tb - Q.b0;
-            if (ia < 0 || ia >= wa || ib < 0 || ib >= wb) {
-                hz_lo = min(hz_lo, tz);
-                hz_hi = max(hz_hi, tz);
-                continue;
-            }
-            if (tz < 0 || tz >= R.NZ) continue;
-            int ncls = site_class(L, ta, tb, tz);
-            uint32_t tkey = (uint32_t)key_of(ia + HALO, ib + HALO, tz);
-            int ts = find_slot(S, tkey, use_pos, zw0);
+        // stage 2 (four lanes): the four neighbours, independent of one another
+        int r2 = 0, ya = 0, yb = 0, yz = 0;
+        if (lane < 4) r2 = ev_neighbour(L, S.ev, lane, ya, yb, yz);
+        unsigned wallm = __ballot_sync(FULL, lane < 4 && r2 == 1);
+        unsigned errm = __ballot_sync(FULL, lane < 4 && r2 < 0);
+        if (errm) return -DERR_INVARIANT;
+        // stage 3 (one lane): final state of the event site
+        if (lane == 0) S.abort_code = ev_finish(L, S.ev, __popc(wallm)) ? 1 : 0;
+        __syncwarp();
+        if (S.abort_code) return -DERR_INVARIANT;
+        // re-classify the five touched sites, one per lane (lane 0 the event site)
+        int ta = __shfl_sync(FULL, ya, (lane + 31) & 31);
+        int tb = __shfl_sync(FULL, yb, (lane + 31) & 31);
+        int tz = __shfl_sync(FULL, yz, (lane + 31) & 31);
+        if (lane == 0) {
+            ta = a;
+            tb = b;
+            tz = z;
+        }
+        bool act = lane < 5 && tz >= 0 && tz < NZ;
+        int ia = ta - Q.a0, ib = tb - Q.b0;
+        bool interior = act && ia >= 0 && ia < wa && ib >= 0 && ib < wb;
+        if (act && !interior) {
+            hz_lo = min(hz_lo, tz);
+            hz_hi = max(hz_hi, tz);
+        }
+        int ncls = interior ? site_class(L, ta, tb, tz) : CLS_NONE;
+        uint32_t tkey = interior ? (uint32_t)key_of(ia + HALO, ib + HALO, tz) : 0u;
+        unsigned im = __ballot_sync(FULL, interior);
+        while (im) {
+            int src = __ffs(im) - 1;
+            im &= im - 1;
+            uint32_t kk = __shfl_sync(FULL, tkey, src);
+            int nc = __shfl_sync(FULL, ncls, src);
+            int ts = find_slot(S, kk, use_pos, zw0);
             if (lane == 0) {
                 if (ts >= 0) {
                     int oc = S.list[ts] & 0xFF;
-                    if (ncls == CLS_NONE) {
+                    if (nc == CLS_NONE) {
                         S.cnt[oc]--;
                         int last = S.nlist - 1;
                         uint32_t le = S.list[last];
@@ -487,22 +515,26 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
                             uint32_t lk = le >> 8;
                             int la = (lk & 31) - HALO, lb = ((lk >> 5) & 31) - HALO, lz = lk >> 10;
                             S.pos[((lz - zw0) * QMAX + lb) * QMAX + la] = (uint16_t)ts;
-                            S.pos[((tz - zw0) * QMAX + ib) * QMAX + ia] = NOPOS;
+                            int qa = (kk & 31) - HALO, qb = ((kk >> 5) & 31) - HALO, qz = kk >> 10;
+                            S.pos[((qz - zw0) * QMAX + qb) * QMAX + qa] = NOPOS;
                         }
                         S.nlist = last;
-                    } else if (ncls != oc) {
+                    } else if (nc != oc) {
                         S.cnt[oc]--;
-                        S.cnt[ncls]++;
-                        S.list[ts] = (tkey << 8) | (uint32_t)ncls;
+                        S.cnt[nc]++;
+                        S.list[ts] = (kk << 8) | (uint32_t)nc;
                     }
-                } else if (ncls != CLS_NONE) {
+                } else if (nc != CLS_NONE) {
                     if (S.nlist >= MCCAP) {
                         S.abort_code = DERR_CAPACITY;
                     } else {
                         int ns = S.nlist++;
-                        S.list[ns] = (tkey << 8) | (uint32_t)ncls;
-                        if (use_pos) S.pos[((tz - zw0) * QMAX + ib) * QMAX + ia] = (uint16_t)ns;
-                        S.cnt[ncls]++;
+                        S.list[ns] = (kk << 8) | (uint32_t)nc;
+                        if (use_pos) {
+                            int qa = (kk & 31) - HALO, qb = ((kk >> 5) & 31) - HALO, qz = kk >> 10;
+                            S.pos[((qz - zw0) * QMAX + qb) * QMAX + qa] = (uint16_t)ns;
+                        }
+                        S.cnt[nc]++;
                     }
                 }
             }
@@ -548,40 +580,61 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
         int need = zhi - zlo + 5;
         if (need <= WMAX) {
             // stage tile + halo and the layer band in shared memory
-            int spare = WMAX - need;
-            int zw0 = max(0, zlo - 2 - min(ZMARGIN, spare / 2));
-            int zw1 = min(R.NZ, zw0 + WMAX);
-            if (zw1 - zw0 < WMAX) zw0 = max(0, zw1 - WMAX);
+            int WZ = min(WMAX, need + 2 * ZMARGIN);
+            int zw0 = max(0, zlo - 2 - (WZ - need) / 2);
+            int zw1 = min(R.NZ, zw0 + WZ);
+            if (zw1 - zw0 < WZ) zw0 = max(0, zw1 - WZ);
+            WZ = zw1 - zw0;
             int ax0 = Q.a0 - HALO, bx0 = Q.b0 - HALO;
-            int WA = wa + 2 * HALO, WB = wb + 2 * HALO, WZ = zw1 - zw0;
-            int tot = WA * WB * WZ;
-            for (int i = lane; i < tot; i += 32) {
-                int ia = i % WA;
-                int r = i / WA;
+            int WA = wa + 2 * HALO, WB = wb + 2 * HALO;
+            int nrows = WB * WZ;
+            bool inner = ax0 >= 0 && ax0 + WA <= R.NA;
+            int w0 = ax0 >> 2;                            // first aligned word (inner rows)
+            int nwords = ((ax0 + WA + 3) >> 2) - w0;      // <= 5
+            if (lane < (WX * WMAX + 31) / 32) S.dirty[lane] = 0u;
+#pragma unroll 2
+            for (int r = lane; r < nrows; r += 32) {
                 int ib = r % WB, iz = r / WB;
-                S.win[(iz * WX + ib) * WX + ia] = G.get(ax0 + ia, bx0 + ib, zw0 + iz);
+                const uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
+                uint8_t *dst = &S.win[(iz * WX + ib) * WX];
+                if (inner) {
+                    const uint32_t *rw = reinterpret_cast<const uint32_t *>(row) + w0;
+                    uint32_t v[5];
+#pragma unroll
+                    for (int k = 0; k < 5; k++) v[k] = (k < nwords) ? rw[k] : 0u;   // coherent loads: the tile re-stages rows it wrote
+#pragma unroll
+                    for (int k = 0; k < 5; k++)
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            int ia = 4 * (w0 + k) + j - ax0;
+                            if (k < nwords && ia >= 0 && ia < WA) dst[ia] = (uint8_t)(v[k] >> (8 * j));
+                        }
+                } else {
+                    for (int ia = 0; ia < WA; ia++) dst[ia] = row[wrapi(ax0 + ia, R.NA)];
+                }
             }
             __syncwarp();
-            SLat L{S.win, ax0, bx0, zw0, R.NZ};
-            if (!build_list(S, L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0)) {
+            SLat L{S.win, S.dirty, ax0, bx0, zw0, R.NZ};
+            if (!build_list(S, L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
             rc = run_events(S, L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag);
-            // write back the tile and the one-column ring its events can change
-            int wa1 = wa + 2, wb1 = wb + 2;
-            int tot1 = wa1 * wb1 * WZ;
-            for (int i = lane; i < tot1; i += 32) {
-                int ia = i % wa1;
-                int r = i / wa1;
-                int ib = r % wb1, iz = r / wb1;
-                G.put(Q.a0 - 1 + ia, Q.b0 - 1 + ib, zw0 + iz, S.win[(iz * WX + ib + 1) * WX + ia + 1]);
+            __syncwarp();
+            // write back the rows that events changed (tile and its one-column ring)
+            for (int r = lane; r < nrows; r += 32) {
+                int ib = r % WB, iz = r / WB;
+                int bit = iz * WX + ib;                   // the row index SLat::put marks
+                if (!((S.dirty[bit >> 5] >> (bit & 31)) & 1u)) continue;
+                uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
+                const uint8_t *src = &S.win[(iz * WX + ib) * WX];
+                for (int ia = 1; ia < WA - 1; ia++) row[wrapi(ax0 + ia, R.NA)] = src[ia];
             }
             if (rc > 0 && lane == 0) atomicAdd(&status->reloads, 1ull);
         } else {
             // band taller than the staging buffer: run from global memory
             if (lane == 0) atomicAdd(&status->fallback, 1ull);
-            if (!build_list(S, G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0)) {
+            if (!build_list(S, G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -610,6 +663,10 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
         __syncwarp();
     }
     __syncwarp();
+    for (int o = 16; o > 0; o >>= 1) {
+        hz_lo = min(hz_lo, __shfl_xor_sync(0xffffffffu, hz_lo, o));
+        hz_hi = max(hz_hi, __shfl_xor_sync(0xffffffffu, hz_hi, o));
+    }
     if (lane == 0) {
         quads[qid].zlo = zlo;
         quads[qid].zhi = zhi;
@@ -932,9 +989,7 @@ int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_
     }
     rc = upload_reps(h, d);
     if (rc) return rc;
-    rc = rescan(h);
-    if (rc) return rc;
-    h->last_kernels = 1;
+    h->last_kernels = 0;
     h->last_graphs = 0;
     h->last_phase_launches = 0;
     // capture a block of windows once, replay it
@@ -1149,8 +1204,11 @@ int mks_get_state(mks_handle *h, uint8_t *out, int64_t n)
 {
     if (!h || !out || n < mks_state_size(h)) return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[0];
-    CK(cudaMemcpy2DAsync(out, r.NA, h->d_st + r.st_off, r.pitch, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyDeviceToHost,
-                         h->stream));
+    if (r.NA == r.pitch)
+        CK(cudaMemcpyAsync(out, h->d_st + r.st_off, (size_t)mks_state_size(h), cudaMemcpyDeviceToHost, h->stream));
+    else
+        CK(cudaMemcpy2DAsync(out, r.NA, h->d_st + r.st_off, r.pitch, r.NA, (size_t)r.NZ * r.NB,
+                             cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
@@ -1159,8 +1217,11 @@ int mks_set_state(mks_handle *h, const uint8_t *in, int64_t n)
 {
     if (!h || !in || n < mks_state_size(h) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[0];
-    CK(cudaMemcpy2DAsync(h->d_st + r.st_off, r.pitch, in, r.NA, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyHostToDevice,
-                         h->stream));
+    if (r.NA == r.pitch)
+        CK(cudaMemcpyAsync(h->d_st + r.st_off, in, (size_t)mks_state_size(h), cudaMemcpyHostToDevice, h->stream));
+    else
+        CK(cudaMemcpy2DAsync(h->d_st + r.st_off, r.pitch, in, r.NA, r.NA, (size_t)r.NZ * r.NB,
+                             cudaMemcpyHostToDevice, h->stream));
     return rescan(h);
 }
 

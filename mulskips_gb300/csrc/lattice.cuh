@@ -54,11 +54,9 @@ MKS_HD void nb_off(int zpar, int d, int &da, int &db, int &dz)
 {
     // even layer: (0,0,+1) (0,-1,-1) (-1,-1,+1) (-1,0,-1)
     // odd  layer: (+1,+1,-1) (+1,0,+1) (0,0,-1) (0,+1,+1)
-    const int8_t t[2][4][3] = {{{0, 0, 1}, {0, -1, -1}, {-1, -1, 1}, {-1, 0, -1}},
-                               {{1, 1, -1}, {1, 0, 1}, {0, 0, -1}, {0, 1, 1}}};
-    da = t[zpar][d][0];
-    db = t[zpar][d][1];
-    dz = t[zpar][d][2];
+    da = zpar - (d >> 1);
+    db = zpar - ((d ^ (d >> 1)) & 1);
+    dz = ((d ^ zpar) & 1) ? -1 : 1;
 }
 MKS_HD int rev_dir(int d) { return (d + 2) & 3; }
 
@@ -101,19 +99,22 @@ MKS_HD int site_class(const L &lat, int a, int b, int z)
         return CLS_NONE;
     }
     if (co >= 4) return CLS_NONE;
-    int n[4] = {0, 0, 0, 0};
+    int n1 = 0, n2 = 0, n3 = 0;
     int zp = z & 1;
+#pragma unroll
     for (int d = 0; d < 4; d++) {
         int da, db, dz;
         nb_off(zp, d, da, db, dz);
         uint8_t t = lat.get(a + da, b + db, z + dz);
-        if (t == WALL) n[1]++;
-        else n[sp_of(t)]++;
+        int st = sp_of(t);
+        n1 += (t == WALL || st == 1) ? 1 : 0;
+        n2 += st == 2 ? 1 : 0;
+        n3 += st == 3 ? 1 : 0;
     }
-    int tot = n[1] + n[2] + n[3];
+    int tot = n1 + n2 + n3;
     if (tot == 0) return CLS_ISO;
     if (tot > 3) return CLS_NONE;
-    return CLS_OCC0 + (sp - 1) * NCENSUS + census_index(n[1], n[2], n[3]);
+    return CLS_OCC0 + (sp - 1) * NCENSUS + census_index(n1, n2, n3);
 }
 
 // Direction of the unique occupied non-wall neighbour (the NBuff of
@@ -136,75 +137,69 @@ struct Touched {            // sites whose class may have changed
     int a[5], b[5], z[5];
 };
 
-// Deposition of species sp on the empty site (a,b,z), deposition.f:24-251.
-// Returns 0, or a nonzero code when the state contradicts the cubic model.
+// One event split in three stages.  The four neighbour updates of stage 2
+// are independent of one another -- two neighbours of a diamond site are
+// never bonded, and each rule reads only its own site's bonds -- so they may
+// run in any order or concurrently with the same result as the reference's
+// loop over the four neighbours.
+struct EvCtx {
+    int a, b, z;
+    int sp;        // deposited species, 0 for an evaporation
+    int c0;        // coordination bits of the site before the event
+    int fdx;       // first-list-entry direction of the site
+};
+
+// Stage 1: occupancy and species of the event site change first; its
+// coordination bits keep their old value until stage 3 (deposition.f:43-46,
+// 237; Evaporation.f:40-44,218).  Returns 0 or 1 if the event does not apply.
 template <class L>
-MKS_HD int apply_deposition(L &lat, int a, int b, int z, int sp, Touched &tc)
+MKS_HD int ev_begin(L &lat, int a, int b, int z, int sp, EvCtx &e)
 {
     uint8_t sx = lat.get(a, b, z);
-    if (sp_of(sx) != 0 || sx == WALL) return 1;
-    int c_old = co_of(sx), fdx = fd_of(sx);
-    // occupancy and species are set first; the coordination bits keep the
-    // empty-site value until the end (deposition.f:43-46,237)
-    lat.put(a, b, z, mk(sp, c_old, fdx, 0));
-    int walls = 0, zp = z & 1;
-    tc.n = 1;
-    tc.a[0] = a; tc.b[0] = b; tc.z[0] = z;
-    for (int d = 0; d < 4; d++) {
-        int da, db, dz;
-        nb_off(zp, d, da, db, dz);
-        int ya = a + da, yb = b + db, yz = z + dz;
-        uint8_t sy = lat.get(ya, yb, yz);
-        tc.a[tc.n] = ya; tc.b[tc.n] = yb; tc.z[tc.n] = yz; tc.n++;
-        if (sy == WALL) { walls++; continue; }
-        int cy = co_of(sy);
+    if (sx == WALL) return 1;
+    if (sp ? sp_of(sx) != 0 : sp_of(sx) == 0) return 1;
+    e.a = a; e.b = b; e.z = z; e.sp = sp;
+    e.c0 = co_of(sx);
+    e.fdx = fd_of(sx);
+    lat.put(a, b, z, mk(sp, e.c0, e.fdx, 0));
+    return 0;
+}
+
+// Stage 2: update neighbour d.  Returns 1 if it is a wall, 0 otherwise, or a
+// negative code when the state contradicts the cubic model.
+template <class L>
+MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz)
+{
+    int da, db, dz;
+    nb_off(e.z & 1, d, da, db, dz);
+    ya = e.a + da; yb = e.b + db; yz = e.z + dz;
+    uint8_t sy = lat.get(ya, yb, yz);
+    if (sy == WALL) return 1;
+    int cy = co_of(sy);
+    if (e.sp) {                                // deposition.f:78-235
         if (sp_of(sy) != 0) {                  // occupied neighbour, :192-230
             if (cy <= 3) lat.put(ya, yb, yz, mk(sp_of(sy), cy + 1, fd_of(sy), 0));
         } else if (cy == 0) {                  // new coor-1 MC site, :86-99
-            // Get_Prob checks the coordination bits of its single neighbour,
-            // i.e. of this site before its own update (Get_Prob.f:156-158)
-            lat.put(ya, yb, yz, mk(0, 1, rev_dir(d), c_old < 2 ? 1 : 0));
+            // Get_Prob reads the coordination bits of its single neighbour,
+            // i.e. of the event site before stage 3 (Get_Prob.f:156-158)
+            lat.put(ya, yb, yz, mk(0, 1, rev_dir(d), e.c0 < 2 ? 1 : 0));
         } else if (cy == 1) {                  // coor 1 -> 2 with FIND_NN, :100-160
             int cnt = 0, yzp = yz & 1;
-            for (int e = 0; e < 4; e++) {
+            for (int f = 0; f < 4; f++) {
                 int ea, eb, ez;
-                nb_off(yzp, e, ea, eb, ez);
+                nb_off(yzp, f, ea, eb, ez);
                 uint8_t t = lat.get(ya + ea, yb + eb, yz + ez);
                 if (t != WALL && sp_of(t) != 0) cnt++;
             }
-            if (cnt < 2) return 2;
+            if (cnt < 2) return -2;
             lat.put(ya, yb, yz, mk(0, cnt, fd_of(sy), 0));
         } else if (cy == 2 || cy == 3) {       // :161-191
             lat.put(ya, yb, yz, mk(0, cy + 1, fd_of(sy), 0));
         }
-    }
-    lat.put(a, b, z, mk(sp, c_old + walls, fdx, 0));
-    return 0;
-}
-
-// Evaporation of the atom at (a,b,z), Evaporation.f:25-262.
-template <class L>
-MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc)
-{
-    uint8_t sx = lat.get(a, b, z);
-    if (sp_of(sx) == 0 || sx == WALL) return 1;
-    int c_atom = co_of(sx), fdx = fd_of(sx);
-    // occupancy cleared first, coordination bits kept until the end (:40-44,218)
-    lat.put(a, b, z, mk(0, c_atom, fdx, 0));
-    int walls = 0, zp = z & 1;
-    tc.n = 1;
-    tc.a[0] = a; tc.b[0] = b; tc.z[0] = z;
-    for (int d = 0; d < 4; d++) {
-        int da, db, dz;
-        nb_off(zp, d, da, db, dz);
-        int ya = a + da, yb = b + db, yz = z + dz;
-        uint8_t sy = lat.get(ya, yb, yz);
-        tc.a[tc.n] = ya; tc.b[tc.n] = yb; tc.z[tc.n] = yz; tc.n++;
-        if (sy == WALL) { walls++; continue; }
-        int cy = co_of(sy);
+    } else {                                   // Evaporation.f:46-215
         if (sp_of(sy) != 0) {                  // :166-210
             if (cy >= 1) lat.put(ya, yb, yz, mk(sp_of(sy), cy - 1, fd_of(sy), 0));
-            else return 3;
+            else return -3;
         } else if (cy == 1) {                  // :51-68, reciprocal only
             if (fd_of(sy) == rev_dir(d)) lat.put(ya, yb, yz, 0);
         } else if (cy == 2) {                  // :69-123
@@ -213,7 +208,7 @@ MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc)
             nb_off(yz & 1, f, fa, fb, fz);
             uint8_t sf = lat.get(ya + fa, yb + fb, yz + fz);
             int w = occupied_dir(lat, ya, yb, yz);
-            if (w < 0) return 4;
+            if (w < 0) return -4;
             lat.put(ya, yb, yz, mk(0, 1, w, co_of(sf) < 2 ? 1 : 0));
         } else if (cy == 3) {                  // :124-141
             lat.put(ya, yb, yz, mk(0, 2, fd_of(sy), 0));
@@ -221,20 +216,64 @@ MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc)
             lat.put(ya, yb, yz, mk(0, 3, fd_of(sy), 0));
         }
     }
-    int c = c_atom - walls;                     // :216-261
+    return 0;
+}
+
+// Stage 3: final coordination and list head of the event site
+// (deposition.f:236-250; Evaporation.f:216-261).  Returns 0 or -5.
+template <class L>
+MKS_HD int ev_finish(L &lat, const EvCtx &e, int walls)
+{
+    if (e.sp) {
+        lat.put(e.a, e.b, e.z, mk(e.sp, e.c0 + walls, e.fdx, 0));
+        return 0;
+    }
+    int c = e.c0 - walls;
     if (c <= 0) {
-        lat.put(a, b, z, 0);
+        lat.put(e.a, e.b, e.z, 0);
     } else if (c == 1) {
         int fa, fb, fz;
-        nb_off(zp, fdx, fa, fb, fz);
-        uint8_t sf = lat.get(a + fa, b + fb, z + fz);
-        int w = occupied_dir(lat, a, b, z);
-        if (w < 0) return 5;
-        lat.put(a, b, z, mk(0, 1, w, co_of(sf) < 2 ? 1 : 0));
+        nb_off(e.z & 1, e.fdx, fa, fb, fz);
+        uint8_t sf = lat.get(e.a + fa, e.b + fb, e.z + fz);
+        int w = occupied_dir(lat, e.a, e.b, e.z);
+        if (w < 0) return -5;
+        lat.put(e.a, e.b, e.z, mk(0, 1, w, co_of(sf) < 2 ? 1 : 0));
     } else {
-        lat.put(a, b, z, mk(0, c, fdx, 0));
+        lat.put(e.a, e.b, e.z, mk(0, c, e.fdx, 0));
     }
     return 0;
+}
+
+// Serial form: deposition of species sp on the empty site (a,b,z)
+// (deposition.f:24-251) or, with sp = 0, evaporation of the atom there
+// (Evaporation.f:25-262).  Returns 0 or a nonzero code.
+template <class L>
+MKS_HD int apply_event(L &lat, int a, int b, int z, int sp, Touched &tc)
+{
+    EvCtx e;
+    if (ev_begin(lat, a, b, z, sp, e)) return 1;
+    tc.n = 5;
+    tc.a[0] = a; tc.b[0] = b; tc.z[0] = z;
+    int walls = 0;
+    for (int d = 0; d < 4; d++) {
+        int r = ev_neighbour(lat, e, d, tc.a[d + 1], tc.b[d + 1], tc.z[d + 1]);
+        if (r < 0) return -r;
+        walls += r;
+    }
+    int r = ev_finish(lat, e, walls);
+    return r < 0 ? -r : 0;
+}
+
+template <class L>
+MKS_HD int apply_deposition(L &lat, int a, int b, int z, int sp, Touched &tc)
+{
+    return sp >= 1 && sp <= 3 ? apply_event(lat, a, b, z, sp, tc) : 1;
+}
+
+template <class L>
+MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc)
+{
+    return apply_event(lat, a, b, z, 0, tc);
 }
 
 // Initial state of SetSi ('FS', SetSi.f:25-221) and SetSiC3C ('F',

@@ -1747,6 +1747,17 @@ int ora_run(ora_t *o, int64_t n, const char *outdir)
     return 0;
 }
 
+int ora_run_until(ora_t *o, double tmax)
+{
+    if (setjmp(o->jb)) return -1;
+    o->started = 1;
+    while (o->time <= tmax) {
+        int r = kmc_step(o, NULL);
+        if (r) return r;
+    }
+    return 0;
+}
+
 int ora_main(ora_t *o, const char *outdir)
 {
     o->log = stdout;

@@ -50,6 +50,10 @@ int ora_init(ora_t *o);
  * <0 error.  Writes output frames into `outdir` when non-NULL.             */
 int ora_run(ora_t *o, int64_t n, const char *outdir);
 
+/* Advance until the clock passes tmax (or an exit condition); returns as
+ * ora_run.  No output frames. */
+int ora_run_until(ora_t *o, double tmax);
+
 /* Run the whole program like mulskips.e in directory `outdir`. */
 int ora_main(ora_t *o, const char *outdir);
 

@@ -36,6 +36,7 @@ def lib():
         L.ora_init.argtypes = [C.c_void_p]
         L.ora_run.argtypes = [C.c_void_p, C.c_int64, C.c_char_p]
         L.ora_main.argtypes = [C.c_void_p, C.c_char_p]
+        L.ora_run_until.argtypes = [C.c_void_p, C.c_double]
         L.ora_trace_enable.argtypes = [C.c_void_p, C.c_int]
         L.ora_trace_len.restype = C.c_int64
         L.ora_trace_len.argtypes = [C.c_void_p]
@@ -88,6 +89,16 @@ class Oracle:
         if r < 0:
             raise RuntimeError(lib().ora_last_error().decode())
         return r
+
+    def run_until(self, tmax):
+        r = lib().ora_run_until(self._h, float(tmax))
+        if r < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return r
+
+    def atoms(self):
+        st, _ = compact_state(self)
+        return int(np.count_nonzero((st & 3) != 0))
 
     def trace_enable(self, on=True):
         lib().ora_trace_enable(self._h, 1 if on else 0)

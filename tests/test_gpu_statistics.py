@@ -1,0 +1,68 @@
+"""Statistical parity of the sublattice KMC with the serial reference.
+
+The plain Si(001) model at T = 1100 K (the benchmark's model, 480^3 box,
+Len1 = 120 slab) etches.  Observable: atoms left at time T_obs (the etch
+rate).  32 seeds of the serial oracle (RunType R, exact reference dynamics,
+deterministic dt = 1/R_tot) against 32 GPU replicas (exponential waiting
+times, synchronous sublattice windows of length tau).  The difference of the
+means must lie inside the 95 % confidence band of the difference."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+T_OBS = 4e-7
+NSEEDS = 32
+
+
+def oracle_atoms(ora, tmp_path, seed):
+    from mulskips_gb300.startdat import write_plain_si_startdat
+    p = tmp_path / f"start{seed}.dat"
+    write_plain_si_startdat(str(p), T=1100.0, len1=120, max_iter=10 ** 9, seed=seed)
+    o = ora.Oracle(str(p), 480, 480, 480, numbers=None)
+    o.init()
+    o.run_until(T_OBS)
+    n = o.atoms()
+    o.close()
+    return n
+
+
+def gpu_atoms(tau, seeds):
+    from mulskips_gb300 import Batch, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    n = len(seeds)
+    b = Batch([(480, 480, 480)] * n, seeds=seeds)
+    b.set_rates(np.stack([pE] * n), np.stack([pD] * n))
+    b.init_flat("S", [120] * n)
+    nwin = int(round(T_OBS / tau))
+    b.run(tau, nwin)
+    obs = b.observables()
+    b.close()
+    assert all(abs(o["time"] - nwin * tau) < 1e-12 for o in obs)
+    return np.array([o["atoms"] for o in obs], dtype=float)
+
+
+def band(x, y):
+    d = x.mean() - y.mean()
+    se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
+    return d, 1.96 * se
+
+
+@pytest.fixture(scope="module")
+def oracle_sample(oracle_lib, tmp_path_factory):
+    tmp = tmp_path_factory.mktemp("stat")
+    return np.array([oracle_atoms(oracle_lib, tmp, 100 + s) for s in range(NSEEDS)], dtype=float)
+
+
+@pytest.mark.parametrize("tau", [2e-9])
+def test_etch_rate_matches_serial_reference(oracle_sample, tau):
+    g = gpu_atoms(tau, [1 + s for s in range(NSEEDS)])
+    d, hw = band(g, oracle_sample)
+    start = 3200 * 36
+    print(f"tau={tau}: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f}  serial {oracle_sample.mean():.1f}"
+          f"+-{oracle_sample.std(ddof=1):.1f}  diff {d:.1f}  95% band +-{hw:.1f}")
+    assert g.mean() < start and oracle_sample.mean() < start       # etching happened
+    assert abs(d) <= hw, f"etch-rate difference {d:.1f} atoms outside the 95% band {hw:.1f}"
