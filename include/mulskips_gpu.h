@@ -151,6 +151,16 @@ int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
 int mks_batch_observables(mks_handle *h, mks_observables *obs /* n entries */);
 int32_t mks_batch_size(mks_handle *h);
 
+/* Tile width (sites, 4..12) of the sublattice decomposition; the default
+ * is 8.  Re-partitions every replica (no counterpart in the reference, whose
+ * loop is serial; the tile shape is one of the autotuner's knobs).         */
+int mks_set_tiling(mks_handle *h, int32_t width);
+int32_t mks_get_tiling(mks_handle *h);
+/* Schedule of the sublattice windows: 1 (default) one persistent kernel in
+ * which each tile waits only for its eight neighbours, 0 one launch per
+ * colour phase.  Both give the same lattice for the same seed.           */
+int mks_set_schedule(mks_handle *h, int32_t persistent);
+
 /* Launch statistics of the last mks_run / mks_batch_run: kernel launches,
  * graph launches, and the device time (ms) of the sublattice kernels
  * measured with CUDA events on the engine's stream.                        */

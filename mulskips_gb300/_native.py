@@ -74,6 +74,9 @@ SIGNATURES = {
                                 C.POINTER(C.c_int64)]),
     "mks_batch_observables": (C.c_int, [C.c_void_p, C.POINTER(MksObservables)]),
     "mks_batch_size": (C.c_int32, [C.c_void_p]),
+    "mks_set_tiling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mks_get_tiling": (C.c_int32, [C.c_void_p]),
+    "mks_set_schedule": (C.c_int, [C.c_void_p, C.c_int32]),
     "mks_last_run_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }

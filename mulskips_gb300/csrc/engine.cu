@@ -38,7 +38,8 @@ namespace {
 // ---------------------------------------------------------------- limits
 constexpr int QMAX = 12;                 // max tile width (sites) in a or b
 constexpr int HALO = 2;                  // read range of an event, in columns
-constexpr int WX = QMAX + 2 * HALO;      // 16: window row stride
+constexpr int WB_MAX = QMAX + 2 * HALO;  // 16: staged rows per layer
+constexpr int RS = 32;                   // staged row stride: one aligned 32-byte row segment
 constexpr int WMAX = 24;                 // max staged layers
 constexpr int MCCAP = 768;               // max event sites per tile
 constexpr int ZMARGIN = 2;               // extra staged layers beyond the band on each side
@@ -67,11 +68,13 @@ struct RepDev {
 
 struct QuadDev {
     int rep, a0, a1, b0, b1;
-    int zlo, zhi, mc;
+    int zlo, zhi, mc;        // mutable: band of event sites and their count
+    int qa, qb, colour, pad;
+    int nbr[8];              // the eight neighbouring tiles (periodic)
 };
 
 struct DevStatus {
-    int error;
+    int error;               // first error code; nonzero also tells waiting warps to leave
     int err_quad;
     unsigned long long fallback;
     unsigned long long reloads;
@@ -82,10 +85,12 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 struct GLat {
     uint8_t *st;
     int NA, NB, NZ, pitch;
+    // reads go to L2 (ld.global.cg): other SMs write the lattice during a
+    // persistent launch and L1 is not coherent with them
     __device__ __forceinline__ uint8_t get(int a, int b, int z) const
     {
         if (z < 0 || z >= NZ) return 0;
-        return st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)];
+        return __ldcg(&st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)]);
     }
     __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
     {
@@ -97,17 +102,17 @@ struct GLat {
 struct SLat {
     uint8_t *w;
     uint32_t *dirty;     // one bit per staged row (b, z)
-    int ax0, bx0, zw0, NZ;
+    int ax0, bx0, zw0, NZ;   // (a, b, z) of staged byte 0
     __device__ __forceinline__ uint8_t get(int a, int b, int z) const
     {
         if (z < 0 || z >= NZ) return 0;
-        return w[((z - zw0) * WX + (b - bx0)) * WX + (a - ax0)];
+        return w[((z - zw0) * WB_MAX + (b - bx0)) * RS + (a - ax0)];
     }
     __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
     {
         if (z < 0 || z >= NZ) return;
-        int row = (z - zw0) * WX + (b - bx0);
-        w[row * WX + (a - ax0)] = v;
+        int row = (z - zw0) * WB_MAX + (b - bx0);
+        w[row * RS + (a - ax0)] = v;
         atomicOr(&dirty[row >> 5], 1u << (row & 31));   // lanes may mark rows concurrently
     }
 };
@@ -274,89 +279,69 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
 }
 
 // ------------------------------------------------ the sublattice kernel
-struct TileShared {
-    uint8_t win[WX * WX * WMAX];
-    uint32_t dirty[(WX * WMAX + 31) / 32];
-    uint32_t list[MCCAP];
-    uint16_t pos[QMAX * QMAX * WMAX];
+struct __align__(16) TileShared {
+    uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments
+    uint32_t list[MCCAP];                      // (site key << 8) | class; class 0 = dead entry
+    uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each tile site, NOPOS if never listed
+    uint32_t dirty[(WB_MAX * WMAX + 31) / 32];
     int cnt[64];
     float rate[64];
     float spcum[3][2];
-    EvCtx ev;
     int nlist;
-    int abort_code;
 };
 
 __device__ __forceinline__ int key_of(int ia, int ib, int z) { return (z << 10) | (ib << 5) | ia; }
+__device__ __forceinline__ int pos_index(uint32_t key, int zw0)
+{
+    return ((int)(key >> 10) - zw0) * (QMAX * QMAX) + (((int)(key >> 5) & 31) - HALO) * QMAX + ((int)(key & 31) - HALO);
+}
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
 
-// Scan the tile interior (staged in `L`), build the event-site list and class
-// counts.  ia/ib are window coordinates (HALO-based).
+// Scan the tile's sites in layers [zl, zh] and build the event-site list and
+// the class counts (ballot compaction, per-class counts aggregated with
+// match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
 __device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh, bool use_pos,
                            int zw0, int wz)
 {
+    const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     for (int c = lane; c < 64; c += 32) S.cnt[c] = 0;
-    if (lane == 0) S.nlist = 0;
-    __syncwarp();
-    int ncol = wa * wb;
-    int total = ncol * (zh - zl + 1);
-    bool overflow = false;
     if (use_pos) {
-        // every staged layer: events may create sites anywhere in the band
         uint32_t *p32 = reinterpret_cast<uint32_t *>(S.pos);
         int nw = QMAX * QMAX * wz / 2;
         for (int i = lane; i < nw; i += 32) p32[i] = 0xFFFFFFFFu;
-        __syncwarp();
     }
+    __syncwarp();
+    int ncol = wa * wb;
+    int total = ncol * (zh - zl + 1);
+    int nl = 0;
     for (int base = 0; base < total; base += 32) {
         int i = base + lane;
-        int cls = CLS_NONE, key = 0;
+        int cls = CLS_NONE;
+        uint32_t key = 0;
         if (i < total) {
             int col = i % ncol, z = zl + i / ncol;
             int ia = col % wa, ib = col / wa;
             int a = a0 + ia, b = b0 + ib;
             if (((a + b + (z >> 1)) & 1) == 0) cls = site_class(L, a, b, z);
-            key = key_of(ia + HALO, ib + HALO, z);
+            key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
         }
-        unsigned m = __ballot_sync(0xffffffffu, cls != CLS_NONE);
-        int before = __popc(m & ((1u << lane) - 1u));
-        int nl = S.nlist;
+        unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
         if (cls != CLS_NONE) {
-            int slot = nl + before;
+            int slot = nl + __popc(m & lanemask_lt());
             if (slot < MCCAP) {
-                S.list[slot] = ((uint32_t)key << 8) | (uint32_t)cls;
-                if (use_pos) {
-                    int ia = (key & 31) - HALO, ib = ((key >> 5) & 31) - HALO, z = key >> 10;
-                    S.pos[((z - zw0) * QMAX + ib) * QMAX + ia] = (uint16_t)slot;
-                }
-                atomicAdd(&S.cnt[cls], 1);
+                S.list[slot] = (key << 8) | (uint32_t)cls;
+                if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
             }
+            unsigned g = __match_any_sync(m, cls);
+            if ((int)(__ffs(g) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(g));
         }
-        __syncwarp();
-        if (lane == 0) S.nlist = nl + __popc(m);
-        __syncwarp();
-        if (S.nlist > MCCAP) overflow = true;
+        nl += __popc(m);
     }
+    if (lane == 0) S.nlist = min(nl, MCCAP);
     __syncwarp();
-    return !overflow;
-}
-
-__device__ __forceinline__ int find_slot(TileShared &S, uint32_t key, bool use_pos, int zw0)
-{
-    if (use_pos) {
-        int ia = (key & 31) - HALO, ib = ((key >> 5) & 31) - HALO, z = key >> 10;
-        uint16_t p = S.pos[((z - zw0) * QMAX + ib) * QMAX + ia];
-        return p == NOPOS ? -1 : (int)p;
-    }
-    int lane = threadIdx.x & 31;
-    for (int base = 0; base < S.nlist; base += 32) {
-        int i = base + lane;
-        bool hit = i < S.nlist && (S.list[i] >> 8) == key;
-        unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (m) return base + __ffs(m) - 1;
-    }
-    return -1;
+    return nl <= MCCAP;
 }
 
 // Run events of one tile on accessor L until the tile clock reaches t_end,
@@ -366,18 +351,20 @@ __device__ __forceinline__ int find_slot(TileShared &S, uint32_t key, bool use_p
 template <class Lat>
 __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev &Q, int qid, double &t, double t_end,
                           unsigned int &evc, int zw0, int zw1, bool use_pos, int &hz_lo, int &hz_hi,
-                          unsigned long long &nev, uint32_t k0, uint32_t k1, uint32_t phase_tag)
+                          unsigned long long &nev, uint32_t k0, uint32_t k1, uint32_t phase_tag, unsigned int window)
 {
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
-    const unsigned int window = R.window;
     const int NZ = R.NZ;
     // Philox draws of 32 consecutive events, one event per lane
     unsigned int pre_base = evc;
     U4 pre = philox4x32_10(U4{pre_base + (unsigned)lane, (uint32_t)qid, window, phase_tag}, k0, k1);
     int used = 0;
+    bool fresh = true;                                 // no event since the list was built
     for (;;) {
+        int nlist = S.nlist;
+        if (nlist > MCCAP - 5) return fresh ? -DERR_CAPACITY : 1;   // compact the list by re-staging
         // cumulative class weights: lane l owns classes 2l and 2l+1 (ISO apart)
         int c0 = 2 * lane, c1 = 2 * lane + 1;
         float w0 = (c0 < NCLASS && c0 != CLS_ISO) ? (float)S.cnt[c0] * S.rate[c0] : 0.f;
@@ -436,12 +423,12 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
                 if (cls < 0) return 0;
             }
         }
-        // member selection: the k-th list entry of class cls (ballot scan)
+        // member selection: the k-th live list entry of class cls (ballot scan)
         int k = min((int)(u01(rnd.y) * (float)S.cnt[cls]), S.cnt[cls] - 1);
         int slot = -1;
-        for (int base = 0; base < S.nlist; base += 32) {
+        for (int base = 0; base < nlist; base += 32) {
             int i = base + lane;
-            bool hit = i < S.nlist && (int)(S.list[i] & 0xFF) == cls;
+            bool hit = i < nlist && (int)(S.list[i] & 0xFF) == cls;
             unsigned m = __ballot_sync(FULL, hit);
             int nh = __popc(m);
             if (k < nh) {
@@ -456,37 +443,29 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         int a = Q.a0 + (int)(key & 31) - HALO, b = Q.b0 + (int)((key >> 5) & 31) - HALO;
         if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return 1;   // needs re-staging
         t += (double)dt;
-        // stage 1 (one lane): the event site
-        if (lane == 0) {
-            int sp = 0;
-            if (cls >= CLS_C1 && cls <= CLS_C3) {
-                int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
-                float u = u01(rnd.w);
-                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
-            }
-            S.abort_code = ev_begin(L, a, b, z, sp, S.ev);
+        int sp = 0;
+        if (cls >= CLS_C1 && cls <= CLS_C3) {
+            int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
+            float u = u01(rnd.w);
+            sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
         }
+        // stage 1: the event site (every lane derives the context, lane 0 writes)
+        EvCtx e;
+        if (ev_prepare(L.get(a, b, z), a, b, z, sp, e)) return -DERR_INVARIANT;
+        if (lane == 0) L.put(a, b, z, ev_begin_state(e));
         __syncwarp();
-        if (S.abort_code) return -DERR_INVARIANT;
-        // stage 2 (four lanes): the four neighbours, independent of one another
-        int r2 = 0, ya = 0, yb = 0, yz = 0;
-        if (lane < 4) r2 = ev_neighbour(L, S.ev, lane, ya, yb, yz);
-        unsigned wallm = __ballot_sync(FULL, lane < 4 && r2 == 1);
-        unsigned errm = __ballot_sync(FULL, lane < 4 && r2 < 0);
-        if (errm) return -DERR_INVARIANT;
-        // stage 3 (one lane): final state of the event site
-        if (lane == 0) S.abort_code = ev_finish(L, S.ev, __popc(wallm)) ? 1 : 0;
+        // stage 2: lanes 1..4 update the four neighbours, independent of one another
+        int ta = a, tb = b, tz = z, r2 = 0;
+        if (lane >= 1 && lane <= 4) r2 = ev_neighbour(L, e, lane - 1, ta, tb, tz);
+        unsigned wallm = __ballot_sync(FULL, lane >= 1 && lane <= 4 && r2 == 1);
+        if (__ballot_sync(FULL, r2 < 0)) return -DERR_INVARIANT;
         __syncwarp();
-        if (S.abort_code) return -DERR_INVARIANT;
+        // stage 3: final state of the event site
+        int r3 = 0;
+        if (lane == 0) r3 = ev_finish(L, e, __popc(wallm));
+        if (__shfl_sync(FULL, r3, 0)) return -DERR_INVARIANT;
+        __syncwarp();
         // re-classify the five touched sites, one per lane (lane 0 the event site)
-        int ta = __shfl_sync(FULL, ya, (lane + 31) & 31);
-        int tb = __shfl_sync(FULL, yb, (lane + 31) & 31);
-        int tz = __shfl_sync(FULL, yz, (lane + 31) & 31);
-        if (lane == 0) {
-            ta = a;
-            tb = b;
-            tz = z;
-        }
         bool act = lane < 5 && tz >= 0 && tz < NZ;
         int ia = ta - Q.a0, ib = tb - Q.b0;
         bool interior = act && ia >= 0 && ia < wa && ib >= 0 && ib < wb;
@@ -496,75 +475,75 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         }
         int ncls = interior ? site_class(L, ta, tb, tz) : CLS_NONE;
         uint32_t tkey = interior ? (uint32_t)key_of(ia + HALO, ib + HALO, tz) : 0u;
-        unsigned im = __ballot_sync(FULL, interior);
-        while (im) {
-            int src = __ffs(im) - 1;
-            im &= im - 1;
-            uint32_t kk = __shfl_sync(FULL, tkey, src);
-            int nc = __shfl_sync(FULL, ncls, src);
-            int ts = find_slot(S, kk, use_pos, zw0);
-            if (lane == 0) {
-                if (ts >= 0) {
-                    int oc = S.list[ts] & 0xFF;
-                    if (nc == CLS_NONE) {
-                        S.cnt[oc]--;
-                        int last = S.nlist - 1;
-                        uint32_t le = S.list[last];
-                        S.list[ts] = le;
-                        if (use_pos) {
-                            uint32_t lk = le >> 8;
-                            int la = (lk & 31) - HALO, lb = ((lk >> 5) & 31) - HALO, lz = lk >> 10;
-                            S.pos[((lz - zw0) * QMAX + lb) * QMAX + la] = (uint16_t)ts;
-                            int qa = (kk & 31) - HALO, qb = ((kk >> 5) & 31) - HALO, qz = kk >> 10;
-                            S.pos[((qz - zw0) * QMAX + qb) * QMAX + qa] = NOPOS;
-                        }
-                        S.nlist = last;
-                    } else if (nc != oc) {
-                        S.cnt[oc]--;
-                        S.cnt[nc]++;
-                        S.list[ts] = (kk << 8) | (uint32_t)nc;
-                    }
-                } else if (nc != CLS_NONE) {
-                    if (S.nlist >= MCCAP) {
-                        S.abort_code = DERR_CAPACITY;
-                    } else {
-                        int ns = S.nlist++;
-                        S.list[ns] = (kk << 8) | (uint32_t)nc;
-                        if (use_pos) {
-                            int qa = (kk & 31) - HALO, qb = ((kk >> 5) & 31) - HALO, qz = kk >> 10;
-                            S.pos[((qz - zw0) * QMAX + qb) * QMAX + qa] = (uint16_t)ns;
-                        }
-                        S.cnt[nc]++;
-                    }
-                }
+        // old list slot of each touched site
+        int my_slot = -1;
+        if (use_pos) {
+            if (interior) {
+                uint16_t p = S.pos[pos_index(tkey, zw0)];
+                my_slot = p == NOPOS ? -1 : (int)p;
             }
-            __syncwarp();
-            if (S.abort_code) return -S.abort_code;
+        } else {
+            unsigned im = __ballot_sync(FULL, interior);
+            while (im) {
+                int src = __ffs(im) - 1;
+                im &= im - 1;
+                uint32_t kk = __shfl_sync(FULL, tkey, src);
+                int found = -1;
+                for (int base = 0; base < nlist && found < 0; base += 32) {
+                    int i = base + lane;
+                    unsigned m = __ballot_sync(FULL, i < nlist && (S.list[i] >> 8) == kk);
+                    if (m) found = base + __ffs(m) - 1;
+                }
+                if (lane == src) my_slot = found;
+            }
         }
+        // update the list in one parallel step: entries leaving the list are
+        // marked dead in place, new ones appended
+        int old_cls = (interior && my_slot >= 0) ? (int)(S.list[my_slot] & 0xFF) : CLS_NONE;
+        bool append = interior && my_slot < 0 && ncls != CLS_NONE;
+        if (interior && old_cls != ncls) {
+            if (my_slot >= 0) S.list[my_slot] = (tkey << 8) | (uint32_t)ncls;
+            if (old_cls != CLS_NONE) atomicSub(&S.cnt[old_cls], 1);
+            if (ncls != CLS_NONE) atomicAdd(&S.cnt[ncls], 1);
+        }
+        unsigned am = __ballot_sync(FULL, append);
+        if (append) {
+            int ns = nlist + __popc(am & lanemask_lt());
+            S.list[ns] = (tkey << 8) | (uint32_t)ncls;
+            if (use_pos) S.pos[pos_index(tkey, zw0)] = (uint16_t)ns;
+        }
+        if (lane == 0) S.nlist = nlist + __popc(am);
+        __syncwarp();
         nev++;
+        fresh = false;
     }
 }
 
-__global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
-                                                 uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
+// One tile for one colour phase of one window: stage, run events from
+// t_start to t_start + tau, write back.  Called by the per-colour kernel and
+// by the persistent kernel.
+__device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
+                             DevStatus *status, uint32_t phase_tag, unsigned int window, double t_start)
 {
-    __shared__ TileShared S;
     int lane = threadIdx.x & 31;
-    int qi = blockIdx.x;
-    if (qi >= nq) return;
-    int qid = qlist[qi];
-    QuadDev Q = quads[qid];
+    QuadDev Q;
+    Q.rep = quads[qid].rep;
+    Q.a0 = quads[qid].a0;
+    Q.a1 = quads[qid].a1;
+    Q.b0 = quads[qid].b0;
+    Q.b1 = quads[qid].b1;
+    Q.zlo = __ldcg(&quads[qid].zlo);     // widened by neighbouring tiles' atomics
+    Q.zhi = __ldcg(&quads[qid].zhi);
     RepDev &R = reps[Q.rep];
     if (!R.active) return;
     if (Q.zhi < Q.zlo) return;   // no event sites in this tile
     for (int c = lane; c < 64; c += 32) S.rate[c] = R.rate[c];
     if (lane < 6) S.spcum[lane >> 1][lane & 1] = R.spcum[lane >> 1][lane & 1];
-    if (lane == 0) S.abort_code = 0;
     __syncwarp();
     uint8_t *st = st_all + R.st_off;
     GLat G{st, R.NA, R.NB, R.NZ, R.pitch};
-    const double t_end = R.T0 + R.tau;
-    double t = R.T0;
+    const double t_end = t_start + R.tau;
+    double t = t_start;
     unsigned int evc = 0;
     unsigned long long nev = 0;
     int hz_lo = 1 << 30, hz_hi = -1;
@@ -585,32 +564,46 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
             int zw1 = min(R.NZ, zw0 + WZ);
             if (zw1 - zw0 < WZ) zw0 = max(0, zw1 - WZ);
             WZ = zw1 - zw0;
-            int ax0 = Q.a0 - HALO, bx0 = Q.b0 - HALO;
             int WA = wa + 2 * HALO, WB = wb + 2 * HALO;
+            int lo_a = Q.a0 - HALO;                        // first staged column
+            bool inner = lo_a >= 0 && lo_a + WA <= R.NA;
+            int ax0 = inner ? (lo_a & ~15) : lo_a;         // column of staged byte 0
+            int bx0 = Q.b0 - HALO;
             int nrows = WB * WZ;
-            bool inner = ax0 >= 0 && ax0 + WA <= R.NA;
-            int w0 = ax0 >> 2;                            // first aligned word (inner rows)
-            int nwords = ((ax0 + WA + 3) >> 2) - w0;      // <= 5
-            if (lane < (WX * WMAX + 31) / 32) S.dirty[lane] = 0u;
-#pragma unroll 2
-            for (int r = lane; r < nrows; r += 32) {
-                int ib = r % WB, iz = r / WB;
-                const uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
-                uint8_t *dst = &S.win[(iz * WX + ib) * WX];
-                if (inner) {
-                    const uint32_t *rw = reinterpret_cast<const uint32_t *>(row) + w0;
-                    uint32_t v[5];
+            if (lane < (WB_MAX * WMAX + 31) / 32) S.dirty[lane] = 0u;
+            if (inner) {
+                // aligned 16-byte chunks: one or two per row, many in flight per lane
+                int nchunk = ((lo_a - ax0) + WA > 16) ? 2 : 1;
+                int total = nrows * nchunk;
+                for (int base = 0; base < total; base += 32 * 8) {
+                    uint4 v[8];
 #pragma unroll
-                    for (int k = 0; k < 5; k++) v[k] = (k < nwords) ? rw[k] : 0u;   // coherent loads: the tile re-stages rows it wrote
-#pragma unroll
-                    for (int k = 0; k < 5; k++)
-#pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            int ia = 4 * (w0 + k) + j - ax0;
-                            if (k < nwords && ia >= 0 && ia < WA) dst[ia] = (uint8_t)(v[k] >> (8 * j));
+                    for (int u = 0; u < 8; u++) {
+                        int p = base + u * 32 + lane;
+                        if (p < total) {
+                            int r = p / nchunk, c = p - r * nchunk;
+                            int ib = r % WB, iz = r / WB;
+                            const uint8_t *row =
+                                st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch + ax0 + 16 * c;
+                            v[u] = __ldcg(reinterpret_cast<const uint4 *>(row));
                         }
-                } else {
-                    for (int ia = 0; ia < WA; ia++) dst[ia] = row[wrapi(ax0 + ia, R.NA)];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        int p = base + u * 32 + lane;
+                        if (p < total) {
+                            int r = p / nchunk, c = p - r * nchunk;
+                            int ib = r % WB, iz = r / WB;
+                            *reinterpret_cast<uint4 *>(&S.win[(iz * WB_MAX + ib) * RS + 16 * c]) = v[u];
+                        }
+                    }
+                }
+            } else {
+                for (int r = lane; r < nrows; r += 32) {
+                    int ib = r % WB, iz = r / WB;
+                    const uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
+                    uint8_t *dst = &S.win[(iz * WB_MAX + ib) * RS];
+                    for (int ia = 0; ia < WA; ia++) dst[ia] = __ldcg(&row[wrapi(ax0 + ia, R.NA)]);
                 }
             }
             __syncwarp();
@@ -619,16 +612,17 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
-            rc = run_events(S, L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag);
+            rc = run_events(S, L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
+                            window);
             __syncwarp();
             // write back the rows that events changed (tile and its one-column ring)
             for (int r = lane; r < nrows; r += 32) {
                 int ib = r % WB, iz = r / WB;
-                int bit = iz * WX + ib;                   // the row index SLat::put marks
+                int bit = iz * WB_MAX + ib;               // the row index SLat::put marks
                 if (!((S.dirty[bit >> 5] >> (bit & 31)) & 1u)) continue;
                 uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
-                const uint8_t *src = &S.win[(iz * WX + ib) * WX];
-                for (int ia = 1; ia < WA - 1; ia++) row[wrapi(ax0 + ia, R.NA)] = src[ia];
+                const uint8_t *src = &S.win[bit * RS];
+                for (int a = Q.a0 - 1; a < Q.a1 + 1; a++) row[wrapi(a, R.NA)] = src[a - ax0];
             }
             if (rc > 0 && lane == 0) atomicAdd(&status->reloads, 1ull);
         } else {
@@ -639,13 +633,17 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
                 return;
             }
             GLat G2 = G;
-            rc = run_events(S, G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag);
+            rc = run_events(S, G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag,
+                            window);
         }
         __syncwarp();
-        // z band of the remaining event sites
+        // z band of the remaining (live) event sites
         int lo = 1 << 30, hi = -1;
-        for (int i = lane; i < S.nlist; i += 32) {
-            int z = (int)(S.list[i] >> 18);
+        int nl = S.nlist;
+        for (int i = lane; i < nl; i += 32) {
+            uint32_t en = S.list[i];
+            if ((en & 0xFF) == 0) continue;
+            int z = (int)(en >> 18);
             lo = min(lo, z);
             hi = max(hi, z);
         }
@@ -667,33 +665,86 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
         hz_lo = min(hz_lo, __shfl_xor_sync(0xffffffffu, hz_lo, o));
         hz_hi = max(hz_hi, __shfl_xor_sync(0xffffffffu, hz_hi, o));
     }
+    int live = 0;
+    for (int c = lane; c < NCLASS; c += 32) live += (c == CLS_NONE) ? 0 : S.cnt[c];
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
     if (lane == 0) {
         quads[qid].zlo = zlo;
         quads[qid].zhi = zhi;
-        quads[qid].mc = S.nlist;
+        quads[qid].mc = live;
         if (nev) atomicAdd(&R.events, nev);
         if (hz_hi >= 0) {
             // widen the z bands of the neighbouring tiles whose sites changed
-            int qa = (Q.a0 * R.nqa) / R.NA, qb = (Q.b0 * R.nqb) / R.NB;
-            // recover exact tile indices (tiles are [floor(i*NA/nqa), floor((i+1)*NA/nqa)))
-            while (qa > 0 && (qa * R.NA) / R.nqa > Q.a0) qa--;
-            while (qa + 1 < R.nqa && ((qa + 1) * R.NA) / R.nqa <= Q.a0) qa++;
-            while (qb > 0 && (qb * R.NB) / R.nqb > Q.b0) qb--;
-            while (qb + 1 < R.nqb && ((qb + 1) * R.NB) / R.nqb <= Q.b0) qb++;
-            for (int db = -1; db <= 1; db++)
-                for (int da = -1; da <= 1; da++) {
-                    if (!da && !db) continue;
-                    int na = (qa + da + R.nqa) % R.nqa, nb = (qb + db + R.nqb) % R.nqb;
-                    QuadDev *N = &quads[R.quad_base + nb * R.nqa + na];
-                    atomicMin(&N->zlo, hz_lo);
-                    atomicMax(&N->zhi, hz_hi);
+            for (int k = 0; k < 8; k++) {
+                QuadDev *N = &quads[quads[qid].nbr[k]];
+                atomicMin(&N->zlo, hz_lo);
+                atomicMax(&N->zhi, hz_hi);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
+                                                 uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
+{
+    __shared__ TileShared S;
+    int qi = blockIdx.x;
+    if (qi >= nq) return;
+    int qid = qlist[qi];
+    const RepDev &R = reps[quads[qid].rep];
+    process_tile(S, reps, quads, qid, st_all, status, phase_tag, R.window, R.T0);
+}
+
+// Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
+// g owns tiles g, g+G, ... and runs them in increasing P.  A tile of colour c
+// may run phase P once each neighbour (all of another colour) has finished
+// its last phase before P, i.e. progress[n] >= P - ((c - colour(n)) & 3); a
+// neighbour cannot start a later phase before this tile publishes P.  All
+// waits point to strictly earlier phases and all blocks are co-resident
+// (cooperative launch), so the schedule cannot deadlock; every wait is still
+// bounded and gives up with DERR_TIMEOUT.  The result equals running the four
+// colour launches per window in order.
+constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
+
+__global__ void __launch_bounds__(32) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
+                                                      DevStatus *status, int *progress, int nwin)
+{
+    __shared__ TileShared S;
+    int lane = threadIdx.x & 31;
+    for (int P = 0; P < 4 * nwin; P++) {
+        int c = P & 3, w = P >> 2;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            if (quads[t].colour != c) continue;
+            if (lane < 8) {
+                int n = quads[t].nbr[lane];
+                int need = P - ((c - quads[n].colour) & 3);
+                long long t0 = clock64();
+                volatile int *pr = progress + n;
+                volatile int *err = &status->error;
+                while (*pr < need) {
+                    if (*err) break;
+                    if (clock64() - t0 > SPIN_LIMIT_CYCLES) {
+                        set_error(status, DERR_TIMEOUT, t);
+                        break;
+                    }
+                    __nanosleep(64);
                 }
+            }
+            __syncwarp();
+            __threadfence();                                // acquire: neighbours' writes before their flag
+            if (*(volatile int *)&status->error) return;
+            const RepDev &R = reps[quads[t].rep];
+            process_tile(S, reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
+                         R.T0 + (double)w * R.tau);
+            __threadfence();                                // release: each lane's writes reach L2 ...
+            __syncwarp();                                   // ... before lane 0 publishes the flag
+            if (lane == 0) atomicExch(progress + t, P);
         }
     }
 }
 
 // End of a window: advance the replica clock, apply the exit conditions.
-__global__ void k_window_end(RepDev *reps, QuadDev *quads)
+__global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin)
 {
     RepDev &R = reps[blockIdx.x];
     long long s = 0;
@@ -709,8 +760,8 @@ __global__ void k_window_end(RepDev *reps, QuadDev *quads)
     if (threadIdx.x == 0) {
         R.mc_count = sh[0];
         if (!R.active) return;
-        R.T0 += R.tau;
-        R.window++;
+        R.T0 += (double)nwin * R.tau;
+        R.window += (unsigned)nwin;
         if (R.mc_count <= 20) {
             R.active = 0;
             R.stop_reason = 1;
@@ -770,6 +821,10 @@ struct mks_handle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_windows = 0;
+    int tile_width = 8;
+    int *d_progress = nullptr;
+    int coop_grid = 0;
+    int schedule = 1;            // 1 persistent dataflow kernel, 0 one launch per colour phase
     uint32_t phase_counter = 0;
     int64_t last_kernels = 0, last_graphs = 0, last_phase_launches = 0;
     double last_ms = 0.0;
@@ -818,9 +873,12 @@ int check_config(const mks_config &c)
 }
 
 // even number of tiles per side, widths within [8, QMAX]
-int tiles_for(int n)
+// even number of tiles along a side of n sites, each about `width` wide
+// (at least 4: the write ring of one tile and the read halo of the next
+// same-colour tile must not meet) and at most QMAX
+int tiles_for(int n, int width)
 {
-    int t = 2 * (n / 16);
+    int t = 2 * (n / (2 * width));
     if (t < 2) t = 2;
     while ((n + t - 1) / t > QMAX) t += 2;
     return t;
@@ -857,6 +915,74 @@ int rescan(mks_handle *h)
     return 0;
 }
 
+// cut every replica's (a,b) plane into tiles of about `width` sites
+void partition(mks_handle *h, int width)
+{
+    h->quads_h.clear();
+    for (int c = 0; c < 4; c++) h->color_list_h[c].clear();
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        RepHost &r = h->reps[i];
+        r.nqa = tiles_for(r.NA, width);
+        r.nqb = tiles_for(r.NB, width);
+        r.quad_base = (int)h->quads_h.size();
+        for (int qb = 0; qb < r.nqb; qb++)
+            for (int qa = 0; qa < r.nqa; qa++) {
+                QuadDev q;
+                q.rep = (int)i;
+                q.a0 = (qa * r.NA) / r.nqa;
+                q.a1 = ((qa + 1) * r.NA) / r.nqa;
+                q.b0 = (qb * r.NB) / r.nqb;
+                q.b1 = ((qb + 1) * r.NB) / r.nqb;
+                q.zlo = 1 << 30;
+                q.zhi = -1;
+                q.mc = 0;
+                q.qa = qa;
+                q.qb = qb;
+                q.colour = (qa & 1) + 2 * (qb & 1);
+                q.pad = 0;
+                int k = 0;
+                for (int db = -1; db <= 1; db++)
+                    for (int da = -1; da <= 1; da++) {
+                        if (!da && !db) continue;
+                        int na = (qa + da + r.nqa) % r.nqa, nb = (qb + db + r.nqb) % r.nqb;
+                        q.nbr[k++] = r.quad_base + nb * r.nqa + na;
+                    }
+                h->color_list_h[q.colour].push_back((int)h->quads_h.size());
+                h->quads_h.push_back(q);
+            }
+    }
+    h->tile_width = width;
+}
+
+int upload_tiles(mks_handle *h)
+{
+    cudaFree(h->d_quads);
+    h->d_quads = nullptr;
+    CK(cudaMalloc(&h->d_quads, sizeof(QuadDev) * h->quads_h.size()));
+    CK(cudaMemcpyAsync(h->d_quads, h->quads_h.data(), sizeof(QuadDev) * h->quads_h.size(), cudaMemcpyHostToDevice,
+                       h->stream));
+    for (int c = 0; c < 4; c++) {
+        cudaFree(h->d_clist[c]);
+        h->d_clist[c] = nullptr;
+        size_t nb = sizeof(int) * std::max<size_t>(1, h->color_list_h[c].size());
+        CK(cudaMalloc(&h->d_clist[c], nb));
+        if (!h->color_list_h[c].empty())
+            CK(cudaMemcpyAsync(h->d_clist[c], h->color_list_h[c].data(), sizeof(int) * h->color_list_h[c].size(),
+                               cudaMemcpyHostToDevice, h->stream));
+    }
+    cudaFree(h->d_progress);
+    h->d_progress = nullptr;
+    CK(cudaMalloc(&h->d_progress, sizeof(int) * h->quads_h.size()));
+    // resident grid of the persistent kernel (cooperative launch)
+    int dev = 0, nsm = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl_persistent, 32, 0));
+    h->coop_grid = (int)std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (int64_t)h->quads_h.size());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
 int create_impl(const mks_config *cfgs, int n, mks_handle **out)
 {
     if (!cfgs || n <= 0 || !out) return fail(MKS_ERR_ARG, "bad arguments");
@@ -877,31 +1003,15 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         r.NB = cfgs[i].leny / 6;
         r.NZ = cfgs[i].lenz / 3 + 1;
         r.pitch = (r.NA + 15) & ~15;
-        r.nqa = tiles_for(r.NA);
-        r.nqb = tiles_for(r.NB);
-        r.quad_base = (int)h->quads_h.size();
         r.st_off = off;
         off += (int64_t)r.NZ * r.NB * r.pitch;
         off = (off + 255) & ~(int64_t)255;
         memset(r.ptransE, 0, sizeof r.ptransE);
         memset(r.ptransD, 0, sizeof r.ptransD);
-        for (int qb = 0; qb < r.nqb; qb++)
-            for (int qa = 0; qa < r.nqa; qa++) {
-                QuadDev q;
-                q.rep = i;
-                q.a0 = (qa * r.NA) / r.nqa;
-                q.a1 = ((qa + 1) * r.NA) / r.nqa;
-                q.b0 = (qb * r.NB) / r.nqb;
-                q.b1 = ((qb + 1) * r.NB) / r.nqb;
-                q.zlo = 1 << 30;
-                q.zhi = -1;
-                q.mc = 0;
-                h->color_list_h[(qa & 1) + 2 * (qb & 1)].push_back((int)h->quads_h.size());
-                h->quads_h.push_back(q);
-            }
         h->reps.push_back(r);
     }
     h->st_bytes = off;
+    partition(h, 8);
     auto cleanup_fail = [&](const char *what, cudaError_t e) {
         fail(MKS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
         mks_destroy(h);
@@ -914,20 +1024,15 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     if ((e = cudaMalloc(&h->d_st, (size_t)h->st_bytes)) != cudaSuccess) return cleanup_fail("lattice allocation", e);
     if ((e = cudaMemsetAsync(h->d_st, 0, (size_t)h->st_bytes, h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
     if ((e = cudaMalloc(&h->d_reps, sizeof(RepDev) * n)) != cudaSuccess) return cleanup_fail("alloc", e);
-    if ((e = cudaMalloc(&h->d_quads, sizeof(QuadDev) * h->quads_h.size())) != cudaSuccess) return cleanup_fail("alloc", e);
     if ((e = cudaMalloc(&h->d_status, sizeof(DevStatus))) != cudaSuccess) return cleanup_fail("alloc", e);
     if ((e = cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
-    for (int c = 0; c < 4; c++) {
-        size_t nb = sizeof(int) * std::max<size_t>(1, h->color_list_h[c].size());
-        if ((e = cudaMalloc(&h->d_clist[c], nb)) != cudaSuccess) return cleanup_fail("alloc", e);
-        if (!h->color_list_h[c].empty() &&
-            (e = cudaMemcpyAsync(h->d_clist[c], h->color_list_h[c].data(), sizeof(int) * h->color_list_h[c].size(),
-                                 cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
-            return cleanup_fail("copy", e);
+    {
+        int rc_t = upload_tiles(h);
+        if (rc_t) {
+            mks_destroy(h);
+            return rc_t;
+        }
     }
-    if ((e = cudaMemcpyAsync(h->d_quads, h->quads_h.data(), sizeof(QuadDev) * h->quads_h.size(),
-                             cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
-        return cleanup_fail("copy", e);
     std::vector<RepDev> d(n);
     for (int i = 0; i < n; i++) {
         memset(&d[i], 0, sizeof(RepDev));
@@ -968,9 +1073,55 @@ int launch_window(mks_handle *h)
         h->last_kernels++;
         h->last_phase_launches++;
     }
-    k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads);
+    k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, 1);
     h->last_kernels++;
     CK(cudaGetLastError());
+    return 0;
+}
+
+// Persistent schedule: one cooperative launch advances every tile through up
+// to 64 windows, then k_window_end advances the clocks and applies the exit
+// conditions (checked per launch).
+int run_persistent(mks_handle *h, int64_t max_windows)
+{
+    std::vector<RepDev> d;
+    int nt = (int)h->quads_h.size();
+    CK(cudaEventRecord(h->ev0, h->stream));
+    int64_t done = 0;
+    int launches = 0;
+    while (done < max_windows) {
+        int nw = (int)std::min<int64_t>(64, max_windows - done);
+        CK(cudaMemsetAsync(h->d_progress, 0xFF, sizeof(int) * (size_t)nt, h->stream));
+        void *args[] = {&h->d_reps, &h->d_quads, &nt, &h->d_st, &h->d_status, &h->d_progress, &nw};
+        CK(cudaLaunchCooperativeKernel((const void *)k_sl_persistent, dim3(h->coop_grid), dim3(32), args, 0,
+                                       h->stream));
+        k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw);
+        CK(cudaGetLastError());
+        h->last_kernels += 2;
+        h->last_phase_launches += 1;
+        done += nw;
+        launches++;
+        if ((launches & 3) == 0 || done >= max_windows) {
+            DevStatus s;
+            int rc = read_status(h, s);
+            if (rc) return rc;
+            if (s.error) return fail(s.error, "device error %d in tile %d", s.error, s.err_quad);
+            rc = download_reps(h, d);
+            if (rc) return rc;
+            bool any = false;
+            for (auto &x : d) any |= x.active != 0;
+            if (!any) break;
+        }
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->last_ms = ms;
+    DevStatus s;
+    int rc = read_status(h, s);
+    if (rc) return rc;
+    if (s.error) return fail(s.error, "device error %d in tile %d", s.error, s.err_quad);
     return 0;
 }
 
@@ -992,6 +1143,7 @@ int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_
     h->last_kernels = 0;
     h->last_graphs = 0;
     h->last_phase_launches = 0;
+    if (h->schedule == 1) return run_persistent(h, max_windows);
     // capture a block of windows once, replay it
     const int WPG = (int)std::max<int64_t>(1, std::min<int64_t>(8, max_windows));
     if (!h->graph_exec || h->graph_windows != WPG) {
@@ -1134,6 +1286,7 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_reps);
     cudaFree(h->d_quads);
     cudaFree(h->d_status);
+    cudaFree(h->d_progress);
     for (int c = 0; c < 4; c++) cudaFree(h->d_clist[c]);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1487,6 +1640,37 @@ int mks_get_status(mks_handle *h, mks_status *st)
     st->windows = d[0].window;
     st->active = d[0].active;
     st->stop_reason = d[0].stop_reason;
+    return 0;
+}
+
+int mks_set_tiling(mks_handle *h, int32_t width)
+{
+    if (!h || width < 4 || width > QMAX) return fail(MKS_ERR_ARG, "tile width must be 4..%d", QMAX);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+    h->graph_windows = 0;
+    partition(h, width);
+    int rc = upload_tiles(h);
+    if (rc) return rc;
+    std::vector<RepDev> d;
+    rc = download_reps(h, d);
+    if (rc) return rc;
+    for (size_t i = 0; i < d.size(); i++) {
+        d[i].nqa = h->reps[i].nqa;
+        d[i].nqb = h->reps[i].nqb;
+        d[i].quad_base = h->reps[i].quad_base;
+    }
+    rc = upload_reps(h, d);
+    if (rc) return rc;
+    return rescan(h);
+}
+
+int32_t mks_get_tiling(mks_handle *h) { return h ? h->tile_width : 0; }
+
+int mks_set_schedule(mks_handle *h, int32_t persistent)
+{
+    if (!h || (persistent != 0 && persistent != 1)) return fail(MKS_ERR_ARG, "schedule must be 0 or 1");
+    h->schedule = persistent;
     return 0;
 }
 

@@ -151,17 +151,25 @@ struct EvCtx {
 
 // Stage 1: occupancy and species of the event site change first; its
 // coordination bits keep their old value until stage 3 (deposition.f:43-46,
-// 237; Evaporation.f:40-44,218).  Returns 0 or 1 if the event does not apply.
-template <class L>
-MKS_HD int ev_begin(L &lat, int a, int b, int z, int sp, EvCtx &e)
+// 237; Evaporation.f:40-44,218).  ev_prepare only reads the site byte sx;
+// ev_begin also writes the site.  Both return 0, or 1 if the event does not
+// apply to the site.
+MKS_HD int ev_prepare(uint8_t sx, int a, int b, int z, int sp, EvCtx &e)
 {
-    uint8_t sx = lat.get(a, b, z);
     if (sx == WALL) return 1;
     if (sp ? sp_of(sx) != 0 : sp_of(sx) == 0) return 1;
     e.a = a; e.b = b; e.z = z; e.sp = sp;
     e.c0 = co_of(sx);
     e.fdx = fd_of(sx);
-    lat.put(a, b, z, mk(sp, e.c0, e.fdx, 0));
+    return 0;
+}
+MKS_HD uint8_t ev_begin_state(const EvCtx &e) { return mk(e.sp, e.c0, e.fdx, 0); }
+
+template <class L>
+MKS_HD int ev_begin(L &lat, int a, int b, int z, int sp, EvCtx &e)
+{
+    if (ev_prepare(lat.get(a, b, z), a, b, z, sp, e)) return 1;
+    lat.put(a, b, z, ev_begin_state(e));
     return 0;
 }
 

@@ -132,6 +132,15 @@ class Lattice:
         assert a.size == lx * ly * (lz + 1)
         N.check(N.lib().mks_load_lattice(self._h, N.ptr(a)))
 
+    def set_tiling(self, width):
+        N.check(N.lib().mks_set_tiling(self._h, int(width)))
+
+    def tiling(self):
+        return N.lib().mks_get_tiling(self._h)
+
+    def set_schedule(self, persistent):
+        N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
+
     def run_stats(self):
         k, g, p = C.c_int64(), C.c_int64(), C.c_int64()
         ms = C.c_double()
@@ -180,10 +189,25 @@ class Batch:
                                       float(max_time_each), C.byref(ne)))
         return ne.value
 
+    def set_tiling(self, width):
+        N.check(N.lib().mks_set_tiling(self._h, int(width)))
+
+    def set_schedule(self, persistent):
+        N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
+
     def observables(self):
         o = (N.MksObservables * self.n)()
         N.check(N.lib().mks_batch_observables(self._h, o))
         return [x.as_dict() for x in o]
+
+    def set_tiling(self, width):
+        N.check(N.lib().mks_set_tiling(self._h, int(width)))
+
+    def tiling(self):
+        return N.lib().mks_get_tiling(self._h)
+
+    def set_schedule(self, persistent):
+        N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
 
     def run_stats(self):
         k, g, p = C.c_int64(), C.c_int64(), C.c_int64()

@@ -102,3 +102,33 @@ def test_unsupported_config_is_rejected():
         Lattice(480, 480, 480, ptrans_zig=0.8)
     with pytest.raises(MksError):
         Lattice(100, 480, 480)
+
+
+def test_persistent_schedule_equals_per_colour_launches():
+    """The persistent kernel (each tile waits only for its eight neighbours)
+    and one launch per colour phase give the same lattice bit for bit."""
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    states = []
+    for persistent in (0, 1):
+        with Lattice(480, 480, 480, seed=21) as lat:
+            lat.set_schedule(persistent)
+            lat.set_rates(pE, pD)
+            lat.init_flat("S", 240)
+            ev, t = lat.run(1e-8, 40)
+            states.append((lat.state(), ev))
+    assert states[0][1] == states[1][1] and states[0][1] > 0
+    assert np.array_equal(states[0][0], states[1][0])
+
+
+@pytest.mark.parametrize("width", [4, 6, 12])
+def test_tile_widths_keep_invariants(width):
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    with Lattice(480, 480, 480, seed=4) as lat:
+        lat.set_tiling(width)
+        lat.set_rates(pE, pD)
+        lat.init_flat("S", 240)
+        ev, _ = lat.run(2e-8, 24)
+        assert ev > 0
+        check_invariants(lat.state())
