@@ -151,7 +151,7 @@ int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
 int mks_batch_observables(mks_handle *h, mks_observables *obs /* n entries */);
 int32_t mks_batch_size(mks_handle *h);
 
-/* Tile width (sites, 4..12) of the sublattice decomposition; the default
+/* Tile width (sites, 4..8) of the sublattice decomposition; the default
  * is 8.  Re-partitions every replica (no counterpart in the reference, whose
  * loop is serial; the tile shape is one of the autotuner's knobs).         */
 int mks_set_tiling(mks_handle *h, int32_t width);

@@ -36,12 +36,12 @@ using namespace mks;
 namespace {
 
 // ---------------------------------------------------------------- limits
-constexpr int QMAX = 12;                 // max tile width (sites) in a or b
+constexpr int QMAX = 8;                  // max tile width (sites) in a or b
 constexpr int HALO = 2;                  // read range of an event, in columns
-constexpr int WB_MAX = QMAX + 2 * HALO;  // 16: staged rows per layer
+constexpr int WB_MAX = QMAX + 2 * HALO;  // 12: staged rows per layer
 constexpr int RS = 32;                   // staged row stride: one aligned 32-byte row segment
-constexpr int WMAX = 24;                 // max staged layers
-constexpr int MCCAP = 768;               // max event sites per tile
+constexpr int WMAX = 20;                 // max staged layers
+constexpr int MCCAP = 512;               // max event sites per tile
 constexpr int ZMARGIN = 2;               // extra staged layers beyond the band on each side
 constexpr int NRELOAD = 512;             // bounded re-staging per tile and phase
 constexpr uint16_t NOPOS = 0xFFFF;
@@ -96,24 +96,6 @@ struct GLat {
     {
         if (z < 0 || z >= NZ) return;
         st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)] = v;
-    }
-};
-
-struct SLat {
-    uint8_t *w;
-    uint32_t *dirty;     // one bit per staged row (b, z)
-    int ax0, bx0, zw0, NZ;   // (a, b, z) of staged byte 0
-    __device__ __forceinline__ uint8_t get(int a, int b, int z) const
-    {
-        if (z < 0 || z >= NZ) return 0;
-        return w[((z - zw0) * WB_MAX + (b - bx0)) * RS + (a - ax0)];
-    }
-    __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
-    {
-        if (z < 0 || z >= NZ) return;
-        int row = (z - zw0) * WB_MAX + (b - bx0);
-        w[row * RS + (a - ax0)] = v;
-        atomicOr(&dirty[row >> 5], 1u << (row & 31));   // lanes may mark rows concurrently
     }
 };
 
@@ -283,12 +265,54 @@ struct __align__(16) TileShared {
     uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments
     uint32_t list[MCCAP];                      // (site key << 8) | class; class 0 = dead entry
     uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each tile site, NOPOS if never listed
-    uint32_t dirty[(WB_MAX * WMAX + 31) / 32];
+    uint8_t dirty[WB_MAX * WMAX];              // staged rows changed by events
     int cnt[64];
     float rate[64];
     float spcum[3][2];
     int nlist;
 };
+
+// The one tile a warp works on (one warp per block).  Declared at file scope so
+// every access compiles to shared-memory instructions.
+__shared__ TileShared g_tile;
+
+struct SLat {
+    int ax0, bx0, zw0, NZ;   // (a, b, z) of staged byte 0
+    __device__ __forceinline__ uint8_t get(int a, int b, int z) const
+    {
+        if (z < 0 || z >= NZ) return 0;
+        return g_tile.win[((z - zw0) * WB_MAX + (b - bx0)) * RS + (a - ax0)];
+    }
+    __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
+    {
+        if (z < 0 || z >= NZ) return;
+        int row = (z - zw0) * WB_MAX + (b - bx0);
+        g_tile.win[row * RS + (a - ax0)] = v;
+        g_tile.dirty[row] = 1;
+    }
+};
+
+// Replica scalars the tile kernels need, held in registers.
+struct RepLocal {
+    int64_t st_off;
+    int NA, NB, NZ, pitch;
+    double tau;
+    unsigned long long seed;
+    int active;
+};
+__device__ __forceinline__ RepLocal rep_local(const RepDev &R)
+{
+    RepLocal r;
+    r.st_off = R.st_off;
+    r.NA = R.NA;
+    r.NB = R.NB;
+    r.NZ = R.NZ;
+    r.pitch = R.pitch;
+    r.tau = R.tau;
+    r.seed = R.seed;
+    r.active = R.active;
+    return r;
+}
 
 __device__ __forceinline__ int key_of(int ia, int ib, int z) { return (z << 10) | (ib << 5) | ia; }
 __device__ __forceinline__ int pos_index(uint32_t key, int zw0)
@@ -301,9 +325,10 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 // the class counts (ballot compaction, per-class counts aggregated with
 // match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
-__device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh, bool use_pos,
-                           int zw0, int wz)
+__device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh,
+                                           bool use_pos, int zw0, int wz)
 {
+    TileShared &S = g_tile;
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     for (int c = lane; c < 64; c += 32) S.cnt[c] = 0;
@@ -314,30 +339,28 @@ __device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, 
     }
     __syncwarp();
     int ncol = wa * wb;
-    int total = ncol * (zh - zl + 1);
     int nl = 0;
-    for (int base = 0; base < total; base += 32) {
-        int i = base + lane;
-        int cls = CLS_NONE;
-        uint32_t key = 0;
-        if (i < total) {
-            int col = i % ncol, z = zl + i / ncol;
-            int ia = col % wa, ib = col / wa;
-            int a = a0 + ia, b = b0 + ib;
-            if (((a + b + (z >> 1)) & 1) == 0) cls = site_class(L, a, b, z);
-            key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
-        }
-        unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
-        if (cls != CLS_NONE) {
-            int slot = nl + __popc(m & lanemask_lt());
-            if (slot < MCCAP) {
-                S.list[slot] = (key << 8) | (uint32_t)cls;
-                if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
+    for (int col0 = 0; col0 < ncol; col0 += 32) {
+        int col = col0 + lane;
+        bool cv = col < ncol;
+        int ib = cv ? col / wa : 0, ia = cv ? col - ib * wa : 0;
+        int a = a0 + ia, b = b0 + ib;
+        for (int z = zl; z <= zh; z++) {
+            int cls = CLS_NONE;
+            if (cv && ((a + b + (z >> 1)) & 1) == 0) cls = site_class(L, a, b, z);
+            unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
+            if (cls != CLS_NONE) {
+                uint32_t key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
+                int slot = nl + __popc(m & lanemask_lt());
+                if (slot < MCCAP) {
+                    S.list[slot] = (key << 8) | (uint32_t)cls;
+                    if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
+                }
+                unsigned g = __match_any_sync(m, cls);
+                if ((int)(__ffs(g) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(g));
             }
-            unsigned g = __match_any_sync(m, cls);
-            if ((int)(__ffs(g) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(g));
+            nl += __popc(m);
         }
-        nl += __popc(m);
     }
     if (lane == 0) S.nlist = min(nl, MCCAP);
     __syncwarp();
@@ -349,10 +372,12 @@ __device__ bool build_list(TileShared &S, const Lat &L, int a0, int b0, int wa, 
 // Returns 0 done, 1 needs re-staging, <0 error.  hz_lo/hz_hi (per lane) collect
 // the layers of changed sites outside the tile.
 template <class Lat>
-__device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev &Q, int qid, double &t, double t_end,
-                          unsigned int &evc, int zw0, int zw1, bool use_pos, int &hz_lo, int &hz_hi,
-                          unsigned long long &nev, uint32_t k0, uint32_t k1, uint32_t phase_tag, unsigned int window)
+__device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadDev &Q, int qid, double &t,
+                                          double t_end, unsigned int &evc, int zw0, int zw1, bool use_pos,
+                                          int &hz_lo, int &hz_hi, unsigned long long &nev, uint32_t k0, uint32_t k1,
+                                          uint32_t phase_tag, unsigned int window)
 {
+    TileShared &S = g_tile;
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
@@ -362,6 +387,9 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
     U4 pre = philox4x32_10(U4{pre_base + (unsigned)lane, (uint32_t)qid, window, phase_tag}, k0, k1);
     int used = 0;
     bool fresh = true;                                 // no event since the list was built
+    // time left in the window, FP32 on the critical path; the FP64 clock t is
+    // still accumulated event by event
+    float rem = (float)(t_end - t);
     for (;;) {
         int nlist = S.nlist;
         if (nlist > MCCAP - 5) return fresh ? -DERR_CAPACITY : 1;   // compact the list by re-staging
@@ -392,8 +420,8 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         rnd.w = __shfl_sync(FULL, pre.w, used);
         used++;
         evc++;
-        float dt = -__logf(u01(rnd.z)) / rtot;
-        if (t + (double)dt > t_end) {
+        float dt = __fdividef(-__logf(u01(rnd.z)), rtot);
+        if (dt > rem) {
             t = t_end;
             return 0;
         }
@@ -432,7 +460,9 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
             unsigned m = __ballot_sync(FULL, hit);
             int nh = __popc(m);
             if (k < nh) {
-                slot = base + __fns(m, 0, k + 1);
+                // the lane holding the k-th hit of this chunk
+                unsigned pick = __ballot_sync(FULL, hit && __popc(m & lanemask_lt()) == k);
+                slot = base + __ffs(pick) - 1;
                 break;
             }
             k -= nh;
@@ -443,6 +473,7 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
         int a = Q.a0 + (int)(key & 31) - HALO, b = Q.b0 + (int)((key >> 5) & 31) - HALO;
         if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return 1;   // needs re-staging
         t += (double)dt;
+        rem -= dt;
         int sp = 0;
         if (cls >= CLS_C1 && cls <= CLS_C3) {
             int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
@@ -522,9 +553,11 @@ __device__ int run_events(TileShared &S, Lat &L, const RepDev &R, const QuadDev 
 // One tile for one colour phase of one window: stage, run events from
 // t_start to t_start + tau, write back.  Called by the per-colour kernel and
 // by the persistent kernel.
-__device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
-                             DevStatus *status, uint32_t phase_tag, unsigned int window, double t_start)
+__device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
+                                             DevStatus *status, uint32_t phase_tag, unsigned int window,
+                                             double t_start)
 {
+    TileShared &S = g_tile;
     int lane = threadIdx.x & 31;
     QuadDev Q;
     Q.rep = quads[qid].rep;
@@ -534,11 +567,12 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
     Q.b1 = quads[qid].b1;
     Q.zlo = __ldcg(&quads[qid].zlo);     // widened by neighbouring tiles' atomics
     Q.zhi = __ldcg(&quads[qid].zhi);
-    RepDev &R = reps[Q.rep];
+    RepDev &Rg = reps[Q.rep];
+    const RepLocal R = rep_local(Rg);
     if (!R.active) return;
     if (Q.zhi < Q.zlo) return;   // no event sites in this tile
-    for (int c = lane; c < 64; c += 32) S.rate[c] = R.rate[c];
-    if (lane < 6) S.spcum[lane >> 1][lane & 1] = R.spcum[lane >> 1][lane & 1];
+    for (int c = lane; c < 64; c += 32) S.rate[c] = Rg.rate[c];
+    if (lane < 6) S.spcum[lane >> 1][lane & 1] = Rg.spcum[lane >> 1][lane & 1];
     __syncwarp();
     uint8_t *st = st_all + R.st_off;
     GLat G{st, R.NA, R.NB, R.NZ, R.pitch};
@@ -570,7 +604,7 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
             int ax0 = inner ? (lo_a & ~15) : lo_a;         // column of staged byte 0
             int bx0 = Q.b0 - HALO;
             int nrows = WB * WZ;
-            if (lane < (WB_MAX * WMAX + 31) / 32) S.dirty[lane] = 0u;
+            for (int i = lane; i < WB_MAX * WMAX / 4; i += 32) reinterpret_cast<uint32_t *>(S.dirty)[i] = 0u;
             if (inner) {
                 // aligned 16-byte chunks: one or two per row, many in flight per lane
                 int nchunk = ((lo_a - ax0) + WA > 16) ? 2 : 1;
@@ -607,19 +641,19 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
                 }
             }
             __syncwarp();
-            SLat L{S.win, S.dirty, ax0, bx0, zw0, R.NZ};
-            if (!build_list(S, L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ)) {
+            SLat L{ax0, bx0, zw0, R.NZ};
+            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
-            rc = run_events(S, L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
+            rc = run_events(L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
                             window);
             __syncwarp();
             // write back the rows that events changed (tile and its one-column ring)
             for (int r = lane; r < nrows; r += 32) {
                 int ib = r % WB, iz = r / WB;
                 int bit = iz * WB_MAX + ib;               // the row index SLat::put marks
-                if (!((S.dirty[bit >> 5] >> (bit & 31)) & 1u)) continue;
+                if (!S.dirty[bit]) continue;
                 uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
                 const uint8_t *src = &S.win[bit * RS];
                 for (int a = Q.a0 - 1; a < Q.a1 + 1; a++) row[wrapi(a, R.NA)] = src[a - ax0];
@@ -628,12 +662,12 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
         } else {
             // band taller than the staging buffer: run from global memory
             if (lane == 0) atomicAdd(&status->fallback, 1ull);
-            if (!build_list(S, G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0)) {
+            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
             GLat G2 = G;
-            rc = run_events(S, G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag,
+            rc = run_events(G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag,
                             window);
         }
         __syncwarp();
@@ -672,7 +706,7 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
         quads[qid].zlo = zlo;
         quads[qid].zhi = zhi;
         quads[qid].mc = live;
-        if (nev) atomicAdd(&R.events, nev);
+        if (nev) atomicAdd(&Rg.events, nev);
         if (hz_hi >= 0) {
             // widen the z bands of the neighbouring tiles whose sites changed
             for (int k = 0; k < 8; k++) {
@@ -687,12 +721,11 @@ __device__ void process_tile(TileShared &S, RepDev *reps, QuadDev *quads, int qi
 __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
                                                  uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
 {
-    __shared__ TileShared S;
     int qi = blockIdx.x;
     if (qi >= nq) return;
     int qid = qlist[qi];
     const RepDev &R = reps[quads[qid].rep];
-    process_tile(S, reps, quads, qid, st_all, status, phase_tag, R.window, R.T0);
+    process_tile(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0);
 }
 
 // Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
@@ -709,7 +742,6 @@ constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 __global__ void __launch_bounds__(32) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
                                                       DevStatus *status, int *progress, int nwin)
 {
-    __shared__ TileShared S;
     int lane = threadIdx.x & 31;
     for (int P = 0; P < 4 * nwin; P++) {
         int c = P & 3, w = P >> 2;
@@ -734,7 +766,7 @@ __global__ void __launch_bounds__(32) k_sl_persistent(RepDev *reps, QuadDev *qua
             __threadfence();                                // acquire: neighbours' writes before their flag
             if (*(volatile int *)&status->error) return;
             const RepDev &R = reps[quads[t].rep];
-            process_tile(S, reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
+            process_tile(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
                          R.T0 + (double)w * R.tau);
             __threadfence();                                // release: each lane's writes reach L2 ...
             __syncwarp();                                   // ... before lane 0 publishes the flag
@@ -872,7 +904,7 @@ int check_config(const mks_config &c)
     return 0;
 }
 
-// even number of tiles per side, widths within [8, QMAX]
+// even number of tiles per side
 // even number of tiles along a side of n sites, each about `width` wide
 // (at least 4: the write ring of one tile and the read halo of the next
 // same-colour tile must not meet) and at most QMAX
