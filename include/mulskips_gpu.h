@@ -136,6 +136,11 @@ int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n);
 int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events,
             double max_time, int64_t *events_done, double *time_out);
 int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
+/* Sites listed in an output frame, as compact-state indices in the
+ * reference's z, y, x scan order (WriteMolMolXYZFile.f:171-260): kind 0 the
+ * atoms with coordination <= 3, kind 1 the voids.  *n gets the count; the
+ * indices are written when idx is non-NULL and cap >= *n.                  */
+int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int64_t *n);
 int mks_get_observables(mks_handle *h, mks_observables *obs);
 int mks_get_status(mks_handle *h, mks_status *st);
 
@@ -160,6 +165,13 @@ int32_t mks_get_tiling(mks_handle *h);
  * which each tile waits only for its eight neighbours, 0 one launch per
  * colour phase.  Both give the same lattice for the same seed.           */
 int mks_set_schedule(mks_handle *h, int32_t persistent);
+
+/* Window length per replica (n entries): tau = f / r*, r* the rate of the
+ * class carrying the largest share of the replica's total rate.  f = 0.3 is
+ * the largest tested value whose etch rate matches the serial reference
+ * within its 95 % band (no counterpart in the reference, whose loop is
+ * serial).                                                               */
+int mks_suggest_tau(mks_handle *h, double f, double *tau);
 
 /* Launch statistics of the last mks_run / mks_batch_run: kernel launches,
  * graph launches, and the device time (ms) of the sublattice kernels

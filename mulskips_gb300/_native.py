@@ -64,6 +64,7 @@ SIGNATURES = {
     "mks_replay_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_int64, C.c_double,
                           C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "mks_frame_sites": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "mks_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_get_observables": (C.c_int, [C.c_void_p, C.POINTER(MksObservables)]),
     "mks_get_status": (C.c_int, [C.c_void_p, C.POINTER(MksStatus)]),
@@ -77,6 +78,7 @@ SIGNATURES = {
     "mks_set_tiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "mks_get_tiling": (C.c_int32, [C.c_void_p]),
     "mks_set_schedule": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mks_suggest_tau": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
     "mks_last_run_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }

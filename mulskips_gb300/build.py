@@ -44,6 +44,11 @@ def host_cmd(out, lib):
             "-L", os.path.dirname(lib), "-lmulskips_gpu", "-Xlinker", "-rpath=$ORIGIN"]
 
 
+def host_only(out=None):
+    out = out or os.path.join(LIB, "mulskips.e")
+    return _run(host_cmd(out, os.path.join(LIB, "libmulskips_gpu.so")))
+
+
 def build_all(verbose=False):
     os.makedirs(LIB, exist_ok=True)
     lib = os.path.join(LIB, "libmulskips_gpu.so")

@@ -718,7 +718,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     }
 }
 
-__global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
+__global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
                                                  uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
 {
     int qi = blockIdx.x;
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(32) k_sl_phase(RepDev *reps, QuadDev *quads, c
 // colour launches per window in order.
 constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 
-__global__ void __launch_bounds__(32) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
+__global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
                                                       DevStatus *status, int *progress, int nwin)
 {
     int lane = threadIdx.x & 31;
@@ -804,6 +804,76 @@ __global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin)
             R.active = 0;
             R.stop_reason = 3;
         }
+    }
+}
+
+// ---- frame writer support: order-preserving selection of listed sites ----
+// kind 0: atoms with coordination <= 3 (the main I*.xyz list,
+// WriteMolMolXYZFile.f:171-215); kind 1: voids (empty, coordination 4, the
+// O lines and _v.xyz, :216-260).  Sites are visited in layer, row, column
+// order, which is the reference's z, y, x scan order.
+__device__ __forceinline__ bool frame_pick(uint8_t s, int kind)
+{
+    if (s == 0 || s == WALL) return false;
+    if (kind == 0) return sp_of(s) != 0 && co_of(s) <= 3;
+    return sp_of(s) == 0 && co_of(s) == 4;
+}
+
+constexpr int FRAME_CHUNK = 4096;
+
+__global__ void k_frame_count(const RepDev *reps, int rep, const uint8_t *st_all, int kind, unsigned int *counts)
+{
+    const RepDev &R = reps[rep];
+    const uint8_t *st = st_all + R.st_off;
+    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
+    int64_t c0 = (int64_t)blockIdx.x * FRAME_CHUNK;
+    unsigned int cnt = 0;
+    for (int64_t i = c0 + threadIdx.x; i < c0 + FRAME_CHUNK && i < n; i += blockDim.x) {
+        int a = (int)(i % R.NA);
+        int64_t r = i / R.NA;
+        if (frame_pick(st[r * R.pitch + a], kind)) cnt++;
+    }
+    __shared__ unsigned int sh;
+    if (threadIdx.x == 0) sh = 0;
+    __syncthreads();
+    atomicAdd(&sh, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) counts[blockIdx.x] = sh;
+}
+
+// one block per chunk; a block-wide ordered scan writes the compact indices
+__global__ void k_frame_write(const RepDev *reps, int rep, const uint8_t *st_all, int kind,
+                              const unsigned long long *offsets, uint32_t *out)
+{
+    const RepDev &R = reps[rep];
+    const uint8_t *st = st_all + R.st_off;
+    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
+    int64_t c0 = (int64_t)blockIdx.x * FRAME_CHUNK;
+    __shared__ unsigned int warp_tot[32];
+    __shared__ unsigned long long base;
+    if (threadIdx.x == 0) base = offsets[blockIdx.x];
+    __syncthreads();
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t s0 = c0; s0 < c0 + FRAME_CHUNK && s0 < n; s0 += blockDim.x) {
+        int64_t i = s0 + threadIdx.x;
+        bool p = false;
+        if (i < c0 + FRAME_CHUNK && i < n) {
+            int a = (int)(i % R.NA);
+            int64_t r = i / R.NA;
+            p = frame_pick(st[r * R.pitch + a], kind);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, p);
+        if (lane == 0) warp_tot[wid] = __popc(m);
+        __syncthreads();
+        unsigned int before = 0, total = 0;
+        for (int w = 0; w < nw; w++) {
+            if (w < wid) before += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (p) out[base + before + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+        __syncthreads();
+        if (threadIdx.x == 0) base += total;
+        __syncthreads();
     }
 }
 
@@ -1698,6 +1768,82 @@ int mks_set_tiling(mks_handle *h, int32_t width)
 }
 
 int32_t mks_get_tiling(mks_handle *h) { return h ? h->tile_width : 0; }
+
+// tau = f / r*, with r* the rate of the class that carries the largest share
+// of the replica's total rate; f = 0.3 keeps the etch rate of the plain
+// Si(001) model inside the 95 % band of the serial reference at 1000-1200 K
+// (events per event site per window ~ f).
+int mks_suggest_tau(mks_handle *h, double f, double *tau)
+{
+    if (!h || !tau || !(f > 0.0)) return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    unsigned long long *d_hist = nullptr;
+    size_t nb = sizeof(unsigned long long) * NCLASS;
+    CK(cudaMallocAsync(&d_hist, nb * h->reps.size(), h->stream));
+    CK(cudaMemsetAsync(d_hist, 0, nb * h->reps.size(), h->stream));
+    for (size_t i = 0; i < h->reps.size(); i++)
+        k_class_hist<<<256, 256, 0, h->stream>>>(h->d_reps, (int)i, h->d_st, d_hist + i * NCLASS);
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> hist(NCLASS * h->reps.size());
+    CK(cudaMemcpyAsync(hist.data(), d_hist, nb * h->reps.size(), cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_hist, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        double best = 0.0, rstar = 0.0;
+        for (int c = 1; c < NCLASS; c++) {
+            if (c == CLS_ISO || c == CLS_C1D) continue;
+            double w = (double)hist[i * NCLASS + c] * (double)d[i].rate[c];
+            if (w > best) {
+                best = w;
+                rstar = d[i].rate[c];
+            }
+        }
+        tau[i] = rstar > 0.0 ? f / rstar : 1.0;
+    }
+    return 0;
+}
+
+int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int64_t *n_out)
+{
+    if (!h || !n_out || (kind != 0 && kind != 1) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    int64_t nsite = (int64_t)r.NZ * r.NB * r.NA;
+    int nchunk = (int)((nsite + FRAME_CHUNK - 1) / FRAME_CHUNK);
+    unsigned int *d_cnt = nullptr;
+    CK(cudaMallocAsync(&d_cnt, sizeof(unsigned int) * nchunk, h->stream));
+    k_frame_count<<<nchunk, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, kind, d_cnt);
+    CK(cudaGetLastError());
+    std::vector<unsigned int> cnt(nchunk);
+    CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned int) * nchunk, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::vector<unsigned long long> off(nchunk);
+    unsigned long long tot = 0;
+    for (int i = 0; i < nchunk; i++) {
+        off[i] = tot;
+        tot += cnt[i];
+    }
+    *n_out = (int64_t)tot;
+    if (!idx || (int64_t)tot > cap || tot == 0) {
+        cudaFreeAsync(d_cnt, h->stream);
+        CK(cudaStreamSynchronize(h->stream));
+        return 0;
+    }
+    unsigned long long *d_off = nullptr;
+    uint32_t *d_out = nullptr;
+    CK(cudaMallocAsync(&d_off, sizeof(unsigned long long) * nchunk, h->stream));
+    CK(cudaMallocAsync(&d_out, sizeof(uint32_t) * tot, h->stream));
+    CK(cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nchunk, cudaMemcpyHostToDevice, h->stream));
+    k_frame_write<<<nchunk, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, kind, d_off, d_out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(idx, d_out, sizeof(uint32_t) * tot, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_cnt, h->stream);
+    cudaFreeAsync(d_off, h->stream);
+    cudaFreeAsync(d_out, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
 
 int mks_set_schedule(mks_handle *h, int32_t persistent)
 {

@@ -141,6 +141,11 @@ class Lattice:
     def set_schedule(self, persistent):
         N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
 
+    def suggest_tau(self, f=0.3):
+        t = np.zeros(1)
+        N.check(N.lib().mks_suggest_tau(self._h, float(f), N.ptr(t)))
+        return float(t[0])
+
     def run_stats(self):
         k, g, p = C.c_int64(), C.c_int64(), C.c_int64()
         ms = C.c_double()
@@ -194,6 +199,11 @@ class Batch:
 
     def set_schedule(self, persistent):
         N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
+
+    def suggest_tau(self, f=0.3):
+        t = np.zeros(self.n)
+        N.check(N.lib().mks_suggest_tau(self._h, float(f), N.ptr(t)))
+        return t
 
     def observables(self):
         o = (N.MksObservables * self.n)()

@@ -1,0 +1,440 @@
+// mulskips.e — drop-in replacement of the reference executable, driving the
+// GB300 engine through the C ABI (include/mulskips_gpu.h).
+//
+// Like the reference program (mulskips-source/main.f) it reads ./start.dat,
+// builds the initial lattice, runs the KMC loop to the exit condition and
+// writes the I%08d.xyz / _d.xyz / _v.xyz / .src frames and movie.mos in the
+// current directory, printing the same progress lines (pymulskips greps
+// "few MC particles: stop MC", pymulskips/setuprun.py:429-434).
+//
+// The reference fixes the box at compile time (LenX/LenY/LenZ PARAMETER,
+// mulskips-source/modules/defsystem.f:27, rewritten by
+// pymulskips/setuprun.py:499-521).  Here the box is read at run time from
+// mulskips_box.dat next to this executable ("LenX LenY LenZ"), else from the
+// MULSKIPS_BOX environment variable, else 480 480 480.
+//
+// The loop is the synchronous-sublattice engine: events are counted per
+// window, so the Iter exit and the frame schedule are met at the first window
+// boundary at or after the requested event count.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <string>
+#include <vector>
+#include <unistd.h>
+#include <limits.h>
+
+#include "mulskips_gpu.h"
+
+namespace {
+
+struct Input {
+    int ncrystal = 1, ncov = 0;
+    int list_crystal[3] = {14, 0, 0};
+    int list_cov[3] = {0, 0, 0};
+    std::string init_st;
+    int len[4] = {120, 120, 120, 120};
+    double alloy = 0.0, ptrans_zig = 1.0, sf = 0.4525;
+    std::string exit_strategy = "Iter";
+    long long max_iter = 2100000000LL, out_molmol = 100000000LL;
+    double max_time = 1e8, out_time = 1e7;
+    std::string run_type = "R";
+    long long idum = 9117116;
+    std::string save_final = "F", restart_file, save_coo = "F", coo_file;
+    std::vector<double> pE = std::vector<double>(3 * 4096, 0.0);
+    std::vector<double> pD = std::vector<double>(9, 0.0);
+};
+
+[[noreturn]] void die(const char *msg)
+{
+    printf(" %s\n", msg);
+    fflush(stdout);
+    exit(1);
+}
+
+// positional list-directed records of start.dat (main.f:83-212)
+struct Records {
+    FILE *f;
+    std::vector<std::string> toks;
+    explicit Records(FILE *fp) : f(fp) {}
+    bool line(std::string &out)
+    {
+        char buf[8192];
+        if (!fgets(buf, sizeof buf, f)) return false;
+        out = buf;
+        while (!out.empty() && (out.back() == '\n' || out.back() == '\r')) out.pop_back();
+        return true;
+    }
+    std::vector<std::string> items(int n)
+    {
+        std::vector<std::string> r;
+        std::string l;
+        if (!line(l)) die("start.dat: unexpected end of file");
+        toks.clear();
+        auto split = [&](const std::string &s) {
+            size_t i = 0;
+            while (i < s.size()) {
+                while (i < s.size() && (isspace((unsigned char)s[i]) || s[i] == ',')) i++;
+                size_t j = i;
+                while (j < s.size() && !isspace((unsigned char)s[j]) && s[j] != ',') j++;
+                if (j > i) toks.push_back(s.substr(i, j - i));
+                i = j;
+            }
+        };
+        split(l);
+        size_t k = 0;
+        while ((int)r.size() < n) {
+            if (k >= toks.size()) {
+                if (!line(l)) die("start.dat: unexpected end of file");
+                toks.clear();
+                k = 0;
+                split(l);
+                continue;
+            }
+            r.push_back(toks[k++]);
+        }
+        return r;
+    }
+};
+
+double real_of(std::string s)
+{
+    for (auto &c : s)
+        if (c == 'd' || c == 'D') c = 'e';
+    return strtod(s.c_str(), nullptr);
+}
+
+Input read_startdat(const char *path)
+{
+    Input in;
+    FILE *f = fopen(path, "r");
+    if (!f) die("cannot open start.dat");
+    Records r(f);
+    auto it = r.items(2);
+    in.ncrystal = atoi(it[0].c_str());
+    in.ncov = atoi(it[1].c_str());
+    if (in.ncrystal < 1 || in.ncrystal > 3) die("ERR NOT IMPLEMENTED: NCrystal must be <= 3");
+    it = r.items(in.ncrystal);
+    for (int i = 0; i < in.ncrystal; i++) in.list_crystal[i] = atoi(it[i].c_str());
+    if (in.ncov > 0) {
+        it = r.items(in.ncov);
+        for (int i = 0; i < in.ncov; i++) in.list_cov[i] = atoi(it[i].c_str());
+    }
+    in.init_st = r.items(1)[0].substr(0, 2);
+    if (in.init_st == "FF") {
+        it = r.items(4);
+        for (int i = 0; i < 4; i++) in.len[i] = atoi(it[i].c_str());
+    } else if (in.init_st == "IN" || in.init_st == "SH" || in.init_st == "LA" || in.init_st == "ST") {
+        die("initialization not_implemented in the GPU engine (FS and F are)");
+    } else {
+        it = r.items(3);
+        for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
+    }
+    bool sige = in.ncrystal >= 2 && in.list_crystal[0] == 14 && in.list_crystal[1] == 32 &&
+                (in.ncrystal == 2 || in.list_crystal[2] == 5);
+    if (sige) in.alloy = real_of(r.items(1)[0]);
+    in.ptrans_zig = real_of(r.items(1)[0]);
+    in.sf = real_of(r.items(1)[0]);
+    in.exit_strategy = r.items(1)[0].substr(0, 4);
+    if (in.exit_strategy == "Iter") {
+        in.max_iter = atoll(r.items(1)[0].c_str());
+        in.out_molmol = atoll(r.items(1)[0].c_str());
+    } else if (in.exit_strategy == "Time") {
+        in.max_time = real_of(r.items(1)[0]);
+        in.out_time = real_of(r.items(1)[0]);
+    }
+    in.run_type = r.items(1)[0].substr(0, 2);
+    in.idum = atoll(r.items(1)[0].c_str());
+    in.save_final = r.items(1)[0].substr(0, 2);
+    if (in.save_final == "T") r.line(in.restart_file);
+    in.save_coo = r.items(1)[0].substr(0, 2);
+    if (in.save_coo == "T") r.line(in.coo_file);
+    // SetProbability.f:21-143
+    static const int maxe[4][4] = {{0, 3, 18, 57}, {0, 9, 50, 150}, {0, 19, 100, 288}, {0, 34, 172, 480}};
+    int ne = maxe[in.ncov < 4 ? in.ncov : 0][in.ncrystal];
+    printf(" maxElines %d\n", ne);
+    for (int i = 0; i < ne; i++) {
+        it = r.items(3);
+        int s = atoi(it[0].c_str());
+        long el = atol(it[1].c_str());
+        if (s < 1 || s > in.ncrystal) die("ERROR: 1st index in evap prob must be <= NCrystal");
+        int idx[6] = {0, 0, 0, 0, 0, 0};
+        int nd = in.ncrystal + in.ncov;
+        for (int j = 1; j <= in.ncrystal; j++) {
+            long p = 1;
+            for (int q = 0; q < nd - j; q++) p *= 10;
+            idx[j - 1] = (int)((el / p) % 10);
+        }
+        for (int j = in.ncrystal + 1; j <= nd; j++) {
+            long p = 1;
+            for (int q = 0; q < nd - j; q++) p *= 10;
+            idx[3 + j - in.ncrystal - 1] = (int)((el / p) % 10);
+        }
+        int k = (s - 1) * 4096 + idx[0] * 1024 + idx[1] * 256 + idx[2] * 64 + idx[3] * 16 + idx[4] * 4 + idx[5];
+        in.pE[k] = real_of(it[2]);
+    }
+    for (int j = 0; j < in.ncrystal * 3; j++) {
+        it = r.items(3);
+        int s = atoi(it[0].c_str()), el = atoi(it[1].c_str());
+        if (s < 1 || s > in.ncrystal || el < 1 || el > 3) die("ERROR: 1st index in depo prob block must be <= NCrystal");
+        in.pD[(s - 1) * 3 + el - 1] = real_of(it[2]);
+    }
+    fclose(f);
+    return in;
+}
+
+void box_size(int &lx, int &ly, int &lz)
+{
+    lx = ly = lz = 480;
+    char exe[PATH_MAX];
+    ssize_t n = readlink("/proc/self/exe", exe, sizeof exe - 1);
+    if (n > 0) {
+        exe[n] = 0;
+        std::string d(exe);
+        d = d.substr(0, d.rfind('/'));
+        FILE *f = fopen((d + "/mulskips_box.dat").c_str(), "r");
+        if (f) {
+            if (fscanf(f, "%d %d %d", &lx, &ly, &lz) != 3) lx = ly = lz = 480;
+            fclose(f);
+            return;
+        }
+    }
+    const char *e = getenv("MULSKIPS_BOX");
+    if (e) sscanf(e, "%d %d %d", &lx, &ly, &lz);
+}
+
+void check(int rc)
+{
+    if (rc) {
+        char buf[512];
+        mks_last_error(buf, sizeof buf);
+        printf(" ERROR (code %d): %s\n", rc, buf);
+        fflush(stdout);
+        exit(1);
+    }
+}
+
+// Fortran Ew.d
+std::string fmt_e(double v, int w, int d)
+{
+    char b[64], m[64];
+    if (v == 0.0) {
+        snprintf(b, sizeof b, "0.%0*dE+00", d, 0);
+    } else {
+        snprintf(m, sizeof m, "%.*e", d - 1, fabs(v));
+        std::string digits;
+        const char *p = m;
+        digits += *p++;
+        if (*p == '.') p++;
+        while (*p && *p != 'e') digits += *p++;
+        int ex = atoi(p + 1) + 1;
+        snprintf(b, sizeof b, "%s0.%sE%c%02d", v < 0 ? "-" : "", digits.c_str(), ex < 0 ? '-' : '+', abs(ex));
+    }
+    char out[64];
+    snprintf(out, sizeof out, "%*s", w, b);
+    return out;
+}
+
+struct Frames {
+    mks_handle *h;
+    const Input &in;
+    int lx, ly, lz;
+    int na, nb;
+
+    const char *symbol(int sp) const
+    {
+        if (sp == 1) return "Si";
+        int z = in.list_crystal[sp - 1];
+        if (z == 6) return "C";
+        if (z == 32) return "Ge";
+        if (z == 5) return "B";
+        return "X";
+    }
+    std::string name(long long iout) const
+    {   // GetOutputFileName.f:22-81: first 8 of the 9 digits of 10*Iout
+        char d[32];
+        snprintf(d, sizeof d, "%09lld", iout * 10);
+        return std::string("I") + std::string(d, 8);
+    }
+    void xyz(int64_t i, double &x, double &y, double &z) const
+    {
+        int a = (int)(i % na);
+        int64_t r = i / na;
+        int b = (int)(r % nb), z1 = (int)(r / nb);
+        x = in.sf * 3.0 * (2 * a + (z1 & 1));
+        y = in.sf * 3.0 * (2 * b + (z1 & 1));
+        z = in.sf * 3.0 * z1;
+    }
+    void write(double time, long long iter, long long iout)
+    {   // WriteMolMolSource.f:22-112, WriteMolMolXYZFile.f:22-406
+        std::string base = name(iout);
+        printf(" %s\n", base.c_str());
+        std::vector<uint32_t> at, vd;
+        std::vector<uint8_t> st((size_t)mks_state_size(h));
+        int64_t n0 = 0, n1 = 0;
+        check(mks_frame_sites(h, 0, nullptr, 0, &n0));
+        check(mks_frame_sites(h, 1, nullptr, 0, &n1));
+        at.resize((size_t)n0);
+        vd.resize((size_t)n1);
+        if (n0) check(mks_frame_sites(h, 0, at.data(), n0, &n0));
+        if (n1) check(mks_frame_sites(h, 1, vd.data(), n1, &n1));
+        check(mks_get_state(h, st.data(), (int64_t)st.size()));
+        std::string per = " periodic " + fmt_e(in.sf * lx, 15, 8) + " " + fmt_e(in.sf * ly, 15, 8) + " " +
+                          fmt_e(in.sf * lz, 15, 8) + "\n";
+        char hdr[256];
+        FILE *f = fopen((base + ".xyz").c_str(), "w");
+        snprintf(hdr, sizeof hdr, " %8lld angstroem KMC-time: %s Iter: %12lld\n", (long long)(n0 + n1),
+                 fmt_e(time, 15, 8).c_str(), iter);
+        fputs(hdr, f);
+        fputs(per.c_str(), f);
+        for (uint32_t i : at) {
+            double x, y, z;
+            xyz(i, x, y, z);
+            fprintf(f, "%s %10.5f %10.5f %10.5f  \n", symbol(st[i] & 3), x, y, z);
+        }
+        for (uint32_t i : vd) {
+            double x, y, z;
+            xyz(i, x, y, z);
+            fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
+        }
+        fclose(f);
+        // cubic stacking only: no non-epitaxial bulk atoms
+        f = fopen((base + "_d.xyz").c_str(), "w");
+        snprintf(hdr, sizeof hdr, " %8d angstroem KMC-time: %s Iter: %12lld\n", 0, fmt_e(time, 15, 8).c_str(), iter);
+        fputs(hdr, f);
+        fputs(per.c_str(), f);
+        fclose(f);
+        f = fopen((base + "_v.xyz").c_str(), "w");
+        fprintf(f, " %8lld angstroem\n", (long long)n1);
+        fputs(per.c_str(), f);
+        for (uint32_t i : vd) {
+            double x, y, z;
+            xyz(i, x, y, z);
+            fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
+        }
+        fclose(f);
+        f = fopen((base + ".src").c_str(), "w");
+        fprintf(f, " load xyz %s.xyz\n color temperature\n set background white\n set boundbox true\n zoom 140\n"
+                   " rotate x 41\n rotate y 4\n spacefill 2\n color axes black\n wireframe 2\n color atom green\n"
+                   " wireframe 12\n color atom purple\n set bondmode and\n",
+                base.c_str());
+        fclose(f);
+        f = fopen("movie.mos", "a");
+        fprintf(f, " source    %s.src\n write gif %s.gif\n zap\n", base.c_str(), base.c_str());
+        fclose(f);
+    }
+};
+
+}  // namespace
+
+int main()
+{
+    int lx, ly, lz;
+    box_size(lx, ly, lz);
+    printf(" KMC box size: %d %d %d\n", lx, ly, lz);
+    Input in = read_startdat("start.dat");
+    printf(" Crystal species (NCrystal= %d ) --> Z: %d %d %d\n", in.ncrystal, in.list_crystal[0], in.list_crystal[1],
+           in.list_crystal[2]);
+    printf(" KMC Super-Lattice parameter (ang): %.17g\n", in.sf);
+    printf(" Exit strategy: %s\n", in.exit_strategy.c_str());
+    printf(" IDUM %lld\n", in.idum);
+    if (in.ncov > 0) die("ERR NOT IMPLEMENTED: coverage species are not in the GPU engine");
+    if (in.init_st != "FS" && in.init_st != "F") die("initialization not_implemented");
+    mks_config cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.lenx = lx;
+    cfg.leny = ly;
+    cfg.lenz = lz;
+    cfg.ncrystal = in.ncrystal;
+    cfg.ncov = 0;
+    for (int i = 0; i < 3; i++) cfg.list_crystal[i] = in.list_crystal[i];
+    cfg.ptrans_zig = in.ptrans_zig;
+    cfg.sf = in.sf;
+    cfg.seed = (uint64_t)in.idum;
+    mks_handle *h = nullptr;
+    check(mks_create(&cfg, &h));
+    check(mks_set_rates(h, in.pE.data(), in.pD.data()));
+    int len1 = in.len[0] - in.len[0] % 24;
+    check(mks_init_flat(h, in.init_st == "FS" ? 'S' : 'C', len1));
+    mks_observables ob;
+    check(mks_get_observables(h, &ob));
+    printf(" Atoms,Voids,AdAtoms %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,
+           (long long)ob.mc_sites);
+    Frames fr{h, in, lx, ly, lz, lx / 6, ly / 6};
+    fr.write(0.0, 0, 0);
+    bool iter_mode = in.exit_strategy == "Iter";
+    long long frame = 0, events = 0;
+    double time = 0.0, tau = 0.0;
+    int chunk = 16;
+    bool few = false;
+    for (long long block = 0;; block++) {
+        if (block % 4 == 0) check(mks_suggest_tau(h, 0.3, &tau));
+        int64_t ev = 0;
+        check(mks_run(h, tau, chunk, 0, 0.0, &ev, &time));
+        events += ev;
+        mks_status st;
+        check(mks_get_status(h, &st));
+        if (st.stop_reason == 1) {
+            check(mks_get_observables(h, &ob));
+            printf(" few MC particles: stop MC %lld %lld\n", events, (long long)ob.mc_sites);
+            few = true;
+            break;
+        }
+        if (iter_mode) {
+            while (in.out_molmol > 0 && events >= (frame + 1) * in.out_molmol && events < in.max_iter) {
+                frame++;
+                fr.write(time, events, frame);
+                check(mks_get_observables(h, &ob));
+                printf(" Iter, Time %lld %.17g\n", events, time);
+                printf(" NatNvoidNad %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,
+                       (long long)ob.mc_sites);
+            }
+            if (events >= in.max_iter) break;
+        } else {
+            while (time >= (frame + 1) * in.out_time && time <= in.max_time) {
+                frame++;
+                fr.write(time, events, frame);
+                printf(" Iter, Time %lld %.17g\n", events, time);
+            }
+            if (time > in.max_time) break;
+        }
+    }
+    if (iter_mode)
+        fr.write(time, events, in.out_molmol > 0 ? events / in.out_molmol : 0);
+    else
+        fr.write(time, events, frame);
+    check(mks_get_observables(h, &ob));
+    printf(" Iter, Time %lld %.17g\n", events, time);
+    printf(" NatNvoidNad %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,
+           (long long)ob.mc_sites);
+    if (in.save_final == "T" || in.save_coo == "T") {
+        std::vector<int32_t> lc((size_t)lx * ly * (lz + 1));
+        check(mks_get_lattice(h, lc.data()));
+        if (in.save_final == "T") {   // main.f:385-403, one plane per record
+            FILE *f = fopen(in.restart_file.c_str(), "w");
+            for (int z = 0; z < lz; z++) {
+                for (size_t k = 0; k < (size_t)lx * ly; k++) fprintf(f, " %d", lc[(size_t)lx * ly * z + k]);
+                fputc('\n', f);
+            }
+            fclose(f);
+        }
+        if (in.save_coo == "T") {     // main.f:407-430, FORMAT(500000I4)
+            FILE *f = fopen(in.coo_file.c_str(), "w");
+            for (int z = 0; z < lz; z++) {
+                for (size_t k = 0; k < (size_t)lx * ly; k++) {
+                    int32_t v = lc[(size_t)lx * ly * z + k];
+                    int out = 0;
+                    if ((v & 255) == 113) out = 10;
+                    else if ((v >> 23) & 1) out = (v >> 24) & 7;
+                    fprintf(f, "%4d", out);
+                }
+                fputc('\n', f);
+            }
+            fclose(f);
+        }
+    }
+    mks_destroy(h);
+    (void)few;
+    return 0;
+}

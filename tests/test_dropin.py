@@ -1,0 +1,71 @@
+"""Drop-in boundary on the CPU: start.dat written by mulskips_gb300.setuprun
+matches, record by record, the one the reference's own
+pymulskips.setuprun.run_mulskips writes for the same process object; the
+reader agrees with the oracle's parser; setup_mulskips_src leaves the
+make.log line the reference checks."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+REF = os.environ.get("MULSKIPS_REF", "/root/reference")
+
+
+def first_tokens(path):
+    out = []
+    for line in open(path):
+        toks = line.split("!")[0].split()
+        out.append(toks)
+    return out
+
+
+def test_startdat_matches_reference_writer(tmp_path):
+    if not os.path.isdir(os.path.join(REF, "pymulskips")):
+        pytest.skip("reference pymulskips not present")
+    sys.path.insert(0, REF)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import pymulskips.setuprun as ref_setup
+    from mulskips_gb300.setuprun import PlainSi, run_mulskips
+
+    class PVD(PlainSi):    # the reference dispatches on the class name
+        pass
+
+    mp = PVD(T=1100.0)
+    cwd = os.getcwd()
+    try:
+        ref_setup.run_mulskips(execpath=str(tmp_path), runpath=str(tmp_path / "ref"), Simulation="FS", mp=mp,
+                               PtransZig=1.0, ExitStrategy="Iter", OutMolMol=1000, IterMax=100000,
+                               Seed_box=[120, 120, 120], RunType="R", IDUM=5, setup_only=True)
+    finally:
+        os.chdir(cwd)
+    run_mulskips(runpath=str(tmp_path / "ours"), Simulation="FS", mp=mp, PtransZig=1.0, ExitStrategy="Iter",
+                 OutMolMol=1000, IterMax=100000, Seed_box=[120, 120, 120], RunType="R", IDUM=5, setup_only=True)
+    a = first_tokens(tmp_path / "ref" / "start.dat")
+    b = first_tokens(tmp_path / "ours" / "start.dat")
+    assert a == b
+
+
+def test_reader_agrees_with_oracle(oracle_lib):
+    from mulskips_gb300.startdat import parse_startdat
+    for case in ("Si-SL", "surface"):
+        p = os.path.join(GOLDEN, case, "start.dat")
+        d = parse_startdat(p)
+        o = oracle_lib.Oracle(p, 480, 480, 480)
+        pE, pD = o.rates()
+        o.close()
+        assert np.array_equal(pE, d["ptransE"]) and np.array_equal(pD, d["ptransD"])
+
+
+def test_setup_src_writes_box_and_make_log(tmp_path):
+    from mulskips_gb300.setuprun import setup_mulskips_src
+    (tmp_path / "mulskips.e").write_text("")
+    assert setup_mulskips_src(str(tmp_path), 240, 240, 480)
+    assert open(tmp_path / "mulskips_box.dat").read().split() == ["240", "240", "480"]
+    assert "Compilation terminated" in open(tmp_path / "make.log").read()
+    with pytest.raises(ValueError):
+        setup_mulskips_src(str(tmp_path), 100, 240, 480)

@@ -1,0 +1,59 @@
+"""The drop-in mulskips.e (C++ host over the C ABI) on a GB300: reads the
+reference's start.dat, writes the reference's frame files.  The initial
+frame is deterministic and must equal the reference's I00000000.xyz byte for
+byte; the run then follows the GPU engine's own dynamics."""
+import gzip
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+pytestmark = pytest.mark.gpu
+EXE = os.path.join(ROOT, "mulskips_gb300", "_lib", "mulskips.e")
+
+
+def run_exe(d, box="480 480 480"):
+    env = dict(os.environ, MULSKIPS_BOX=box)
+    r = subprocess.run([EXE], cwd=d, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    return r
+
+
+def test_initial_frame_identical_and_run_completes(tmp_path):
+    """Si-SL start.dat with the exit moved to 200000 events (the frame names
+    follow Iter/OutMolMol as in the reference, so a run that stops early
+    overwrites I00000000 with its final frame, like the reference)."""
+    d = tmp_path / "si"
+    d.mkdir()
+    txt = open(os.path.join(GOLDEN, "Si-SL", "start.dat")).read()
+    txt = txt.replace("10000000 ! IterMax", "200000 ! IterMax").replace("10000000  ! OutMolMol", "200000  ! OutMolMol")
+    (d / "start.dat").write_text(txt)
+    r = run_exe(d)
+    assert r.returncode == 0, r.stdout[-3000:]
+    with gzip.open(os.path.join(GOLDEN, "Si-SL", "I00000000.xyz.gz"), "rb") as f:
+        gold = f.read()
+    assert (d / "I00000000.xyz").read_bytes() == gold
+    hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
+    assert hdr[1] == "angstroem" and int(hdr[-1]) >= 200000
+    assert "NatNvoidNad" in r.stdout and "Atoms,Voids,AdAtoms" in r.stdout
+    for name in ("I00000000_d.xyz", "I00000000_v.xyz", "I00000000.src", "movie.mos"):
+        assert (d / name).exists()
+
+
+def test_run_mulskips_wrapper_etch_stop(tmp_path):
+    """pymulskips-style call; at 1100 K the slab etches away and the run ends
+    on the few-MC-particles rule, which run_mulskips reports as False."""
+    from mulskips_gb300.setuprun import PlainSi, run_mulskips
+    os.environ["MULSKIPS_BOX"] = "240 240 240"
+    try:
+        ok = run_mulskips(runpath=str(tmp_path / "run"), Simulation="FS", mp=PlainSi(T=1100.0),
+                          ExitStrategy="Iter", OutMolMol=4000, IterMax=10 ** 8, Seed_box=[72, 72, 72])
+    finally:
+        del os.environ["MULSKIPS_BOX"]
+    assert ok is False
+    log = open(tmp_path / "run" / "log.txt").read()
+    assert "few MC particles: stop MC" in log
+    assert (tmp_path / "run" / "I00000001.xyz").exists()

@@ -66,3 +66,38 @@ def test_etch_rate_matches_serial_reference(oracle_sample, tau):
           f"+-{oracle_sample.std(ddof=1):.1f}  diff {d:.1f}  95% band +-{hw:.1f}")
     assert g.mean() < start and oracle_sample.mean() < start       # etching happened
     assert abs(d) <= hw, f"etch-rate difference {d:.1f} atoms outside the 95% band {hw:.1f}"
+
+
+def test_deposition_evaporation_regime_matches_serial_reference(oracle_lib, tmp_path):
+    """The Si-SL regression rates with RunType R (deposition 9.3e-4 against
+    coor-2 evaporation 2.0e-3, so both event kinds matter): atoms left at
+    t = 1e4 s, 16 oracle seeds against 16 GPU replicas at the autotuned tau."""
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.startdat import parse_startdat
+    from conftest import GOLDEN
+    txt = open(os.path.join(GOLDEN, "Si-SL", "start.dat")).read().replace("T   ! R = production run",
+                                                                            "R   ! R = production run")
+    ref = []
+    for s in range(16):
+        p = tmp_path / f"sl{s}.dat"
+        p.write_text(txt.replace("9117116 ! Random seed", f"{200 + s} ! Random seed"))
+        o = oracle_lib.Oracle(str(p), 480, 480, 480, numbers=None)
+        o.init()
+        o.run_until(1e4)
+        ref.append(o.atoms())
+        o.close()
+    ref = np.array(ref, float)
+    d = parse_startdat(str(tmp_path / "sl0.dat"))
+    n = 16
+    b = Batch([(480, 480, 480)] * n, seeds=[31 + s for s in range(n)], sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
+    b.init_flat("S", [360] * n)
+    tau = float(b.suggest_tau(0.3)[0])
+    nwin = int(round(1e4 / tau))
+    b.run(1e4 / nwin, nwin)
+    g = np.array([o["atoms"] for o in b.observables()], float)
+    b.close()
+    diff, hw = band(g, ref)
+    print(f"Si-SL rates: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f} serial {ref.mean():.1f}+-{ref.std(ddof=1):.1f} "
+          f"diff {diff:.1f} 95% band +-{hw:.1f}")
+    assert abs(diff) <= hw
