@@ -93,7 +93,8 @@ typedef struct {
     int64_t fallback_tiles;        /* tiles run from global memory               */
     int64_t windows;               /* sublattice windows completed               */
     int32_t active;                /* 1 while the replica still runs             */
-    int32_t stop_reason;           /* 0 running, 1 few MC sites, 2 max events, 3 max time */
+    int32_t stop_reason;           /* 0 running, 1 few MC sites, 2 max events, 3 max time,
+                                      4 regrown (LA mode) */
 } mks_status;
 
 /* ---- plain (single-replica) interface ---- */
@@ -172,6 +173,46 @@ int mks_set_schedule(mks_handle *h, int32_t persistent);
  * within its 95 % band (no counterpart in the reference, whose loop is
  * serial).                                                               */
 int mks_suggest_tau(mks_handle *h, double f, double *tau);
+
+/* ---- laser-anneal rate law and barrier gradients ---- */
+/* LA mode (mulskips-source/mcevent/Get_Prob.f:127-149 and
+ * mulskips-source-LaserAnnealing/mcevent/Get_Prob.f:127-152): after this
+ * call the PTransE / PTransD tables given to mks_batch_set_rates are barriers
+ * in eV.  Melting of an atom: P0(s) exp(-E / kB T); solidification of species
+ * s on a liquid site of coordination n: 0.5 P0(s) xliq(s) exp(-Ed(s,n) / kB
+ * Tm(s)) (1 + erf((T - Tflex(s)) / sigma(s))), xliq(s) the fraction of the
+ * molten atoms that are of species s (CountLiquid / SUM(CountLiquid),
+ * LaserAnnealing main.f:637; the atoms present at this call count as solid),
+ * refreshed every 8 windows.  A replica stops (stop reason 4) once it holds
+ * more atoms than at this call (LaserAnnealing main.f:714-723).  T is the prescribed field
+ * T(z,t) = Tb + Ta exp(-((t-t0)/w)^2) exp(-depth/L), depth = max(0, (zsurf -
+ * z) sf / 10) nm, in integer K, evaluated per layer at each window's midpoint.
+ * With score != 0 each replica accumulates (FP64) the likelihood-ratio score
+ * sum_events d log k / d theta - int d R_tot / d theta dt for four
+ * parameters theta, given dptransE (n*3*4096*4, d PTransE / d theta in the
+ * PTransE layout) and dptransD (n*9*4).  No counterpart in the reference
+ * (which has no derivatives); exponential waiting times are used.          */
+typedef struct {
+    float P0[3], Tm[3], Tflex[3], sigma[3];
+    float Tb, Ta, t0, w;
+    float L_nm, zsurf;
+    int32_t score;
+} mks_la_params;
+int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptransE, const double *dptransD);
+int mks_batch_get_score(mks_handle *h, double *score, int32_t reset);
+/* LA mode: crystal atoms per species (n*3) and the liquid fractions in use
+ * (n*3, may be NULL).  Replaces the CountCrystal / CountLiquid report of
+ * LaserAnnealing inpout/WriteMolMolSource.f:44-49.                        */
+int mks_batch_la_counts(mks_handle *h, int64_t *crystal, double *xliq);
+/* Backward step of the score: from one value f[i] per replica (host, n) the
+ * likelihood-ratio gradient of E[f], grad[j] = mean_i (f_i - b_i) S_ij with
+ * S the FP64 scores accumulated since the last reset and b_i the mean of the
+ * other replicas' f (use_baseline != 0) or 0; se[j] (may be NULL) is its
+ * standard error.  No counterpart in the reference.                      */
+int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, double *grad, double *se);
+/* SetSi-like slab with species 2 substituted on each atom with probability
+ * x[i] (SetSiGex.f places Ge with the compiler's RAND(); here Philox).     */
+int mks_batch_init_alloy(mks_handle *h, const int32_t *len1, const double *x, uint64_t seed);
 
 /* Launch statistics of the last mks_run / mks_batch_run: kernel launches,
  * graph launches, and the device time (ms) of the sublattice kernels

@@ -42,6 +42,12 @@ class MksObservables(C.Structure):
         return d
 
 
+class MksLaParams(C.Structure):
+    _fields_ = [("P0", C.c_float * 3), ("Tm", C.c_float * 3), ("Tflex", C.c_float * 3), ("sigma", C.c_float * 3),
+                ("Tb", C.c_float), ("Ta", C.c_float), ("t0", C.c_float), ("w", C.c_float), ("L_nm", C.c_float),
+                ("zsurf", C.c_float), ("score", C.c_int32)]
+
+
 class MksStatus(C.Structure):
     _fields_ = [("error", C.c_int32), ("pending_tiles", C.c_int32), ("fallback_tiles", C.c_int64),
                 ("windows", C.c_int64), ("active", C.c_int32), ("stop_reason", C.c_int32)]
@@ -79,6 +85,11 @@ SIGNATURES = {
     "mks_get_tiling": (C.c_int32, [C.c_void_p]),
     "mks_set_schedule": (C.c_int, [C.c_void_p, C.c_int32]),
     "mks_suggest_tau": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
+    "mks_batch_set_la": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mks_batch_get_score": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "mks_batch_la_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "mks_batch_init_alloy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "mks_last_run_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }

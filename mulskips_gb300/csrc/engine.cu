@@ -73,6 +73,83 @@ struct QuadDev {
     int nbr[8];              // the eight neighbouring tiles (periodic)
 };
 
+// Laser-anneal rate law of the reference (mulskips-source/mcevent/Get_Prob.f:
+// 127-149): the PTransE / PTransD tables hold barriers in eV and the rates
+// follow the site temperature.  Melting of an atom of class c:
+//   P0(s) exp(-E_c / kB T); solidification of species s on a liquid (empty)
+// site of coordination n: 0.5 P0(s) exp(-Ed(s,n) / kB Tm(s)) (1 + erf((T -
+// Tflex(s)) / sigma(s))); a zero barrier means no such event.  The
+// temperature is the prescribed field T(z,t) = Tb + Ta exp(-((t-t0)/w)^2)
+// exp(-depth/L), depth = max(0, (zsurf - z) sf / 10) nm, rounded to integer K
+// as LattCoo bits 9-21 store it, evaluated at the window's midpoint.
+struct LADev {
+    // crystal atoms per species: init_cnt at mks_batch_set_la, cnt updated by
+    // the tiles (atomics); the liquid of species s is init_cnt[s] - cnt[s]
+    // (CountLiquid = InitCountCrystal - CountCrystal, LaserAnnealing
+    // main.f:637) and xliq its fraction, refreshed every LA_PHASE windows
+    long long init_cnt[3];
+    long long cnt[3];
+    float xliq[3];
+    int on, score_on, pad0;
+    float P0[3], Tm[3], Tflex[3], sigma[3];
+    float E[64];             // melting barrier of each occupied class
+    float dE[64][4];         // d E / d theta
+    float Edep[3][3];        // solidification barrier [species][coordination-1]
+    float dEdep[3][3][4];
+    float Tb, Ta, t0, w;
+    float L, zsurf, sf, pad2;
+};
+
+constexpr float KB_EV_F = 8.617330350e-5f;   // Get_Prob.f:70
+constexpr int LA_PHASE = 8;                  // windows between liquid-fraction refreshes
+
+__device__ __forceinline__ float la_temp(const LADev &A, int z1, double t)
+{
+    float depth = fmaxf(0.f, (A.zsurf - 3.f * (float)z1) * A.sf * 0.1f);
+    float g = (float)((t - (double)A.t0) / (double)A.w);
+    return rintf(A.Tb + A.Ta * __expf(-g * g) * __expf(-depth / A.L));
+}
+__device__ __forceinline__ float la_dep(const LADev &A, int s, int co, float T)
+{
+    // LaserAnnealing Get_Prob.f:147-151: weighted by the liquid fraction of s
+    float E = A.Edep[s][co - 1];
+    if (E == 0.f || !(A.xliq[s] > 0.f)) return 0.f;
+    return 0.5f * A.P0[s] * A.xliq[s] * __expf(-E / (KB_EV_F * A.Tm[s])) *
+           (1.f + erff((T - A.Tflex[s]) / A.sigma[s]));
+}
+__device__ __forceinline__ int la_coor(int c) { return c == CLS_C3 ? 3 : (c == CLS_C2 ? 2 : 1); }
+// rate of one site of class c at temperature T
+__device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
+{
+    if (c >= CLS_OCC0) {
+        float E = A.E[c];
+        return E != 0.f ? A.P0[(c - CLS_OCC0) / NCENSUS] * __expf(-E / (KB_EV_F * T)) : 0.f;
+    }
+    if (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) {
+        int co = la_coor(c);
+        return la_dep(A, 0, co, T) + la_dep(A, 1, co, T) + la_dep(A, 2, co, T);
+    }
+    if (c == CLS_C1D) return 1.e-8f;
+    return 0.f;
+}
+// d(rate)/d theta_j of one site of class c at temperature T (isolated atoms,
+// whose rate is a numerical device of the reference, are left out)
+__device__ __forceinline__ void la_drate(const LADev &A, int c, float T, float d[4])
+{
+    d[0] = d[1] = d[2] = d[3] = 0.f;
+    if (c >= CLS_OCC0) {
+        float k = la_rate(A, c, T);
+        for (int j = 0; j < 4; j++) d[j] = -k * A.dE[c][j] / (KB_EV_F * T);
+    } else if (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) {
+        int co = la_coor(c);
+        for (int s = 0; s < 3; s++) {
+            float k = la_dep(A, s, co, T);
+            if (k == 0.f) continue;
+            for (int j = 0; j < 4; j++) d[j] -= k * A.dEdep[s][co - 1][j] / (KB_EV_F * A.Tm[s]);
+        }
+    }
+}
+
 struct DevStatus {
     int error;               // first error code; nonzero also tells waiting warps to leave
     int err_quad;
@@ -105,7 +182,11 @@ __device__ void set_error(DevStatus *s, int code, int quad)
 }
 
 // --------------------------------------------------------------- kernels
-__global__ void k_init_flat(uint8_t *st, int NA, int NB, int NZ, int pitch, int lz, int len1, int sic)
+// alloy_x > 0: substitutional species 2 on each occupied site with
+// probability alloy_x (Philox on the site index, key alloy_seed), as SetSiGex
+// places Ge at random (mulskips-source/initial/SetSiGex.f:60 uses RAND()).
+__global__ void k_init_flat(uint8_t *st, int NA, int NB, int NZ, int pitch, int lz, int len1, int sic,
+                            float alloy_x = 0.f, unsigned long long alloy_seed = 0ull)
 {
     int64_t n = (int64_t)NZ * NB * pitch;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -115,6 +196,11 @@ __global__ void k_init_flat(uint8_t *st, int NA, int NB, int NZ, int pitch, int 
         int z = (int)(r / NB);
         uint8_t v = 0;
         if (a < NA && ((a + b + (z >> 1)) & 1) == 0) v = flat_init_state(z, lz, len1, sic != 0);
+        if (alloy_x > 0.f && v != WALL && sp_of(v) == 1) {
+            U4 r = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 0x5147u, 0u}, (uint32_t)alloy_seed,
+                                 (uint32_t)(alloy_seed >> 32));
+            if (u01(r.x) < alloy_x) v = (uint8_t)((v & ~3) | 2);
+        }
         st[i] = v;
     }
 }
@@ -269,6 +355,8 @@ struct __align__(16) TileShared {
     int cnt[64];
     float rate[64];
     float spcum[3][2];
+    float G[4];                                // LA: sum over event sites of d(rate)/d(theta)
+    int dcnt[3];                               // LA: net crystal atoms per species added by this tile
     int nlist;
 };
 
@@ -326,7 +414,8 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 // match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
 __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh,
-                                           bool use_pos, int zw0, int wz)
+                                           bool use_pos, int zw0, int wz, const LADev *A = nullptr,
+                                           double t_mid = 0.0)
 {
     TileShared &S = g_tile;
     const unsigned FULL = 0xffffffffu;
@@ -340,6 +429,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
     __syncwarp();
     int ncol = wa * wb;
     int nl = 0;
+    float g[4] = {0.f, 0.f, 0.f, 0.f};
     for (int col0 = 0; col0 < ncol; col0 += 32) {
         int col = col0 + lane;
         bool cv = col < ncol;
@@ -356,10 +446,22 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
                     S.list[slot] = (key << 8) | (uint32_t)cls;
                     if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
                 }
-                unsigned g = __match_any_sync(m, cls);
-                if ((int)(__ffs(g) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(g));
+                unsigned gm = __match_any_sync(m, cls);
+                if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
+                if (A) {
+                    float d[4];
+                    la_drate(*A, cls, la_temp(*A, z, t_mid), d);
+                    for (int j = 0; j < 4; j++) g[j] += d[j];
+                }
             }
             nl += __popc(m);
+        }
+    }
+    if (A) {
+        for (int j = 0; j < 4; j++) {
+            float v = g[j];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane == 0) S.G[j] = v;
         }
     }
     if (lane == 0) S.nlist = min(nl, MCCAP);
@@ -375,9 +477,14 @@ template <class Lat>
 __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadDev &Q, int qid, double &t,
                                           double t_end, unsigned int &evc, int zw0, int zw1, bool use_pos,
                                           int &hz_lo, int &hz_hi, unsigned long long &nev, uint32_t k0, uint32_t k1,
-                                          uint32_t phase_tag, unsigned int window)
+                                          uint32_t phase_tag, unsigned int window, const LADev *A = nullptr,
+                                          double t_mid = 0.0, double *sc = nullptr)
 {
     TileShared &S = g_tile;
+    // LA score: G (uniform over lanes) and the accumulator sc (lane 0, FP64)
+    float G[4] = {0.f, 0.f, 0.f, 0.f};
+    if (A && sc)
+        for (int j = 0; j < 4; j++) G[j] = S.G[j];
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
@@ -422,6 +529,8 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         evc++;
         float dt = __fdividef(-__logf(u01(rnd.z)), rtot);
         if (dt > rem) {
+            if (sc && lane == 0)
+                for (int j = 0; j < 4; j++) sc[j] -= (double)G[j] * (double)rem;
             t = t_end;
             return 0;
         }
@@ -474,15 +583,50 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return 1;   // needs re-staging
         t += (double)dt;
         rem -= dt;
+        if (sc && lane == 0)
+            for (int j = 0; j < 4; j++) sc[j] -= (double)G[j] * (double)dt;
         int sp = 0;
-        if (cls >= CLS_C1 && cls <= CLS_C3) {
+        float Tsite = 0.f;
+        if (A) {
+            // thinning: the class rate is the tile's bound; accept with k(T_site)/bound
+            Tsite = la_temp(*A, z, t_mid);
+            if (cls != CLS_ISO) {
+                float r_true = la_rate(*A, cls, Tsite);
+                float uu = u01(rnd.y) * (float)S.cnt[cls];
+                float uacc = uu - floorf(uu);
+                if (!(uacc * S.rate[cls] < r_true)) continue;   // null event: time only
+            }
+        }
+        if (cls == CLS_C1D) {
+            // unsupported coor-1 site: Get_Prob.f:181-184 fixes IndexEvent = 1
+            // (species 1) with its 1e-8 rate, whatever the tables say
+            sp = 1;
+        } else if (cls >= CLS_C1 && cls <= CLS_C3) {
             int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
             float u = u01(rnd.w);
-            sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
+            if (A) {
+                float p1 = la_dep(*A, 0, co, Tsite), p2 = la_dep(*A, 1, co, Tsite), p3 = la_dep(*A, 2, co, Tsite);
+                float tot = p1 + p2 + p3;
+                sp = u * tot < p1 ? 1 : (u * tot < p1 + p2 ? 2 : 3);
+                if (sc && lane == 0) {
+                    int s0 = sp - 1;
+                    for (int j = 0; j < 4; j++)
+                        sc[j] += -(double)A->dEdep[s0][co - 1][j] / ((double)KB_EV_F * (double)A->Tm[s0]);
+                }
+            } else {
+                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
+            }
+        } else if (A && sc && lane == 0 && cls >= CLS_OCC0) {
+            for (int j = 0; j < 4; j++) sc[j] += -(double)A->dE[cls][j] / ((double)KB_EV_F * (double)Tsite);
         }
         // stage 1: the event site (every lane derives the context, lane 0 writes)
         EvCtx e;
-        if (ev_prepare(L.get(a, b, z), a, b, z, sp, e)) return -DERR_INVARIANT;
+        uint8_t sx0 = L.get(a, b, z);
+        if (ev_prepare(sx0, a, b, z, sp, e)) return -DERR_INVARIANT;
+        if (A && lane == 0) {
+            if (sp) S.dcnt[sp - 1]++;
+            else S.dcnt[sp_of(sx0) - 1]--;
+        }
         if (lane == 0) L.put(a, b, z, ev_begin_state(e));
         __syncwarp();
         // stage 2: lanes 1..4 update the four neighbours, independent of one another
@@ -537,6 +681,19 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             if (old_cls != CLS_NONE) atomicSub(&S.cnt[old_cls], 1);
             if (ncls != CLS_NONE) atomicAdd(&S.cnt[ncls], 1);
         }
+        if (A && sc) {
+            float dn[4] = {0.f, 0.f, 0.f, 0.f}, dold[4] = {0.f, 0.f, 0.f, 0.f};
+            if (interior && old_cls != ncls) {
+                float Tt = la_temp(*A, tz, t_mid);
+                la_drate(*A, ncls, Tt, dn);
+                la_drate(*A, old_cls, Tt, dold);
+            }
+            for (int j = 0; j < 4; j++) {
+                float v = dn[j] - dold[j];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+                G[j] += v;
+            }
+        }
         unsigned am = __ballot_sync(FULL, append);
         if (append) {
             int ns = nlist + __popc(am & lanemask_lt());
@@ -553,9 +710,10 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
 // One tile for one colour phase of one window: stage, run events from
 // t_start to t_start + tau, write back.  Called by the per-colour kernel and
 // by the persistent kernel.
+template <bool LAM>
 __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
                                              DevStatus *status, uint32_t phase_tag, unsigned int window,
-                                             double t_start)
+                                             double t_start, LADev *la_all, double *score_all)
 {
     TileShared &S = g_tile;
     int lane = threadIdx.x & 31;
@@ -585,6 +743,20 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     uint32_t k0 = (uint32_t)R.seed, k1 = (uint32_t)(R.seed >> 32) ^ (0x9E3779B9u * (uint32_t)(Q.rep + 1));
     int zlo = Q.zlo, zhi = Q.zhi;
     int rc = 0;
+    const LADev *A = (LAM && la_all[Q.rep].on) ? &la_all[Q.rep] : nullptr;
+    const double t_mid = t_start + 0.5 * R.tau;
+    double sc[4] = {0.0, 0.0, 0.0, 0.0};
+    double *scp = (A && A->score_on) ? sc : nullptr;
+    if (lane < 3) S.dcnt[lane] = 0;
+    __syncwarp();
+    // LA: class rates are bounds at the hottest of the layers [l0, l1]
+    auto la_bounds = [&](int l0, int l1) {
+        float th = 0.f;
+        for (int z = l0 + lane; z <= l1; z += 32) th = fmaxf(th, la_temp(*A, z, t_mid));
+        for (int o = 16; o > 0; o >>= 1) th = fmaxf(th, __shfl_xor_sync(0xffffffffu, th, o));
+        for (int c = lane; c < 64; c += 32) S.rate[c] = (c == CLS_ISO) ? 0.f : la_rate(*A, c, th);
+        __syncwarp();
+    };
     for (int reload = 0;; reload++) {
         if (reload >= NRELOAD) {
             if (lane == 0) set_error(status, DERR_TIMEOUT, qid);
@@ -642,12 +814,14 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             }
             __syncwarp();
             SLat L{ax0, bx0, zw0, R.NZ};
-            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ)) {
+            if (A) la_bounds(zw0, zw1 - 1);
+            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, scp ? A : nullptr,
+                            t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
             rc = run_events(L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
-                            window);
+                            window, A, t_mid, scp);
             __syncwarp();
             // write back the rows that events changed (tile and its one-column ring)
             for (int r = lane; r < nrows; r += 32) {
@@ -662,13 +836,16 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
         } else {
             // band taller than the staging buffer: run from global memory
             if (lane == 0) atomicAdd(&status->fallback, 1ull);
-            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0)) {
+            // events here may walk the band upwards without re-staging: bound
+            // the rates by the top layer (T rises with z)
+            if (A) la_bounds(max(0, zlo - 2), R.NZ - 1);
+            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
             GLat G2 = G;
             rc = run_events(G2, R, Q, qid, t, t_end, evc, 0, R.NZ, false, hz_lo, hz_hi, nev, k0, k1, phase_tag,
-                            window);
+                            window, A, t_mid, scp);
         }
         __syncwarp();
         // z band of the remaining (live) event sites
@@ -707,6 +884,11 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
         quads[qid].zhi = zhi;
         quads[qid].mc = live;
         if (nev) atomicAdd(&Rg.events, nev);
+        if (scp)
+            for (int j = 0; j < 4; j++) atomicAdd(&score_all[4 * Q.rep + j], sc[j]);
+        if (A)
+            for (int s2 = 0; s2 < 3; s2++)
+                if (S.dcnt[s2]) atomicAdd((unsigned long long *)&la_all[Q.rep].cnt[s2], (unsigned long long)(long long)S.dcnt[s2]);
         if (hz_hi >= 0) {
             // widen the z bands of the neighbouring tiles whose sites changed
             for (int k = 0; k < 8; k++) {
@@ -718,14 +900,16 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     }
 }
 
+template <bool LAM>
 __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
-                                                 uint8_t *st_all, DevStatus *status, uint32_t phase_tag)
+                                                 uint8_t *st_all, DevStatus *status, uint32_t phase_tag,
+                                                 LADev *la, double *score)
 {
     int qi = blockIdx.x;
     if (qi >= nq) return;
     int qid = qlist[qi];
     const RepDev &R = reps[quads[qid].rep];
-    process_tile(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0);
+    process_tile<LAM>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score);
 }
 
 // Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
@@ -739,8 +923,10 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
 // colour launches per window in order.
 constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 
+template <bool LAM>
 __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
-                                                      DevStatus *status, int *progress, int nwin)
+                                                          DevStatus *status, int *progress, int nwin,
+                                                          LADev *la, double *score)
 {
     int lane = threadIdx.x & 31;
     for (int P = 0; P < 4 * nwin; P++) {
@@ -766,8 +952,8 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
             __threadfence();                                // acquire: neighbours' writes before their flag
             if (*(volatile int *)&status->error) return;
             const RepDev &R = reps[quads[t].rep];
-            process_tile(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
-                         R.T0 + (double)w * R.tau);
+            process_tile<LAM>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
+                         R.T0 + (double)w * R.tau, la, score);
             __threadfence();                                // release: each lane's writes reach L2 ...
             __syncwarp();                                   // ... before lane 0 publishes the flag
             if (lane == 0) atomicExch(progress + t, P);
@@ -776,7 +962,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
 }
 
 // End of a window: advance the replica clock, apply the exit conditions.
-__global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin)
+__global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin, LADev *la)
 {
     RepDev &R = reps[blockIdx.x];
     long long s = 0;
@@ -793,7 +979,28 @@ __global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin)
         R.mc_count = sh[0];
         if (!R.active) return;
         R.T0 += (double)nwin * R.tau;
+        unsigned wold = R.window;
         R.window += (unsigned)nwin;
+        if (la && la[blockIdx.x].on) {
+            LADev &A = la[blockIdx.x];
+            long long liq[3], sum = 0, crys = 0, init = 0;
+            for (int s = 0; s < 3; s++) {
+                liq[s] = A.init_cnt[s] - A.cnt[s];
+                if (liq[s] < 0) liq[s] = 0;
+                sum += liq[s];
+                crys += A.cnt[s];
+                init += A.init_cnt[s];
+            }
+            if (R.window / LA_PHASE != wold / LA_PHASE)
+                for (int s = 0; s < 3; s++) A.xliq[s] = sum > 0 ? (float)((double)liq[s] / (double)sum) : 0.f;
+            // LaserAnnealing main.f:714-723: stop once more sites are occupied
+            // than before the melt
+            if (crys > init) {
+                R.active = 0;
+                R.stop_reason = 4;
+                return;
+            }
+        }
         if (R.mc_count <= 20) {
             R.active = 0;
             R.stop_reason = 1;
@@ -803,6 +1010,47 @@ __global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin)
         } else if (R.T0 >= R.t_max) {
             R.active = 0;
             R.stop_reason = 3;
+        }
+    }
+}
+
+// LR gradient of E[f] from the FP64 scores (the backward step of the LA
+// score): grad_j = 1/(n-1) sum_i (f_i - mean f) S_ij, which equals the mean of
+// (f_i - b_i) S_ij with the leave-one-out baseline b_i and is unbiased; se_j
+// is its standard error.  One block, FP64.
+__global__ void k_lr_grad(const double *score, const double *f, int n, int use_b, double *out)
+{
+    __shared__ double sh[256];
+    int tid = threadIdx.x;
+    auto block_sum = [&](double v) {
+        sh[tid] = v;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (tid < o) sh[tid] += sh[tid + o];
+            __syncthreads();
+        }
+        double r = sh[0];
+        __syncthreads();
+        return r;
+    };
+    double fs = 0.0;
+    for (int i = tid; i < n; i += blockDim.x) fs += f[i];
+    double fbar = use_b ? block_sum(fs) / n : 0.0;
+    double scale = (use_b && n > 1) ? (double)n / (double)(n - 1) : 1.0;
+    for (int j = 0; j < 4; j++) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = tid; i < n; i += blockDim.x) {
+            double x = scale * (f[i] - fbar) * score[4 * i + j];
+            s1 += x;
+            s2 += x * x;
+        }
+        s1 = block_sum(s1);
+        s2 = block_sum(s2);
+        if (tid == 0) {
+            double m = s1 / n;
+            double var = n > 1 ? fmax(0.0, (s2 - n * m * m) / (n - 1)) : 0.0;
+            out[j] = m;
+            out[4 + j] = sqrt(var / n);
         }
     }
 }
@@ -925,6 +1173,11 @@ struct mks_handle {
     int graph_windows = 0;
     int tile_width = 8;
     int *d_progress = nullptr;
+    LADev *d_la = nullptr;
+    double *d_score = nullptr;
+    int la_on = 0;
+    int64_t la_window = 0;
+    double *d_lr = nullptr;  // f values and result of mks_batch_lr_grad   // windows run since mks_batch_set_la (persistent launch alignment)
     int coop_grid = 0;
     int schedule = 1;            // 1 persistent dataflow kernel, 0 one launch per colour phase
     uint32_t phase_counter = 0;
@@ -1079,7 +1332,10 @@ int upload_tiles(mks_handle *h)
     int dev = 0, nsm = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl_persistent, 32, 0));
+    int per_sm_la = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl_persistent<false>, 32, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_la, k_sl_persistent<true>, 32, 0));
+    per_sm = std::min(per_sm, per_sm_la);
     h->coop_grid = (int)std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (int64_t)h->quads_h.size());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
@@ -1127,6 +1383,11 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     if ((e = cudaMemsetAsync(h->d_st, 0, (size_t)h->st_bytes, h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
     if ((e = cudaMalloc(&h->d_reps, sizeof(RepDev) * n)) != cudaSuccess) return cleanup_fail("alloc", e);
     if ((e = cudaMalloc(&h->d_status, sizeof(DevStatus))) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMalloc(&h->d_la, sizeof(LADev) * n)) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMemsetAsync(h->d_la, 0, sizeof(LADev) * n, h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
+    if ((e = cudaMalloc(&h->d_score, sizeof(double) * 4 * n)) != cudaSuccess) return cleanup_fail("alloc", e);
+    if ((e = cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream)) != cudaSuccess)
+        return cleanup_fail("memset", e);
     if ((e = cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
     {
         int rc_t = upload_tiles(h);
@@ -1170,12 +1431,17 @@ int launch_window(mks_handle *h)
     for (int c = 0; c < 4; c++) {
         int nq = (int)h->color_list_h[c].size();
         if (!nq) continue;
-        k_sl_phase<<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st, h->d_status,
-                                             (uint32_t)c);
+        if (h->la_on)
+            k_sl_phase<true><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
+                                                       h->d_status, (uint32_t)c, h->d_la, h->d_score);
+        else
+            k_sl_phase<false><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
+                                                        h->d_status, (uint32_t)c, h->d_la, h->d_score);
         h->last_kernels++;
         h->last_phase_launches++;
     }
-    k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, 1);
+    k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, 1,
+                                                             h->la_on ? h->d_la : nullptr);
     h->last_kernels++;
     CK(cudaGetLastError());
     return 0;
@@ -1193,11 +1459,17 @@ int run_persistent(mks_handle *h, int64_t max_windows)
     int launches = 0;
     while (done < max_windows) {
         int nw = (int)std::min<int64_t>(64, max_windows - done);
+        // LA: launches end on liquid-fraction refresh boundaries, as the
+        // per-window schedule refreshes them
+        if (h->la_on) nw = std::min<int64_t>(nw, LA_PHASE - (int64_t)(h->la_window % LA_PHASE));
         CK(cudaMemsetAsync(h->d_progress, 0xFF, sizeof(int) * (size_t)nt, h->stream));
-        void *args[] = {&h->d_reps, &h->d_quads, &nt, &h->d_st, &h->d_status, &h->d_progress, &nw};
-        CK(cudaLaunchCooperativeKernel((const void *)k_sl_persistent, dim3(h->coop_grid), dim3(32), args, 0,
-                                       h->stream));
-        k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw);
+        LADev *la = h->d_la;
+        void *args[] = {&h->d_reps, &h->d_quads, &nt, &h->d_st, &h->d_status, &h->d_progress, &nw, &la, &h->d_score};
+        const void *fn = h->la_on ? (const void *)k_sl_persistent<true> : (const void *)k_sl_persistent<false>;
+        CK(cudaLaunchCooperativeKernel(fn, dim3(h->coop_grid), dim3(32), args, 0, h->stream));
+        k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw,
+                                                                 h->la_on ? h->d_la : nullptr);
+        h->la_window += nw;
         CK(cudaGetLastError());
         h->last_kernels += 2;
         h->last_phase_launches += 1;
@@ -1237,7 +1509,8 @@ int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_
         d[i].tau = tau[i];
         d[i].ev_max = max_events > 0 ? (long long)(d[i].events + (unsigned long long)max_events) : (long long)9e18;
         d[i].t_max = max_time > 0 ? max_time : 1e300;
-        d[i].active = d[i].stop_reason == 1 ? 0 : 1;
+        // "few MC particles" and "regrown" (LA) stops are final
+        d[i].active = (d[i].stop_reason == 1 || d[i].stop_reason == 4) ? 0 : 1;
         if (d[i].active) d[i].stop_reason = 0;
     }
     rc = upload_reps(h, d);
@@ -1278,6 +1551,7 @@ int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_
     while (done < max_windows) {
         CK(cudaGraphLaunch(h->graph_exec, h->stream));
         h->last_graphs++;
+        h->la_window += WPG;
         h->last_kernels += kernels_per_graph;
         h->last_phase_launches += phases_per_graph;
         done += WPG;
@@ -1389,6 +1663,9 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_quads);
     cudaFree(h->d_status);
     cudaFree(h->d_progress);
+    cudaFree(h->d_la);
+    if (h->d_lr) cudaFree(h->d_lr);
+    cudaFree(h->d_score);
     for (int c = 0; c < 4; c++) cudaFree(h->d_clist[c]);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1447,6 +1724,137 @@ int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1)
 }
 
 int mks_init_flat(mks_handle *h, char kind, int32_t len1) { return mks_batch_init_flat(h, kind, &len1); }
+
+int mks_batch_init_alloy(mks_handle *h, const int32_t *len1, const double *x, uint64_t seed)
+{
+    if (!h || !len1 || !x) return fail(MKS_ERR_ARG, "bad arguments");
+    int rc = mks_batch_init_flat(h, 'S', len1);
+    if (rc) return rc;
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        const RepHost &r = h->reps[i];
+        if (x[i] <= 0.0) continue;
+        if (r.cfg.ncrystal < 2) return fail(MKS_ERR_ARG, "an alloy needs NCrystal >= 2");
+        int l1 = len1[i] - len1[i] % 24;
+        int64_t n = (int64_t)r.NZ * r.NB * r.pitch;
+        int blocks = (int)std::min<int64_t>(4096, (n + 255) / 256);
+        k_init_flat<<<blocks, 256, 0, h->stream>>>(h->d_st + r.st_off, r.NA, r.NB, r.NZ, r.pitch, r.cfg.lenz, l1, 0,
+                                                   (float)x[i], seed + 0x9E3779B97F4A7C15ull * i);
+    }
+    CK(cudaGetLastError());
+    return rescan(h);
+}
+
+int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptransE, const double *dptransD)
+{
+    if (!h || !p) return fail(MKS_ERR_ARG, "bad arguments");
+    size_t n = h->reps.size();
+    std::vector<LADev> la(n);
+    for (size_t i = 0; i < n; i++) {
+        const RepHost &r = h->reps[i];
+        LADev &A = la[i];
+        memset(&A, 0, sizeof A);
+        A.on = 1;
+        A.score_on = p[i].score ? 1 : 0;
+        for (int s = 0; s < 3; s++) {
+            A.P0[s] = p[i].P0[s];
+            A.Tm[s] = p[i].Tm[s] > 0 ? p[i].Tm[s] : 1.f;
+            A.Tflex[s] = p[i].Tflex[s];
+            A.sigma[s] = p[i].sigma[s] > 0 ? p[i].sigma[s] : 1.f;
+        }
+        A.Tb = p[i].Tb;
+        A.Ta = p[i].Ta;
+        A.t0 = p[i].t0;
+        A.w = p[i].w > 0 ? p[i].w : 1.f;
+        A.L = p[i].L_nm > 0 ? p[i].L_nm : 1e30f;
+        A.zsurf = p[i].zsurf;
+        A.sf = (float)r.cfg.sf;
+        // barriers: the PTransE / PTransD tables given to mks_batch_set_rates (eV)
+        for (int sp = 1; sp <= 3; sp++)
+            for (int n1 = 0; n1 <= 3; n1++)
+                for (int n2 = 0; n2 <= 3; n2++)
+                    for (int n3 = 0; n3 <= 3; n3++) {
+                        int t = n1 + n2 + n3;
+                        if (t < 1 || t > 3) continue;
+                        int c = CLS_OCC0 + (sp - 1) * NCENSUS + census_index(n1, n2, n3);
+                        size_t k = (size_t)(sp - 1) * 4096 + n1 * 1024 + n2 * 256 + n3 * 64;
+                        A.E[c] = (float)r.ptransE[k];
+                        if (dptransE)
+                            for (int j = 0; j < 4; j++) A.dE[c][j] = (float)dptransE[(i * 3 * 4096 + k) * 4 + j];
+                    }
+        for (int sp = 0; sp < 3; sp++)
+            for (int co = 0; co < 3; co++) {
+                A.Edep[sp][co] = (float)r.ptransD[sp * 3 + co];
+                if (dptransD)
+                    for (int j = 0; j < 4; j++) A.dEdep[sp][co][j] = (float)dptransD[(i * 9 + sp * 3 + co) * 4 + j];
+            }
+    }
+    // crystal atoms now: nothing is liquid yet (InitCountCrystal = CountCrystal)
+    for (size_t i = 0; i < n; i++) {
+        mks_observables o;
+        int rc = obs_impl(h, (int)i, &o);
+        if (rc) return rc;
+        for (int s = 0; s < 3; s++) la[i].init_cnt[s] = la[i].cnt[s] = o.species[s];
+    }
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    h->la_window = d.empty() ? 0 : d[0].window;
+    // a captured window graph holds the plain kernels: capture again
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    CK(cudaMemcpyAsync(h->d_la, la.data(), sizeof(LADev) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->la_on = 1;
+    return 0;
+}
+
+int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, double *grad, double *se)
+{
+    if (!h || !f || !grad) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->la_on) return fail(MKS_ERR_ARG, "LA mode is not set (mks_batch_set_la)");
+    int n = (int)h->reps.size();
+    if (!h->d_lr) CK(cudaMalloc(&h->d_lr, sizeof(double) * (size_t)(n + 8)));
+    CK(cudaMemcpyAsync(h->d_lr, f, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    k_lr_grad<<<1, 256, 0, h->stream>>>(h->d_score, h->d_lr, n, use_baseline ? 1 : 0, h->d_lr + n);
+    CK(cudaGetLastError());
+    double out[8];
+    CK(cudaMemcpyAsync(out, h->d_lr + n, sizeof out, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int j = 0; j < 4; j++) {
+        grad[j] = out[j];
+        if (se) se[j] = out[4 + j];
+    }
+    return 0;
+}
+
+int mks_batch_la_counts(mks_handle *h, int64_t *crystal, double *xliq)
+{
+    if (!h || !crystal) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->la_on) return fail(MKS_ERR_ARG, "LA mode is not set (mks_batch_set_la)");
+    size_t n = h->reps.size();
+    std::vector<LADev> la(n);
+    CK(cudaMemcpyAsync(la.data(), h->d_la, sizeof(LADev) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < n; i++)
+        for (int s = 0; s < 3; s++) {
+            crystal[3 * i + s] = la[i].cnt[s];
+            if (xliq) xliq[3 * i + s] = la[i].xliq[s];
+        }
+    return 0;
+}
+
+int mks_batch_get_score(mks_handle *h, double *score, int32_t reset)
+{
+    if (!h || !score) return fail(MKS_ERR_ARG, "bad arguments");
+    size_t n = h->reps.size();
+    CK(cudaMemcpyAsync(score, h->d_score, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, h->stream));
+    if (reset) CK(cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
 
 int64_t mks_state_size(mks_handle *h)
 {

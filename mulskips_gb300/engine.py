@@ -194,12 +194,6 @@ class Batch:
                                       float(max_time_each), C.byref(ne)))
         return ne.value
 
-    def set_tiling(self, width):
-        N.check(N.lib().mks_set_tiling(self._h, int(width)))
-
-    def set_schedule(self, persistent):
-        N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
-
     def suggest_tau(self, f=0.3):
         t = np.zeros(self.n)
         N.check(N.lib().mks_suggest_tau(self._h, float(f), N.ptr(t)))
@@ -225,3 +219,44 @@ class Batch:
         N.check(N.lib().mks_last_run_stats(self._h, C.byref(k), C.byref(g), C.byref(ms), C.byref(p)))
         return {"kernel_launches": k.value, "graph_launches": g.value, "kernel_ms": ms.value,
                 "phase_launches": p.value}
+
+    # ---- laser anneal (LA) mode ----
+    def init_alloy(self, len1, x, seed):
+        """SetSi-like slabs with species 2 substituted at fraction x[i]."""
+        l1 = np.ascontiguousarray(np.broadcast_to(np.asarray(len1, dtype=np.int32), (self.n,)))
+        xs = np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.n,)))
+        N.check(N.lib().mks_batch_init_alloy(self._h, N.ptr(l1), N.ptr(xs), int(seed) & 0xFFFFFFFFFFFFFFFF))
+
+    def set_la(self, params, dptransE=None, dptransD=None):
+        """params: one MksLaParams per replica (or one for all)."""
+        if isinstance(params, N.MksLaParams):
+            params = [params] * self.n
+        arr = (N.MksLaParams * self.n)(*params)
+        de = None if dptransE is None else np.ascontiguousarray(dptransE, dtype=np.float64).reshape(-1)
+        dd = None if dptransD is None else np.ascontiguousarray(dptransD, dtype=np.float64).reshape(-1)
+        if de is not None:
+            assert de.size == self.n * 3 * 4096 * 4 and dd is not None and dd.size == self.n * 9 * 4
+        N.check(N.lib().mks_batch_set_la(self._h, arr, None if de is None else N.ptr(de),
+                                         None if dd is None else N.ptr(dd)))
+        self._la_keep = (de, dd)
+
+    def score(self, reset=False):
+        out = np.zeros((self.n, 4))
+        N.check(N.lib().mks_batch_get_score(self._h, N.ptr(out), 1 if reset else 0))
+        return out
+
+    def la_counts(self):
+        """(crystal atoms per species (n, 3), liquid fractions in use (n, 3))."""
+        c = np.zeros((self.n, 3), dtype=np.int64)
+        x = np.zeros((self.n, 3))
+        N.check(N.lib().mks_batch_la_counts(self._h, N.ptr(c), N.ptr(x)))
+        return c, x
+
+    def lr_grad(self, f, baseline=True):
+        """Likelihood-ratio gradient of E[f] (one f per replica) and its
+        standard error, computed on the GPU from the accumulated scores."""
+        fv = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        assert fv.size == self.n
+        g, se = np.zeros(4), np.zeros(4)
+        N.check(N.lib().mks_batch_lr_grad(self._h, N.ptr(fv), 1 if baseline else 0, N.ptr(g), N.ptr(se)))
+        return g, se

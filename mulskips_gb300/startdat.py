@@ -6,6 +6,7 @@ mulskips-source/main.f:83-212 and mulskips-source/mcevent/SetProbability.f:21-14
 rest of the record, including '!' comments, is ignored).  The writer follows
 pymulskips/setuprun.py:292-389 (print_file_input).
 """
+import itertools
 import math
 
 import numpy as np
@@ -136,5 +137,38 @@ def write_plain_si_startdat(path, T=1100.0, e_bond=0.6, nu=1e13, flux=0.5, len1=
              "F ! Save final state", "F ! Save final Coor"]
     lines += [f"1 {n} {e[n - 1]!r} ! PtransE[1,{n}]" for n in (1, 2, 3)]
     lines += [f"1 {n} {flux!r} ! PtransD[1,{n}]" for n in (1, 2, 3)]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_startdat(path, ptransE, ptransD, ncrystal=1, list_crystal=(14,), init_st="FS", len1=120,
+                   max_iter=1000000, out_molmol=None, run_type="R", seed=1, sf=5.43 / 12, lens=(120, 120),
+                   alloy_fraction=0.0):
+    """start.dat for NCrystal 1..3 species without coverage (main.f:83-212
+    grammar): every PTransE(s, n_1..n_NCrystal) entry with 1 <= sum n <= 3 and
+    the 3 PTransD entries of each species, from arrays in the engine layout
+    (ptransE (3,4,4,4,4,4,4), ptransD (3,3)).  Si/Ge lists carry the alloy
+    fraction record that main.f reads after the box sizes."""
+    E = np.asarray(ptransE, dtype=np.float64).reshape(3, 4, 4, 4, 4, 4, 4)
+    D = np.asarray(ptransD, dtype=np.float64).reshape(3, 3)
+    out_molmol = out_molmol or max_iter
+    lc = " ".join(str(int(z)) for z in list_crystal[:ncrystal])
+    lines = [f"{ncrystal} 0 ! NCrystal, NCov", f"{lc} ! Atomic numbers of crystal species",
+             f"{init_st} ! Initstat", f"{len1} {lens[0]} {lens[1]} ! Len1 Len2 Len3"]
+    if ncrystal >= 2 and tuple(list_crystal[:2]) == (14, 32):
+        lines.append(f"{float(alloy_fraction)!r} ! alloy fraction")
+    lines += ["1.0 ! PtransZig", f"{sf:.15f} ! KMC_sf", "Iter ! ExitStrategy", f"{max_iter} ! IterMax",
+              f"{out_molmol} ! OutMolMol", f"{run_type} ! RunType", f"{seed} ! Random seed",
+              "F ! Save final state", "F ! Save final Coor"]
+    for s in range(ncrystal):
+        for n in itertools.product(range(4), repeat=ncrystal):
+            if not 1 <= sum(n) <= 3:
+                continue
+            idx = tuple(n) + (0,) * (3 - ncrystal)
+            code = "".join(str(d) for d in n)
+            lines.append(f"{s + 1} {code} {float(E[(s,) + idx + (0, 0, 0)])!r} ! PtransE")
+    for s in range(ncrystal):
+        for n in (1, 2, 3):
+            lines.append(f"{s + 1} {n} {float(D[s, n - 1])!r} ! PtransD")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")

@@ -96,6 +96,18 @@ struct ora {
     double alloyfraction;
     /* LA law parameters (MS/modules/definitions.f:30) */
     double Tm, P0, sigma, Tflex;
+    /* per-species LA law with liquid fractions and the LR score (ora_la_*) */
+    int la2;
+    ora_la_t lap;
+    double dE[NCRYSTAL_MAX][4][4][4][4];    /* d PTransE(s,n1,n2,n3,0,0,0) / d theta_j */
+    double dEd[NCRYSTAL_MAX][3][4];         /* d PTransD(s,n) / d theta_j              */
+    double xliq[3];
+    int64_t la_init[3], la_cnt[3], la_win, la_events;
+    double la_score[4];
+    uint64_t la_rng[4];
+    int la_stop;
+    double *la_k, *la_dk, *la_ps;           /* per-MC-particle rates of the last scan */
+    int *la_kind, la_cap;
     char init_st[3], run_type[3], exit_strategy[5];
     char save_final[3], save_coo[3];
     char restartfile[2048], coofile[2048];
@@ -391,21 +403,48 @@ static const double KB = 0.00008617330350;   /* Get_Prob.f:70 */
 static double pe_entry(ora_t *o, int s, int i1, int i2, int i3, int i4, int i5, int i6, int temperature)
 {
     double v = o->ptransE[s - 1][i1][i2][i3][i4][i5][i6];
+    if (o->la2) return v != 0.0 ? o->lap.P0[s - 1] * exp(-v / (KB * (double)temperature)) : 0.0;
     if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
         double e = o->P0 * exp(-v / (KB * (double)temperature));
         return e * (v != 0.0 ? 1.0 : 0.0);
     }
     return v;
 }
+static double la2_pd(ora_t *o, int s, int coor, int temperature);
 static double pd_entry(ora_t *o, int s, int coor, int temperature)
 {
     double v = o->ptransD[s - 1][coor - 1];
+    if (o->la2) return la2_pd(o, s, coor, temperature);
     if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
         double e = 0.5 * o->P0 * exp(-v / (KB * o->Tm)) *
                    (1.0 + erf(((double)temperature - o->Tflex) / o->sigma));
         return e * (v != 0.0 ? 1.0 : 0.0);
     }
     return v;
+}
+
+/* Prescribed temperature of grid layer z in the current window (integer K):
+ * T = Tb + Ta exp(-((t_mid - t0)/w)^2) exp(-depth/L), depth = max(0, (zsurf
+ * - z) sf / 10) nm, t_mid the window midpoint.  Replaces the per-site
+ * temperature bits of the LaserAnnealing variant (LA/mcevent/Get_Prob.f:131). */
+static int la2_temp(ora_t *o, int z)
+{
+    const ora_la_t *p = &o->lap;
+    double tmid = ((double)o->la_win + 0.5) * p->tau;
+    double g = (tmid - p->t0) / p->w;
+    double depth = (p->zsurf - (double)z) * o->sf * 0.1;
+    if (depth < 0.0) depth = 0.0;
+    return (int)rint(p->Tb + p->Ta * exp(-g * g) * exp(-depth / p->L_nm));
+}
+
+/* Solidification of species s on a liquid site of coordination coor,
+ * LaserAnnealing mcevent/Get_Prob.f:147-151 (liquid fraction xliq). */
+static double la2_pd(ora_t *o, int s, int coor, int temperature)
+{
+    double v = o->ptransD[s - 1][coor - 1];
+    if (v == 0.0 || !(o->xliq[s - 1] > 0.0)) return 0.0;
+    return 0.5 * o->lap.P0[s - 1] * o->xliq[s - 1] * exp(-v / (KB * o->lap.Tm[s - 1])) *
+           (1.0 + erf(((double)temperature - o->lap.Tflex[s - 1]) / o->lap.sigma[s - 1]));
 }
 
 /* IndexEvent_Abs, MS/mcevent/Get_Prob.f:22-52 */
@@ -457,7 +496,9 @@ static void get_prob(ora_t *o, int occ, int nsic, int covind, int coor,
 {
     int temperature = 0;
     int la = (o->init_st[0] == 'L' && o->init_st[1] == 'A');
-    if (la) {
+    if (o->la2) {
+        temperature = la2_temp(o, site[2]);
+    } else if (la) {
         temperature = ibits(*LC(o, site), POS_T, LEN_T);
         if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob()");
     }
@@ -575,7 +616,10 @@ static void get_prob(ora_t *o, int occ, int nsic, int covind, int coor,
             *prob_event = pe_entry(o, nsic, n_si + n_wall, n_c, n_b, c1, c2, c3, temperature);
         }
     }
-    if (*index_event != 0 && *prob_event < (double)1e-12f)
+    /* LA2: a liquid-starved site keeps its list entry (the selection of
+     * ora_la_run_until recomputes every rate) */
+    if (o->la2 && *index_event != 0 && *prob_event == 0.0) *prob_event = 1e-300;
+    if (*index_event != 0 && *prob_event < (double)1e-12f && !o->la2)
         lg(o, " %d %.17g %d\n", *index_event, *prob_event, coor);
 }
 
@@ -1631,6 +1675,10 @@ ora_t *ora_create(const char *startdat_path, const char *numbers_path, int lenx,
 void ora_destroy(ora_t *o)
 {
     if (!o) return;
+    free(o->la_k);
+    free(o->la_dk);
+    free(o->la_ps);
+    free(o->la_kind);
     free(o->latt_base);
     free(o->lind_base);
     free(o->mc);
@@ -1945,4 +1993,303 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
         rate[i - 1] = p->prob;
     }
     return o->num_mc;
+}
+
+/* ============ per-species LA law, liquid fractions and LR score ============
+ * The LaserAnnealing variant's rate law (LA/mcevent/Get_Prob.f:127-152,
+ * per-species P0, Tm, Tflex, sigma; solidification weighted by the liquid
+ * fraction CountLiquid/SUM(CountLiquid) with CountLiquid = InitCountCrystal -
+ * CountCrystal, LA/main.f:637, Evaporation.f:41, main.f:683) on the lists and
+ * event routines above, with a prescribed temperature field.  The clock is a
+ * continuous-time Markov chain with exponential waiting times and every rate
+ * recomputed from the lattice before each draw (a linear scan instead of the
+ * sum tree), so that the likelihood-ratio score
+ *     S_j = sum_events d log k / d theta_j - int sum_sites d k / d theta_j dt
+ * is exact; it is accumulated in FP64.  Time is cut into windows of length
+ * tau: the temperature of a window is taken at its midpoint, the liquid
+ * fractions are refreshed every `phase` windows and the stop rules (more atoms
+ * than at the start, LA/main.f:714-723; <= 20 MC particles, main.f:307-310)
+ * are checked at window ends — the schedule of the GPU engine's LA mode.
+ * The Ge/Si swap of LA/main.f:676-681 is not applied (a species with no liquid
+ * left has zero solidification rate from the next refresh on).            */
+
+static uint64_t la_next(ora_t *o)
+{   /* xoshiro256** (Blackman & Vigna) */
+    uint64_t *q = o->la_rng;
+    uint64_t r = q[1] * 5;
+    r = ((r << 7) | (r >> 57)) * 9;
+    uint64_t t = q[1] << 17;
+    q[2] ^= q[0]; q[3] ^= q[1]; q[1] ^= q[2]; q[0] ^= q[3];
+    q[2] ^= t;
+    q[3] = (q[3] << 45) | (q[3] >> 19);
+    return r;
+}
+static double la_u01(ora_t *o) { return ((double)(la_next(o) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+/* reciprocal occupied neighbours by species (walls count as species 1), as
+ * the occupied branch of get_prob (Get_Prob.f:230-300) */
+static int la2_census(ora_t *o, const int site[3], int nextn[4][3], int *n1, int *n2, int *n3)
+{
+    int n_si = 0, n_c = 0, n_b = 0, n_wall = 0;
+    for (int i = 0; i < 4; i++) {
+        int32_t v = *LC(o, nextn[i]);
+        if (ibits(v, POS_OCC, LEN_OCC) == 0) continue;
+        if (ibits(v, POS_INDEX, LEN_INDEX) == WALL) { n_wall++; continue; }
+        int coornn = ibits(v, POS_COOR, LEN_COOR);
+        int nnn[4][3];
+        get_nn_list(o, *LI(o, nextn[i]), (coornn >= 1 && coornn <= 3) ? 1 : 2, nnn);
+        if (!in_list(nnn, site)) continue;
+        int sp = ibits(v, POS_SIC, LEN_SIC);
+        if (sp == 1) n_si++;
+        if (sp == 2) n_c++;
+        if (sp == 3) n_b++;
+    }
+    *n1 = n_si + n_wall; *n2 = n_c; *n3 = n_b;
+    return n_si + n_c + n_b + n_wall;
+}
+
+enum { LK_NONE = 0, LK_DEP = 1, LK_DUMMY = 2, LK_MELT = 3, LK_ISO = 4 };
+
+/* rate k of MC particle ind, dk/dtheta, and per-species solidification rates */
+static int la2_rate(ora_t *o, int ind, double *k, double dk[4], double ps[3])
+{
+    mcp_t *m = &o->mc[ind];
+    int32_t v = *LC(o, m->xyz);
+    int occ = ibits(v, POS_OCC, LEN_OCC), coor = ibits(v, POS_COOR, LEN_COOR);
+    int T = la2_temp(o, m->xyz[2]);
+    *k = 0.0;
+    for (int j = 0; j < 4; j++) dk[j] = 0.0;
+    ps[0] = ps[1] = ps[2] = 0.0;
+    if (occ) {
+        int n1, n2, n3, sp = ibits(v, POS_SIC, LEN_SIC);
+        int tot = la2_census(o, m->xyz, m->nn, &n1, &n2, &n3);
+        if (tot > 3 || sp < 1) return LK_NONE;
+        if (tot == 0) return LK_ISO;
+        double E = o->ptransE[sp - 1][n1][n2][n3][0][0][0];
+        if (E == 0.0) return LK_NONE;
+        *k = o->lap.P0[sp - 1] * exp(-E / (KB * (double)T));
+        for (int j = 0; j < 4; j++) dk[j] = -*k * o->dE[sp - 1][n1][n2][n3][j] / (KB * (double)T);
+        return LK_MELT;
+    }
+    if (coor == 1 && m->prob == (double)1.e-8f) {   /* Get_Prob.f:181-184 */
+        *k = (double)1.e-8f;
+        return LK_DUMMY;
+    }
+    if (coor < 1 || coor > 3) return LK_NONE;
+    for (int s = 0; s < 3; s++) {
+        ps[s] = la2_pd(o, s + 1, coor, T);
+        *k += ps[s];
+        for (int j = 0; j < 4; j++) dk[j] -= ps[s] * o->dEd[s][coor - 1][j] / (KB * o->lap.Tm[s]);
+    }
+    return LK_DEP;
+}
+
+static void la2_refresh_xliq(ora_t *o)
+{
+    int64_t liq[3], sum = 0;
+    for (int s = 0; s < 3; s++) {
+        liq[s] = o->la_init[s] - o->la_cnt[s];
+        if (liq[s] < 0) liq[s] = 0;
+        sum += liq[s];
+    }
+    for (int s = 0; s < 3; s++) o->xliq[s] = sum > 0 ? (double)liq[s] / (double)sum : 0.0;
+}
+
+static int64_t la2_species_count(ora_t *o, int64_t out[3])
+{
+    out[0] = out[1] = out[2] = 0;
+    for (int z = 0; z <= o->lz; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (!ibits(v, POS_OCC, LEN_OCC) || ibits(v, POS_INDEX, LEN_INDEX) == WALL) continue;
+                int sp = ibits(v, POS_SIC, LEN_SIC);
+                if (sp >= 1 && sp <= 3) out[sp - 1]++;
+            }
+    return out[0] + out[1] + out[2];
+}
+
+int ora_la_alloy(ora_t *o, double x, uint64_t seed)
+{
+    if (setjmp(o->jb)) return -1;
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    for (int i = 0; i < 4; i++) {   /* splitmix64 */
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t r = z;
+        r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ull;
+        r = (r ^ (r >> 27)) * 0x94D049BB133111EBull;
+        o->la_rng[i] = r ^ (r >> 31);
+    }
+    for (int zz = 0; zz <= o->lz; zz++)
+        for (int y = 0; y < o->ly; y++)
+            for (int xx = 0; xx < o->lx; xx++) {
+                int32_t *v = &o->latt[lidx(o, xx, y, zz)];
+                if (!ibits(*v, POS_OCC, LEN_OCC) || ibits(*v, POS_INDEX, LEN_INDEX) == WALL) continue;
+                if (la_u01(o) < x) mvbits(2, LEN_SIC, v, POS_SIC);
+            }
+    return 0;
+}
+
+int ora_la_set(ora_t *o, const ora_la_t *p, const double *ptransE, const double *dptransE,
+               const double *ptransD, const double *dptransD, uint64_t seed)
+{
+    if (setjmp(o->jb)) return -1;
+    if (o->ncov != 0) ora_fail(o, "LA mode with coverage species is not restated");
+    if (!(p->tau > 0.0) || p->phase < 1) ora_fail(o, "LA mode needs tau > 0 and phase >= 1");
+    o->lap = *p;
+    memset(o->ptransE, 0, sizeof o->ptransE);
+    memset(o->dE, 0, sizeof o->dE);
+    for (int s = 0; s < 3; s++)
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++)
+                for (int c = 0; c < 4; c++) {
+                    size_t k = (size_t)s * 4096 + a * 1024 + b * 256 + c * 64;
+                    o->ptransE[s][a][b][c][0][0][0] = ptransE[k];
+                    for (int j = 0; j < 4; j++) o->dE[s][a][b][c][j] = dptransE ? dptransE[k * 4 + j] : 0.0;
+                }
+    for (int s = 0; s < 3; s++)
+        for (int n = 0; n < 3; n++) {
+            o->ptransD[s][n] = ptransD[s * 3 + n];
+            for (int j = 0; j < 4; j++) o->dEd[s][n][j] = dptransD ? dptransD[(s * 3 + n) * 4 + j] : 0.0;
+        }
+    uint64_t z = seed;
+    for (int i = 0; i < 4; i++) {   /* splitmix64 */
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t r = z;
+        r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ull;
+        r = (r ^ (r >> 27)) * 0x94D049BB133111EBull;
+        o->la_rng[i] = r ^ (r >> 31);
+    }
+    la2_species_count(o, o->la_init);
+    memcpy(o->la_cnt, o->la_init, sizeof o->la_init);
+    o->xliq[0] = o->xliq[1] = o->xliq[2] = 0.0;
+    o->la_win = (int64_t)floor(o->time / p->tau + 0.5);
+    o->time = (double)o->la_win * p->tau;
+    o->la_events = 0;
+    o->la_stop = 0;
+    memset(o->la_score, 0, sizeof o->la_score);
+    o->la2 = 1;
+    o->started = 1;
+    return 0;
+}
+
+int ora_la_run_until(ora_t *o, double t_end)
+{
+    if (setjmp(o->jb)) return -1;
+    if (!o->la2) ora_fail(o, "LA mode is not set (ora_la_set)");
+    const double tau = o->lap.tau;
+    int nz = o->lz + 1;
+    int *tprof = (int *)malloc(sizeof(int) * (size_t)nz);
+    if (!tprof) ora_fail(o, "allocation failed");
+    for (int z = 0; z < nz; z++) tprof[z] = la2_temp(o, z);
+    int dirty = 1, niso = 0;
+    double R = 0.0, Rrest = 0.0, G[4] = {0.0, 0.0, 0.0, 0.0};
+    while (!o->la_stop && o->time < t_end - 0.5 * tau) {
+        double wend = (double)(o->la_win + 1) * tau;
+        if (dirty) {
+            if (o->la_cap < o->num_mc + 2) {
+                o->la_cap = 2 * (o->num_mc + 2);
+                o->la_k = (double *)realloc(o->la_k, sizeof(double) * (size_t)o->la_cap);
+                o->la_dk = (double *)realloc(o->la_dk, sizeof(double) * 4 * (size_t)o->la_cap);
+                o->la_ps = (double *)realloc(o->la_ps, sizeof(double) * 3 * (size_t)o->la_cap);
+                o->la_kind = (int *)realloc(o->la_kind, sizeof(int) * (size_t)o->la_cap);
+                if (!o->la_k || !o->la_dk || !o->la_ps || !o->la_kind) {
+                    free(tprof);
+                    ora_fail(o, "allocation failed");
+                }
+            }
+            Rrest = 0.0;
+            niso = 0;
+            for (int j = 0; j < 4; j++) G[j] = 0.0;
+            for (int ind = 1; ind <= o->num_mc; ind++) {
+                int kind = la2_rate(o, ind, &o->la_k[ind], &o->la_dk[4 * ind], &o->la_ps[3 * ind]);
+                o->la_kind[ind] = kind;
+                if (kind == LK_ISO) niso++;
+                Rrest += o->la_k[ind];
+                for (int j = 0; j < 4; j++) G[j] += o->la_dk[4 * ind + j];
+            }
+            R = Rrest * (1.0 + 1.0e5 * niso);   /* isolated atoms: 1e5 x total, Get_Prob.f:305 */
+            dirty = 0;
+        }
+        double dt = R > 0.0 ? -log(la_u01(o)) / R : INFINITY;
+        if (o->time + dt >= wend) {
+            for (int j = 0; j < 4; j++) o->la_score[j] -= G[j] * (wend - o->time);
+            o->time = wend;
+            o->la_win++;
+            if (o->la_win % o->lap.phase == 0) {
+                double x0[3];
+                memcpy(x0, o->xliq, sizeof x0);
+                la2_refresh_xliq(o);
+                if (memcmp(x0, o->xliq, sizeof x0)) dirty = 1;
+            }
+            int64_t crys = o->la_cnt[0] + o->la_cnt[1] + o->la_cnt[2];
+            int64_t init = o->la_init[0] + o->la_init[1] + o->la_init[2];
+            if (crys > init) o->la_stop = 4;
+            else if (o->num_mc <= 20) o->la_stop = 1;
+            for (int z = 0; z < nz; z++) {
+                int t = la2_temp(o, z);
+                if (t != tprof[z]) { tprof[z] = t; dirty = 1; }
+            }
+            continue;
+        }
+        o->time += dt;
+        for (int j = 0; j < 4; j++) o->la_score[j] -= G[j] * dt;
+        double target = la_u01(o) * R, acc = 0.0;
+        int ind = 0;
+        for (int i = 1; i <= o->num_mc; i++) {
+            acc += o->la_kind[i] == LK_ISO ? 1.0e5 * Rrest : o->la_k[i];
+            if (acc > target) { ind = i; break; }
+        }
+        if (ind == 0)   /* rounding at the top end: the last particle with a rate */
+            for (int i = o->num_mc; i >= 1 && !ind; i--)
+                if (o->la_kind[i] == LK_ISO || o->la_k[i] > 0.0) ind = i;
+        if (ind == 0) break;
+        mcp_t *m = &o->mc[ind];
+        int site[3];
+        cp3(site, m->xyz);
+        int kind = o->la_kind[ind];
+        int32_t v = *LC(o, site);
+        int sp = ibits(v, POS_SIC, LEN_SIC), coor = ibits(v, POS_COOR, LEN_COOR);
+        if (kind == LK_DEP) {
+            const double *ps = &o->la_ps[3 * ind];
+            double u = la_u01(o) * (ps[0] + ps[1] + ps[2]);
+            int s = u < ps[0] ? 0 : (u < ps[0] + ps[1] ? 1 : 2);
+            for (int j = 0; j < 4; j++) o->la_score[j] -= o->dEd[s][coor - 1][j] / (KB * o->lap.Tm[s]);
+            deposition(o, ind, s + 1);
+            o->la_cnt[s]++;
+            o->count_crystal[s]++;
+        } else if (kind == LK_DUMMY) {
+            deposition(o, ind, 1);
+            o->la_cnt[0]++;
+            o->count_crystal[0]++;
+        } else if (kind == LK_MELT) {
+            int n1, n2, n3;
+            la2_census(o, site, m->nn, &n1, &n2, &n3);
+            int T = la2_temp(o, site[2]);
+            for (int j = 0; j < 4; j++) o->la_score[j] -= o->dE[sp - 1][n1][n2][n3][j] / (KB * (double)T);
+            evaporation(o, ind);
+            o->la_cnt[sp - 1]--;
+        } else if (kind == LK_ISO) {
+            evaporation(o, ind);
+            o->la_cnt[sp - 1]--;
+        } else {
+            free(tprof);
+            ora_fail(o, "picked a particle without an event");
+        }
+        o->la_events++;
+        o->iter++;
+        dirty = 1;
+    }
+    free(tprof);
+    return o->la_stop;
+}
+
+void ora_la_state(const ora_t *o, double score[4], int64_t crystal[3], double xliq[3], int64_t *events)
+{
+    for (int j = 0; j < 4; j++) score[j] = o->la_score[j];
+    for (int s = 0; s < 3; s++) {
+        crystal[s] = o->la_cnt[s];
+        xliq[s] = o->xliq[s];
+    }
+    *events = o->la_events;
 }

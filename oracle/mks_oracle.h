@@ -94,6 +94,30 @@ int64_t ora_mc_classes(const ora_t *o, int32_t *cls, double *rate, int64_t n);
 
 /* Export the rate tables parsed from start.dat. */
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);
+/* ---- per-species LA law with liquid fractions and LR score ----
+ * (LaserAnnealing variant: LA/mcevent/Get_Prob.f:127-152, LA/main.f:637,
+ * 676-723).  Prescribed T(z,t) = Tb + Ta exp(-((t_mid-t0)/w)^2)
+ * exp(-max(0, (zsurf - z) sf/10 nm)/L), t_mid the midpoint of the window of
+ * length tau holding t; liquid fractions refreshed every `phase` windows.
+ * The clock of ora_la_run_until is exponential (CTMC) and the FP64 score of
+ * theta is accumulated; see mks_oracle.c.                                  */
+typedef struct {
+    double P0[3], Tm[3], Tflex[3], sigma[3];
+    double Tb, Ta, t0, w, L_nm, zsurf;
+    double tau;
+    int phase;
+} ora_la_t;
+/* Substitute species 2 on every atom with probability x (after ora_init). */
+int ora_la_alloy(ora_t *o, double x, uint64_t seed);
+/* Switch to LA mode: PTransE (3*4096, PTransE(s,n1,n2,n3,c1,c2,c3) layout,
+ * barriers in eV), its theta-derivatives (3*4096*4, may be NULL), PTransD (9)
+ * and derivatives (9*4, may be NULL); the atoms present count as crystal. */
+int ora_la_set(ora_t *o, const ora_la_t *p, const double *ptransE, const double *dptransE,
+               const double *ptransD, const double *dptransD, uint64_t seed);
+/* Advance to t_end (a window boundary).  Returns 0, 4 (more atoms than at
+ * ora_la_set), 1 (<= 20 MC particles) or < 0 on error. */
+int ora_la_run_until(ora_t *o, double t_end);
+void ora_la_state(const ora_t *o, double score[4], int64_t crystal[3], double xliq[3], int64_t *events);
 /* Raw ran3 for testing: seed then draw n values. */
 void ora_ran3_sequence(int idum, int n, double *out);
 

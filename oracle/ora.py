@@ -59,8 +59,21 @@ def lib():
         L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
+        L.ora_la_alloy.argtypes = [C.c_void_p, C.c_double, C.c_uint64]
+        L.ora_la_set.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_uint64]
+        L.ora_la_run_until.argtypes = [C.c_void_p, C.c_double]
+        L.ora_la_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
+
+
+class OraLa(C.Structure):
+    """ora_la_t of mks_oracle.h."""
+    _fields_ = [("P0", C.c_double * 3), ("Tm", C.c_double * 3), ("Tflex", C.c_double * 3),
+                ("sigma", C.c_double * 3), ("Tb", C.c_double), ("Ta", C.c_double), ("t0", C.c_double),
+                ("w", C.c_double), ("L_nm", C.c_double), ("zsurf", C.c_double), ("tau", C.c_double),
+                ("phase", C.c_int)]
 
 
 class Oracle:
@@ -95,6 +108,35 @@ class Oracle:
         if r < 0:
             raise RuntimeError(lib().ora_last_error().decode())
         return r
+
+    # ---- per-species LA law with liquid fractions and FP64 score ----
+    def la_alloy(self, x, seed):
+        if lib().ora_la_alloy(self._h, float(x), int(seed) & 0xFFFFFFFFFFFFFFFF):
+            raise RuntimeError(lib().ora_last_error().decode())
+
+    def la_set(self, params, E, dE, D, dD, seed):
+        self._la_keep = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if a is not None else None
+                         for a in (E, dE, D, dD)]
+        k = self._la_keep
+        r = lib().ora_la_set(self._h, C.byref(params), *(None if a is None else a.ctypes.data_as(C.c_void_p)
+                                                         for a in k), int(seed) & 0xFFFFFFFFFFFFFFFF)
+        if r:
+            raise RuntimeError(lib().ora_last_error().decode())
+
+    def la_run_until(self, t):
+        r = lib().ora_la_run_until(self._h, float(t))
+        if r < 0:
+            raise RuntimeError(lib().ora_last_error().decode())
+        return r
+
+    def la_state(self):
+        sc = np.zeros(4)
+        cr = np.zeros(3, dtype=np.int64)
+        xl = np.zeros(3)
+        ev = C.c_int64()
+        lib().ora_la_state(self._h, sc.ctypes.data_as(C.c_void_p), cr.ctypes.data_as(C.c_void_p),
+                           xl.ctypes.data_as(C.c_void_p), C.byref(ev))
+        return {"score": sc, "crystal": cr, "xliq": xl, "events": ev.value}
 
     def atoms(self):
         st, _ = compact_state(self)
@@ -186,3 +228,34 @@ def rate_of_site(o, x, y, z):
     """(list kind, Ind_Event, rate) of the site, from the oracle's lists."""
     which, _, ie, pr = o.site_info(x, y, z)
     return which, ie, pr
+
+
+def la_replica(args):
+    """One oracle LA replica (for a spawn process pool): SiGe slab of Ge
+    fraction x in a (lx, ly, lz) box, barrier tables E/dE/D/dD, LA parameters
+    `la` (dict of OraLa fields); returns the crystal counts and FP64 scores at
+    each time of `marks`."""
+    import tempfile
+    (startdat_text, dims, x, alloy_seed, la, E, dE, D, dD, seed, marks) = args
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "start.dat")
+        with open(p, "w") as f:
+            f.write(startdat_text)
+        o = Oracle(p, *dims, numbers=None)
+        o.init()
+        o.la_alloy(x, alloy_seed)
+        prm = OraLa()
+        for k, v in la.items():
+            if isinstance(v, (list, tuple)):
+                for i, vi in enumerate(v):
+                    getattr(prm, k)[i] = vi
+            else:
+                setattr(prm, k, v)
+        o.la_set(prm, E, dE, D, dD, seed)
+        out = []
+        for t in marks:
+            rc = o.la_run_until(t)
+            st = o.la_state()
+            out.append((st["crystal"].copy(), st["score"].copy(), st["events"], rc))
+        o.close()
+    return out

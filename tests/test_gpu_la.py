@@ -1,0 +1,174 @@
+"""LA melt/regrowth of SiGe and the likelihood-ratio gradient (GPU).
+
+Small SiGe slabs (96 x 96 x 192 grid, Len1 = 144, Ge fraction 0.2) under a
+static temperature field (1750 K at the surface, decaying with depth over
+5 nm), 20 ns.  Checked against the oracle's LA mode (serial CTMC on the
+reference's lists, FP64 score, same window schedule) and against
+common-random-number finite differences on the GPU:
+
+* crystal atoms at 10 and 20 ns and Ge atoms at 20 ns: GPU mean within the
+  3-sigma band of the oracle mean;
+* the score has mean zero (E[S] = 0) on both;
+* the LR gradient of f = crystal(20 ns) - crystal(10 ns) on the GPU agrees
+  with the oracle's FP64 LR gradient and with CRN central differences
+  (h = 0.02 eV) within 3 sigma, and the differences resolve a nonzero
+  gradient (so the comparison has power).
+"""
+import math
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BOX = (96, 96, 192)
+LEN1 = 144
+XGE = 0.2
+N = 512
+T1, T2 = 10e-9, 20e-9
+PULSE = dict(Tb=300.0, Ta=1450.0, t0=0.0, w=1.0, L_nm=5.0)
+H = 0.02
+
+
+def _tau(theta):
+    from mulskips_gb300 import la
+    r = la.max_rate(theta, la.Material(), PULSE["Tb"] + PULSE["Ta"])
+    k = math.ceil(T1 / 8.0 / (0.3 / r))
+    return T1 / (8.0 * k)
+
+
+def _sim(n=N, seed=4):
+    from mulskips_gb300 import la
+    return la.Anneal(n=n, box=BOX, len1=LEN1, x_ge=XGE, seed=seed, pulse=la.Pulse(**PULSE))
+
+
+def _gpu_run(sim, theta, tau, score=True):
+    sim.start(theta, score=score, tau=tau)
+    sim.advance(T1)
+    c1, x1 = sim.batch.la_counts()
+    sim.advance(T2)
+    c2, x2 = sim.batch.la_counts()
+    return c1, c2, x2
+
+
+@pytest.fixture(scope="module")
+def theta():
+    from mulskips_gb300 import la
+    return np.array(la.THETA_REF)
+
+
+@pytest.fixture(scope="module")
+def gpu(theta):
+    sim = _sim()
+    tau = _tau(theta)
+    c1, c2, x2 = _gpu_run(sim, theta, tau)
+    f = (c2.sum(1) - c1.sum(1)).astype(np.float64)
+    score = sim.batch.score()
+    g, se = sim.batch.lr_grad(f)
+    st = sim.batch.observables()
+    out = dict(c1=c1, c2=c2, x2=x2, f=f, score=score, g=g, se=se, sim=sim, tau=tau,
+               events=np.array([o["events"] for o in st]))
+    yield out
+    sim.batch.close()
+
+
+@pytest.fixture(scope="module")
+def oracle(oracle_lib, theta):
+    from mulskips_gb300 import la
+    from mulskips_gb300.startdat import write_startdat
+    import tempfile
+    E, dE, D, dD = la.sige_barriers(theta)
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "start.dat")
+        write_startdat(p, E, D, ncrystal=2, list_crystal=(14, 32), len1=LEN1, lens=BOX[:2],
+                       alloy_fraction=XGE)
+        txt = open(p).read()
+    mat = la.Material()
+    zsurf = LEN1 - LEN1 % 24 - 3
+    lap = dict(P0=list(mat.P0) + [0.0], Tm=list(mat.Tm) + [mat.Tm[-1]], Tflex=list(mat.Tflex) + [mat.Tflex[-1]],
+               sigma=list(mat.A) + [mat.A[-1]], zsurf=float(zsurf), tau=_tau(theta), phase=8, **PULSE)
+    jobs = [(txt, BOX, XGE, 7000 + i, lap, E, dE, D, dD, 9000 + i, [T1, T2]) for i in range(N)]
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        res = pool.map(oracle_lib.la_replica, jobs, chunksize=8)
+    c1 = np.array([r[0][0] for r in res])
+    c2 = np.array([r[1][0] for r in res])
+    score = np.array([r[1][1] for r in res])
+    events = np.array([r[1][2] for r in res])
+    f = (c2.sum(1) - c1.sum(1)).astype(np.float64)
+    fc = f - f.mean()
+    gx = (fc[:, None] * score) * N / (N - 1)
+    return dict(c1=c1, c2=c2, score=score, f=f, g=gx.mean(0), se=gx.std(0, ddof=1) / math.sqrt(N), events=events)
+
+
+def _band(x, y, k=3.0):
+    d = x.mean() - y.mean()
+    se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
+    return d, k * se
+
+
+def test_la_crystal_matches_oracle(gpu, oracle):
+    c0 = gpu["sim"].c0.astype(float)
+    print("\ntau", gpu["tau"], "events/replica gpu", gpu["events"].mean(), "oracle", oracle["events"].mean())
+    for name, xg, xo in (("crystal(10ns)", gpu["c1"].sum(1) - c0, oracle["c1"].sum(1) - c0),
+                         ("crystal(20ns)", gpu["c2"].sum(1) - c0, oracle["c2"].sum(1) - c0),
+                         ("Ge(20ns)", gpu["c2"][:, 1], oracle["c2"][:, 1])):
+        d, b = _band(xg.astype(float), xo.astype(float))
+        print(f"{name}: gpu {xg.mean():.2f} oracle {xo.mean():.2f} diff {d:.2f} band +-{b:.2f}")
+        assert abs(d) < b, name
+    # molten material exists and the liquid fractions in use are fractions
+    assert (gpu["c2"].sum(1) < c0).mean() > 0.9
+    x = gpu["x2"]
+    live = x.sum(1) > 0
+    assert live.mean() > 0.9 and np.allclose(x[live].sum(1), 1.0, atol=1e-5)
+
+
+def test_la_score_mean_zero(gpu, oracle):
+    for name, s in (("gpu", gpu["score"]), ("oracle", oracle["score"])):
+        m = s.mean(0)
+        se = s.std(0, ddof=1) / math.sqrt(len(s))
+        print(f"\nE[S] {name}: {m} se {se}")
+        assert np.all(np.abs(m) < 4.0 * se), name
+        assert np.all(se > 0)
+
+
+def test_la_lr_gradient(gpu, oracle, theta):
+    sim = gpu["sim"]
+    tau = gpu["tau"]
+    fd = np.zeros(4)
+    fd_se = np.zeros(4)
+    for j in range(4):
+        e = np.zeros(4)
+        e[j] = H
+        c1p, c2p, _ = _gpu_run(sim, theta + e, tau, score=False)
+        c1m, c2m, _ = _gpu_run(sim, theta - e, tau, score=False)
+        dp = (c2p.sum(1) - c1p.sum(1)).astype(float)
+        dm = (c2m.sum(1) - c1m.sum(1)).astype(float)
+        q = (dp - dm) / (2 * H)
+        fd[j] = q.mean()
+        fd_se[j] = q.std(ddof=1) / math.sqrt(len(q))
+    print("\nLR gpu   ", gpu["g"], "+-", gpu["se"])
+    print("LR oracle", oracle["g"], "+-", oracle["se"])
+    print("CRN FD   ", fd, "+-", fd_se)
+    for j in range(4):
+        b1 = 3.0 * math.hypot(gpu["se"][j], oracle["se"][j])
+        b2 = 3.0 * math.hypot(gpu["se"][j], fd_se[j])
+        assert abs(gpu["g"][j] - oracle["g"][j]) < b1, j
+        assert abs(gpu["g"][j] - fd[j]) < b2, j
+    # the test resolves a gradient
+    assert np.max(np.abs(fd) / fd_se) > 4.0
+
+
+def test_la_schedules_agree(theta):
+    """Per-colour launches and the persistent kernel give the same lattices;
+    the FP64 score sums agree to rounding (atomic order)."""
+    res = []
+    for sched in (0, 1):
+        sim = _sim(n=16, seed=5)
+        sim.batch.set_schedule(sched)
+        c1, c2, _ = _gpu_run(sim, theta, _tau(theta))
+        res.append((c2, sim.batch.score()))
+        sim.batch.close()
+    assert np.array_equal(res[0][0], res[1][0])
+    np.testing.assert_allclose(res[0][1], res[1][1], rtol=1e-9, atol=1e-9)
