@@ -155,6 +155,9 @@ int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1);
 int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
                   int64_t max_events_each, double max_time_each, int64_t *events_total);
 int mks_batch_observables(mks_handle *h, mks_observables *obs /* n entries */);
+/* Class histogram of every replica (n * nclass, nclass >= 63), the
+ * per-replica view of mks_class_histogram.                               */
+int mks_batch_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
 int32_t mks_batch_size(mks_handle *h);
 
 /* Tile width (sites, 4..8) of the sublattice decomposition; the default

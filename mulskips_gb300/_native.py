@@ -88,6 +88,7 @@ SIGNATURES = {
     "mks_batch_set_la": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_batch_get_score": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_batch_la_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mks_batch_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mks_batch_init_alloy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "mks_last_run_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),

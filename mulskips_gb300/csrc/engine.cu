@@ -132,11 +132,19 @@ __device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
     if (c == CLS_C1D) return 1.e-8f;
     return 0.f;
 }
+// Empty sites above the initial surface are vacuum, not liquid: nothing
+// solidifies there (the liquid of the reference's LA runs is the molten part
+// of the initially occupied domain, LaserAnnealing main.f:597-637)
+__device__ __forceinline__ bool la_vacuum(const LADev &A, int c, int z1)
+{
+    return (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) && 3.f * (float)z1 > A.zsurf;
+}
 // d(rate)/d theta_j of one site of class c at temperature T (isolated atoms,
 // whose rate is a numerical device of the reference, are left out)
-__device__ __forceinline__ void la_drate(const LADev &A, int c, float T, float d[4])
+__device__ __forceinline__ void la_drate(const LADev &A, int c, float T, float d[4], bool vac = false)
 {
     d[0] = d[1] = d[2] = d[3] = 0.f;
+    if (vac) return;
     if (c >= CLS_OCC0) {
         float k = la_rate(A, c, T);
         for (int j = 0; j < 4; j++) d[j] = -k * A.dE[c][j] / (KB_EV_F * T);
@@ -450,7 +458,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
                 if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
                 if (A) {
                     float d[4];
-                    la_drate(*A, cls, la_temp(*A, z, t_mid), d);
+                    la_drate(*A, cls, la_temp(*A, z, t_mid), d, la_vacuum(*A, cls, z));
                     for (int j = 0; j < 4; j++) g[j] += d[j];
                 }
             }
@@ -591,7 +599,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             // thinning: the class rate is the tile's bound; accept with k(T_site)/bound
             Tsite = la_temp(*A, z, t_mid);
             if (cls != CLS_ISO) {
-                float r_true = la_rate(*A, cls, Tsite);
+                float r_true = la_vacuum(*A, cls, z) ? 0.f : la_rate(*A, cls, Tsite);
                 float uu = u01(rnd.y) * (float)S.cnt[cls];
                 float uacc = uu - floorf(uu);
                 if (!(uacc * S.rate[cls] < r_true)) continue;   // null event: time only
@@ -685,8 +693,8 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             float dn[4] = {0.f, 0.f, 0.f, 0.f}, dold[4] = {0.f, 0.f, 0.f, 0.f};
             if (interior && old_cls != ncls) {
                 float Tt = la_temp(*A, tz, t_mid);
-                la_drate(*A, ncls, Tt, dn);
-                la_drate(*A, old_cls, Tt, dold);
+                la_drate(*A, ncls, Tt, dn, la_vacuum(*A, ncls, tz));
+                la_drate(*A, old_cls, Tt, dold, la_vacuum(*A, old_cls, tz));
             }
             for (int j = 0; j < 4; j++) {
                 float v = dn[j] - dold[j];
@@ -2116,6 +2124,25 @@ int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
     cudaFreeAsync(d_hist, h->stream);
     CK(cudaStreamSynchronize(h->stream));
     for (int i = 0; i < nclass; i++) hist[i] = i < NCLASS ? (int64_t)tmp[i] : 0;
+    return 0;
+}
+
+int mks_batch_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
+{
+    if (!h || !hist || nclass < NCLASS) return fail(MKS_ERR_ARG, "bad arguments");
+    size_t n = h->reps.size(), nb = sizeof(unsigned long long) * NCLASS;
+    unsigned long long *d_hist = nullptr;
+    CK(cudaMallocAsync(&d_hist, nb * n, h->stream));
+    CK(cudaMemsetAsync(d_hist, 0, nb * n, h->stream));
+    for (size_t i = 0; i < n; i++)
+        k_class_hist<<<256, 256, 0, h->stream>>>(h->d_reps, (int)i, h->d_st, d_hist + i * NCLASS);
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> tmp(NCLASS * n);
+    CK(cudaMemcpyAsync(tmp.data(), d_hist, nb * n, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_hist, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t r = 0; r < n; r++)
+        for (int i = 0; i < nclass; i++) hist[r * nclass + i] = i < NCLASS ? (int64_t)tmp[r * NCLASS + i] : 0;
     return 0;
 }
 

@@ -220,6 +220,12 @@ class Batch:
         return {"kernel_launches": k.value, "graph_launches": g.value, "kernel_ms": ms.value,
                 "phase_launches": p.value}
 
+    def class_histogram(self):
+        """(n, 63) event sites per rate class of every replica."""
+        h = np.zeros((self.n, 63), dtype=np.int64)
+        N.check(N.lib().mks_batch_class_histogram(self._h, N.ptr(h), 63))
+        return h
+
     # ---- laser anneal (LA) mode ----
     def init_alloy(self, len1, x, seed):
         """SetSi-like slabs with species 2 substituted at fraction x[i]."""

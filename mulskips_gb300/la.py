@@ -143,6 +143,54 @@ def max_rate(theta, mat, T_peak):
     return r
 
 
+# rate classes of the engine (mulskips_gb300/csrc/lattice.cuh)
+CLS_C1, CLS_C1D, CLS_C2, CLS_C3, CLS_ISO, CLS_OCC0, NCENSUS, NCLASS = 1, 2, 3, 4, 5, 6, 19, 63
+
+
+def census_index(n1, n2, n3):
+    """Index of the neighbour census (n1, n2, n3), 1 <= sum <= 3, ordered by
+    total, then n1 and n2 descending (the engine's enumeration)."""
+    t = n1 + n2 + n3
+    k = {1: 0, 2: 3, 3: 9}[t]
+    for a in range(t, n1, -1):
+        k += t - a + 1
+    return k + (t - n1) - n2
+
+
+def class_rates(theta, mat, T, xliq=(1.0, 1.0, 1.0)):
+    """Rate of one site of every engine class under the LA law at
+    temperature T (liquid fractions xliq for the solidification classes)."""
+    E, _, Ed, _ = sige_barriers(theta)
+    r = np.zeros(NCLASS)
+    for sp in (0, 1):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                for n3 in range(4 - n1 - n2):
+                    if n1 + n2 + n3 == 0:
+                        continue
+                    e = E[sp, n1, n2, n3, 0, 0, 0]
+                    if e:
+                        r[CLS_OCC0 + sp * NCENSUS + census_index(n1, n2, n3)] = \
+                            mat.P0[sp] * math.exp(-e / (KB_EV * T))
+    for co, cls in ((1, CLS_C1), (2, CLS_C2), (3, CLS_C3)):
+        for sp in (0, 1):
+            d = Ed[sp, co - 1]
+            if d:
+                r[cls] += 0.5 * mat.P0[sp] * xliq[sp] * math.exp(-d / (KB_EV * mat.Tm[sp])) * \
+                    (1.0 + math.erf((T - mat.Tflex[sp]) / mat.A[sp]))
+    r[CLS_C1D] = 1e-8
+    return r
+
+
+def share_rate(hist, rates):
+    """Rate of the class carrying the largest share of the total rate (the
+    isolated-atom and dummy classes left out), per replica."""
+    w = hist.astype(np.float64) * rates[None, :]
+    w[:, CLS_ISO] = 0.0
+    w[:, CLS_C1D] = 0.0
+    return rates[np.argmax(w, axis=1)]
+
+
 @dataclass
 class Anneal:
     """A batch of SiGe LA replicas: box (LenX, LenY, LenZ) grid units, slab
@@ -156,6 +204,7 @@ class Anneal:
     pulse: Pulse = field(default_factory=Pulse)
     f_tau: float = 0.3
     sf: float = 5.43 / 12
+    tau_rule: str = "share"     # "share": dominant class; "max": fastest class
 
     def __post_init__(self):
         self.batch = Batch([self.box] * self.n, [self.seed * 1000003 + i for i in range(self.n)], ncrystal=2,
@@ -177,21 +226,45 @@ class Anneal:
         p = la_params(self.mat, self.pulse, self.zsurf, score)
         b.set_la(p, np.broadcast_to(dE, (self.n,) + dE.shape) if score else None,
                  np.broadcast_to(dEd, (self.n,) + dEd.shape) if score else None)
-        T_peak = self.pulse.Tb + self.pulse.Ta
-        self.tau = tau if tau else self.f_tau / max_rate(theta, self.mat, T_peak)
+        self.tau_fixed = tau
         self.t = 0.0
         self.c0 = b.la_counts()[0].sum(axis=1)
 
-    def advance(self, t_end):
-        """Run every replica to time t_end (windows of length <= tau ending
-        exactly at t_end, a multiple of 8 of them)."""
-        dt = t_end - self.t
-        if dt <= 0:
-            return 0
-        nw = max(8, int(math.ceil(dt / self.tau / 8.0 - 1e-9)) * 8)
-        tau = dt / nw
-        ev = self.batch.run(tau, nw, 0, self.t + dt - 0.5 * tau)
-        self.t = t_end
+    def tau_at(self, ta, tb):
+        """Window length for [ta, tb] at the hottest surface temperature the
+        pulse reaches in that interval: f_tau over the rate of the class
+        carrying the largest share of the current event sites' total rate
+        (rule "share", the accuracy rule of the plain model), or over the
+        fastest rate the law allows (rule "max"); one length for the batch."""
+        p = self.pulse
+        tc = min(max(p.t0, ta), tb)
+        T_max = p.Tb + p.Ta * math.exp(-((tc - p.t0) / p.w) ** 2)
+        if self.tau_rule == "max":
+            return self.f_tau / max_rate(self.theta, self.mat, T_max)
+        r = share_rate(self.batch.class_histogram(), class_rates(self.theta, self.mat, T_max))
+        return self.f_tau / float(np.max(r))
+
+    def advance(self, t_end, segment=1e-9):
+        """Run every replica to time t_end in segments, each cut into a
+        multiple of 8 windows no longer than its tau (the fixed tau given to
+        start, else tau_at of the segment) and ending exactly at the segment
+        end.  A segment is `segment` long, or 8 windows when those are
+        longer (cold stretches of the pulse)."""
+        ev = 0
+        while self.t < t_end * (1.0 - 1e-12):
+            if self.tau_fixed:
+                te, tau0 = t_end, self.tau_fixed
+            else:
+                te = min(t_end, self.t + segment)
+                tau0 = self.tau_at(self.t, te)
+                if 8.0 * tau0 > te - self.t and te < t_end:
+                    te = min(t_end, self.t + 8.0 * tau0)
+                    tau0 = min(tau0, self.tau_at(self.t, te))
+            dt = te - self.t
+            nw = max(8, int(math.ceil(dt / tau0 / 8.0 - 1e-9)) * 8)
+            tau = dt / nw
+            ev += self.batch.run(tau, nw, 0, self.t + dt - 0.5 * tau)
+            self.t = te
         return ev
 
     def crystal(self):
@@ -205,7 +278,8 @@ class Anneal:
         n1 = self.crystal()
         self.advance(t2)
         n2 = self.crystal()
-        return (n2 - n1).astype(np.float64) / self.area * self.layer_nm * 1e-9 / (t2 - t1)
+        self.last_v = (n2 - n1).astype(np.float64) / self.area * self.layer_nm * 1e-9 / (t2 - t1)
+        return self.last_v
 
 
 def regrowth_velocity_lr(sim, theta, t1, t2):

@@ -108,6 +108,7 @@ struct ora {
     int la_stop;
     double *la_k, *la_dk, *la_ps;           /* per-MC-particle rates of the last scan */
     int *la_kind, la_cap;
+    int la_cur_z;                           /* grid z of the site whose rate la2_pd evaluates */
     char init_st[3], run_type[3], exit_strategy[5];
     char save_final[3], save_coo[3];
     char restartfile[2048], coofile[2048];
@@ -442,7 +443,8 @@ static int la2_temp(ora_t *o, int z)
 static double la2_pd(ora_t *o, int s, int coor, int temperature)
 {
     double v = o->ptransD[s - 1][coor - 1];
-    if (v == 0.0 || !(o->xliq[s - 1] > 0.0)) return 0.0;
+    /* empty sites above the initial surface are vacuum, not liquid */
+    if (v == 0.0 || !(o->xliq[s - 1] > 0.0) || (double)o->la_cur_z > o->lap.zsurf) return 0.0;
     return 0.5 * o->lap.P0[s - 1] * o->xliq[s - 1] * exp(-v / (KB * o->lap.Tm[s - 1])) *
            (1.0 + erf(((double)temperature - o->lap.Tflex[s - 1]) / o->lap.sigma[s - 1]));
 }
@@ -498,6 +500,7 @@ static void get_prob(ora_t *o, int occ, int nsic, int covind, int coor,
     int la = (o->init_st[0] == 'L' && o->init_st[1] == 'A');
     if (o->la2) {
         temperature = la2_temp(o, site[2]);
+        o->la_cur_z = site[2];
     } else if (la) {
         temperature = ibits(*LC(o, site), POS_T, LEN_T);
         if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob()");
@@ -2076,6 +2079,7 @@ static int la2_rate(ora_t *o, int ind, double *k, double dk[4], double ps[3])
         return LK_DUMMY;
     }
     if (coor < 1 || coor > 3) return LK_NONE;
+    o->la_cur_z = m->xyz[2];
     for (int s = 0; s < 3; s++) {
         ps[s] = la2_pd(o, s + 1, coor, T);
         *k += ps[s];

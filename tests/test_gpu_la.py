@@ -74,8 +74,19 @@ def gpu(theta):
     sim.batch.close()
 
 
-@pytest.fixture(scope="module")
-def oracle(oracle_lib, theta):
+def _share_tau(theta):
+    """Window length of the dominant-share rule at the start of the run,
+    rounded so that T1 is a multiple of 8 windows."""
+    from mulskips_gb300 import la
+    sim = _sim(n=64, seed=8)
+    sim.start(theta, score=False, tau=1.0)
+    r = la.share_rate(sim.batch.class_histogram(), la.class_rates(theta, sim.mat, PULSE["Tb"] + PULSE["Ta"]))
+    sim.batch.close()
+    k = math.ceil(T1 / 8.0 / (0.3 / float(np.max(r))))
+    return T1 / (8.0 * k)
+
+
+def _oracle_sample(ora, theta, tau):
     from mulskips_gb300 import la
     from mulskips_gb300.startdat import write_startdat
     import tempfile
@@ -88,10 +99,10 @@ def oracle(oracle_lib, theta):
     mat = la.Material()
     zsurf = LEN1 - LEN1 % 24 - 3
     lap = dict(P0=list(mat.P0) + [0.0], Tm=list(mat.Tm) + [mat.Tm[-1]], Tflex=list(mat.Tflex) + [mat.Tflex[-1]],
-               sigma=list(mat.A) + [mat.A[-1]], zsurf=float(zsurf), tau=_tau(theta), phase=8, **PULSE)
+               sigma=list(mat.A) + [mat.A[-1]], zsurf=float(zsurf), tau=tau, phase=8, **PULSE)
     jobs = [(txt, BOX, XGE, 7000 + i, lap, E, dE, D, dD, 9000 + i, [T1, T2]) for i in range(N)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        res = pool.map(oracle_lib.la_replica, jobs, chunksize=8)
+        res = pool.map(ora.la_replica, jobs, chunksize=8)
     c1 = np.array([r[0][0] for r in res])
     c2 = np.array([r[1][0] for r in res])
     score = np.array([r[1][1] for r in res])
@@ -100,6 +111,11 @@ def oracle(oracle_lib, theta):
     fc = f - f.mean()
     gx = (fc[:, None] * score) * N / (N - 1)
     return dict(c1=c1, c2=c2, score=score, f=f, g=gx.mean(0), se=gx.std(0, ddof=1) / math.sqrt(N), events=events)
+
+
+@pytest.fixture(scope="module")
+def oracle(oracle_lib, theta):
+    return _oracle_sample(oracle_lib, theta, _tau(theta))
 
 
 def _band(x, y, k=3.0):
@@ -122,6 +138,25 @@ def test_la_crystal_matches_oracle(gpu, oracle):
     x = gpu["x2"]
     live = x.sum(1) > 0
     assert live.mean() > 0.9 and np.allclose(x[live].sum(1), 1.0, atol=1e-5)
+
+
+def test_la_share_tau_matches_oracle(oracle_lib, theta):
+    """Windows of the dominant-share rule (f = 0.3 of the class carrying the
+    largest share of the rate, about 75x longer than the fastest-class
+    rule here): same observables, same bands."""
+    tau = _share_tau(theta)
+    sim = _sim(seed=9)
+    c1, c2, _ = _gpu_run(sim, theta, tau, score=False)
+    c0 = sim.c0.astype(float)
+    sim.batch.close()
+    o = _oracle_sample(oracle_lib, theta, tau)
+    print(f"\nshare-rule tau {tau:.3e} (fastest-class rule {_tau(theta):.3e})")
+    for name, xg, xo in (("crystal(10ns)", c1.sum(1) - c0, o["c1"].sum(1) - c0),
+                         ("crystal(20ns)", c2.sum(1) - c0, o["c2"].sum(1) - c0),
+                         ("Ge(20ns)", c2[:, 1], o["c2"][:, 1])):
+        d, b = _band(xg.astype(float), xo.astype(float))
+        print(f"{name}: gpu {xg.mean():.2f} oracle {xo.mean():.2f} diff {d:.2f} band +-{b:.2f}")
+        assert abs(d) < b, name
 
 
 def test_la_score_mean_zero(gpu, oracle):
@@ -172,3 +207,19 @@ def test_la_schedules_agree(theta):
         sim.batch.close()
     assert np.array_equal(res[0][0], res[1][0])
     np.testing.assert_allclose(res[0][1], res[1][1], rtol=1e-9, atol=1e-9)
+
+
+def test_autograd_function(theta):
+    """torch.autograd.Function: forward = mean regrowth velocity of the batch,
+    backward = the LR gradient the GPU reduction returns for it."""
+    torch = pytest.importorskip("torch")
+    from mulskips_gb300 import la
+    sim = _sim(n=64, seed=6)
+    th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+    v = la.regrowth_velocity(th, sim, T1, T2)
+    assert v.dim() == 0 and abs(float(v) - sim.last_v.mean()) < 1e-12 * max(1.0, abs(float(v)))
+    v.backward()
+    g, se = sim.batch.lr_grad(sim.last_v)
+    np.testing.assert_allclose(th.grad.numpy(), g, rtol=1e-12, atol=0)
+    assert np.all(np.isfinite(g)) and np.all(se > 0)
+    sim.batch.close()

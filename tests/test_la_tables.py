@@ -90,3 +90,30 @@ def test_la_params_struct():
     assert p.P0[0] == pytest.approx(1e13) and p.P0[2] == 0.0
     assert p.Tm[1] == pytest.approx(1210.0) and p.sigma[0] == pytest.approx(300.0)
     assert p.t0 == pytest.approx(100e-9) and p.L_nm == pytest.approx(200.0) and p.score == 1
+
+
+def test_census_index_enumeration():
+    seen = []
+    for t in (1, 2, 3):
+        for n1 in range(t, -1, -1):
+            for n2 in range(t - n1, -1, -1):
+                seen.append(la.census_index(n1, n2, t - n1 - n2))
+    assert seen == list(range(la.NCENSUS))
+
+
+def test_class_rates_and_share():
+    mat = la.Material()
+    r = la.class_rates(la.THETA_REF, mat, 1750.0)
+    kb = la.KB_EV
+    # Si atom with two Si (or wall) neighbours, Ge atom with two Ge neighbours
+    si2 = la.CLS_OCC0 + la.census_index(2, 0, 0)
+    ge2 = la.CLS_OCC0 + la.NCENSUS + la.census_index(0, 2, 0)
+    assert r[si2] == pytest.approx(1e13 * np.exp(-1.8 / (kb * 1750.0)), rel=1e-12)
+    assert r[ge2] == pytest.approx(1e13 * np.exp(-1.3 / (kb * 1750.0)), rel=1e-12)
+    assert r[la.CLS_C1D] == 1e-8 and r[la.CLS_ISO] == 0.0
+    hist = np.zeros((2, la.NCLASS), dtype=np.int64)
+    hist[0, si2] = 1000
+    hist[0, ge2] = 1
+    hist[1, ge2] = 1000
+    hist[:, la.CLS_ISO] = 10 ** 6
+    np.testing.assert_allclose(la.share_rate(hist, r), [r[si2], r[ge2]])
