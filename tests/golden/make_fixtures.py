@@ -11,6 +11,9 @@ Fixtures written:
   <case>/start.dat       regression-tests/input-and-references-files/start-<case>.dat
   <case>/I00000000.xyz.gz, I00000001.xyz.gz, log.txt
                          the reference's own regression outputs for that case
+  refwriter/start.dat    start.dat written by the reference's
+                         pymulskips.setuprun.run_mulskips (setup_only) for the
+                         plain Si(001) process object of mulskips_gb300.setuprun
 """
 import gzip
 import os
@@ -40,10 +43,39 @@ def cases():
         shutil.copyfile(os.path.join(RT, f"log-{case}.txt"), os.path.join(d, "log.txt"))
         for fr in ("I00000000", "I00000001"):
             with open(os.path.join(RT, f"{fr}-{case}.xyz"), "rb") as fi, \
-                    gzip.open(os.path.join(d, f"{fr}.xyz.gz"), "wb", compresslevel=9) as fo:
+                    gzip.GzipFile(os.path.join(d, f"{fr}.xyz.gz"), "wb", compresslevel=9, mtime=0) as fo:
                 fo.write(fi.read())
+
+
+def reference_writer():
+    import sys
+    import tempfile
+    import warnings
+    sys.path.insert(0, REF)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import pymulskips.setuprun as ref_setup
+    from mulskips_gb300.setuprun import PlainSi
+
+    class PVD(PlainSi):    # the reference dispatches on the class name
+        pass
+
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        try:
+            ref_setup.run_mulskips(execpath=tmp, runpath=os.path.join(tmp, "ref"), Simulation="FS",
+                                   mp=PVD(T=1100.0), PtransZig=1.0, ExitStrategy="Iter", OutMolMol=1000,
+                                   IterMax=100000, Seed_box=[120, 120, 120], RunType="R", IDUM=5,
+                                   setup_only=True)
+        finally:
+            os.chdir(cwd)
+        d = os.path.join(HERE, "refwriter")
+        os.makedirs(d, exist_ok=True)
+        shutil.copyfile(os.path.join(tmp, "ref", "start.dat"), os.path.join(d, "start.dat"))
 
 
 if __name__ == "__main__":
     numbers_list()
     cases()
+    reference_writer()

@@ -4,15 +4,11 @@ pymulskips.setuprun.run_mulskips writes for the same process object; the
 reader agrees with the oracle's parser; setup_mulskips_src leaves the
 make.log line the reference checks."""
 import os
-import sys
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN
-
-REF = os.environ.get("MULSKIPS_REF", "/root/reference")
-
 
 def first_tokens(path):
     out = []
@@ -23,29 +19,18 @@ def first_tokens(path):
 
 
 def test_startdat_matches_reference_writer(tmp_path):
-    if not os.path.isdir(os.path.join(REF, "pymulskips")):
-        pytest.skip("reference pymulskips not present")
-    sys.path.insert(0, REF)
-    import warnings
-    with warnings.catch_warnings():
-        warnings.simplefilter("ignore")
-        import pymulskips.setuprun as ref_setup
+    """tests/golden/refwriter/start.dat was written by the reference's
+    pymulskips.setuprun.run_mulskips(setup_only=True) for the same process
+    object and arguments (tests/golden/make_fixtures.py)."""
     from mulskips_gb300.setuprun import PlainSi, run_mulskips
 
-    class PVD(PlainSi):    # the reference dispatches on the class name
+    class PVD(PlainSi):
         pass
 
-    mp = PVD(T=1100.0)
-    cwd = os.getcwd()
-    try:
-        ref_setup.run_mulskips(execpath=str(tmp_path), runpath=str(tmp_path / "ref"), Simulation="FS", mp=mp,
-                               PtransZig=1.0, ExitStrategy="Iter", OutMolMol=1000, IterMax=100000,
-                               Seed_box=[120, 120, 120], RunType="R", IDUM=5, setup_only=True)
-    finally:
-        os.chdir(cwd)
-    run_mulskips(runpath=str(tmp_path / "ours"), Simulation="FS", mp=mp, PtransZig=1.0, ExitStrategy="Iter",
-                 OutMolMol=1000, IterMax=100000, Seed_box=[120, 120, 120], RunType="R", IDUM=5, setup_only=True)
-    a = first_tokens(tmp_path / "ref" / "start.dat")
+    run_mulskips(runpath=str(tmp_path / "ours"), Simulation="FS", mp=PVD(T=1100.0), PtransZig=1.0,
+                 ExitStrategy="Iter", OutMolMol=1000, IterMax=100000, Seed_box=[120, 120, 120], RunType="R",
+                 IDUM=5, setup_only=True)
+    a = first_tokens(os.path.join(GOLDEN, "refwriter", "start.dat"))
     b = first_tokens(tmp_path / "ours" / "start.dat")
     assert a == b
 

@@ -57,7 +57,10 @@ def oracle_sample(oracle_lib, tmp_path_factory):
     return np.array([oracle_atoms(oracle_lib, tmp, 100 + s) for s in range(NSEEDS)], dtype=float)
 
 
-@pytest.mark.parametrize("tau", [2e-9])
+# k2 = 1e13 exp(-1.2 eV / kT) at 1100 K is the coor-2 evaporation rate: 2e-9 s
+# is k2 tau = 0.064; T_OBS / 43 is k2 tau = 0.296, the f = 0.3 window rule of
+# the engine's tau suggestion
+@pytest.mark.parametrize("tau", [2e-9, T_OBS / 43])
 def test_etch_rate_matches_serial_reference(oracle_sample, tau):
     g = gpu_atoms(tau, [1 + s for s in range(NSEEDS)])
     d, hw = band(g, oracle_sample)
