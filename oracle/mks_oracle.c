@@ -94,8 +94,11 @@ struct ora {
     double ptrans_zig;
     double sf;
     double alloyfraction;
-    /* LA law parameters (MS/modules/definitions.f:30) */
+    /* LA law parameters (MS/modules/definitions.f:30) and the LA start.dat
+     * block (MS/main.f:118-138) */
     double Tm, P0, sigma, Tflex;
+    double len_vac, len_nuc;
+    char homogeneous[3];
     /* per-species LA law with liquid fractions and the LR score (ora_la_*) */
     int la2;
     ora_la_t lap;
@@ -109,6 +112,8 @@ struct ora {
     double *la_k, *la_dk, *la_ps;           /* per-MC-particle rates of the last scan */
     int *la_kind, la_cap;
     int la_cur_z;                           /* grid z of the site whose rate la2_pd evaluates */
+    int8_t *la_geo;                         /* InitSt LA input (ora_set_la_input) */
+    int16_t *la_tsub;
     char init_st[3], run_type[3], exit_strategy[5];
     char save_final[3], save_coo[3];
     char restartfile[2048], coofile[2048];
@@ -1181,6 +1186,198 @@ static void set_flat(ora_t *o, int len, int sic)
     if (!sic) set_walls(o, o->lz - 6, o->lz - 1);
 }
 
+/* Get_Prob_Ini, MS/mcevent/Get_Prob_Ini.f:23-161: init-time rate of a site
+ * (no reciprocity check; walls counted by their index; dummy rate 1e-6). */
+static void get_prob_ini(ora_t *o, int occ, int nsic, int coor, const int site[3], int nextn[4][3],
+                         int *index_event, double *prob_event)
+{
+    int temperature = 0;
+    if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
+        temperature = ibits(*LC(o, site), POS_T, LEN_T);
+        if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob_ini()");
+    }
+    *index_event = 0;
+    *prob_event = 0.0;
+    if (occ == 0) {
+        int draw = 0;
+        if (coor == 1) {
+            int coornn = ibits(*LC(o, nextn[0]), POS_COOR, LEN_COOR);
+            if (coornn >= 2) draw = 1;
+            else { *index_event = 1; *prob_event = (double)1.e-6f; }
+        } else if (coor == 2 || coor == 3) {
+            draw = 1;
+        } else if (coor == 4) {
+            lg(o, " %d Get Prob Vacancy Generation\n", coor);
+        }
+        if (draw) {
+            double pd1 = pd_entry(o, 1, coor, temperature), pd2 = pd_entry(o, 2, coor, temperature);
+            double pd3 = pd_entry(o, 3, coor, temperature);
+            double ptot = pd1 + pd2 + pd3;
+            double pcurr = rnd(o) * ptot;
+            if (pcurr <= pd1) *index_event = 1;
+            else if (pcurr > pd1 + pd2) *index_event = 3;
+            else *index_event = 2;
+            *prob_event = ptot;
+        }
+    } else {
+        int n_si = 0, n_c = 0, n_b = 0, n_cov = 0;
+        for (int i = 0; i < 4; i++) {
+            int32_t v = *LC(o, nextn[i]);
+            if (ibits(v, POS_INDEX, LEN_INDEX) == 0) {
+                int sp = ibits(v, POS_SIC, LEN_SIC);
+                if (sp == 1) n_si++;
+                if (sp == 2) n_c++;
+                if (sp == 3) n_b++;
+            } else {
+                n_cov++;
+            }
+        }
+        int tot = n_si + n_c + n_b + n_cov;
+        if (tot != coor) ora_fail(o, "Get Prob Error N_Si+N_C++N_B+N_cov.NE.Coor at %d %d %d", site[0], site[1], site[2]);
+        if (tot > 3) {
+            *index_event = 0;
+            *prob_event = 0.0;
+        } else if (tot == 0) {
+            *index_event = 4;
+            *prob_event = 100000.0 * o->tree[1];
+        } else {
+            *index_event = 4;
+            *prob_event = pe_entry(o, nsic, n_si + n_cov, n_c, n_b, 0, 0, 0, temperature);
+        }
+    }
+}
+
+/* SetT + SetCAD for InitSt 'LA' (MS/initial/SetT.f:25-50,
+ * MS/initial/SetCAD.f:24-421, fresh start): geometry id per layer z
+ * (`geo[z]`, 1 = Si, 10 = wall/air, as LattGeo; a layer-uniform geometry)
+ * and the temperature (K) of the grid points whose coordinates are all
+ * multiples of 3, `tsub[((z/3)*(ly/3) + y/3)*(lx/3) + x/3]` (TempStat; 10
+ * marks a wall and is not stored).  Only NCrystal = 1, no alloy. */
+static void set_cad_la(ora_t *o, const int8_t *geo, const int16_t *tsub)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz, nx3 = lx / 3, ny3 = ly / 3;
+    /* SetT */
+    for (int z = 0; z < lz; z += 3)
+        for (int y = 0; y < ly; y += 3)
+            for (int x = 0; x < lx; x += 3) {
+                int t = tsub[((size_t)(z / 3) * ny3 + y / 3) * nx3 + x / 3];
+                if (t != 10) mvbits(t, LEN_T, &o->latt[lidx(o, x, y, z)], POS_T);
+            }
+    /* walls of SetCAD.f:137-153 and the geometry of :160-236 */
+    for (int z = 0; z < lz; z++) {
+        int wall = (z <= 3 || z >= lz - 4) || geo[z] == 10;
+        int si = !wall && geo[z] == 1;
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (wall) {
+                    *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
+                    mvbits(WALL, LEN_INDEX, v, POS_INDEX);
+                } else if (si && dia_kind(x, y, z)) {
+                    int occ;
+                    if (o->homogeneous[0] == 'T') {
+                        occ = z <= lz - (int)((o->len_vac + o->len_nuc) / o->sf);
+                    } else {
+                        int x0 = lx / 2, y0 = ly / 2, z0 = lz - (int)(o->len_vac / o->sf);
+                        long d2 = (long)(x - x0) * (x - x0) + (long)(y - y0) * (y - y0) + (long)(z - z0) * (z - z0);
+                        occ = d2 > (long)((o->len_nuc / o->sf) * (o->len_nuc / o->sf));
+                    }
+                    if (occ) *v = (int32_t)((uint32_t)*v | (1u << POS_OCC) | (1u << POS_SI));
+                }
+            }
+    }
+    int site[3], nextn[4][3];
+    /* coordinations, removal of isolated atoms (SetCAD.f:241-341) */
+    for (int z = 0; z < lz; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (ibits(*v, POS_INDEX, LEN_INDEX) == WALL) continue;
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int occ = ibits(*v, POS_OCC, LEN_OCC), coor = 0;
+                for (int i = 0; i < 4; i++) {
+                    int32_t w = *LC(o, nextn[i]);
+                    int occn = ibits(w, POS_OCC, LEN_OCC);
+                    if (occ > 0) {
+                        if (occn > 0) coor++;
+                    } else if (occn > 0 && ibits(w, POS_INDEX, LEN_INDEX) != WALL) {
+                        coor++;
+                    }
+                }
+                if (occ != 0 && coor == 0) {
+                    int t = ibits(*v, POS_T, LEN_T);
+                    *v = 0;
+                    mvbits(t, LEN_T, v, POS_T);
+                    for (int i = 0; i < 4; i++) {
+                        int32_t *w = LC(o, nextn[i]);
+                        int cn = ibits(*w, POS_COOR, LEN_COOR) - 1;
+                        if (cn < 0) cn = 0;
+                        mvbits(cn, LEN_COOR, w, POS_COOR);
+                    }
+                } else {
+                    mvbits(coor, LEN_COOR, v, POS_COOR);
+                }
+            }
+    /* lists and first rates (SetCAD.f:344-421) */
+    int nbuff[3] = {0, 0, 0};
+    for (int z = 0; z < lz; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (ibits(v, POS_INDEX, LEN_INDEX) == WALL) continue;
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int occ = ibits(v, POS_OCC, LEN_OCC), coor = ibits(v, POS_COOR, LEN_COOR);
+                int index_event;
+                double prob;
+                if (occ == 0) {
+                    if (coor == 0) continue;
+                    if (coor == 1) {
+                        for (int i = 0; i < 4; i++) {
+                            int32_t w = *LC(o, nextn[i]);
+                            if (ibits(w, POS_OCC, LEN_OCC) != 0 && ibits(w, POS_INDEX, LEN_INDEX) != WALL)
+                                cp3(nbuff, nextn[i]);
+                            nextn[i][0] = nextn[i][1] = nextn[i][2] = 0;
+                        }
+                        cp3(nextn[0], nbuff);
+                    }
+                    if (coor == 4) {
+                        add_void(o, site, nextn);
+                    } else {
+                        get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
+                        add_mc(o, site, nextn, index_event, prob);
+                    }
+                } else if (coor <= 3) {
+                    get_prob_ini(o, 1, ibits(v, POS_SIC, LEN_SIC), coor, site, nextn, &index_event, &prob);
+                    add_mc(o, site, nextn, index_event, prob);
+                } else {
+                    add_bulk(o, site, nextn);
+                }
+            }
+}
+
+int ora_set_la_input(ora_t *o, const int8_t *geo, const int16_t *tsub)
+{
+    if (setjmp(o->jb)) return -1;
+    if (strcmp(o->init_st, "LA")) ora_fail(o, "LA input given for InitSt %s", o->init_st);
+    if (o->ncrystal != 1) ora_fail(o, "the LA initializer is restated for NCrystal = 1");
+    if (o->lx % 3 || o->ly % 3 || o->lz % 3) ora_fail(o, "box sides must be multiples of 3");
+    size_t nt = (size_t)(o->lx / 3) * (o->ly / 3) * (o->lz / 3);
+    free(o->la_geo);
+    free(o->la_tsub);
+    o->la_geo = (int8_t *)malloc((size_t)o->lz);
+    o->la_tsub = (int16_t *)malloc(nt * sizeof(int16_t));
+    if (!o->la_geo || !o->la_tsub) ora_fail(o, "allocation failed");
+    memcpy(o->la_geo, geo, (size_t)o->lz);
+    memcpy(o->la_tsub, tsub, nt * sizeof(int16_t));
+    return 0;
+}
+
 /* ============ start.dat parsing (MS/main.f:80-212, SetProbability.f) ============ */
 typedef struct {
     FILE *f;
@@ -1301,8 +1498,17 @@ static void parse_startdat(ora_t *o, const char *path)
     if (!strcmp(o->init_st, "FF")) {
         rd_items(o, &r, 4, it);
         o->len1 = atoi(it[0]); o->len2 = atoi(it[1]); o->len3 = atoi(it[2]); o->len4 = atoi(it[3]);
-    } else if (!strcmp(o->init_st, "IN") || !strcmp(o->init_st, "SH") || !strcmp(o->init_st, "LA") ||
-               !strcmp(o->init_st, "ST")) {
+    } else if (!strcmp(o->init_st, "LA")) {    /* MS/main.f:118-138 */
+        if (o->ncov > 0) { fclose(r.f); ora_fail(o, "ERR NOT IMPLEMENTED: NCov=0 for LA"); }
+        if (!rd_line(&r) || !rd_line(&r)) { fclose(r.f); ora_fail(o, "start.dat: missing LA file names"); }
+        rd_items(o, &r, 1, it); o->Tm = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->P0 = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->sigma = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->Tflex = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->len_vac = to_real(it[0]);
+        rd_items(o, &r, 1, it); o->len_nuc = to_real(it[0]);
+        rd_items(o, &r, 1, it); snprintf(o->homogeneous, sizeof o->homogeneous, "%.1s", it[0]);
+    } else if (!strcmp(o->init_st, "IN") || !strcmp(o->init_st, "SH") || !strcmp(o->init_st, "ST")) {
         fclose(r.f);
         ora_fail(o, "InitSt %s is not restated by the oracle", o->init_st);
     } else {
@@ -1682,6 +1888,8 @@ void ora_destroy(ora_t *o)
     free(o->la_dk);
     free(o->la_ps);
     free(o->la_kind);
+    free(o->la_geo);
+    free(o->la_tsub);
     free(o->latt_base);
     free(o->lind_base);
     free(o->mc);
@@ -1703,6 +1911,9 @@ int ora_init(ora_t *o)
     } else if (!strcmp(o->init_st, "F")) {
         o->len1 -= o->len1 % 24;
         set_flat(o, o->len1, 1);
+    } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
+        if (!o->la_geo) ora_fail(o, "InitSt LA needs the geometry and temperature input (ora_set_la_input)");
+        set_cad_la(o, o->la_geo, o->la_tsub);
     } else {
         ora_fail(o, "initialization not_implemented in the oracle: %s", o->init_st);
     }

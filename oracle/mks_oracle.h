@@ -42,9 +42,15 @@ ora_t *ora_create(const char *startdat_path, const char *numbers_path,
 void ora_destroy(ora_t *o);
 const char *ora_last_error(void);
 
-/* Run the initializer named by InitSt (FS, F supported).  0 on success. */
+/* Run the initializer named by InitSt (FS, F, LA supported).  0 on success. */
 int ora_init(ora_t *o);
 
+/* Input of InitSt 'LA' (SetT + SetCAD, fresh start, NCrystal 1), used by
+ * ora_init: `geo` holds the LattGeo id of each layer z = 0..LenZ-1 (1 Si,
+ * 10 wall/air; the geometry must be uniform per layer), `tsub` the TempStat
+ * temperature (K) of the grid points with x, y, z multiples of 3, index
+ * ((z/3)*(LenY/3) + y/3)*(LenX/3) + x/3.  Copied.  0 on success. */
+int ora_set_la_input(ora_t *o, const int8_t *geo, const int16_t *tsub);
 /* Advance up to n events (stops early on the reference's exit conditions).
  * Returns 0 ok, 1 "few MC particles" stop, 2 exit condition reached,
  * <0 error.  Writes output frames into `outdir` when non-NULL.             */

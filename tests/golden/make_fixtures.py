@@ -11,6 +11,13 @@ Fixtures written:
   <case>/start.dat       regression-tests/input-and-references-files/start-<case>.dat
   <case>/I00000000.xyz.gz, I00000001.xyz.gz, log.txt
                          the reference's own regression outputs for that case
+  LA/start.dat, I0000000{0,1}.xyz.gz, log.txt
+                         the reference's LA regression case, and its inputs from
+                         LA-input.tar.gz in compact form: LA/geo_layers.npy
+                         (LattGeo id of each layer z; the file is uniform per
+                         layer, checked here) and LA/temp_sub.npz (TempStat at
+                         the grid points with x, y, z multiples of 3, int16,
+                         index [z/3, y/3, x/3])
   refwriter/start.dat    start.dat written by the reference's
                          pymulskips.setuprun.run_mulskips (setup_only) for the
                          plain Si(001) process object of mulskips_gb300.setuprun
@@ -47,6 +54,29 @@ def cases():
                 fo.write(fi.read())
 
 
+def la_case(lx=480, ly=240, lz=240):
+    import io
+    import tarfile
+    import numpy as np
+    d = os.path.join(HERE, "LA")
+    os.makedirs(d, exist_ok=True)
+    shutil.copyfile(os.path.join(RT, "start-LA.dat"), os.path.join(d, "start.dat"))
+    shutil.copyfile(os.path.join(RT, "log-LA.txt"), os.path.join(d, "log.txt"))
+    for fr in ("I00000000", "I00000001"):
+        with open(os.path.join(RT, f"{fr}-LA.xyz"), "rb") as fi, \
+                gzip.GzipFile(os.path.join(d, f"{fr}.xyz.gz"), "wb", compresslevel=9, mtime=0) as fo:
+            fo.write(fi.read())
+    with tarfile.open(os.path.join(RT, "LA-input.tar.gz")) as tf:
+        geo = np.loadtxt(io.TextIOWrapper(tf.extractfile(f"LattGeo.{lx}x{ly}x{lz}.dat")))
+        tmp = np.loadtxt(io.TextIOWrapper(tf.extractfile(f"TempStat.{lx}x{ly}x{lz}.dat")))
+    geo = geo.reshape(lz, ly, lx)
+    assert (geo == geo[:, :1, :1]).all(), "LattGeo is not uniform per layer"
+    np.save(os.path.join(d, "geo_layers.npy"), geo[:, 0, 0].astype(np.int8))
+    tmp = tmp.reshape(lz, ly, lx)
+    assert (tmp == np.rint(tmp)).all()
+    np.savez_compressed(os.path.join(d, "temp_sub.npz"), t=tmp[::3, ::3, ::3].astype(np.int16))
+
+
 def reference_writer():
     import sys
     import tempfile
@@ -78,4 +108,5 @@ def reference_writer():
 if __name__ == "__main__":
     numbers_list()
     cases()
+    la_case()
     reference_writer()
