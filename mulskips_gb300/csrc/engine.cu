@@ -435,35 +435,38 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
         for (int i = lane; i < nw; i += 32) p32[i] = 0xFFFFFFFFu;
     }
     __syncwarp();
-    int ncol = wa * wb;
+    // lanes walk the diamond sites of the band only: per layer, row ib holds
+    // the sites ia = 2 ja + p with p the row's parity, ja < ceil(wa/2)
+    const int hw = (wa + 1) >> 1, per = wb * hw, nsl = per * (zh - zl + 1);
     int nl = 0;
     float g[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int col0 = 0; col0 < ncol; col0 += 32) {
-        int col = col0 + lane;
-        bool cv = col < ncol;
-        int ib = cv ? col / wa : 0, ia = cv ? col - ib * wa : 0;
-        int a = a0 + ia, b = b0 + ib;
-        for (int z = zl; z <= zh; z++) {
-            int cls = CLS_NONE;
-            if (cv && ((a + b + (z >> 1)) & 1) == 0) cls = site_class(L, a, b, z);
-            unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
-            if (cls != CLS_NONE) {
-                uint32_t key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
-                int slot = nl + __popc(m & lanemask_lt());
-                if (slot < MCCAP) {
-                    S.list[slot] = (key << 8) | (uint32_t)cls;
-                    if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
-                }
-                unsigned gm = __match_any_sync(m, cls);
-                if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
-                if (A) {
-                    float d[4];
-                    la_drate(*A, cls, la_temp(*A, z, t_mid), d, la_vacuum(*A, cls, z));
-                    for (int j = 0; j < 4; j++) g[j] += d[j];
-                }
-            }
-            nl += __popc(m);
+    for (int s0 = 0; s0 < nsl; s0 += 32) {
+        int sidx = s0 + lane;
+        int cls = CLS_NONE, ia = 0, ib = 0, z = zl;
+        if (sidx < nsl) {
+            int dz = sidx / per, k = sidx - dz * per;
+            z = zl + dz;
+            ib = k / hw;
+            ia = 2 * (k - ib * hw) + ((a0 + b0 + ib + (z >> 1)) & 1);
+            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z);
         }
+        unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
+        if (cls != CLS_NONE) {
+            uint32_t key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
+            int slot = nl + __popc(m & lanemask_lt());
+            if (slot < MCCAP) {
+                S.list[slot] = (key << 8) | (uint32_t)cls;
+                if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
+            }
+            unsigned gm = __match_any_sync(m, cls);
+            if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
+            if (A) {
+                float d[4];
+                la_drate(*A, cls, la_temp(*A, z, t_mid), d, la_vacuum(*A, cls, z));
+                for (int j = 0; j < 4; j++) g[j] += d[j];
+            }
+        }
+        nl += __popc(m);
     }
     if (A) {
         for (int j = 0; j < 4; j++) {
@@ -786,31 +789,24 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             int nrows = WB * WZ;
             for (int i = lane; i < WB_MAX * WMAX / 4; i += 32) reinterpret_cast<uint32_t *>(S.dirty)[i] = 0u;
             if (inner) {
-                // aligned 16-byte chunks: one or two per row, many in flight per lane
+                // aligned 16-byte chunks, one or two per row: lane -> (row ib,
+                // chunk c), eight layers in flight per lane
                 int nchunk = ((lo_a - ax0) + WA > 16) ? 2 : 1;
-                int total = nrows * nchunk;
-                for (int base = 0; base < total; base += 32 * 8) {
+                int c = lane & (nchunk - 1), ib = lane >> (nchunk - 1);
+                bool lv = ib < WB;
+                const uint8_t *col = st + (int64_t)wrapi(bx0 + ib, R.NB) * R.pitch + ax0 + 16 * c;
+                const int64_t zstride = (int64_t)R.NB * R.pitch;
+                uint8_t *dst = &S.win[ib * RS + 16 * c];
+                for (int iz0 = 0; iz0 < WZ; iz0 += 8) {
                     uint4 v[8];
 #pragma unroll
-                    for (int u = 0; u < 8; u++) {
-                        int p = base + u * 32 + lane;
-                        if (p < total) {
-                            int r = p / nchunk, c = p - r * nchunk;
-                            int ib = r % WB, iz = r / WB;
-                            const uint8_t *row =
-                                st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch + ax0 + 16 * c;
-                            v[u] = __ldcg(reinterpret_cast<const uint4 *>(row));
-                        }
-                    }
+                    for (int u = 0; u < 8; u++)
+                        if (lv && iz0 + u < WZ)
+                            v[u] = __ldcg(reinterpret_cast<const uint4 *>(col + (int64_t)(zw0 + iz0 + u) * zstride));
 #pragma unroll
-                    for (int u = 0; u < 8; u++) {
-                        int p = base + u * 32 + lane;
-                        if (p < total) {
-                            int r = p / nchunk, c = p - r * nchunk;
-                            int ib = r % WB, iz = r / WB;
-                            *reinterpret_cast<uint4 *>(&S.win[(iz * WB_MAX + ib) * RS + 16 * c]) = v[u];
-                        }
-                    }
+                    for (int u = 0; u < 8; u++)
+                        if (lv && iz0 + u < WZ)
+                            *reinterpret_cast<uint4 *>(dst + (iz0 + u) * (WB_MAX * RS)) = v[u];
                 }
             } else {
                 for (int r = lane; r < nrows; r += 32) {
