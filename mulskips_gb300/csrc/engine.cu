@@ -221,18 +221,28 @@ __global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint
     if (q >= nquads) return;
     QuadDev Q = quads[q];
     const RepDev &R = reps[Q.rep];
-    GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
-    int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
-    int ncol = wa * wb;
+    const uint8_t *st = st_all + R.st_off;
+    int wb = Q.b1 - Q.b0;
+    // the tile's columns [a0, a1) of a row lie in the aligned 16-byte chunks
+    // from c0 (at most two, tiles being <= 8 wide)
+    int c0 = Q.a0 & ~15, nch = (Q.a1 - 1 - c0) / 16 + 1;
     int zlo = 1 << 30, zhi = -1, cnt = 0;
-    for (int i = threadIdx.x; i < ncol * R.NZ; i += blockDim.x) {
-        int col = i % ncol, z = i / ncol;
-        int a = Q.a0 + col % wa, b = Q.b0 + col / wa;
-        if ((a + b + (z >> 1)) & 1) continue;
-        if (site_class(L, a, b, z) != CLS_NONE) {
-            cnt++;
-            zlo = min(zlo, z);
-            zhi = max(zhi, z);
+    for (int r = threadIdx.x; r < R.NZ * wb; r += blockDim.x) {
+        int z = r / wb, b = Q.b0 + r - (r / wb) * wb;
+        const uint8_t *row = st + ((int64_t)z * R.NB + b) * R.pitch;
+        for (int c = 0; c < nch; c++) {
+            uint4 v = __ldcg(reinterpret_cast<const uint4 *>(row + c0 + 16 * c));
+            const uint8_t *by = reinterpret_cast<const uint8_t *>(&v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                int a = c0 + 16 * c + k;
+                if (a < Q.a0 || a >= Q.a1 || ((a + b + (z >> 1)) & 1)) continue;
+                if (event_byte(by[k])) {
+                    cnt++;
+                    zlo = min(zlo, z);
+                    zhi = max(zhi, z);
+                }
+            }
         }
     }
     __shared__ int s_lo, s_hi, s_cnt;
@@ -249,67 +259,89 @@ __global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint
     }
 }
 
-// Class histogram of one replica (int64 counts per class) and FP64 total rate.
-__global__ void k_class_hist(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *hist)
+// Class histograms from the tiles' z bands (which hold every event site):
+// block per tile of replicas [rep0, rep1), hist[rep - rep0][class].
+__global__ void k_class_hist(const RepDev *reps, const QuadDev *quads, int q0, int q1, int rep0, uint8_t *st_all,
+                             unsigned long long *hist)
 {
-    const RepDev &R = reps[rep];
-    GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
     __shared__ unsigned int sh[NCLASS];
-    for (int i = threadIdx.x; i < NCLASS; i += blockDim.x) sh[i] = 0;
-    __syncthreads();
-    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int a = (int)(i % R.NA);
-        int64_t r = i / R.NA;
-        int b = (int)(r % R.NB);
-        int z = (int)(r / R.NB);
-        if ((a + b + (z >> 1)) & 1) continue;
-        int c = site_class(L, a, b, z);
-        if (c == CLS_NONE) continue;
-        // warp-aggregated increment of the same class
-        unsigned m = __match_any_sync(__activemask(), c);
-        int leader = __ffs(m) - 1;
-        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&sh[c], __popc(m));
+    for (int q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
+        for (int i = threadIdx.x; i < NCLASS; i += blockDim.x) sh[i] = 0;
+        __syncthreads();
+        const QuadDev &Q = quads[q];
+        const RepDev &R = reps[Q.rep];
+        GLat L{st_all + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
+        int wa = Q.a1 - Q.a0, wb = Q.b1 - Q.b0;
+        int zlo = max(0, Q.zlo), zhi = min(R.NZ - 1, Q.zhi);
+        int n = (zhi - zlo + 1) * wa * wb;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            int ia = i % wa, r = i / wa, ib = r % wb, z = zlo + r / wb;
+            int a = Q.a0 + ia, b = Q.b0 + ib;
+            if ((a + b + (z >> 1)) & 1) continue;
+            if (!event_byte(L.get(a, b, z))) continue;
+            atomicAdd(&sh[site_class(L, a, b, z)], 1u);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < NCLASS; i += blockDim.x)
+            if (sh[i]) atomicAdd(&hist[(size_t)(Q.rep - rep0) * NCLASS + i], (unsigned long long)sh[i]);
+        __syncthreads();
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < NCLASS; i += blockDim.x)
-        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
 }
 
-// Observables of one replica: column heights, atom counts.
+// Observables of one replica: thread per (row b, 16-column chunk), walking
+// the layers with 16-byte loads; counts, and the top atom of each column.
 __global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *cnt, double *hsum)
 {
     const RepDev &R = reps[rep];
     const uint8_t *st = st_all + R.st_off;
-    int ncol = R.NA * R.NB;
+    int nch = R.pitch / 16;
     unsigned long long atoms = 0, under = 0, voids = 0, sp1 = 0, sp2 = 0, sp3 = 0;
     double h1 = 0.0, h2 = 0.0;
     int cols = 0;
-    for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol; col += gridDim.x * blockDim.x) {
-        int a = col % R.NA, b = col / R.NA;
-        int top = -1;
-        for (int z = 0; z < R.NZ; z++) {
-            if ((a + b + (z >> 1)) & 1) continue;
-            uint8_t s = st[((int64_t)z * R.NB + b) * R.pitch + a];
-            if (s == 0 || s == WALL) continue;
-            int sp = sp_of(s), co = co_of(s);
-            if (sp) {
-                atoms++;
-                if (co <= 3) under++;
-                if (sp == 1) sp1++;
-                if (sp == 2) sp2++;
-                if (sp == 3) sp3++;
-                top = z;
-            } else if (co == 4) {
-                voids++;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < R.NB * nch; t += gridDim.x * blockDim.x) {
+        int b = t / nch, a0 = 16 * (t - b * nch);
+        int top[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) top[k] = -1;
+        const uint8_t *col = st + (int64_t)b * R.pitch + a0;
+        const int64_t zs = (int64_t)R.NB * R.pitch;
+        for (int z0 = 0; z0 < R.NZ; z0 += 4) {
+            uint4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (z0 + u < R.NZ) v[u] = __ldcs(reinterpret_cast<const uint4 *>(col + (z0 + u) * zs));
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                int z = z0 + u;
+                if (z >= R.NZ) break;
+                const uint8_t *by = reinterpret_cast<const uint8_t *>(&v[u]);
+                int par = (a0 + b + (z >> 1)) & 1;     // a0 is even: byte k is a site iff k+par even
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    uint8_t s = by[k];
+                    if (((k + par) & 1) || s == 0 || s == WALL) continue;
+                    int sp = sp_of(s), co = co_of(s);
+                    if (sp) {
+                        atoms++;
+                        under += co <= 3;
+                        sp1 += sp == 1;
+                        sp2 += sp == 2;
+                        sp3 += sp == 3;
+                        top[k] = z;
+                    } else {
+                        voids += co == 4;
+                    }
+                }
             }
         }
-        if (top >= 0) {
-            double h = 3.0 * top;
-            h1 += h;
-            h2 += h * h;
-            cols++;
-        }
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (top[k] >= 0 && a0 + k < R.NA) {
+                double hh = 3.0 * top[k];
+                h1 += hh;
+                h2 += hh * hh;
+                cols++;
+            }
     }
     atomicAdd(&cnt[0], atoms);
     atomicAdd(&cnt[1], under);
@@ -1071,61 +1103,78 @@ __device__ __forceinline__ bool frame_pick(uint8_t s, int kind)
     return sp_of(s) == 0 && co_of(s) == 4;
 }
 
-constexpr int FRAME_CHUNK = 4096;
+// The padded lattice is read as 16-byte units (row-major, so unit order is
+// the reference's z, y, x order); a block takes FRAME_UNITS consecutive
+// units, four per thread.  Padding bytes and non-site bytes are 0.
+constexpr int FRAME_UNITS = 1024;
+
+__device__ __forceinline__ unsigned frame_mask(uint4 v, int kind)
+{
+    const uint8_t *by = reinterpret_cast<const uint8_t *>(&v);
+    unsigned m = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) m |= frame_pick(by[k], kind) ? (1u << k) : 0u;
+    return m;
+}
 
 __global__ void k_frame_count(const RepDev *reps, int rep, const uint8_t *st_all, int kind, unsigned int *counts)
 {
     const RepDev &R = reps[rep];
-    const uint8_t *st = st_all + R.st_off;
-    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
-    int64_t c0 = (int64_t)blockIdx.x * FRAME_CHUNK;
+    const uint4 *st = reinterpret_cast<const uint4 *>(st_all + R.st_off);
+    int64_t nu = (int64_t)R.NZ * R.NB * (R.pitch / 16);
+    int64_t u0 = (int64_t)blockIdx.x * FRAME_UNITS + 4 * threadIdx.x;
     unsigned int cnt = 0;
-    for (int64_t i = c0 + threadIdx.x; i < c0 + FRAME_CHUNK && i < n; i += blockDim.x) {
-        int a = (int)(i % R.NA);
-        int64_t r = i / R.NA;
-        if (frame_pick(st[r * R.pitch + a], kind)) cnt++;
-    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (u0 + j < nu) cnt += __popc(frame_mask(__ldcs(st + u0 + j), kind));
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     __shared__ unsigned int sh;
     if (threadIdx.x == 0) sh = 0;
     __syncthreads();
-    atomicAdd(&sh, cnt);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sh, cnt);
     __syncthreads();
     if (threadIdx.x == 0) counts[blockIdx.x] = sh;
 }
 
-// one block per chunk; a block-wide ordered scan writes the compact indices
+// ordered compaction: block-wide exclusive scan of the per-thread counts
 __global__ void k_frame_write(const RepDev *reps, int rep, const uint8_t *st_all, int kind,
                               const unsigned long long *offsets, uint32_t *out)
 {
     const RepDev &R = reps[rep];
-    const uint8_t *st = st_all + R.st_off;
-    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
-    int64_t c0 = (int64_t)blockIdx.x * FRAME_CHUNK;
-    __shared__ unsigned int warp_tot[32];
-    __shared__ unsigned long long base;
-    if (threadIdx.x == 0) base = offsets[blockIdx.x];
+    const uint4 *st = reinterpret_cast<const uint4 *>(st_all + R.st_off);
+    const int upr = R.pitch / 16;                               // units per row
+    int64_t nu = (int64_t)R.NZ * R.NB * upr;
+    int64_t u0 = (int64_t)blockIdx.x * FRAME_UNITS + 4 * threadIdx.x;
+    unsigned m[4];
+    unsigned int cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        m[j] = u0 + j < nu ? frame_mask(__ldcs(st + u0 + j), kind) : 0u;
+        cnt += __popc(m[j]);
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned int x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __shared__ unsigned int wsum[32];
+    if (lane == 31) wsum[wid] = x;
     __syncthreads();
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int64_t s0 = c0; s0 < c0 + FRAME_CHUNK && s0 < n; s0 += blockDim.x) {
-        int64_t i = s0 + threadIdx.x;
-        bool p = false;
-        if (i < c0 + FRAME_CHUNK && i < n) {
-            int a = (int)(i % R.NA);
-            int64_t r = i / R.NA;
-            p = frame_pick(st[r * R.pitch + a], kind);
+    unsigned int before = x - cnt;
+    for (int w = 0; w < wid; w++) before += wsum[w];
+    unsigned long long pos = offsets[blockIdx.x] + before;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        unsigned mm = m[j];
+        int64_t row = (u0 + j) / upr;
+        int abase = 16 * (int)((u0 + j) - row * upr);
+        while (mm) {
+            int k = __ffs(mm) - 1;
+            mm &= mm - 1;
+            out[pos++] = (uint32_t)(row * R.NA + abase + k);
         }
-        unsigned m = __ballot_sync(0xffffffffu, p);
-        if (lane == 0) warp_tot[wid] = __popc(m);
-        __syncthreads();
-        unsigned int before = 0, total = 0;
-        for (int w = 0; w < nw; w++) {
-            if (w < wid) before += warp_tot[w];
-            total += warp_tot[w];
-        }
-        if (p) out[base + before + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
-        __syncthreads();
-        if (threadIdx.x == 0) base += total;
-        __syncthreads();
     }
 }
 
@@ -1272,6 +1321,15 @@ int rescan(mks_handle *h)
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
+}
+
+// class histograms of replicas [r0, r1) into hist (zeroed by the caller)
+void class_hist(mks_handle *h, int r0, int r1, unsigned long long *hist)
+{
+    int q0 = h->reps[r0].quad_base;
+    int q1 = r1 < (int)h->reps.size() ? h->reps[r1].quad_base : (int)h->quads_h.size();
+    int nb = std::min(q1 - q0, 8192);
+    if (nb > 0) k_class_hist<<<nb, 128, 0, h->stream>>>(h->d_reps, h->d_quads, q0, q1, r0, h->d_st, hist);
 }
 
 // cut every replica's (a,b) plane into tiles of about `width` sites
@@ -1596,9 +1654,9 @@ int obs_impl(mks_handle *h, int rep, mks_observables *o)
     CK(cudaMemsetAsync(d_h, 0, sizeof(double) * 2, h->stream));
     CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
     const RepHost &r = h->reps[rep];
-    int ncol = r.NA * r.NB;
-    k_observables<<<std::min(1024, (ncol + 255) / 256), 256, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_cnt, d_h);
-    k_class_hist<<<1024, 256, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_hist);
+    int nthr = r.NB * (r.pitch / 16);
+    k_observables<<<std::min(4096, (nthr + 127) / 128), 128, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_cnt, d_h);
+    class_hist(h, rep, rep + 1, d_hist);
     CK(cudaGetLastError());
     unsigned long long cnt[8], hist[NCLASS];
     double hs[2];
@@ -2113,7 +2171,7 @@ int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
     unsigned long long *d_hist = nullptr;
     CK(cudaMallocAsync(&d_hist, sizeof(unsigned long long) * NCLASS, h->stream));
     CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
-    k_class_hist<<<1024, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, d_hist);
+    class_hist(h, 0, 1, d_hist);
     CK(cudaGetLastError());
     unsigned long long tmp[NCLASS];
     CK(cudaMemcpyAsync(tmp, d_hist, sizeof tmp, cudaMemcpyDeviceToHost, h->stream));
@@ -2130,8 +2188,7 @@ int mks_batch_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
     unsigned long long *d_hist = nullptr;
     CK(cudaMallocAsync(&d_hist, nb * n, h->stream));
     CK(cudaMemsetAsync(d_hist, 0, nb * n, h->stream));
-    for (size_t i = 0; i < n; i++)
-        k_class_hist<<<256, 256, 0, h->stream>>>(h->d_reps, (int)i, h->d_st, d_hist + i * NCLASS);
+    class_hist(h, 0, (int)n, d_hist);
     CK(cudaGetLastError());
     std::vector<unsigned long long> tmp(NCLASS * n);
     CK(cudaMemcpyAsync(tmp.data(), d_hist, nb * n, cudaMemcpyDeviceToHost, h->stream));
@@ -2214,8 +2271,7 @@ int mks_suggest_tau(mks_handle *h, double f, double *tau)
     size_t nb = sizeof(unsigned long long) * NCLASS;
     CK(cudaMallocAsync(&d_hist, nb * h->reps.size(), h->stream));
     CK(cudaMemsetAsync(d_hist, 0, nb * h->reps.size(), h->stream));
-    for (size_t i = 0; i < h->reps.size(); i++)
-        k_class_hist<<<256, 256, 0, h->stream>>>(h->d_reps, (int)i, h->d_st, d_hist + i * NCLASS);
+    class_hist(h, 0, (int)h->reps.size(), d_hist);
     CK(cudaGetLastError());
     std::vector<unsigned long long> hist(NCLASS * h->reps.size());
     CK(cudaMemcpyAsync(hist.data(), d_hist, nb * h->reps.size(), cudaMemcpyDeviceToHost, h->stream));
@@ -2240,8 +2296,8 @@ int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int
 {
     if (!h || !n_out || (kind != 0 && kind != 1) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[0];
-    int64_t nsite = (int64_t)r.NZ * r.NB * r.NA;
-    int nchunk = (int)((nsite + FRAME_CHUNK - 1) / FRAME_CHUNK);
+    int64_t nunit = (int64_t)r.NZ * r.NB * (r.pitch / 16);
+    int nchunk = (int)((nunit + FRAME_UNITS - 1) / FRAME_UNITS);
     unsigned int *d_cnt = nullptr;
     CK(cudaMallocAsync(&d_cnt, sizeof(unsigned int) * nchunk, h->stream));
     k_frame_count<<<nchunk, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, kind, d_cnt);

@@ -81,6 +81,16 @@ MKS_HD int census_index(int n1, int n2, int n3)
     return base + k;
 }
 
+// Does the site carry an event (site_class != CLS_NONE)?  Decided by its own
+// byte: an empty site with 1..3 occupied neighbours, or an atom with <= 3
+// (its census equals its coordination; census 4 is bulk).
+MKS_HD bool event_byte(uint8_t s)
+{
+    if (s == 0 || s == WALL) return false;
+    int co = co_of(s);
+    return sp_of(s) ? co <= 3 : (co >= 1 && co <= 3);
+}
+
 // Accessor concept: uint8_t get(int a, int b, int z) const; void put(int a, int b, int z, uint8_t v);
 // with periodic wrap in a, b handled by the accessor and 0 outside the z range.
 

@@ -105,6 +105,15 @@ class Lattice:
     def get_state_ptr(self, addr, n):
         N.check(N.lib().mks_get_state(self._h, C.c_void_p(addr), int(n)))
 
+    def frame_sites_ptr(self, kind, addr, cap):
+        """Compact-state indices of the sites listed in an output frame (kind 0:
+        atoms with coordination <= 3, kind 1: voids), in the reference's z, y,
+        x order, written to device-visible host memory at addr (cap entries);
+        returns their number."""
+        n = C.c_int64()
+        N.check(N.lib().mks_frame_sites(self._h, int(kind), C.c_void_p(addr), int(cap), C.byref(n)))
+        return n.value
+
     def class_histogram(self):
         h = np.zeros(N.MKS_NCLASS, dtype=np.int64)
         N.check(N.lib().mks_class_histogram(self._h, N.ptr(h), N.MKS_NCLASS))
