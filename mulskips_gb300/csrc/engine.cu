@@ -54,7 +54,8 @@ constexpr int DERR_TIMEOUT = MKS_ERR_TIMEOUT;
 struct RepDev {
     int64_t st_off;
     int NA, NB, NZ, pitch;
-    int nqa, nqb, quad_base, pad0;
+    int nqa, nqb, quad_base;
+    int single;              // NCrystal = 1: only species 1 on the lattice
     double tau, T0, t_max;
     long long ev_max;
     unsigned long long seed;
@@ -227,6 +228,7 @@ __global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint
     // from c0 (at most two, tiles being <= 8 wide)
     int c0 = Q.a0 & ~15, nch = (Q.a1 - 1 - c0) / 16 + 1;
     int zlo = 1 << 30, zhi = -1, cnt = 0;
+    bool bad = false;
     for (int r = threadIdx.x; r < R.NZ * wb; r += blockDim.x) {
         int z = r / wb, b = Q.b0 + r - (r / wb) * wb;
         const uint8_t *row = st + ((int64_t)z * R.NB + b) * R.pitch;
@@ -237,6 +239,7 @@ __global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint
             for (int k = 0; k < 16; k++) {
                 int a = c0 + 16 * c + k;
                 if (a < Q.a0 || a >= Q.a1 || ((a + b + (z >> 1)) & 1)) continue;
+                if (R.single && sp_of(by[k]) > 1) bad = true;
                 if (event_byte(by[k])) {
                     cnt++;
                     zlo = min(zlo, z);
@@ -251,6 +254,7 @@ __global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint
     atomicMin(&s_lo, zlo);
     atomicMax(&s_hi, zhi);
     atomicAdd(&s_cnt, cnt);
+    if (bad) set_error(status, DERR_INVARIANT, q);     // species > 1 in an NCrystal = 1 replica
     __syncthreads();
     if (threadIdx.x == 0) {
         quads[q].zlo = s_lo;
@@ -398,6 +402,7 @@ struct __align__(16) TileShared {
     float G[4];                                // LA: sum over event sites of d(rate)/d(theta)
     int dcnt[3];                               // LA: net crystal atoms per species added by this tile
     int nlist;
+    int rate_rep;                              // replica whose rate table is in rate/spcum (-1 none)
 };
 
 // The one tile a warp works on (one warp per block).  Declared at file scope so
@@ -426,7 +431,7 @@ struct RepLocal {
     int NA, NB, NZ, pitch;
     double tau;
     unsigned long long seed;
-    int active;
+    int active, single;
 };
 __device__ __forceinline__ RepLocal rep_local(const RepDev &R)
 {
@@ -439,6 +444,7 @@ __device__ __forceinline__ RepLocal rep_local(const RepDev &R)
     r.tau = R.tau;
     r.seed = R.seed;
     r.active = R.active;
+    r.single = R.single;
     return r;
 }
 
@@ -454,7 +460,7 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 // match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
 __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh,
-                                           bool use_pos, int zw0, int wz, const LADev *A = nullptr,
+                                           bool use_pos, int zw0, int wz, bool single, const LADev *A = nullptr,
                                            double t_mid = 0.0)
 {
     TileShared &S = g_tile;
@@ -480,7 +486,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             z = zl + dz;
             ib = k / hw;
             ia = 2 * (k - ib * hw) + ((a0 + b0 + ib + (z >> 1)) & 1);
-            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z);
+            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single);
         }
         unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
         if (cls != CLS_NONE) {
@@ -691,7 +697,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             hz_lo = min(hz_lo, tz);
             hz_hi = max(hz_hi, tz);
         }
-        int ncls = interior ? site_class(L, ta, tb, tz) : CLS_NONE;
+        int ncls = interior ? site_class(L, ta, tb, tz, R.single != 0) : CLS_NONE;
         uint32_t tkey = interior ? (uint32_t)key_of(ia + HALO, ib + HALO, tz) : 0u;
         // old list slot of each touched site
         int my_slot = -1;
@@ -772,8 +778,15 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     const RepLocal R = rep_local(Rg);
     if (!R.active) return;
     if (Q.zhi < Q.zlo) return;   // no event sites in this tile
-    for (int c = lane; c < 64; c += 32) S.rate[c] = Rg.rate[c];
-    if (lane < 6) S.spcum[lane >> 1][lane & 1] = Rg.spcum[lane >> 1][lane & 1];
+    // the rate table stays in shared memory while the warp works on tiles of
+    // one replica (tables change only between launches); LA staging rewrites
+    // the class rates as bounds, so LA tiles reload it
+    if (LAM || S.rate_rep != Q.rep) {
+        for (int c = lane; c < 64; c += 32) S.rate[c] = Rg.rate[c];
+        if (lane < 6) S.spcum[lane >> 1][lane & 1] = Rg.spcum[lane >> 1][lane & 1];
+        __syncwarp();
+        if (lane == 0) S.rate_rep = LAM ? -1 : Q.rep;
+    }
     __syncwarp();
     uint8_t *st = st_all + R.st_off;
     GLat G{st, R.NA, R.NB, R.NZ, R.pitch};
@@ -851,8 +864,8 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             __syncwarp();
             SLat L{ax0, bx0, zw0, R.NZ};
             if (A) la_bounds(zw0, zw1 - 1);
-            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, scp ? A : nullptr,
-                            t_mid)) {
+            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, R.single != 0,
+                            scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -875,7 +888,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             // events here may walk the band upwards without re-staging: bound
             // the rates by the top layer (T rises with z)
             if (A) la_bounds(max(0, zlo - 2), R.NZ - 1);
-            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, scp ? A : nullptr, t_mid)) {
+            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, R.single != 0, scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -943,13 +956,16 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
 {
     int qi = blockIdx.x;
     if (qi >= nq) return;
+    if (threadIdx.x == 0) g_tile.rate_rep = -1;
+    __syncwarp();
     int qid = qlist[qi];
     const RepDev &R = reps[quads[qid].rep];
     process_tile<LAM>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score);
 }
 
 // Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
-// g owns tiles g, g+G, ... and runs them in increasing P.  A tile of colour c
+// g owns tile i of each colour list for i = g mod G (so at most one tile per
+// phase when a colour has <= G tiles) and runs them in increasing P.  A tile of colour c
 // may run phase P once each neighbour (all of another colour) has finished
 // its last phase before P, i.e. progress[n] >= P - ((c - colour(n)) & 3); a
 // neighbour cannot start a later phase before this tile publishes P.  All
@@ -960,15 +976,22 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
 constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 
 template <bool LAM>
-__global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, int ntiles, uint8_t *st_all,
-                                                          DevStatus *status, int *progress, int nwin,
-                                                          LADev *la, double *score)
+__global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, const int *woff,
+                                                          const int *wtiles, uint8_t *st_all, DevStatus *status,
+                                                          int *progress, int nwin, LADev *la, double *score)
 {
     int lane = threadIdx.x & 31;
+    if (lane == 0) g_tile.rate_rep = -1;
+    __syncwarp();
+    // this warp's tiles of colour c: wtiles[woff[4 g + c] .. woff[4 g + c + 1])
+    const int o0 = woff[4 * blockIdx.x], o1 = woff[4 * blockIdx.x + 1], o2 = woff[4 * blockIdx.x + 2],
+              o3 = woff[4 * blockIdx.x + 3], o4 = woff[4 * blockIdx.x + 4];
     for (int P = 0; P < 4 * nwin; P++) {
         int c = P & 3, w = P >> 2;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            if (quads[t].colour != c) continue;
+        int kb = c == 0 ? o0 : (c == 1 ? o1 : (c == 2 ? o2 : o3));
+        int ke = c == 0 ? o1 : (c == 1 ? o2 : (c == 2 ? o3 : o4));
+        for (int k = kb; k < ke; k++) {
+            int t = wtiles[k];
             if (lane < 8) {
                 int n = quads[t].nbr[lane];
                 int need = P - ((c - quads[n].colour) & 3);
@@ -1226,6 +1249,7 @@ struct mks_handle {
     int graph_windows = 0;
     int tile_width = 8;
     int *d_progress = nullptr;
+    int *d_woff = nullptr, *d_wtiles = nullptr;   // persistent schedule (upload_tiles)
     LADev *d_la = nullptr;
     double *d_score = nullptr;
     int la_on = 0;
@@ -1314,12 +1338,18 @@ int read_status(mks_handle *h, DevStatus &s)
     return 0;
 }
 
+int read_status(mks_handle *h, DevStatus &s);
+
 int rescan(mks_handle *h)
 {
     k_quad_scan<<<(int)h->quads_h.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, (int)h->quads_h.size(), h->d_st,
                                                                h->d_status);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
+    DevStatus s;
+    int rc = read_status(h, s);
+    if (rc) return rc;
+    if (s.error) return fail(MKS_ERR_INVARIANT, "lattice check failed in tile %d (species above NCrystal?)", s.err_quad);
     return 0;
 }
 
@@ -1398,7 +1428,31 @@ int upload_tiles(mks_handle *h)
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl_persistent<false>, 32, 0));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_la, k_sl_persistent<true>, 32, 0));
     per_sm = std::min(per_sm, per_sm_la);
-    h->coop_grid = (int)std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (int64_t)h->quads_h.size());
+    size_t maxc = 0;
+    for (int c = 0; c < 4; c++) maxc = std::max(maxc, h->color_list_h[c].size());
+    h->coop_grid = (int)std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (int64_t)std::max<size_t>(1, maxc));
+    // persistent schedule: tile i of colour list c goes to warp i mod G, so a
+    // warp holds at most ceil(n_c / G) tiles of a colour, and neighbouring
+    // warps hold neighbouring tiles
+    int G = h->coop_grid;
+    std::vector<int> woff(4 * (size_t)G + 1, 0), wtiles;
+    wtiles.reserve(h->quads_h.size());
+    for (int g = 0; g < G; g++)
+        for (int c = 0; c < 4; c++) {
+            woff[4 * (size_t)g + c] = (int)wtiles.size();
+            const std::vector<int> &L = h->color_list_h[c];
+            for (size_t i = (size_t)g; i < L.size(); i += (size_t)G) wtiles.push_back(L[i]);
+        }
+    woff[4 * (size_t)G] = (int)wtiles.size();
+    cudaFree(h->d_woff);
+    cudaFree(h->d_wtiles);
+    h->d_woff = h->d_wtiles = nullptr;
+    CK(cudaMalloc(&h->d_woff, sizeof(int) * woff.size()));
+    CK(cudaMalloc(&h->d_wtiles, sizeof(int) * std::max<size_t>(1, wtiles.size())));
+    CK(cudaMemcpyAsync(h->d_woff, woff.data(), sizeof(int) * woff.size(), cudaMemcpyHostToDevice, h->stream));
+    if (!wtiles.empty())
+        CK(cudaMemcpyAsync(h->d_wtiles, wtiles.data(), sizeof(int) * wtiles.size(), cudaMemcpyHostToDevice,
+                           h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
@@ -1476,6 +1530,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         d[i].ev_max = (long long)9e18;
         d[i].seed = r.cfg.seed;
         d[i].active = 1;
+        d[i].single = r.cfg.ncrystal == 1;
         rate_tables(r, d[i]);
     }
     int rc = upload_reps(h, d);
@@ -1526,7 +1581,8 @@ int run_persistent(mks_handle *h, int64_t max_windows)
         if (h->la_on) nw = std::min<int64_t>(nw, LA_PHASE - (int64_t)(h->la_window % LA_PHASE));
         CK(cudaMemsetAsync(h->d_progress, 0xFF, sizeof(int) * (size_t)nt, h->stream));
         LADev *la = h->d_la;
-        void *args[] = {&h->d_reps, &h->d_quads, &nt, &h->d_st, &h->d_status, &h->d_progress, &nw, &la, &h->d_score};
+        void *args[] = {&h->d_reps, &h->d_quads, &h->d_woff, &h->d_wtiles, &h->d_st, &h->d_status, &h->d_progress,
+                        &nw, &la, &h->d_score};
         const void *fn = h->la_on ? (const void *)k_sl_persistent<true> : (const void *)k_sl_persistent<false>;
         CK(cudaLaunchCooperativeKernel(fn, dim3(h->coop_grid), dim3(32), args, 0, h->stream));
         k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw,
@@ -1725,6 +1781,8 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_quads);
     cudaFree(h->d_status);
     cudaFree(h->d_progress);
+    cudaFree(h->d_woff);
+    cudaFree(h->d_wtiles);
     cudaFree(h->d_la);
     if (h->d_lr) cudaFree(h->d_lr);
     cudaFree(h->d_score);

@@ -96,8 +96,11 @@ MKS_HD bool event_byte(uint8_t s)
 
 // Class of the site (a,b,z): Get_Prob's branch selection (Get_Prob.f:151-323)
 // restated for the one-byte state.
+// single: the lattice holds species 1 only, so an atom's census is
+// (coordination, 0, 0) — walls count with species 1 and reciprocity holds —
+// and the neighbours need not be read.
 template <class L>
-MKS_HD int site_class(const L &lat, int a, int b, int z)
+MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false)
 {
     uint8_t s = lat.get(a, b, z);
     if (s == 0 || s == WALL) return CLS_NONE;
@@ -109,6 +112,7 @@ MKS_HD int site_class(const L &lat, int a, int b, int z)
         return CLS_NONE;
     }
     if (co >= 4) return CLS_NONE;
+    if (single) return co == 0 ? CLS_ISO : CLS_OCC0 + census_index(co, 0, 0);
     int n1 = 0, n2 = 0, n3 = 0;
     int zp = z & 1;
 #pragma unroll
