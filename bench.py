@@ -247,7 +247,7 @@ def gb300(args, rank, world):
     per_launch_s = (dev_ms / 1e3) / max(phases, 1)
     achieved = per_launch_events * ALGO_BYTES_PER_EVENT / per_launch_s / 1e9
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "sl_phase_traffic.json")
+    tp = os.path.join(ROOT, "profiles", "sl_persistent_traffic.json")
     if os.path.exists(tp):
         try:
             tj = json.load(open(tp))
@@ -276,7 +276,8 @@ def gb300(args, rank, world):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "note": f"28 B/event algorithmic x events per k_sl_phase launch / mean launch time; "
+                     "note": f"28 B/event algorithmic x events per k_sl_persistent launch (64 windows) / mean "
+                             f"launch time; traffic: ncu dram bytes of one such launch; "
                              f"peak {peak_kind}"},
         "cpu_baseline": {"value": base_v, "unit": "events/s", "cores": 1, "kind": "port",
                          "sample": f"oracle (serial C restatement) on {base_runs} runs of the same model in a "
