@@ -15,6 +15,7 @@
 // selects events rejection-free: class by cumulative rate (warp scan), member
 // by a ballot scan of the class.  Rates are an FP32 table per class; the tile
 // clock is FP64.  The reference's serial loop is mulskips-source/main.f:304-371.
+#include <cuda.h>            // CUtensorMap and its enums (the encoder is fetched at run time)
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -391,8 +392,8 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
 }
 
 // ------------------------------------------------ the sublattice kernel
-struct __align__(16) TileShared {
-    uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments
+struct __align__(128) TileShared {
+    uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments (TMA box target)
     uint32_t list[MCCAP];                      // (site key << 8) | class; class 0 = dead entry
     uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each tile site, NOPOS if never listed
     uint8_t dirty[WB_MAX * WMAX];              // staged rows changed by events
@@ -403,11 +404,67 @@ struct __align__(16) TileShared {
     int dcnt[3];                               // LA: net crystal atoms per species added by this tile
     int nlist;
     int rate_rep;                              // replica whose rate table is in rate/spcum (-1 none)
+    unsigned long long mbar;                   // TMA staging barrier
+    unsigned int tma_phase;                    // its parity
 };
 
 // The one tile a warp works on (one warp per block).  Declared at file scope so
 // every access compiles to shared-memory instructions.
 __shared__ TileShared g_tile;
+
+// ---- TMA staging: one cp.async.bulk.tensor per 4 layers of the band ----
+// tensor map per replica: dims (pitch, NB, NZ) bytes, box (32, WB_MAX, 4)
+constexpr int TMA_BZ = 4;
+constexpr unsigned TMA_BOX_BYTES = RS * WB_MAX * TMA_BZ;
+constexpr long long TMA_WAIT_LIMIT = 1LL << 22;      // try_wait polls before the copy is declared lost
+static_assert(WMAX % TMA_BZ == 0, "staged layers must be whole boxes");
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_barrier_init()
+{
+    if ((threadIdx.x & 31) == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&g_tile.mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        g_tile.tma_phase = 0;
+    }
+    __syncwarp();
+}
+
+// Stage layers [zw0, zw0 + wz) of the rows bx0.. (WB_MAX of them) and the 32
+// columns from ax0 (a multiple of 16) into g_tile.win.  Returns false if the
+// copy did not complete within the wait limit.
+__device__ __forceinline__ bool tma_stage(const CUtensorMap *tmap, int ax0, int bx0, int zw0, int wz)
+{
+    int lane = threadIdx.x & 31;
+    uint32_t mb = smem_addr(&g_tile.mbar);
+    uint32_t ph = g_tile.tma_phase;
+    int nbox = (wz + TMA_BZ - 1) / TMA_BZ;
+    __syncwarp();
+    if (lane == 0) {
+        // earlier generic accesses (this warp's shared reads/writes, the
+        // neighbours' global writes it acquired) before the async copies
+        asm volatile("fence.proxy.async;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(nbox * TMA_BOX_BYTES)
+                     : "memory");
+        for (int i = 0; i < nbox; i++)
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+                "[%5];" ::"r"(smem_addr(&g_tile.win[i * TMA_BZ * WB_MAX * RS])),
+                "l"(reinterpret_cast<uint64_t>(tmap)), "r"(ax0), "r"(bx0), "r"(zw0 + i * TMA_BZ), "r"(mb)
+                : "memory");
+    }
+    uint32_t done = 0;
+    for (long long it = 0; it < TMA_WAIT_LIMIT && !done; it++)
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done)
+                     : "r"(mb), "r"(ph)
+                     : "memory");
+    bool ok = __all_sync(0xffffffffu, done != 0);
+    if (lane == 0) g_tile.tma_phase = ph ^ 1u;
+    __syncwarp();
+    return ok;
+}
 
 struct SLat {
     int ax0, bx0, zw0, NZ;   // (a, b, z) of staged byte 0
@@ -762,7 +819,8 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
 template <bool LAM>
 __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
                                              DevStatus *status, uint32_t phase_tag, unsigned int window,
-                                             double t_start, LADev *la_all, double *score_all)
+                                             double t_start, LADev *la_all, double *score_all,
+                                             const CUtensorMap *tmaps)
 {
     TileShared &S = g_tile;
     int lane = threadIdx.x & 31;
@@ -833,7 +891,13 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             int bx0 = Q.b0 - HALO;
             int nrows = WB * WZ;
             for (int i = lane; i < WB_MAX * WMAX / 4; i += 32) reinterpret_cast<uint32_t *>(S.dirty)[i] = 0u;
-            if (inner) {
+            if (tmaps && inner && bx0 >= 0 && bx0 + WB <= R.NB) {
+                // no periodic wrap inside the box: one tensor copy per 4 layers
+                if (!tma_stage(&tmaps[Q.rep], ax0, bx0, zw0, WZ)) {
+                    if (lane == 0) set_error(status, DERR_TIMEOUT, qid);
+                    return;
+                }
+            } else if (inner) {
                 // aligned 16-byte chunks, one or two per row: lane -> (row ib,
                 // chunk c), eight layers in flight per lane
                 int nchunk = ((lo_a - ax0) + WA > 16) ? 2 : 1;
@@ -952,15 +1016,15 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
 template <bool LAM>
 __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
                                                  uint8_t *st_all, DevStatus *status, uint32_t phase_tag,
-                                                 LADev *la, double *score)
+                                                 LADev *la, double *score, const CUtensorMap *tmaps)
 {
     int qi = blockIdx.x;
     if (qi >= nq) return;
     if (threadIdx.x == 0) g_tile.rate_rep = -1;
-    __syncwarp();
+    tma_barrier_init();
     int qid = qlist[qi];
     const RepDev &R = reps[quads[qid].rep];
-    process_tile<LAM>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score);
+    process_tile<LAM>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score, tmaps);
 }
 
 // Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
@@ -978,11 +1042,12 @@ constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 template <bool LAM>
 __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, const int *woff,
                                                           const int *wtiles, uint8_t *st_all, DevStatus *status,
-                                                          int *progress, int nwin, LADev *la, double *score)
+                                                          int *progress, int nwin, LADev *la, double *score,
+                                                          const CUtensorMap *tmaps)
 {
     int lane = threadIdx.x & 31;
     if (lane == 0) g_tile.rate_rep = -1;
-    __syncwarp();
+    tma_barrier_init();
     // this warp's tiles of colour c: wtiles[woff[4 g + c] .. woff[4 g + c + 1])
     const int o0 = woff[4 * blockIdx.x], o1 = woff[4 * blockIdx.x + 1], o2 = woff[4 * blockIdx.x + 2],
               o3 = woff[4 * blockIdx.x + 3], o4 = woff[4 * blockIdx.x + 4];
@@ -1012,7 +1077,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
             if (*(volatile int *)&status->error) return;
             const RepDev &R = reps[quads[t].rep];
             process_tile<LAM>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
-                         R.T0 + (double)w * R.tau, la, score);
+                         R.T0 + (double)w * R.tau, la, score, tmaps);
             __threadfence();                                // release: each lane's writes reach L2 ...
             __syncwarp();                                   // ... before lane 0 publishes the flag
             if (lane == 0) atomicExch(progress + t, P);
@@ -1250,6 +1315,7 @@ struct mks_handle {
     int tile_width = 8;
     int *d_progress = nullptr;
     int *d_woff = nullptr, *d_wtiles = nullptr;   // persistent schedule (upload_tiles)
+    CUtensorMap *d_tmaps = nullptr;               // one per replica for TMA staging; null: plain loads
     LADev *d_la = nullptr;
     double *d_score = nullptr;
     int la_on = 0;
@@ -1457,6 +1523,45 @@ int upload_tiles(mks_handle *h)
     return 0;
 }
 
+// One TMA tensor map per replica over its lattice: dims (pitch, NB, NZ)
+// bytes, box (32, WB_MAX, TMA_BZ).  Left unset (the tiles then stage with
+// plain loads) if the driver has no encoder or a replica is narrower than a
+// box row.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int make_tensor_maps(mks_handle *h)
+{
+    cudaFree(h->d_tmaps);
+    h->d_tmaps = nullptr;
+    for (const RepHost &r : h->reps)
+        if (r.pitch < RS || r.NB < WB_MAX || r.NZ < TMA_BZ) return 0;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return 0;
+    }
+    EncodeTiledFn enc = (EncodeTiledFn)fn;
+    std::vector<CUtensorMap> maps(h->reps.size());
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        const RepHost &r = h->reps[i];
+        cuuint64_t dims[3] = {(cuuint64_t)r.pitch, (cuuint64_t)r.NB, (cuuint64_t)r.NZ};
+        cuuint64_t strides[2] = {(cuuint64_t)r.pitch, (cuuint64_t)r.NB * (cuuint64_t)r.pitch};
+        cuuint32_t box[3] = {(cuuint32_t)RS, (cuuint32_t)WB_MAX, (cuuint32_t)TMA_BZ};
+        cuuint32_t es[3] = {1, 1, 1};
+        if (enc(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->d_st + r.st_off, dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return 0;
+    }
+    CK(cudaMalloc(&h->d_tmaps, sizeof(CUtensorMap) * maps.size()));
+    CK(cudaMemcpy(h->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+    return 0;
+}
+
 int create_impl(const mks_config *cfgs, int n, mks_handle **out)
 {
     if (!cfgs || n <= 0 || !out) return fail(MKS_ERR_ARG, "bad arguments");
@@ -1507,6 +1612,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     if ((e = cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
     {
         int rc_t = upload_tiles(h);
+        if (!rc_t) rc_t = make_tensor_maps(h);
         if (rc_t) {
             mks_destroy(h);
             return rc_t;
@@ -1550,10 +1656,10 @@ int launch_window(mks_handle *h)
         if (!nq) continue;
         if (h->la_on)
             k_sl_phase<true><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
-                                                       h->d_status, (uint32_t)c, h->d_la, h->d_score);
+                                                       h->d_status, (uint32_t)c, h->d_la, h->d_score, h->d_tmaps);
         else
             k_sl_phase<false><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
-                                                        h->d_status, (uint32_t)c, h->d_la, h->d_score);
+                                                        h->d_status, (uint32_t)c, h->d_la, h->d_score, h->d_tmaps);
         h->last_kernels++;
         h->last_phase_launches++;
     }
@@ -1582,7 +1688,7 @@ int run_persistent(mks_handle *h, int64_t max_windows)
         CK(cudaMemsetAsync(h->d_progress, 0xFF, sizeof(int) * (size_t)nt, h->stream));
         LADev *la = h->d_la;
         void *args[] = {&h->d_reps, &h->d_quads, &h->d_woff, &h->d_wtiles, &h->d_st, &h->d_status, &h->d_progress,
-                        &nw, &la, &h->d_score};
+                        &nw, &la, &h->d_score, &h->d_tmaps};
         const void *fn = h->la_on ? (const void *)k_sl_persistent<true> : (const void *)k_sl_persistent<false>;
         CK(cudaLaunchCooperativeKernel(fn, dim3(h->coop_grid), dim3(32), args, 0, h->stream));
         k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw,
@@ -1783,6 +1889,7 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_progress);
     cudaFree(h->d_woff);
     cudaFree(h->d_wtiles);
+    cudaFree(h->d_tmaps);
     cudaFree(h->d_la);
     if (h->d_lr) cudaFree(h->d_lr);
     cudaFree(h->d_score);
