@@ -200,6 +200,9 @@ typedef struct {
     float Tb, Ta, t0, w;
     float L_nm, zsurf;
     int32_t score;
+    int32_t liquid_weighting;  /* 1: LaserAnnealing law (liquid fractions, vacuum
+                                  above zsurf, stop rule); 0: the law of
+                                  mulskips-source/mcevent/Get_Prob.f:127-149 */
 } mks_la_params;
 int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptransE, const double *dptransD);
 int mks_batch_get_score(mks_handle *h, double *score, int32_t reset);
@@ -213,6 +216,12 @@ int mks_batch_la_counts(mks_handle *h, int64_t *crystal, double *xliq);
  * other replicas' f (use_baseline != 0) or 0; se[j] (may be NULL) is its
  * standard error.  No counterpart in the reference.                      */
 int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, double *grad, double *se);
+/* Static per-site temperatures for LA mode, from the T bits (9..21) of a
+ * LattCoo array (SetT, mulskips-source/initial/SetT.f:25-50), replacing T(z,t)
+ * for replica rep.  Call before mks_batch_set_la.                          */
+int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lattcoo);
+/* mks_load_lattice for replica rep of a batch.                            */
+int mks_batch_load_lattice(mks_handle *h, int32_t rep, const int32_t *lattcoo);
 /* SetSi-like slab with species 2 substituted on each atom with probability
  * x[i] (SetSiGex.f places Ge with the compiler's RAND(); here Philox).     */
 int mks_batch_init_alloy(mks_handle *h, const int32_t *len1, const double *x, uint64_t seed);

@@ -45,7 +45,7 @@ class MksObservables(C.Structure):
 class MksLaParams(C.Structure):
     _fields_ = [("P0", C.c_float * 3), ("Tm", C.c_float * 3), ("Tflex", C.c_float * 3), ("sigma", C.c_float * 3),
                 ("Tb", C.c_float), ("Ta", C.c_float), ("t0", C.c_float), ("w", C.c_float), ("L_nm", C.c_float),
-                ("zsurf", C.c_float), ("score", C.c_int32)]
+                ("zsurf", C.c_float), ("score", C.c_int32), ("liquid_weighting", C.c_int32)]
 
 
 class MksStatus(C.Structure):
@@ -89,6 +89,8 @@ SIGNATURES = {
     "mks_batch_get_score": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_batch_la_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_batch_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "mks_batch_load_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mks_batch_load_lattice": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mks_batch_init_alloy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "mks_last_run_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),

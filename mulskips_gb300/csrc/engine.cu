@@ -99,7 +99,13 @@ struct LADev {
     float Edep[3][3];        // solidification barrier [species][coordination-1]
     float dEdep[3][3][4];
     float Tb, Ta, t0, w;
-    float L, zsurf, sf, pad2;
+    float L, zsurf, sf;
+    int liquid_weighting;    // 0: the MS law (no liquid fraction, no vacuum, no stop rule)
+    // optional static per-site temperature (K, the LattCoo T bits of SetT),
+    // same layout as the lattice, and its maximum per layer
+    const uint16_t *tfield;
+    const float *tlayer;
+    int tNB, tpitch;
 };
 
 constexpr float KB_EV_F = 8.617330350e-5f;   // Get_Prob.f:70
@@ -110,6 +116,13 @@ __device__ __forceinline__ float la_temp(const LADev &A, int z1, double t)
     float depth = fmaxf(0.f, (A.zsurf - 3.f * (float)z1) * A.sf * 0.1f);
     float g = (float)((t - (double)A.t0) / (double)A.w);
     return rintf(A.Tb + A.Ta * __expf(-g * g) * __expf(-depth / A.L));
+}
+// temperature of site (a, b, z1): the static field when one is loaded, else
+// the prescribed T(z, t)
+__device__ __forceinline__ float la_temp_at(const LADev &A, int a, int b, int z1, double t)
+{
+    if (A.tfield) return (float)__ldg(&A.tfield[((int64_t)z1 * A.tNB + b) * A.tpitch + a]);
+    return la_temp(A, z1, t);
 }
 __device__ __forceinline__ float la_dep(const LADev &A, int s, int co, float T)
 {
@@ -139,7 +152,7 @@ __device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
 // of the initially occupied domain, LaserAnnealing main.f:597-637)
 __device__ __forceinline__ bool la_vacuum(const LADev &A, int c, int z1)
 {
-    return (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) && 3.f * (float)z1 > A.zsurf;
+    return A.liquid_weighting && (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) && 3.f * (float)z1 > A.zsurf;
 }
 // d(rate)/d theta_j of one site of class c at temperature T (isolated atoms,
 // whose rate is a numerical device of the reference, are left out)
@@ -557,7 +570,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
             if (A) {
                 float d[4];
-                la_drate(*A, cls, la_temp(*A, z, t_mid), d, la_vacuum(*A, cls, z));
+                la_drate(*A, cls, la_temp_at(*A, a0 + ia, b0 + ib, z, t_mid), d, la_vacuum(*A, cls, z));
                 for (int j = 0; j < 4; j++) g[j] += d[j];
             }
         }
@@ -695,7 +708,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         float Tsite = 0.f;
         if (A) {
             // thinning: the class rate is the tile's bound; accept with k(T_site)/bound
-            Tsite = la_temp(*A, z, t_mid);
+            Tsite = la_temp_at(*A, a, b, z, t_mid);
             if (cls != CLS_ISO) {
                 float r_true = la_vacuum(*A, cls, z) ? 0.f : la_rate(*A, cls, Tsite);
                 float uu = u01(rnd.y) * (float)S.cnt[cls];
@@ -790,7 +803,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         if (A && sc) {
             float dn[4] = {0.f, 0.f, 0.f, 0.f}, dold[4] = {0.f, 0.f, 0.f, 0.f};
             if (interior && old_cls != ncls) {
-                float Tt = la_temp(*A, tz, t_mid);
+                float Tt = la_temp_at(*A, ta, tb, tz, t_mid);
                 la_drate(*A, ncls, Tt, dn, la_vacuum(*A, ncls, tz));
                 la_drate(*A, old_cls, Tt, dold, la_vacuum(*A, old_cls, tz));
             }
@@ -866,7 +879,8 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     // LA: class rates are bounds at the hottest of the layers [l0, l1]
     auto la_bounds = [&](int l0, int l1) {
         float th = 0.f;
-        for (int z = l0 + lane; z <= l1; z += 32) th = fmaxf(th, la_temp(*A, z, t_mid));
+        for (int z = l0 + lane; z <= l1; z += 32)
+            th = fmaxf(th, A->tfield ? A->tlayer[z] : la_temp(*A, z, t_mid));
         for (int o = 16; o > 0; o >>= 1) th = fmaxf(th, __shfl_xor_sync(0xffffffffu, th, o));
         for (int c = lane; c < 64; c += 32) S.rate[c] = (c == CLS_ISO) ? 0.f : la_rate(*A, c, th);
         __syncwarp();
@@ -1105,7 +1119,7 @@ __global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin, LADev *la)
         R.T0 += (double)nwin * R.tau;
         unsigned wold = R.window;
         R.window += (unsigned)nwin;
-        if (la && la[blockIdx.x].on) {
+        if (la && la[blockIdx.x].on && la[blockIdx.x].liquid_weighting) {
             LADev &A = la[blockIdx.x];
             long long liq[3], sum = 0, crys = 0, init = 0;
             for (int s = 0; s < 3; s++) {
@@ -1294,6 +1308,7 @@ struct RepHost {
     double ptransE[3 * 4096];
     double ptransD[9];
     bool rates_set = false;
+    int64_t t_layer_off = -1;   // offset in d_tlayer once a temperature field is loaded
 };
 
 }  // namespace
@@ -1316,6 +1331,8 @@ struct mks_handle {
     int *d_progress = nullptr;
     int *d_woff = nullptr, *d_wtiles = nullptr;   // persistent schedule (upload_tiles)
     CUtensorMap *d_tmaps = nullptr;               // one per replica for TMA staging; null: plain loads
+    uint16_t *d_tfield = nullptr;                 // LA static temperatures, lattice layout
+    float *d_tlayer = nullptr;                    // their maximum per layer (all replicas)
     LADev *d_la = nullptr;
     double *d_score = nullptr;
     int la_on = 0;
@@ -1890,6 +1907,8 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_woff);
     cudaFree(h->d_wtiles);
     cudaFree(h->d_tmaps);
+    cudaFree(h->d_tfield);
+    cudaFree(h->d_tlayer);
     cudaFree(h->d_la);
     if (h->d_lr) cudaFree(h->d_lr);
     cudaFree(h->d_score);
@@ -1995,6 +2014,13 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
         A.L = p[i].L_nm > 0 ? p[i].L_nm : 1e30f;
         A.zsurf = p[i].zsurf;
         A.sf = (float)r.cfg.sf;
+        A.liquid_weighting = p[i].liquid_weighting ? 1 : 0;
+        if (r.t_layer_off >= 0) {
+            A.tfield = h->d_tfield + r.st_off;
+            A.tlayer = h->d_tlayer + r.t_layer_off;
+            A.tNB = r.NB;
+            A.tpitch = r.pitch;
+        }
         // barriers: the PTransE / PTransD tables given to mks_batch_set_rates (eV)
         for (int sp = 1; sp <= 3; sp++)
             for (int n1 = 0; n1 <= 3; n1++)
@@ -2015,12 +2041,16 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
                     for (int j = 0; j < 4; j++) A.dEdep[sp][co][j] = (float)dptransD[(i * 9 + sp * 3 + co) * 4 + j];
             }
     }
-    // crystal atoms now: nothing is liquid yet (InitCountCrystal = CountCrystal)
+    // crystal atoms now: nothing is liquid yet (InitCountCrystal = CountCrystal);
+    // the MS law has no liquid fraction (it is 1 for every species)
     for (size_t i = 0; i < n; i++) {
         mks_observables o;
         int rc = obs_impl(h, (int)i, &o);
         if (rc) return rc;
-        for (int s = 0; s < 3; s++) la[i].init_cnt[s] = la[i].cnt[s] = o.species[s];
+        for (int s = 0; s < 3; s++) {
+            la[i].init_cnt[s] = la[i].cnt[s] = o.species[s];
+            if (!la[i].liquid_weighting) la[i].xliq[s] = 1.f;
+        }
     }
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
@@ -2147,10 +2177,9 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
     return 0;
 }
 
-int mks_load_lattice(mks_handle *h, const int32_t *lc)
+int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
 {
-    if (!h || !lc || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
-    const RepHost &r = h->reps[0];
+    const RepHost &r = h->reps[rep];
     int lx = r.cfg.lenx, ly = r.cfg.leny;
     std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
     auto at = [&](int a, int b, int z) -> uint8_t & {
@@ -2200,6 +2229,55 @@ int mks_load_lattice(mks_handle *h, const int32_t *lc)
     CK(cudaMemcpyAsync(h->d_st + r.st_off, st.data(), st.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return rescan(h);
+}
+
+int mks_load_lattice(mks_handle *h, const int32_t *lc)
+{
+    if (!h || !lc || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    return load_lattice_impl(h, 0, lc);
+}
+
+int mks_batch_load_lattice(mks_handle *h, int32_t rep, const int32_t *lc)
+{
+    if (!h || !lc || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    return load_lattice_impl(h, rep, lc);
+}
+
+int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lc)
+{
+    if (!h || !lc || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->d_tfield) {
+        int64_t nl = 0;
+        for (RepHost &x : h->reps) nl += x.NZ;
+        CK(cudaMalloc(&h->d_tfield, sizeof(uint16_t) * (size_t)h->st_bytes));
+        CK(cudaMemset(h->d_tfield, 0, sizeof(uint16_t) * (size_t)h->st_bytes));
+        CK(cudaMalloc(&h->d_tlayer, sizeof(float) * (size_t)nl));
+        CK(cudaMemset(h->d_tlayer, 0, sizeof(float) * (size_t)nl));
+        nl = 0;
+        for (RepHost &x : h->reps) {
+            x.t_layer_off = -1;
+            nl += x.NZ;
+        }
+    }
+    RepHost &r = h->reps[rep];
+    int64_t loff = 0;
+    for (int i = 0; i < rep; i++) loff += h->reps[i].NZ;
+    int lx = r.cfg.lenx, ly = r.cfg.leny;
+    std::vector<uint16_t> t((size_t)r.NZ * r.NB * r.pitch, 0);
+    std::vector<float> tl((size_t)r.NZ, 0.f);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            for (int a = 0; a < r.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                int x = 3 * (2 * a + (z1 & 1)), y = 3 * (2 * b + (z1 & 1)), z = 3 * z1;
+                int T = (lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] >> 9) & 8191;   // PosT, LenT
+                t[((size_t)z1 * r.NB + b) * r.pitch + a] = (uint16_t)T;
+                tl[z1] = std::max(tl[z1], (float)T);
+            }
+    CK(cudaMemcpy(h->d_tfield + r.st_off, t.data(), sizeof(uint16_t) * t.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_tlayer + loff, tl.data(), sizeof(float) * tl.size(), cudaMemcpyHostToDevice));
+    r.t_layer_off = loff;
+    return 0;
 }
 
 int mks_replay(mks_handle *h, const mks_event *trace, int64_t n)

@@ -235,6 +235,16 @@ class Batch:
         N.check(N.lib().mks_batch_class_histogram(self._h, N.ptr(h), 63))
         return h
 
+    def load_lattice(self, rep, lattcoo):
+        """Replica rep from a LattCoo(0:LenX-1,0:LenY-1,0:LenZ) array (x fastest)."""
+        lc = np.ascontiguousarray(lattcoo, dtype=np.int32)
+        N.check(N.lib().mks_batch_load_lattice(self._h, int(rep), N.ptr(lc)))
+
+    def load_temperature(self, rep, lattcoo):
+        """Static LA temperatures of replica rep from the LattCoo T bits."""
+        lc = np.ascontiguousarray(lattcoo, dtype=np.int32)
+        N.check(N.lib().mks_batch_load_temperature(self._h, int(rep), N.ptr(lc)))
+
     # ---- laser anneal (LA) mode ----
     def init_alloy(self, len1, x, seed):
         """SetSi-like slabs with species 2 substituted at fraction x[i]."""

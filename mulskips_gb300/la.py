@@ -125,6 +125,7 @@ def la_params(mat, pulse, zsurf, score=True):
     p.Tb, p.Ta, p.t0, p.w, p.L_nm = pulse.Tb, pulse.Ta, pulse.t0, pulse.w, pulse.L_nm
     p.zsurf = float(zsurf)
     p.score = 1 if score else 0
+    p.liquid_weighting = 1
     return p
 
 
@@ -161,8 +162,15 @@ def class_rates(theta, mat, T, xliq=(1.0, 1.0, 1.0)):
     """Rate of one site of every engine class under the LA law at
     temperature T (liquid fractions xliq for the solidification classes)."""
     E, _, Ed, _ = sige_barriers(theta)
+    return class_rates_tables(E, Ed, mat, T, xliq)
+
+
+def class_rates_tables(E, Ed, mat, T, xliq=(1.0, 1.0, 1.0)):
+    """class_rates for barrier tables E (PTransE layout) and Ed (3, 3)."""
+    E = np.asarray(E, dtype=np.float64).reshape(3, 4, 4, 4, 4, 4, 4)
+    Ed = np.asarray(Ed, dtype=np.float64).reshape(3, 3)
     r = np.zeros(NCLASS)
-    for sp in (0, 1):
+    for sp in range(min(3, len(mat.P0))):
         for n1 in range(4):
             for n2 in range(4 - n1):
                 for n3 in range(4 - n1 - n2):
@@ -173,7 +181,7 @@ def class_rates(theta, mat, T, xliq=(1.0, 1.0, 1.0)):
                         r[CLS_OCC0 + sp * NCENSUS + census_index(n1, n2, n3)] = \
                             mat.P0[sp] * math.exp(-e / (KB_EV * T))
     for co, cls in ((1, CLS_C1), (2, CLS_C2), (3, CLS_C3)):
-        for sp in (0, 1):
+        for sp in range(min(3, len(mat.P0))):
             d = Ed[sp, co - 1]
             if d:
                 r[cls] += 0.5 * mat.P0[sp] * xliq[sp] * math.exp(-d / (KB_EV * mat.Tm[sp])) * \

@@ -59,6 +59,7 @@ def lib():
         L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
+        L.ora_set_la_input.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ora_la_alloy.argtypes = [C.c_void_p, C.c_double, C.c_uint64]
         L.ora_la_set.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_uint64]
@@ -108,6 +109,12 @@ class Oracle:
         if r < 0:
             raise RuntimeError(lib().ora_last_error().decode())
         return r
+
+    def set_la_input(self, geo, tsub):
+        """InitSt LA input (see ora_set_la_input): layer ids and 3-grid temperatures."""
+        self._la_in = (np.ascontiguousarray(geo, dtype=np.int8), np.ascontiguousarray(tsub, dtype=np.int16))
+        if lib().ora_set_la_input(self._h, *(a.ctypes.data_as(C.c_void_p) for a in self._la_in)):
+            raise RuntimeError(lib().ora_last_error().decode())
 
     # ---- per-species LA law with liquid fractions and FP64 score ----
     def la_alloy(self, x, seed):
@@ -257,5 +264,25 @@ def la_replica(args):
             rc = o.la_run_until(t)
             st = o.la_state()
             out.append((st["crystal"].copy(), st["score"].copy(), st["events"], rc))
+        o.close()
+    return out
+
+
+def la_regression_replica(args):
+    """One oracle run of the LA regression input with RunType R (for a spawn
+    pool): atoms (occupied non-wall sites) at each time of `marks`."""
+    import tempfile
+    startdat_text, dims, geo, tsub, marks = args
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "start.dat")
+        with open(p, "w") as f:
+            f.write(startdat_text)
+        o = Oracle(p, *dims, numbers=None)
+        o.set_la_input(geo, tsub)
+        o.init()
+        out = []
+        for t in marks:
+            r = o.run_until(t)
+            out.append((o.atoms(), o.iter, r))
         o.close()
     return out
