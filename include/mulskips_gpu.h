@@ -171,10 +171,10 @@ int32_t mks_get_tiling(mks_handle *h);
 int mks_set_schedule(mks_handle *h, int32_t persistent);
 
 /* Window length per replica (n entries): tau = f / r*, r* the rate of the
- * class carrying the largest share of the replica's total rate.  f = 0.3 is
- * the largest tested value whose etch rate matches the serial reference
- * within its 95 % band (no counterpart in the reference, whose loop is
- * serial).                                                               */
+ * class carrying the largest share of the replica's total rate.  Validated
+ * against the serial reference: f = 0.3 for one species (plain Si), f = 0.03
+ * for two (3C-SiC rates).  No counterpart in the reference, whose loop is
+ * serial.                                                                */
 int mks_suggest_tau(mks_handle *h, double f, double *tau);
 
 /* ---- laser-anneal rate law and barrier gradients ---- */

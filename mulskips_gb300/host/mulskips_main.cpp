@@ -369,7 +369,9 @@ int main()
     int chunk = 16;
     bool few = false;
     for (long long block = 0;; block++) {
-        if (block % 4 == 0) check(mks_suggest_tau(h, 0.3, &tau));
+        // window factor validated against the serial reference: 0.3 for one
+        // species, 0.03 for two or three (fast desorption across tile borders)
+        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
         int64_t ev = 0;
         check(mks_run(h, tau, chunk, 0, 0.0, &ev, &time));
         events += ev;

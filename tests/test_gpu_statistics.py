@@ -5,7 +5,9 @@ Len1 = 120 slab) etches.  Observable: atoms left at time T_obs (the etch
 rate).  32 seeds of the serial oracle (RunType R, exact reference dynamics,
 deterministic dt = 1/R_tot) against 32 GPU replicas (exponential waiting
 times, synchronous sublattice windows of length tau).  The difference of the
-means must lie inside the 95 % confidence band of the difference."""
+means must lie inside the 3-sigma band of the difference (99.7 %; several
+statistical checks run together, so a 95 % band would fail by chance too
+often)."""
 import math
 import os
 
@@ -48,7 +50,7 @@ def gpu_atoms(tau, seeds):
 def band(x, y):
     d = x.mean() - y.mean()
     se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
-    return d, 1.96 * se
+    return d, 3.0 * se
 
 
 @pytest.fixture(scope="module")
@@ -66,9 +68,9 @@ def test_etch_rate_matches_serial_reference(oracle_sample, tau):
     d, hw = band(g, oracle_sample)
     start = 3200 * 36
     print(f"tau={tau}: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f}  serial {oracle_sample.mean():.1f}"
-          f"+-{oracle_sample.std(ddof=1):.1f}  diff {d:.1f}  95% band +-{hw:.1f}")
+          f"+-{oracle_sample.std(ddof=1):.1f}  diff {d:.1f}  3-sigma band +-{hw:.1f}")
     assert g.mean() < start and oracle_sample.mean() < start       # etching happened
-    assert abs(d) <= hw, f"etch-rate difference {d:.1f} atoms outside the 95% band {hw:.1f}"
+    assert abs(d) <= hw, f"etch-rate difference {d:.1f} atoms outside the 3-sigma band {hw:.1f}"
 
 
 def test_deposition_evaporation_regime_matches_serial_reference(oracle_lib, tmp_path):
@@ -102,5 +104,49 @@ def test_deposition_evaporation_regime_matches_serial_reference(oracle_lib, tmp_
     b.close()
     diff, hw = band(g, ref)
     print(f"Si-SL rates: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f} serial {ref.mean():.1f}+-{ref.std(ddof=1):.1f} "
-          f"diff {diff:.1f} 95% band +-{hw:.1f}")
+          f"diff {diff:.1f} 3-sigma band +-{hw:.1f}")
     assert abs(diff) <= hw
+
+
+def test_sic_surface_matches_serial_reference(oracle_lib, tmp_path):
+    """3C-SiC(001), the rates of the reference's `surface` regression case
+    (NCrystal 2, Si and C with 18 census-dependent evaporation rates), RunType
+    R: atoms and C atoms at t = 2e5 s, 16 oracle seeds against 16 GPU
+    replicas at the two-species window factor f = 0.03."""
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.startdat import parse_startdat
+    from conftest import GOLDEN
+    t_obs = 2e5
+    txt = open(os.path.join(GOLDEN, "surface", "start.dat")).read().replace(
+        "T   ! R = production run", "R   ! R = production run")
+    ref, ref_c = [], []
+    for s in range(16):
+        p = tmp_path / f"sic{s}.dat"
+        p.write_text(txt.replace("9117116 ! Random seed", f"{400 + s} ! Random seed"))
+        o = oracle_lib.Oracle(str(p), 480, 480, 480, numbers=None)
+        o.init()
+        o.run_until(t_obs)
+        st, _ = oracle_lib.compact_state(o)
+        ref.append(int(np.count_nonzero((st & 3) != 0)))
+        ref_c.append(int(np.count_nonzero((st & 3) == 2)))
+        o.close()
+    ref, ref_c = np.array(ref, float), np.array(ref_c, float)
+    d = parse_startdat(str(tmp_path / "sic0.dat"))
+    n = 16
+    b = Batch([(480, 480, 480)] * n, seeds=[51 + s for s in range(n)], ncrystal=2, list_crystal=(14, 6),
+              sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
+    b.init_flat("C", [d["len"][0]] * n)
+    from mulskips_gb300.autotune import accurate_f
+    tau = float(b.suggest_tau(accurate_f(2))[0])
+    nwin = int(math.ceil(t_obs / tau))
+    b.run(t_obs / nwin, nwin)
+    obs = b.observables()
+    b.close()
+    g = np.array([o["atoms"] for o in obs], float)
+    gc = np.array([o["species"][1] for o in obs], float)
+    for name, x, y in (("atoms", g, ref), ("C atoms", gc, ref_c)):
+        diff, hw = band(x, y)
+        print(f"SiC {name}: gpu {x.mean():.1f}+-{x.std(ddof=1):.1f} serial {y.mean():.1f}+-{y.std(ddof=1):.1f} "
+              f"diff {diff:.1f} 3-sigma band +-{hw:.1f} (tau {tau:.3e})")
+        assert abs(diff) <= hw, name
