@@ -117,6 +117,14 @@ int64_t mks_state_size(mks_handle *h);
 int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
 /* Upload compact state bytes (same layout); the per-tile bands are rebuilt. */
 int mks_set_state(mks_handle *h, const uint8_t *st, int64_t n);
+/* Double-buffered input: mks_prefetch_state starts copying a compact state
+ * (layout of mks_get_state; pinned host memory makes it asynchronous) into a
+ * second device buffer on its own stream, overlapping the work in flight;
+ * mks_swap_state makes it the lattice once the copy is done (ordered on the
+ * engine's stream) and rescans the tiles.  No counterpart in the reference
+ * (the Fortran program has one in-memory lattice).                        */
+int mks_prefetch_state(mks_handle *h, const uint8_t *st, int64_t n);
+int mks_swap_state(mks_handle *h);
 int mks_replay(mks_handle *h, const mks_event *trace, int64_t n);
 /* mks_replay without any device allocation: no counterpart in the reference
  * (the Fortran program has no device memory at all).  For callers that may

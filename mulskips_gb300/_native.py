@@ -89,6 +89,8 @@ SIGNATURES = {
     "mks_batch_get_score": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_batch_la_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_batch_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "mks_prefetch_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "mks_swap_state": (C.c_int, [C.c_void_p]),
     "mks_batch_load_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_load_lattice": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

@@ -1331,6 +1331,11 @@ struct mks_handle {
     int *d_progress = nullptr;
     int *d_woff = nullptr, *d_wtiles = nullptr;   // persistent schedule (upload_tiles)
     CUtensorMap *d_tmaps = nullptr;               // one per replica for TMA staging; null: plain loads
+    uint8_t *d_st2 = nullptr;                     // second lattice buffer (mks_prefetch_state)
+    CUtensorMap *d_tmaps2 = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr, ev_swap = nullptr;
+    bool prefetched = false;
     uint16_t *d_tfield = nullptr;                 // LA static temperatures, lattice layout
     float *d_tlayer = nullptr;                    // their maximum per layer (all replicas)
     LADev *d_la = nullptr;
@@ -1548,10 +1553,10 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-int make_tensor_maps(mks_handle *h)
+int make_tensor_maps(mks_handle *h, uint8_t *base, CUtensorMap **out)
 {
-    cudaFree(h->d_tmaps);
-    h->d_tmaps = nullptr;
+    cudaFree(*out);
+    *out = nullptr;
     for (const RepHost &r : h->reps)
         if (r.pitch < RS || r.NB < WB_MAX || r.NZ < TMA_BZ) return 0;
     void *fn = nullptr;
@@ -1569,13 +1574,13 @@ int make_tensor_maps(mks_handle *h)
         cuuint64_t strides[2] = {(cuuint64_t)r.pitch, (cuuint64_t)r.NB * (cuuint64_t)r.pitch};
         cuuint32_t box[3] = {(cuuint32_t)RS, (cuuint32_t)WB_MAX, (cuuint32_t)TMA_BZ};
         cuuint32_t es[3] = {1, 1, 1};
-        if (enc(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->d_st + r.st_off, dims, strides, box, es,
+        if (enc(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, base + r.st_off, dims, strides, box, es,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return 0;
     }
-    CK(cudaMalloc(&h->d_tmaps, sizeof(CUtensorMap) * maps.size()));
-    CK(cudaMemcpy(h->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(out, sizeof(CUtensorMap) * maps.size()));
+    CK(cudaMemcpy(*out, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -1629,7 +1634,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     if ((e = cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream)) != cudaSuccess) return cleanup_fail("memset", e);
     {
         int rc_t = upload_tiles(h);
-        if (!rc_t) rc_t = make_tensor_maps(h);
+        if (!rc_t) rc_t = make_tensor_maps(h, h->d_st, &h->d_tmaps);
         if (rc_t) {
             mks_destroy(h);
             return rc_t;
@@ -1907,6 +1912,11 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_woff);
     cudaFree(h->d_wtiles);
     cudaFree(h->d_tmaps);
+    cudaFree(h->d_st2);
+    cudaFree(h->d_tmaps2);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->ev_copy) cudaEventDestroy(h->ev_copy);
+    if (h->ev_swap) cudaEventDestroy(h->ev_swap);
     cudaFree(h->d_tfield);
     cudaFree(h->d_tlayer);
     cudaFree(h->d_la);
@@ -2131,6 +2141,47 @@ int mks_get_state(mks_handle *h, uint8_t *out, int64_t n)
                              cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return 0;
+}
+
+int mks_prefetch_state(mks_handle *h, const uint8_t *in, int64_t n)
+{
+    if (!h || !in || n < mks_state_size(h) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[0];
+    if (!h->d_st2) {
+        CK(cudaMalloc(&h->d_st2, (size_t)h->st_bytes));
+        CK(cudaMemset(h->d_st2, 0, (size_t)h->st_bytes));
+        CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_swap, cudaEventDisableTiming));
+        int rc = make_tensor_maps(h, h->d_st2, &h->d_tmaps2);
+        if (rc) return rc;
+    }
+    // the buffer may still be read by work queued before the last swap
+    CK(cudaStreamWaitEvent(h->copy_stream, h->ev_swap, 0));
+    if (r.NA == r.pitch)
+        CK(cudaMemcpyAsync(h->d_st2 + r.st_off, in, (size_t)mks_state_size(h), cudaMemcpyHostToDevice,
+                           h->copy_stream));
+    else
+        CK(cudaMemcpy2DAsync(h->d_st2 + r.st_off, r.pitch, in, r.NA, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyHostToDevice,
+                             h->copy_stream));
+    CK(cudaEventRecord(h->ev_copy, h->copy_stream));
+    h->prefetched = true;
+    return 0;
+}
+
+int mks_swap_state(mks_handle *h)
+{
+    if (!h || !h->prefetched) return fail(MKS_ERR_ARG, "no state prefetched (mks_prefetch_state)");
+    CK(cudaStreamWaitEvent(h->stream, h->ev_copy, 0));
+    std::swap(h->d_st, h->d_st2);
+    std::swap(h->d_tmaps, h->d_tmaps2);
+    if (h->graph_exec) {                   // captured windows hold the old lattice pointer
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    h->prefetched = false;
+    CK(cudaEventRecord(h->ev_swap, h->stream));
+    return rescan(h);
 }
 
 int mks_set_state(mks_handle *h, const uint8_t *in, int64_t n)

@@ -102,6 +102,14 @@ class Lattice:
         """Upload from a raw host address (e.g. a pinned buffer)."""
         N.check(N.lib().mks_set_state(self._h, C.c_void_p(addr), int(n)))
 
+    def prefetch_state_ptr(self, addr, n):
+        """Start copying a compact state from (pinned) host memory into the
+        second device buffer; it becomes the lattice at swap_state()."""
+        N.check(N.lib().mks_prefetch_state(self._h, C.c_void_p(addr), int(n)))
+
+    def swap_state(self):
+        N.check(N.lib().mks_swap_state(self._h))
+
     def get_state_ptr(self, addr, n):
         N.check(N.lib().mks_get_state(self._h, C.c_void_p(addr), int(n)))
 

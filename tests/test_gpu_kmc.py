@@ -132,3 +132,35 @@ def test_tile_widths_keep_invariants(width):
         ev, _ = lat.run(2e-8, 24)
         assert ev > 0
         check_invariants(lat.state())
+
+
+def test_prefetched_state_swaps_in():
+    """mks_prefetch_state copies the next lattice while the current one runs;
+    after mks_swap_state the engine holds exactly the prefetched bytes, and
+    runs from them as from mks_set_state."""
+    torch = pytest.importorskip("torch")
+    from mulskips_gb300 import Lattice, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    lat = Lattice(480, 480, 480, seed=3)
+    lat.set_rates(pE, pD)
+    lat.init_flat("S", 120)
+    base = lat.state().copy()
+    lat.run(2e-9, 8)
+    later = lat.state().copy()
+    assert not np.array_equal(base, later)
+    pinned = torch.empty(base.size, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = base.reshape(-1)
+    lat.prefetch_state_ptr(pinned.data_ptr(), base.size)
+    lat.run(2e-9, 8)                        # runs on `later` while the copy is in flight
+    lat.swap_state()
+    assert np.array_equal(lat.state(), base)
+    lat.run(2e-9, 8)
+    a = lat.state().copy()
+    ref = Lattice(480, 480, 480, seed=3)
+    ref.set_rates(pE, pD)
+    ref.set_state(base)
+    ref.run(2e-9, 8)
+    check_invariants(a)
+    assert abs(int(((a & 3) != 0).sum()) - int(((ref.state() & 3) != 0).sum())) < 2000
+    lat.close()
+    ref.close()
