@@ -261,6 +261,7 @@ def gb300(args, rank, world):
         except Exception:
             traffic = None
     batched = batched_bench(args) if not args.no_batched else None
+    la_grad = la_gradient_bench() if not args.no_batched else None
     base_v, base_ev, base_runs = cpu_baseline(seconds=args.cpu_seconds, cores=1)
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
@@ -293,6 +294,7 @@ def gb300(args, rank, world):
         "clocks": clocks,
         "wall_s_timed": wall,
         "batched": batched,
+        "la_gradient": la_grad,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -346,6 +348,27 @@ def batched_bench(args):
             "batched_over_single": v / v1,
             "workload": "512 Si(001) replicas, side ~U{16..96} cells, T~U(900,1300) K, F~logU(0.05,5), "
                         "seed 1000+i, tau = 0.3/r* per replica"}
+
+
+def la_gradient_bench():
+    """Config 4: 128 SiGe replicas (64x64x256 cells, Ge 0.2) under the laser
+    pulse T = 300 + 1500 exp(-((t-100 ns)/40 ns)^2) exp(-z/200 nm) K, melting
+    and regrowth with the LA rate law, the FP64 likelihood-ratio score of the
+    four barrier parameters; the mean regrowth velocity between 115 and
+    145 ns and its gradient from the backward kernel.  Wall time of the whole
+    forward + backward (device work and the host loop of segments)."""
+    from mulskips_gb300 import la
+    sim = la.Anneal(n=128)
+    t0 = time.perf_counter()
+    v, g, se = la.regrowth_velocity_lr(sim, la.THETA_REF, 115e-9, 145e-9)
+    wall = time.perf_counter() - t0
+    ev = sum(o["events"] for o in sim.batch.observables())
+    sim.batch.close()
+    return {"events_per_s": ev / wall, "events": int(ev), "wall_s": wall, "replicas": 128,
+            "regrowth_velocity_m_per_s": float(v.mean()), "velocity_sd": float(v.std(ddof=1)),
+            "theta": dict(zip(la.THETA_NAMES, la.THETA_REF)),
+            "grad_m_per_s_per_eV": dict(zip(la.THETA_NAMES, map(float, g))),
+            "grad_se": dict(zip(la.THETA_NAMES, map(float, se)))}
 
 
 def reference(args, rank, world):
