@@ -230,50 +230,65 @@ __global__ void k_init_flat(uint8_t *st, int NA, int NB, int NZ, int pitch, int 
 
 // Per-tile z range and count of event sites (and invariant check of the
 // coordination bytes against the occupancy).
-__global__ void k_quad_scan(const RepDev *reps, QuadDev *quads, int nquads, uint8_t *st_all, DevStatus *status)
+// Band scan of one replica: z band and count of the event sites of every
+// tile.  One pass over the lattice in 16-byte units (thread per unit of a
+// row), the site test from the byte alone, per-tile atomics for the few
+// event sites.  k_band_init resets the replica's tiles first.
+__global__ void k_band_init(QuadDev *quads, int q0, int nq)
 {
-    int q = blockIdx.x;
-    if (q >= nquads) return;
-    QuadDev Q = quads[q];
-    const RepDev &R = reps[Q.rep];
-    const uint8_t *st = st_all + R.st_off;
-    int wb = Q.b1 - Q.b0;
-    // the tile's columns [a0, a1) of a row lie in the aligned 16-byte chunks
-    // from c0 (at most two, tiles being <= 8 wide)
-    int c0 = Q.a0 & ~15, nch = (Q.a1 - 1 - c0) / 16 + 1;
-    int zlo = 1 << 30, zhi = -1, cnt = 0;
-    bool bad = false;
-    for (int r = threadIdx.x; r < R.NZ * wb; r += blockDim.x) {
-        int z = r / wb, b = Q.b0 + r - (r / wb) * wb;
-        const uint8_t *row = st + ((int64_t)z * R.NB + b) * R.pitch;
-        for (int c = 0; c < nch; c++) {
-            uint4 v = __ldcg(reinterpret_cast<const uint4 *>(row + c0 + 16 * c));
-            const uint8_t *by = reinterpret_cast<const uint8_t *>(&v);
-#pragma unroll
-            for (int k = 0; k < 16; k++) {
-                int a = c0 + 16 * c + k;
-                if (a < Q.a0 || a >= Q.a1 || ((a + b + (z >> 1)) & 1)) continue;
-                if (R.single && sp_of(by[k]) > 1) bad = true;
-                if (event_byte(by[k])) {
-                    cnt++;
-                    zlo = min(zlo, z);
-                    zhi = max(zhi, z);
-                }
-            }
-        }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+        quads[q0 + i].zlo = 1 << 30;
+        quads[q0 + i].zhi = -1;
+        quads[q0 + i].mc = 0;
     }
-    __shared__ int s_lo, s_hi, s_cnt;
-    if (threadIdx.x == 0) { s_lo = 1 << 30; s_hi = -1; s_cnt = 0; }
-    __syncthreads();
-    atomicMin(&s_lo, zlo);
-    atomicMax(&s_hi, zhi);
-    atomicAdd(&s_cnt, cnt);
-    if (bad) set_error(status, DERR_INVARIANT, q);     // species > 1 in an NCrystal = 1 replica
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        quads[q].zlo = s_lo;
-        quads[q].zhi = s_hi;
-        quads[q].mc = s_cnt;
+}
+
+__global__ void k_band_scan(const RepDev *reps, int rep, QuadDev *quads, const uint8_t *st_all, DevStatus *status)
+{
+    const RepDev &R = reps[rep];
+    const uint4 *st = reinterpret_cast<const uint4 *>(st_all + R.st_off);
+    const int upr = R.pitch / 16;
+    const int64_t nu = (int64_t)R.NZ * R.NB * upr;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nu; u += (int64_t)gridDim.x * blockDim.x) {
+        uint4 v = __ldcs(st + u);
+        if ((v.x | v.y | v.z | v.w) == 0u) continue;
+        int64_t row = u / upr;
+        int a0 = 16 * (int)(u - row * upr);
+        int z = (int)(row / R.NB), b = (int)(row - (int64_t)z * R.NB);
+        int qb = ((b + 1) * R.nqb - 1) / R.NB;       // the tile row holding b
+        const uint8_t *by = reinterpret_cast<const uint8_t *>(&v);
+        int q = -1, lo = 1 << 30, hi = -1, cnt = 0;
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            int a = a0 + k;
+            uint8_t sb = by[k];
+            if (a >= R.NA || !event_byte(sb)) {
+                if (R.single && sb != WALL && sp_of(sb) > 1) bad = true;
+                continue;
+            }
+            if (R.single && sp_of(sb) > 1) bad = true;
+            int qa = ((a + 1) * R.nqa - 1) / R.NA;   // the tile column holding a
+            int qq = R.quad_base + qb * R.nqa + qa;
+            if (qq != q) {
+                if (q >= 0) {
+                    atomicMin(&quads[q].zlo, lo);
+                    atomicMax(&quads[q].zhi, hi);
+                    atomicAdd(&quads[q].mc, cnt);
+                }
+                q = qq;
+                lo = z;
+                hi = z;
+                cnt = 0;
+            }
+            cnt++;
+        }
+        if (q >= 0) {
+            atomicMin(&quads[q].zlo, lo);
+            atomicMax(&quads[q].zhi, hi);
+            atomicAdd(&quads[q].mc, cnt);
+        }
+        if (bad) set_error(status, DERR_INVARIANT, R.quad_base + qb * R.nqa);   // species > 1 with NCrystal = 1
     }
 }
 
@@ -306,70 +321,97 @@ __global__ void k_class_hist(const RepDev *reps, const QuadDev *quads, int q0, i
     }
 }
 
-// Observables of one replica: thread per (row b, 16-column chunk), walking
-// the layers with 16-byte loads; counts, and the top atom of each column.
-__global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *cnt, double *hsum)
+// Observables of one replica, pass 1: thread per (64-layer slab, row b,
+// 16-column unit) with 16-byte loads; counts reduced per warp, the top atom of
+// each column within the slab stored in top[(slab * NB + b) * NA + a] (-1:
+// none).
+constexpr int OBS_ZSLAB = 64;
+__global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsigned long long *cnt, int *top)
 {
     const RepDev &R = reps[rep];
     const uint8_t *st = st_all + R.st_off;
-    int nch = R.pitch / 16;
+    const int upr = R.pitch / 16, nslab = (R.NZ + OBS_ZSLAB - 1) / OBS_ZSLAB;
+    const int64_t zs = (int64_t)R.NB * R.pitch;
     unsigned long long atoms = 0, under = 0, voids = 0, sp1 = 0, sp2 = 0, sp3 = 0;
-    double h1 = 0.0, h2 = 0.0;
-    int cols = 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < R.NB * nch; t += gridDim.x * blockDim.x) {
-        int b = t / nch, a0 = 16 * (t - b * nch);
-        int top[16];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)nslab * R.NB * upr;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int unit = (int)(t % upr);
+        int64_t r = t / upr;
+        int b = (int)(r % R.NB), slab = (int)(r / R.NB);
+        int a0 = 16 * unit, z0 = slab * OBS_ZSLAB, z1 = min(R.NZ, z0 + OBS_ZSLAB);
+        int tk[16];
 #pragma unroll
-        for (int k = 0; k < 16; k++) top[k] = -1;
+        for (int k = 0; k < 16; k++) tk[k] = -1;
         const uint8_t *col = st + (int64_t)b * R.pitch + a0;
-        const int64_t zs = (int64_t)R.NB * R.pitch;
-        for (int z0 = 0; z0 < R.NZ; z0 += 4) {
+        for (int zb = z0; zb < z1; zb += 4) {
             uint4 v[4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
-                if (z0 + u < R.NZ) v[u] = __ldcs(reinterpret_cast<const uint4 *>(col + (z0 + u) * zs));
+                if (zb + u < z1) v[u] = __ldcs(reinterpret_cast<const uint4 *>(col + (zb + u) * zs));
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                int z = z0 + u;
-                if (z >= R.NZ) break;
+                int z = zb + u;
+                if (z >= z1) break;
+                if ((v[u].x | v[u].y | v[u].z | v[u].w) == 0u) continue;
                 const uint8_t *by = reinterpret_cast<const uint8_t *>(&v[u]);
                 int par = (a0 + b + (z >> 1)) & 1;     // a0 is even: byte k is a site iff k+par even
 #pragma unroll
                 for (int k = 0; k < 16; k++) {
-                    uint8_t s = by[k];
-                    if (((k + par) & 1) || s == 0 || s == WALL) continue;
-                    int sp = sp_of(s), co = co_of(s);
+                    uint8_t sb = by[k];
+                    if (((k + par) & 1) || sb == 0 || sb == WALL) continue;
+                    int sp = sp_of(sb), co = co_of(sb);
                     if (sp) {
                         atoms++;
                         under += co <= 3;
                         sp1 += sp == 1;
                         sp2 += sp == 2;
                         sp3 += sp == 3;
-                        top[k] = z;
+                        tk[k] = z;
                     } else {
                         voids += co == 4;
                     }
                 }
             }
         }
+        int *tp = top + ((int64_t)slab * R.NB + b) * R.NA + a0;
 #pragma unroll
         for (int k = 0; k < 16; k++)
-            if (top[k] >= 0 && a0 + k < R.NA) {
-                double hh = 3.0 * top[k];
-                h1 += hh;
-                h2 += hh * hh;
-                cols++;
-            }
+            if (a0 + k < R.NA) tp[k] = tk[k];
     }
-    atomicAdd(&cnt[0], atoms);
-    atomicAdd(&cnt[1], under);
-    atomicAdd(&cnt[2], voids);
-    atomicAdd(&cnt[3], sp1);
-    atomicAdd(&cnt[4], sp2);
-    atomicAdd(&cnt[5], sp3);
-    atomicAdd(&cnt[6], (unsigned long long)cols);
-    atomicAdd(&hsum[0], h1);
-    atomicAdd(&hsum[1], h2);
+    unsigned long long c[6] = {atoms, under, voids, sp1, sp2, sp3};
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        unsigned long long x = c[j];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&cnt[j], x);
+    }
+}
+
+// pass 2: per column the highest slab top; mean and mean square of the
+// column heights (top atom, grid units)
+__global__ void k_observables_heights(const int *top, int64_t ncol, int nslab, unsigned long long *cnt, double *hsum)
+{
+    double h1 = 0.0, h2 = 0.0;
+    unsigned long long cols = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncol; i += (int64_t)gridDim.x * blockDim.x) {
+        int tz = -1;
+        for (int sl = nslab - 1; sl >= 0 && tz < 0; sl--) tz = top[(int64_t)sl * ncol + i];
+        if (tz < 0) continue;
+        double hh = 3.0 * tz;
+        h1 += hh;
+        h2 += hh * hh;
+        cols++;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        h1 += __shfl_xor_sync(0xffffffffu, h1, o);
+        h2 += __shfl_xor_sync(0xffffffffu, h2, o);
+        cols += __shfl_xor_sync(0xffffffffu, cols, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cols) {
+        atomicAdd(&hsum[0], h1);
+        atomicAdd(&hsum[1], h2);
+        atomicAdd(&cnt[6], cols);
+    }
 }
 
 // Apply a given event sequence in order (one thread; the sequence is serial by
@@ -1430,8 +1472,14 @@ int read_status(mks_handle *h, DevStatus &s);
 
 int rescan(mks_handle *h)
 {
-    k_quad_scan<<<(int)h->quads_h.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, (int)h->quads_h.size(), h->d_st,
-                                                               h->d_status);
+    int nq = (int)h->quads_h.size();
+    k_band_init<<<std::min(1024, (nq + 255) / 256), 256, 0, h->stream>>>(h->d_quads, 0, nq);
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        const RepHost &r = h->reps[i];
+        int64_t nu = (int64_t)r.NZ * r.NB * (r.pitch / 16);
+        int blocks = (int)std::min<int64_t>(152 * 16, (nu + 255) / 256);
+        k_band_scan<<<blocks, 256, 0, h->stream>>>(h->d_reps, (int)i, h->d_quads, h->d_st, h->d_status);
+    }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     DevStatus s;
@@ -1838,8 +1886,15 @@ int obs_impl(mks_handle *h, int rep, mks_observables *o)
     CK(cudaMemsetAsync(d_h, 0, sizeof(double) * 2, h->stream));
     CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
     const RepHost &r = h->reps[rep];
-    int nthr = r.NB * (r.pitch / 16);
-    k_observables<<<std::min(4096, (nthr + 127) / 128), 128, 0, h->stream>>>(h->d_reps, rep, h->d_st, d_cnt, d_h);
+    int64_t ncol = (int64_t)r.NA * r.NB;
+    int nslab = (r.NZ + OBS_ZSLAB - 1) / OBS_ZSLAB;
+    int *d_top = nullptr;
+    CK(cudaMallocAsync(&d_top, sizeof(int) * (size_t)ncol * nslab, h->stream));
+    int64_t nthr = (int64_t)nslab * r.NB * (r.pitch / 16);
+    k_observables<<<(int)std::min<int64_t>(152 * 8, (nthr + 255) / 256), 256, 0, h->stream>>>(h->d_reps, rep, h->d_st,
+                                                                                              d_cnt, d_top);
+    k_observables_heights<<<(int)std::min<int64_t>(152 * 4, (ncol + 255) / 256), 256, 0, h->stream>>>(
+        d_top, ncol, nslab, d_cnt, d_h);
     class_hist(h, rep, rep + 1, d_hist);
     CK(cudaGetLastError());
     unsigned long long cnt[8], hist[NCLASS];
@@ -1850,6 +1905,7 @@ int obs_impl(mks_handle *h, int rep, mks_observables *o)
     cudaFreeAsync(d_cnt, h->stream);
     cudaFreeAsync(d_h, h->stream);
     cudaFreeAsync(d_hist, h->stream);
+    cudaFreeAsync(d_top, h->stream);
     CK(cudaStreamSynchronize(h->stream));
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
