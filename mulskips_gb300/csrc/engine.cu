@@ -1741,8 +1741,9 @@ int launch_window(mks_handle *h)
 }
 
 // Persistent schedule: one cooperative launch advances every tile through up
-// to 64 windows, then k_window_end advances the clocks and applies the exit
-// conditions (checked per launch).
+// to PERSIST_WINDOWS windows, then k_window_end advances the clocks and
+// applies the exit conditions (checked per launch).
+constexpr int PERSIST_WINDOWS = 256;
 int run_persistent(mks_handle *h, int64_t max_windows)
 {
     std::vector<RepDev> d;
@@ -1751,7 +1752,7 @@ int run_persistent(mks_handle *h, int64_t max_windows)
     int64_t done = 0;
     int launches = 0;
     while (done < max_windows) {
-        int nw = (int)std::min<int64_t>(64, max_windows - done);
+        int nw = (int)std::min<int64_t>(PERSIST_WINDOWS, max_windows - done);
         // LA: launches end on liquid-fraction refresh boundaries, as the
         // per-window schedule refreshes them
         if (h->la_on) nw = std::min<int64_t>(nw, LA_PHASE - (int64_t)(h->la_window % LA_PHASE));
