@@ -177,6 +177,17 @@ int32_t mks_get_tiling(mks_handle *h);
  * which each tile waits only for its eight neighbours, 0 one launch per
  * colour phase.  Both give the same lattice for the same seed.           */
 int mks_set_schedule(mks_handle *h, int32_t persistent);
+/* Replica clock: simulated time, windows run (the counter the random draws
+ * are keyed on) and accepted events.  Saving them with mks_get_state and
+ * restoring both into a handle with the same seed continues a run bit for bit
+ * (the reference's RunType C resume re-seeds its generator instead).      */
+int mks_get_clock(mks_handle *h, int32_t rep, double *time, int64_t *window, int64_t *events);
+int mks_set_clock(mks_handle *h, int32_t rep, double time, int64_t window, int64_t events);
+/* Failure injection for tests: tile `tile` (-1: none) never publishes its
+ * progress in the persistent schedule, so its neighbours' bounded waits
+ * (spin_limit_cycles, default about 2 s) run out and the run returns
+ * MKS_ERR_TIMEOUT with the context intact.  No counterpart in the reference. */
+int mks_debug_hold_tile(mks_handle *h, int32_t tile, int64_t spin_limit_cycles);
 
 /* Window length per replica (n entries): tau = f / r*, r* the rate of the
  * class carrying the largest share of the replica's total rate.  Validated

@@ -91,6 +91,10 @@ SIGNATURES = {
     "mks_batch_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_prefetch_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_swap_state": (C.c_int, [C.c_void_p]),
+    "mks_get_clock": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_int64)]),
+    "mks_set_clock": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int64, C.c_int64]),
+    "mks_debug_hold_tile": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
     "mks_batch_load_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_load_lattice": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

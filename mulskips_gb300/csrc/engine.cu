@@ -16,6 +16,7 @@
 // by a ballot scan of the class.  Rates are an FP32 table per class; the tile
 // clock is FP64.  The reference's serial loop is mulskips-source/main.f:304-371.
 #include <cuda.h>            // CUtensorMap and its enums (the encoder is fetched at run time)
+#include <nvtx3/nvToolsExt.h>  // named ranges for profiler timelines (header-only)
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -1099,7 +1100,8 @@ template <bool LAM>
 __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, const int *woff,
                                                           const int *wtiles, uint8_t *st_all, DevStatus *status,
                                                           int *progress, int nwin, LADev *la, double *score,
-                                                          const CUtensorMap *tmaps)
+                                                          const CUtensorMap *tmaps, long long spin_limit,
+                                                          int hold_tile)
 {
     int lane = threadIdx.x & 31;
     if (lane == 0) g_tile.rate_rep = -1;
@@ -1121,7 +1123,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
                 volatile int *err = &status->error;
                 while (*pr < need) {
                     if (*err) break;
-                    if (clock64() - t0 > SPIN_LIMIT_CYCLES) {
+                    if (clock64() - t0 > spin_limit) {
                         set_error(status, DERR_TIMEOUT, t);
                         break;
                     }
@@ -1136,7 +1138,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
                          R.T0 + (double)w * R.tau, la, score, tmaps);
             __threadfence();                                // release: each lane's writes reach L2 ...
             __syncwarp();                                   // ... before lane 0 publishes the flag
-            if (lane == 0) atomicExch(progress + t, P);
+            if (lane == 0 && t != hold_tile) atomicExch(progress + t, P);
         }
     }
 }
@@ -1323,6 +1325,12 @@ __global__ void k_frame_write(const RepDev *reps, int rep, const uint8_t *st_all
 }
 
 // ------------------------------------------------------------ host side
+// named profiler range for the duration of a scope
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 thread_local std::string g_err;
 
 int fail(int code, const char *fmt, ...)
@@ -1372,6 +1380,8 @@ struct mks_handle {
     int tile_width = 8;
     int *d_progress = nullptr;
     int *d_woff = nullptr, *d_wtiles = nullptr;   // persistent schedule (upload_tiles)
+    long long spin_limit = SPIN_LIMIT_CYCLES;     // bounded neighbour waits (cycles)
+    int hold_tile = -1;                           // failure injection: a tile that never publishes
     CUtensorMap *d_tmaps = nullptr;               // one per replica for TMA staging; null: plain loads
     uint8_t *d_st2 = nullptr;                     // second lattice buffer (mks_prefetch_state)
     CUtensorMap *d_tmaps2 = nullptr;
@@ -1472,6 +1482,7 @@ int read_status(mks_handle *h, DevStatus &s);
 
 int rescan(mks_handle *h)
 {
+    NvtxRange nr("mks_rescan");
     int nq = (int)h->quads_h.size();
     k_band_init<<<std::min(1024, (nq + 255) / 256), 256, 0, h->stream>>>(h->d_quads, 0, nq);
     for (size_t i = 0; i < h->reps.size(); i++) {
@@ -1759,7 +1770,7 @@ int run_persistent(mks_handle *h, int64_t max_windows)
         CK(cudaMemsetAsync(h->d_progress, 0xFF, sizeof(int) * (size_t)nt, h->stream));
         LADev *la = h->d_la;
         void *args[] = {&h->d_reps, &h->d_quads, &h->d_woff, &h->d_wtiles, &h->d_st, &h->d_status, &h->d_progress,
-                        &nw, &la, &h->d_score, &h->d_tmaps};
+                        &nw, &la, &h->d_score, &h->d_tmaps, &h->spin_limit, &h->hold_tile};
         const void *fn = h->la_on ? (const void *)k_sl_persistent<true> : (const void *)k_sl_persistent<false>;
         CK(cudaLaunchCooperativeKernel(fn, dim3(h->coop_grid), dim3(32), args, 0, h->stream));
         k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw,
@@ -1796,6 +1807,7 @@ int run_persistent(mks_handle *h, int64_t max_windows)
 
 int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_events, double max_time)
 {
+    NvtxRange nr("mks_run");
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
     if (rc) return rc;
@@ -1877,6 +1889,7 @@ int run_impl(mks_handle *h, const double *tau, int64_t max_windows, int64_t max_
 
 int obs_impl(mks_handle *h, int rep, mks_observables *o)
 {
+    NvtxRange nr("mks_observables");
     memset(o, 0, sizeof *o);
     unsigned long long *d_cnt = nullptr, *d_hist = nullptr;
     double *d_h = nullptr;
@@ -2680,6 +2693,40 @@ int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int
     cudaFreeAsync(d_off, h->stream);
     cudaFreeAsync(d_out, h->stream);
     CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int mks_get_clock(mks_handle *h, int32_t rep, double *time, int64_t *window, int64_t *events)
+{
+    if (!h || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    if (time) *time = d[rep].T0;
+    if (window) *window = (int64_t)d[rep].window;
+    if (events) *events = (int64_t)d[rep].events;
+    return 0;
+}
+
+int mks_set_clock(mks_handle *h, int32_t rep, double time, int64_t window, int64_t events)
+{
+    if (!h || rep < 0 || rep >= (int)h->reps.size() || window < 0 || events < 0 || !(time >= 0.0))
+        return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    d[rep].T0 = time;
+    d[rep].window = (unsigned int)window;
+    d[rep].events = (unsigned long long)events;
+    return upload_reps(h, d);
+}
+
+int mks_debug_hold_tile(mks_handle *h, int32_t tile, int64_t spin_limit_cycles)
+{
+    if (!h || tile < -1 || tile >= (int)h->quads_h.size() || spin_limit_cycles <= 0)
+        return fail(MKS_ERR_ARG, "bad arguments");
+    h->hold_tile = tile;
+    h->spin_limit = spin_limit_cycles;
     return 0;
 }
 

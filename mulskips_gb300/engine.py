@@ -102,6 +102,15 @@ class Lattice:
         """Upload from a raw host address (e.g. a pinned buffer)."""
         N.check(N.lib().mks_set_state(self._h, C.c_void_p(addr), int(n)))
 
+    def clock(self):
+        """(simulated time, windows run, accepted events) of the lattice."""
+        t, w, e = C.c_double(), C.c_int64(), C.c_int64()
+        N.check(N.lib().mks_get_clock(self._h, 0, C.byref(t), C.byref(w), C.byref(e)))
+        return t.value, w.value, e.value
+
+    def set_clock(self, time, window, events):
+        N.check(N.lib().mks_set_clock(self._h, 0, float(time), int(window), int(events)))
+
     def prefetch_state_ptr(self, addr, n):
         """Start copying a compact state from (pinned) host memory into the
         second device buffer; it becomes the lattice at swap_state()."""
