@@ -1247,6 +1247,82 @@ static void get_prob_ini(ora_t *o, int occ, int nsic, int coor, const int site[3
     }
 }
 
+/* SetNC, MS/initial/SetNC.f:24-235 (InitSt 'C'): a free-standing 3C
+ * parallelepiped of Len1 x Len2 x Len3 grid units centred in the box (species
+ * 1 on the (x1+y1+z1) mod 4 = 0 sublattice, 2 on the other), coordinations
+ * and isolated-atom removal over the box grown by 10, then the lists. */
+static void set_nc(ora_t *o, int len1, int len2, int len3)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz;
+    int x0 = lx / 2 - len1 / 2, x1e = lx / 2 + len1 / 2 - 1;
+    int y0 = ly / 2 - len2 / 2, y1e = ly / 2 + len2 / 2 - 1;
+    int z0 = lz / 2 - len3 / 2, z1e = lz / 2 + len3 / 2 - 1;
+    lg(o, " %d %d\n", z0, lz / 2 + len3 / 2 + 1);
+    lg(o, " %d %d\n", x0, lx / 2 + len1 / 2 + 1);
+    for (int z = z0; z <= z1e; z++)
+        for (int y = y0; y <= y1e; y++)
+            for (int x = x0; x <= x1e; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+            }
+    int site[3], nextn[4][3];
+    for (int z = z0 - 10; z <= z1e + 10; z++)
+        for (int y = y0 - 10; y <= y1e + 10; y++)
+            for (int x = x0 - 10; x <= x1e + 10; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int coor = 0;
+                for (int i = 0; i < 4; i++)
+                    if (ibits(*LC(o, nextn[i]), POS_OCC, LEN_OCC) > 0) coor++;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (ibits(*v, POS_OCC, LEN_OCC) != 0 && coor == 0) {
+                    *v = 0;
+                    for (int i = 0; i < 4; i++) {
+                        int32_t *w = LC(o, nextn[i]);
+                        int cn = ibits(*w, POS_COOR, LEN_COOR) - 1;
+                        if (cn < 0) cn = 0;
+                        mvbits(cn, LEN_COOR, w, POS_COOR);
+                    }
+                } else {
+                    mvbits(coor, LEN_COOR, v, POS_COOR);
+                }
+            }
+    int nbuff[3] = {0, 0, 0};
+    for (int z = z0 - 10; z <= z1e + 10; z++)
+        for (int y = y0 - 10; y <= y1e + 10; y++)
+            for (int x = x0 - 10; x <= x1e + 10; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                int occ = ibits(v, POS_OCC, LEN_OCC), coor = ibits(v, POS_COOR, LEN_COOR);
+                int index_event;
+                double prob;
+                if (occ == 0) {
+                    if (coor == 0) continue;
+                    if (coor == 1) {
+                        for (int i = 0; i < 4; i++) {
+                            if (ibits(*LC(o, nextn[i]), POS_OCC, LEN_OCC) != 0) cp3(nbuff, nextn[i]);
+                            nextn[i][0] = nextn[i][1] = nextn[i][2] = 0;
+                        }
+                        cp3(nextn[0], nbuff);
+                    }
+                    get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
+                    add_mc(o, site, nextn, index_event, prob);
+                } else if (coor <= 3) {
+                    get_prob_ini(o, 1, ibits(v, POS_SIC, LEN_SIC), coor, site, nextn, &index_event, &prob);
+                    add_mc(o, site, nextn, index_event, prob);
+                } else {
+                    add_bulk(o, site, nextn);
+                }
+            }
+}
+
 /* SetT + SetCAD for InitSt 'LA' (MS/initial/SetT.f:25-50,
  * MS/initial/SetCAD.f:24-421, fresh start): geometry id per layer z
  * (`geo[z]`, 1 = Si, 10 = wall/air, as LattGeo; a layer-uniform geometry)
@@ -1911,6 +1987,8 @@ int ora_init(ora_t *o)
     } else if (!strcmp(o->init_st, "F")) {
         o->len1 -= o->len1 % 24;
         set_flat(o, o->len1, 1);
+    } else if (!strcmp(o->init_st, "C")) {       /* MS/main.f:261-262 */
+        set_nc(o, o->len1, o->len2, o->len3);
     } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
         if (!o->la_geo) ora_fail(o, "InitSt LA needs the geometry and temperature input (ora_set_la_input)");
         set_cad_la(o, o->la_geo, o->la_tsub);
@@ -2149,7 +2227,8 @@ int64_t ora_compact_state(const ora_t *o, uint8_t *out)
                     }
                     if (fd < 0) return -1;
                 }
-                int dm = (!occ && co == 1 && which == 1 && pr == (double)1.e-8f) ? 1 : 0;
+                /* the dummy rates of Get_Prob (1e-8) and Get_Prob_Ini (1e-6) share the one flag */
+                int dm = (!occ && co == 1 && which == 1 && (pr == (double)1.e-8f || pr == (double)1.e-6f)) ? 1 : 0;
                 *d = (uint8_t)((sp & 3) | ((co & 7) << 2) | (fd << 5) | (dm << 7));
             }
     return offgrid;

@@ -26,7 +26,10 @@ def replay_case(ora, startdat, len1, kind, total, chunk, lenxyz=480):
     lat = Lattice(lenxyz, lenxyz, lenxyz, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"])
     try:
         lat.set_rates(pE, pD)
-        lat.init_flat(kind, len1)
+        if kind:
+            lat.init_flat(kind, len1)
+        else:                               # the oracle's own initializer, through LattCoo
+            lat.load_lattcoo(o.lattcoo())
         st0, off = ora.compact_state(o)
         assert off == 0
         assert np.array_equal(lat.state(), st0), "initial lattice differs"
@@ -61,6 +64,14 @@ def test_replay_si001(oracle_lib):
 def test_replay_sic001(oracle_lib):
     n = replay_case(oracle_lib, os.path.join(GOLDEN, "surface", "start.dat"), 120, "C", 200000, 100000)
     assert n == 200000
+
+
+def test_replay_sic_cube(oracle_lib):
+    """The free-standing 3C-SiC parallelepiped of the reference's `cube` case
+    (SetNC, no walls), loaded from the oracle's LattCoo through
+    mks_load_lattice: the growth of its six faces replays exactly."""
+    n = replay_case(oracle_lib, os.path.join(GOLDEN, "cube", "start.dat"), 0, None, 300000, 100000)
+    assert n == 300000
 
 
 def test_replay_etch_to_walls(oracle_lib, tmp_path):

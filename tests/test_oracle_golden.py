@@ -1,8 +1,11 @@
 """The oracle (serial C restatement of the reference) reproduces the
 reference's own regression outputs byte for byte
 (regression-tests/input-and-references-files: Si-SL and surface, 10^7 events
-each, RunType T, IDUM 9117116, 480^3 box; LA, the laser-anneal rate law on a
-480x240x240 box with a per-site temperature field, 10^6 events)."""
+each, RunType T, IDUM 9117116, 480^3 box; cube and cube-zigzag, a free-standing
+3C-SiC parallelepiped (SetNC) grown for 10^7 events, the latter with
+PtransZig = 0.8, i.e. arm-chair stacking through IF_Arm_Choice / FIND_SN /
+FIND_NN; LA, the laser-anneal rate law on a 480x240x240 box with a per-site
+temperature field, 10^6 events)."""
 import numpy as np
 import gzip
 import os
@@ -36,7 +39,7 @@ def golden_log_numbers(case):
     return m.groups(), n.groups()
 
 
-@pytest.mark.parametrize("case", ["Si-SL", "surface"])
+@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag"])
 def test_regression_frames_identical(case, oracle_lib, tmp_path):
     d, out = run_case(case, tmp_path)
     for fr in ("I00000000", "I00000001"):
