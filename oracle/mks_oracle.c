@@ -1250,18 +1250,27 @@ static void get_prob_ini(ora_t *o, int occ, int nsic, int coor, const int site[3
 /* SetNC, MS/initial/SetNC.f:24-235 (InitSt 'C'): a free-standing 3C
  * parallelepiped of Len1 x Len2 x Len3 grid units centred in the box (species
  * 1 on the (x1+y1+z1) mod 4 = 0 sublattice, 2 on the other), coordinations
- * and isolated-atom removal over the box grown by 10, then the lists. */
-static void set_nc(ora_t *o, int len1, int len2, int len3)
+ * and isolated-atom removal over the box grown by 10, then the lists.  With
+ * sphere != 0 it is SetNCSp (MS/initial/SetNCSp.f:24-237, InitSt 'S'): the
+ * cube of side Len1 cut to the ball d^2 <= Len1^2/4 around the box centre. */
+static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere)
 {
     int lx = o->lx, ly = o->ly, lz = o->lz;
     int x0 = lx / 2 - len1 / 2, x1e = lx / 2 + len1 / 2 - 1;
     int y0 = ly / 2 - len2 / 2, y1e = ly / 2 + len2 / 2 - 1;
     int z0 = lz / 2 - len3 / 2, z1e = lz / 2 + len3 / 2 - 1;
-    lg(o, " %d %d\n", z0, lz / 2 + len3 / 2 + 1);
-    lg(o, " %d %d\n", x0, lx / 2 + len1 / 2 + 1);
+    if (!sphere) {
+        lg(o, " %d %d\n", z0, lz / 2 + len3 / 2 + 1);
+        lg(o, " %d %d\n", x0, lx / 2 + len1 / 2 + 1);
+    }
     for (int z = z0; z <= z1e; z++)
         for (int y = y0; y <= y1e; y++)
             for (int x = x0; x <= x1e; x++) {
+                if (sphere) {
+                    long d2 = (long)(x - lx / 2) * (x - lx / 2) + (long)(y - ly / 2) * (y - ly / 2) +
+                              (long)(z - lz / 2) * (z - lz / 2);
+                    if (d2 > (long)len1 * len1 / 4) continue;
+                }
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
@@ -1988,7 +1997,9 @@ int ora_init(ora_t *o)
         o->len1 -= o->len1 % 24;
         set_flat(o, o->len1, 1);
     } else if (!strcmp(o->init_st, "C")) {       /* MS/main.f:261-262 */
-        set_nc(o, o->len1, o->len2, o->len3);
+        set_nc(o, o->len1, o->len2, o->len3, 0);
+    } else if (!strcmp(o->init_st, "S")) {       /* MS/main.f:257-258 */
+        set_nc(o, o->len1, o->len1, o->len1, 1);
     } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
         if (!o->la_geo) ora_fail(o, "InitSt LA needs the geometry and temperature input (ora_set_la_input)");
         set_cad_la(o, o->la_geo, o->la_tsub);

@@ -42,7 +42,7 @@ ora_t *ora_create(const char *startdat_path, const char *numbers_path,
 void ora_destroy(ora_t *o);
 const char *ora_last_error(void);
 
-/* Run the initializer named by InitSt (FS, F, C, LA supported).  0 on success. */
+/* Run the initializer named by InitSt (FS, F, C, S, LA supported).  0 on success. */
 int ora_init(ora_t *o);
 
 /* Input of InitSt 'LA' (SetT + SetCAD, fresh start, NCrystal 1), used by

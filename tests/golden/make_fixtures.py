@@ -30,7 +30,7 @@ import shutil
 REF = os.environ.get("MULSKIPS_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 RT = os.path.join(REF, "regression-tests", "input-and-references-files")
-CASES = ["Si-SL", "surface", "cube", "cube-zigzag"]
+CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere"]
 
 
 def numbers_list():

@@ -39,7 +39,7 @@ def golden_log_numbers(case):
     return m.groups(), n.groups()
 
 
-@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag"])
+@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag", "sphere"])
 def test_regression_frames_identical(case, oracle_lib, tmp_path):
     d, out = run_case(case, tmp_path)
     for fr in ("I00000000", "I00000001"):
