@@ -114,6 +114,7 @@ struct ora {
     int la_cur_z;                           /* grid z of the site whose rate la2_pd evaluates */
     int8_t *la_geo;                         /* InitSt LA input (ora_set_la_input) */
     int16_t *la_tsub;
+    int8_t *cad_geo;                        /* InitSt IN input (ora_set_geometry) */
     char init_st[3], run_type[3], exit_strategy[5];
     char save_final[3], save_coo[3];
     char restartfile[2048], coofile[2048];
@@ -1247,6 +1248,85 @@ static void get_prob_ini(ora_t *o, int occ, int nsic, int coor, const int site[3
     }
 }
 
+/* The two passes that close the free-form initial states (SetNC.f:62-234,
+ * SetNCSp.f:64-236, SetInvPOff.f:113-285, SetSiFINFET.f:120-311): over the
+ * box [xa,xb] x [ya,yb] x [za,zb] every diamond site gets its coordination
+ * from its occupied neighbours, occupied sites with none are removed (their
+ * neighbours' counts drop by one, floored at 0); then every site with
+ * coor > 0 or occupied joins the MC list (Get_Prob_Ini) or, occupied with
+ * coor 4, the bulk list.  With walls != 0 (SetSiFINFET) wall sites (index
+ * 113) are skipped, an empty site does not count wall neighbours, and the
+ * one neighbour kept for an empty coor-1 site is never a wall. */
+static inline int is_wall(int32_t v) { return ibits(v, POS_INDEX, LEN_INDEX) == WALL; }
+
+static void coor_pass(ora_t *o, int xa, int xb, int ya, int yb, int za, int zb, int walls)
+{
+    int site[3], nextn[4][3];
+    for (int z = za; z <= zb; z++)
+        for (int y = ya; y <= yb; y++)
+            for (int x = xa; x <= xb; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (walls && is_wall(*v)) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int coor = 0, occ = ibits(*v, POS_OCC, LEN_OCC);
+                for (int i = 0; i < 4; i++) {
+                    int32_t w = *LC(o, nextn[i]);
+                    if (ibits(w, POS_OCC, LEN_OCC) > 0 && (occ || !walls || !is_wall(w))) coor++;
+                }
+                if (occ != 0 && coor == 0) {
+                    *v = 0;
+                    for (int i = 0; i < 4; i++) {
+                        int32_t *w = LC(o, nextn[i]);
+                        int cn = ibits(*w, POS_COOR, LEN_COOR) - 1;
+                        if (cn < 0) cn = 0;
+                        mvbits(cn, LEN_COOR, w, POS_COOR);
+                    }
+                } else {
+                    mvbits(coor, LEN_COOR, v, POS_COOR);
+                }
+            }
+}
+
+static void list_pass(ora_t *o, int xa, int xb, int ya, int yb, int za, int zb, int walls)
+{
+    int site[3], nextn[4][3];
+    int nbuff[3] = {0, 0, 0};
+    for (int z = za; z <= zb; z++)
+        for (int y = ya; y <= yb; y++)
+            for (int x = xa; x <= xb; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t v = o->latt[lidx(o, x, y, z)];
+                if (walls && is_wall(v)) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                int occ = ibits(v, POS_OCC, LEN_OCC), coor = ibits(v, POS_COOR, LEN_COOR);
+                int index_event;
+                double prob;
+                if (occ == 0) {
+                    if (coor == 0) continue;
+                    if (coor == 1) {
+                        for (int i = 0; i < 4; i++) {
+                            int32_t w = *LC(o, nextn[i]);
+                            if (ibits(w, POS_OCC, LEN_OCC) != 0 && !(walls && is_wall(w))) cp3(nbuff, nextn[i]);
+                            nextn[i][0] = nextn[i][1] = nextn[i][2] = 0;
+                        }
+                        cp3(nextn[0], nbuff);
+                    }
+                    get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
+                    add_mc(o, site, nextn, index_event, prob);
+                } else if (coor <= 3) {
+                    get_prob_ini(o, 1, ibits(v, POS_SIC, LEN_SIC), coor, site, nextn, &index_event, &prob);
+                    add_mc(o, site, nextn, index_event, prob);
+                } else {
+                    add_bulk(o, site, nextn);
+                }
+            }
+}
+
 /* SetNC, MS/initial/SetNC.f:24-235 (InitSt 'C'): a free-standing 3C
  * parallelepiped of Len1 x Len2 x Len3 grid units centred in the box (species
  * 1 on the (x1+y1+z1) mod 4 = 0 sublattice, 2 on the other), coordinations
@@ -1276,91 +1356,124 @@ static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere)
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
                 *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
             }
-    int site[3], nextn[4][3];
-    for (int z = z0 - 10; z <= z1e + 10; z++)
-        for (int y = y0 - 10; y <= y1e + 10; y++)
-            for (int x = x0 - 10; x <= x1e + 10; x++) {
-                int k = dia_kind(x, y, z);
-                if (!k) continue;
-                site[0] = x; site[1] = y; site[2] = z;
-                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
-                int coor = 0;
-                for (int i = 0; i < 4; i++)
-                    if (ibits(*LC(o, nextn[i]), POS_OCC, LEN_OCC) > 0) coor++;
-                int32_t *v = &o->latt[lidx(o, x, y, z)];
-                if (ibits(*v, POS_OCC, LEN_OCC) != 0 && coor == 0) {
-                    *v = 0;
-                    for (int i = 0; i < 4; i++) {
-                        int32_t *w = LC(o, nextn[i]);
-                        int cn = ibits(*w, POS_COOR, LEN_COOR) - 1;
-                        if (cn < 0) cn = 0;
-                        mvbits(cn, LEN_COOR, w, POS_COOR);
-                    }
-                } else {
-                    mvbits(coor, LEN_COOR, v, POS_COOR);
-                }
-            }
-    int nbuff[3] = {0, 0, 0};
-    for (int z = z0 - 10; z <= z1e + 10; z++)
-        for (int y = y0 - 10; y <= y1e + 10; y++)
-            for (int x = x0 - 10; x <= x1e + 10; x++) {
-                int k = dia_kind(x, y, z);
-                if (!k) continue;
-                site[0] = x; site[1] = y; site[2] = z;
-                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
-                int32_t v = o->latt[lidx(o, x, y, z)];
-                int occ = ibits(v, POS_OCC, LEN_OCC), coor = ibits(v, POS_COOR, LEN_COOR);
-                int index_event;
-                double prob;
-                if (occ == 0) {
-                    if (coor == 0) continue;
-                    if (coor == 1) {
-                        for (int i = 0; i < 4; i++) {
-                            if (ibits(*LC(o, nextn[i]), POS_OCC, LEN_OCC) != 0) cp3(nbuff, nextn[i]);
-                            nextn[i][0] = nextn[i][1] = nextn[i][2] = 0;
-                        }
-                        cp3(nextn[0], nbuff);
-                    }
-                    get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
-                    add_mc(o, site, nextn, index_event, prob);
-                } else if (coor <= 3) {
-                    get_prob_ini(o, 1, ibits(v, POS_SIC, LEN_SIC), coor, site, nextn, &index_event, &prob);
-                    add_mc(o, site, nextn, index_event, prob);
-                } else {
-                    add_bulk(o, site, nextn);
-                }
-            }
+    coor_pass(o, x0 - 10, x1e + 10, y0 - 10, y1e + 10, z0 - 10, z1e + 10, 0);
+    list_pass(o, x0 - 10, x1e + 10, y0 - 10, y1e + 10, z0 - 10, z1e + 10, 0);
 }
 
-/* SetT + SetCAD for InitSt 'LA' (MS/initial/SetT.f:25-50,
- * MS/initial/SetCAD.f:24-421, fresh start): geometry id per layer z
- * (`geo[z]`, 1 = Si, 10 = wall/air, as LattGeo; a layer-uniform geometry)
- * and the temperature (K) of the grid points whose coordinates are all
- * multiples of 3, `tsub[((z/3)*(ly/3) + y/3)*(lx/3) + x/3]` (TempStat; 10
- * marks a wall and is not stored).  Only NCrystal = 1, no alloy. */
-static void set_cad_la(ora_t *o, const int8_t *geo, const int16_t *tsub)
+/* SetInvPOff, MS/initial/SetInvPOff.f:22-286 (InitSt 'I', called with
+ * (Len1, Len2), MS/main.f:245-246): a 3C substrate z = 0..20 (bulk, coor 4)
+ * under a 3C layer z = 21..Len3-1 from which inverted pyramids are cut, one
+ * at the box centre (Lenh = LenX/2 - 1) and quarters at the four corners:
+ * a site is left empty when |x-xc| + |y-yc| - 1.10 (z - Len3) <= Len for
+ * any of the five centres.  The test is evaluated in single precision, as
+ * the reference's default-REAL constant 1.10 makes it.  Then the two
+ * closing passes over z = 21..Len3+9 on the whole x-y plane. */
+static void set_invp(ora_t *o, int len, int len3)
 {
-    int lx = o->lx, ly = o->ly, lz = o->lz, nx3 = lx / 3, ny3 = ly / 3;
-    /* SetT */
-    for (int z = 0; z < lz; z += 3)
-        for (int y = 0; y < ly; y += 3)
-            for (int x = 0; x < lx; x += 3) {
-                int t = tsub[((size_t)(z / 3) * ny3 + y / 3) * nx3 + x / 3];
-                if (t != 10) mvbits(t, LEN_T, &o->latt[lidx(o, x, y, z)], POS_T);
+    int lx = o->lx, ly = o->ly;
+    int lenh = lx / 2 - 1;
+    int site[3], nextn[4][3];
+    lg(o, " %d %d %d\n", lenh, len, len3);
+    for (int z = 0; z <= 20; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+                mvbits(4, LEN_COOR, v, POS_COOR);
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                add_bulk(o, site, nextn);
             }
-    /* walls of SetCAD.f:137-153 and the geometry of :160-236 */
-    for (int z = 0; z < lz; z++) {
-        int wall = (z <= 3 || z >= lz - 4) || geo[z] == 10;
-        int si = !wall && geo[z] == 1;
+    const int cx[5] = {lenh, 0, lx, 0, lx}, cy[5] = {lenh, 0, 0, ly, ly};
+    for (int z = 21; z <= len3 - 1; z++) {
+        float dz = 1.10f * (float)(z - len3);
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int pit = 0;
+                for (int c = 0; c < 5 && !pit; c++)
+                    pit = (float)(abs(x - cx[c]) + abs(y - cy[c])) - dz <= (float)len;
+                if (pit) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+            }
+    }
+    coor_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
+    list_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
+}
+
+/* SetSiFINFET, MS/initial/SetSiFINFET.f:23-312 (InitSt 'FF', Len1..Len4
+ * each rounded down to a multiple of 24, MS/main.f:273-278): walls (index
+ * 113) at z = 0..5 and z = LenZ-6..LenZ-1, a wall layer z = Lenwwtop..LenZ-7
+ * and, from z = Lenww up, side walls leaving an aperture of Laperture grid
+ * units around the box centre in x; Si (both sublattices) fills the non-wall
+ * sites of z = 6..Len-1; then the two closing passes in wall mode over
+ * z = 6..Lenwwtop+9. */
+static void set_finfet(ora_t *o, int len, int lenww, int lenwwtop, int lap)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz;
+    int xl = (int)(0.5f * (float)(lx - lap)), xr = (int)(0.5f * (float)(lx + lap));
+    set_walls(o, 0, 5);
+    for (int z = lenww; z <= lz - 7; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                if (x >= xl && x < xr) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
+                mvbits(WALL, LEN_INDEX, v, POS_INDEX);
+            }
+    set_walls(o, lenwwtop, lz - 7);
+    set_walls(o, lz - 6, lz - 1);
+    for (int z = 6; z <= len - 1; z++)
         for (int y = 0; y < ly; y++)
             for (int x = 0; x < lx; x++) {
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                if (wall) {
+                if (is_wall(*v) || !dia_kind(x, y, z)) continue;
+                *v = (int32_t)((uint32_t)*v | (1u << POS_SI) | (1u << POS_OCC));
+            }
+    coor_pass(o, 0, lx - 1, 0, ly - 1, 6, lenwwtop + 9, 1);
+    list_pass(o, 0, lx - 1, 0, ly - 1, 6, lenwwtop + 9, 1);
+}
+
+/* SetCAD, MS/initial/SetCAD.f:24-421 (fresh start), for InitSt 'LA' after
+ * SetT (MS/initial/SetT.f:25-50) and for InitSt 'IN' (MS/main.f:279-280).
+ * LA: geometry id per layer z (`la_geo[z]`, 1 = Si, 10 = wall/air, as
+ * LattGeo; a layer-uniform geometry) and the temperature (K) of the grid
+ * points whose coordinates are all multiples of 3,
+ * `tsub[((z/3)*(ly/3) + y/3)*(lx/3) + x/3]` (TempStat; 10 marks a wall and
+ * is not stored); the Si sites are kept according to the nucleus rule
+ * (Homogeneous T/F).  IN: geometry id per site (`cad_geo[(z*ly + y)*lx + x]`),
+ * every Si site of id 1 occupied.  Only NCrystal = 1, no alloy (the
+ * reference draws the alloy species from the compiler's RAND stream). */
+static void set_cad(ora_t *o, int la)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz, nx3 = lx / 3, ny3 = ly / 3;
+    if (la) {   /* SetT */
+        const int16_t *tsub = o->la_tsub;
+        for (int z = 0; z < lz; z += 3)
+            for (int y = 0; y < ly; y += 3)
+                for (int x = 0; x < lx; x += 3) {
+                    int t = tsub[((size_t)(z / 3) * ny3 + y / 3) * nx3 + x / 3];
+                    if (t != 10) mvbits(t, LEN_T, &o->latt[lidx(o, x, y, z)], POS_T);
+                }
+    }
+    /* walls of SetCAD.f:137-153 and the geometry of :160-236 */
+    for (int z = 0; z < lz; z++) {
+        int edge = z <= 3 || z >= lz - 4;
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int id = la ? o->la_geo[z] : o->cad_geo[((size_t)z * ly + y) * lx + x];
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (edge || id == 10) {
                     *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
                     mvbits(WALL, LEN_INDEX, v, POS_INDEX);
-                } else if (si && dia_kind(x, y, z)) {
-                    int occ;
-                    if (o->homogeneous[0] == 'T') {
+                } else if (id == 1 && dia_kind(x, y, z)) {
+                    int occ = 1;
+                    if (!la) {
+                    } else if (o->homogeneous[0] == 'T') {
                         occ = z <= lz - (int)((o->len_vac + o->len_nuc) / o->sf);
                     } else {
                         int x0 = lx / 2, y0 = ly / 2, z0 = lz - (int)(o->len_vac / o->sf);
@@ -1460,6 +1573,18 @@ int ora_set_la_input(ora_t *o, const int8_t *geo, const int16_t *tsub)
     if (!o->la_geo || !o->la_tsub) ora_fail(o, "allocation failed");
     memcpy(o->la_geo, geo, (size_t)o->lz);
     memcpy(o->la_tsub, tsub, nt * sizeof(int16_t));
+    return 0;
+}
+
+int ora_set_geometry(ora_t *o, const int8_t *geo)
+{
+    if (setjmp(o->jb)) return -1;
+    if (strcmp(o->init_st, "IN")) ora_fail(o, "a per-site geometry is given for InitSt %s", o->init_st);
+    size_t n = (size_t)o->lx * o->ly * o->lz;
+    free(o->cad_geo);
+    o->cad_geo = (int8_t *)malloc(n);
+    if (!o->cad_geo) ora_fail(o, "allocation failed");
+    memcpy(o->cad_geo, geo, n);
     return 0;
 }
 
@@ -1593,7 +1718,9 @@ static void parse_startdat(ora_t *o, const char *path)
         rd_items(o, &r, 1, it); o->len_vac = to_real(it[0]);
         rd_items(o, &r, 1, it); o->len_nuc = to_real(it[0]);
         rd_items(o, &r, 1, it); snprintf(o->homogeneous, sizeof o->homogeneous, "%.1s", it[0]);
-    } else if (!strcmp(o->init_st, "IN") || !strcmp(o->init_st, "SH") || !strcmp(o->init_st, "ST")) {
+    } else if (!strcmp(o->init_st, "IN")) {     /* MS/main.f:116-117: the geometry file name */
+        if (!rd_line(&r)) { fclose(r.f); ora_fail(o, "start.dat: missing geometry file name"); }
+    } else if (!strcmp(o->init_st, "SH") || !strcmp(o->init_st, "ST")) {
         fclose(r.f);
         ora_fail(o, "InitSt %s is not restated by the oracle", o->init_st);
     } else {
@@ -1975,6 +2102,7 @@ void ora_destroy(ora_t *o)
     free(o->la_kind);
     free(o->la_geo);
     free(o->la_tsub);
+    free(o->cad_geo);
     free(o->latt_base);
     free(o->lind_base);
     free(o->mc);
@@ -1993,6 +2121,12 @@ int ora_init(ora_t *o)
     if (!strcmp(o->init_st, "FS")) {
         o->len1 -= o->len1 % 24;
         set_flat(o, o->len1, 0);
+    } else if (!strcmp(o->init_st, "FF")) {      /* MS/main.f:273-278 */
+        o->len1 -= o->len1 % 24;
+        o->len2 -= o->len2 % 24;
+        o->len3 -= o->len3 % 24;
+        o->len4 -= o->len4 % 24;
+        set_finfet(o, o->len1, o->len2, o->len3, o->len4);
     } else if (!strcmp(o->init_st, "F")) {
         o->len1 -= o->len1 % 24;
         set_flat(o, o->len1, 1);
@@ -2000,9 +2134,15 @@ int ora_init(ora_t *o)
         set_nc(o, o->len1, o->len2, o->len3, 0);
     } else if (!strcmp(o->init_st, "S")) {       /* MS/main.f:257-258 */
         set_nc(o, o->len1, o->len1, o->len1, 1);
+    } else if (!strcmp(o->init_st, "I")) {       /* MS/main.f:245-246 */
+        set_invp(o, o->len1, o->len2);
     } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
         if (!o->la_geo) ora_fail(o, "InitSt LA needs the geometry and temperature input (ora_set_la_input)");
-        set_cad_la(o, o->la_geo, o->la_tsub);
+        set_cad(o, 1);
+    } else if (!strcmp(o->init_st, "IN")) {      /* MS/main.f:279-280 */
+        if (!o->cad_geo) ora_fail(o, "InitSt IN needs the per-site geometry (ora_set_geometry)");
+        if (o->ncrystal != 1) ora_fail(o, "the IN initializer is restated for NCrystal = 1");
+        set_cad(o, 0);
     } else {
         ora_fail(o, "initialization not_implemented in the oracle: %s", o->init_st);
     }

@@ -51,6 +51,9 @@ int ora_init(ora_t *o);
  * temperature (K) of the grid points with x, y, z multiples of 3, index
  * ((z/3)*(LenY/3) + y/3)*(LenX/3) + x/3.  Copied.  0 on success. */
 int ora_set_la_input(ora_t *o, const int8_t *geo, const int16_t *tsub);
+/* InitSt IN input: the LattGeo id of every site (1 = Si, 10 = wall, 0 =
+ * empty), int8 [z][y][x], LENZ*LENY*LENX values (SetCAD.f:155-236). */
+int ora_set_geometry(ora_t *o, const int8_t *geo);
 /* Advance up to n events (stops early on the reference's exit conditions).
  * Returns 0 ok, 1 "few MC particles" stop, 2 exit condition reached,
  * <0 error.  Writes output frames into `outdir` when non-NULL.             */

@@ -2,8 +2,9 @@
  * mks_oracle_main.c — command-line driver for the oracle (test
  * infrastructure): runs a start.dat the way mulskips.e does, in the current
  * directory.  Usage: mks_oracle LENX LENY LENZ [numbers.txt] [num_mc_max]
- * [geo.bin temp.bin]; the last two are the InitSt LA input of
- * ora_set_la_input as raw int8 / int16 arrays.
+ * [geo.bin [temp.bin]]; with both, the InitSt LA input of
+ * ora_set_la_input as raw int8 / int16 arrays; with geo.bin alone, the
+ * InitSt IN per-site geometry of ora_set_geometry (raw int8).
  */
 #include <stdio.h>
 #include <stdint.h>
@@ -13,7 +14,7 @@
 int main(int argc, char **argv)
 {
     if (argc < 4) {
-        fprintf(stderr, "usage: %s LENX LENY LENZ [numbers.txt] [num_mc_max] [geo.bin temp.bin]\n", argv[0]);
+        fprintf(stderr, "usage: %s LENX LENY LENZ [numbers.txt] [num_mc_max] [geo.bin [temp.bin]]\n", argv[0]);
         return 2;
     }
     const char *numbers = argc > 4 ? argv[4] : NULL;
@@ -24,7 +25,18 @@ int main(int argc, char **argv)
         printf("%s\n", ora_last_error());
         return 1;
     }
-    if (argc > 7) {
+    if (argc == 7) {
+        size_t n = (size_t)atoi(argv[1]) * atoi(argv[2]) * atoi(argv[3]);
+        int8_t *geo = (int8_t *)malloc(n);
+        FILE *fg = fopen(argv[6], "rb");
+        int ok = geo && fg && fread(geo, 1, n, fg) == n;
+        if (fg) fclose(fg);
+        if (!ok || ora_set_geometry(o, geo)) {
+            printf("cannot load the geometry %s\n", argv[6]);
+            return 1;
+        }
+        free(geo);
+    } else if (argc > 7) {
         size_t nz = (size_t)atoi(argv[3]);
         size_t nt = (size_t)(atoi(argv[1]) / 3) * (atoi(argv[2]) / 3) * (atoi(argv[3]) / 3);
         int8_t *geo = (int8_t *)malloc(nz);

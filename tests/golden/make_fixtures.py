@@ -18,6 +18,14 @@ Fixtures written:
                          layer, checked here) and LA/temp_sub.npz (TempStat at
                          the grid points with x, y, z multiples of 3, int16,
                          index [z/3, y/3, x/3])
+  CAD/start.dat, I0000000{0,1}.xyz.gz, log.txt
+                         the reference's CAD regression case (InitSt IN, one
+                         coverage species), and its geometry from
+                         CAD-input.tar.gz as CAD/geo.npz: the LattGeo id of
+                         every site, int8 [z, y, x]; each line of the file is
+                         one layer and, as Fortran's list-directed READ does,
+                         only its first LenX*LenY values are kept (line 168
+                         carries one value more)
   refwriter/start.dat    start.dat written by the reference's
                          pymulskips.setuprun.run_mulskips (setup_only) for the
                          plain Si(001) process object of mulskips_gb300.setuprun
@@ -30,7 +38,7 @@ import shutil
 REF = os.environ.get("MULSKIPS_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 RT = os.path.join(REF, "regression-tests", "input-and-references-files")
-CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere"]
+CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet"]
 
 
 def numbers_list():
@@ -77,6 +85,28 @@ def la_case(lx=480, ly=240, lz=240):
     np.savez_compressed(os.path.join(d, "temp_sub.npz"), t=tmp[::3, ::3, ::3].astype(np.int16))
 
 
+def cad_case(lx=480, ly=240, lz=240):
+    import io
+    import tarfile
+    import numpy as np
+    d = os.path.join(HERE, "CAD")
+    os.makedirs(d, exist_ok=True)
+    shutil.copyfile(os.path.join(RT, "start-CAD.dat"), os.path.join(d, "start.dat"))
+    shutil.copyfile(os.path.join(RT, "log-CAD.txt"), os.path.join(d, "log.txt"))
+    for fr in ("I00000000", "I00000001"):
+        with open(os.path.join(RT, f"{fr}-CAD.xyz"), "rb") as fi, \
+                gzip.GzipFile(os.path.join(d, f"{fr}.xyz.gz"), "wb", compresslevel=9, mtime=0) as fo:
+            fo.write(fi.read())
+    rows = []
+    with tarfile.open(os.path.join(RT, "CAD-input.tar.gz")) as tf:
+        for line in io.TextIOWrapper(tf.extractfile(f"LattGeo.{lx}x{ly}x{lz}.withzeros.dat")):
+            vals = line.split()
+            assert len(vals) >= lx * ly
+            rows.append(np.array(vals[:lx * ly], dtype=np.int8))
+    assert len(rows) == lz
+    np.savez_compressed(os.path.join(d, "geo.npz"), g=np.stack(rows).reshape(lz, ly, lx))
+
+
 def reference_writer():
     import sys
     import tempfile
@@ -109,4 +139,5 @@ if __name__ == "__main__":
     numbers_list()
     cases()
     la_case()
+    cad_case()
     reference_writer()

@@ -4,8 +4,10 @@ reference's own regression outputs byte for byte
 each, RunType T, IDUM 9117116, 480^3 box; cube and cube-zigzag, a free-standing
 3C-SiC parallelepiped (SetNC) grown for 10^7 events, the latter with
 PtransZig = 0.8, i.e. arm-chair stacking through IF_Arm_Choice / FIND_SN /
-FIND_NN; LA, the laser-anneal rate law on a 480x240x240 box with a per-site
-temperature field, 10^6 events)."""
+FIND_NN; sphere (SetNCSp); inverted-pyramid (SetInvPOff, 3C-SiC); finfet
+(SetSiFINFET, Si between walls); LA, the laser-anneal rate law on a
+480x240x240 box with a per-site temperature field, 10^6 events; CAD, SetCAD
+on a per-site geometry grown by CVD with one coverage species)."""
 import numpy as np
 import gzip
 import os
@@ -39,7 +41,7 @@ def golden_log_numbers(case):
     return m.groups(), n.groups()
 
 
-@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag", "sphere"])
+@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet"])
 def test_regression_frames_identical(case, oracle_lib, tmp_path):
     d, out = run_case(case, tmp_path)
     for fr in ("I00000000", "I00000001"):
@@ -85,6 +87,36 @@ def test_la_regression_frames_identical(oracle_lib, tmp_path):
     n = re.search(r"NatNvoidNad\s+(\d+)\s+(\d+)\s+(\d+)", r.stdout)
     assert n.groups() == (nat, nvoid, nad)
     assert "Atoms,Voids,AdAtoms 63828 0 2856" in " ".join(r.stdout.split())
+
+
+def test_cad_regression_frames_identical(oracle_lib, tmp_path):
+    """InitSt IN: SetCAD on the per-site regression geometry (tests/golden/CAD,
+    480x240x240, Si below a patterned wall layer) grown by CVD with one
+    coverage species (H: PtransAbs / PtransDes, SetProbability.f and
+    Get_Prob.f's coverage branches), 3e6 events, RunType T.  As for the LA
+    case the reference frames come from a SetCAD that applied LattGeo line
+    z-4 to layer z, so the geometry is fed shifted by four layers."""
+    d = tmp_path / "CAD"
+    d.mkdir()
+    shutil.copy(os.path.join(GOLDEN, "CAD", "start.dat"), d / "start.dat")
+    geo = np.load(os.path.join(GOLDEN, "CAD", "geo.npz"))["g"].astype(np.int8)
+    shifted = geo.copy()
+    shifted[4:] = geo[:-4]
+    shifted.tofile(d / "geo.bin")
+    r = subprocess.run([ORACLE_EXE, *LA_BOX, os.path.join(GOLDEN, "numberslist.txt"), "0", str(d / "geo.bin")],
+                       cwd=d, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    for fr in ("I00000000", "I00000001"):
+        with gzip.open(os.path.join(GOLDEN, "CAD", fr + ".xyz.gz"), "rb") as f:
+            gold = f.read()
+        assert (d / (fr + ".xyz")).read_bytes() == gold, f"CAD {fr}.xyz differs from the reference"
+    (it, t, x, y, z), (nat, nvoid, nad) = golden_log_numbers("CAD")
+    m = re.search(r"Iter, Time, Site\s+(\d+)\s+([0-9.Ee+-]+)\s+(\d+)\s+(\d+)\s+(\d+)", r.stdout)
+    assert m.group(1) == it and (m.group(3), m.group(4), m.group(5)) == (x, y, z)
+    assert abs(float(m.group(2)) - float(t)) <= 1e-10 * abs(float(t))
+    n = re.search(r"NatNvoidNad\s+(\d+)\s+(\d+)\s+(\d+)", r.stdout)
+    assert n.groups() == (nat, nvoid, nad)
+    assert "Atoms,Voids,AdAtoms 78400 0 3198" in " ".join(r.stdout.split())
 
 
 def test_ran3_is_deterministic_and_in_range(oracle_lib):
