@@ -38,7 +38,7 @@ import shutil
 REF = os.environ.get("MULSKIPS_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 RT = os.path.join(REF, "regression-tests", "input-and-references-files")
-CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet"]
+CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet", "CVD-Si-SiH2"]
 
 
 def numbers_list():

@@ -5,7 +5,8 @@ each, RunType T, IDUM 9117116, 480^3 box; cube and cube-zigzag, a free-standing
 3C-SiC parallelepiped (SetNC) grown for 10^7 events, the latter with
 PtransZig = 0.8, i.e. arm-chair stacking through IF_Arm_Choice / FIND_SN /
 FIND_NN; sphere (SetNCSp); inverted-pyramid (SetInvPOff, 3C-SiC); finfet
-(SetSiFINFET, Si between walls); LA, the laser-anneal rate law on a
+(SetSiFINFET, Si between walls); CVD-Si-SiH2, Si(001) under one coverage
+species to a KMC time of 105 s (4.3e7 events); LA, the laser-anneal rate law on a
 480x240x240 box with a per-site temperature field, 10^6 events; CAD, SetCAD
 on a per-site geometry grown by CVD with one coverage species)."""
 import numpy as np
@@ -41,7 +42,8 @@ def golden_log_numbers(case):
     return m.groups(), n.groups()
 
 
-@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet"])
+@pytest.mark.parametrize("case", ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet",
+                                  "CVD-Si-SiH2"])
 def test_regression_frames_identical(case, oracle_lib, tmp_path):
     d, out = run_case(case, tmp_path)
     for fr in ("I00000000", "I00000001"):
