@@ -12,6 +12,9 @@
  *   mks_create / mks_destroy     module state + AllocateArrays
  *                                (defsystem.f:49-68, AllocateArrays.f:24-45)
  *   mks_set_rates                SetProbability (SetProbability.f:21-143)
+ *   mks_set_coverage_rates       its PtransAbs / PtransDes part (:121-140),
+ *                                with IndexEvent_Abs (Get_Prob.f:22-52),
+ *                                absorption.f and desorption.f
  *   mks_init_flat                SetSi / SetSiC3C (SetSi.f:25-221,
  *                                SetSiC3C.f:25-199), main.f:237-239,224-226
  *   mks_load_lattice             continuation / CAD load of LattCoo
@@ -58,17 +61,20 @@ typedef struct mks_handle mks_handle;
 /* One replica's setup (the scalar part of start.dat, main.f:83-212). */
 typedef struct {
     int32_t lenx, leny, lenz;      /* LenX, LenY, LenZ; LenX, LenY multiples of 12, LenZ of 3 */
-    int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (must be 0)          */
+    int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (0, or 1 with NCrystal <= 2) */
     int32_t list_crystal[3];       /* atomic numbers (ListCrystal)               */
     double ptrans_zig;             /* PtransZig; the engine requires 1.0         */
     double sf;                     /* super-lattice parameter in Angstrom        */
     uint64_t seed;                 /* IDUM / replica seed                        */
+    int32_t list_cov[3];           /* coverage atomic numbers (ListCov, main.f:91) */
+    int32_t pad;
 } mks_config;
 
 /* One applied event (the trace format of the oracle and of mks_replay). */
 typedef struct {
     int32_t x, y, z;               /* grid coordinates of the event site         */
-    int8_t itrans;                 /* 1..3 deposition of that species, 4 evaporation */
+    int8_t itrans;                 /* 1..3 deposition of that species, 4 evaporation,
+                                      5 desorption, 6 absorption of coverage species 1 */
     int8_t arm;                    /* arm-chair stacking choice (must be 0)      */
     int16_t pad;
 } mks_event;
@@ -85,6 +91,7 @@ typedef struct {
     double rms_roughness;          /* RMS of the column heights, grid units      */
     double total_rate;             /* sum of all event rates (FP64)              */
     int64_t nonepitaxial;          /* off-lattice bulk atoms (stacking faults)   */
+    int64_t covered;               /* empty sites carrying the coverage species (NumCovTotal) */
 } mks_observables;
 
 typedef struct {
@@ -106,6 +113,15 @@ int mks_last_error(char *buf, int32_t len);
 /* ptransE: 3*4^6 doubles indexed [s][n1][n2][n3][c1][c2][c3] (the PTransE
  * array of defsystem.f:63-64); ptransD: 3x3 doubles [s][coor-1].          */
 int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
+/* Coverage species (NCov = 1): ptransAbs, ptransDes are 3x3 doubles
+ * [coverage species][coor-1] (PtransAbs / PtransDes, SetProbability.f:
+ * 121-140; only the first species' row may be nonzero).  An empty site of
+ * coordination n then carries deposition + absorption at
+ * sum_s PtransD(s,n) + PtransAbs(1,n) (Get_Prob.f:186-201), a covered site
+ * desorbs at PtransDes(1,n) (:93-118), and an atom's evaporation key counts
+ * its covered neighbours (PE(NSiC,n1,n2,0,c,0,0), :309-312).  Replaces
+ * IndexEvent_Abs / absorption.f / desorption.f.                            */
+int mks_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes);
 /* kind 'S' = SetSi (InitSt FS), 'C' = SetSiC3C (InitSt F); len1 is the slab
  * height, rounded down to a multiple of 24 as main.f:226,238 does.         */
 int mks_init_flat(mks_handle *h, char kind, int32_t len1);
@@ -147,8 +163,10 @@ int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events,
 int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
 /* Sites listed in an output frame, as compact-state indices in the
  * reference's z, y, x scan order (WriteMolMolXYZFile.f:171-260): kind 0 the
- * atoms with coordination <= 3, kind 1 the voids.  *n gets the count; the
- * indices are written when idx is non-NULL and cap >= *n.                  */
+ * atoms with coordination <= 3 and, with a coverage species, the covered
+ * sites (the H / Cl lines, :176-178), kind 1 the voids (covered or not).
+ * *n gets the count; the indices are written when idx is non-NULL and
+ * cap >= *n.                                                               */
 int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int64_t *n);
 int mks_get_observables(mks_handle *h, mks_observables *obs);
 int mks_get_status(mks_handle *h, mks_status *st);
@@ -159,6 +177,9 @@ int mks_get_status(mks_handle *h, mks_status *st);
  * ptransD + i*9.                                                           */
 int mks_batch_create(const mks_config *cfgs, int32_t n, mks_handle **out);
 int mks_batch_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
+/* mks_set_coverage_rates per replica: replica i uses ptransAbs + i*9 and
+ * ptransDes + i*9.                                                         */
+int mks_batch_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes);
 int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1);
 int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
                   int64_t max_events_each, double max_time_each, int64_t *events_total);

@@ -18,7 +18,8 @@ ERRORS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "invariant violated", 
 class MksConfig(C.Structure):
     _fields_ = [("lenx", C.c_int32), ("leny", C.c_int32), ("lenz", C.c_int32),
                 ("ncrystal", C.c_int32), ("ncov", C.c_int32), ("list_crystal", C.c_int32 * 3),
-                ("ptrans_zig", C.c_double), ("sf", C.c_double), ("seed", C.c_uint64)]
+                ("ptrans_zig", C.c_double), ("sf", C.c_double), ("seed", C.c_uint64),
+                ("list_cov", C.c_int32 * 3), ("pad", C.c_int32)]
 
 
 class MksEvent(C.Structure):
@@ -34,7 +35,7 @@ class MksObservables(C.Structure):
     _fields_ = [("events", C.c_int64), ("time", C.c_double), ("atoms", C.c_int64),
                 ("undercoord", C.c_int64), ("mc_sites", C.c_int64), ("voids", C.c_int64),
                 ("species", C.c_int64 * 3), ("mean_height", C.c_double), ("rms_roughness", C.c_double),
-                ("total_rate", C.c_double), ("nonepitaxial", C.c_int64)]
+                ("total_rate", C.c_double), ("nonepitaxial", C.c_int64), ("covered", C.c_int64)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -60,6 +61,7 @@ SIGNATURES = {
     "mks_version": (C.c_char_p, []),
     "mks_last_error": (C.c_int, [C.c_char_p, C.c_int32]),
     "mks_set_rates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mks_set_coverage_rates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_init_flat": (C.c_int, [C.c_void_p, C.c_char, C.c_int32]),
     "mks_load_lattice": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mks_get_lattice": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -76,6 +78,7 @@ SIGNATURES = {
     "mks_get_status": (C.c_int, [C.c_void_p, C.POINTER(MksStatus)]),
     "mks_batch_create": (C.c_int, [C.POINTER(MksConfig), C.c_int32, C.POINTER(C.c_void_p)]),
     "mks_batch_set_rates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mks_batch_set_coverage_rates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_batch_init_flat": (C.c_int, [C.c_void_p, C.c_char, C.c_void_p]),
     "mks_batch_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double,
                                 C.POINTER(C.c_int64)]),

@@ -58,6 +58,7 @@ struct RepDev {
     int NA, NB, NZ, pitch;
     int nqa, nqb, quad_base;
     int single;              // NCrystal = 1: only species 1 on the lattice
+    int cov;                 // one coverage species: species value 3 is a covered empty site
     double tau, T0, t_max;
     long long ev_max;
     unsigned long long seed;
@@ -66,7 +67,7 @@ struct RepDev {
     unsigned int window;
     int active, stop_reason, pad1;
     float rate[64];          // per class; CLS_ISO is computed per event
-    float spcum[3][2];       // cumulative species fractions per deposition coordination
+    float spcum[3][3];       // per coordination: cumulative fractions of species 1, 1+2, all deposition
 };
 
 struct QuadDev {
@@ -313,7 +314,7 @@ __global__ void k_class_hist(const RepDev *reps, const QuadDev *quads, int q0, i
             int a = Q.a0 + ia, b = Q.b0 + ib;
             if ((a + b + (z >> 1)) & 1) continue;
             if (!event_byte(L.get(a, b, z))) continue;
-            atomicAdd(&sh[site_class(L, a, b, z)], 1u);
+            atomicAdd(&sh[site_class(L, a, b, z, false, R.cov != 0)], 1u);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < NCLASS; i += blockDim.x)
@@ -333,6 +334,7 @@ __global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsi
     const uint8_t *st = st_all + R.st_off;
     const int upr = R.pitch / 16, nslab = (R.NZ + OBS_ZSLAB - 1) / OBS_ZSLAB;
     const int64_t zs = (int64_t)R.NB * R.pitch;
+    const bool covm = R.cov != 0;
     unsigned long long atoms = 0, under = 0, voids = 0, sp1 = 0, sp2 = 0, sp3 = 0;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)nslab * R.NB * upr;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -361,7 +363,10 @@ __global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsi
                     uint8_t sb = by[k];
                     if (((k + par) & 1) || sb == 0 || sb == WALL) continue;
                     int sp = sp_of(sb), co = co_of(sb);
-                    if (sp) {
+                    if (covm && sp == COVSP) {         // covered empty site: counted in the species-3 slot
+                        sp3++;
+                        voids += co == 4;
+                    } else if (sp) {
                         atoms++;
                         under += co <= 3;
                         sp1 += sp == 1;
@@ -429,14 +434,20 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
         int a = x1 >> 1, b = y1 >> 1;
         bool ok = (e.x % 3 == 0) && (e.y % 3 == 0) && (e.z % 3 == 0) && ((x1 & 1) == (z1 & 1)) &&
                   ((y1 & 1) == (z1 & 1)) && z1 >= 0 && z1 < R.NZ && a < R.NA && b < R.NB && e.arm == 0;
-        int c = ok ? site_class(L, a, b, z1) : CLS_NONE;
+        const bool cov = R.cov != 0;
+        int c = ok ? site_class(L, a, b, z1, false, cov) : CLS_NONE;
+        bool atom_cls = c == CLS_ISO || (cov ? c >= CLS_COV0 : c >= CLS_OCC0);
         Touched tc;
         int err = 1;
         if (ok && c != CLS_NONE) {
             if (e.itrans >= 1 && e.itrans <= 3 && c >= CLS_C1 && c <= CLS_C3)
-                err = apply_deposition(L, a, b, z1, e.itrans, tc);
-            else if (e.itrans == 4 && c >= CLS_ISO)
-                err = apply_evaporation(L, a, b, z1, tc);
+                err = apply_deposition(L, a, b, z1, e.itrans, tc, cov);
+            else if (e.itrans == 4 && atom_cls)
+                err = apply_evaporation(L, a, b, z1, tc, cov);
+            else if (cov && e.itrans == 5 && c >= CLS_D1 && c < CLS_COV0)   // desorption, main.f:346-349
+                err = apply_coverage(L, a, b, z1, false, tc);
+            else if (cov && e.itrans == 6 && c >= CLS_C1 && c <= CLS_C3 && c != CLS_C1D)   // absorption, :350-356
+                err = apply_coverage(L, a, b, z1, true, tc);
         }
         if (err) {
             set_error(status, DERR_INVARIANT, (int)i);
@@ -455,7 +466,7 @@ struct __align__(128) TileShared {
     uint8_t dirty[WB_MAX * WMAX];              // staged rows changed by events
     int cnt[64];
     float rate[64];
-    float spcum[3][2];
+    float spcum[3][3];
     float G[4];                                // LA: sum over event sites of d(rate)/d(theta)
     int dcnt[3];                               // LA: net crystal atoms per species added by this tile
     int nlist;
@@ -544,7 +555,7 @@ struct RepLocal {
     int NA, NB, NZ, pitch;
     double tau;
     unsigned long long seed;
-    int active, single;
+    int active, single, cov;
 };
 __device__ __forceinline__ RepLocal rep_local(const RepDev &R)
 {
@@ -558,6 +569,7 @@ __device__ __forceinline__ RepLocal rep_local(const RepDev &R)
     r.seed = R.seed;
     r.active = R.active;
     r.single = R.single;
+    r.cov = R.cov;
     return r;
 }
 
@@ -573,8 +585,8 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 // match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
 __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh,
-                                           bool use_pos, int zw0, int wz, bool single, const LADev *A = nullptr,
-                                           double t_mid = 0.0)
+                                           bool use_pos, int zw0, int wz, bool single, bool cov,
+                                           const LADev *A = nullptr, double t_mid = 0.0)
 {
     TileShared &S = g_tile;
     const unsigned FULL = 0xffffffffu;
@@ -599,7 +611,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             z = zl + dz;
             ib = k / hw;
             ia = 2 * (k - ib * hw) + ((a0 + b0 + ib + (z >> 1)) & 1);
-            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single);
+            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single, cov);
         }
         unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
         if (cls != CLS_NONE) {
@@ -759,7 +771,10 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                 if (!(uacc * S.rate[cls] < r_true)) continue;   // null event: time only
             }
         }
-        if (cls == CLS_C1D) {
+        int covev = 0;                                 // 1 absorption, 2 desorption
+        if (R.cov && cls >= CLS_D1 && cls < CLS_COV0) {
+            covev = 2;                                 // main.f:346-349
+        } else if (cls == CLS_C1D) {
             // unsupported coor-1 site: Get_Prob.f:181-184 fixes IndexEvent = 1
             // (species 1) with its 1e-8 rate, whatever the tables say
             sp = 1;
@@ -776,15 +791,35 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                         sc[j] += -(double)A->dEdep[s0][co - 1][j] / ((double)KB_EV_F * (double)A->Tm[s0]);
                 }
             } else {
-                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
+                // deposition of a species or, past the deposition share,
+                // absorption of the coverage species (Get_Prob.f:186-201)
+                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : (u < S.spcum[co - 1][2] ? 3 : 0));
+                if (!sp) covev = 1;
             }
         } else if (A && sc && lane == 0 && cls >= CLS_OCC0) {
             for (int j = 0; j < 4; j++) sc[j] += -(double)A->dE[cls][j] / ((double)KB_EV_F * (double)Tsite);
         }
+        int ta = a, tb = b, tz = z;
+        if (covev) {
+            // absorption.f / desorption.f: only the site byte changes; lanes
+            // 1..4 take its neighbours for re-classification
+            int v = lane == 0 ? cov_event_state(L, a, b, z, covev == 1) : 0;
+            if (__shfl_sync(FULL, v, 0) < 0) return -DERR_INVARIANT;
+            __syncwarp();
+            if (lane == 0) L.put(a, b, z, (uint8_t)v);
+            if (lane >= 1 && lane <= 4) {
+                int da, db, dz;
+                nb_off(z & 1, lane - 1, da, db, dz);
+                ta = a + da;
+                tb = b + db;
+                tz = z + dz;
+            }
+            __syncwarp();
+        } else {
         // stage 1: the event site (every lane derives the context, lane 0 writes)
         EvCtx e;
         uint8_t sx0 = L.get(a, b, z);
-        if (ev_prepare(sx0, a, b, z, sp, e)) return -DERR_INVARIANT;
+        if (ev_prepare(sx0, a, b, z, sp, e, R.cov != 0)) return -DERR_INVARIANT;
         if (A && lane == 0) {
             if (sp) S.dcnt[sp - 1]++;
             else S.dcnt[sp_of(sx0) - 1]--;
@@ -792,7 +827,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         if (lane == 0) L.put(a, b, z, ev_begin_state(e));
         __syncwarp();
         // stage 2: lanes 1..4 update the four neighbours, independent of one another
-        int ta = a, tb = b, tz = z, r2 = 0;
+        int r2 = 0;
         if (lane >= 1 && lane <= 4) r2 = ev_neighbour(L, e, lane - 1, ta, tb, tz);
         unsigned wallm = __ballot_sync(FULL, lane >= 1 && lane <= 4 && r2 == 1);
         if (__ballot_sync(FULL, r2 < 0)) return -DERR_INVARIANT;
@@ -802,6 +837,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         if (lane == 0) r3 = ev_finish(L, e, __popc(wallm));
         if (__shfl_sync(FULL, r3, 0)) return -DERR_INVARIANT;
         __syncwarp();
+        }
         // re-classify the five touched sites, one per lane (lane 0 the event site)
         bool act = lane < 5 && tz >= 0 && tz < NZ;
         int ia = ta - Q.a0, ib = tb - Q.b0;
@@ -810,7 +846,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             hz_lo = min(hz_lo, tz);
             hz_hi = max(hz_hi, tz);
         }
-        int ncls = interior ? site_class(L, ta, tb, tz, R.single != 0) : CLS_NONE;
+        int ncls = interior ? site_class(L, ta, tb, tz, R.single != 0, R.cov != 0) : CLS_NONE;
         uint32_t tkey = interior ? (uint32_t)key_of(ia + HALO, ib + HALO, tz) : 0u;
         // old list slot of each touched site
         int my_slot = -1;
@@ -897,7 +933,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     // the class rates as bounds, so LA tiles reload it
     if (LAM || S.rate_rep != Q.rep) {
         for (int c = lane; c < 64; c += 32) S.rate[c] = Rg.rate[c];
-        if (lane < 6) S.spcum[lane >> 1][lane & 1] = Rg.spcum[lane >> 1][lane & 1];
+        if (lane < 9) S.spcum[lane / 3][lane % 3] = Rg.spcum[lane / 3][lane % 3];
         __syncwarp();
         if (lane == 0) S.rate_rep = LAM ? -1 : Q.rep;
     }
@@ -985,7 +1021,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             __syncwarp();
             SLat L{ax0, bx0, zw0, R.NZ};
             if (A) la_bounds(zw0, zw1 - 1);
-            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, R.single != 0,
+            if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, R.single != 0, R.cov != 0,
                             scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
@@ -1009,7 +1045,8 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             // events here may walk the band upwards without re-staging: bound
             // the rates by the top layer (T rises with z)
             if (A) la_bounds(max(0, zlo - 2), R.NZ - 1);
-            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, R.single != 0, scp ? A : nullptr, t_mid)) {
+            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, R.single != 0, R.cov != 0, scp ? A : nullptr,
+                            t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -1240,13 +1277,18 @@ __global__ void k_lr_grad(const double *score, const double *f, int n, int use_b
 // ---- frame writer support: order-preserving selection of listed sites ----
 // kind 0: atoms with coordination <= 3 (the main I*.xyz list,
 // WriteMolMolXYZFile.f:171-215); kind 1: voids (empty, coordination 4, the
-// O lines and _v.xyz, :216-260).  Sites are visited in layer, row, column
-// order, which is the reference's z, y, x scan order.
+// O lines and _v.xyz, :216-260).  Kinds 2 and 3 are the same lists in
+// coverage mode: covered sites join the main list (the H / Cl lines of
+// :176-178) and covered voids the voids.  Sites are visited in layer, row,
+// column order, which is the reference's z, y, x scan order.
 __device__ __forceinline__ bool frame_pick(uint8_t s, int kind)
 {
     if (s == 0 || s == WALL) return false;
-    if (kind == 0) return sp_of(s) != 0 && co_of(s) <= 3;
-    return sp_of(s) == 0 && co_of(s) == 4;
+    int sp = sp_of(s), co = co_of(s);
+    if (kind == 0) return sp != 0 && co <= 3;
+    if (kind == 1) return sp == 0 && co == 4;
+    if (kind == 2) return sp == COVSP || (sp != 0 && co <= 3);
+    return (sp == 0 || sp == COVSP) && co == 4;
 }
 
 // The padded lattice is read as 16-byte units (row-major, so unit order is
@@ -1357,6 +1399,8 @@ struct RepHost {
     int64_t st_off;
     double ptransE[3 * 4096];
     double ptransD[9];
+    double ptransAbs[9] = {0};  // [coverage species][coor-1] (SetProbability.f:121-131)
+    double ptransDes[9] = {0};  // [coverage species][coor-1] (:132-140)
     bool rates_set = false;
     int64_t t_layer_off = -1;   // offset in d_tlayer once a temperature field is loaded
 };
@@ -1408,17 +1452,37 @@ namespace {
 void rate_tables(const RepHost &r, RepDev &d)
 {
     for (int c = 0; c < 64; c++) d.rate[c] = 0.f;
+    const bool cov = r.cfg.ncov > 0;
     const double *pD = r.ptransD;
     for (int co = 1; co <= 3; co++) {
         double p1 = pD[co - 1], p2 = pD[3 + co - 1], p3 = pD[6 + co - 1];
-        double tot = p1 + p2 + p3;
+        double dep = p1 + p2 + p3;
+        // empty site: deposition of any species or absorption of the coverage
+        // species, one rate (Get_Prob.f:186-201)
+        double tot = dep + (cov ? r.ptransAbs[co - 1] : 0.0);
         int cls = co == 1 ? CLS_C1 : (co == 2 ? CLS_C2 : CLS_C3);
         d.rate[cls] = (float)tot;
         d.spcum[co - 1][0] = tot > 0 ? (float)(p1 / tot) : 1.f;
         d.spcum[co - 1][1] = tot > 0 ? (float)((p1 + p2) / tot) : 1.f;
+        d.spcum[co - 1][2] = (tot > 0 && cov) ? (float)(dep / tot) : 1.f;
+        if (cov) d.rate[CLS_D1 + co - 1] = (float)r.ptransDes[co - 1];   // Get_Prob.f:114
     }
     d.rate[CLS_C1D] = 1.e-8f;   // Get_Prob.f:183
     d.rate[CLS_ISO] = 0.f;      // dynamic: 1e5 x tile rate (Get_Prob.f:305)
+    if (cov) {
+        // PE(NSiC, n1, n2, 0, c, 0, 0), Get_Prob.f:309-312
+        for (int sp = 1; sp <= 2; sp++)
+            for (int n1 = 0; n1 <= 3; n1++)
+                for (int n2 = 0; n1 + n2 <= 3; n2++) {
+                    int t = n1 + n2;
+                    if (t < 1) continue;
+                    for (int c = 0; c <= 4 - t; c++) {
+                        double v = r.ptransE[(sp - 1) * 4096 + n1 * 1024 + n2 * 256 + c * 16];
+                        d.rate[CLS_COV0 + (sp - 1) * NCOVCENSUS + cov_census_index(n1, n2, c)] = (float)v;
+                    }
+                }
+        return;
+    }
     for (int sp = 1; sp <= 3; sp++)
         for (int n1 = 0; n1 <= 3; n1++)
             for (int n2 = 0; n2 <= 3; n2++)
@@ -1438,7 +1502,12 @@ int check_config(const mks_config &c)
     if (c.lenx / 6 < 16 || c.leny / 6 < 16)
         return fail(MKS_ERR_ARG, "box side %d/%d too small (needs >= 96 grid units)", c.lenx, c.leny);
     if (c.ncrystal < 1 || c.ncrystal > 3) return fail(MKS_ERR_ARG, "NCrystal must be 1..3");
-    if (c.ncov != 0) return fail(MKS_ERR_UNSUPPORTED, "coverage species (NCov>0) are not in the GPU engine");
+    if (c.ncov < 0 || c.ncov > 1)
+        return fail(MKS_ERR_UNSUPPORTED, "NCov=%d: the GPU engine holds one coverage species at most", c.ncov);
+    if (c.ncov == 1 && c.ncrystal > 2)
+        return fail(MKS_ERR_UNSUPPORTED, "a coverage species needs NCrystal <= 2 (species value 3 marks covered sites)");
+    if (c.ncov == 1 && (c.list_cov[0] <= 0 || c.list_cov[0] >= 113))
+        return fail(MKS_ERR_ARG, "coverage species atomic number %d", c.list_cov[0]);
     if (c.ptrans_zig != 1.0)
         return fail(MKS_ERR_UNSUPPORTED, "PtransZig=%g: arm-chair stacking is not in the compact GPU lattice", c.ptrans_zig);
     return 0;
@@ -1717,7 +1786,8 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         d[i].ev_max = (long long)9e18;
         d[i].seed = r.cfg.seed;
         d[i].active = 1;
-        d[i].single = r.cfg.ncrystal == 1;
+        d[i].single = r.cfg.ncrystal == 1 && r.cfg.ncov == 0;
+        d[i].cov = r.cfg.ncov == 1;
         rate_tables(r, d[i]);
     }
     int rc = upload_reps(h, d);
@@ -1932,6 +2002,10 @@ int obs_impl(mks_handle *h, int rep, mks_observables *o)
     o->species[0] = (int64_t)cnt[3];
     o->species[1] = (int64_t)cnt[4];
     o->species[2] = (int64_t)cnt[5];
+    if (r.cfg.ncov) {              // the species-3 slot counted covered sites
+        o->covered = o->species[2];
+        o->species[2] = 0;
+    }
     double ncols = (double)cnt[6];
     if (ncols > 0) {
         o->mean_height = hs[0] / ncols;
@@ -2006,8 +2080,11 @@ int mks_batch_set_rates(mks_handle *h, const double *ptransE, const double *ptra
     int rc = download_reps(h, d);
     if (rc) return rc;
     for (size_t i = 0; i < h->reps.size(); i++) {
+        const double *pD = ptransD + i * 9;
+        if (h->reps[i].cfg.ncov && (pD[6] != 0.0 || pD[7] != 0.0 || pD[8] != 0.0))
+            return fail(MKS_ERR_UNSUPPORTED, "replica %zu: deposition of a third species with a coverage species", i);
         memcpy(h->reps[i].ptransE, ptransE + i * 3 * 4096, sizeof(double) * 3 * 4096);
-        memcpy(h->reps[i].ptransD, ptransD + i * 9, sizeof(double) * 9);
+        memcpy(h->reps[i].ptransD, pD, sizeof(double) * 9);
         h->reps[i].rates_set = true;
         rate_tables(h->reps[i], d[i]);
     }
@@ -2018,6 +2095,34 @@ int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD)
 {
     if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_set_rates needs a single-replica handle");
     return mks_batch_set_rates(h, ptransE, ptransD);
+}
+
+int mks_batch_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes)
+{
+    if (!h || !ptransAbs || !ptransDes) return fail(MKS_ERR_ARG, "bad arguments");
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        RepHost &r = h->reps[i];
+        if (!r.cfg.ncov) return fail(MKS_ERR_ARG, "replica %zu has no coverage species (NCov = 0)", i);
+        for (int k = 0; k < 9; k++) {
+            double a = ptransAbs[i * 9 + k], b = ptransDes[i * 9 + k];
+            if (!(a >= 0.0) || !(b >= 0.0)) return fail(MKS_ERR_ARG, "negative or NaN coverage rate");
+            if (k >= 3 && (a != 0.0 || b != 0.0))
+                return fail(MKS_ERR_UNSUPPORTED, "rates for a second or third coverage species");
+        }
+        memcpy(r.ptransAbs, ptransAbs + i * 9, sizeof(double) * 9);
+        memcpy(r.ptransDes, ptransDes + i * 9, sizeof(double) * 9);
+        rate_tables(r, d[i]);
+    }
+    return upload_reps(h, d);
+}
+
+int mks_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes)
+{
+    if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_set_coverage_rates needs a single-replica handle");
+    return mks_batch_set_coverage_rates(h, ptransAbs, ptransDes);
 }
 
 int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1)
@@ -2077,6 +2182,7 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
     std::vector<LADev> la(n);
     for (size_t i = 0; i < n; i++) {
         const RepHost &r = h->reps[i];
+        if (r.cfg.ncov) return fail(MKS_ERR_UNSUPPORTED, "LA mode needs NCov = 0 (main.f:118-123)");
         LADev &A = la[i];
         memset(&A, 0, sizeof A);
         A.on = 1;
@@ -2292,7 +2398,10 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
                 int32_t v;
                 if (s == WALL) continue;
                 int sp = sp_of(s), co = co_of(s);
-                v = (co << 24) | (sp ? (1 << 23) : 0) | (sp << 27);
+                if (r.cfg.ncov && sp == COVSP)      // covered empty site: CovInd = ListCov(1), absorption.f:34-36
+                    v = (co << 24) | r.cfg.list_cov[0];
+                else
+                    v = (co << 24) | (sp ? (1 << 23) : 0) | (sp << 27);
                 lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] = v;
             }
     return 0;
@@ -2318,9 +2427,16 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
                     at(a, b, z1) = WALL;
                     continue;
                 }
-                if ((v & 255) != 0) return fail(MKS_ERR_UNSUPPORTED, "coverage species in LattCoo");
                 int occ = (v >> 23) & 1, co = (v >> 24) & 7, sp = (v >> 27) & 7;
-                if (sp > 3 || (occ && !sp) || (!occ && sp)) return fail(MKS_ERR_INVARIANT, "bad LattCoo word %d", v);
+                if ((v & 255) != 0) {
+                    if (!r.cfg.ncov || (v & 255) != r.cfg.list_cov[0])
+                        return fail(MKS_ERR_UNSUPPORTED, "coverage index %d in LattCoo", v & 255);
+                    if (occ || sp || co < 1 || co > 4) return fail(MKS_ERR_INVARIANT, "bad covered LattCoo word %d", v);
+                    at(a, b, z1) = mk(COVSP, co, 0, 0);
+                    continue;
+                }
+                if (sp > (r.cfg.ncov ? 2 : 3) || (occ && !sp) || (!occ && sp))
+                    return fail(MKS_ERR_INVARIANT, "bad LattCoo word %d", v);
                 at(a, b, z1) = mk(sp, co, 0, 0);
             }
     // the first list entry of a coor-1 empty site is its one occupied
@@ -2331,7 +2447,9 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
             for (int a = 0; a < r.NA; a++) {
                 if ((a + b + (z1 >> 1)) & 1) continue;
                 uint8_t s = at(a, b, z1);
-                if (s == WALL || sp_of(s) || co_of(s) != 1) continue;
+                const bool cov = r.cfg.ncov != 0;
+                bool covered = is_cov(s, cov);
+                if (s == WALL || (sp_of(s) && !covered) || co_of(s) != 1) continue;
                 int found = -1;
                 uint8_t ns = 0;
                 for (int d = 0; d < 4; d++) {
@@ -2339,13 +2457,13 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
                     nb_off(z1 & 1, d, da, db, dz);
                     if (z1 + dz < 0 || z1 + dz >= r.NZ) continue;
                     uint8_t t = at(a + da, b + db, z1 + dz);
-                    if (t != WALL && sp_of(t)) {
+                    if (t != WALL && atom_sp(t, cov)) {
                         found = d;
                         ns = t;
                     }
                 }
                 if (found < 0) return fail(MKS_ERR_INVARIANT, "coor-1 site without neighbour");
-                at(a, b, z1) = mk(0, 1, found, co_of(ns) < 2 ? 1 : 0);
+                at(a, b, z1) = covered ? mk(COVSP, 1, found, 0) : mk(0, 1, found, co_of(ns) < 2 ? 1 : 0);
             }
     CK(cudaMemcpyAsync(h->d_st + r.st_off, st.data(), st.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -2664,6 +2782,7 @@ int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int
     int nchunk = (int)((nunit + FRAME_UNITS - 1) / FRAME_UNITS);
     unsigned int *d_cnt = nullptr;
     CK(cudaMallocAsync(&d_cnt, sizeof(unsigned int) * nchunk, h->stream));
+    if (r.cfg.ncov) kind += 2;
     k_frame_count<<<nchunk, 256, 0, h->stream>>>(h->d_reps, 0, h->d_st, kind, d_cnt);
     CK(cudaGetLastError());
     std::vector<unsigned int> cnt(nchunk);

@@ -18,6 +18,13 @@
 //             (Get_Prob.f:181-184); with species 0 and coordination 0 the
 //             value 0x80 marks a wall site (CovInd 113, SetSi.f:38-46)
 //
+// Coverage mode (one coverage species, NCrystal <= 2): species value 3 marks
+// an EMPTY site carrying the coverage species (LattCoo Occ = 0 with CovInd =
+// ListCov(1), absorption.f:34-36).  A covered site keeps its coordination and
+// list head; the reference clears the whole word when its last neighbour
+// leaves (Evaporation.f:60-67), so a covered site always has coordination
+// 1..4.
+//
 // Site (a, b, z1) sits at grid point x = 3(2a + (z1&1)), y = 3(2b + (z1&1)),
 // z = 3 z1 and exists when (a + b + (z1 >> 1)) is even.  Even layers hold the
 // (x1+y1+z1) mod 4 == 0 sublattice (JumpDia columns 1-4), odd layers the
@@ -41,6 +48,10 @@ MKS_HD int fd_of(uint8_t s) { return (s >> 5) & 3; }
 MKS_HD int dm_of(uint8_t s) { return (s >> 7) & 1; }
 MKS_HD bool is_wall(uint8_t s) { return s == WALL; }
 MKS_HD bool is_occ(uint8_t s) { return s == WALL || (s & 3) != 0; }
+constexpr int COVSP = 3;                       // species value of a covered empty site
+// species of an atom, 0 for an empty (or covered) site; cov selects coverage mode
+MKS_HD int atom_sp(uint8_t s, bool cov) { int sp = s & 3; return (cov && sp == COVSP) ? 0 : sp; }
+MKS_HD bool is_cov(uint8_t s, bool cov) { return cov && (s & 3) == COVSP; }
 MKS_HD uint8_t mk(int sp, int co, int fd, int dm)
 {
     return (uint8_t)((sp & 3) | ((co & 7) << 2) | ((fd & 3) << 5) | ((dm & 1) << 7));
@@ -68,6 +79,21 @@ MKS_HD int rev_dir(int d) { return (d + 2) & 3; }
 constexpr int CLS_NONE = 0, CLS_C1 = 1, CLS_C1D = 2, CLS_C2 = 3, CLS_C3 = 4, CLS_ISO = 5, CLS_OCC0 = 6;
 constexpr int NCENSUS = 19;
 constexpr int NCLASS = CLS_OCC0 + 3 * NCENSUS;   // 63
+// Coverage mode: 6..8 covered site of coordination 1..3 (desorption,
+// Get_Prob.f:93-118), 9.. atom of species sp (1..2) with census (nSi+nWall,
+// nC) summing to 1..3 and c covered neighbours, c <= 4 - census (the PTransE
+// key PE(NSiC, n1, n2, 0, c, 0, 0) of Get_Prob.f:309-312).  C1..C3 carry
+// deposition + absorption (Get_Prob.f:155-201).
+constexpr int CLS_D1 = 6, CLS_COV0 = 9;
+constexpr int NCOVCENSUS = 25;
+
+MKS_HD int cov_census_index(int n1, int n2, int c)
+{
+    // total t = n1 + n2 in 1..3, n1 descending, then c = 0..4-t
+    int t = n1 + n2;
+    int base = (t == 1) ? 0 : (t == 2) ? 8 : 17;
+    return base + (t - n1) * (5 - t) + c;
+}
 
 MKS_HD int census_index(int n1, int n2, int n3)
 {
@@ -99,12 +125,35 @@ MKS_HD bool event_byte(uint8_t s)
 // single: the lattice holds species 1 only, so an atom's census is
 // (coordination, 0, 0) — walls count with species 1 and reciprocity holds —
 // and the neighbours need not be read.
+// cov: coverage mode (then single is ignored: the census reads the neighbours).
 template <class L>
-MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false)
+MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false, bool cov = false)
 {
     uint8_t s = lat.get(a, b, z);
     if (s == 0 || s == WALL) return CLS_NONE;
     int sp = sp_of(s), co = co_of(s);
+    if (cov) {
+        if (sp == COVSP) return (co >= 1 && co <= 3) ? CLS_D1 + co - 1 : CLS_NONE;
+        if (sp != 0) {
+            if (co >= 4) return CLS_NONE;
+            int n1 = 0, n2 = 0, nc = 0;
+            int zp = z & 1;
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+                int da, db, dz;
+                nb_off(zp, d, da, db, dz);
+                uint8_t t = lat.get(a + da, b + db, z + dz);
+                int st = sp_of(t);
+                n1 += (t == WALL || st == 1) ? 1 : 0;
+                n2 += st == 2 ? 1 : 0;
+                nc += st == COVSP ? 1 : 0;
+            }
+            int tot = n1 + n2;
+            if (tot == 0) return CLS_ISO;
+            if (tot > 3) return CLS_NONE;
+            return CLS_COV0 + (sp - 1) * NCOVCENSUS + cov_census_index(n1, n2, nc);
+        }
+    }
     if (sp == 0) {
         if (co == 1) return dm_of(s) ? CLS_C1D : CLS_C1;
         if (co == 2) return CLS_C2;
@@ -134,14 +183,14 @@ MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false)
 // Direction of the unique occupied non-wall neighbour (the NBuff of
 // Evaporation.f:87-104,238-253); -1 if there is none.
 template <class L>
-MKS_HD int occupied_dir(const L &lat, int a, int b, int z)
+MKS_HD int occupied_dir(const L &lat, int a, int b, int z, bool cov = false)
 {
     int r = -1, zp = z & 1;
     for (int d = 0; d < 4; d++) {
         int da, db, dz;
         nb_off(zp, d, da, db, dz);
         uint8_t t = lat.get(a + da, b + db, z + dz);
-        if (t != WALL && sp_of(t) != 0 && co_of(t) <= 3) r = d;
+        if (t != WALL && atom_sp(t, cov) != 0 && co_of(t) <= 3) r = d;
     }
     return r;
 }
@@ -161,6 +210,7 @@ struct EvCtx {
     int sp;        // deposited species, 0 for an evaporation
     int c0;        // coordination bits of the site before the event
     int fdx;       // first-list-entry direction of the site
+    bool cov;      // coverage mode: species 3 is a covered empty site
 };
 
 // Stage 1: occupancy and species of the event site change first; its
@@ -168,27 +218,31 @@ struct EvCtx {
 // 237; Evaporation.f:40-44,218).  ev_prepare only reads the site byte sx;
 // ev_begin also writes the site.  Both return 0, or 1 if the event does not
 // apply to the site.
-MKS_HD int ev_prepare(uint8_t sx, int a, int b, int z, int sp, EvCtx &e)
+MKS_HD int ev_prepare(uint8_t sx, int a, int b, int z, int sp, EvCtx &e, bool cov = false)
 {
     if (sx == WALL) return 1;
-    if (sp ? sp_of(sx) != 0 : sp_of(sx) == 0) return 1;
+    if (sp ? sp_of(sx) != 0 : atom_sp(sx, cov) == 0) return 1;
     e.a = a; e.b = b; e.z = z; e.sp = sp;
     e.c0 = co_of(sx);
     e.fdx = fd_of(sx);
+    e.cov = cov;
     return 0;
 }
 MKS_HD uint8_t ev_begin_state(const EvCtx &e) { return mk(e.sp, e.c0, e.fdx, 0); }
 
 template <class L>
-MKS_HD int ev_begin(L &lat, int a, int b, int z, int sp, EvCtx &e)
+MKS_HD int ev_begin(L &lat, int a, int b, int z, int sp, EvCtx &e, bool cov = false)
 {
-    if (ev_prepare(lat.get(a, b, z), a, b, z, sp, e)) return 1;
+    if (ev_prepare(lat.get(a, b, z), a, b, z, sp, e, cov)) return 1;
     lat.put(a, b, z, ev_begin_state(e));
     return 0;
 }
 
 // Stage 2: update neighbour d.  Returns 1 if it is a wall, 0 otherwise, or a
-// negative code when the state contradicts the cubic model.
+// negative code when the state contradicts the cubic model.  A covered
+// neighbour is an empty site whose coverage survives every change but the
+// loss of its last neighbour (deposition.f:82-191 and Evaporation.f:51-164
+// pass its CovInd on to Get_Prob).
 template <class L>
 MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz)
 {
@@ -198,10 +252,13 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
     uint8_t sy = lat.get(ya, yb, yz);
     if (sy == WALL) return 1;
     int cy = co_of(sy);
+    int ay = atom_sp(sy, e.cov);               // species of an atom, 0 if empty
+    int cv = sp_of(sy) - ay;                   // COVSP on a covered site, else 0
     if (e.sp) {                                // deposition.f:78-235
-        if (sp_of(sy) != 0) {                  // occupied neighbour, :192-230
-            if (cy <= 3) lat.put(ya, yb, yz, mk(sp_of(sy), cy + 1, fd_of(sy), 0));
+        if (ay != 0) {                         // occupied neighbour, :192-230
+            if (cy <= 3) lat.put(ya, yb, yz, mk(ay, cy + 1, fd_of(sy), 0));
         } else if (cy == 0) {                  // new coor-1 MC site, :86-99
+            if (cv) return -6;
             // Get_Prob reads the coordination bits of its single neighbour,
             // i.e. of the event site before stage 3 (Get_Prob.f:156-158)
             lat.put(ya, yb, yz, mk(0, 1, rev_dir(d), e.c0 < 2 ? 1 : 0));
@@ -211,16 +268,16 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
                 int ea, eb, ez;
                 nb_off(yzp, f, ea, eb, ez);
                 uint8_t t = lat.get(ya + ea, yb + eb, yz + ez);
-                if (t != WALL && sp_of(t) != 0) cnt++;
+                if (t != WALL && atom_sp(t, e.cov) != 0) cnt++;
             }
             if (cnt < 2) return -2;
-            lat.put(ya, yb, yz, mk(0, cnt, fd_of(sy), 0));
+            lat.put(ya, yb, yz, mk(cv, cnt, fd_of(sy), 0));
         } else if (cy == 2 || cy == 3) {       // :161-191
-            lat.put(ya, yb, yz, mk(0, cy + 1, fd_of(sy), 0));
+            lat.put(ya, yb, yz, mk(cv, cy + 1, fd_of(sy), 0));
         }
     } else {                                   // Evaporation.f:46-215
-        if (sp_of(sy) != 0) {                  // :166-210
-            if (cy >= 1) lat.put(ya, yb, yz, mk(sp_of(sy), cy - 1, fd_of(sy), 0));
+        if (ay != 0) {                         // :166-210
+            if (cy >= 1) lat.put(ya, yb, yz, mk(ay, cy - 1, fd_of(sy), 0));
             else return -3;
         } else if (cy == 1) {                  // :51-68, reciprocal only
             if (fd_of(sy) == rev_dir(d)) lat.put(ya, yb, yz, 0);
@@ -229,13 +286,13 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
             int f = fd_of(sy), fa, fb, fz;
             nb_off(yz & 1, f, fa, fb, fz);
             uint8_t sf = lat.get(ya + fa, yb + fb, yz + fz);
-            int w = occupied_dir(lat, ya, yb, yz);
+            int w = occupied_dir(lat, ya, yb, yz, e.cov);
             if (w < 0) return -4;
-            lat.put(ya, yb, yz, mk(0, 1, w, co_of(sf) < 2 ? 1 : 0));
+            lat.put(ya, yb, yz, mk(cv, 1, w, (!cv && co_of(sf) < 2) ? 1 : 0));
         } else if (cy == 3) {                  // :124-141
-            lat.put(ya, yb, yz, mk(0, 2, fd_of(sy), 0));
+            lat.put(ya, yb, yz, mk(cv, 2, fd_of(sy), 0));
         } else if (cy == 4) {                  // void -> MC, :142-164
-            lat.put(ya, yb, yz, mk(0, 3, fd_of(sy), 0));
+            lat.put(ya, yb, yz, mk(cv, 3, fd_of(sy), 0));
         }
     }
     return 0;
@@ -257,7 +314,7 @@ MKS_HD int ev_finish(L &lat, const EvCtx &e, int walls)
         int fa, fb, fz;
         nb_off(e.z & 1, e.fdx, fa, fb, fz);
         uint8_t sf = lat.get(e.a + fa, e.b + fb, e.z + fz);
-        int w = occupied_dir(lat, e.a, e.b, e.z);
+        int w = occupied_dir(lat, e.a, e.b, e.z, e.cov);
         if (w < 0) return -5;
         lat.put(e.a, e.b, e.z, mk(0, 1, w, co_of(sf) < 2 ? 1 : 0));
     } else {
@@ -270,10 +327,10 @@ MKS_HD int ev_finish(L &lat, const EvCtx &e, int walls)
 // (deposition.f:24-251) or, with sp = 0, evaporation of the atom there
 // (Evaporation.f:25-262).  Returns 0 or a nonzero code.
 template <class L>
-MKS_HD int apply_event(L &lat, int a, int b, int z, int sp, Touched &tc)
+MKS_HD int apply_event(L &lat, int a, int b, int z, int sp, Touched &tc, bool cov = false)
 {
     EvCtx e;
-    if (ev_begin(lat, a, b, z, sp, e)) return 1;
+    if (ev_begin(lat, a, b, z, sp, e, cov)) return 1;
     tc.n = 5;
     tc.a[0] = a; tc.b[0] = b; tc.z[0] = z;
     int walls = 0;
@@ -287,15 +344,54 @@ MKS_HD int apply_event(L &lat, int a, int b, int z, int sp, Touched &tc)
 }
 
 template <class L>
-MKS_HD int apply_deposition(L &lat, int a, int b, int z, int sp, Touched &tc)
+MKS_HD int apply_deposition(L &lat, int a, int b, int z, int sp, Touched &tc, bool cov = false)
 {
-    return sp >= 1 && sp <= 3 ? apply_event(lat, a, b, z, sp, tc) : 1;
+    return sp >= 1 && sp <= (cov ? 2 : 3) ? apply_event(lat, a, b, z, sp, tc, cov) : 1;
 }
 
 template <class L>
-MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc)
+MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc, bool cov = false)
 {
-    return apply_event(lat, a, b, z, 0, tc);
+    return apply_event(lat, a, b, z, 0, tc, cov);
+}
+
+// Coverage events: the new state of the event site, or -1 if the event does
+// not apply.  Absorption (absorption.f:24-78) covers an empty site of
+// coordination 1..3 keeping its coordination and list; desorption
+// (desorption.f:24-117) uncovers it, and Get_Prob then recomputes the dummy
+// flag of a coor-1 site from its list head's coordination (Get_Prob.f:156-158).
+// Only the site byte changes; its four neighbours' classes follow from it.
+template <class L>
+MKS_HD int cov_event_state(const L &lat, int a, int b, int z, bool absorb)
+{
+    uint8_t s = lat.get(a, b, z);
+    int co = co_of(s);
+    if (s == WALL || co < 1 || co > 3) return -1;
+    if (absorb) return sp_of(s) == 0 ? mk(COVSP, co, fd_of(s), 0) : -1;
+    if (sp_of(s) != COVSP) return -1;
+    int dm = 0;
+    if (co == 1) {
+        int fa, fb, fz;
+        nb_off(z & 1, fd_of(s), fa, fb, fz);
+        dm = co_of(lat.get(a + fa, b + fb, z + fz)) < 2 ? 1 : 0;
+    }
+    return mk(0, co, fd_of(s), dm);
+}
+
+template <class L>
+MKS_HD int apply_coverage(L &lat, int a, int b, int z, bool absorb, Touched &tc)
+{
+    int v = cov_event_state(lat, a, b, z, absorb);
+    if (v < 0) return 1;
+    lat.put(a, b, z, (uint8_t)v);
+    tc.n = 5;
+    tc.a[0] = a; tc.b[0] = b; tc.z[0] = z;
+    for (int d = 0; d < 4; d++) {
+        int da, db, dz;
+        nb_off(z & 1, d, da, db, dz);
+        tc.a[d + 1] = a + da; tc.b[d + 1] = b + db; tc.z[d + 1] = z + dz;
+    }
+    return 0;
 }
 
 // Initial state of SetSi ('FS', SetSi.f:25-221) and SetSiC3C ('F',

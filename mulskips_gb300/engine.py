@@ -26,13 +26,15 @@ def arrhenius_tables(T, e_bond=0.6, nu=1e13, flux=0.5, ncrystal=1):
     return pE, pD
 
 
-def _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed):
+def _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed, list_cov=()):
     c = N.MksConfig()
     c.lenx, c.leny, c.lenz = int(lenx), int(leny), int(lenz)
-    c.ncrystal, c.ncov = int(ncrystal), 0
+    c.ncrystal, c.ncov = int(ncrystal), len(list_cov)
     lc = list(list_crystal) + [0] * (3 - len(list_crystal))
+    lv = list(list_cov) + [0] * (3 - len(list_cov))
     for i in range(3):
         c.list_crystal[i] = int(lc[i])
+        c.list_cov[i] = int(lv[i])
     c.ptrans_zig = float(ptrans_zig)
     c.sf = float(sf)
     c.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -40,15 +42,16 @@ def _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed):
 
 
 class Lattice:
-    """One KMC system on the GPU."""
+    """One KMC system on the GPU.  list_cov: atomic number of the coverage
+    species (at most one; e.g. (1,) for H in CVD)."""
 
     def __init__(self, lenx, leny, lenz, ncrystal=1, list_crystal=(14,), ptrans_zig=1.0, sf=5.43 / 12,
-                 seed=1):
+                 seed=1, list_cov=()):
         self.dims = (int(lenx), int(leny), int(lenz))
         self.na, self.nb, self.nz = lenx // 6, leny // 6, lenz // 3 + 1
         h = C.c_void_p()
         N.check(N.lib().mks_create(C.byref(_cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf,
-                                                 seed)), C.byref(h)))
+                                                 seed, list_cov)), C.byref(h)))
         self._h = h
 
     def close(self):
@@ -73,6 +76,13 @@ class Lattice:
         d = np.ascontiguousarray(ptransD, dtype=np.float64).reshape(-1)
         assert e.size == 3 * 4096 and d.size == 9
         N.check(N.lib().mks_set_rates(self._h, N.ptr(e), N.ptr(d)))
+
+    def set_coverage_rates(self, ptransAbs, ptransDes):
+        """PtransAbs / PtransDes as 3x3 [coverage species][coor-1]."""
+        a = np.ascontiguousarray(ptransAbs, dtype=np.float64).reshape(-1)
+        d = np.ascontiguousarray(ptransDes, dtype=np.float64).reshape(-1)
+        assert a.size == 9 and d.size == 9
+        N.check(N.lib().mks_set_coverage_rates(self._h, N.ptr(a), N.ptr(d)))
 
     def init_flat(self, kind="S", len1=120):
         N.check(N.lib().mks_init_flat(self._h, kind.encode()[:1], int(len1)))
@@ -183,10 +193,10 @@ class Lattice:
 class Batch:
     """Independent replicas of uneven boxes advanced together."""
 
-    def __init__(self, boxes, seeds, ncrystal=1, list_crystal=(14,), sf=5.43 / 12):
+    def __init__(self, boxes, seeds, ncrystal=1, list_crystal=(14,), sf=5.43 / 12, list_cov=()):
         cfgs = (N.MksConfig * len(boxes))()
         for i, (b, s) in enumerate(zip(boxes, seeds)):
-            cfgs[i] = _cfg(b[0], b[1], b[2], ncrystal, list_crystal, 1.0, sf, s)
+            cfgs[i] = _cfg(b[0], b[1], b[2], ncrystal, list_crystal, 1.0, sf, s, list_cov)
         h = C.c_void_p()
         N.check(N.lib().mks_batch_create(cfgs, len(boxes), C.byref(h)))
         self._h = h
@@ -208,6 +218,13 @@ class Batch:
         d = np.ascontiguousarray(ptransD, dtype=np.float64).reshape(-1)
         assert e.size == self.n * 3 * 4096 and d.size == self.n * 9
         N.check(N.lib().mks_batch_set_rates(self._h, N.ptr(e), N.ptr(d)))
+
+    def set_coverage_rates(self, ptransAbs, ptransDes):
+        """Per replica PtransAbs / PtransDes, n x 3 x 3."""
+        a = np.ascontiguousarray(ptransAbs, dtype=np.float64).reshape(-1)
+        d = np.ascontiguousarray(ptransDes, dtype=np.float64).reshape(-1)
+        assert a.size == self.n * 9 and d.size == self.n * 9
+        N.check(N.lib().mks_batch_set_coverage_rates(self._h, N.ptr(a), N.ptr(d)))
 
     def init_flat(self, kind, len1):
         l1 = np.ascontiguousarray(len1, dtype=np.int32)

@@ -44,6 +44,8 @@ struct Input {
     std::string save_final = "F", restart_file, save_coo = "F", coo_file;
     std::vector<double> pE = std::vector<double>(3 * 4096, 0.0);
     std::vector<double> pD = std::vector<double>(9, 0.0);
+    std::vector<double> pAbs = std::vector<double>(9, 0.0);   // [coverage species][coor-1]
+    std::vector<double> pDes = std::vector<double>(9, 0.0);
 };
 
 [[noreturn]] void die(const char *msg)
@@ -180,6 +182,15 @@ Input read_startdat(const char *path)
         if (s < 1 || s > in.ncrystal || el < 1 || el > 3) die("ERROR: 1st index in depo prob block must be <= NCrystal");
         in.pD[(s - 1) * 3 + el - 1] = real_of(it[2]);
     }
+    // absorption, then desorption: NCov*3 records "NCrystal+i  coor  rate"
+    // (SetProbability.f:117-140)
+    for (int blk = 0; blk < 2; blk++)
+        for (int j = 0; j < in.ncov * 3; j++) {
+            it = r.items(3);
+            int s = atoi(it[0].c_str()) - in.ncrystal, el = atoi(it[1].c_str());
+            if (s < 1 || s > in.ncov || el < 1 || el > 3) die("ERROR: index in absorption/desorption block");
+            (blk ? in.pDes : in.pAbs)[(s - 1) * 3 + el - 1] = real_of(it[2]);
+        }
     fclose(f);
     return in;
 }
@@ -251,6 +262,10 @@ struct Frames {
         if (z == 5) return "B";
         return "X";
     }
+    const char *cov_symbol() const
+    {   // WriteMolMolXYZFile.f:177-178: H for CovInd 1, Cl for 17
+        return in.list_cov[0] == 17 ? "Cl" : "H";
+    }
     std::string name(long long iout) const
     {   // GetOutputFileName.f:22-81: first 8 of the 9 digits of 10*Iout
         char d[32];
@@ -291,7 +306,8 @@ struct Frames {
         for (uint32_t i : at) {
             double x, y, z;
             xyz(i, x, y, z);
-            fprintf(f, "%s %10.5f %10.5f %10.5f  \n", symbol(st[i] & 3), x, y, z);
+            fprintf(f, "%s %10.5f %10.5f %10.5f  \n", in.ncov && (st[i] & 3) == 3 ? cov_symbol() : symbol(st[i] & 3),
+                    x, y, z);
         }
         for (uint32_t i : vd) {
             double x, y, z;
@@ -339,7 +355,11 @@ int main()
     printf(" KMC Super-Lattice parameter (ang): %.17g\n", in.sf);
     printf(" Exit strategy: %s\n", in.exit_strategy.c_str());
     printf(" IDUM %lld\n", in.idum);
-    if (in.ncov > 0) die("ERR NOT IMPLEMENTED: coverage species are not in the GPU engine");
+    if (in.ncov > 0) {
+        printf(" Coverage species (NCov= %d ) --> Z: %d %d %d\n", in.ncov, in.list_cov[0], in.list_cov[1],
+               in.list_cov[2]);
+        if (in.ncov > 1) die("ERR NOT IMPLEMENTED: the GPU engine holds one coverage species");
+    }
     if (in.init_st != "FS" && in.init_st != "F") die("initialization not_implemented");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
@@ -347,14 +367,16 @@ int main()
     cfg.leny = ly;
     cfg.lenz = lz;
     cfg.ncrystal = in.ncrystal;
-    cfg.ncov = 0;
+    cfg.ncov = in.ncov;
     for (int i = 0; i < 3; i++) cfg.list_crystal[i] = in.list_crystal[i];
+    for (int i = 0; i < 3; i++) cfg.list_cov[i] = in.list_cov[i];
     cfg.ptrans_zig = in.ptrans_zig;
     cfg.sf = in.sf;
     cfg.seed = (uint64_t)in.idum;
     mks_handle *h = nullptr;
     check(mks_create(&cfg, &h));
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
+    if (in.ncov) check(mks_set_coverage_rates(h, in.pAbs.data(), in.pDes.data()));
     int len1 = in.len[0] - in.len[0] % 24;
     check(mks_init_flat(h, in.init_st == "FS" ? 'S' : 'C', len1));
     mks_observables ob;
@@ -371,7 +393,8 @@ int main()
     for (long long block = 0;; block++) {
         // window factor validated against the serial reference: 0.3 for one
         // species, 0.03 for two or three (fast desorption across tile borders)
-        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
+        // and with a coverage species
+        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 && in.ncov == 0 ? 0.3 : 0.03, &tau));
         int64_t ev = 0;
         check(mks_run(h, tau, chunk, 0, 0.0, &ev, &time));
         events += ev;
@@ -394,7 +417,9 @@ int main()
             }
             if (events >= in.max_iter) break;
         } else {
-            while (time >= (frame + 1) * in.out_time && time <= in.max_time) {
+            // main.f:324-330: a frame whenever Time passes the next output
+            // time, checked before the exit test of :365
+            while (in.out_time > 0 && time >= (frame + 1) * in.out_time) {
                 frame++;
                 fr.write(time, events, frame);
                 printf(" Iter, Time %lld %.17g\n", events, time);

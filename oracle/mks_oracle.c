@@ -2339,6 +2339,17 @@ void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9])
         for (int c = 0; c < 3; c++) ptransD[s * 3 + c] = o->ptransD[s][c];
 }
 
+int ora_ncov(const ora_t *o) { return o->ncov; }
+
+void ora_get_cov_rates(const ora_t *o, double ptransAbs[9], double ptransDes[9])
+{   /* [coverage species][coor-1] */
+    for (int s = 0; s < 3; s++)
+        for (int c = 1; c <= 3; c++) {
+            ptransAbs[s * 3 + c - 1] = o->ptransAbs[s][c];
+            ptransDes[s * 3 + c - 1] = o->ptransDes[s][c];
+        }
+}
+
 /* Conversion to the one-byte-per-site layout of the GPU engine (used by the
  * parity tests to compare states). */
 int64_t ora_compact_state(const ora_t *o, uint8_t *out)
@@ -2380,6 +2391,11 @@ int64_t ora_compact_state(const ora_t *o, uint8_t *out)
                 }
                 /* the dummy rates of Get_Prob (1e-8) and Get_Prob_Ini (1e-6) share the one flag */
                 int dm = (!occ && co == 1 && which == 1 && (pr == (double)1.e-8f || pr == (double)1.e-6f)) ? 1 : 0;
+                /* an empty site carrying a coverage species is species value 3 */
+                if (!occ && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
+                    sp = 3;
+                    dm = 0;
+                }
                 *d = (uint8_t)((sp & 3) | ((co & 7) << 2) | (fd << 5) | (dm << 7));
             }
     return offgrid;
@@ -2409,10 +2425,39 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
         int occ = ibits(v, POS_OCC, LEN_OCC), co = ibits(v, POS_COOR, LEN_COOR);
         int sp = ibits(v, POS_SIC, LEN_SIC);
         int c = 0;
-        if (!occ) {
+        if (!occ && o->ncov > 0 && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
+            if (co >= 1 && co <= 3) c = 6 + co - 1;      /* covered: desorption */
+        } else if (!occ) {
             if (co == 1) c = (p->prob == (double)1.e-8f) ? 2 : 1;
             else if (co == 2) c = 3;
             else if (co == 3) c = 4;
+        } else if (o->ncov > 0) {
+            /* census (nSi+nWall, nC) and covered neighbours as Get_Prob.f:
+             * 215-291 counts them, reciprocity through each neighbour's list */
+            int n_si = 0, n_c = 0, n_w = 0, n_cov = 0;
+            for (int k = 0; k < 4; k++) {
+                int32_t w = *LC(o, p->nn[k]);
+                int cn = ibits(w, POS_COOR, LEN_COOR), ind = *LI(o, p->nn[k]);
+                int nnn[4][3];
+                if (!ibits(w, POS_OCC, LEN_OCC)) {
+                    if (ibits(w, POS_INDEX, LEN_INDEX) == 0) continue;
+                    get_nn_list(o, ind, 1, nnn);
+                    if (in_list(nnn, p->xyz)) n_cov++;
+                    continue;
+                }
+                if (ibits(w, POS_INDEX, LEN_INDEX) == WALL) { n_w++; continue; }
+                get_nn_list(o, ind, (cn >= 1 && cn <= 3) ? 1 : 2, nnn);
+                if (!in_list(nnn, p->xyz)) continue;
+                int s2 = ibits(w, POS_SIC, LEN_SIC);
+                if (s2 == 1) n_si++;
+                if (s2 == 2) n_c++;
+            }
+            int t = n_si + n_c + n_w;
+            if (t == 0) c = 5;
+            else if (t <= 3) {
+                int n1 = n_si + n_w, base = t == 1 ? 0 : (t == 2 ? 8 : 17);
+                c = 9 + (sp - 1) * 25 + base + (t - n1) * (5 - t) + n_cov;
+            }
         } else {
             int n_si = 0, n_c = 0, n_b = 0, n_w = 0;
             for (int k = 0; k < 4; k++) {

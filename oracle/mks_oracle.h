@@ -103,6 +103,9 @@ int64_t ora_mc_classes(const ora_t *o, int32_t *cls, double *rate, int64_t n);
 
 /* Export the rate tables parsed from start.dat. */
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);
+int ora_ncov(const ora_t *o);
+/* PtransAbs / PtransDes as [coverage species][coor-1]. */
+void ora_get_cov_rates(const ora_t *o, double ptransAbs[9], double ptransDes[9]);
 /* ---- per-species LA law with liquid fractions and LR score ----
  * (LaserAnnealing variant: LA/mcevent/Get_Prob.f:127-152, LA/main.f:637,
  * 676-723).  Prescribed T(z,t) = Tb + Ta exp(-((t_mid-t0)/w)^2)

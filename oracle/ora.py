@@ -54,6 +54,8 @@ def lib():
         L.ora_site_info.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.ora_write_xyz.argtypes = [C.c_void_p, C.c_char_p]
         L.ora_get_rates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ora_get_cov_rates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ora_ncov.argtypes = [C.c_void_p]
         L.ora_ran3_sequence.argtypes = [C.c_int, C.c_int, C.c_void_p]
         L.ora_mc_classes.restype = C.c_int64
         L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
@@ -147,7 +149,10 @@ class Oracle:
 
     def atoms(self):
         st, _ = compact_state(self)
-        return int(np.count_nonzero((st & 3) != 0))
+        sp = st & 3
+        if lib().ora_ncov(self._h):           # species value 3 marks a covered empty site
+            return int(np.count_nonzero((sp == 1) | (sp == 2)))
+        return int(np.count_nonzero(sp != 0))
 
     def trace_enable(self, on=True):
         lib().ora_trace_enable(self._h, 1 if on else 0)
@@ -203,6 +208,13 @@ class Oracle:
         d = np.zeros(9)
         lib().ora_get_rates(self._h, e.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p))
         return e.reshape(3, 4, 4, 4, 4, 4, 4), d.reshape(3, 3)
+
+    def cov_rates(self):
+        """PtransAbs, PtransDes as 3x3 [coverage species][coor-1]."""
+        a = np.zeros(9)
+        d = np.zeros(9)
+        lib().ora_get_cov_rates(self._h, a.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p))
+        return a.reshape(3, 3), d.reshape(3, 3)
 
 
 def ran3_sequence(idum, n):

@@ -57,3 +57,24 @@ def test_run_mulskips_wrapper_etch_stop(tmp_path):
     log = open(tmp_path / "run" / "log.txt").read()
     assert "few MC particles: stop MC" in log
     assert (tmp_path / "run" / "I00000001.xyz").exists()
+
+
+def test_cvd_start_dat_runs_with_coverage(tmp_path):
+    """The reference's CVD-Si-SiH2 start.dat (one coverage species, H; Time
+    exit) cut to 0.5 s: the initial frame equals the reference's byte for
+    byte, and the final frame lists H lines for covered sites."""
+    d = tmp_path / "cvd"
+    d.mkdir()
+    txt = open(os.path.join(GOLDEN, "CVD-Si-SiH2", "start.dat")).read()
+    txt = txt.replace("105.144755160701223 ! TotTime", "0.5 ! TotTime").replace(
+        "105.14475516070123 ! OutTime", "0.5 ! OutTime")
+    (d / "start.dat").write_text(txt)
+    r = run_exe(d)
+    assert r.returncode == 0, r.stdout[-3000:]
+    with gzip.open(os.path.join(GOLDEN, "CVD-Si-SiH2", "I00000000.xyz.gz"), "rb") as f:
+        gold = f.read()
+    assert (d / "I00000000.xyz").read_bytes() == gold
+    assert "Coverage species (NCov= 1 )" in r.stdout
+    lines = (d / "I00000001.xyz").read_text().splitlines()
+    nh = sum(1 for ln in lines[2:] if ln.startswith("H "))
+    assert int(lines[0].split()[0]) == len(lines) - 2 and nh > 500

@@ -1,7 +1,7 @@
 """Replay parity: the reference's event sequence (from the pinned oracle),
 applied by the GPU engine through the C ABI, gives bit-identical lattice
-occupancy, coordination, neighbour-list head and dummy flags, and the same
-rate-class histogram as the oracle's own lists."""
+occupancy, coordination, neighbour-list head, dummy flags and coverage, and
+the same rate-class histogram as the oracle's own lists."""
 import os
 
 import numpy as np
@@ -23,9 +23,12 @@ def replay_case(ora, startdat, len1, kind, total, chunk, lenxyz=480):
     o.init()
     d = __import__("mulskips_gb300.startdat", fromlist=["x"]).parse_startdat(startdat)
     pE, pD = o.rates()
-    lat = Lattice(lenxyz, lenxyz, lenxyz, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"])
+    lat = Lattice(lenxyz, lenxyz, lenxyz, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"],
+                  list_cov=d["list_cov"])
     try:
         lat.set_rates(pE, pD)
+        if d["list_cov"]:
+            lat.set_coverage_rates(*o.cov_rates())
         if kind:
             lat.init_flat(kind, len1)
         else:                               # the oracle's own initializer, through LattCoo
@@ -64,6 +67,14 @@ def test_replay_si001(oracle_lib):
 def test_replay_sic001(oracle_lib):
     n = replay_case(oracle_lib, os.path.join(GOLDEN, "surface", "start.dat"), 120, "C", 200000, 100000)
     assert n == 200000
+
+
+def test_replay_cvd_si001_hydrogen(oracle_lib):
+    """CVD of Si(001) under one coverage species (H), the reference's
+    CVD-Si-SiH2 case: absorption (itrans 6) and desorption (5) events among
+    the depositions and evaporations replay exactly, covered sites included."""
+    n = replay_case(oracle_lib, os.path.join(GOLDEN, "CVD-Si-SiH2", "start.dat"), 48, "S", 400000, 100000)
+    assert n == 400000
 
 
 def test_replay_sic_cube(oracle_lib):

@@ -150,3 +150,59 @@ def test_sic_surface_matches_serial_reference(oracle_lib, tmp_path):
         print(f"SiC {name}: gpu {x.mean():.1f}+-{x.std(ddof=1):.1f} serial {y.mean():.1f}+-{y.std(ddof=1):.1f} "
               f"diff {diff:.1f} 3-sigma band +-{hw:.1f} (tau {tau:.3e})")
         assert abs(diff) <= hw, name
+
+
+def _cvd_oracle(args):
+    """One RunType R oracle run of the CVD case to t_obs: (atoms, covered)."""
+    import sys
+    path, t_obs, root = args
+    sys.path.insert(0, root)
+    from oracle import ora
+    o = ora.Oracle(path, 480, 480, 480, numbers=None)
+    o.init()
+    o.run_until(t_obs)
+    st, _ = ora.compact_state(o)
+    out = (o.atoms(), int(np.count_nonzero((st & 3) == 3)))
+    o.close()
+    return out
+
+
+def test_cvd_hydrogen_coverage_matches_serial_reference(oracle_lib, tmp_path):
+    """CVD of Si(001) under one coverage species (H), the rates of the
+    reference's CVD-Si-SiH2 case (deposition 85/s, absorption 287/s and
+    desorption 40/s per site, evaporation keyed by covered neighbours),
+    RunType R: atoms and covered sites at t = 3 s, 16 oracle seeds against 16
+    GPU replicas at the window factor f = 0.03."""
+    import multiprocessing as mp
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.startdat import parse_startdat
+    from conftest import GOLDEN, ROOT
+    t_obs, n = 3.0, 16
+    txt = open(os.path.join(GOLDEN, "CVD-Si-SiH2", "start.dat")).read().replace(
+        "T ! RunType", "R ! RunType")
+    paths = []
+    for s in range(n):
+        p = tmp_path / f"cvd{s}.dat"
+        p.write_text(txt.replace("9117116 ! Random seed", f"{500 + s} ! Random seed"))
+        paths.append(str(p))
+    with mp.get_context("spawn").Pool(min(n, os.cpu_count() or 1)) as pool:
+        ref = np.array(pool.map(_cvd_oracle, [(p, t_obs, ROOT) for p in paths]), float)
+    d = parse_startdat(paths[0])
+    assert d["run_type"] == "R" and d["list_cov"] == [1]
+    b = Batch([(480, 480, 480)] * n, seeds=[71 + s for s in range(n)], sf=d["sf"], list_cov=d["list_cov"])
+    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
+    b.set_coverage_rates(np.stack([d["ptransAbs"][:, 1:]] * n), np.stack([d["ptransDes"][:, 1:]] * n))
+    b.init_flat("S", [48] * n)
+    tau = float(b.suggest_tau(0.03)[0])
+    nwin = int(math.ceil(t_obs / tau))
+    b.run(t_obs / nwin, nwin)
+    obs = b.observables()
+    b.close()
+    g = np.array([(o["atoms"], o["covered"]) for o in obs], float)
+    print(f"\nCVD tau {t_obs / nwin:.3e} ({nwin} windows)")
+    for k, name in enumerate(("atoms", "covered")):
+        diff, hw = band(g[:, k], ref[:, k])
+        print(f"{name}: gpu {g[:, k].mean():.1f}+-{g[:, k].std(ddof=1):.1f} serial {ref[:, k].mean():.1f}"
+              f"+-{ref[:, k].std(ddof=1):.1f} diff {diff:.1f} 3-sigma band +-{hw:.1f}")
+        assert abs(diff) <= hw, name
+    assert ref[:, 1].mean() > 1000 and g[:, 0].mean() > 0
