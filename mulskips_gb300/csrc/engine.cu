@@ -791,10 +791,13 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                         sc[j] += -(double)A->dEdep[s0][co - 1][j] / ((double)KB_EV_F * (double)A->Tm[s0]);
                 }
             } else {
-                // deposition of a species or, past the deposition share,
-                // absorption of the coverage species (Get_Prob.f:186-201)
-                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : (u < S.spcum[co - 1][2] ? 3 : 0));
-                if (!sp) covev = 1;
+                sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
+                // past the deposition share: absorption of the coverage
+                // species (Get_Prob.f:186-201)
+                if (R.cov && !(u < S.spcum[co - 1][2])) {
+                    sp = 0;
+                    covev = 1;
+                }
             }
         } else if (A && sc && lane == 0 && cls >= CLS_OCC0) {
             for (int j = 0; j < 4; j++) sc[j] += -(double)A->dE[cls][j] / ((double)KB_EV_F * (double)Tsite);
@@ -907,8 +910,9 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
 
 // One tile for one colour phase of one window: stage, run events from
 // t_start to t_start + tau, write back.  Called by the per-colour kernel and
-// by the persistent kernel.
-template <bool LAM>
+// by the persistent kernel.  COV: the coverage-species rules are compiled in
+// (without it every coverage branch folds away).
+template <bool LAM, bool COV = false>
 __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int qid, uint8_t *st_all,
                                              DevStatus *status, uint32_t phase_tag, unsigned int window,
                                              double t_start, LADev *la_all, double *score_all,
@@ -925,7 +929,8 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     Q.zlo = __ldcg(&quads[qid].zlo);     // widened by neighbouring tiles' atomics
     Q.zhi = __ldcg(&quads[qid].zhi);
     RepDev &Rg = reps[Q.rep];
-    const RepLocal R = rep_local(Rg);
+    RepLocal R = rep_local(Rg);
+    if (!COV) R.cov = 0;
     if (!R.active) return;
     if (Q.zhi < Q.zlo) return;   // no event sites in this tile
     // the rate table stays in shared memory while the warp works on tiles of
@@ -1107,7 +1112,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     }
 }
 
-template <bool LAM>
+template <bool LAM, bool COV = false>
 __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quads, const int *qlist, int nq,
                                                  uint8_t *st_all, DevStatus *status, uint32_t phase_tag,
                                                  LADev *la, double *score, const CUtensorMap *tmaps)
@@ -1118,7 +1123,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
     tma_barrier_init();
     int qid = qlist[qi];
     const RepDev &R = reps[quads[qid].rep];
-    process_tile<LAM>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score, tmaps);
+    process_tile<LAM, COV>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score, tmaps);
 }
 
 // Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
@@ -1133,7 +1138,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
 // colour launches per window in order.
 constexpr long long SPIN_LIMIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
 
-template <bool LAM>
+template <bool LAM, bool COV = false>
 __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev *quads, const int *woff,
                                                           const int *wtiles, uint8_t *st_all, DevStatus *status,
                                                           int *progress, int nwin, LADev *la, double *score,
@@ -1171,7 +1176,7 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
             __threadfence();                                // acquire: neighbours' writes before their flag
             if (*(volatile int *)&status->error) return;
             const RepDev &R = reps[quads[t].rep];
-            process_tile<LAM>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
+            process_tile<LAM, COV>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
                          R.T0 + (double)w * R.tau, la, score, tmaps);
             __threadfence();                                // release: each lane's writes reach L2 ...
             __syncwarp();                                   // ... before lane 0 publishes the flag
@@ -1440,6 +1445,7 @@ struct mks_handle {
     int64_t la_window = 0;
     double *d_lr = nullptr;  // f values and result of mks_batch_lr_grad   // windows run since mks_batch_set_la (persistent launch alignment)
     int coop_grid = 0;
+    bool any_cov = false;        // a replica has a coverage species: the COV kernels run
     int schedule = 1;            // 1 persistent dataflow kernel, 0 one launch per colour phase
     uint32_t phase_counter = 0;
     int64_t last_kernels = 0, last_graphs = 0, last_phase_launches = 0;
@@ -1640,10 +1646,11 @@ int upload_tiles(mks_handle *h)
     int dev = 0, nsm = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    int per_sm_la = 0;
+    int per_sm_la = 0, per_sm_cov = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl_persistent<false>, 32, 0));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_la, k_sl_persistent<true>, 32, 0));
-    per_sm = std::min(per_sm, per_sm_la);
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cov, k_sl_persistent<false, true>, 32, 0));
+    per_sm = std::min(per_sm, std::min(per_sm_la, per_sm_cov));
     size_t maxc = 0;
     for (int c = 0; c < 4; c++) maxc = std::max(maxc, h->color_list_h[c].size());
     h->coop_grid = (int)std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (int64_t)std::max<size_t>(1, maxc));
@@ -1788,6 +1795,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         d[i].active = 1;
         d[i].single = r.cfg.ncrystal == 1 && r.cfg.ncov == 0;
         d[i].cov = r.cfg.ncov == 1;
+        if (d[i].cov) h->any_cov = true;
         rate_tables(r, d[i]);
     }
     int rc = upload_reps(h, d);
@@ -1808,6 +1816,10 @@ int launch_window(mks_handle *h)
         if (h->la_on)
             k_sl_phase<true><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
                                                        h->d_status, (uint32_t)c, h->d_la, h->d_score, h->d_tmaps);
+        else if (h->any_cov)
+            k_sl_phase<false, true><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
+                                                              h->d_status, (uint32_t)c, h->d_la, h->d_score,
+                                                              h->d_tmaps);
         else
             k_sl_phase<false><<<nq, 32, 0, h->stream>>>(h->d_reps, h->d_quads, h->d_clist[c], nq, h->d_st,
                                                         h->d_status, (uint32_t)c, h->d_la, h->d_score, h->d_tmaps);
@@ -1841,7 +1853,9 @@ int run_persistent(mks_handle *h, int64_t max_windows)
         LADev *la = h->d_la;
         void *args[] = {&h->d_reps, &h->d_quads, &h->d_woff, &h->d_wtiles, &h->d_st, &h->d_status, &h->d_progress,
                         &nw, &la, &h->d_score, &h->d_tmaps, &h->spin_limit, &h->hold_tile};
-        const void *fn = h->la_on ? (const void *)k_sl_persistent<true> : (const void *)k_sl_persistent<false>;
+        const void *fn = h->la_on ? (const void *)k_sl_persistent<true>
+                         : h->any_cov ? (const void *)k_sl_persistent<false, true>
+                                      : (const void *)k_sl_persistent<false>;
         CK(cudaLaunchCooperativeKernel(fn, dim3(h->coop_grid), dim3(32), args, 0, h->stream));
         k_window_end<<<(int)h->reps.size(), 256, 0, h->stream>>>(h->d_reps, h->d_quads, nw,
                                                                  h->la_on ? h->d_la : nullptr);
