@@ -117,7 +117,7 @@ int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
  * [coverage species][coor-1] (PtransAbs / PtransDes, SetProbability.f:
  * 121-140; only the first species' row may be nonzero).  An empty site of
  * coordination n then carries deposition + absorption at
- * sum_s PtransD(s,n) + PtransAbs(1,n) (Get_Prob.f:186-201), a covered site
+ * sum_s PtransD(s,n) + PtransAbs(1,n) (Get_Prob.f:155-204), a covered site
  * desorbs at PtransDes(1,n) (:93-118), and an atom's evaporation key counts
  * its covered neighbours (PE(NSiC,n1,n2,0,c,0,0), :309-312).  Replaces
  * IndexEvent_Abs / absorption.f / desorption.f.                            */

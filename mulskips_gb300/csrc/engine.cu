@@ -793,7 +793,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             } else {
                 sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
                 // past the deposition share: absorption of the coverage
-                // species (Get_Prob.f:186-201)
+                // species (Get_Prob.f:155-204)
                 if (R.cov && !(u < S.spcum[co - 1][2])) {
                     sp = 0;
                     covev = 1;
@@ -1464,7 +1464,7 @@ void rate_tables(const RepHost &r, RepDev &d)
         double p1 = pD[co - 1], p2 = pD[3 + co - 1], p3 = pD[6 + co - 1];
         double dep = p1 + p2 + p3;
         // empty site: deposition of any species or absorption of the coverage
-        // species, one rate (Get_Prob.f:186-201)
+        // species, one rate (Get_Prob.f:155-204)
         double tot = dep + (cov ? r.ptransAbs[co - 1] : 0.0);
         int cls = co == 1 ? CLS_C1 : (co == 2 ? CLS_C2 : CLS_C3);
         d.rate[cls] = (float)tot;

@@ -83,7 +83,7 @@ constexpr int NCLASS = CLS_OCC0 + 3 * NCENSUS;   // 63
 // Get_Prob.f:93-118), 9.. atom of species sp (1..2) with census (nSi+nWall,
 // nC) summing to 1..3 and c covered neighbours, c <= 4 - census (the PTransE
 // key PE(NSiC, n1, n2, 0, c, 0, 0) of Get_Prob.f:309-312).  C1..C3 carry
-// deposition + absorption (Get_Prob.f:155-201).
+// deposition + absorption (Get_Prob.f:155-204).
 constexpr int CLS_D1 = 6, CLS_COV0 = 9;
 constexpr int NCOVCENSUS = 25;
 
