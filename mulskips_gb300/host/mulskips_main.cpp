@@ -392,9 +392,9 @@ int main()
     bool few = false;
     for (long long block = 0;; block++) {
         // window factor validated against the serial reference: 0.3 for one
-        // species, 0.03 for two or three (fast desorption across tile borders)
-        // and with a coverage species
-        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 && in.ncov == 0 ? 0.3 : 0.03, &tau));
+        // crystal species (with or without a coverage species), 0.03 for two
+        // or three (fast desorption across tile borders)
+        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
         int64_t ev = 0;
         check(mks_run(h, tau, chunk, 0, 0.0, &ev, &time));
         events += ev;

@@ -167,12 +167,14 @@ def _cvd_oracle(args):
     return out
 
 
-def test_cvd_hydrogen_coverage_matches_serial_reference(oracle_lib, tmp_path):
+@pytest.mark.parametrize("f", [0.3, 0.03])
+def test_cvd_hydrogen_coverage_matches_serial_reference(oracle_lib, tmp_path, f):
     """CVD of Si(001) under one coverage species (H), the rates of the
     reference's CVD-Si-SiH2 case (deposition 85/s, absorption 287/s and
     desorption 40/s per site, evaporation keyed by covered neighbours),
     RunType R: atoms and covered sites at t = 3 s, 16 oracle seeds against 16
-    GPU replicas at the window factor f = 0.03."""
+    GPU replicas at the window factors f = 0.3 (the one-crystal-species rule
+    mulskips.e uses) and 0.03."""
     import multiprocessing as mp
     from mulskips_gb300 import Batch
     from mulskips_gb300.startdat import parse_startdat
@@ -193,7 +195,7 @@ def test_cvd_hydrogen_coverage_matches_serial_reference(oracle_lib, tmp_path):
     b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
     b.set_coverage_rates(np.stack([d["ptransAbs"][:, 1:]] * n), np.stack([d["ptransDes"][:, 1:]] * n))
     b.init_flat("S", [48] * n)
-    tau = float(b.suggest_tau(0.03)[0])
+    tau = float(b.suggest_tau(f)[0])
     nwin = int(math.ceil(t_obs / tau))
     b.run(t_obs / nwin, nwin)
     obs = b.observables()
