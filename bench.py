@@ -15,6 +15,9 @@ engine's stream), inputs resident.  `e2e`: the same through the C ABI with
 host buffers, timed on the host: the lattice uploaded from pinned memory,
 the windows, then the step's result as the reference writes it (the frame's
 site list and the observables) read back.
+Side lines (not the headline): `batched` (512 small replicas), `la_gradient`
+(the SiGe laser-anneal gradient) and `cvd` (Si(001) + H, one coverage
+species, with the serial oracle's events/s on the reference's 480^3 case).
 `--impl reference`: the reference CPU path (the oracle restatement; the
 Fortran reference has no compiler here) on all host cores.
 """
@@ -263,6 +266,7 @@ def gb300(args, rank, world):
             traffic = None
     batched = batched_bench(args) if not args.no_batched else None
     la_grad = la_gradient_bench() if not args.no_batched else None
+    cvd = cvd_bench() if not args.no_batched else None
     base_v, base_ev, base_runs = cpu_baseline(seconds=args.cpu_seconds, cores=1)
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
@@ -296,6 +300,7 @@ def gb300(args, rank, world):
         "wall_s_timed": wall,
         "batched": batched,
         "la_gradient": la_grad,
+        "cvd": cvd,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -349,6 +354,50 @@ def batched_bench(args):
             "batched_over_single": v / v1,
             "workload": "512 Si(001) replicas, side ~U{16..96} cells, T~U(900,1300) K, F~logU(0.05,5), "
                         "seed 1000+i, tau = 0.3/r* per replica"}
+
+
+def cvd_bench(windows=4096, oracle_events=3000000):
+    """CVD of Si(001) under one coverage species (H) with the rates of the
+    reference's CVD-Si-SiH2 case, on a 3072 x 3072 x 240 grid (Len1 = 48 slab,
+    41x the reference's 480^2 surface), window factor f = 0.3: events/s of one
+    mks_run call over `windows` windows after a 256-window warm-up (wall time
+    of the synchronous call), against the serial oracle on the reference's own
+    480^3 case (RunType R)."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    from oracle import ora
+    path = os.path.join(ROOT, "tests", "golden", "CVD-Si-SiH2", "start.dat")
+    d = parse_startdat(path)
+    lat = Lattice(3072, 3072, 240, sf=d["sf"], list_cov=d["list_cov"], seed=5)
+    lat.set_rates(d["ptransE"], d["ptransD"])
+    lat.set_coverage_rates(d["ptransAbs"][:, 1:], d["ptransDes"][:, 1:])
+    lat.init_flat("S", 48)
+    tau = lat.suggest_tau(ACCURATE_F)
+    lat.run(tau, 256)
+    e0 = lat.observables()["events"]
+    t0 = time.perf_counter()
+    lat.run(tau, windows)
+    wall = time.perf_counter() - t0
+    obs = lat.observables()
+    lat.close()
+    ev = obs["events"] - e0
+    txt = open(path).read().replace("T ! RunType", "R ! RunType")
+    tmp = tempfile.mkdtemp()
+    p = os.path.join(tmp, "start.dat")
+    open(p, "w").write(txt)
+    o = ora.Oracle(p, 480, 480, 480, numbers=None)
+    o.init()
+    c0 = time.perf_counter()
+    o.run(oracle_events)
+    cdt = time.perf_counter() - c0
+    n = o.iter - 1
+    o.close()
+    shutil.rmtree(tmp, ignore_errors=True)
+    return {"value": ev / wall, "unit": "events/s", "events": int(ev), "windows": windows, "tau_s": tau,
+            "covered_sites": int(obs["covered"]), "atoms": int(obs["atoms"]),
+            "oracle_events_per_s": n / cdt, "oracle_events": int(n),
+            "workload": "Si(001) + H CVD, rates of the reference's CVD-Si-SiH2 case, 3072x3072x240 grid, "
+                        "Len1=48, f=0.3; oracle: the reference's 480^3 case, serial, 1 core"}
 
 
 def la_gradient_bench():
