@@ -46,7 +46,6 @@ constexpr int WMAX = 20;                 // max staged layers
 constexpr int MCCAP = 512;               // max event sites per tile
 constexpr int ZMARGIN = 2;               // extra staged layers beyond the band on each side
 constexpr int NRELOAD = 512;             // bounded re-staging per tile and phase
-constexpr uint16_t NOPOS = 0xFFFF;
 
 // device error codes (status word)
 constexpr int DERR_INVARIANT = MKS_ERR_INVARIANT;
@@ -462,7 +461,7 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
 struct __align__(128) TileShared {
     uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments (TMA box target)
     uint32_t list[MCCAP];                      // (site key << 8) | class; class 0 = dead entry
-    uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each tile site, NOPOS if never listed
+    uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each listed tile site (others stale: checked against list)
     uint8_t dirty[WB_MAX * WMAX];              // staged rows changed by events
     int cnt[64];
     float rate[64];
@@ -591,27 +590,34 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
     TileShared &S = g_tile;
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
+    // pos is not cleared: every listed site's slot is written below or on
+    // append, and a lookup accepts a slot only if the list entry there holds
+    // the same site key
     for (int c = lane; c < 64; c += 32) S.cnt[c] = 0;
-    if (use_pos) {
-        uint32_t *p32 = reinterpret_cast<uint32_t *>(S.pos);
-        int nw = QMAX * QMAX * wz / 2;
-        for (int i = lane; i < nw; i += 32) p32[i] = 0xFFFFFFFFu;
-    }
     __syncwarp();
     // lanes walk the diamond sites of the band only: per layer, row ib holds
     // the sites ia = 2 ja + p with p the row's parity, ja < ceil(wa/2)
     const int hw = (wa + 1) >> 1, per = wb * hw, nsl = per * (zh - zl + 1);
     int nl = 0;
     float g[4] = {0.f, 0.f, 0.f, 0.f};
+    // site s0 + lane is (layer dz, index k) with k = ib * hw + ja; both are
+    // advanced by 32 sites per step without divisions (k / hw by a 16-bit
+    // reciprocal: exact for k < 64 and hw <= 4)
+    int dz = lane / per, k = lane - dz * per;
+    const unsigned hmul = 65536u / (unsigned)hw + 1u;
     for (int s0 = 0; s0 < nsl; s0 += 32) {
         int sidx = s0 + lane;
         int cls = CLS_NONE, ia = 0, ib = 0, z = zl;
         if (sidx < nsl) {
-            int dz = sidx / per, k = sidx - dz * per;
             z = zl + dz;
-            ib = k / hw;
+            ib = (int)(((unsigned)k * hmul) >> 16);
             ia = 2 * (k - ib * hw) + ((a0 + b0 + ib + (z >> 1)) & 1);
             if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single, cov);
+        }
+        k += 32;
+        while (k >= per) {
+            k -= per;
+            dz++;
         }
         unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
         if (cls != CLS_NONE) {
@@ -621,8 +627,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
                 S.list[slot] = (key << 8) | (uint32_t)cls;
                 if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
             }
-            unsigned gm = __match_any_sync(m, cls);
-            if ((int)(__ffs(gm) - 1) == lane) atomicAdd(&S.cnt[cls], __popc(gm));
+            atomicAdd(&S.cnt[cls], 1);
             if (A) {
                 float d[4];
                 la_drate(*A, cls, la_temp_at(*A, a0 + ia, b0 + ib, z, t_mid), d, la_vacuum(*A, cls, z));
@@ -855,8 +860,8 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         int my_slot = -1;
         if (use_pos) {
             if (interior) {
-                uint16_t p = S.pos[pos_index(tkey, zw0)];
-                my_slot = p == NOPOS ? -1 : (int)p;
+                int p = (int)S.pos[pos_index(tkey, zw0)];
+                my_slot = (p < nlist && (S.list[p] >> 8) == tkey) ? p : -1;
             }
         } else {
             unsigned im = __ballot_sync(FULL, interior);
@@ -1034,14 +1039,22 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             rc = run_events(L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
                             window, A, t_mid, scp);
             __syncwarp();
-            // write back the rows that events changed (tile and its one-column ring)
-            for (int r = lane; r < nrows; r += 32) {
-                int ib = r % WB, iz = r / WB;
-                int bit = iz * WB_MAX + ib;               // the row index SLat::put marks
-                if (!S.dirty[bit]) continue;
+            // write back the rows that events changed (tile and its one-column
+            // ring); lane per staged row index bit = iz * WB_MAX + ib, the index
+            // SLat::put marks
+            const bool wrap_a = Q.a0 - 1 < 0 || Q.a1 + 1 > R.NA;
+            for (int bit = lane; bit < WZ * WB_MAX; bit += 32) {
+                int iz = bit / WB_MAX, ib = bit - iz * WB_MAX;
+                if (ib >= WB || !S.dirty[bit]) continue;
                 uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
                 const uint8_t *src = &S.win[bit * RS];
-                for (int a = Q.a0 - 1; a < Q.a1 + 1; a++) row[wrapi(a, R.NA)] = src[a - ax0];
+                if (wrap_a) {
+                    for (int a = Q.a0 - 1; a < Q.a1 + 1; a++) row[wrapi(a, R.NA)] = src[a - ax0];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < QMAX + 2; j++)
+                        if (j < wa + 2) row[Q.a0 - 1 + j] = src[Q.a0 - 1 + j - ax0];
+                }
             }
             if (rc > 0 && lane == 0) atomicAdd(&status->reloads, 1ull);
         } else {
