@@ -72,7 +72,8 @@ struct RepDev {
 struct QuadDev {
     int rep, a0, a1, b0, b1;
     int zlo, zhi, mc;        // mutable: band of event sites and their count
-    int qa, qb, colour, pad;
+    int qa, qb, colour;
+    int ev;                  // events of this tile since the last window end (k_window_end folds them)
     int nbr[8];              // the eight neighbouring tiles (periodic)
 };
 
@@ -1108,7 +1109,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
         quads[qid].zlo = zlo;
         quads[qid].zhi = zhi;
         quads[qid].mc = live;
-        if (nev) atomicAdd(&Rg.events, nev);
+        if (nev) quads[qid].ev += (int)nev;      // only this tile writes its count
         if (scp)
             for (int j = 0; j < 4; j++) atomicAdd(&score_all[4 * Q.rep + j], sc[j]);
         if (A)
@@ -1202,16 +1203,26 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
 __global__ void k_window_end(RepDev *reps, QuadDev *quads, int nwin, LADev *la)
 {
     RepDev &R = reps[blockIdx.x];
-    long long s = 0;
+    long long s = 0, e = 0;
     int nqt = R.nqa * R.nqb;
-    for (int i = threadIdx.x; i < nqt; i += blockDim.x) s += quads[R.quad_base + i].mc;
-    __shared__ long long sh[256];
+    for (int i = threadIdx.x; i < nqt; i += blockDim.x) {
+        QuadDev &q = quads[R.quad_base + i];
+        s += q.mc;
+        e += q.ev;
+        q.ev = 0;
+    }
+    __shared__ long long sh[256], she[256];
     sh[threadIdx.x] = s;
+    she[threadIdx.x] = e;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        if ((int)threadIdx.x < o) {
+            sh[threadIdx.x] += sh[threadIdx.x + o];
+            she[threadIdx.x] += she[threadIdx.x + o];
+        }
         __syncthreads();
     }
+    if (threadIdx.x == 0) R.events += (unsigned long long)she[0];
     if (threadIdx.x == 0) {
         R.mc_count = sh[0];
         if (!R.active) return;
@@ -1621,7 +1632,7 @@ void partition(mks_handle *h, int width)
                 q.qa = qa;
                 q.qb = qb;
                 q.colour = (qa & 1) + 2 * (qb & 1);
-                q.pad = 0;
+                q.ev = 0;
                 int k = 0;
                 for (int db = -1; db <= 1; db++)
                     for (int da = -1; da <= 1; da++) {
