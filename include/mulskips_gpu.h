@@ -260,6 +260,22 @@ int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, doub
  * LattCoo array (SetT, mulskips-source/initial/SetT.f:25-50), replacing T(z,t)
  * for replica rep.  Call before mks_batch_set_la.                          */
 int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lattcoo);
+/* In-process LA coupling: the arrays of the reference's FEM <-> KMC socket
+ * messages (LaserAnnealing main.f:160-345), int32 at every grid point in the
+ * message layout, index z + LenZ * (x + LenX * y) (the Fortran arrays
+ * b / c / d(LenZ, LenX*LenY)).
+ * mks_batch_set_field replaces SENDFIELD + SetT (initial/SetT.f:34-48): the
+ * temperature (K) of each site for LA mode; 10 marks a wall and keeps the
+ * site's previous temperature.  It may be called between runs (after
+ * mks_batch_set_la too).
+ * mks_batch_get_phases replaces GETPHASES / GETXGE (main.f:796-817): coo gets
+ * the coordination of every occupied site, species its ListCrystal index,
+ * both 10 on walls and 0 elsewhere; grid points off the diamond sub-grid get
+ * 10 in layers whose diamond sites are all walls, else 0 (pymulskips reads
+ * the values 1..4 only, pymulskips/io.py:1013-1066).  Either pointer may be
+ * NULL.                                                                    */
+int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field);
+int mks_batch_get_phases(mks_handle *h, int32_t rep, int32_t *coo, int32_t *species);
 /* mks_load_lattice for replica rep of a batch.                            */
 int mks_batch_load_lattice(mks_handle *h, int32_t rep, const int32_t *lattcoo);
 /* SetSi-like slab with species 2 substituted on each atom with probability

@@ -99,6 +99,8 @@ SIGNATURES = {
     "mks_set_clock": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int64, C.c_int64]),
     "mks_debug_hold_tile": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
     "mks_batch_load_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mks_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mks_batch_get_phases": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mks_batch_load_lattice": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_lr_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mks_batch_init_alloy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),

@@ -2520,9 +2520,15 @@ int mks_batch_load_lattice(mks_handle *h, int32_t rep, const int32_t *lc)
     return load_lattice_impl(h, rep, lc);
 }
 
-int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lc)
+}  // extern "C"
+
+namespace {
+
+// The LA temperature field of replica rep from a per-grid-point source:
+// T(x, y, z, previous) gives each diamond site's temperature.
+template <class F>
+int set_temperature_impl(mks_handle *h, int rep, F temp_of)
 {
-    if (!h || !lc || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
     if (!h->d_tfield) {
         int64_t nl = 0;
         for (RepHost &x : h->reps) nl += x.NZ;
@@ -2530,30 +2536,130 @@ int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lc)
         CK(cudaMemset(h->d_tfield, 0, sizeof(uint16_t) * (size_t)h->st_bytes));
         CK(cudaMalloc(&h->d_tlayer, sizeof(float) * (size_t)nl));
         CK(cudaMemset(h->d_tlayer, 0, sizeof(float) * (size_t)nl));
-        nl = 0;
-        for (RepHost &x : h->reps) {
-            x.t_layer_off = -1;
-            nl += x.NZ;
-        }
+        for (RepHost &x : h->reps) x.t_layer_off = -1;
     }
     RepHost &r = h->reps[rep];
     int64_t loff = 0;
     for (int i = 0; i < rep; i++) loff += h->reps[i].NZ;
-    int lx = r.cfg.lenx, ly = r.cfg.leny;
     std::vector<uint16_t> t((size_t)r.NZ * r.NB * r.pitch, 0);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(t.data(), h->d_tfield + r.st_off, sizeof(uint16_t) * t.size(), cudaMemcpyDeviceToHost));
     std::vector<float> tl((size_t)r.NZ, 0.f);
     for (int z1 = 0; z1 < r.NZ; z1++)
         for (int b = 0; b < r.NB; b++)
             for (int a = 0; a < r.NA; a++) {
                 if ((a + b + (z1 >> 1)) & 1) continue;
                 int x = 3 * (2 * a + (z1 & 1)), y = 3 * (2 * b + (z1 & 1)), z = 3 * z1;
-                int T = (lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] >> 9) & 8191;   // PosT, LenT
-                t[((size_t)z1 * r.NB + b) * r.pitch + a] = (uint16_t)T;
+                uint16_t &v = t[((size_t)z1 * r.NB + b) * r.pitch + a];
+                int T = z < r.cfg.lenz ? temp_of(x, y, z, (int)v) : (int)v;
+                v = (uint16_t)T;
                 tl[z1] = std::max(tl[z1], (float)T);
             }
     CK(cudaMemcpy(h->d_tfield + r.st_off, t.data(), sizeof(uint16_t) * t.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_tlayer + loff, tl.data(), sizeof(float) * tl.size(), cudaMemcpyHostToDevice));
     r.t_layer_off = loff;
+    return 0;
+}
+
+// Phases of the LA coupling messages (LaserAnnealing main.f:796-817), one
+// thread per grid point of the socket layout: index z + LenZ (x + LenX y).
+__global__ void k_wall_layers(const RepDev *reps, int rep, const uint8_t *st_all, int *wall)
+{
+    const RepDev &R = reps[rep];
+    const uint8_t *st = st_all + R.st_off;
+    int64_t n = (int64_t)R.NZ * R.NB * R.NA;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int a = (int)(i % R.NA);
+        int64_t r = i / R.NA;
+        int b = (int)(r % R.NB), z1 = (int)(r / R.NB);
+        if ((a + b + (z1 >> 1)) & 1) continue;
+        if (st[((int64_t)z1 * R.NB + b) * R.pitch + a] != WALL) wall[z1] = 0;
+    }
+}
+
+__global__ void k_phases(const RepDev *reps, int rep, const uint8_t *st_all, int lx, int ly, int lz,
+                         const int *wall, int32_t *coo, int32_t *spc)
+{
+    const RepDev &R = reps[rep];
+    const uint8_t *st = st_all + R.st_off;
+    const bool cov = R.cov != 0;
+    int64_t n = (int64_t)lz * lx * ly;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int z = (int)(i % lz);
+        int64_t r = i / lz;
+        int x = (int)(r % lx), y = (int)(r / lx);
+        int z1 = z / 3, c = 0, s = 0;
+        bool site = false;
+        if (x % 3 == 0 && y % 3 == 0 && z % 3 == 0) {
+            int x1 = x / 3, y1 = y / 3;
+            if ((x1 & 1) == (z1 & 1) && (y1 & 1) == (z1 & 1) && (((x1 >> 1) + (y1 >> 1) + (z1 >> 1)) & 1) == 0) {
+                site = true;
+                uint8_t v = st[((int64_t)z1 * R.NB + (y1 >> 1)) * R.pitch + (x1 >> 1)];
+                int sp = atom_sp(v, cov);
+                if (v == WALL) {
+                    c = s = 10;
+                } else if (sp) {
+                    c = co_of(v);
+                    s = sp;
+                }
+            }
+        }
+        if (!site && z1 < R.NZ && wall[z1]) c = s = 10;
+        if (coo) coo[i] = c;
+        if (spc) spc[i] = s;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lc)
+{
+    if (!h || !lc || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    const int lx = h->reps[rep].cfg.lenx, ly = h->reps[rep].cfg.leny;
+    return set_temperature_impl(h, rep, [&](int x, int y, int z, int) {
+        return (lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] >> 9) & 8191;   // PosT, LenT
+    });
+}
+
+int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field)
+{
+    if (!h || !field || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    const int lx = h->reps[rep].cfg.lenx, lz = h->reps[rep].cfg.lenz;
+    for (size_t i = 0, n = (size_t)lz * lx * h->reps[rep].cfg.leny; i < n; i++)
+        if (field[i] < 0 || field[i] > 8191) return fail(MKS_ERR_ARG, "temperature %d K outside the 13-bit field", field[i]);
+    // SetT (LaserAnnealing initial/SetT.f:34-48): 10 marks a wall and keeps the site's temperature
+    return set_temperature_impl(h, rep, [&](int x, int y, int z, int old) {
+        int T = field[(size_t)z + (size_t)lz * ((size_t)x + (size_t)lx * y)];
+        return T == 10 ? old : T;
+    });
+}
+
+int mks_batch_get_phases(mks_handle *h, int32_t rep, int32_t *coo, int32_t *species)
+{
+    if (!h || rep < 0 || rep >= (int)h->reps.size() || (!coo && !species)) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    const int lx = r.cfg.lenx, ly = r.cfg.leny, lz = r.cfg.lenz;
+    const size_t n = (size_t)lz * lx * ly;
+    int *d_wall = nullptr;
+    int32_t *d_out = nullptr;
+    CK(cudaMallocAsync(&d_wall, sizeof(int) * (size_t)r.NZ, h->stream));
+    CK(cudaMallocAsync(&d_out, sizeof(int32_t) * n * ((coo && species) ? 2 : 1), h->stream));
+    std::vector<int> ones((size_t)r.NZ, 1);
+    CK(cudaMemcpyAsync(d_wall, ones.data(), sizeof(int) * ones.size(), cudaMemcpyHostToDevice, h->stream));
+    int64_t ns = (int64_t)r.NZ * r.NB * r.NA;
+    k_wall_layers<<<(int)std::min<int64_t>(152 * 8, (ns + 255) / 256), 256, 0, h->stream>>>(h->d_reps, rep, h->d_st,
+                                                                                               d_wall);
+    int32_t *d_coo = coo ? d_out : nullptr, *d_sp = species ? (coo ? d_out + n : d_out) : nullptr;
+    k_phases<<<(int)std::min<int64_t>(152 * 16, ((int64_t)n + 255) / 256), 256, 0, h->stream>>>(
+        h->d_reps, rep, h->d_st, lx, ly, lz, d_wall, d_coo, d_sp);
+    CK(cudaGetLastError());
+    if (coo) CK(cudaMemcpyAsync(coo, d_coo, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    if (species) CK(cudaMemcpyAsync(species, d_sp, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_wall, h->stream);
+    cudaFreeAsync(d_out, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
 

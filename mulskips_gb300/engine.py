@@ -201,6 +201,7 @@ class Batch:
         N.check(N.lib().mks_batch_create(cfgs, len(boxes), C.byref(h)))
         self._h = h
         self.n = len(boxes)
+        self.boxes = [tuple(int(v) for v in b) for b in boxes]
 
     def close(self):
         if self._h:
@@ -278,6 +279,35 @@ class Batch:
         """Static LA temperatures of replica rep from the LattCoo T bits."""
         lc = np.ascontiguousarray(lattcoo, dtype=np.int32)
         N.check(N.lib().mks_batch_load_temperature(self._h, int(rep), N.ptr(lc)))
+
+    # ---- in-process LA coupling: the FEM <-> KMC socket messages ----
+    def set_field(self, rep, field):
+        """Temperature field (K) of replica rep as the reference's SENDFIELD
+        message: field[z, x + LenX*y] (shape (LenZ, LenX*LenY)), or that
+        array flattened with z fastest; 10 marks a wall (temperature kept)."""
+        f = np.asarray(field, dtype=np.int32)
+        if f.ndim == 2:
+            f = f.T                      # [z, j] -> memory order z fastest
+        f = np.ascontiguousarray(f).reshape(-1)
+        N.check(N.lib().mks_batch_set_field(self._h, int(rep), N.ptr(f)))
+
+    def get_phases(self, rep=0):
+        """(coo, species) of replica rep as the reference's GETPHASES / GETXGE
+        messages: arrays [z, x + LenX*y] of shape (LenZ, LenX*LenY) (views
+        of buffers with z fastest)."""
+        lx, ly, lz = self.boxes[rep]
+        c = np.empty(lz * lx * ly, dtype=np.int32)
+        d = np.empty(lz * lx * ly, dtype=np.int32)
+        N.check(N.lib().mks_batch_get_phases(self._h, int(rep), N.ptr(c), N.ptr(d)))
+        return c.reshape(lx * ly, lz).T, d.reshape(lx * ly, lz).T
+
+    def lattcoo(self):
+        """LattCoo(0:LenX-1, 0:LenY-1, 0:LenZ) of a one-replica batch."""
+        assert self.n == 1
+        lx, ly, lz = self.boxes[0]
+        a = np.empty((lz + 1, ly, lx), dtype=np.int32)
+        N.check(N.lib().mks_get_lattice(self._h, N.ptr(a)))
+        return a
 
     # ---- laser anneal (LA) mode ----
     def init_alloy(self, len1, x, seed):
