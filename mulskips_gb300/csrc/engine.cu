@@ -1177,13 +1177,14 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
                 long long t0 = clock64();
                 volatile int *pr = progress + n;
                 volatile int *err = &status->error;
+                // tight poll (one L2 round trip per check; a sleep between
+                // checks oversleeps the flag and lengthens every phase)
                 while (*pr < need) {
                     if (*err) break;
                     if (clock64() - t0 > spin_limit) {
                         set_error(status, DERR_TIMEOUT, t);
                         break;
                     }
-                    __nanosleep(64);
                 }
             }
             __syncwarp();
