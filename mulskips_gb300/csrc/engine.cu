@@ -463,7 +463,6 @@ struct __align__(128) TileShared {
     uint8_t win[RS * WB_MAX * WMAX];           // staged rows, 32-byte aligned segments (TMA box target)
     uint32_t list[MCCAP];                      // (site key << 8) | class; class 0 = dead entry
     uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each listed tile site (others stale: checked against list)
-    uint8_t dirty[WB_MAX * WMAX];              // staged rows changed by events
     int cnt[64];
     float rate[64];
     float spcum[3][3];
@@ -533,8 +532,15 @@ __device__ __forceinline__ bool tma_stage(const CUtensorMap *tmap, int ax0, int 
     return ok;
 }
 
+// Staged window with write-through: every byte an event writes goes to the
+// shared copy and, at once, to the lattice in global memory, so the stores
+// drain while the tile keeps working and the phase ends without a write-back
+// pass.  No other tile reads or writes these bytes during the phase (same-
+// colour tiles are two tiles apart; the others wait for this tile's flag).
 struct SLat {
     int ax0, bx0, zw0, NZ;   // (a, b, z) of staged byte 0
+    uint8_t *st;             // the replica's lattice
+    int NA, NB, pitch;
     __device__ __forceinline__ uint8_t get(int a, int b, int z) const
     {
         if (z < 0 || z >= NZ) return 0;
@@ -543,9 +549,8 @@ struct SLat {
     __device__ __forceinline__ void put(int a, int b, int z, uint8_t v) const
     {
         if (z < 0 || z >= NZ) return;
-        int row = (z - zw0) * WB_MAX + (b - bx0);
-        g_tile.win[row * RS + (a - ax0)] = v;
-        g_tile.dirty[row] = 1;
+        g_tile.win[((z - zw0) * WB_MAX + (b - bx0)) * RS + (a - ax0)] = v;
+        st[((int64_t)z * NB + wrapi(b, NB)) * pitch + wrapi(a, NA)] = v;
     }
 };
 
@@ -994,7 +999,6 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             int ax0 = inner ? (lo_a & ~15) : lo_a;         // column of staged byte 0
             int bx0 = Q.b0 - HALO;
             int nrows = WB * WZ;
-            for (int i = lane; i < WB_MAX * WMAX / 4; i += 32) reinterpret_cast<uint32_t *>(S.dirty)[i] = 0u;
             if (tmaps && inner && bx0 >= 0 && bx0 + WB <= R.NB) {
                 // no periodic wrap inside the box: one tensor copy per 4 layers
                 if (!tma_stage(&tmaps[Q.rep], ax0, bx0, zw0, WZ)) {
@@ -1030,7 +1034,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
                 }
             }
             __syncwarp();
-            SLat L{ax0, bx0, zw0, R.NZ};
+            SLat L{ax0, bx0, zw0, R.NZ, st, R.NA, R.NB, R.pitch};
             if (A) la_bounds(zw0, zw1 - 1);
             if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, R.single != 0, R.cov != 0,
                             scp ? A : nullptr, t_mid)) {
@@ -1040,23 +1044,6 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             rc = run_events(L, R, Q, qid, t, t_end, evc, zw0, zw1, true, hz_lo, hz_hi, nev, k0, k1, phase_tag,
                             window, A, t_mid, scp);
             __syncwarp();
-            // write back the rows that events changed (tile and its one-column
-            // ring); lane per staged row index bit = iz * WB_MAX + ib, the index
-            // SLat::put marks
-            const bool wrap_a = Q.a0 - 1 < 0 || Q.a1 + 1 > R.NA;
-            for (int bit = lane; bit < WZ * WB_MAX; bit += 32) {
-                int iz = bit / WB_MAX, ib = bit - iz * WB_MAX;
-                if (ib >= WB || !S.dirty[bit]) continue;
-                uint8_t *row = st + ((int64_t)(zw0 + iz) * R.NB + wrapi(bx0 + ib, R.NB)) * R.pitch;
-                const uint8_t *src = &S.win[bit * RS];
-                if (wrap_a) {
-                    for (int a = Q.a0 - 1; a < Q.a1 + 1; a++) row[wrapi(a, R.NA)] = src[a - ax0];
-                } else {
-#pragma unroll
-                    for (int j = 0; j < QMAX + 2; j++)
-                        if (j < wa + 2) row[Q.a0 - 1 + j] = src[Q.a0 - 1 + j - ax0];
-                }
-            }
             if (rc > 0 && lane == 0) atomicAdd(&status->reloads, 1ull);
         } else {
             // band taller than the staging buffer: run from global memory
