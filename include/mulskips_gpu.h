@@ -128,7 +128,9 @@ int mks_init_flat(mks_handle *h, char kind, int32_t len1);
 /* LattCoo(0:LenX-1,0:LenY-1,0:LenZ), x fastest (Fortran order).           */
 int mks_load_lattice(mks_handle *h, const int32_t *lattcoo);
 int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
-/* Compact state bytes (layer-major, see DESIGN); n >= mks_state_size(). */
+/* Compact state: one byte per diamond site (a, b, z1) at index
+ * (z1 * (LenY/6) + b) * (LenX/6) + a (bits 0-1 species, 2-4 coordination,
+ * 5-6 first list entry, 7 dummy flag; 0x80 a wall); n >= mks_state_size(). */
 int64_t mks_state_size(mks_handle *h);
 int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
 /* Upload compact state bytes (same layout); the per-tile bands are rebuilt. */
@@ -168,6 +170,17 @@ int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
  * *n gets the count; the indices are written when idx is non-NULL and
  * cap >= *n.                                                               */
 int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int64_t *n);
+/* The output frame files of WriteMolMolXYZFile.f:22-406 for the current
+ * lattice: <base>.xyz (atoms of coordination <= 3 and covered sites in the
+ * z, y, x scan, then the voids), <base>_d.xyz (non-epitaxial bulk: none with
+ * cubic stacking), <base>_v.xyz (voids; for SiC labelled by their neighbours'
+ * species, :216-260) and, for SiC, <base>_w.xyz (bulk atoms with three
+ * neighbours of the right species once those with none have been counted as
+ * swapped, :264-398; the reference's swap-and-restore of LattCoo, which
+ * gives every swapped site the type of the last one, is not applied to the
+ * run).  Voids follow the scan order, not the reference's ListVoid order.
+ * *num_at_wrong (may be NULL) gets the SiC NumAtWrong count, else 0.       */
+int mks_write_frame(mks_handle *h, const char *base, double time, int64_t iter, int64_t *num_at_wrong);
 int mks_get_observables(mks_handle *h, mks_observables *obs);
 int mks_get_status(mks_handle *h, mks_status *st);
 

@@ -73,6 +73,7 @@ SIGNATURES = {
     "mks_run": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_int64, C.c_double,
                           C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "mks_frame_sites": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "mks_write_frame": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, C.c_int64, C.c_void_p]),
     "mks_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_get_observables": (C.c_int, [C.c_void_p, C.POINTER(MksObservables)]),
     "mks_get_status": (C.c_int, [C.c_void_p, C.POINTER(MksStatus)]),

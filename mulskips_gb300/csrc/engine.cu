@@ -182,7 +182,7 @@ struct DevStatus {
     unsigned long long reloads;
 };
 
-__device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+__host__ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 struct GLat {
     uint8_t *st;
@@ -2944,6 +2944,185 @@ int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int
     cudaFreeAsync(d_off, h->stream);
     cudaFreeAsync(d_out, h->stream);
     CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Fortran Ew.d of the frame headers (WriteMolMolXYZFile.f:166-169)
+std::string fortran_e(double v, int w, int d)
+{
+    char b[64], m[64];
+    if (v == 0.0) {
+        snprintf(b, sizeof b, "0.%0*dE+00", d, 0);
+    } else {
+        snprintf(m, sizeof m, "%.*e", d - 1, fabs(v));
+        std::string digits;
+        const char *p = m;
+        digits += *p++;
+        if (*p == '.') p++;
+        while (*p && *p != 'e') digits += *p++;
+        int ex = atoi(p + 1) + 1;
+        snprintf(b, sizeof b, "%s0.%sE%c%02d", v < 0 ? "-" : "", digits.c_str(), ex < 0 ? '-' : '+', abs(ex));
+    }
+    char out[80];
+    snprintf(out, sizeof out, "%*s", w, b);
+    return out;
+}
+
+const char *crystal_symbol(const mks_config &c, int sp)
+{   // WriteMolMolXYZFile.f:177-215: species 1 is Si; the second is C, Ge or B
+    if (sp == 1) return "Si";
+    int z = c.list_crystal[sp - 1];
+    return z == 6 ? "C" : (z == 32 ? "Ge" : (z == 5 ? "B" : nullptr));
+}
+
+}  // namespace
+
+extern "C" {
+
+int mks_write_frame(mks_handle *h, const char *base, double time, int64_t iter, int64_t *num_at_wrong)
+{
+    if (num_at_wrong) *num_at_wrong = 0;
+    if (!h || !base || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_write_frame needs a single-replica handle");
+    const RepHost &r = h->reps[0];
+    const mks_config &c = r.cfg;
+    const bool cov = c.ncov > 0;
+    const int NA = r.NA, NB = r.NB;
+    int64_t n0 = 0, n1 = 0;
+    int rc = mks_frame_sites(h, 0, nullptr, 0, &n0);
+    if (!rc) rc = mks_frame_sites(h, 1, nullptr, 0, &n1);
+    if (rc) return rc;
+    std::vector<uint32_t> at((size_t)n0), vd((size_t)n1);
+    if (n0 && (rc = mks_frame_sites(h, 0, at.data(), n0, &n0))) return rc;
+    if (n1 && (rc = mks_frame_sites(h, 1, vd.data(), n1, &n1))) return rc;
+    std::vector<uint8_t> st((size_t)mks_state_size(h));
+    if ((rc = mks_get_state(h, st.data(), (int64_t)st.size()))) return rc;
+    auto site_xyz = [&](int64_t i, double &x, double &y, double &z) {
+        int a = (int)(i % NA);
+        int64_t q = i / NA;
+        int b = (int)(q % NB), z1 = (int)(q / NB);
+        x = c.sf * 3.0 * (2 * a + (z1 & 1));
+        y = c.sf * 3.0 * (2 * b + (z1 & 1));
+        z = c.sf * 3.0 * z1;
+    };
+    auto nb_byte = [&](int64_t i, int d) -> uint8_t {
+        int a = (int)(i % NA);
+        int64_t q = i / NA;
+        int b = (int)(q % NB), z1 = (int)(q / NB);
+        int da, db, dz;
+        nb_off(z1 & 1, d, da, db, dz);
+        int zz = z1 + dz;
+        if (zz < 0 || zz >= r.NZ) return 0;
+        return st[((size_t)zz * NB + (size_t)wrapi(b + db, NB)) * NA + (size_t)wrapi(a + da, NA)];
+    };
+    const std::string per = " periodic " + fortran_e(c.sf * c.lenx, 15, 8) + " " + fortran_e(c.sf * c.leny, 15, 8) +
+                            " " + fortran_e(c.sf * c.lenz, 15, 8) + "\n";
+    const int64_t layer = (int64_t)NA * NB;
+    // the header counts atoms and covered sites from z = 1 (:74-89), the voids all
+    int64_t counted = 0;
+    for (uint32_t i : at) counted += (int64_t)i >= layer;
+    auto header = [&](FILE *f, int64_t n) {
+        fprintf(f, " %8lld angstroem KMC-time: %s Iter: %12lld\n", (long long)n, fortran_e(time, 15, 8).c_str(),
+                (long long)iter);
+        fputs(per.c_str(), f);
+    };
+    std::string b(base);
+    FILE *f = fopen((b + "_d.xyz").c_str(), "w");          // :96-160, cubic stacking: none
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_d.xyz", base);
+    header(f, 0);
+    fclose(f);
+    f = fopen((b + ".xyz").c_str(), "w");
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s.xyz", base);
+    header(f, counted + n1);
+    for (uint32_t i : at) {
+        double x, y, z;
+        site_xyz(i, x, y, z);
+        int sp = st[i] & 3;
+        const char *sym = (cov && sp == COVSP) ? (c.list_cov[0] == 17 ? "Cl" : "H") : crystal_symbol(c, sp);
+        if (!sym) {
+            fclose(f);
+            return fail(MKS_ERR_INVARIANT, "ERROR: 2nd crystal specie can only be C/Ge/B");
+        }
+        fprintf(f, "%s %10.5f %10.5f %10.5f  \n", sym, x, y, z);
+    }
+    for (uint32_t i : vd) {
+        double x, y, z;
+        site_xyz(i, x, y, z);
+        fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
+    }
+    fclose(f);
+    const bool sic = c.ncrystal == 2 && (c.list_crystal[0] == 6 || c.list_crystal[1] == 6 || c.list_crystal[2] == 6);
+    f = fopen((b + "_v.xyz").c_str(), "w");                 // :216-260
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_v.xyz", base);
+    fprintf(f, " %8lld angstroem\n", (long long)n1);
+    fputs(per.c_str(), f);
+    for (uint32_t i : vd) {
+        double x, y, z;
+        site_xyz(i, x, y, z);
+        if (sic && !cov) {
+            int s = 0;
+            for (int d = 0; d < 4; d++) s += nb_byte(i, d) & 3;   // species index, 0 on walls
+            const char *lbl = s == 4 ? "Mg %10.5f %10.5f %10.5f # CV (C vacancy)\n"
+                            : s == 8 ? "He %10.5f %10.5f %10.5f # SV (Si vacancy)\n"
+                            : s == 7 ? "Ne %10.5f %10.5f %10.5f # SAV (Si antisite vac)\n"
+                            : s == 5 ? "Be %10.5f %10.5f %10.5f # CAV (C antisite vac)\n"
+                            : s == 6 ? "Ar %10.5f %10.5f %10.5f # XV (near 2C and 2Si)\n" : nullptr;
+            if (!lbl) {
+                fclose(f);
+                return fail(MKS_ERR_INVARIANT, "ERROR: Weird Defect type was formed");
+            }
+            fprintf(f, lbl, x, y, z);
+        } else {
+            fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
+        }
+    }
+    fclose(f);
+    if (!sic) return 0;
+    // :264-398 on a copy: bulk atoms (z >= 1) with no neighbour of the other
+    // species are swapped, then bulk atoms with three are listed
+    std::vector<uint8_t> sw(st);
+    auto is_bulk = [&](uint8_t v) { return v != WALL && (v & 3) != 0 && co_of(v) == 4; };
+    auto other = [&](int sp, uint8_t w) { return (sp == 1 && (w & 3) == 2) || (sp == 2 && (w & 3) == 1); };
+    for (size_t i = (size_t)layer; i < st.size(); i++) {
+        uint8_t v = st[i];
+        int sp = v & 3;
+        if (!is_bulk(v) || (sp != 1 && sp != 2)) continue;
+        int nc = 0;
+        for (int d = 0; d < 4; d++) nc += other(sp, nb_byte((int64_t)i, d));
+        if (nc == 0) sw[i] = (uint8_t)((v & ~3) | (sp == 1 ? 2 : 1));
+    }
+    std::vector<size_t> wrong;
+    for (size_t i = (size_t)layer; i < sw.size(); i++) {
+        uint8_t v = sw[i];
+        int sp = v & 3;
+        if (!is_bulk(v) || (sp != 1 && sp != 2)) continue;
+        int a = (int)(i % NA);
+        size_t q = i / NA;
+        int bb = (int)(q % NB), z1 = (int)(q / NB);
+        int nc = 0;
+        for (int d = 0; d < 4; d++) {
+            int da, db, dz;
+            nb_off(z1 & 1, d, da, db, dz);
+            int zz = z1 + dz;
+            uint8_t w = (zz < 0 || zz >= r.NZ) ? 0 : sw[((size_t)zz * NB + (size_t)wrapi(bb + db, NB)) * NA + (size_t)wrapi(a + da, NA)];
+            nc += other(sp, w);
+        }
+        if (nc == 3) wrong.push_back(i);
+    }
+    if (num_at_wrong) *num_at_wrong = (int64_t)wrong.size();
+    f = fopen((b + "_w.xyz").c_str(), "w");
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_w.xyz", base);
+    fprintf(f, " %8lld angstroem\n", (long long)wrong.size());
+    fputs(per.c_str(), f);
+    for (size_t i : wrong) {
+        double x, y, z;
+        site_xyz((int64_t)i, x, y, z);
+        fprintf(f, "%s %10.5f %10.5f %10.5f  \n", (sw[i] & 3) == 1 ? "Si" : "C", x, y, z);
+    }
+    fclose(f);
     return 0;
 }
 

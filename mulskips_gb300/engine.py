@@ -146,6 +146,13 @@ class Lattice:
         N.check(N.lib().mks_class_histogram(self._h, N.ptr(h), N.MKS_NCLASS))
         return h
 
+    def write_frame(self, base, time, it):
+        """The frame files <base>.xyz, _d, _v (and _w for SiC) of the
+        current lattice; returns the SiC NumAtWrong count (0 otherwise)."""
+        w = C.c_int64()
+        N.check(N.lib().mks_write_frame(self._h, str(base).encode(), float(time), int(it), C.byref(w)))
+        return w.value
+
     def observables(self):
         o = N.MksObservables()
         N.check(N.lib().mks_get_observables(self._h, C.byref(o)))

@@ -226,45 +226,13 @@ void check(int rc)
     }
 }
 
-// Fortran Ew.d
-std::string fmt_e(double v, int w, int d)
-{
-    char b[64], m[64];
-    if (v == 0.0) {
-        snprintf(b, sizeof b, "0.%0*dE+00", d, 0);
-    } else {
-        snprintf(m, sizeof m, "%.*e", d - 1, fabs(v));
-        std::string digits;
-        const char *p = m;
-        digits += *p++;
-        if (*p == '.') p++;
-        while (*p && *p != 'e') digits += *p++;
-        int ex = atoi(p + 1) + 1;
-        snprintf(b, sizeof b, "%s0.%sE%c%02d", v < 0 ? "-" : "", digits.c_str(), ex < 0 ? '-' : '+', abs(ex));
-    }
-    char out[64];
-    snprintf(out, sizeof out, "%*s", w, b);
-    return out;
-}
-
 struct Frames {
     mks_handle *h;
     const Input &in;
-    int lx, ly, lz;
-    int na, nb;
 
-    const char *symbol(int sp) const
+    bool sic() const
     {
-        if (sp == 1) return "Si";
-        int z = in.list_crystal[sp - 1];
-        if (z == 6) return "C";
-        if (z == 32) return "Ge";
-        if (z == 5) return "B";
-        return "X";
-    }
-    const char *cov_symbol() const
-    {   // WriteMolMolXYZFile.f:177-178: H for CovInd 1, Cl for 17
-        return in.list_cov[0] == 17 ? "Cl" : "H";
+        return in.ncrystal == 2 && (in.list_crystal[0] == 6 || in.list_crystal[1] == 6 || in.list_crystal[2] == 6);
     }
     std::string name(long long iout) const
     {   // GetOutputFileName.f:22-81: first 8 of the 9 digits of 10*Iout
@@ -272,64 +240,15 @@ struct Frames {
         snprintf(d, sizeof d, "%09lld", iout * 10);
         return std::string("I") + std::string(d, 8);
     }
-    void xyz(int64_t i, double &x, double &y, double &z) const
-    {
-        int a = (int)(i % na);
-        int64_t r = i / na;
-        int b = (int)(r % nb), z1 = (int)(r / nb);
-        x = in.sf * 3.0 * (2 * a + (z1 & 1));
-        y = in.sf * 3.0 * (2 * b + (z1 & 1));
-        z = in.sf * 3.0 * z1;
-    }
     void write(double time, long long iter, long long iout)
-    {   // WriteMolMolSource.f:22-112, WriteMolMolXYZFile.f:22-406
+    {   // WriteMolMolSource.f:22-112; the xyz files come from mks_write_frame
+        // (WriteMolMolXYZFile.f:22-406)
         std::string base = name(iout);
         printf(" %s\n", base.c_str());
-        std::vector<uint32_t> at, vd;
-        std::vector<uint8_t> st((size_t)mks_state_size(h));
-        int64_t n0 = 0, n1 = 0;
-        check(mks_frame_sites(h, 0, nullptr, 0, &n0));
-        check(mks_frame_sites(h, 1, nullptr, 0, &n1));
-        at.resize((size_t)n0);
-        vd.resize((size_t)n1);
-        if (n0) check(mks_frame_sites(h, 0, at.data(), n0, &n0));
-        if (n1) check(mks_frame_sites(h, 1, vd.data(), n1, &n1));
-        check(mks_get_state(h, st.data(), (int64_t)st.size()));
-        std::string per = " periodic " + fmt_e(in.sf * lx, 15, 8) + " " + fmt_e(in.sf * ly, 15, 8) + " " +
-                          fmt_e(in.sf * lz, 15, 8) + "\n";
-        char hdr[256];
-        FILE *f = fopen((base + ".xyz").c_str(), "w");
-        snprintf(hdr, sizeof hdr, " %8lld angstroem KMC-time: %s Iter: %12lld\n", (long long)(n0 + n1),
-                 fmt_e(time, 15, 8).c_str(), iter);
-        fputs(hdr, f);
-        fputs(per.c_str(), f);
-        for (uint32_t i : at) {
-            double x, y, z;
-            xyz(i, x, y, z);
-            fprintf(f, "%s %10.5f %10.5f %10.5f  \n", in.ncov && (st[i] & 3) == 3 ? cov_symbol() : symbol(st[i] & 3),
-                    x, y, z);
-        }
-        for (uint32_t i : vd) {
-            double x, y, z;
-            xyz(i, x, y, z);
-            fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
-        }
-        fclose(f);
-        // cubic stacking only: no non-epitaxial bulk atoms
-        f = fopen((base + "_d.xyz").c_str(), "w");
-        snprintf(hdr, sizeof hdr, " %8d angstroem KMC-time: %s Iter: %12lld\n", 0, fmt_e(time, 15, 8).c_str(), iter);
-        fputs(hdr, f);
-        fputs(per.c_str(), f);
-        fclose(f);
-        f = fopen((base + "_v.xyz").c_str(), "w");
-        fprintf(f, " %8lld angstroem\n", (long long)n1);
-        fputs(per.c_str(), f);
-        for (uint32_t i : vd) {
-            double x, y, z;
-            xyz(i, x, y, z);
-            fprintf(f, "O %10.5f %10.5f %10.5f  \n", x, y, z);
-        }
-        fclose(f);
+        int64_t wrong = 0;
+        check(mks_write_frame(h, base.c_str(), time, (int64_t)iter, &wrong));
+        if (sic()) printf(" NumAtWrong: %lld\n", (long long)wrong);
+        FILE *f;
         f = fopen((base + ".src").c_str(), "w");
         fprintf(f, " load xyz %s.xyz\n color temperature\n set background white\n set boundbox true\n zoom 140\n"
                    " rotate x 41\n rotate y 4\n spacefill 2\n color axes black\n wireframe 2\n color atom green\n"
@@ -383,7 +302,7 @@ int main()
     check(mks_get_observables(h, &ob));
     printf(" Atoms,Voids,AdAtoms %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,
            (long long)ob.mc_sites);
-    Frames fr{h, in, lx, ly, lz, lx / 6, ly / 6};
+    Frames fr{h, in};
     fr.write(0.0, 0, 0);
     bool iter_mode = in.exit_strategy == "Iter";
     long long frame = 0, events = 0;

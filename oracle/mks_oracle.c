@@ -2325,6 +2325,30 @@ int ora_write_xyz(ora_t *o, const char *path)
     fclose(f);
     return 0;
 }
+/* All four frame files of WriteMolMolXYZFile (<base>.xyz, _d, _v, _w) with
+ * the given clock and iteration; for SiC the swap-and-restore of the wrong
+ * sites is applied to the oracle's lattice, as the reference does. */
+int ora_write_frame(ora_t *o, const char *base, double time, int64_t iter)
+{
+    if (setjmp(o->jb)) return -1;
+    char p[4][2100];
+    snprintf(p[0], sizeof p[0], "%s.xyz", base);
+    snprintf(p[1], sizeof p[1], "%s_d.xyz", base);
+    snprintf(p[2], sizeof p[2], "%s_v.xyz", base);
+    snprintf(p[3], sizeof p[3], "%s_w.xyz", base);
+    FILE *f[4];
+    for (int i = 0; i < 4; i++) {
+        f[i] = fopen(p[i], "w");
+        if (!f[i]) {
+            for (int j = 0; j < i; j++) fclose(f[j]);
+            return -1;
+        }
+    }
+    write_xyz_files(o, f[0], f[1], f[2], f[3], time, iter);
+    for (int i = 0; i < 4; i++) fclose(f[i]);
+    return 0;
+}
+
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9])
 {
     int k = 0;

@@ -86,6 +86,7 @@ int ora_site_info(const ora_t *o, int x, int y, int z, int32_t nn[12],
                   int32_t *ind_event, double *prob);
 /* Write the xyz frame exactly as WriteMolMolXYZFile would. */
 int ora_write_xyz(ora_t *o, const char *path);
+int ora_write_frame(ora_t *o, const char *base, double time, int64_t iter);
 
 /* The state as one byte per diamond site, in the GPU engine's layout
  * (mulskips_gb300/csrc/lattice.cuh): out[(z1*LenY/6 + b)*LenX/6 + a] =

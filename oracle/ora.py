@@ -53,6 +53,7 @@ def lib():
         L.ora_get_lattcoo.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_site_info.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.ora_write_xyz.argtypes = [C.c_void_p, C.c_char_p]
+        L.ora_write_frame.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_int64]
         L.ora_get_rates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ora_get_cov_rates.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ora_ncov.argtypes = [C.c_void_p]
@@ -201,6 +202,11 @@ class Oracle:
 
     def write_xyz(self, path):
         if lib().ora_write_xyz(self._h, path.encode()):
+            raise RuntimeError(lib().ora_last_error().decode())
+
+    def write_frame(self, base, time, it):
+        """<base>.xyz, _d, _v, _w as WriteMolMolXYZFile writes them."""
+        if lib().ora_write_frame(self._h, base.encode(), float(time), int(it)):
             raise RuntimeError(lib().ora_last_error().decode())
 
     def rates(self):
