@@ -115,6 +115,14 @@ struct ora {
     int8_t *la_geo;                         /* InitSt LA input (ora_set_la_input) */
     int16_t *la_tsub;
     int8_t *cad_geo;                        /* InitSt IN input (ora_set_geometry) */
+    /* InitSt ST: probability tables per temperature (SetProbabilityFromField.f)
+     * and the interpolation pair of the last site (InterpProbFromField.f) */
+    int st, st_fixed, st_n;
+    int st_T[300];
+    double (*st_E)[NCRYSTAL_MAX][4][4][4][4][4][4];
+    double (*st_D)[NCRYSTAL_MAX][3];
+    double st_angle, st_ttop, st_tbottom;
+    int st_lo, st_hi, st_wl, st_wu;
     char init_st[3], run_type[3], exit_strategy[5];
     char save_final[3], save_coo[3];
     char restartfile[2048], coofile[2048];
@@ -405,10 +413,44 @@ static void erase_void(ora_t *o, const int site[3])
 /* ============ rate tables ============ */
 static const double KB = 0.00008617330350;   /* Get_Prob.f:70 */
 
+/* InterpProbFromField, MS/mcevent/InterpProbFromField.f:22-57: the table
+ * row at temperature t if there is one (FINDLOC), else the rows around it
+ * (MINLOC of the positive differences and the row before) with integer
+ * weights |T_upper - t| for the lower row and |T_lower - t| for the upper.
+ * The reference copies whole interpolated tables on every call; the oracle
+ * keeps the row pair and weights and mixes the entries Get_Prob reads (the
+ * same values). */
+static void st_interp(ora_t *o, int t)
+{
+    for (int i = 0; i < o->st_n; i++)
+        if (o->st_T[i] == t) {
+            o->st_lo = o->st_hi = i;
+            return;
+        }
+    int iu = -1;
+    for (int i = 0; i < o->st_n; i++) {
+        int d = o->st_T[i] - t;
+        if (d > 0 && (iu < 0 || d < o->st_T[iu] - t)) iu = i;
+    }
+    if (iu <= 0) ora_fail(o, "temperature %d K outside the probability table", t);
+    o->st_lo = iu - 1;
+    o->st_hi = iu;
+    o->st_wl = abs(o->st_T[iu] - t);
+    o->st_wu = abs(o->st_T[iu - 1] - t);
+}
+static double st_mix(const ora_t *o, double lo, double hi)
+{
+    if (o->st_lo == o->st_hi) return lo;
+    return ((double)o->st_wl * lo + (double)o->st_wu * hi) / (double)(o->st_wl + o->st_wu);
+}
+static int st_live(const ora_t *o) { return o->st && !o->st_fixed; }
+
 /* PE(...) entry; the LA law of Get_Prob.f:127-149 is evaluated per element,
  * which equals recomputing the whole table and reading one entry. */
 static double pe_entry(ora_t *o, int s, int i1, int i2, int i3, int i4, int i5, int i6, int temperature)
 {
+    if (st_live(o))
+        return st_mix(o, o->st_E[o->st_lo][s - 1][i1][i2][i3][i4][i5][i6], o->st_E[o->st_hi][s - 1][i1][i2][i3][i4][i5][i6]);
     double v = o->ptransE[s - 1][i1][i2][i3][i4][i5][i6];
     if (o->la2) return v != 0.0 ? o->lap.P0[s - 1] * exp(-v / (KB * (double)temperature)) : 0.0;
     if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
@@ -420,6 +462,7 @@ static double pe_entry(ora_t *o, int s, int i1, int i2, int i3, int i4, int i5, 
 static double la2_pd(ora_t *o, int s, int coor, int temperature);
 static double pd_entry(ora_t *o, int s, int coor, int temperature)
 {
+    if (st_live(o)) return st_mix(o, o->st_D[o->st_lo][s - 1][coor - 1], o->st_D[o->st_hi][s - 1][coor - 1]);
     double v = o->ptransD[s - 1][coor - 1];
     if (o->la2) return la2_pd(o, s, coor, temperature);
     if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
@@ -510,6 +553,10 @@ static void get_prob(ora_t *o, int occ, int nsic, int covind, int coor,
     } else if (la) {
         temperature = ibits(*LC(o, site), POS_T, LEN_T);
         if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob()");
+    } else if (st_live(o)) {                   /* Get_Prob.f:77-91 */
+        temperature = ibits(*LC(o, site), POS_T, LEN_T);
+        if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob()");
+        st_interp(o, temperature);
     }
     if (covind > 0 && covind < WALL) {            /* desorption, :91-119 */
         if (occ != 0) ora_fail(o, "ERROR Covind!=0 with Occ!=0 in get_prob");
@@ -1196,6 +1243,10 @@ static void get_prob_ini(ora_t *o, int occ, int nsic, int coor, const int site[3
     if (o->init_st[0] == 'L' && o->init_st[1] == 'A') {
         temperature = ibits(*LC(o, site), POS_T, LEN_T);
         if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob_ini()");
+    } else if (st_live(o)) {                   /* Get_Prob_Ini.f:42-53 */
+        temperature = ibits(*LC(o, site), POS_T, LEN_T);
+        if (temperature == 0) ora_fail(o, "Temperature is zero in get_prob_ini()");
+        st_interp(o, temperature);
     }
     *index_event = 0;
     *prob_event = 0.0;
@@ -1438,6 +1489,65 @@ static void set_finfet(ora_t *o, int len, int lenww, int lenwwtop, int lap)
     list_pass(o, 0, lx - 1, 0, ly - 1, 6, lenwwtop + 9, 1);
 }
 
+/* SetTrenchSi, MS/initial/SetTrenchSi.f:22-338 (InitSt ST, MS/main.f:265-266):
+ * temperature T(z) = INT(Tbottom + (Ttop - Tbottom) z / (Len3 - 1)) below
+ * Len3 and INT(Ttop) above, on every grid point; walls at z = 0..3 and
+ * LenZ-4..LenZ-1; Si bulk (coor 4) at z = 4..20; Si at z = 21..Len3-1 except
+ * the trench |x - Lenh| <= Len - (Len3 - z) cot(angle), Len2 < z < Len3; then
+ * the closing passes over z = 21..Len3+9.  Pi is the reference's
+ * REAL(8) :: Pi initialised from a default-REAL literal, i.e. single
+ * precision.  With Ttop = Tbottom the tables are interpolated once at Ttop. */
+static void set_trench(ora_t *o, int len, int len2, int len3)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz;
+    const double pi = (double)3.1415926535897932384626433832795028841971f;
+    double arad = o->st_angle * pi / 180.0;
+    int lenh = lx / 2 - 1;
+    int site[3], nextn[4][3];
+    lg(o, " %d %d %d\n", lenh, len, len3);
+    for (int z = 0; z < lz; z++) {
+        int t = z < len3 ? (int)(o->st_tbottom + (o->st_ttop - o->st_tbottom) * z / (len3 - 1)) : (int)o->st_ttop;
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) mvbits(t, LEN_T, &o->latt[lidx(o, x, y, z)], POS_T);
+    }
+    if (o->st_fixed) {
+        st_interp(o, (int)o->st_ttop);
+        for (int sp = 0; sp < NCRYSTAL_MAX; sp++) {
+            double *e = &o->ptransE[sp][0][0][0][0][0][0];
+            const double *lo = &o->st_E[o->st_lo][sp][0][0][0][0][0][0], *hi = &o->st_E[o->st_hi][sp][0][0][0][0][0][0];
+            for (int k = 0; k < 4096; k++) e[k] = st_mix(o, lo[k], hi[k]);
+            for (int c = 0; c < 3; c++) o->ptransD[sp][c] = st_mix(o, o->st_D[o->st_lo][sp][c], o->st_D[o->st_hi][sp][c]);
+        }
+    }
+    set_walls(o, 0, 3);
+    set_walls(o, lz - 4, lz - 1);
+    for (int z = 4; z <= 20; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << POS_SI) | (1u << POS_OCC));
+                mvbits(4, LEN_COOR, v, POS_COOR);
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                add_bulk(o, site, nextn);
+            }
+    for (int z = 21; z <= len3 - 1; z++) {
+        double half = (double)len - (double)(len3 - z) * cos(arad) / sin(arad);
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                if ((double)abs(x - lenh) <= half && z > len2 && z < len3) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << POS_SI) | (1u << POS_OCC));
+            }
+    }
+    coor_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
+    list_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
+}
+
 /* SetCAD, MS/initial/SetCAD.f:24-421 (fresh start), for InitSt 'LA' after
  * SetT (MS/initial/SetT.f:25-50) and for InitSt 'IN' (MS/main.f:279-280).
  * LA: geometry id per layer z (`la_geo[z]`, 1 = Si, 10 = wall/air, as
@@ -1631,15 +1741,17 @@ static double to_real(const char *s)
     return strtod(b, NULL);
 }
 
-static void set_probability(ora_t *o, rd_t *r)
+/* One block of rate lines (evaporation, deposition, absorption, desorption)
+ * into the given tables; log: print the maxElines line. */
+static void read_rate_block(ora_t *o, rd_t *r, double (*pE)[4][4][4][4][4][4], double (*pD)[3], int log)
 {   /* SetProbability, MS/mcevent/SetProbability.f:21-143 */
     static const int maxe[4][4] = {   /* [ncov][ncrystal] */
         {0, 3, 18, 57}, {0, 9, 50, 150}, {0, 19, 100, 288}, {0, 34, 172, 480}};
-    memset(o->ptransE, 0, sizeof o->ptransE);
+    memset(pE, 0, sizeof(double) * NCRYSTAL_MAX * 4096);
     if (o->ncrystal < 1 || o->ncrystal > 3 || o->ncov < 0 || o->ncov > 3)
         ora_fail(o, "ERROR NOT IMPLEMENTED: NCrystal and NCov must be <= 3 3");
     int maxlines = maxe[o->ncov][o->ncrystal];
-    lg(o, " maxElines %d\n", maxlines);
+    if (log) lg(o, " maxElines %d\n", maxlines);
     char it[3][256];
     for (int i = 0; i < maxlines; i++) {
         rd_items(o, r, 3, it);
@@ -1661,13 +1773,13 @@ static void set_probability(ora_t *o, rd_t *r)
         }
         for (int j = 0; j < 6; j++)
             if (ind[j] > 3) ora_fail(o, "evaporation index digit > 3");
-        o->ptransE[indsp - 1][ind[0]][ind[1]][ind[2]][ind[3]][ind[4]][ind[5]] = val;
+        pE[indsp - 1][ind[0]][ind[1]][ind[2]][ind[3]][ind[4]][ind[5]] = val;
     }
     for (int j = 0; j < o->ncrystal * 3; j++) {
         rd_items(o, r, 3, it);
         int indsp = atoi(it[0]), el = atoi(it[1]);
         if (indsp > o->ncrystal || indsp < 1 || el < 1 || el > 3) ora_fail(o, "ERROR: 1st index in depo prob block must be <= NCrystal");
-        o->ptransD[indsp - 1][el - 1] = to_real(it[2]);
+        pD[indsp - 1][el - 1] = to_real(it[2]);
     }
     for (int j = 0; j < o->ncov * 3; j++) {
         rd_items(o, r, 3, it);
@@ -1681,6 +1793,49 @@ static void set_probability(ora_t *o, rd_t *r)
         if (indsp <= o->ncrystal || indsp > o->ncrystal + o->ncov || el < 0 || el > 3) ora_fail(o, "ERROR: desorption index");
         o->ptransDes[indsp - o->ncrystal - 1][el] = to_real(it[2]);
     }
+}
+
+static void set_probability(ora_t *o, rd_t *r)
+{   /* SetProbability.f:21-143 */
+    read_rate_block(o, r, o->ptransE, o->ptransD, 1);
+}
+
+/* SetProbabilityFromField, MS/mcevent/SetProbabilityFromField.f:23-171: the
+ * table file named on the next line of start.dat: ntemp, nprob, then per
+ * temperature its value and one block of rate lines. */
+static void set_probability_from_field(ora_t *o, rd_t *r, const char *startdat)
+{
+    if (!rd_line(r)) ora_fail(o, "start.dat: missing probability table file name");
+    char name[4096];
+    snprintf(name, sizeof name, "%s", r->line);
+    for (char *e = name + strlen(name); e > name && isspace((unsigned char)e[-1]); e--) e[-1] = 0;
+    rd_t t;
+    memset(&t, 0, sizeof t);
+    t.f = fopen(name, "r");
+    if (!t.f && name[0] != '/') {              /* relative to the start.dat's directory */
+        char alt[8192];
+        const char *sl = strrchr(startdat, '/');
+        if (sl) {
+            snprintf(alt, sizeof alt, "%.*s/%s", (int)(sl - startdat), startdat, name);
+            t.f = fopen(alt, "r");
+        }
+    }
+    if (!t.f) ora_fail(o, "cannot open probability table %s", name);
+    char it[2][256];
+    rd_items(o, &t, 1, it);
+    int n = atoi(it[0]);
+    rd_items(o, &t, 1, it);                    /* nprob, unused by the reference too */
+    if (n < 1 || n > 300) { fclose(t.f); ora_fail(o, "ntemp %d outside 1..300", n); }
+    o->st_n = n;
+    o->st_E = calloc((size_t)n, sizeof *o->st_E);
+    o->st_D = calloc((size_t)n, sizeof *o->st_D);
+    if (!o->st_E || !o->st_D) { fclose(t.f); ora_fail(o, "allocation failed"); }
+    for (int i = 0; i < n; i++) {
+        rd_items(o, &t, 1, it);
+        o->st_T[i] = atoi(it[0]);
+        read_rate_block(o, &t, o->st_E[i], o->st_D[i], i == 0);
+    }
+    fclose(t.f);
 }
 
 static void parse_startdat(ora_t *o, const char *path)
@@ -1720,7 +1875,16 @@ static void parse_startdat(ora_t *o, const char *path)
         rd_items(o, &r, 1, it); snprintf(o->homogeneous, sizeof o->homogeneous, "%.1s", it[0]);
     } else if (!strcmp(o->init_st, "IN")) {     /* MS/main.f:116-117: the geometry file name */
         if (!rd_line(&r)) { fclose(r.f); ora_fail(o, "start.dat: missing geometry file name"); }
-    } else if (!strcmp(o->init_st, "SH") || !strcmp(o->init_st, "ST")) {
+    } else if (!strcmp(o->init_st, "ST")) {     /* MS/main.f:109-115 */
+        rd_items(o, &r, 6, it);
+        o->len1 = atoi(it[0]); o->len2 = atoi(it[1]); o->len3 = atoi(it[2]);
+        o->st_angle = to_real(it[3]); o->st_ttop = to_real(it[4]); o->st_tbottom = to_real(it[5]);
+        lg(o, " Temperature on top in Kelvin: %.17g\n", o->st_ttop);
+        lg(o, " Temperature on bottom in Kelvin: %.17g\n", o->st_tbottom);
+        o->st = 1;
+        o->st_fixed = o->st_ttop == o->st_tbottom;
+        if (o->ncov != 0) { fclose(r.f); ora_fail(o, "InitSt ST with coverage species is not restated"); }
+    } else if (!strcmp(o->init_st, "SH")) {
         fclose(r.f);
         ora_fail(o, "InitSt %s is not restated by the oracle", o->init_st);
     } else {
@@ -1762,7 +1926,8 @@ static void parse_startdat(ora_t *o, const char *path)
         if (!rd_line(&r)) ora_fail(o, "start.dat: missing coo file name");
         snprintf(o->coofile, sizeof o->coofile, "%s", r.line);
     }
-    set_probability(o, &r);
+    if (o->st) set_probability_from_field(o, &r, path);   /* MS/main.f:215-219 */
+    else set_probability(o, &r);
     fclose(r.f);
 }
 
@@ -2103,6 +2268,8 @@ void ora_destroy(ora_t *o)
     free(o->la_geo);
     free(o->la_tsub);
     free(o->cad_geo);
+    free(o->st_E);
+    free(o->st_D);
     free(o->latt_base);
     free(o->lind_base);
     free(o->mc);
@@ -2134,6 +2301,8 @@ int ora_init(ora_t *o)
         set_nc(o, o->len1, o->len2, o->len3, 0);
     } else if (!strcmp(o->init_st, "S")) {       /* MS/main.f:257-258 */
         set_nc(o, o->len1, o->len1, o->len1, 1);
+    } else if (!strcmp(o->init_st, "ST")) {      /* MS/main.f:265-266 */
+        set_trench(o, o->len1, o->len2, o->len3);
     } else if (!strcmp(o->init_st, "I")) {       /* MS/main.f:245-246 */
         set_invp(o, o->len1, o->len2);
     } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
