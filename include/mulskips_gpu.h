@@ -288,6 +288,19 @@ int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lattco
  * the values 1..4 only, pymulskips/io.py:1013-1066).  Either pointer may be
  * NULL.                                                                    */
 int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field);
+/* Tabulated rates instead of fixed tables (InitSt ST: SetProbabilityFromField.f,
+ * InterpProbFromField.f, Get_Prob.f:77-91): each site's rates are the
+ * PtransE / PtransD tables at its own temperature, linear in T between the
+ * ntemp (<= 32) tabulated temperatures (the reference's integer-weighted
+ * interpolation) and clamped outside them.  Replica i uses temps + i*ntemp
+ * (increasing), ptransE + (i*ntemp + k)*3*4096 and ptransD + (i*ntemp + k)*9
+ * for row k.  The temperatures are the replica's static field
+ * (mks_batch_load_temperature or mks_batch_set_field, loaded first).  Every
+ * class rate and deposition sum must not decrease with T (the kernel bounds a
+ * tile's rates at its hottest layer and thins).  NCov = 0.  Switches the
+ * replicas to the per-site-temperature kernels, like mks_batch_set_la.     */
+int mks_batch_set_tabulated(mks_handle *h, int32_t ntemp, const int32_t *temps, const double *ptransE,
+                            const double *ptransD);
 int mks_batch_get_phases(mks_handle *h, int32_t rep, int32_t *coo, int32_t *species);
 /* mks_load_lattice for replica rep of a batch.                            */
 int mks_batch_load_lattice(mks_handle *h, int32_t rep, const int32_t *lattcoo);

@@ -86,6 +86,8 @@ struct QuadDev {
 // temperature is the prescribed field T(z,t) = Tb + Ta exp(-((t-t0)/w)^2)
 // exp(-depth/L), depth = max(0, (zsurf - z) sf / 10) nm, rounded to integer K
 // as LattCoo bits 9-21 store it, evaluated at the window's midpoint.
+constexpr int LA_NTAB = 32;                  // temperatures of a tabulated rate law
+
 struct LADev {
     // crystal atoms per species: init_cnt at mks_batch_set_la, cnt updated by
     // the tiles (atomics); the liquid of species s is init_cnt[s] - cnt[s]
@@ -108,6 +110,13 @@ struct LADev {
     const uint16_t *tfield;
     const float *tlayer;
     int tNB, tpitch;
+    // tabulated rates instead of the law above (InitSt ST, SetProbabilityFromField.f,
+    // InterpProbFromField.f): class rates and deposition rates at ntab
+    // temperatures, linear in T between them (0: not tabulated)
+    int ntab;
+    float tabT[LA_NTAB];
+    float tabE[LA_NTAB][64];
+    float tabD[LA_NTAB][3][3];
 };
 
 constexpr float KB_EV_F = 8.617330350e-5f;   // Get_Prob.f:70
@@ -126,8 +135,32 @@ __device__ __forceinline__ float la_temp_at(const LADev &A, int a, int b, int z1
     if (A.tfield) return (float)__ldg(&A.tfield[((int64_t)z1 * A.tNB + b) * A.tpitch + a]);
     return la_temp(A, z1, t);
 }
+// row i and upper weight w of temperature T in the table: T between tabT[i]
+// and tabT[i+1] (clamped to the table's ends)
+__device__ __forceinline__ void la_tab_at(const LADev &A, float T, int &i, float &w)
+{
+    i = 0;
+    w = 0.f;
+    if (T <= A.tabT[0]) return;
+    if (T >= A.tabT[A.ntab - 1]) {
+        i = A.ntab - 1;
+        return;
+    }
+    while (i + 2 < A.ntab && A.tabT[i + 1] <= T) i++;
+    w = (T - A.tabT[i]) / (A.tabT[i + 1] - A.tabT[i]);
+}
+__device__ __forceinline__ float la_tab_mix(const LADev &A, int i, float w, float lo, float hi)
+{
+    return w > 0.f ? (1.f - w) * lo + w * hi : lo;
+}
 __device__ __forceinline__ float la_dep(const LADev &A, int s, int co, float T)
 {
+    if (A.ntab) {
+        int i;
+        float w;
+        la_tab_at(A, T, i, w);
+        return la_tab_mix(A, i, w, A.tabD[i][s][co - 1], w > 0.f ? A.tabD[i + 1][s][co - 1] : 0.f);
+    }
     // LaserAnnealing Get_Prob.f:147-151: weighted by the liquid fraction of s
     float E = A.Edep[s][co - 1];
     if (E == 0.f || !(A.xliq[s] > 0.f)) return 0.f;
@@ -138,6 +171,12 @@ __device__ __forceinline__ int la_coor(int c) { return c == CLS_C3 ? 3 : (c == C
 // rate of one site of class c at temperature T
 __device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
 {
+    if (A.ntab && c >= CLS_OCC0) {
+        int i;
+        float w;
+        la_tab_at(A, T, i, w);
+        return la_tab_mix(A, i, w, A.tabE[i][c], w > 0.f ? A.tabE[i + 1][c] : 0.f);
+    }
     if (c >= CLS_OCC0) {
         float E = A.E[c];
         return E != 0.f ? A.P0[(c - CLS_OCC0) / NCENSUS] * __expf(-E / (KB_EV_F * T)) : 0.f;
@@ -2269,6 +2308,74 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
     if (rc) return rc;
     h->la_window = d.empty() ? 0 : d[0].window;
     // a captured window graph holds the plain kernels: capture again
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    CK(cudaMemcpyAsync(h->d_la, la.data(), sizeof(LADev) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->la_on = 1;
+    return 0;
+}
+
+int mks_batch_set_tabulated(mks_handle *h, int32_t ntemp, const int32_t *temps, const double *ptransE,
+                            const double *ptransD)
+{
+    if (!h || !temps || !ptransE || !ptransD) return fail(MKS_ERR_ARG, "bad arguments");
+    if (ntemp < 1 || ntemp > LA_NTAB) return fail(MKS_ERR_ARG, "ntemp %d outside 1..%d", ntemp, LA_NTAB);
+    size_t n = h->reps.size();
+    std::vector<LADev> la(n);
+    for (size_t i = 0; i < n; i++) {
+        const RepHost &r = h->reps[i];
+        if (r.cfg.ncov) return fail(MKS_ERR_UNSUPPORTED, "tabulated rates with a coverage species");
+        if (r.t_layer_off < 0) return fail(MKS_ERR_ARG, "replica %zu: load its temperature field first", i);
+        LADev &A = la[i];
+        memset(&A, 0, sizeof A);
+        A.on = 1;
+        A.sf = (float)r.cfg.sf;
+        A.tfield = h->d_tfield + r.st_off;
+        A.tlayer = h->d_tlayer + r.t_layer_off;
+        A.tNB = r.NB;
+        A.tpitch = r.pitch;
+        A.ntab = ntemp;
+        for (int s = 0; s < 3; s++) {
+            A.xliq[s] = 1.f;
+            A.Tm[s] = A.sigma[s] = A.w = A.L = 1.f;
+        }
+        for (int k = 0; k < ntemp; k++) {
+            A.tabT[k] = (float)temps[i * ntemp + k];
+            if (k && !(A.tabT[k] > A.tabT[k - 1]))
+                return fail(MKS_ERR_ARG, "replica %zu: table temperatures must increase", i);
+            RepHost row = r;                   // the class mapping of rate_tables on row k
+            memcpy(row.ptransE, ptransE + ((size_t)i * ntemp + k) * 3 * 4096, sizeof row.ptransE);
+            memcpy(row.ptransD, ptransD + ((size_t)i * ntemp + k) * 9, sizeof row.ptransD);
+            RepDev d;
+            memset(&d, 0, sizeof d);
+            rate_tables(row, d);
+            for (int c = 0; c < 64; c++) A.tabE[k][c] = c >= CLS_OCC0 ? d.rate[c] : 0.f;
+            for (int sp = 0; sp < 3; sp++)
+                for (int co = 0; co < 3; co++) A.tabD[k][sp][co] = (float)row.ptransD[sp * 3 + co];
+        }
+        // the per-tile bound takes the rates at the hottest staged layer
+        for (int k = 1; k < ntemp; k++) {
+            for (int c = CLS_OCC0; c < NCLASS; c++)
+                if (A.tabE[k][c] < A.tabE[k - 1][c])
+                    return fail(MKS_ERR_UNSUPPORTED, "replica %zu: tabulated rate of class %d decreases with T", i, c);
+            for (int co = 0; co < 3; co++) {
+                float a = 0.f, b = 0.f;
+                for (int sp = 0; sp < 3; sp++) {
+                    a += A.tabD[k - 1][sp][co];
+                    b += A.tabD[k][sp][co];
+                }
+                if (b < a) return fail(MKS_ERR_UNSUPPORTED, "replica %zu: tabulated deposition decreases with T", i);
+            }
+        }
+    }
+    std::vector<RepDev> d;
+    int rc = download_reps(h, d);
+    if (rc) return rc;
+    h->la_window = d.empty() ? 0 : d[0].window;
     if (h->graph_exec) {
         cudaGraphExecDestroy(h->graph_exec);
         h->graph_exec = nullptr;

@@ -298,6 +298,17 @@ class Batch:
         f = np.ascontiguousarray(f).reshape(-1)
         N.check(N.lib().mks_batch_set_field(self._h, int(rep), N.ptr(f)))
 
+    def set_tabulated(self, temps, ptransE, ptransD):
+        """Rates interpolated per site from tables at temperatures temps (InitSt
+        ST): temps (n, ntemp) increasing, ptransE (n, ntemp, 3, 4, 4, 4, 4, 4, 4),
+        ptransD (n, ntemp, 3, 3); the temperature fields must be loaded."""
+        t = np.ascontiguousarray(temps, dtype=np.int32).reshape(self.n, -1)
+        nt = t.shape[1]
+        e = np.ascontiguousarray(ptransE, dtype=np.float64).reshape(-1)
+        d = np.ascontiguousarray(ptransD, dtype=np.float64).reshape(-1)
+        assert e.size == self.n * nt * 3 * 4096 and d.size == self.n * nt * 9
+        N.check(N.lib().mks_batch_set_tabulated(self._h, nt, N.ptr(t), N.ptr(e), N.ptr(d)))
+
     def get_phases(self, rep=0):
         """(coo, species) of replica rep as the reference's GETPHASES / GETXGE
         messages: arrays [z, x + LenX*y] of shape (LenZ, LenX*LenY) (views

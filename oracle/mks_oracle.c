@@ -1827,8 +1827,8 @@ static void set_probability_from_field(ora_t *o, rd_t *r, const char *startdat)
     rd_items(o, &t, 1, it);                    /* nprob, unused by the reference too */
     if (n < 1 || n > 300) { fclose(t.f); ora_fail(o, "ntemp %d outside 1..300", n); }
     o->st_n = n;
-    o->st_E = calloc((size_t)n, sizeof *o->st_E);
-    o->st_D = calloc((size_t)n, sizeof *o->st_D);
+    o->st_E = (double (*)[NCRYSTAL_MAX][4][4][4][4][4][4])calloc((size_t)n, sizeof *o->st_E);
+    o->st_D = (double (*)[NCRYSTAL_MAX][3])calloc((size_t)n, sizeof *o->st_D);
     if (!o->st_E || !o->st_D) { fclose(t.f); ora_fail(o, "allocation failed"); }
     for (int i = 0; i < n; i++) {
         rd_items(o, &t, 1, it);
