@@ -30,6 +30,7 @@
 #include <mutex>
 
 #include "lattice.cuh"
+#include "shapes.cuh"
 #include "rng.cuh"
 #include "../../include/mulskips_gpu.h"
 
@@ -2540,6 +2541,8 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
     return 0;
 }
 
+int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st);
+
 int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
 {
     const RepHost &r = h->reps[rep];
@@ -2572,6 +2575,19 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
                     return fail(MKS_ERR_INVARIANT, "bad LattCoo word %d", v);
                 at(a, b, z1) = mk(sp, co, 0, 0);
             }
+    return upload_compact(h, rep, st);
+}
+
+// The first list entry and dummy flag of coor-1 sites, then the upload of the
+// padded compact state st of replica rep and the event-site scan.
+int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st)
+{
+    const RepHost &r = h->reps[rep];
+    auto at = [&](int a, int b, int z) -> uint8_t & {
+        a = (a % r.NA + r.NA) % r.NA;
+        b = (b % r.NB + r.NB) % r.NB;
+        return st[((size_t)z * r.NB + b) * r.pitch + a];
+    };
     // the first list entry of a coor-1 empty site is its one occupied
     // neighbour; its dummy flag follows that neighbour's coordination
     // (Get_Prob.f:156-184), as a rebuild from LattCoo gives (SetCAD.f:301-418)
@@ -2729,6 +2745,54 @@ int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field)
         int T = field[(size_t)z + (size_t)lz * ((size_t)x + (size_t)lx * y)];
         return T == 10 ? old : T;
     });
+}
+
+int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const int32_t *lens, const double *params)
+{
+    if (!h || !init_st || !lens || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    const int lx = r.cfg.lenx, ly = r.cfg.leny, lz = r.cfg.lenz;
+    mks_shapes::Grid g(lx, ly, lz);
+    std::string kind(init_st);
+    std::vector<int> temp;
+    auto within = [&](int v, int lo, int hi) { return v >= lo && v <= hi; };
+    if (kind == "C") {                                        // main.f:261-262
+        if (!within(lens[0], 1, lx - 24) || !within(lens[1], 1, ly - 24) || !within(lens[2], 1, lz - 24))
+            return fail(MKS_ERR_ARG, "SetNC lengths %d %d %d do not fit the box", lens[0], lens[1], lens[2]);
+        mks_shapes::set_nc(g, lens[0], lens[1], lens[2], false);
+    } else if (kind == "S") {                                 // main.f:257-258
+        if (!within(lens[0], 1, std::min(std::min(lx, ly), lz) - 24)) return fail(MKS_ERR_ARG, "SetNCSp length %d", lens[0]);
+        mks_shapes::set_nc(g, lens[0], lens[0], lens[0], true);
+    } else if (kind == "I") {                                 // main.f:245-246: SetInvPOff(Len1, Len2)
+        if (!within(lens[1], 24, lz - 12)) return fail(MKS_ERR_ARG, "SetInvPOff Len3 %d outside the box", lens[1]);
+        mks_shapes::set_invp(g, lens[0], lens[1]);
+    } else if (kind == "FF") {                                // main.f:273-278
+        int l[4];
+        for (int i = 0; i < 4; i++) l[i] = lens[i] - lens[i] % 24;
+        if (!within(l[0], 6, lz - 7) || !within(l[2], 6, lz - 16)) return fail(MKS_ERR_ARG, "SetSiFINFET lengths");
+        mks_shapes::set_finfet(g, l[0], l[1], l[2], l[3]);
+    } else if (kind == "ST") {                                // main.f:265-266
+        if (!params) return fail(MKS_ERR_ARG, "SetTrenchSi needs angle, Ttop, Tbottom");
+        if (!within(lens[2], 22, lz - 14)) return fail(MKS_ERR_ARG, "SetTrenchSi Len3 %d outside the box", lens[2]);
+        mks_shapes::set_trench(g, lens[0], lens[1], lens[2], params[0], params[1], params[2], temp);
+    } else {
+        return fail(MKS_ERR_UNSUPPORTED, "InitSt %s has no shape initializer", init_st);
+    }
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
+    int rc = upload_compact(h, rep, st);
+    if (rc) return rc;
+    if (kind == "ST")   // the temperatures of SetTrenchSi.f:46-63 as the replica's field
+        return set_temperature_impl(h, rep, [&](int, int, int z, int) { return temp[(size_t)z] & 8191; });
+    return 0;
+}
+
+int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params)
+{
+    if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_init_shape needs a single-replica handle");
+    return mks_batch_init_shape(h, 0, init_st, lens, params);
 }
 
 int mks_batch_get_phases(mks_handle *h, int32_t rep, int32_t *coo, int32_t *species)

@@ -1,0 +1,213 @@
+// shapes.cuh — the reference's free-form initial lattices, built on the host
+// directly in the compact one-byte-per-diamond-site layout (lattice.cuh):
+// SetNC / SetNCSp (a 3C parallelepiped or ball), SetInvPOff (inverted
+// pyramids in a 3C layer), SetSiFINFET (Si between walls) and SetTrenchSi
+// (a Si trench under a temperature gradient).  Each writes occupancy,
+// species, walls and the coordinations of its closing passes; the list heads
+// and dummy flags of coor-1 sites follow from those (as Get_Prob_Ini finds
+// them).  Only diamond sites exist here: the walls' off-grid points never
+// neighbour a diamond site.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <vector>
+
+#include "lattice.cuh"
+
+namespace mks_shapes {
+
+using mks::WALL;
+
+struct Grid {
+    int lx, ly, lz, NA, NB, NZ;
+    std::vector<uint8_t> st;   // index (z1 * NB + b) * NA + a
+    Grid(int lx_, int ly_, int lz_) : lx(lx_), ly(ly_), lz(lz_), NA(lx_ / 6), NB(ly_ / 6), NZ(lz_ / 3 + 1)
+    {
+        st.assign((size_t)NZ * NB * NA, 0);
+    }
+    // the byte of grid point (x, y, z), or nullptr if it is not a diamond site
+    uint8_t *at(int x, int y, int z)
+    {
+        if (x < 0 || y < 0 || z < 0 || x >= lx || y >= ly || z > lz) return nullptr;
+        if (x % 3 || y % 3 || z % 3) return nullptr;
+        int x1 = x / 3, y1 = y / 3, z1 = z / 3;
+        if ((x1 & 1) != (z1 & 1) || (y1 & 1) != (z1 & 1)) return nullptr;
+        int a = x1 >> 1, b = y1 >> 1;
+        if ((a + b + (z1 >> 1)) & 1) return nullptr;
+        return &st[((size_t)z1 * NB + b) * NA + a];
+    }
+    // neighbour d of site (a, b, z1), periodic in a and b; nullptr outside z
+    uint8_t *nb(int a, int b, int z1, int d)
+    {
+        int da, db, dz;
+        mks::nb_off(z1 & 1, d, da, db, dz);
+        int zz = z1 + dz;
+        if (zz < 0 || zz >= NZ) return nullptr;
+        int aa = (a + da + NA) % NA, bb = (b + db + NB) % NB;
+        return &st[((size_t)zz * NB + bb) * NA + aa];
+    }
+};
+
+// sublattice of a diamond grid point: 1 for (x1+y1+z1) mod 4 == 0, 2 for 3
+inline int kind_of(int x, int y, int z) { return ((x / 3 + y / 3 + z / 3) % 4 == 0) ? 1 : 2; }
+
+inline bool occupied(uint8_t v) { return v == WALL || (v & 3) != 0; }
+
+// The coordination pass of the closing passes over grid points x in [xa, xb],
+// y in [ya, yb], z in [za, zb] (z, y, x order, SetNC.f:62-134 and kin): a
+// site's coordination is its occupied neighbours (with walls: an empty site
+// does not count wall neighbours, SetSiFINFET.f:120-200); an occupied site
+// with none is removed and its neighbours' counts drop by one (floored at 0).
+inline void coor_pass(Grid &g, int xa, int xb, int ya, int yb, int za, int zb, bool walls)
+{
+    for (int z = za; z <= zb; z++) {
+        if (z % 3) continue;
+        int z1 = z / 3;
+        if (z < 0 || z1 >= g.NZ) continue;
+        for (int y = ya; y <= yb; y++)
+            for (int x = xa; x <= xb; x++) {
+                uint8_t *v = g.at((x % g.lx + g.lx) % g.lx, (y % g.ly + g.ly) % g.ly, z);
+                if (!v || (x % 3) || (y % 3)) continue;
+                if (walls && *v == WALL) continue;
+                int a = (int)((v - g.st.data()) % g.NA);
+                int b = (int)(((v - g.st.data()) / g.NA) % g.NB);
+                bool occ = occupied(*v);
+                int coor = 0;
+                for (int d = 0; d < 4; d++) {
+                    uint8_t *w = g.nb(a, b, z1, d);
+                    if (!w || !occupied(*w)) continue;
+                    if (occ || !walls || *w != WALL) coor++;
+                }
+                if (occ && *v != WALL && coor == 0) {
+                    *v = 0;
+                    for (int d = 0; d < 4; d++) {
+                        uint8_t *w = g.nb(a, b, z1, d);
+                        if (!w || *w == WALL) continue;
+                        int c = mks::co_of(*w) - 1;
+                        *w = mks::mk(mks::sp_of(*w), c < 0 ? 0 : c, mks::fd_of(*w), mks::dm_of(*w));
+                    }
+                } else if (*v != WALL) {
+                    *v = mks::mk(mks::sp_of(*v), coor, mks::fd_of(*v), mks::dm_of(*v));
+                }
+            }
+    }
+}
+
+inline void fill(Grid &g, int x, int y, int z, int sp)
+{
+    uint8_t *v = g.at(x, y, z);
+    if (v && *v != WALL) *v = mks::mk(sp, mks::co_of(*v), 0, 0);
+}
+
+// SetNC (SetNC.f:24-235) or, with sphere, SetNCSp (SetNCSp.f:24-237)
+inline void set_nc(Grid &g, int len1, int len2, int len3, bool sphere)
+{
+    int x0 = g.lx / 2 - len1 / 2, x1 = g.lx / 2 + len1 / 2 - 1;
+    int y0 = g.ly / 2 - len2 / 2, y1 = g.ly / 2 + len2 / 2 - 1;
+    int z0 = g.lz / 2 - len3 / 2, z1 = g.lz / 2 + len3 / 2 - 1;
+    for (int z = z0; z <= z1; z++)
+        for (int y = y0; y <= y1; y++)
+            for (int x = x0; x <= x1; x++) {
+                if (!g.at(x, y, z)) continue;
+                if (sphere) {
+                    long dx = x - g.lx / 2, dy = y - g.ly / 2, dz = z - g.lz / 2;
+                    if (dx * dx + dy * dy + dz * dz > (long)len1 * len1 / 4) continue;
+                }
+                fill(g, x, y, z, kind_of(x, y, z));
+            }
+    coor_pass(g, x0 - 10, x1 + 10, y0 - 10, y1 + 10, z0 - 10, z1 + 10, false);
+}
+
+// SetInvPOff (SetInvPOff.f:22-286), called with (Len1, Len2): pits where
+// |x-xc| + |y-yc| - 1.10 (z - Len3) <= Len for the box centre or a corner,
+// evaluated in single precision like the reference's default-REAL literal
+inline void set_invp(Grid &g, int len, int len3)
+{
+    int lenh = g.lx / 2 - 1;
+    for (int z = 0; z <= 20; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                uint8_t *v = g.at(x, y, z);
+                if (v) *v = mks::mk(kind_of(x, y, z), 4, 0, 0);
+            }
+    const int cx[5] = {lenh, 0, g.lx, 0, g.lx}, cy[5] = {lenh, 0, 0, g.ly, g.ly};
+    for (int z = 21; z <= len3 - 1; z++) {
+        float dz = 1.10f * (float)(z - len3);
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                if (!g.at(x, y, z)) continue;
+                bool pit = false;
+                for (int c = 0; c < 5 && !pit; c++)
+                    pit = (float)(std::abs(x - cx[c]) + std::abs(y - cy[c])) - dz <= (float)len;
+                if (!pit) fill(g, x, y, z, kind_of(x, y, z));
+            }
+    }
+    coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
+}
+
+// SetSiFINFET (SetSiFINFET.f:23-312): walls at z = 0..5 and LenZ-6..LenZ-1, a
+// wall layer from Lenwwtop, side walls from Lenww leaving an aperture of
+// Laperture around the centre in x; Si below Len
+inline void set_finfet(Grid &g, int len, int lenww, int lenwwtop, int lap)
+{
+    int xl = (int)(0.5f * (float)(g.lx - lap)), xr = (int)(0.5f * (float)(g.lx + lap));
+    auto wall = [&](int z, int xa, int xb) {
+        for (int y = 0; y < g.ly; y++)
+            for (int x = xa; x < xb; x++) {
+                uint8_t *v = g.at(x, y, z);
+                if (v) *v = WALL;
+            }
+    };
+    for (int z = 0; z <= 5; z++) wall(z, 0, g.lx);
+    for (int z = lenww; z <= g.lz - 7; z++) {
+        wall(z, 0, xl);
+        wall(z, xr, g.lx);
+    }
+    for (int z = lenwwtop; z <= g.lz - 7; z++) wall(z, 0, g.lx);
+    for (int z = g.lz - 6; z <= g.lz - 1; z++) wall(z, 0, g.lx);
+    for (int z = 6; z <= len - 1; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) fill(g, x, y, z, 1);
+    coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 6, lenwwtop + 9, true);
+}
+
+// SetTrenchSi (SetTrenchSi.f:22-338): walls at z = 0..3 and LenZ-4..LenZ-1, Si
+// bulk at z = 4..20, Si at z = 21..Len3-1 except the trench |x - Lenh| <=
+// Len - (Len3 - z) cot(angle), Len2 < z < Len3.  The reference's Pi is a
+// REAL(8) set from a default-REAL literal (single precision).  temp[z] gets
+// the temperature of layer z.
+inline void set_trench(Grid &g, int len, int len2, int len3, double angle, double ttop, double tbottom,
+                       std::vector<int> &temp)
+{
+    const double pi = (double)3.1415926535897932384626433832795028841971f;
+    double arad = angle * pi / 180.0;
+    int lenh = g.lx / 2 - 1;
+    temp.assign((size_t)g.lz + 1, 0);
+    for (int z = 0; z <= g.lz; z++)
+        temp[z] = z < len3 ? (int)(tbottom + (ttop - tbottom) * z / (len3 - 1)) : (int)ttop;
+    for (int z = 0; z <= 3; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++)
+                if (uint8_t *v = g.at(x, y, z)) *v = WALL;
+    for (int z = g.lz - 4; z <= g.lz - 1; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++)
+                if (uint8_t *v = g.at(x, y, z)) *v = WALL;
+    for (int z = 4; z <= 20; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++)
+                if (uint8_t *v = g.at(x, y, z)) *v = mks::mk(1, 4, 0, 0);
+    for (int z = 21; z <= len3 - 1; z++) {
+        double half = (double)len - (double)(len3 - z) * std::cos(arad) / std::sin(arad);
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                if (!g.at(x, y, z)) continue;
+                if ((double)std::abs(x - lenh) <= half && z > len2 && z < len3) continue;
+                fill(g, x, y, z, 1);
+            }
+    }
+    coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
+}
+
+}  // namespace mks_shapes

@@ -87,6 +87,15 @@ class Lattice:
     def init_flat(self, kind="S", len1=120):
         N.check(N.lib().mks_init_flat(self._h, kind.encode()[:1], int(len1)))
 
+    def init_shape(self, init_st, lens, params=None):
+        """The reference's shaped lattices: 'C' (SetNC), 'S' (SetNCSp), 'I'
+        (SetInvPOff), 'FF' (SetSiFINFET), 'ST' (SetTrenchSi, params = angle,
+        Ttop, Tbottom)."""
+        l = np.zeros(4, dtype=np.int32)
+        l[:len(lens)] = lens
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        N.check(N.lib().mks_init_shape(self._h, init_st.encode(), N.ptr(l), None if p is None else N.ptr(p)))
+
     def replay(self, events):
         ev = np.ascontiguousarray(events, dtype=N.EVENT_DTYPE)
         N.check(N.lib().mks_replay(self._h, N.ptr(ev), int(ev.size)))

@@ -20,6 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <algorithm>
 #include <string>
 #include <vector>
 #include <unistd.h>
@@ -46,6 +47,10 @@ struct Input {
     std::vector<double> pD = std::vector<double>(9, 0.0);
     std::vector<double> pAbs = std::vector<double>(9, 0.0);   // [coverage species][coor-1]
     std::vector<double> pDes = std::vector<double>(9, 0.0);
+    // InitSt ST: angle, Ttop, Tbottom and the probability table rows
+    double st_par[3] = {0, 0, 0};
+    std::vector<int> st_T;
+    std::vector<double> st_E, st_D;
 };
 
 [[noreturn]] void die(const char *msg)
@@ -107,6 +112,51 @@ double real_of(std::string s)
     return strtod(s.c_str(), nullptr);
 }
 
+// One block of rate records (SetProbability.f:21-143) into in.pE, pD, pAbs, pDes
+void read_rate_block(Records &r, Input &in, bool log)
+{
+    static const int maxe[4][4] = {{0, 3, 18, 57}, {0, 9, 50, 150}, {0, 19, 100, 288}, {0, 34, 172, 480}};
+    std::fill(in.pE.begin(), in.pE.end(), 0.0);
+    std::fill(in.pD.begin(), in.pD.end(), 0.0);
+    int ne = maxe[in.ncov < 4 ? in.ncov : 0][in.ncrystal];
+    if (log) printf(" maxElines %d\n", ne);
+    for (int i = 0; i < ne; i++) {
+        auto it = r.items(3);
+        int s = atoi(it[0].c_str());
+        long el = atol(it[1].c_str());
+        if (s < 1 || s > in.ncrystal) die("ERROR: 1st index in evap prob must be <= NCrystal");
+        int idx[6] = {0, 0, 0, 0, 0, 0};
+        int nd = in.ncrystal + in.ncov;
+        for (int j = 1; j <= in.ncrystal; j++) {
+            long p = 1;
+            for (int q = 0; q < nd - j; q++) p *= 10;
+            idx[j - 1] = (int)((el / p) % 10);
+        }
+        for (int j = in.ncrystal + 1; j <= nd; j++) {
+            long p = 1;
+            for (int q = 0; q < nd - j; q++) p *= 10;
+            idx[3 + j - in.ncrystal - 1] = (int)((el / p) % 10);
+        }
+        int k = (s - 1) * 4096 + idx[0] * 1024 + idx[1] * 256 + idx[2] * 64 + idx[3] * 16 + idx[4] * 4 + idx[5];
+        in.pE[k] = real_of(it[2]);
+    }
+    for (int j = 0; j < in.ncrystal * 3; j++) {
+        auto it = r.items(3);
+        int s = atoi(it[0].c_str()), el = atoi(it[1].c_str());
+        if (s < 1 || s > in.ncrystal || el < 1 || el > 3) die("ERROR: 1st index in depo prob block must be <= NCrystal");
+        in.pD[(s - 1) * 3 + el - 1] = real_of(it[2]);
+    }
+    // absorption, then desorption: NCov*3 records "NCrystal+i  coor  rate"
+    // (SetProbability.f:117-140)
+    for (int blk = 0; blk < 2; blk++)
+        for (int j = 0; j < in.ncov * 3; j++) {
+            auto it = r.items(3);
+            int s = atoi(it[0].c_str()) - in.ncrystal, el = atoi(it[1].c_str());
+            if (s < 1 || s > in.ncov || el < 1 || el > 3) die("ERROR: index in absorption/desorption block");
+            (blk ? in.pDes : in.pAbs)[(s - 1) * 3 + el - 1] = real_of(it[2]);
+        }
+}
+
 Input read_startdat(const char *path)
 {
     Input in;
@@ -127,8 +177,14 @@ Input read_startdat(const char *path)
     if (in.init_st == "FF") {
         it = r.items(4);
         for (int i = 0; i < 4; i++) in.len[i] = atoi(it[i].c_str());
-    } else if (in.init_st == "IN" || in.init_st == "SH" || in.init_st == "LA" || in.init_st == "ST") {
-        die("initialization not_implemented in the GPU engine (FS and F are)");
+    } else if (in.init_st == "ST") {                  // main.f:109-115
+        it = r.items(6);
+        for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
+        for (int i = 0; i < 3; i++) in.st_par[i] = real_of(it[3 + i]);
+        printf(" Temperature on top in Kelvin: %.17g\n", in.st_par[1]);
+        printf(" Temperature on bottom in Kelvin: %.17g\n", in.st_par[2]);
+    } else if (in.init_st == "IN" || in.init_st == "SH" || in.init_st == "LA") {
+        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF and ST are)");
     } else {
         it = r.items(3);
         for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
@@ -152,45 +208,29 @@ Input read_startdat(const char *path)
     if (in.save_final == "T") r.line(in.restart_file);
     in.save_coo = r.items(1)[0].substr(0, 2);
     if (in.save_coo == "T") r.line(in.coo_file);
-    // SetProbability.f:21-143
-    static const int maxe[4][4] = {{0, 3, 18, 57}, {0, 9, 50, 150}, {0, 19, 100, 288}, {0, 34, 172, 480}};
-    int ne = maxe[in.ncov < 4 ? in.ncov : 0][in.ncrystal];
-    printf(" maxElines %d\n", ne);
-    for (int i = 0; i < ne; i++) {
-        it = r.items(3);
-        int s = atoi(it[0].c_str());
-        long el = atol(it[1].c_str());
-        if (s < 1 || s > in.ncrystal) die("ERROR: 1st index in evap prob must be <= NCrystal");
-        int idx[6] = {0, 0, 0, 0, 0, 0};
-        int nd = in.ncrystal + in.ncov;
-        for (int j = 1; j <= in.ncrystal; j++) {
-            long p = 1;
-            for (int q = 0; q < nd - j; q++) p *= 10;
-            idx[j - 1] = (int)((el / p) % 10);
+    if (in.init_st == "ST") {
+        // SetProbabilityFromField.f:23-171: the table file named on the next
+        // line: ntemp, nprob, then per temperature its value and one block
+        std::string name;
+        if (!r.line(name)) die("start.dat: missing probability table file name");
+        while (!name.empty() && isspace((unsigned char)name.back())) name.pop_back();
+        while (!name.empty() && isspace((unsigned char)name.front())) name.erase(name.begin());
+        FILE *tf = fopen(name.c_str(), "r");
+        if (!tf) die("cannot open the probability table file");
+        Records t(tf);
+        int n = atoi(t.items(1)[0].c_str());
+        t.items(1);                                   // nprob, unused by the reference too
+        if (n < 1 || n > 32) die("ERROR: the GPU engine takes 1..32 table temperatures");
+        for (int k = 0; k < n; k++) {
+            in.st_T.push_back(atoi(t.items(1)[0].c_str()));
+            read_rate_block(t, in, k == 0);
+            in.st_E.insert(in.st_E.end(), in.pE.begin(), in.pE.end());
+            in.st_D.insert(in.st_D.end(), in.pD.begin(), in.pD.end());
         }
-        for (int j = in.ncrystal + 1; j <= nd; j++) {
-            long p = 1;
-            for (int q = 0; q < nd - j; q++) p *= 10;
-            idx[3 + j - in.ncrystal - 1] = (int)((el / p) % 10);
-        }
-        int k = (s - 1) * 4096 + idx[0] * 1024 + idx[1] * 256 + idx[2] * 64 + idx[3] * 16 + idx[4] * 4 + idx[5];
-        in.pE[k] = real_of(it[2]);
+        fclose(tf);
+    } else {
+        read_rate_block(r, in, true);
     }
-    for (int j = 0; j < in.ncrystal * 3; j++) {
-        it = r.items(3);
-        int s = atoi(it[0].c_str()), el = atoi(it[1].c_str());
-        if (s < 1 || s > in.ncrystal || el < 1 || el > 3) die("ERROR: 1st index in depo prob block must be <= NCrystal");
-        in.pD[(s - 1) * 3 + el - 1] = real_of(it[2]);
-    }
-    // absorption, then desorption: NCov*3 records "NCrystal+i  coor  rate"
-    // (SetProbability.f:117-140)
-    for (int blk = 0; blk < 2; blk++)
-        for (int j = 0; j < in.ncov * 3; j++) {
-            it = r.items(3);
-            int s = atoi(it[0].c_str()) - in.ncrystal, el = atoi(it[1].c_str());
-            if (s < 1 || s > in.ncov || el < 1 || el > 3) die("ERROR: index in absorption/desorption block");
-            (blk ? in.pDes : in.pAbs)[(s - 1) * 3 + el - 1] = real_of(it[2]);
-        }
     fclose(f);
     return in;
 }
@@ -279,7 +319,9 @@ int main()
                in.list_cov[2]);
         if (in.ncov > 1) die("ERR NOT IMPLEMENTED: the GPU engine holds one coverage species");
     }
-    if (in.init_st != "FS" && in.init_st != "F") die("initialization not_implemented");
+    const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "I" || in.init_st == "FF" ||
+                        in.init_st == "ST";
+    if (in.init_st != "FS" && in.init_st != "F" && !shaped) die("initialization not_implemented");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.lenx = lx;
@@ -296,8 +338,15 @@ int main()
     check(mks_create(&cfg, &h));
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
     if (in.ncov) check(mks_set_coverage_rates(h, in.pAbs.data(), in.pDes.data()));
-    int len1 = in.len[0] - in.len[0] % 24;
-    check(mks_init_flat(h, in.init_st == "FS" ? 'S' : 'C', len1));
+    if (shaped) {                                     // main.f:240-278
+        int32_t lens[4] = {in.len[0], in.len[1], in.len[2], in.len[3]};
+        check(mks_init_shape(h, in.init_st.c_str(), lens, in.st_par));
+    } else {
+        int len1 = in.len[0] - in.len[0] % 24;
+        check(mks_init_flat(h, in.init_st == "FS" ? 'S' : 'C', len1));
+    }
+    if (in.init_st == "ST")                           // rates from the table at each site's temperature
+        check(mks_batch_set_tabulated(h, (int32_t)in.st_T.size(), in.st_T.data(), in.st_E.data(), in.st_D.data()));
     mks_observables ob;
     check(mks_get_observables(h, &ob));
     printf(" Atoms,Voids,AdAtoms %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,

@@ -1,0 +1,98 @@
+"""The shaped initial lattices of the library (mks_init_shape: SetNC,
+SetNCSp, SetInvPOff, SetSiFINFET, SetTrenchSi) against the oracle's, which
+reproduce the reference's regression frames byte for byte (GPU): the
+compact lattice after initialization is identical, and mulskips.e run on the
+reference's own start.dat writes the reference's initial frame byte for
+byte."""
+import gzip
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+from test_oracle_st import write_st
+
+pytestmark = pytest.mark.gpu
+EXE = os.path.join(ROOT, "mulskips_gb300", "_lib", "mulskips.e")
+CASES = ["cube", "sphere", "inverted-pyramid", "finfet"]
+
+
+def _lens(d):
+    k, L = d["init_st"], d["len"]
+    return [L[0]] if k == "S" else ([L[0], L[1]] if k == "I" else list(L))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_shape_matches_oracle(oracle_lib, case):
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    start = os.path.join(GOLDEN, case, "start.dat")
+    d = parse_startdat(start)
+    o = oracle_lib.Oracle(start, 480, 480, 480)
+    o.init()
+    ref, off = oracle_lib.compact_state(o)
+    o.close()
+    assert off == 0
+    with Lattice(480, 480, 480, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"]) as lat:
+        lat.set_rates(d["ptransE"], d["ptransD"])
+        lat.init_shape(d["init_st"], _lens(d))
+        st = lat.state()
+    bad = np.argwhere(st != ref)
+    assert bad.size == 0, f"{len(bad)} sites differ, first {bad[:3]}"
+
+
+def test_trench_matches_oracle(oracle_lib, tmp_path):
+    from mulskips_gb300 import Lattice
+    rows = [(950, (3.0e2, 0.15, 0.002), (0.5, 0.5, 0.5)), (1300, (9.0e2, 0.6, 0.008), (0.6, 0.6, 0.6))]
+    p = write_st(str(tmp_path / "st"), 1250.0, 1000.0, rows, lens=(60, 60, 120, 70.0))
+    o = oracle_lib.Oracle(p, 480, 480, 480)
+    o.init()
+    ref, _ = oracle_lib.compact_state(o)
+    o.close()
+    with Lattice(480, 480, 480, sf=0.4525) as lat:
+        lat.init_shape("ST", [60, 60, 120], [70.0, 1250.0, 1000.0])
+        st = lat.state()
+    assert np.array_equal(st, ref)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mulskips_e_initial_frame(tmp_path, case):
+    d = tmp_path / case
+    d.mkdir()
+    txt = open(os.path.join(GOLDEN, case, "start.dat")).read()
+    out = []
+    for line in txt.splitlines():
+        if "! IterMax" in line:
+            line = "20000 ! IterMax"
+        elif "! OutMolMol" in line:
+            line = "20000 ! OutMolMol"
+        out.append(line)
+    (d / "start.dat").write_text("\n".join(out) + "\n")
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 480 480"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    with gzip.open(os.path.join(GOLDEN, case, "I00000000.xyz.gz"), "rb") as f:
+        gold = f.read()
+    assert (d / "I00000000.xyz").read_bytes() == gold
+    assert (d / "I00000001.xyz").exists()
+
+
+def test_mulskips_e_trench_with_tables(oracle_lib, tmp_path):
+    """InitSt ST through mulskips.e: the table file, SetTrenchSi and the
+    per-site interpolated rates; the initial frame equals the oracle's."""
+    rows = [(950, (3.0e2, 0.15, 0.002), (0.5, 0.5, 0.5)), (1100, (5.0e2, 0.3, 0.004), (0.55, 0.55, 0.55)),
+            (1300, (9.0e2, 0.6, 0.008), (0.6, 0.6, 0.6))]
+    d = tmp_path / "st"
+    p = write_st(str(d), 1250.0, 1000.0, rows, run_type="R", iters=200000)
+    o = oracle_lib.Oracle(p, 480, 480, 480, numbers=None)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 480 480"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+    hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
+    assert hdr[1] == "angstroem" and int(hdr[-1]) >= 200000
