@@ -299,6 +299,10 @@ int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field);
  * coordination passes.                                                      */
 int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const int32_t *lens, const double *params);
 int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params);
+/* SetCAD for InitSt IN (SetCAD.f:80-341): geo holds the LattGeo id of every
+ * grid point, int8 [z][y][x] (LenZ*LenY*LenX; 1 Si, 10 wall, 0 empty; the
+ * layers z <= 3 and >= LenZ-4 are walls whatever they hold).  NCrystal = 1. */
+int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo);
 /* Tabulated rates instead of fixed tables (InitSt ST: SetProbabilityFromField.f,
  * InterpProbFromField.f, Get_Prob.f:77-91): each site's rates are the
  * PtransE / PtransD tables at its own temperature, linear in T between the

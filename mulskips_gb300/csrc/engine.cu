@@ -2789,6 +2789,20 @@ int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const 
     return 0;
 }
 
+int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
+{
+    if (!h || !geo || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    if (r.cfg.ncrystal != 1) return fail(MKS_ERR_UNSUPPORTED, "SetCAD is built for NCrystal = 1");
+    mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
+    mks_shapes::set_cad(g, geo);
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
+    return upload_compact(h, rep, st);
+}
+
 int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params)
 {
     if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_init_shape needs a single-replica handle");

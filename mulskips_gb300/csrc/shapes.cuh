@@ -1,12 +1,12 @@
 // shapes.cuh — the reference's free-form initial lattices, built on the host
 // directly in the compact one-byte-per-diamond-site layout (lattice.cuh):
 // SetNC / SetNCSp (a 3C parallelepiped or ball), SetInvPOff (inverted
-// pyramids in a 3C layer), SetSiFINFET (Si between walls) and SetTrenchSi
-// (a Si trench under a temperature gradient).  Each writes occupancy,
-// species, walls and the coordinations of its closing passes; the list heads
-// and dummy flags of coor-1 sites follow from those (as Get_Prob_Ini finds
-// them).  Only diamond sites exist here: the walls' off-grid points never
-// neighbour a diamond site.
+// pyramids in a 3C layer), SetSiFINFET (Si between walls), SetTrenchSi (a Si
+// trench under a temperature gradient) and SetCAD (a geometry file).  Each
+// writes occupancy, species, walls and the coordinations of its closing
+// passes; the list heads and dummy flags of coor-1 sites follow from those
+// (as Get_Prob_Ini finds them).  Only diamond sites exist here: the walls'
+// off-grid points never neighbour a diamond site.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -208,6 +208,30 @@ inline void set_trench(Grid &g, int len, int len2, int len3, double angle, doubl
             }
     }
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
+}
+
+// SetCAD for InitSt IN (SetCAD.f:80-341, fresh start): walls at z = 0..3 and
+// LenZ-4..LenZ-1; from the geometry id of every grid point (geo[(z * LenY +
+// y) * LenX + x], z = 4..LenZ-5): 10 a wall, 1 Si on both sublattices; then
+// the coordination pass with the wall rules over the whole box.  The alloy
+// draw of SetCAD.f:215-222 uses the compiler's RAND stream and is not taken
+// (alloy fraction 0).
+inline void set_cad(Grid &g, const int8_t *geo)
+{
+    for (int z = 0; z < g.lz; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                uint8_t *v = g.at(x, y, z);
+                if (!v) continue;
+                if (z <= 3 || z >= g.lz - 4) {
+                    *v = WALL;
+                    continue;
+                }
+                int id = geo[((size_t)z * g.ly + y) * g.lx + x];
+                if (id == 10) *v = WALL;
+                else if (id == 1) *v = mks::mk(1, 0, 0, 0);
+            }
+    coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 0, g.lz - 1, true);
 }
 
 }  // namespace mks_shapes

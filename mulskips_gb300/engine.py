@@ -96,6 +96,12 @@ class Lattice:
         p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
         N.check(N.lib().mks_init_shape(self._h, init_st.encode(), N.ptr(l), None if p is None else N.ptr(p)))
 
+    def init_cad(self, geo):
+        """SetCAD (InitSt IN) from the LattGeo id of every grid point, [z, y, x]."""
+        g = np.ascontiguousarray(geo, dtype=np.int8)
+        assert g.size == self.dims[0] * self.dims[1] * self.dims[2]
+        N.check(N.lib().mks_batch_init_cad(self._h, 0, N.ptr(g)))
+
     def replay(self, events):
         ev = np.ascontiguousarray(events, dtype=N.EVENT_DTYPE)
         N.check(N.lib().mks_replay(self._h, N.ptr(ev), int(ev.size)))

@@ -49,6 +49,7 @@ struct Input {
     std::vector<double> pDes = std::vector<double>(9, 0.0);
     // InitSt ST: angle, Ttop, Tbottom and the probability table rows
     double st_par[3] = {0, 0, 0};
+    std::string cad_file;                 // InitSt IN: the LattGeo file
     std::vector<int> st_T;
     std::vector<double> st_E, st_D;
 };
@@ -183,8 +184,12 @@ Input read_startdat(const char *path)
         for (int i = 0; i < 3; i++) in.st_par[i] = real_of(it[3 + i]);
         printf(" Temperature on top in Kelvin: %.17g\n", in.st_par[1]);
         printf(" Temperature on bottom in Kelvin: %.17g\n", in.st_par[2]);
-    } else if (in.init_st == "IN" || in.init_st == "SH" || in.init_st == "LA") {
-        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF and ST are)");
+    } else if (in.init_st == "IN") {                  // main.f:116-117
+        if (!r.line(in.cad_file)) die("start.dat: missing geometry file name");
+        while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.back())) in.cad_file.pop_back();
+        while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.front())) in.cad_file.erase(in.cad_file.begin());
+    } else if (in.init_st == "SH" || in.init_st == "LA") {
+        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF, ST and IN are)");
     } else {
         it = r.items(3);
         for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
@@ -321,7 +326,8 @@ int main()
     }
     const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "I" || in.init_st == "FF" ||
                         in.init_st == "ST";
-    if (in.init_st != "FS" && in.init_st != "F" && !shaped) die("initialization not_implemented");
+    if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "IN" && !shaped)
+        die("initialization not_implemented");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.lenx = lx;
@@ -338,7 +344,28 @@ int main()
     check(mks_create(&cfg, &h));
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
     if (in.ncov) check(mks_set_coverage_rates(h, in.pAbs.data(), in.pDes.data()));
-    if (shaped) {                                     // main.f:240-278
+    if (in.init_st == "IN") {                         // SetCAD.f:155-236: one record per layer z
+        printf(" Reading input geometry file: %s\n", in.cad_file.c_str());
+        FILE *gf = fopen(in.cad_file.c_str(), "r");
+        if (!gf) die("cannot open the geometry file");
+        std::vector<int8_t> geo((size_t)lx * ly * lz, 0);
+        std::vector<char> line((size_t)lx * ly * 24 + 4096);
+        for (int z = 0; z < lz - 4; z++) {          // the last four layers are walls
+            if (!fgets(line.data(), (int)line.size(), gf)) die("geometry file: too few records");
+            // list-directed READ of LenX*LenY values: the rest of the record is skipped
+            char *p = line.data();
+            for (size_t k = 0; k < (size_t)lx * ly; k++) {
+                char *e;
+                double v = strtod(p, &e);
+                if (e == p) die("geometry file: short record");
+                geo[(size_t)z * lx * ly + k] = (int8_t)v;
+                p = e;
+            }
+        }
+        fclose(gf);
+        printf(" Done reading input geometry file\n");
+        check(mks_batch_init_cad(h, 0, geo.data()));
+    } else if (shaped) {                              // main.f:240-278
         int32_t lens[4] = {in.len[0], in.len[1], in.len[2], in.len[3]};
         check(mks_init_shape(h, in.init_st.c_str(), lens, in.st_par));
     } else {

@@ -63,6 +63,7 @@ def lib():
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_set_la_input.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ora_set_geometry.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_la_alloy.argtypes = [C.c_void_p, C.c_double, C.c_uint64]
         L.ora_la_set.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_uint64]
@@ -112,6 +113,13 @@ class Oracle:
         if r < 0:
             raise RuntimeError(lib().ora_last_error().decode())
         return r
+
+    def set_geometry(self, geo):
+        """InitSt IN input (see ora_set_geometry): LattGeo id of every grid point, [z, y, x]."""
+        g = np.ascontiguousarray(geo, dtype=np.int8)
+        self._geo = g
+        if lib().ora_set_geometry(self._h, g.ctypes.data_as(C.c_void_p)):
+            raise RuntimeError(lib().ora_last_error().decode())
 
     def set_la_input(self, geo, tsub):
         """InitSt LA input (see ora_set_la_input): layer ids and 3-grid temperatures."""

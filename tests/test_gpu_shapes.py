@@ -96,3 +96,57 @@ def test_mulskips_e_trench_with_tables(oracle_lib, tmp_path):
     assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
     hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
     assert hdr[1] == "angstroem" and int(hdr[-1]) >= 200000
+
+
+def _cad_geometry():
+    return np.load(os.path.join(GOLDEN, "CAD", "geo.npz"))["g"].astype(np.int8)
+
+
+def test_cad_matches_oracle(oracle_lib, tmp_path):
+    """SetCAD (InitSt IN) on the reference's CAD geometry, as the current
+    SetCAD.f reads it (record z to layer z)."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    start = os.path.join(GOLDEN, "CAD", "start.dat")
+    d = parse_startdat(start)
+    geo = _cad_geometry()
+    o = oracle_lib.Oracle(start, 480, 240, 240)
+    o.set_geometry(geo)
+    o.init()
+    ref, _ = oracle_lib.compact_state(o)
+    o.close()
+    with Lattice(480, 240, 240, sf=d["sf"], list_cov=d["list_cov"]) as lat:
+        lat.init_cad(geo)
+        st = lat.state()
+    bad = np.argwhere(st != ref)
+    assert bad.size == 0, f"{len(bad)} sites differ, first {bad[:3]}"
+
+
+def test_mulskips_e_cad(oracle_lib, tmp_path):
+    """mulskips.e with the CAD start.dat (one coverage species) and its
+    geometry file: the initial frame equals the oracle's."""
+    geo = _cad_geometry()
+    d = tmp_path / "cad"
+    d.mkdir()
+    with open(d / "LattGeo.dat", "w") as f:
+        for z in range(geo.shape[0]):
+            f.write(" ".join(map(str, geo[z].reshape(-1).tolist())) + "\n")
+    out = []
+    for line in open(os.path.join(GOLDEN, "CAD", "start.dat")).read().splitlines():
+        if "LattGeo" in line:
+            line = "LattGeo.dat"
+        elif "! IterMax" in line:
+            line = "20000 ! IterMax"
+        elif "! OutMolMol" in line:
+            line = "20000 ! OutMolMol"
+        out.append(line)
+    (d / "start.dat").write_text("\n".join(out) + "\n")
+    o = oracle_lib.Oracle(str(d / "start.dat"), 480, 240, 240)
+    o.set_geometry(geo)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 240 240"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
