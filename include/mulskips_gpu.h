@@ -303,6 +303,12 @@ int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, cons
  * grid point, int8 [z][y][x] (LenZ*LenY*LenX; 1 Si, 10 wall, 0 empty; the
  * layers z <= 3 and >= LenZ-4 are walls whatever they hold).  NCrystal = 1. */
 int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo);
+/* The same for InitSt LA (SetCAD.f:166-212, fresh start): homogeneous 1
+ * keeps the Si sites at z <= LenZ - INT((LenVac + LenNuc)/sf), 0 those
+ * outside the nucleus ball of radius LenNuc/sf around (LenX/2, LenY/2,
+ * LenZ - INT(LenVac/sf)); lengths in Angstrom.  -1 is InitSt IN.          */
+int mks_batch_init_cad_la(mks_handle *h, int32_t rep, const int8_t *geo, int32_t homogeneous, double len_vac,
+                          double len_nuc);
 /* Tabulated rates instead of fixed tables (InitSt ST: SetProbabilityFromField.f,
  * InterpProbFromField.f, Get_Prob.f:77-91): each site's rates are the
  * PtransE / PtransD tables at its own temperature, linear in T between the

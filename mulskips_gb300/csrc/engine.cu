@@ -2789,18 +2789,30 @@ int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const 
     return 0;
 }
 
-int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
+int mks_batch_init_cad_la(mks_handle *h, int32_t rep, const int8_t *geo, int32_t homogeneous, double len_vac,
+                          double len_nuc)
 {
     if (!h || !geo || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[rep];
     if (r.cfg.ncrystal != 1) return fail(MKS_ERR_UNSUPPORTED, "SetCAD is built for NCrystal = 1");
     mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
-    mks_shapes::set_cad(g, geo);
+    mks_shapes::CadLA la;
+    la.on = homogeneous >= 0;
+    la.homogeneous = homogeneous > 0;
+    la.len_vac = len_vac;
+    la.len_nuc = len_nuc;
+    la.sf = r.cfg.sf;
+    mks_shapes::set_cad(g, geo, la);
     std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
     for (int z1 = 0; z1 < r.NZ; z1++)
         for (int b = 0; b < r.NB; b++)
             memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
     return upload_compact(h, rep, st);
+}
+
+int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
+{
+    return mks_batch_init_cad_la(h, rep, geo, -1, 0.0, 0.0);
 }
 
 int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params)

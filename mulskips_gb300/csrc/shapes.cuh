@@ -216,8 +216,19 @@ inline void set_trench(Grid &g, int len, int len2, int len3, double angle, doubl
 // the coordination pass with the wall rules over the whole box.  The alloy
 // draw of SetCAD.f:215-222 uses the compiler's RAND stream and is not taken
 // (alloy fraction 0).
-inline void set_cad(Grid &g, const int8_t *geo)
+// With la, the Si sites of InitSt LA (SetCAD.f:166-212): kept below
+// LenZ - INT((LenVac + LenNuc)/sf) when homogeneous, else outside the ball of
+// radius LenNuc/sf around (LenX/2, LenY/2, LenZ - INT(LenVac/sf)).
+struct CadLA {
+    bool on = false, homogeneous = true;
+    double len_vac = 0.0, len_nuc = 0.0, sf = 1.0;
+};
+
+inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA())
 {
+    const int zmax = g.lz - (int)((la.len_vac + la.len_nuc) / la.sf);
+    const int x0 = g.lx / 2, y0 = g.ly / 2, z0 = g.lz - (int)(la.len_vac / la.sf);
+    const long r2 = (long)((la.len_nuc / la.sf) * (la.len_nuc / la.sf));
     for (int z = 0; z < g.lz; z++)
         for (int y = 0; y < g.ly; y++)
             for (int x = 0; x < g.lx; x++) {
@@ -228,8 +239,18 @@ inline void set_cad(Grid &g, const int8_t *geo)
                     continue;
                 }
                 int id = geo[((size_t)z * g.ly + y) * g.lx + x];
-                if (id == 10) *v = WALL;
-                else if (id == 1) *v = mks::mk(1, 0, 0, 0);
+                if (id == 10) {
+                    *v = WALL;
+                } else if (id == 1) {
+                    bool occ = true;
+                    if (la.on && la.homogeneous) {
+                        occ = z <= zmax;
+                    } else if (la.on) {
+                        long d2 = (long)(x - x0) * (x - x0) + (long)(y - y0) * (y - y0) + (long)(z - z0) * (z - z0);
+                        occ = d2 > r2;
+                    }
+                    if (occ) *v = mks::mk(1, 0, 0, 0);
+                }
             }
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 0, g.lz - 1, true);
 }

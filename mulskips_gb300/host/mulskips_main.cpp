@@ -49,7 +49,10 @@ struct Input {
     std::vector<double> pDes = std::vector<double>(9, 0.0);
     // InitSt ST: angle, Ttop, Tbottom and the probability table rows
     double st_par[3] = {0, 0, 0};
-    std::string cad_file;                 // InitSt IN: the LattGeo file
+    std::string cad_file;                 // InitSt IN / LA: the LattGeo file
+    std::string temp_file;                // InitSt LA: the TempStat file
+    double Tm = 0, P0 = 0, sigma = 1, Tflex = 0, len_vac = 0, len_nuc = 0;
+    bool homogeneous = true;
     std::vector<int> st_T;
     std::vector<double> st_E, st_D;
 };
@@ -188,8 +191,26 @@ Input read_startdat(const char *path)
         if (!r.line(in.cad_file)) die("start.dat: missing geometry file name");
         while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.back())) in.cad_file.pop_back();
         while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.front())) in.cad_file.erase(in.cad_file.begin());
-    } else if (in.init_st == "SH" || in.init_st == "LA") {
-        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF, ST and IN are)");
+    } else if (in.init_st == "LA") {                  // main.f:118-138
+        printf(" ****** MulSKIPs run for laser annealing ******\n");
+        if (in.ncov > 0) die("ERR NOT IMPLEMENTED: NCov=0 for LA");
+        auto trimmed = [&](std::string &s) {
+            if (!r.line(s)) die("start.dat: missing LA file name");
+            while (!s.empty() && isspace((unsigned char)s.back())) s.pop_back();
+            while (!s.empty() && isspace((unsigned char)s.front())) s.erase(s.begin());
+        };
+        trimmed(in.cad_file);
+        trimmed(in.temp_file);
+        in.Tm = real_of(r.items(1)[0]);
+        in.P0 = real_of(r.items(1)[0]);
+        in.sigma = real_of(r.items(1)[0]);
+        in.Tflex = real_of(r.items(1)[0]);
+        in.len_vac = real_of(r.items(1)[0]);
+        in.len_nuc = real_of(r.items(1)[0]);
+        in.homogeneous = r.items(1)[0].substr(0, 1) == "T";
+        printf(" Melting temperature in Kelvin: %.17g\n", in.Tm);
+    } else if (in.init_st == "SH") {
+        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF, ST, IN and LA are)");
     } else {
         it = r.items(3);
         for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
@@ -213,6 +234,7 @@ Input read_startdat(const char *path)
     if (in.save_final == "T") r.line(in.restart_file);
     in.save_coo = r.items(1)[0].substr(0, 2);
     if (in.save_coo == "T") r.line(in.coo_file);
+    else if (in.init_st == "LA") die("ERR: SaveCoo flag must be \"T\" for LA simulations!");   // main.f:204-208
     if (in.init_st == "ST") {
         // SetProbabilityFromField.f:23-171: the table file named on the next
         // line: ntemp, nprob, then per temperature its value and one block
@@ -326,7 +348,7 @@ int main()
     }
     const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "I" || in.init_st == "FF" ||
                         in.init_st == "ST";
-    if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "IN" && !shaped)
+    if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "IN" && in.init_st != "LA" && !shaped)
         die("initialization not_implemented");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
@@ -344,7 +366,30 @@ int main()
     check(mks_create(&cfg, &h));
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
     if (in.ncov) check(mks_set_coverage_rates(h, in.pAbs.data(), in.pDes.data()));
-    if (in.init_st == "IN") {                         // SetCAD.f:155-236: one record per layer z
+    double la_tmax = 0.0;
+    if (in.init_st == "LA") {                         // SetT (SetT.f:25-50): TempStat, one record per layer
+        FILE *tf = fopen(in.temp_file.c_str(), "r");
+        if (!tf) die("cannot open the temperature file");
+        std::vector<int32_t> field((size_t)lx * ly * lz, 10);
+        std::vector<char> line((size_t)lx * ly * 32 + 4096);
+        for (int z = 0; z < lz; z++) {
+            if (!fgets(line.data(), (int)line.size(), tf)) die("temperature file: too few records");
+            char *p = line.data();
+            for (int y = 0; y < ly; y++)
+                for (int x = 0; x < lx; x++) {
+                    char *e;
+                    double v = strtod(p, &e);
+                    if (e == p) die("temperature file: short record");
+                    p = e;
+                    int t = (int)v;                   // INT(LenIn)
+                    field[(size_t)z + (size_t)lz * ((size_t)x + (size_t)lx * y)] = t;
+                    if (t != 10) la_tmax = std::max(la_tmax, (double)t);
+                }
+        }
+        fclose(tf);
+        check(mks_batch_set_field(h, 0, field.data()));
+    }
+    if (in.init_st == "IN" || in.init_st == "LA") {   // SetCAD.f:155-236: one record per layer z
         printf(" Reading input geometry file: %s\n", in.cad_file.c_str());
         FILE *gf = fopen(in.cad_file.c_str(), "r");
         if (!gf) die("cannot open the geometry file");
@@ -364,7 +409,10 @@ int main()
         }
         fclose(gf);
         printf(" Done reading input geometry file\n");
-        check(mks_batch_init_cad(h, 0, geo.data()));
+        if (in.init_st == "LA")
+            check(mks_batch_init_cad_la(h, 0, geo.data(), in.homogeneous ? 1 : 0, in.len_vac, in.len_nuc));
+        else
+            check(mks_batch_init_cad(h, 0, geo.data()));
     } else if (shaped) {                              // main.f:240-278
         int32_t lens[4] = {in.len[0], in.len[1], in.len[2], in.len[3]};
         check(mks_init_shape(h, in.init_st.c_str(), lens, in.st_par));
@@ -374,6 +422,44 @@ int main()
     }
     if (in.init_st == "ST")                           // rates from the table at each site's temperature
         check(mks_batch_set_tabulated(h, (int32_t)in.st_T.size(), in.st_T.data(), in.st_E.data(), in.st_D.data()));
+    if (in.init_st == "LA") {                         // the law of Get_Prob.f:127-149 on the static field
+        mks_la_params lp;
+        memset(&lp, 0, sizeof lp);
+        for (int s = 0; s < 3; s++) {
+            lp.P0[s] = s == 0 ? (float)in.P0 : 0.f;
+            lp.Tm[s] = (float)in.Tm;
+            lp.Tflex[s] = (float)in.Tflex;
+            lp.sigma[s] = (float)in.sigma;
+        }
+        lp.w = 1.f;
+        lp.L_nm = 1e30f;
+        lp.zsurf = 1e30f;
+        lp.score = 0;
+        lp.liquid_weighting = 0;
+        check(mks_batch_set_la(h, &lp, nullptr, nullptr));
+    }
+    // LA: the window follows the class with the largest share of the rate at
+    // the field's hottest temperature (PtransE / PtransD are barriers in eV)
+    auto la_tau = [&]() {
+        const double kb = 0.00008617330350;           // Get_Prob.f:70
+        int64_t hist[64] = {0};
+        check(mks_class_histogram(h, hist, 63));
+        double rate[64] = {0};
+        double fe = 0.5 * (1.0 + erf((la_tmax - in.Tflex) / in.sigma));
+        const int dep_cls[3] = {1, 3, 4}, occ_cls[3] = {6, 9, 15};   // C1, C2, C3; census 1, 2, 3
+        for (int n = 1; n <= 3; n++) {
+            double d = in.pD[n - 1], e = in.pE[n * 1024];
+            rate[dep_cls[n - 1]] = d != 0.0 ? in.P0 * exp(-d / (kb * in.Tm)) * fe : 0.0;
+            rate[occ_cls[n - 1]] = e != 0.0 ? in.P0 * exp(-e / (kb * la_tmax)) : 0.0;
+        }
+        double best = 0.0, rs = 0.0;
+        for (int c = 0; c < 63; c++)
+            if ((double)hist[c] * rate[c] > best) {
+                best = (double)hist[c] * rate[c];
+                rs = rate[c];
+            }
+        return rs > 0.0 ? 0.3 / rs : 1e-12;
+    };
     mks_observables ob;
     check(mks_get_observables(h, &ob));
     printf(" Atoms,Voids,AdAtoms %lld %lld %lld\n", (long long)(ob.atoms - ob.undercoord), (long long)ob.voids,
@@ -389,9 +475,21 @@ int main()
         // window factor validated against the serial reference: 0.3 for one
         // crystal species (with or without a coverage species), 0.03 for two
         // or three (fast desorption across tile borders)
-        if (block % 4 == 0) check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
+        if (block % 4 == 0) {
+            if (in.init_st == "LA") tau = la_tau();
+            else check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
+        }
+        // Iter mode: the chunk ends at the window that reaches the next
+        // output multiple or IterMax, so frames land just past each multiple
+        // (one window's events at most) instead of a whole chunk later
+        int64_t cap = 0;
+        if (iter_mode) {
+            long long next = in.max_iter;
+            if (in.out_molmol > 0) next = std::min(next, (frame + 1) * in.out_molmol);
+            cap = next > events ? next - events : 1;
+        }
         int64_t ev = 0;
-        check(mks_run(h, tau, chunk, 0, 0.0, &ev, &time));
+        check(mks_run(h, tau, chunk, cap, 0.0, &ev, &time));
         events += ev;
         mks_status st;
         check(mks_get_status(h, &st));
@@ -422,8 +520,10 @@ int main()
             if (time > in.max_time) break;
         }
     }
+    // main.f:374-377 numbers the final frame Iter/OutMolMol; the reference
+    // stops at IterMax exactly, the window that crosses it may overshoot
     if (iter_mode)
-        fr.write(time, events, in.out_molmol > 0 ? events / in.out_molmol : 0);
+        fr.write(time, events, in.out_molmol > 0 ? std::min(events, in.max_iter) / in.out_molmol : 0);
     else
         fr.write(time, events, frame);
     check(mks_get_observables(h, &ob));

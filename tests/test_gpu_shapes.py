@@ -65,9 +65,9 @@ def test_mulskips_e_initial_frame(tmp_path, case):
     out = []
     for line in txt.splitlines():
         if "! IterMax" in line:
-            line = "20000 ! IterMax"
+            line = "4000 ! IterMax"
         elif "! OutMolMol" in line:
-            line = "20000 ! OutMolMol"
+            line = "4000 ! OutMolMol"
         out.append(line)
     (d / "start.dat").write_text("\n".join(out) + "\n")
     r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 480 480"), stdout=subprocess.PIPE,
@@ -136,9 +136,9 @@ def test_mulskips_e_cad(oracle_lib, tmp_path):
         if "LattGeo" in line:
             line = "LattGeo.dat"
         elif "! IterMax" in line:
-            line = "20000 ! IterMax"
+            line = "4000 ! IterMax"
         elif "! OutMolMol" in line:
-            line = "20000 ! OutMolMol"
+            line = "4000 ! OutMolMol"
         out.append(line)
     (d / "start.dat").write_text("\n".join(out) + "\n")
     o = oracle_lib.Oracle(str(d / "start.dat"), 480, 240, 240)
@@ -150,3 +150,56 @@ def test_mulskips_e_cad(oracle_lib, tmp_path):
                        stderr=subprocess.STDOUT, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-3000:]
     assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+
+
+def test_mulskips_e_la(oracle_lib, tmp_path):
+    """InitSt LA through mulskips.e (main.f:118-138, 287-291): TempStat and
+    LattGeo files, SetT + SetCAD with a molten nucleus, the law of
+    Get_Prob.f:127-149 on the static field.  A 120^3 box with the LA
+    regression's rates and parameters (nucleus radius 20 A): the initial
+    frame equals the oracle's, and the run writes the LA phases file.  The
+    run is capped at 4000 events: the nucleus solidifies to the upper wall
+    within about 13000, after which the reference stops on too few MC sites
+    and its final frame (index 0) would overwrite I00000000."""
+    L = 120
+    d = tmp_path / "la"
+    d.mkdir()
+    layers = np.where(np.arange(L) < 100, 1, 10).astype(np.int8)
+    layers[:4] = 10
+    T = np.where(layers == 10, 10, (1650 + 0.1 * np.arange(L)).astype(np.int64))
+    with open(d / "LattGeo.dat", "w") as fg, open(d / "TempStat.dat", "w") as ft:
+        for z in range(L):
+            fg.write(" ".join([str(int(layers[z]))] * (L * L)) + "\n")
+            ft.write(" ".join([str(int(T[z]))] * (L * L)) + "\n")
+    out, skip = [], False
+    for line in open(os.path.join(GOLDEN, "LA", "start.dat")).read().splitlines():
+        if skip:
+            skip = False
+            continue
+        if line.startswith("LattGeo"):
+            line = "LattGeo.dat"
+        elif line.startswith("TempStat"):
+            line = "TempStat.dat"
+        elif "! LenNuc" in line:
+            line = "20.0 ! LenNuc"
+        elif "! IterMax" in line:
+            line = "4000 ! IterMax"
+        elif "! OutMolMol" in line:
+            line = "4000 ! OutMolMol"
+        elif "! Save final state" in line:
+            line, skip = "F ! Save final state", True
+        out.append(line)
+    (d / "start.dat").write_text("\n".join(out) + "\n")
+    tsub = np.broadcast_to(T[::3, None, None], (L // 3, L // 3, L // 3)).astype(np.int16)
+    o = oracle_lib.Oracle(str(d / "start.dat"), L, L, L)
+    o.set_la_input(layers, np.ascontiguousarray(tsub))
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX=f"{L} {L} {L}"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+    hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
+    assert int(hdr[-1]) >= 4000
+    assert len(open(d / "LattStat.dat").read().splitlines()) == L
