@@ -303,6 +303,19 @@ int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, cons
  * grid point, int8 [z][y][x] (LenZ*LenY*LenX; 1 Si, 10 wall, 0 empty; the
  * layers z <= 3 and >= LenZ-4 are walls whatever they hold).  NCrystal = 1. */
 int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo);
+/* SetShape for InitSt SH (SetShape.f:25-436): n grid points xyz[3*i..3*i+2]
+ * = (x, y, z), 0 <= x < LenX, 0 <= y < LenY, 0 <= z <= LenZ, with
+ * species[i] 1 (Si) or 2 (C / Ge); the points of the reference's point-list
+ * file (sym x y z records).  Points with z <= 3 or z >= LenZ-4 are walls
+ * (their species is not read), every other one an atom on a diamond site.
+ * The coordinations, MC / bulk split and first list entries are those of
+ * SetShape.f's shell scan and ad-void pass.  MKS_ERR_UNSUPPORTED for the
+ * inputs the reference leaves undefined (an atom with fewer than two
+ * neighbours, a reciprocity check reaching a wall, a vacancy with four MC
+ * neighbours) and for an atom off the diamond sites or next to an off-site
+ * wall point.                                                              */
+int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const int8_t *species, int64_t n);
+int mks_init_points(mks_handle *h, const int32_t *xyz, const int8_t *species, int64_t n);
 /* The same for InitSt LA (SetCAD.f:166-212, fresh start): homogeneous 1
  * keeps the Si sites at z <= LenZ - INT((LenVac + LenNuc)/sf), 0 those
  * outside the nucleus ball of radius LenNuc/sf around (LenX/2, LenY/2,

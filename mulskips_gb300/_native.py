@@ -104,6 +104,8 @@ SIGNATURES = {
     "mks_batch_init_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_void_p, C.c_void_p]),
     "mks_init_shape": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p]),
     "mks_batch_init_cad": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mks_batch_init_points": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64]),
+    "mks_init_points": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_batch_init_cad_la": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_double]),
     "mks_batch_set_tabulated": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mks_batch_get_phases": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

@@ -2815,6 +2815,28 @@ int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
     return mks_batch_init_cad_la(h, rep, geo, -1, 0.0, 0.0);
 }
 
+int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const int8_t *species, int64_t n)
+{
+    if (!h || n < 0 || (n && (!xyz || !species)) || rep < 0 || rep >= (int)h->reps.size())
+        return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    for (int64_t i = 0; i < n; i++)
+        if (species[i] > r.cfg.ncrystal) return fail(MKS_ERR_ARG, "point %lld: species %d > NCrystal", (long long)i, species[i]);
+    mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
+    if (const char *e = mks_shapes::set_points(g, xyz, species, n)) return fail(MKS_ERR_UNSUPPORTED, "SetShape: %s", e);
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
+    return upload_compact(h, rep, st);
+}
+
+int mks_init_points(mks_handle *h, const int32_t *xyz, const int8_t *species, int64_t n)
+{
+    if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_init_points needs a single-replica handle");
+    return mks_batch_init_points(h, 0, xyz, species, n);
+}
+
 int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params)
 {
     if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_init_shape needs a single-replica handle");

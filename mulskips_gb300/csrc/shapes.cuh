@@ -255,4 +255,91 @@ inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA())
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 0, g.lz - 1, true);
 }
 
+// SetShape (SetShape.f:25-436, InitSt SH): grid points (x, y, z) with
+// species 1 (Si) or 2 (C or Ge), n of them.  A point with z <= 3 or
+// z >= LenZ-4 is a wall (:58-62), any other an atom, which must sit on a
+// diamond site.  An atom's coordination counts its occupied neighbours,
+// walls included, and its first list entry is the first of them in the
+// reference's shell scan, dz then dy then dx ascending (:87-131); with
+// coordination <= 3 it is an MC particle.  An empty site counts its MC
+// neighbours only, and its first list entry is the first of those in z, y, x
+// order, the order of the MC list (:378-431).  Returns nullptr, or what in
+// the input the reference leaves undefined or this lattice cannot hold: an
+// atom off the diamond sites or next to an off-site wall point, an atom with
+// fewer than two neighbours, an MC particle next to a wall or a bulk atom
+// above z = 12 next to one (the reference's reciprocity checks, :277-373,
+// then read the list entry 0), an empty site with four MC neighbours.
+inline const char *set_points(Grid &g, const int32_t *xyz, const int8_t *sp, int64_t n)
+{
+    std::vector<int64_t> offsite;
+    for (int64_t i = 0; i < n; i++) {
+        const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        if (x < 0 || x >= g.lx || y < 0 || y >= g.ly || z < 0 || z > g.lz) return "a point outside the box";
+        uint8_t *v = g.at(x, y, z);
+        if (z <= 3 || z >= g.lz - 4) {
+            if (v) *v = WALL;
+            else offsite.push_back(i);
+            continue;
+        }
+        if (!v) return "an atom off the diamond sites";
+        if (sp[i] != 1 && sp[i] != 2) return "an atom symbol other than Si, C or Ge";
+        *v = mks::mk(mks::sp_of(*v) | sp[i], 0, 0, 0);
+    }
+    // an off-site wall point within an atom's |d|^2 = 27 shell would count as
+    // a neighbour the one-byte lattice cannot list
+    for (int64_t i : offsite)
+        for (int k = -5; k <= 5; k++)
+            for (int j = -5; j <= 5; j++)
+                for (int l = -5; l <= 5; l++) {
+                    if (l * l + j * j + k * k != 27) continue;
+                    const int z = xyz[3 * i + 2] + k;
+                    if (z < 4 || z > g.lz - 5) continue;
+                    uint8_t *v = g.at(((xyz[3 * i] + l) % g.lx + g.lx) % g.lx, ((xyz[3 * i + 1] + j) % g.ly + g.ly) % g.ly, z);
+                    if (v && *v != WALL && occupied(*v)) return "an atom next to an off-site wall point";
+                }
+    auto is_atom = [](uint8_t v) { return v != WALL && (v & 3) != 0; };
+    for (int z1 = 0; z1 < g.NZ; z1++)
+        for (int b = 0; b < g.NB; b++)
+            for (int a = 0; a < g.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                uint8_t &v = g.st[((size_t)z1 * g.NB + b) * g.NA + a];
+                if (!is_atom(v)) continue;
+                int coor = 0, first = -1, best = 1 << 30;
+                bool wall = false;
+                for (int d = 0; d < 4; d++) {
+                    uint8_t *w = g.nb(a, b, z1, d);
+                    if (!w || !occupied(*w)) continue;
+                    int da, db, dz;
+                    mks::nb_off(z1 & 1, d, da, db, dz);
+                    const int par = ((z1 + dz) & 1) - (z1 & 1);
+                    const int ox = 3 * (2 * da + par), oy = 3 * (2 * db + par), oz = 3 * dz;
+                    const int key = ((oz + 6) * 13 + oy + 6) * 13 + ox + 6;
+                    if (key < best) {
+                        best = key;
+                        first = d;
+                    }
+                    coor++;
+                    wall |= *w == WALL;
+                }
+                if (coor < 2) return "an atom with fewer than two neighbours";
+                if (wall && (coor <= 3 || 3 * z1 >= 13)) return "a reciprocity check that meets a wall";
+                v = mks::mk(mks::sp_of(v), coor, first, 0);
+            }
+    for (int z1 = 0; z1 < g.NZ; z1++)
+        for (int b = 0; b < g.NB; b++)
+            for (int a = 0; a < g.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                const uint8_t v = g.st[((size_t)z1 * g.NB + b) * g.NA + a];
+                if (!is_atom(v) || mks::co_of(v) > 3) continue;
+                for (int d = 0; d < 4; d++) {
+                    uint8_t *w = g.nb(a, b, z1, d);
+                    if (!w || occupied(*w)) continue;
+                    const int c = mks::co_of(*w);
+                    if (c == 3) return "an empty site with four MC neighbours";
+                    *w = mks::mk(0, c + 1, c == 0 ? mks::rev_dir(d) : mks::fd_of(*w), 0);
+                }
+            }
+    return nullptr;
+}
+
 }  // namespace mks_shapes

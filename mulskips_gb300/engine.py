@@ -102,6 +102,14 @@ class Lattice:
         assert g.size == self.dims[0] * self.dims[1] * self.dims[2]
         N.check(N.lib().mks_batch_init_cad(self._h, 0, N.ptr(g)))
 
+    def init_points(self, xyz, species):
+        """SetShape (InitSt SH) from grid points xyz [n, 3] with species 1 (Si)
+        or 2 (C / Ge); startdat.read_shape_points reads the reference's file."""
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        sp = np.ascontiguousarray(species, dtype=np.int8).reshape(-1)
+        assert sp.size == p.shape[0]
+        N.check(N.lib().mks_init_points(self._h, N.ptr(p), N.ptr(sp), int(sp.size)))
+
     def replay(self, events):
         ev = np.ascontiguousarray(events, dtype=N.EVENT_DTYPE)
         N.check(N.lib().mks_replay(self._h, N.ptr(ev), int(ev.size)))

@@ -187,7 +187,7 @@ Input read_startdat(const char *path)
         for (int i = 0; i < 3; i++) in.st_par[i] = real_of(it[3 + i]);
         printf(" Temperature on top in Kelvin: %.17g\n", in.st_par[1]);
         printf(" Temperature on bottom in Kelvin: %.17g\n", in.st_par[2]);
-    } else if (in.init_st == "IN") {                  // main.f:116-117
+    } else if (in.init_st == "IN" || in.init_st == "SH") {   // main.f:116-117
         if (!r.line(in.cad_file)) die("start.dat: missing geometry file name");
         while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.back())) in.cad_file.pop_back();
         while (!in.cad_file.empty() && isspace((unsigned char)in.cad_file.front())) in.cad_file.erase(in.cad_file.begin());
@@ -209,8 +209,6 @@ Input read_startdat(const char *path)
         in.len_nuc = real_of(r.items(1)[0]);
         in.homogeneous = r.items(1)[0].substr(0, 1) == "T";
         printf(" Melting temperature in Kelvin: %.17g\n", in.Tm);
-    } else if (in.init_st == "SH") {
-        die("initialization not_implemented in the GPU engine (FS, F, C, S, I, FF, ST, IN and LA are)");
     } else {
         it = r.items(3);
         for (int i = 0; i < 3; i++) in.len[i] = atoi(it[i].c_str());
@@ -348,8 +346,11 @@ int main()
     }
     const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "I" || in.init_st == "FF" ||
                         in.init_st == "ST";
-    if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "IN" && in.init_st != "LA" && !shaped)
-        die("initialization not_implemented");
+    if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "SG" && in.init_st != "IN" && in.init_st != "LA" &&
+        in.init_st != "SH" && !shaped)
+        die("initialization not_implemented in the GPU engine (FS, F, SG, C, S, I, FF, ST, IN, SH and LA are)");
+    if (in.alloy > 0.0 && (in.init_st == "IN" || in.init_st == "LA"))
+        die("ERR: SetCAD with an alloy fraction > 0 is not built (it draws the species from the compiler's RAND)");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.lenx = lx;
@@ -413,6 +414,29 @@ int main()
             check(mks_batch_init_cad_la(h, 0, geo.data(), in.homogeneous ? 1 : 0, in.len_vac, in.len_nuc));
         else
             check(mks_batch_init_cad(h, 0, geo.data()));
+    } else if (in.init_st == "SH") {                  // main.f:281-286, SetShape.f:52-79
+        printf(" Reading input geometry file (SHAPE): %s\n", in.cad_file.c_str());
+        FILE *sf = fopen(in.cad_file.c_str(), "r");
+        if (!sf) die("cannot open the shape file");
+        Records pr(sf);
+        long long nfilled = atoll(pr.items(1)[0].c_str());
+        std::string skip;
+        if (nfilled < 0 || !pr.line(skip)) die("shape file: bad header");
+        std::vector<int32_t> xyz((size_t)nfilled * 3);
+        std::vector<int8_t> sp((size_t)nfilled);
+        for (long long i = 0; i < nfilled; i++) {
+            auto t = pr.items(4);
+            std::string sym = t[0].substr(0, 2);
+            sp[i] = sym == "Si" ? 1 : (sym == "C" || sym == "Ge") ? 2 : 0;
+            for (int k = 0; k < 3; k++) xyz[3 * i + k] = atoi(t[1 + k].c_str());
+        }
+        fclose(sf);
+        printf(" Done reading input geometry file\n");
+        check(mks_init_points(h, xyz.data(), sp.data(), (int64_t)nfilled));
+    } else if (in.init_st == "SG") {                  // main.f:240-242: SetSiGex with Len1 rounded to 24
+        printf(" Setting up SiGe alloy with fraction = %.17g\n", in.alloy);
+        int32_t len1 = in.len[0] - in.len[0] % 24;
+        check(mks_batch_init_alloy(h, &len1, &in.alloy, (uint64_t)in.idum));
     } else if (shaped) {                              // main.f:240-278
         int32_t lens[4] = {in.len[0], in.len[1], in.len[2], in.len[3]};
         check(mks_init_shape(h, in.init_st.c_str(), lens, in.st_par));

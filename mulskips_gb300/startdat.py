@@ -124,6 +124,31 @@ def parse_startdat(path):
     return d
 
 
+def read_shape_points(path):
+    """The point-list file of InitSt SH (SetShape.f:52-79): NFilled, one
+    skipped record, then NFilled records `sym x y z`.  Returns (xyz [n, 3]
+    int32, species [n] int8): 1 for 'Si', 2 for 'C' or 'Ge', 0 for any other
+    symbol (sym is read as two characters)."""
+    with open(path) as f:
+        n = int(f.readline().replace(",", " ").split()[0])
+        f.readline()
+        xyz = np.zeros((n, 3), dtype=np.int32)
+        sp = np.zeros(n, dtype=np.int8)
+        i = 0
+        while i < n:
+            t = f.readline()
+            if not t:
+                raise ValueError("shape file: fewer than NFilled records")
+            t = t.replace(",", " ").split()
+            if len(t) < 4:
+                raise ValueError("shape file: short record")
+            sym = t[0][:2]
+            sp[i] = 1 if sym == "Si" else (2 if sym in ("C", "Ge") else 0)
+            xyz[i] = [int(t[1]), int(t[2]), int(t[3])]
+            i += 1
+    return xyz, sp
+
+
 def write_plain_si_startdat(path, T=1100.0, e_bond=0.6, nu=1e13, flux=0.5, len1=120, max_iter=1000000,
                             out_molmol=None, run_type="R", seed=1, sf=5.43 / 12, lens=(120, 120)):
     """start.dat of the plain Si(001) model (InitSt FS, NCrystal 1): PTransE(1,n)

@@ -115,6 +115,7 @@ struct ora {
     int8_t *la_geo;                         /* InitSt LA input (ora_set_la_input) */
     int16_t *la_tsub;
     int8_t *cad_geo;                        /* InitSt IN input (ora_set_geometry) */
+    char shapefile[2048];                   /* InitSt SH: the point-list file named in start.dat */
     /* InitSt ST: probability tables per temperature (SetProbabilityFromField.f)
      * and the interpolation pair of the last site (InterpProbFromField.f) */
     int st, st_fixed, st_n;
@@ -1884,9 +1885,15 @@ static void parse_startdat(ora_t *o, const char *path)
         o->st = 1;
         o->st_fixed = o->st_ttop == o->st_tbottom;
         if (o->ncov != 0) { fclose(r.f); ora_fail(o, "InitSt ST with coverage species is not restated"); }
-    } else if (!strcmp(o->init_st, "SH")) {
-        fclose(r.f);
-        ora_fail(o, "InitSt %s is not restated by the oracle", o->init_st);
+    } else if (!strcmp(o->init_st, "SH")) {     /* MS/main.f:116-117: READ(IPF,'(A)') the file name */
+        if (!rd_line(&r)) { fclose(r.f); ora_fail(o, "start.dat: missing shape file name"); }
+        const char *b = r.line;
+        while (*b && isspace((unsigned char)*b)) b++;
+        size_t m = strlen(b);
+        while (m && isspace((unsigned char)b[m - 1])) m--;
+        if (m >= sizeof o->shapefile) { fclose(r.f); ora_fail(o, "shape file name too long"); }
+        memcpy(o->shapefile, b, m);
+        o->shapefile[m] = 0;
     } else {
         rd_items(o, &r, 3, it);
         o->len1 = atoi(it[0]); o->len2 = atoi(it[1]); o->len3 = atoi(it[2]);
@@ -2281,6 +2288,183 @@ void ora_destroy(ora_t *o)
     free(o);
 }
 
+/* SetShape, MS/initial/SetShape.f:25-436 (InitSt 'SH', called from
+ * MS/main.f:281-286).  The point-list file named in start.dat holds NFilled,
+ * one skipped record, then NFilled records `sym x y z` (:52-79): every point
+ * is occupied; one with z <= 3 or z >= LenZ-4 is a wall, any other is Si for
+ * 'Si' and species 2 for 'C' or 'Ge' (sym is CHARACTER(Len=2)).  Then, over
+ * z = 4..LenZ-5 in z, y, x order (:98-186), every occupied point takes as
+ * neighbours the occupied points of its |d|^2 = 27 shell, scanned dz, dy, dx
+ * from -6 to 6 (:87-99, :113-131); with coordination <= 3 it is an MC
+ * particle whose neighbours 3 and 4 come from FIND_NN of the first two
+ * (:136-143), with 4 a bulk atom.  The reciprocity checks of the MC particles
+ * (:277-320) and of the bulk atoms above z = 12 (:325-373) follow, then the
+ * ad-voids: each empty neighbour of the MC particles present before that
+ * pass gains one coordination per MC neighbour, in list order (:378-431).
+ * Two inputs leave the reference undefined and are rejected here: an atom
+ * with fewer than two neighbours (FIND_NN of a zero NextND(2)) or more than
+ * four (NextND overflows), and a reciprocity check that meets a wall (the
+ * wall's LattInd is 0, so ListAdAtom(0) is read). */
+static void set_shape(ora_t *o)
+{
+    int lx = o->lx, ly = o->ly, lz = o->lz;
+    rd_t r;
+    r.f = fopen(o->shapefile, "r");
+    if (!r.f) ora_fail(o, "cannot open the shape file %s", o->shapefile);
+    char it[4][256];
+    lg(o, " Reading input geometry file (SHAPE): %s\n", o->shapefile);
+    rd_items(o, &r, 1, it);
+    int nfilled = atoi(it[0]);
+    if (!rd_line(&r)) { fclose(r.f); ora_fail(o, "shape file: missing second record"); }
+    for (int ia = 0; ia < nfilled; ia++) {
+        rd_items(o, &r, 4, it);
+        int x = atoi(it[1]), y = atoi(it[2]), z = atoi(it[3]);
+        if (x < 0 || x >= lx || y < 0 || y >= ly || z < 0 || z > lz) {
+            fclose(r.f);
+            ora_fail(o, "shape file: point %d %d %d outside the box", x, y, z);
+        }
+        int32_t *v = &o->latt[lidx(o, x, y, z)];
+        *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
+        char sym[3] = {it[0][0], it[0][0] ? it[0][1] : 0, 0};
+        if (z >= lz - 4 || z <= 3) {
+            mvbits(WALL, LEN_INDEX, v, POS_INDEX);
+        } else if (!strcmp(sym, "Si")) {
+            *v = (int32_t)((uint32_t)*v | (1u << POS_SI));
+        } else if (!strcmp(sym, "C") || !strcmp(sym, "Ge")) {
+            *v = (int32_t)((uint32_t)*v | (1u << POS_C));
+        }
+    }
+    fclose(r.f);
+    lg(o, " Done reading input geometry file\n");
+    int list[32][3], nlist = 0;
+    for (int k = -6; k <= 6; k++)
+        for (int j = -6; j <= 6; j++)
+            for (int i = -6; i <= 6; i++)
+                if (i * i + j * j + k * k == 27) {
+                    list[nlist][0] = i; list[nlist][1] = j; list[nlist][2] = k;
+                    nlist++;
+                }
+    int site[3], nextnd[4][3], ns[2][3], buf[3], index_event;
+    double prob;
+    for (int z = 4; z <= lz - 5; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                if (ibits(*v, POS_OCC, LEN_OCC) == 0) continue;
+                site[0] = x; site[1] = y; site[2] = z;
+                memset(nextnd, 0, sizeof nextnd);
+                int coord = 0;
+                for (int i = 0; i < nlist; i++) {
+                    int nsite[3] = {x + list[i][0], y + list[i][1], z + list[i][2]};
+                    if (nsite[0] >= lx) nsite[0] -= lx;
+                    if (nsite[0] < 0) nsite[0] += lx;
+                    if (nsite[1] >= ly) nsite[1] -= ly;
+                    if (nsite[1] < 0) nsite[1] += ly;
+                    if (ibits(*LC(o, nsite), POS_OCC, LEN_OCC) > 0) {
+                        if (coord == 4) ora_fail(o, "SetShape: more than four neighbours at %d %d %d", x, y, z);
+                        cp3(nextnd[coord], nsite);
+                        coord++;
+                    }
+                }
+                mvbits(coord, LEN_COOR, v, POS_COOR);
+                if (coord <= 3) {
+                    if (coord < 2) ora_fail(o, "SetShape: %d neighbours at %d %d %d", coord, x, y, z);
+                    cp3(buf, nextnd[2]);
+                    find_nn(nextnd[0], nextnd[1], site, ns, lx, ly);
+                    cp3(nextnd[2], ns[0]);
+                    cp3(nextnd[3], ns[1]);
+                    if (coord == 3) {
+                        int check = 1;
+                        for (int i = 0; i < 4; i++)
+                            if (nextnd[i][0] == buf[0] && nextnd[i][1] == buf[1] && nextnd[i][2] == buf[2]) check = 0;
+                        if (check) lg(o, " Coord.eq.3 wrong check Buf %d %d %d\n", buf[0], buf[1], buf[2]);
+                    }
+                    get_prob_ini(o, 1, ibits(*v, POS_SIC, LEN_SIC), coord, site, nextnd, &index_event, &prob);
+                    add_mc(o, site, nextnd, index_event, prob);
+                } else {
+                    add_bulk(o, site, nextnd);
+                }
+            }
+    /* reciprocal bonds only: MC particles, then bulk atoms above z = 12 */
+    for (int pass = 0; pass < 2; pass++) {
+        int64_t n0 = pass == 0 ? o->num_mc : o->num_bulk;
+        for (int64_t i = 1; i <= n0; i++) {
+            int nextn[4][3];
+            if (pass == 0) {
+                cp3(site, o->mc[i].xyz);
+                memcpy(nextn, o->mc[i].nn, sizeof nextn);
+            } else {
+                cp3(site, o->bulk[i].xyz);
+                if (site[2] < 13) continue;
+                memcpy(nextn, o->bulk[i].nn, sizeof nextn);
+            }
+            int32_t *v = LC(o, site);
+            int coor = ibits(*v, POS_COOR, LEN_COOR), coorold = coor;
+            for (int j = 0; j < 4; j++) {
+                int32_t w = *LC(o, nextn[j]);
+                if (ibits(w, POS_OCC, LEN_OCC) == 0) continue;
+                if (is_wall(w))
+                    ora_fail(o, "SetShape: the reciprocity check of %d %d %d meets a wall", site[0], site[1], site[2]);
+                int ind = *LI(o, nextn[j]);
+                int (*nnn)[3] = ibits(w, POS_COOR, LEN_COOR) == 4 ? o->bulk[ind].nn : o->mc[ind].nn;
+                int recipr = 0;
+                for (int k = 0; k < 4; k++)
+                    if (nnn[k][0] == site[0] && nnn[k][1] == site[1] && nnn[k][2] == site[2]) recipr = 1;
+                if (!recipr) coor--;
+            }
+            if (coor == coorold) continue;
+            int ind = *LI(o, site), iat = ibits(*v, POS_SIC, LEN_SIC);
+            mvbits(coor, LEN_COOR, v, POS_COOR);
+            get_prob(o, 1, iat, 0, coor, site, nextn, &index_event, &prob);
+            if (pass == 0) {
+                o->mc[ind].ind_event = index_event;
+                o->mc[ind].prob = prob;
+                update_tree(o, ind, prob);
+            } else {
+                erase_bulk(o, site);
+                add_mc(o, site, nextn, index_event, prob);
+            }
+        }
+    }
+    /* the ad-voids */
+    int nmc0 = o->num_mc;
+    for (int i = 1; i <= nmc0; i++) {
+        int nnsite[3];
+        cp3(nnsite, o->mc[i].xyz);
+        for (int j = 0; j < 4; j++) {
+            cp3(site, o->mc[i].nn[j]);
+            int32_t *v = LC(o, site);
+            if (ibits(*v, POS_OCC, LEN_OCC) != 0) continue;
+            int nextn[4][3];
+            memset(nextn, 0, sizeof nextn);
+            int coor = ibits(*v, POS_COOR, LEN_COOR) + 1;
+            if (coor == 1) {
+                cp3(nextn[0], nnsite);
+                mvbits(coor, LEN_COOR, v, POS_COOR);
+                get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
+                add_mc(o, site, nextn, index_event, prob);
+            } else if (coor == 2 || coor == 3) {
+                int ind = *LI(o, site);
+                memcpy(nextn, o->mc[ind].nn, sizeof nextn);
+                if (coor == 2) {
+                    cp3(nextn[1], nnsite);
+                    find_nn(nextn[0], nextn[1], site, ns, lx, ly);
+                    cp3(nextn[2], ns[0]);
+                    cp3(nextn[3], ns[1]);
+                }
+                mvbits(coor, LEN_COOR, v, POS_COOR);
+                get_prob_ini(o, 0, 0, coor, site, nextn, &index_event, &prob);
+                memcpy(o->mc[ind].nn, nextn, sizeof nextn);
+                o->mc[ind].ind_event = index_event;
+                o->mc[ind].prob = prob;
+                update_tree(o, ind, prob);
+            } else {
+                ora_fail(o, "Vacancy in the SF setting");
+            }
+        }
+    }
+}
+
 int ora_init(ora_t *o)
 {
     if (setjmp(o->jb)) return -1;
@@ -2312,6 +2496,8 @@ int ora_init(ora_t *o)
         if (!o->cad_geo) ora_fail(o, "InitSt IN needs the per-site geometry (ora_set_geometry)");
         if (o->ncrystal != 1) ora_fail(o, "the IN initializer is restated for NCrystal = 1");
         set_cad(o, 0);
+    } else if (!strcmp(o->init_st, "SH")) {      /* MS/main.f:281-286 */
+        set_shape(o);
     } else {
         ora_fail(o, "initialization not_implemented in the oracle: %s", o->init_st);
     }

@@ -203,3 +203,90 @@ def test_mulskips_e_la(oracle_lib, tmp_path):
     hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
     assert int(hdr[-1]) >= 4000
     assert len(open(d / "LattStat.dat").read().splitlines()) == L
+
+
+def test_points_match_oracle(oracle_lib, tmp_path):
+    """InitSt SH through the C ABI (mks_init_points): a 3C-SiC slab with a
+    {111}-faceted pyramid, byte-identical to the oracle's SetShape."""
+    from test_shape_points import pyramid_points, sic_startdat, write_points
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat, read_shape_points
+    L = 240
+    xyz, sym, _, _ = pyramid_points(L, 60, 54)
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    sic_startdat(str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    o = oracle_lib.Oracle(str(tmp_path / "start.dat"), L, L, L)
+    o.init()
+    ref, _ = oracle_lib.compact_state(o)
+    o.close()
+    d = parse_startdat(str(tmp_path / "start.dat"))
+    pts, sp = read_shape_points(str(tmp_path / "p.xyz"))
+    with Lattice(L, L, L, ncrystal=2, list_crystal=[14, 6], sf=d["sf"]) as lat:
+        lat.set_rates(d["ptransE"], d["ptransD"])
+        lat.init_points(pts, sp)
+        st = lat.state()
+    bad = np.argwhere(st != ref)
+    assert bad.size == 0, f"{len(bad)} sites differ, first {bad[:3]}"
+
+
+def test_mulskips_e_shape_file(oracle_lib, tmp_path):
+    """mulskips.e with InitSt SH and the point-list file: the initial frame
+    equals the oracle's, and the run goes on from it."""
+    from test_shape_points import pyramid_points, sic_startdat, write_points
+    L = 240
+    d = tmp_path / "sh"
+    d.mkdir()
+    xyz, sym, _, _ = pyramid_points(L, 60, 54)
+    write_points(d / "shape.xyz", xyz, sym)
+    sic_startdat(str(d / "start.dat"), "shape.xyz", L)
+    txt = open(d / "start.dat").read().replace("1000000 ! IterMax", "4000 ! IterMax")
+    txt = txt.replace("1000000 ! OutMolMol", "4000 ! OutMolMol")
+    (d / "start.dat").write_text(txt)
+    cwd = os.getcwd()
+    try:
+        os.chdir(d)
+        o = oracle_lib.Oracle("start.dat", L, L, L)
+        o.init()
+        o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+        o.close()
+    finally:
+        os.chdir(cwd)
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX=f"{L} {L} {L}"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+    hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
+    assert int(hdr[-1]) >= 4000
+
+
+def test_mulskips_e_sige(oracle_lib, tmp_path):
+    """mulskips.e with InitSt SG (SetSiGex): the sites of SetSi's slab, Ge
+    drawn on each atom with the alloy fraction (the reference draws it with
+    the compiler's RAND, here a seeded generator)."""
+    from mulskips_gb300.startdat import write_startdat
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    D = np.full((3, 3), 0.5)
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1100.0))
+    d = tmp_path / "sg"
+    d.mkdir()
+    write_startdat(str(d / "start.dat"), E, D, ncrystal=2, list_crystal=(14, 32), init_st="SG", len1=130,
+                   max_iter=4000, alloy_fraction=0.3)
+    write_startdat(str(tmp_path / "fs.dat"), E, D, ncrystal=1, list_crystal=(14,), init_st="FS", len1=120,
+                   max_iter=4000, run_type="T")
+    o = oracle_lib.Oracle(str(tmp_path / "fs.dat"), 480, 480, 480)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 480 480"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    mine = (d / "I00000000.xyz").read_text().splitlines()
+    ref = (tmp_path / "ora.xyz").read_text().splitlines()
+    assert len(mine) == len(ref) and mine[0] == ref[0]
+    assert [l.split()[1:] for l in mine[2:]] == [l.split()[1:] for l in ref[2:]]
+    sym = [l.split()[0] for l in mine[2:]]
+    assert set(sym) <= {"Si", "Ge"} and 0.25 < sym.count("Ge") / len(sym) < 0.35

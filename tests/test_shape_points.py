@@ -1,0 +1,204 @@
+"""InitSt SH (SetShape.f, a lattice from a point-list file), on the CPU.
+
+The oracle restates SetShape.f list by list (32-site shell scan, FIND_NN,
+reciprocity checks, ad-void pass).  No regression case of the reference uses
+SH, so it is pinned against the pinned flat initializers: the point list of
+the Si(001) (SetSi) and 3C-SiC(001) (SetSiC3C) lattices of the reference's
+Si-SL and surface cases gives back the same occupancy, species, walls and
+coordinations (the first list entries follow SetShape's own scan order).
+The library's one-byte initializer (mks_shapes::set_points, compiled for the
+host by a helper) then builds byte-identical lattices to the oracle's, on
+those lists and on a 3C-SiC slab carrying a {111}-faceted pyramid, and
+refuses the same undefined inputs."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+HELPER_SRC = os.path.join(ROOT, "tests", "native", "shape_check.cpp")
+NUMBERS = os.path.join(GOLDEN, "numberslist.txt")
+# bond directions d of a site (a, b, z1) by the parity of z1: (da, db, dz)
+OFF = np.array([[[0, 0, 1], [0, -1, -1], [-1, -1, 1], [-1, 0, -1]],
+                [[1, 1, -1], [1, 0, 1], [0, 0, -1], [0, 1, 1]]])
+
+
+@pytest.fixture(scope="module")
+def helper(tmp_path_factory, oracle_lib):
+    exe = str(tmp_path_factory.mktemp("native") / "shape_check")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-o", exe, HELPER_SRC,
+                    os.path.join(ROOT, "oracle", "mks_oracle.c"), "-lm"], check=True)
+    return exe
+
+
+def write_points(path, xyz, sym):
+    with open(path, "w") as f:
+        f.write(f"{len(xyz)}\nshape\n")
+        for (x, y, z), s in zip(xyz, sym):
+            f.write(f"{s} {x} {y} {z}\n")
+
+
+def sh_startdat(src_lines, path, points):
+    """A start.dat equal to src_lines with InitSt SH and the point file."""
+    out = []
+    for i, l in enumerate(src_lines):
+        if i == 2:
+            out += ["SH ! Initstat", points]
+        elif i == 3:
+            continue
+        else:
+            out.append(l)
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
+def lattice_points(o, zmax):
+    """Occupied diamond sites of an oracle lattice below zmax, with symbols."""
+    lc = o.lattcoo()
+    z, y, x = np.nonzero(((lc >> 23) & 1) != 0)
+    x1, y1, z1 = x // 3, y // 3, z // 3
+    dia = (x % 3 == 0) & (y % 3 == 0) & (z % 3 == 0) & (x1 % 2 == y1 % 2) & (x1 % 2 == z1 % 2)
+    dia &= np.isin((x1 + y1 + z1) % 4, [0, 3]) & (z < zmax)
+    x, y, z = x[dia], y[dia], z[dia]
+    sp = (lc[z, y, x] >> 27) & 7
+    return np.stack([x, y, z], 1), np.where(sp == 2, "C", "Si")
+
+
+def run_helper(helper, startdat, points, side):
+    r = subprocess.run([helper, startdat, NUMBERS, points, str(side), str(side), str(side)],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    return r.returncode, r.stdout
+
+
+@pytest.mark.parametrize("case", ["Si-SL", "surface"])
+def test_oracle_sh_matches_flat_initializers(oracle_lib, tmp_path, case):
+    src = os.path.join(GOLDEN, case, "start.dat")
+    o = oracle_lib.Oracle(src, 480, 480, 480)
+    o.init()
+    ref, _ = oracle_lib.compact_state(o)
+    xyz, sym = lattice_points(o, 474)
+    o.close()
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    sh_startdat(open(src).read().splitlines(), tmp_path / "start.dat", str(tmp_path / "p.xyz"))
+    o = oracle_lib.Oracle(str(tmp_path / "start.dat"), 480, 480, 480)
+    o.init()
+    mine, off = oracle_lib.compact_state(o)
+    counts = o.counts()
+    o.close()
+    assert off == 0
+    # the walls of SetSi above z = 473 are not in the list; SetSiC3C's atoms
+    # at z <= 3 become SetShape walls
+    keep = np.ones(ref.shape, bool)
+    keep[474 // 3:] = False
+    if case == "surface":
+        keep[:2] = False
+    a = np.where(ref == 0x80, 0x80, ref & 0x1F)
+    b = np.where(mine == 0x80, 0x80, mine & 0x1F)
+    assert np.array_equal(a[keep], b[keep])
+    assert counts["mc"] == 6400
+
+
+@pytest.mark.parametrize("case", ["Si-SL", "surface"])
+def test_library_sh_equals_oracle_flat_lists(helper, oracle_lib, tmp_path, case):
+    src = os.path.join(GOLDEN, case, "start.dat")
+    o = oracle_lib.Oracle(src, 480, 480, 480)
+    o.init()
+    xyz, sym = lattice_points(o, 474)
+    o.close()
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    sh_startdat(open(src).read().splitlines(), tmp_path / "start.dat", str(tmp_path / "p.xyz"))
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), 480)
+    assert rc == 0 and "mismatch 0" in out, out
+
+
+def pyramid_points(L, h_slab, h_pyr, sic=True):
+    """A 3C slab over z = 6..h_slab with a square pyramid of {111} facets
+    (z <= h_slab + h_pyr - |x - L/2| - |y - L/2|) on it, walls at z = 0, 3
+    and at the top two layers; atoms with fewer than two neighbours removed
+    until none is left.  Returns (xyz, symbols) of the points and (xyz,
+    sublattice-1 flags) of the empty sites with exactly one neighbour."""
+    NA = NB = L // 6
+    NZ = L // 3 + 1
+    z1, b, a = np.meshgrid(np.arange(NZ), np.arange(NB), np.arange(NA), indexing="ij")
+    valid = ((a + b + (z1 >> 1)) & 1) == 0
+    x, y, z = 3 * (2 * a + (z1 & 1)), 3 * (2 * b + (z1 & 1)), 3 * z1
+    wall = valid & ((z <= 3) | (z >= L - 4))
+    top = h_slab + h_pyr - np.abs(x - L // 2) - np.abs(y - L // 2)
+    atom = valid & (z >= 6) & ((z <= h_slab) | (z <= top))
+    while True:
+        occ = atom | wall
+        cnt = np.zeros(occ.shape, int)
+        for par in (0, 1):
+            for d in range(4):
+                da, db, dz = OFF[par][d]
+                sh = np.roll(np.roll(occ, -da, axis=2), -db, axis=1)
+                shz = np.zeros_like(sh)
+                if dz == 1:
+                    shz[:-1] = sh[1:]
+                else:
+                    shz[1:] = sh[:-1]
+                cnt[par::2] += shz[par::2]
+        weak = atom & (cnt < 2)
+        if not weak.any():
+            break
+        atom &= ~weak
+    pts = wall | atom
+    kind = ((x // 3 + y // 3 + z // 3) % 4 == 0)
+    sym = np.where(kind | (not sic), "Si", "C")
+    sel = np.nonzero(pts)
+    lone = np.nonzero(valid & ~pts & (cnt == 1) & (z >= 6) & (z <= L - 8))
+    return (np.stack([x[sel], y[sel], z[sel]], 1), sym[sel], np.stack([x[lone], y[lone], z[lone]], 1),
+            kind[lone])
+
+
+def sic_startdat(path, points, L):
+    from mulskips_gb300.startdat import write_startdat
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    D = np.full((3, 3), 0.5)
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1600.0))
+    write_startdat(path, E, D, ncrystal=2, list_crystal=(14, 6), init_st="F", len1=L // 2, run_type="T")
+    sh_startdat(open(path).read().splitlines(), path, points)
+
+
+def test_library_sh_equals_oracle_pyramid(helper, oracle_lib, tmp_path):
+    L = 240
+    xyz, sym, _, _ = pyramid_points(L, 60, 54)
+    # an off-site wall point away from every atom is taken and ignored
+    xyz = np.vstack([xyz, [[1, 1, 1]]])
+    sym = np.append(sym, "Si")
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    sic_startdat(str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    assert rc == 0 and "mismatch 0" in out, out
+    o = oracle_lib.Oracle(str(tmp_path / "start.dat"), L, L, L)
+    o.init()
+    st, _ = oracle_lib.compact_state(o)
+    o.close()
+    # the facets hold 2- and 3-coordinated atoms; first entries vary with the scan
+    co = (st >> 2) & 7
+    occ = (st & 3) != 0
+    assert ((co == 2) & occ).sum() > 100 and ((co == 3) & occ).sum() > 100
+    assert len(np.unique((st[occ & (co <= 3)] >> 5) & 3)) > 1
+
+
+def test_undefined_inputs_refused_by_both(helper, tmp_path):
+    L = 240
+    xyz, sym, lone, lone_kind = pyramid_points(L, 60, 30)
+    assert len(lone) > 0
+    # an atom bonded once: the reference runs FIND_NN on a zero second neighbour
+    xyz1 = np.vstack([xyz, lone[:1]])
+    write_points(tmp_path / "p.xyz", xyz1, np.append(sym, "Si" if lone_kind[0] else "C"))
+    sic_startdat(str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    assert "product: an atom with fewer than two neighbours" in out and "oracle: ok" not in out, out
+    # an atom off the diamond sites: the one-byte lattice refuses it
+    xyz2 = np.vstack([xyz, [[1, 1, 30]]])
+    write_points(tmp_path / "p.xyz", xyz2, np.append(sym, "Si"))
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    assert "product: an atom off the diamond sites" in out, out
