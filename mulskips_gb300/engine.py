@@ -305,6 +305,14 @@ class Batch:
         lc = np.ascontiguousarray(lattcoo, dtype=np.int32)
         N.check(N.lib().mks_batch_load_lattice(self._h, int(rep), N.ptr(lc)))
 
+    def init_points(self, rep, xyz, species):
+        """Replica rep by SetShape (InitSt SH) from grid points xyz [n, 3] with
+        species 1 (Si) or 2 (C / Ge)."""
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        sp = np.ascontiguousarray(species, dtype=np.int8).reshape(-1)
+        assert sp.size == p.shape[0]
+        N.check(N.lib().mks_batch_init_points(self._h, int(rep), N.ptr(p), N.ptr(sp), int(sp.size)))
+
     def load_temperature(self, rep, lattcoo):
         """Static LA temperatures of replica rep from the LattCoo T bits."""
         lc = np.ascontiguousarray(lattcoo, dtype=np.int32)

@@ -152,6 +152,57 @@ def test_sic_surface_matches_serial_reference(oracle_lib, tmp_path):
         assert abs(diff) <= hw, name
 
 
+def test_sic_facets_match_serial_reference(oracle_lib, tmp_path):
+    """3C-SiC on {111} facets: a square pyramid with {111} faces on a (001)
+    slab (InitSt SH point list, 240^3 box), the rates of the reference's
+    `surface` case, RunType R: atoms and C atoms at t = 2e5 s (about 2.5e5
+    events, the facets filling in), 16 oracle seeds against 16 GPU replicas
+    at the two-species window factor."""
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.startdat import parse_startdat, read_shape_points
+    from conftest import GOLDEN
+    from test_shape_points import pyramid_points, sh_startdat, write_points
+    t_obs, n, L = 2e5, 16, 240
+    xyz, sym, _, _ = pyramid_points(L, 60, 54)
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    txt = open(os.path.join(GOLDEN, "surface", "start.dat")).read().replace(
+        "T   ! R = production run", "R   ! R = production run")
+    ref, ref_c = [], []
+    for s in range(n):
+        p = tmp_path / f"fac{s}.dat"
+        sh_startdat(txt.replace("9117116 ! Random seed", f"{600 + s} ! Random seed").splitlines(), p,
+                    str(tmp_path / "p.xyz"))
+        o = oracle_lib.Oracle(str(p), L, L, L, numbers=None)
+        o.init()
+        o.run_until(t_obs)
+        st, _ = oracle_lib.compact_state(o)
+        ref.append(int(np.count_nonzero((st & 3) != 0)))
+        ref_c.append(int(np.count_nonzero((st & 3) == 2)))
+        o.close()
+    ref, ref_c = np.array(ref, float), np.array(ref_c, float)
+    d = parse_startdat(str(tmp_path / "fac0.dat"))
+    pts, sp = read_shape_points(str(tmp_path / "p.xyz"))
+    b = Batch([(L, L, L)] * n, seeds=[81 + s for s in range(n)], ncrystal=2, list_crystal=(14, 6), sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
+    for r in range(n):
+        b.init_points(r, pts, sp)
+    start = np.array([o["atoms"] for o in b.observables()], float)
+    tau = float(b.suggest_tau(accurate_f(2))[0])
+    nwin = int(math.ceil(t_obs / tau))
+    b.run(t_obs / nwin, nwin)
+    obs = b.observables()
+    b.close()
+    g = np.array([o["atoms"] for o in obs], float)
+    gc = np.array([o["species"][1] for o in obs], float)
+    assert g.mean() - start.mean() > 1000
+    for name, x, y in (("atoms", g, ref), ("C atoms", gc, ref_c)):
+        diff, hw = band(x, y)
+        print(f"SiC facets {name}: gpu {x.mean():.1f}+-{x.std(ddof=1):.1f} serial {y.mean():.1f}+-{y.std(ddof=1):.1f} "
+              f"diff {diff:.1f} 3-sigma band +-{hw:.1f} (tau {tau:.3e}, {nwin} windows)")
+        assert abs(diff) <= hw, name
+
+
 def _cvd_oracle(args):
     """One RunType R oracle run of the CVD case to t_obs: (atoms, covered)."""
     import sys
