@@ -290,12 +290,15 @@ int mks_batch_load_temperature(mks_handle *h, int32_t rep, const int32_t *lattco
 int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field);
 /* The reference's shaped initial lattices (main.f:240-278), built in place
  * of replica rep's lattice: init_st "C" SetNC (lens = Len1, Len2, Len3),
- * "S" SetNCSp (Len1), "I" SetInvPOff (Len1, Len2, as main.f:245-246 passes
- * them), "FF" SetSiFINFET (Len1..Len4, each rounded down to a multiple of
- * 24), "ST" SetTrenchSi (Len1, Len2, Len3; params = angle in degrees, Ttop,
- * Tbottom in K; also loads the temperature field T(z) for
- * mks_batch_set_tabulated).  Same result as SetNC.f, SetNCSp.f,
- * SetInvPOff.f, SetSiFINFET.f and SetTrenchSi.f including their closing
+ * "S" SetNCSp (Len1), "SS" SetNCSpSi (Len1), "I" SetInvPOff (Len1, Len2, as
+ * main.f:245-246 passes them) and its variants "D" SetInvPC, "Z" SetInvPSi,
+ * "J" SetInvPwAPB, "K" SetInvPwOnlySiorC, "L" SetInvPwOnlyCorSi (Len1,
+ * Len2), "T" SetTrench (Len1, Len2, Len3), "Fw" SetSiC3Cww (Len1, Len2) and
+ * "Fa" SetSiC3Cwwaperture (Len1, Len2, Len3; these two and "FF" round each
+ * length down to a multiple of 24), "FF" SetSiFINFET (Len1..Len4), "ST"
+ * SetTrenchSi (Len1, Len2, Len3; params = angle in degrees, Ttop, Tbottom in
+ * K; also loads the temperature field T(z) for mks_batch_set_tabulated).
+ * Same result as the reference's routines including their closing
  * coordination passes.                                                      */
 int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const int32_t *lens, const double *params);
 int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, const double *params);

@@ -2755,29 +2755,9 @@ int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const 
     mks_shapes::Grid g(lx, ly, lz);
     std::string kind(init_st);
     std::vector<int> temp;
-    auto within = [&](int v, int lo, int hi) { return v >= lo && v <= hi; };
-    if (kind == "C") {                                        // main.f:261-262
-        if (!within(lens[0], 1, lx - 24) || !within(lens[1], 1, ly - 24) || !within(lens[2], 1, lz - 24))
-            return fail(MKS_ERR_ARG, "SetNC lengths %d %d %d do not fit the box", lens[0], lens[1], lens[2]);
-        mks_shapes::set_nc(g, lens[0], lens[1], lens[2], false);
-    } else if (kind == "S") {                                 // main.f:257-258
-        if (!within(lens[0], 1, std::min(std::min(lx, ly), lz) - 24)) return fail(MKS_ERR_ARG, "SetNCSp length %d", lens[0]);
-        mks_shapes::set_nc(g, lens[0], lens[0], lens[0], true);
-    } else if (kind == "I") {                                 // main.f:245-246: SetInvPOff(Len1, Len2)
-        if (!within(lens[1], 24, lz - 12)) return fail(MKS_ERR_ARG, "SetInvPOff Len3 %d outside the box", lens[1]);
-        mks_shapes::set_invp(g, lens[0], lens[1]);
-    } else if (kind == "FF") {                                // main.f:273-278
-        int l[4];
-        for (int i = 0; i < 4; i++) l[i] = lens[i] - lens[i] % 24;
-        if (!within(l[0], 6, lz - 7) || !within(l[2], 6, lz - 16)) return fail(MKS_ERR_ARG, "SetSiFINFET lengths");
-        mks_shapes::set_finfet(g, l[0], l[1], l[2], l[3]);
-    } else if (kind == "ST") {                                // main.f:265-266
-        if (!params) return fail(MKS_ERR_ARG, "SetTrenchSi needs angle, Ttop, Tbottom");
-        if (!within(lens[2], 22, lz - 14)) return fail(MKS_ERR_ARG, "SetTrenchSi Len3 %d outside the box", lens[2]);
-        mks_shapes::set_trench(g, lens[0], lens[1], lens[2], params[0], params[1], params[2], temp);
-    } else {
-        return fail(MKS_ERR_UNSUPPORTED, "InitSt %s has no shape initializer", init_st);
-    }
+    char msg[160];
+    if (int e = mks_shapes::build_shape(g, kind, lens, params, temp, msg, sizeof msg))
+        return fail(e == 2 ? MKS_ERR_UNSUPPORTED : MKS_ERR_ARG, "%s", msg);
     std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
     for (int z1 = 0; z1 < r.NZ; z1++)
         for (int b = 0; b < r.NB; b++)

@@ -9,8 +9,10 @@
 // off-grid points never neighbour a diamond site.
 #pragma once
 #include <cmath>
+#include <cstdio>
 #include <cstdint>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "lattice.cuh"
@@ -100,8 +102,9 @@ inline void fill(Grid &g, int x, int y, int z, int sp)
     if (v && *v != WALL) *v = mks::mk(sp, mks::co_of(*v), 0, 0);
 }
 
-// SetNC (SetNC.f:24-235) or, with sphere, SetNCSp (SetNCSp.f:24-237)
-inline void set_nc(Grid &g, int len1, int len2, int len3, bool sphere)
+// SetNC (SetNC.f:24-235) or, with sphere, SetNCSp (SetNCSp.f:24-237); with
+// all_si as well, SetNCSpSi (SetNCSpSi.f: the ball with Si on both sublattices)
+inline void set_nc(Grid &g, int len1, int len2, int len3, bool sphere, bool all_si = false)
 {
     int x0 = g.lx / 2 - len1 / 2, x1 = g.lx / 2 + len1 / 2 - 1;
     int y0 = g.ly / 2 - len2 / 2, y1 = g.ly / 2 + len2 / 2 - 1;
@@ -114,7 +117,7 @@ inline void set_nc(Grid &g, int len1, int len2, int len3, bool sphere)
                     long dx = x - g.lx / 2, dy = y - g.ly / 2, dz = z - g.lz / 2;
                     if (dx * dx + dy * dy + dz * dz > (long)len1 * len1 / 4) continue;
                 }
-                fill(g, x, y, z, kind_of(x, y, z));
+                fill(g, x, y, z, all_si ? 1 : kind_of(x, y, z));
             }
     coor_pass(g, x0 - 10, x1 + 10, y0 - 10, y1 + 10, z0 - 10, z1 + 10, false);
 }
@@ -122,14 +125,32 @@ inline void set_nc(Grid &g, int len1, int len2, int len3, bool sphere)
 // SetInvPOff (SetInvPOff.f:22-286), called with (Len1, Len2): pits where
 // |x-xc| + |y-yc| - 1.10 (z - Len3) <= Len for the box centre or a corner,
 // evaluated in single precision like the reference's default-REAL literal
-inline void set_invp(Grid &g, int len, int len3)
+// The species of the inverted-pyramid family at (x, y) on sublattice k:
+// 'I' SetInvPOff (k itself), 'Z' SetInvPSi (Si), 'D' SetInvPC (C), and the
+// antiphase domains of 'K' SetInvPwOnlySiorC (sublattices swapped outside
+// the quadrants x < LenX/2 <= y and y < LenY/2 <= x), 'L' SetInvPwOnlyCorSi
+// (swapped inside them) and 'J' SetInvPwAPB (swapped where x + y > LenY).
+inline int invp_species(char mode, int k, int x, int y, int lx, int ly)
+{
+    if (mode == 'I') return k;
+    if (mode == 'Z') return 1;
+    if (mode == 'D') return 2;
+    bool r = mode == 'J' ? x + y <= ly : ((x < lx / 2 && y >= ly / 2) || (x >= lx / 2 && y < ly / 2));
+    if (mode == 'L') r = !r;
+    return r ? k : 3 - k;
+}
+
+// With mode 'D', 'Z', 'J', 'K' or 'L' the pits have slope 1, tested in
+// integers (SetInvPC.f, SetInvPSi.f, SetInvPwAPB.f, SetInvPwOnlySiorC.f,
+// SetInvPwOnlyCorSi.f), and the species follow invp_species.
+inline void set_invp(Grid &g, int len, int len3, char mode = 'I')
 {
     int lenh = g.lx / 2 - 1;
     for (int z = 0; z <= 20; z++)
         for (int y = 0; y < g.ly; y++)
             for (int x = 0; x < g.lx; x++) {
                 uint8_t *v = g.at(x, y, z);
-                if (v) *v = mks::mk(kind_of(x, y, z), 4, 0, 0);
+                if (v) *v = mks::mk(invp_species(mode, kind_of(x, y, z), x, y, g.lx, g.ly), 4, 0, 0);
             }
     const int cx[5] = {lenh, 0, g.lx, 0, g.lx}, cy[5] = {lenh, 0, 0, g.ly, g.ly};
     for (int z = 21; z <= len3 - 1; z++) {
@@ -138,9 +159,11 @@ inline void set_invp(Grid &g, int len, int len3)
             for (int x = 0; x < g.lx; x++) {
                 if (!g.at(x, y, z)) continue;
                 bool pit = false;
-                for (int c = 0; c < 5 && !pit; c++)
-                    pit = (float)(std::abs(x - cx[c]) + std::abs(y - cy[c])) - dz <= (float)len;
-                if (!pit) fill(g, x, y, z, kind_of(x, y, z));
+                for (int c = 0; c < 5 && !pit; c++) {
+                    int d = std::abs(x - cx[c]) + std::abs(y - cy[c]);
+                    pit = mode == 'I' ? (float)d - dz <= (float)len : d - (z - len3) <= len;
+                }
+                if (!pit) fill(g, x, y, z, invp_species(mode, kind_of(x, y, z), x, y, g.lx, g.ly));
             }
     }
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
@@ -208,6 +231,53 @@ inline void set_trench(Grid &g, int len, int len2, int len3, double angle, doubl
             }
     }
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
+}
+
+// SetTrench (SetTrench.f:23-283, InitSt T): the 3C substrate from z = 0 (no
+// walls, no temperatures) under a layer z = 21..Len3-1 with a trench of
+// vertical sides, |x - Lenh| <= Len for Len2 < z < Len3
+inline void set_trench_sic(Grid &g, int len, int len2, int len3)
+{
+    int lenh = g.lx / 2 - 1;
+    for (int z = 0; z <= 20; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++)
+                if (uint8_t *v = g.at(x, y, z)) *v = mks::mk(kind_of(x, y, z), 4, 0, 0);
+    for (int z = 21; z <= len3 - 1; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                if (!g.at(x, y, z)) continue;
+                if (std::abs(x - lenh) <= len && z > len2 && z < len3) continue;
+                fill(g, x, y, z, kind_of(x, y, z));
+            }
+    coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 21, len3 + 9, false);
+}
+
+// SetSiC3Cww (SetSiC3Cww.f:25-230, InitSt Fw) or, with lap >= 0,
+// SetSiC3Cwwaperture (SetSiC3Cwwaperture.f, Fa): the SetSiC3C slab of height
+// Len over SetSi's walls (z = 0..5 and LenZ-6..LenZ-1, bulk from z = 6; 3C
+// species, surface atoms at Len-3 and the empty layer at Len of coordination
+// 2), then walls over z = Lenww..LenZ-7 (leaving x in [INT(0.5 (LenX - lap)),
+// INT(0.5 (LenX + lap))) open) written without touching the counts.
+inline void set_flat_ww(Grid &g, int len, int lenww, int lap)
+{
+    for (int z = 0; z <= g.lz; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                uint8_t *v = g.at(x, y, z);
+                if (!v) continue;
+                if (z <= 5 || (z >= g.lz - 6 && z <= g.lz - 1)) *v = WALL;
+                else if (z <= len - 4) *v = mks::mk(kind_of(x, y, z), 4, 0, 0);
+                else if (z <= len - 1) *v = mks::mk(kind_of(x, y, z), 2, 0, 0);
+                else if (z == len) *v = mks::mk(0, 2, 0, 0);
+            }
+    const int xa = lap >= 0 ? (int)(0.5 * (g.lx - lap)) : g.lx, xb = lap >= 0 ? (int)(0.5 * (g.lx + lap)) : g.lx;
+    for (int z = lenww; z <= g.lz - 7; z++)
+        for (int y = 0; y < g.ly; y++)
+            for (int x = 0; x < g.lx; x++) {
+                if (lap >= 0 && x >= xa && x < xb) continue;
+                if (uint8_t *v = g.at(x, y, z)) *v = WALL;
+            }
 }
 
 // SetCAD for InitSt IN (SetCAD.f:80-341, fresh start): walls at z = 0..3 and
@@ -340,6 +410,85 @@ inline const char *set_points(Grid &g, const int32_t *xyz, const int8_t *sp, int
                 }
             }
     return nullptr;
+}
+
+// The first list entry of every coor-1 empty site is its one occupied
+// neighbour that is not a wall (Get_Prob_Ini keeps it as NextN(1)); its
+// dummy flag is set when that neighbour has coordination < 2 (the rate of
+// Get_Prob_Ini.f:89-104).
+inline void list_heads(Grid &g)
+{
+    for (int z1 = 0; z1 < g.NZ; z1++)
+        for (int b = 0; b < g.NB; b++)
+            for (int a = 0; a < g.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                uint8_t &v = g.st[((size_t)z1 * g.NB + b) * g.NA + a];
+                if (v == WALL || (v & 3) || mks::co_of(v) != 1) continue;
+                int found = -1;
+                uint8_t ns = 0;
+                for (int d = 0; d < 4; d++) {
+                    uint8_t *w = g.nb(a, b, z1, d);
+                    if (w && *w != WALL && (*w & 3)) {
+                        found = d;
+                        ns = *w;
+                    }
+                }
+                if (found >= 0) v = mks::mk(0, 1, found, mks::co_of(ns) < 2 ? 1 : 0);
+            }
+}
+
+// The shaped initializers by InitSt (main.f:224-278): lens are Len1..Len4 as
+// start.dat gives them, params the angle, Ttop and Tbottom of "ST" (whose
+// temperatures per layer z go to temp).  Returns 0, or 1 for lengths that do
+// not fit the box, 2 for an InitSt without a shape here or an input the
+// reference would leave inconsistent, with the reason in msg.
+inline int build_shape(Grid &g, const std::string &kind, const int32_t *lens, const double *params,
+                       std::vector<int> &temp, char *msg, size_t cap)
+{
+    const int lx = g.lx, ly = g.ly, lz = g.lz;
+    auto within = [&](int v, int lo, int hi) { return v >= lo && v <= hi; };
+    auto err = [&](int code, const char *fmt, auto... a) {
+        snprintf(msg, cap, fmt, a...);
+        return code;
+    };
+    if (kind == "C") {                                        // main.f:261-262
+        if (!within(lens[0], 1, lx - 24) || !within(lens[1], 1, ly - 24) || !within(lens[2], 1, lz - 24))
+            return err(1, "SetNC lengths %d %d %d do not fit the box", lens[0], lens[1], lens[2]);
+        set_nc(g, lens[0], lens[1], lens[2], false);
+    } else if (kind == "S" || kind == "SS") {                 // main.f:257-260: SetNCSp, SetNCSpSi
+        if (!within(lens[0], 1, std::min(std::min(lx, ly), lz) - 24)) return err(1, "SetNCSp length %d", lens[0]);
+        set_nc(g, lens[0], lens[0], lens[0], true, kind == "SS");
+    } else if (kind.size() == 1 && std::string("IDZJKL").find(kind[0]) != std::string::npos) {
+        // main.f:245-256: SetInvPOff, SetInvPC, SetInvPSi, SetInvPwAPB,
+        // SetInvPwOnlySiorC, SetInvPwOnlyCorSi, each called with (Len1, Len2)
+        if (!within(lens[1], 24, lz - 12)) return err(1, "SetInvP Len3 %d outside the box", lens[1]);
+        set_invp(g, lens[0], lens[1], kind[0]);
+    } else if (kind == "T") {                                 // main.f:263-264: SetTrench(Len1, Len2, Len3)
+        if (!within(lens[2], 22, lz - 14)) return err(1, "SetTrench Len3 %d outside the box", lens[2]);
+        set_trench_sic(g, lens[0], lens[1], lens[2]);
+    } else if (kind == "Fw" || kind == "Fa") {                // main.f:228-236, lengths rounded to 24
+        int l[3];
+        for (int i = 0; i < 3; i++) l[i] = lens[i] - lens[i] % 24;
+        if (!within(l[0], 24, lz - 12)) return err(1, "SetSiC3Cww slab height %d", l[0]);
+        // the wall block is written after the lists: over a listed site it
+        // would leave the reference with a stale list entry
+        if (l[1] <= l[0]) return err(2, "SetSiC3Cww wall height %d not above the slab %d", l[1], l[0]);
+        if (kind == "Fa" && !within(l[2], 0, lx)) return err(1, "SetSiC3Cwwaperture aperture %d", l[2]);
+        set_flat_ww(g, l[0], l[1], kind == "Fa" ? l[2] : -1);
+    } else if (kind == "FF") {                                // main.f:273-278
+        int l[4];
+        for (int i = 0; i < 4; i++) l[i] = lens[i] - lens[i] % 24;
+        if (!within(l[0], 6, lz - 7) || !within(l[2], 6, lz - 16)) return err(1, "SetSiFINFET lengths %d %d", l[0], l[2]);
+        set_finfet(g, l[0], l[1], l[2], l[3]);
+    } else if (kind == "ST") {                                // main.f:265-266
+        if (!params) return err(1, "%s", "SetTrenchSi needs angle, Ttop, Tbottom");
+        if (!within(lens[2], 22, lz - 14)) return err(1, "SetTrenchSi Len3 %d outside the box", lens[2]);
+        set_trench(g, lens[0], lens[1], lens[2], params[0], params[1], params[2], temp);
+    } else {
+        return err(2, "InitSt %s has no shape initializer", kind.c_str());
+    }
+    list_heads(g);
+    return 0;
 }
 
 }  // namespace mks_shapes

@@ -88,9 +88,10 @@ class Lattice:
         N.check(N.lib().mks_init_flat(self._h, kind.encode()[:1], int(len1)))
 
     def init_shape(self, init_st, lens, params=None):
-        """The reference's shaped lattices: 'C' (SetNC), 'S' (SetNCSp), 'I'
-        (SetInvPOff), 'FF' (SetSiFINFET), 'ST' (SetTrenchSi, params = angle,
-        Ttop, Tbottom)."""
+        """The reference's shaped lattices: 'C' (SetNC), 'S' (SetNCSp), 'SS'
+        (SetNCSpSi), 'I' (SetInvPOff) and its variants 'D', 'Z', 'J', 'K', 'L',
+        'T' (SetTrench), 'Fw' / 'Fa' (SetSiC3Cww / SetSiC3Cwwaperture), 'FF'
+        (SetSiFINFET), 'ST' (SetTrenchSi, params = angle, Ttop, Tbottom)."""
         l = np.zeros(4, dtype=np.int32)
         l[:len(lens)] = lens
         p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)

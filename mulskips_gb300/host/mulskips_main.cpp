@@ -344,11 +344,14 @@ int main()
                in.list_cov[2]);
         if (in.ncov > 1) die("ERR NOT IMPLEMENTED: the GPU engine holds one coverage species");
     }
-    const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "I" || in.init_st == "FF" ||
-                        in.init_st == "ST";
+    const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "SS" || in.init_st == "I" ||
+                        in.init_st == "D" || in.init_st == "Z" || in.init_st == "J" || in.init_st == "K" ||
+                        in.init_st == "L" || in.init_st == "T" || in.init_st == "Fw" || in.init_st == "Fa" ||
+                        in.init_st == "FF" || in.init_st == "ST";
     if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "SG" && in.init_st != "IN" && in.init_st != "LA" &&
         in.init_st != "SH" && !shaped)
-        die("initialization not_implemented in the GPU engine (FS, F, SG, C, S, I, FF, ST, IN, SH and LA are)");
+        die("initialization not_implemented in the GPU engine (A and E are not: FS, F, Fw, Fa, SG, C, S, SS, I, D, Z, "
+            "J, K, L, T, FF, ST, IN, SH and LA are)");
     if (in.alloy > 0.0 && (in.init_st == "IN" || in.init_st == "LA"))
         die("ERR: SetCAD with an alloy fraction > 0 is not built (it draws the species from the compiler's RAND)");
     mks_config cfg;

@@ -1187,12 +1187,12 @@ static void set_walls(ora_t *o, int z0, int z1)
  * MS/initial/SetSiC3C.f:25-199.  They differ in the walls (SetSi only),
  * the bulk start (z=6 vs z=0) and the species of the second sublattice
  * (Si vs C) and of the surface layer's rate (PtransE(1|2,2,...)). */
-static void set_flat(ora_t *o, int len, int sic)
+static void set_flat(ora_t *o, int len, int sic, int walls)
 {
     int site[3], nextn[4][3], index_event;
     double prob;
-    if (!sic) set_walls(o, 0, 5);
-    int zb = sic ? 0 : 6;
+    if (walls) set_walls(o, 0, 5);
+    int zb = walls ? 6 : 0;
     for (int z = zb; z <= len - 4; z++)
         for (int y = 0; y < o->ly; y++)
             for (int x = 0; x < o->lx; x++) {
@@ -1232,7 +1232,25 @@ static void set_flat(ora_t *o, int len, int sic)
             get_prob(o, 0, 0, 0, 2, site, nextn, &index_event, &prob);
             add_mc(o, site, nextn, index_event, prob);
         }
-    if (!sic) set_walls(o, o->lz - 6, o->lz - 1);
+    if (walls) set_walls(o, o->lz - 6, o->lz - 1);
+}
+
+/* The wall block of SetSiC3Cww (MS/initial/SetSiC3Cww.f:209-218, InitSt
+ * 'Fw') and SetSiC3Cwwaperture (SetSiC3Cwwaperture.f:209-223, 'Fa'): every
+ * grid point of z = Lenww..LenZ-7, or with lap >= 0 those with x below
+ * INT(0.5 (LenX - lap)) or from INT(0.5 (LenX + lap)), written after the
+ * lists without touching them. */
+static void set_wall_block(ora_t *o, int lenww, int lap)
+{
+    int xa = lap >= 0 ? (int)(0.5 * (o->lx - lap)) : o->lx, xb = lap >= 0 ? (int)(0.5 * (o->lx + lap)) : o->lx;
+    for (int z = lenww; z <= o->lz - 7; z++)
+        for (int y = 0; y < o->ly; y++)
+            for (int x = 0; x < o->lx; x++) {
+                if (lap >= 0 && x >= xa && x < xb) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << POS_OCC));
+                mvbits(WALL, LEN_INDEX, v, POS_INDEX);
+            }
 }
 
 /* Get_Prob_Ini, MS/mcevent/Get_Prob_Ini.f:23-161: init-time rate of a site
@@ -1384,8 +1402,10 @@ static void list_pass(ora_t *o, int xa, int xb, int ya, int yb, int za, int zb, 
  * 1 on the (x1+y1+z1) mod 4 = 0 sublattice, 2 on the other), coordinations
  * and isolated-atom removal over the box grown by 10, then the lists.  With
  * sphere != 0 it is SetNCSp (MS/initial/SetNCSp.f:24-237, InitSt 'S'): the
- * cube of side Len1 cut to the ball d^2 <= Len1^2/4 around the box centre. */
-static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere)
+ * cube of side Len1 cut to the ball d^2 <= Len1^2/4 around the box centre.
+ * With all_si it is SetNCSpSi (MS/initial/SetNCSpSi.f, InitSt 'SS'): the
+ * same ball with Si on both sublattices. */
+static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere, int all_si)
 {
     int lx = o->lx, ly = o->ly, lz = o->lz;
     int x0 = lx / 2 - len1 / 2, x1e = lx / 2 + len1 / 2 - 1;
@@ -1406,7 +1426,7 @@ static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere)
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 || all_si ? POS_SI : POS_C)) | (1u << POS_OCC));
             }
     coor_pass(o, x0 - 10, x1e + 10, y0 - 10, y1e + 10, z0 - 10, z1e + 10, 0);
     list_pass(o, x0 - 10, x1e + 10, y0 - 10, y1e + 10, z0 - 10, z1e + 10, 0);
@@ -1419,8 +1439,27 @@ static void set_nc(ora_t *o, int len1, int len2, int len3, int sphere)
  * a site is left empty when |x-xc| + |y-yc| - 1.10 (z - Len3) <= Len for
  * any of the five centres.  The test is evaluated in single precision, as
  * the reference's default-REAL constant 1.10 makes it.  Then the two
- * closing passes over z = 21..Len3+9 on the whole x-y plane. */
-static void set_invp(ora_t *o, int len, int len3)
+ * closing passes over z = 21..Len3+9 on the whole x-y plane.  The same code
+ * with slope 1 in integers and the species of invp_species is SetInvPC
+ * ('D'), SetInvPSi ('Z'), SetInvPwAPB ('J'), SetInvPwOnlySiorC ('K') and
+ * SetInvPwOnlyCorSi ('L'), MS/main.f:247-256. */
+/* The species of a site of sublattice k (1, 2) at (x, y) in the inverted
+ * pyramid family: 'I' SetInvPOff (1 on sublattice 1, 2 on 2), 'Z' SetInvPSi
+ * (all Si), 'D' SetInvPC (all C), 'K' SetInvPwOnlySiorC (sublattices swapped
+ * outside the quadrants x < LenX/2 <= y and y < LenY/2 <= x), 'L'
+ * SetInvPwOnlyCorSi (swapped inside them), 'J' SetInvPwAPB (swapped where
+ * x + y > LenY): antiphase domains. */
+static int invp_species(int mode, int k, int x, int y, int lx, int ly)
+{
+    if (mode == 'I') return k;
+    if (mode == 'Z') return 1;
+    if (mode == 'D') return 2;
+    int r = mode == 'J' ? x + y <= ly : ((x < lx / 2 && y >= ly / 2) || (x >= lx / 2 && y < ly / 2));
+    if (mode == 'L') r = !r;
+    return r ? k : 3 - k;
+}
+
+static void set_invp(ora_t *o, int len, int len3, int mode)
 {
     int lx = o->lx, ly = o->ly;
     int lenh = lx / 2 - 1;
@@ -1432,7 +1471,8 @@ static void set_invp(ora_t *o, int len, int len3)
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+                int sp = invp_species(mode, k, x, y, lx, ly);
+                *v = (int32_t)((uint32_t)*v | (1u << (sp == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
                 mvbits(4, LEN_COOR, v, POS_COOR);
                 site[0] = x; site[1] = y; site[2] = z;
                 std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
@@ -1446,11 +1486,15 @@ static void set_invp(ora_t *o, int len, int len3)
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 int pit = 0;
-                for (int c = 0; c < 5 && !pit; c++)
-                    pit = (float)(abs(x - cx[c]) + abs(y - cy[c])) - dz <= (float)len;
+                for (int c = 0; c < 5 && !pit; c++) {
+                    int d = abs(x - cx[c]) + abs(y - cy[c]);
+                    /* slope 1.10 (a default-REAL literal) for SetInvPOff, 1 (integer) for the others */
+                    pit = mode == 'I' ? (float)d - dz <= (float)len : d - (z - len3) <= len;
+                }
                 if (pit) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+                int sp = invp_species(mode, k, x, y, lx, ly);
+                *v = (int32_t)((uint32_t)*v | (1u << (sp == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
             }
     }
     coor_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
@@ -1498,7 +1542,10 @@ static void set_finfet(ora_t *o, int len, int lenww, int lenwwtop, int lap)
  * the closing passes over z = 21..Len3+9.  Pi is the reference's
  * REAL(8) :: Pi initialised from a default-REAL literal, i.e. single
  * precision.  With Ttop = Tbottom the tables are interpolated once at Ttop. */
-static void set_trench(ora_t *o, int len, int len2, int len3)
+/* With sic it is SetTrench (MS/initial/SetTrench.f:23-283, InitSt 'T'): no
+ * temperatures and no walls, the substrate from z = 0, C on the second
+ * sublattice and vertical trench sides (|x - Lenh| <= Len). */
+static void set_trench(ora_t *o, int len, int len2, int len3, int sic)
 {
     int lx = o->lx, ly = o->ly, lz = o->lz;
     const double pi = (double)3.1415926535897932384626433832795028841971f;
@@ -1506,12 +1553,12 @@ static void set_trench(ora_t *o, int len, int len2, int len3)
     int lenh = lx / 2 - 1;
     int site[3], nextn[4][3];
     lg(o, " %d %d %d\n", lenh, len, len3);
-    for (int z = 0; z < lz; z++) {
+    for (int z = 0; z < lz && !sic; z++) {
         int t = z < len3 ? (int)(o->st_tbottom + (o->st_ttop - o->st_tbottom) * z / (len3 - 1)) : (int)o->st_ttop;
         for (int y = 0; y < ly; y++)
             for (int x = 0; x < lx; x++) mvbits(t, LEN_T, &o->latt[lidx(o, x, y, z)], POS_T);
     }
-    if (o->st_fixed) {
+    if (o->st_fixed && !sic) {
         st_interp(o, (int)o->st_ttop);
         for (int sp = 0; sp < NCRYSTAL_MAX; sp++) {
             double *e = &o->ptransE[sp][0][0][0][0][0][0];
@@ -1520,29 +1567,31 @@ static void set_trench(ora_t *o, int len, int len2, int len3)
             for (int c = 0; c < 3; c++) o->ptransD[sp][c] = st_mix(o, o->st_D[o->st_lo][sp][c], o->st_D[o->st_hi][sp][c]);
         }
     }
-    set_walls(o, 0, 3);
-    set_walls(o, lz - 4, lz - 1);
-    for (int z = 4; z <= 20; z++)
+    if (!sic) {
+        set_walls(o, 0, 3);
+        set_walls(o, lz - 4, lz - 1);
+    }
+    for (int z = sic ? 0 : 4; z <= 20; z++)
         for (int y = 0; y < ly; y++)
             for (int x = 0; x < lx; x++) {
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                *v = (int32_t)((uint32_t)*v | (1u << POS_SI) | (1u << POS_OCC));
+                *v = (int32_t)((uint32_t)*v | (1u << (sic && k == 2 ? POS_C : POS_SI)) | (1u << POS_OCC));
                 mvbits(4, LEN_COOR, v, POS_COOR);
                 site[0] = x; site[1] = y; site[2] = z;
                 std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
                 add_bulk(o, site, nextn);
             }
     for (int z = 21; z <= len3 - 1; z++) {
-        double half = (double)len - (double)(len3 - z) * cos(arad) / sin(arad);
+        double half = sic ? (double)len : (double)len - (double)(len3 - z) * cos(arad) / sin(arad);
         for (int y = 0; y < ly; y++)
             for (int x = 0; x < lx; x++) {
                 int k = dia_kind(x, y, z);
                 if (!k) continue;
                 if ((double)abs(x - lenh) <= half && z > len2 && z < len3) continue;
                 int32_t *v = &o->latt[lidx(o, x, y, z)];
-                *v = (int32_t)((uint32_t)*v | (1u << POS_SI) | (1u << POS_OCC));
+                *v = (int32_t)((uint32_t)*v | (1u << (sic && k == 2 ? POS_C : POS_SI)) | (1u << POS_OCC));
             }
     }
     coor_pass(o, 0, lx - 1, 0, ly - 1, 21, len3 + 9, 0);
@@ -2471,7 +2520,13 @@ int ora_init(ora_t *o)
     /* MS/main.f:224-295 */
     if (!strcmp(o->init_st, "FS")) {
         o->len1 -= o->len1 % 24;
-        set_flat(o, o->len1, 0);
+        set_flat(o, o->len1, 0, 1);
+    } else if (!strcmp(o->init_st, "Fw") || !strcmp(o->init_st, "Fa")) {   /* MS/main.f:228-236 */
+        o->len1 -= o->len1 % 24;
+        o->len2 -= o->len2 % 24;
+        o->len3 -= o->len3 % 24;
+        set_flat(o, o->len1, 1, 1);
+        set_wall_block(o, o->len2, o->init_st[1] == 'a' ? o->len3 : -1);
     } else if (!strcmp(o->init_st, "FF")) {      /* MS/main.f:273-278 */
         o->len1 -= o->len1 % 24;
         o->len2 -= o->len2 % 24;
@@ -2480,15 +2535,17 @@ int ora_init(ora_t *o)
         set_finfet(o, o->len1, o->len2, o->len3, o->len4);
     } else if (!strcmp(o->init_st, "F")) {
         o->len1 -= o->len1 % 24;
-        set_flat(o, o->len1, 1);
+        set_flat(o, o->len1, 1, 0);
     } else if (!strcmp(o->init_st, "C")) {       /* MS/main.f:261-262 */
-        set_nc(o, o->len1, o->len2, o->len3, 0);
-    } else if (!strcmp(o->init_st, "S")) {       /* MS/main.f:257-258 */
-        set_nc(o, o->len1, o->len1, o->len1, 1);
+        set_nc(o, o->len1, o->len2, o->len3, 0, 0);
+    } else if (!strcmp(o->init_st, "S") || !strcmp(o->init_st, "SS")) {   /* MS/main.f:257-260 */
+        set_nc(o, o->len1, o->len1, o->len1, 1, o->init_st[1] == 'S');
     } else if (!strcmp(o->init_st, "ST")) {      /* MS/main.f:265-266 */
-        set_trench(o, o->len1, o->len2, o->len3);
-    } else if (!strcmp(o->init_st, "I")) {       /* MS/main.f:245-246 */
-        set_invp(o, o->len1, o->len2);
+        set_trench(o, o->len1, o->len2, o->len3, 0);
+    } else if (!strcmp(o->init_st, "T")) {       /* MS/main.f:263-264 */
+        set_trench(o, o->len1, o->len2, o->len3, 1);
+    } else if (o->init_st[0] && strchr("IDZJKL", o->init_st[0]) && o->init_st[1] == 0) {   /* MS/main.f:245-256 */
+        set_invp(o, o->len1, o->len2, o->init_st[0]);
     } else if (!strcmp(o->init_st, "LA")) {      /* MS/main.f:287-291 */
         if (!o->la_geo) ora_fail(o, "InitSt LA needs the geometry and temperature input (ora_set_la_input)");
         set_cad(o, 1);

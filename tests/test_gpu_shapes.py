@@ -290,3 +290,34 @@ def test_mulskips_e_sige(oracle_lib, tmp_path):
     assert [l.split()[1:] for l in mine[2:]] == [l.split()[1:] for l in ref[2:]]
     sym = [l.split()[0] for l in mine[2:]]
     assert set(sym) <= {"Si", "Ge"} and 0.25 < sym.count("Ge") / len(sym) < 0.35
+
+
+NEW_SHAPES = [("SS", (96, 0, 0)), ("D", (24, 90, 0)), ("Z", (24, 90, 0)), ("J", (24, 90, 0)), ("K", (24, 90, 0)),
+              ("L", (24, 90, 0)), ("T", (30, 40, 90)), ("Fw", (130, 170, 0)), ("Fa", (130, 170, 75))]
+
+
+@pytest.mark.parametrize("kind,lens", NEW_SHAPES, ids=[k for k, _ in NEW_SHAPES])
+def test_mulskips_e_shape_variants(oracle_lib, tmp_path, kind, lens):
+    """mulskips.e with the other shaped InitSt of main.f:224-278 (SetNCSpSi,
+    the inverted-pyramid variants, SetTrench, SetSiC3Cww and its aperture
+    form): the initial frame equals the oracle's, and the run goes on."""
+    from mulskips_gb300.startdat import write_startdat
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1600.0))
+    d = tmp_path / kind
+    d.mkdir()
+    write_startdat(str(d / "start.dat"), E, np.full((3, 3), 0.5), ncrystal=2, list_crystal=(14, 6), init_st=kind,
+                   len1=lens[0], lens=lens[1:], max_iter=4000, run_type="T")
+    o = oracle_lib.Oracle(str(d / "start.dat"), 240, 240, 240)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="240 240 240"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+    assert int((d / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 4000

@@ -202,3 +202,31 @@ def test_undefined_inputs_refused_by_both(helper, tmp_path):
     write_points(tmp_path / "p.xyz", xyz2, np.append(sym, "Si"))
     rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
     assert "product: an atom off the diamond sites" in out, out
+
+
+# InitSt, (Len1, Len2, Len3) in a 240^3 box: the variants of the reference's
+# shaped initializers (MS/main.f:224-278) besides those its regression cases
+# pin (cube, sphere, inverted-pyramid, finfet), which are covered again here
+SHAPES = [("C", (60, 72, 48)), ("S", (96, 0, 0)), ("SS", (96, 0, 0)), ("I", (24, 90, 0)),
+          ("D", (24, 90, 0)), ("Z", (24, 90, 0)), ("J", (24, 90, 0)), ("K", (24, 90, 0)),
+          ("L", (24, 90, 0)), ("T", (30, 40, 90)), ("Fw", (130, 170, 0)), ("Fa", (130, 170, 75))]
+
+
+@pytest.mark.parametrize("kind,lens", SHAPES, ids=[k for k, _ in SHAPES])
+def test_library_shapes_equal_oracle(helper, tmp_path, kind, lens):
+    """The one-byte shaped initializers (mks_shapes::build_shape, the code
+    behind mks_init_shape) against the oracle's list-based restatements, every
+    site byte, 3C-SiC rates."""
+    from mulskips_gb300.startdat import write_startdat
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1600.0))
+    p = str(tmp_path / "start.dat")
+    write_startdat(p, E, np.full((3, 3), 0.5), ncrystal=2, list_crystal=(14, 6), init_st=kind, len1=lens[0],
+                   lens=lens[1:], run_type="T")
+    r = subprocess.run([helper, p, NUMBERS, "@" + kind, "240", "240", "240", *[str(v) for v in lens]],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    assert r.returncode == 0 and "mismatch 0" in r.stdout, r.stdout
