@@ -2800,8 +2800,11 @@ int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const 
     if (!h || n < 0 || (n && (!xyz || !species)) || rep < 0 || rep >= (int)h->reps.size())
         return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[rep];
-    for (int64_t i = 0; i < n; i++)
-        if (species[i] > r.cfg.ncrystal) return fail(MKS_ERR_ARG, "point %lld: species %d > NCrystal", (long long)i, species[i]);
+    for (int64_t i = 0; i < n; i++) {   // a wall point's species is not read (SetShape.f:58-62)
+        const int z = xyz[3 * i + 2];
+        if (z > 3 && z < r.cfg.lenz - 4 && species[i] > r.cfg.ncrystal)
+            return fail(MKS_ERR_ARG, "point %lld: species %d > NCrystal", (long long)i, species[i]);
+    }
     mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
     if (const char *e = mks_shapes::set_points(g, xyz, species, n)) return fail(MKS_ERR_UNSUPPORTED, "SetShape: %s", e);
     std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
