@@ -229,9 +229,20 @@ Input read_startdat(const char *path)
     in.run_type = r.items(1)[0].substr(0, 2);
     in.idum = atoll(r.items(1)[0].c_str());
     in.save_final = r.items(1)[0].substr(0, 2);
-    if (in.save_final == "T") r.line(in.restart_file);
+    // READ(IPF,'(A)') file names; OPEN drops the blanks around them
+    auto trim = [](std::string &t) {
+        while (!t.empty() && isspace((unsigned char)t.back())) t.pop_back();
+        while (!t.empty() && isspace((unsigned char)t.front())) t.erase(t.begin());
+    };
+    if (in.save_final == "T") {
+        r.line(in.restart_file);
+        trim(in.restart_file);
+    }
     in.save_coo = r.items(1)[0].substr(0, 2);
-    if (in.save_coo == "T") r.line(in.coo_file);
+    if (in.save_coo == "T") {
+        r.line(in.coo_file);
+        trim(in.coo_file);
+    }
     else if (in.init_st == "LA") die("ERR: SaveCoo flag must be \"T\" for LA simulations!");   // main.f:204-208
     if (in.init_st == "ST") {
         // SetProbabilityFromField.f:23-171: the table file named on the next
@@ -393,7 +404,33 @@ int main()
         fclose(tf);
         check(mks_batch_set_field(h, 0, field.data()));
     }
-    if (in.init_st == "IN" || in.init_st == "LA") {   // SetCAD.f:155-236: one record per layer z
+    if ((in.init_st == "IN" || in.init_st == "LA") && in.run_type == "C") {
+        // continuation run (SetCAD.f:54-80, main.f:178-182): LattCoo from the
+        // checkpoint file named in start.dat, one record of LenX*LenY words
+        // per layer z (the dump of main.f:385-403); the lists are rebuilt from
+        // it as after a fresh start (SetCAD.f:302-410), the LA temperatures
+        // stay those of TempStat
+        printf(" ATTENTION!!! You have chosen a continuation run. LattCoo will be read from the following "
+               "checkpoint file: %s\n", in.cad_file.c_str());
+        FILE *cf = fopen(in.cad_file.c_str(), "r");
+        if (!cf) die("cannot open the checkpoint file");
+        std::vector<int32_t> lc((size_t)lx * ly * (lz + 1), 0);
+        std::vector<char> line((size_t)lx * ly * 16 + 4096);
+        for (int z = 0; z < lz; z++) {
+            if (!fgets(line.data(), (int)line.size(), cf)) die("checkpoint file: too few records");
+            char *p = line.data();
+            for (size_t k = 0; k < (size_t)lx * ly; k++) {
+                char *e;
+                long v = strtol(p, &e, 10);
+                if (e == p) die("checkpoint file: short record");
+                lc[(size_t)lx * ly * z + k] = (int32_t)v;
+                p = e;
+            }
+        }
+        fclose(cf);
+        printf(" Done reading checkpoint file\n");
+        check(mks_load_lattice(h, lc.data()));
+    } else if (in.init_st == "IN" || in.init_st == "LA") {   // SetCAD.f:155-236: one record per layer z
         printf(" Reading input geometry file: %s\n", in.cad_file.c_str());
         FILE *gf = fopen(in.cad_file.c_str(), "r");
         if (!gf) die("cannot open the geometry file");

@@ -324,3 +324,48 @@ def test_mulskips_e_shape_variants(oracle_lib, tmp_path, kind, lens):
     assert r.returncode == 0, r.stdout[-3000:]
     assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
     assert int((d / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 300
+
+
+def test_mulskips_e_continuation_run(tmp_path):
+    """RunType C (main.f:178-182, SetCAD.f:54-80): a CAD run with one
+    coverage species saves its final LattCoo (main.f:385-403), and a
+    continuation run started from that checkpoint writes, as its initial
+    frame, the final frame of the first run."""
+    geo = _cad_geometry()
+    d1, d2 = tmp_path / "first", tmp_path / "cont"
+    d1.mkdir()
+    d2.mkdir()
+    with open(d1 / "LattGeo.dat", "w") as f:
+        for z in range(geo.shape[0]):
+            f.write(" ".join(map(str, geo[z].reshape(-1).tolist())) + "\n")
+
+    def startdat(run_type, cadfile, save):
+        out = []
+        for line in open(os.path.join(GOLDEN, "CAD", "start.dat")).read().splitlines():
+            if "LattGeo" in line:
+                line = cadfile
+            elif "! IterMax" in line:
+                line = "4000 ! IterMax"
+            elif "! OutMolMol" in line:
+                line = "4000 ! OutMolMol"
+            elif "! RunType" in line:
+                line = f"{run_type} ! RunType"
+            elif "! Save final state" in line and save:
+                out.append("T ! Save final state")
+                line = "final.dat  "
+            out.append(line)
+        return "\n".join(out) + "\n"
+
+    (d1 / "start.dat").write_text(startdat("R", "LattGeo.dat", True))
+    env = dict(os.environ, MULSKIPS_BOX="480 240 240")
+    r = subprocess.run([EXE], cwd=d1, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert len((d1 / "final.dat").read_text().splitlines()) == 240
+    (d2 / "start.dat").write_text(startdat("C", str(d1 / "final.dat"), False))
+    r = subprocess.run([EXE], cwd=d2, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert "continuation run" in r.stdout
+    last = (d1 / "I00000001.xyz").read_text().splitlines()
+    first = (d2 / "I00000000.xyz").read_text().splitlines()
+    assert first[0].split()[0] == last[0].split()[0] and first[1:] == last[1:]
+    assert int((d2 / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 4000
