@@ -331,10 +331,19 @@ struct Frames {
                    " wireframe 12\n color atom purple\n set bondmode and\n",
                 base.c_str());
         fclose(f);
-        f = fopen("movie.mos", "a");
+        // movie.mos is first opened at its start (the old content goes), then
+        // kept open in APPEND position between frames (WriteMolMolSource.f:74,
+        // :104-109); DefAtEnergy.dat gets one blank record per frame, each
+        // written from the start of the file (:75, :101-102)
+        f = fopen("movie.mos", first ? "w" : "a");
         fprintf(f, " source    %s.src\n write gif %s.gif\n zap\n", base.c_str(), base.c_str());
         fclose(f);
+        f = fopen("DefAtEnergy.dat", "w");
+        fputs(" \n", f);
+        fclose(f);
+        first = false;
     }
+    bool first = true;
 };
 
 }  // namespace
@@ -343,6 +352,7 @@ int main()
 {
     int lx, ly, lz;
     box_size(lx, ly, lz);
+    if (FILE *rt = fopen("Run_time.dat", "w")) fclose(rt);   // FileOpen.f:47, nothing is written to it
     printf(" KMC box size: %d %d %d\n", lx, ly, lz);
     Input in = read_startdat("start.dat");
     printf(" Crystal species (NCrystal= %d ) --> Z: %d %d %d\n", in.ncrystal, in.list_crystal[0], in.list_crystal[1],

@@ -41,6 +41,13 @@ def test_initial_frame_identical_and_run_completes(tmp_path):
     assert "NatNvoidNad" in r.stdout and "Atoms,Voids,AdAtoms" in r.stdout
     for name in ("I00000000_d.xyz", "I00000000_v.xyz", "I00000000.src", "movie.mos"):
         assert (d / name).exists()
+    # movie.mos starts over in each run and lists every frame once;
+    # DefAtEnergy.dat holds one blank record, Run_time.dat nothing
+    assert (d / "movie.mos").read_text().count("zap") == 2
+    assert (d / "DefAtEnergy.dat").read_text() == " \n"
+    assert (d / "Run_time.dat").read_text() == ""
+    r = run_exe(d)
+    assert r.returncode == 0 and (d / "movie.mos").read_text().count("zap") == 2
 
 
 def test_run_mulskips_wrapper_etch_stop(tmp_path):
