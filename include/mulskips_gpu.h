@@ -306,6 +306,11 @@ int mks_init_shape(mks_handle *h, const char *init_st, const int32_t *lens, cons
  * grid point, int8 [z][y][x] (LenZ*LenY*LenX; 1 Si, 10 wall, 0 empty; the
  * layers z <= 3 and >= LenZ-4 are walls whatever they hold).  NCrystal = 1. */
 int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo);
+/* SetCAD for InitSt IN with the alloy fraction of a SiGe start.dat
+ * (SetCAD.f:215-222): each Si site takes species 2 with probability x.  The
+ * reference draws with the compiler's RAND(); here a generator seeded by
+ * seed.  NCrystal >= 2 when x > 0.                                        */
+int mks_batch_init_cad_alloy(mks_handle *h, int32_t rep, const int8_t *geo, double x, uint64_t seed);
 /* SetShape for InitSt SH (SetShape.f:25-436): n grid points xyz[3*i..3*i+2]
  * = (x, y, z), 0 <= x < LenX, 0 <= y < LenY, 0 <= z <= LenZ, with
  * species[i] 1 (Si) or 2 (C / Ge); the points of the reference's point-list

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mks_batch_init_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_void_p, C.c_void_p]),
     "mks_init_shape": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p]),
     "mks_batch_init_cad": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "mks_batch_init_cad_alloy": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_uint64]),
     "mks_batch_init_points": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_init_points": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]),
     "mks_batch_init_cad_la": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_double]),

@@ -2795,6 +2795,21 @@ int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
     return mks_batch_init_cad_la(h, rep, geo, -1, 0.0, 0.0);
 }
 
+int mks_batch_init_cad_alloy(mks_handle *h, int32_t rep, const int8_t *geo, double x, uint64_t seed)
+{
+    if (!h || !geo || rep < 0 || rep >= (int)h->reps.size() || !(x >= 0.0 && x <= 1.0))
+        return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    if (r.cfg.ncrystal < 2 && x > 0.0) return fail(MKS_ERR_ARG, "an alloy needs NCrystal >= 2");
+    mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
+    mks_shapes::set_cad(g, geo, mks_shapes::CadLA(), x, seed);
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
+    return upload_compact(h, rep, st);
+}
+
 int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const int8_t *species, int64_t n)
 {
     if (!h || n < 0 || (n && (!xyz || !species)) || rep < 0 || rep >= (int)h->reps.size())

@@ -284,8 +284,8 @@ inline void set_flat_ww(Grid &g, int len, int lenww, int lap)
 // LenZ-4..LenZ-1; from the geometry id of every grid point (geo[(z * LenY +
 // y) * LenX + x], z = 4..LenZ-5): 10 a wall, 1 Si on both sublattices; then
 // the coordination pass with the wall rules over the whole box.  The alloy
-// draw of SetCAD.f:215-222 uses the compiler's RAND stream and is not taken
-// (alloy fraction 0).
+// draw of SetCAD.f:215-222 uses the compiler's RAND stream; here it is the
+// seeded cad_draw (alloy fraction > 0, InitSt IN).
 // With la, the Si sites of InitSt LA (SetCAD.f:166-212): kept below
 // LenZ - INT((LenVac + LenNuc)/sf) when homogeneous, else outside the ball of
 // radius LenNuc/sf around (LenX/2, LenY/2, LenZ - INT(LenVac/sf)).
@@ -294,7 +294,19 @@ struct CadLA {
     double len_vac = 0.0, len_nuc = 0.0, sf = 1.0;
 };
 
-inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA())
+// With alloy > 0 (InitSt IN only, SetCAD.f:215-222) each Si site of id 1
+// takes species 2 when its draw u < alloy; u is the reference's RAND(), here
+// a splitmix64 hash of (seed, grid point).
+inline double cad_draw(uint64_t seed, uint64_t k)
+{
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA(), double alloy = 0.0, uint64_t seed = 0)
 {
     const int zmax = g.lz - (int)((la.len_vac + la.len_nuc) / la.sf);
     const int x0 = g.lx / 2, y0 = g.ly / 2, z0 = g.lz - (int)(la.len_vac / la.sf);
@@ -319,7 +331,11 @@ inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA())
                         long d2 = (long)(x - x0) * (x - x0) + (long)(y - y0) * (y - y0) + (long)(z - z0) * (z - z0);
                         occ = d2 > r2;
                     }
-                    if (occ) *v = mks::mk(1, 0, 0, 0);
+                    if (occ) {
+                        int sp = 1;
+                        if (alloy > 0.0 && cad_draw(seed, ((uint64_t)z * g.ly + y) * g.lx + x) < alloy) sp = 2;
+                        *v = mks::mk(sp, 0, 0, 0);
+                    }
                 }
             }
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 0, g.lz - 1, true);

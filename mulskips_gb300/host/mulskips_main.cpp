@@ -373,8 +373,8 @@ int main()
         in.init_st != "SH" && !shaped)
         die("initialization not_implemented in the GPU engine (A and E are not: FS, F, Fw, Fa, SG, C, S, SS, I, D, Z, "
             "J, K, L, T, FF, ST, IN, SH and LA are)");
-    if (in.alloy > 0.0 && (in.init_st == "IN" || in.init_st == "LA"))
-        die("ERR: SetCAD with an alloy fraction > 0 is not built (it draws the species from the compiler's RAND)");
+    if (in.alloy > 0.0 && in.init_st == "LA")   // SetCAD.f:142,161 read LenSiGe, which nothing sets
+        die("ERR: InitSt LA with an alloy fraction > 0 is not built (SetCAD reads an unset LenSiGe there)");
     mks_config cfg;
     memset(&cfg, 0, sizeof cfg);
     cfg.lenx = lx;
@@ -462,6 +462,8 @@ int main()
         printf(" Done reading input geometry file\n");
         if (in.init_st == "LA")
             check(mks_batch_init_cad_la(h, 0, geo.data(), in.homogeneous ? 1 : 0, in.len_vac, in.len_nuc));
+        else if (in.alloy > 0.0 || in.ncrystal > 1)   // SetCAD.f:215-222, the RAND() draw seeded by IDUM here
+            check(mks_batch_init_cad_alloy(h, 0, geo.data(), in.alloy, (uint64_t)in.idum));
         else
             check(mks_batch_init_cad(h, 0, geo.data()));
     } else if (in.init_st == "SH") {                  // main.f:281-286, SetShape.f:52-79

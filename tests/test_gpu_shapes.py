@@ -369,3 +369,46 @@ def test_mulskips_e_continuation_run(tmp_path):
     first = (d2 / "I00000000.xyz").read_text().splitlines()
     assert first[0].split()[0] == last[0].split()[0] and first[1:] == last[1:]
     assert int((d2 / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 4000
+
+
+def test_mulskips_e_cad_sige(oracle_lib, tmp_path):
+    """InitSt IN with a SiGe start.dat and alloy fraction 0.3 (SetCAD.f:215-222):
+    the sites of the CAD geometry's Si, Ge drawn on each at the fraction (the
+    reference draws with RAND(), here a seeded generator)."""
+    from mulskips_gb300.startdat import write_startdat
+    geo = _cad_geometry()
+    d = tmp_path / "sige"
+    d.mkdir()
+    with open(d / "LattGeo.dat", "w") as f:
+        for z in range(geo.shape[0]):
+            f.write(" ".join(map(str, geo[z].reshape(-1).tolist())) + "\n")
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.7 * (n1 + n2) / (8.617e-5 * 1000.0))
+
+    def with_geometry(path, ncrystal, lc, alloy):
+        write_startdat(str(path), E, np.full((3, 3), 0.5), ncrystal=ncrystal, list_crystal=lc, init_st="IN",
+                       max_iter=300, run_type="T", alloy_fraction=alloy)
+        lines = open(path).read().splitlines()
+        lines[3] = "LattGeo.dat"
+        open(path, "w").write("\n".join(lines) + "\n")
+
+    with_geometry(d / "start.dat", 2, (14, 32), 0.3)
+    with_geometry(tmp_path / "si.dat", 1, (14,), 0.0)
+    o = oracle_lib.Oracle(str(tmp_path / "si.dat"), 480, 240, 240)
+    o.set_geometry(geo)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX="480 240 240"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    mine = (d / "I00000000.xyz").read_text().splitlines()
+    ref = (tmp_path / "ora.xyz").read_text().splitlines()
+    assert len(mine) == len(ref) and mine[0] == ref[0]
+    assert [l.split()[1:] for l in mine[2:]] == [l.split()[1:] for l in ref[2:]]
+    sym = [l.split()[0] for l in mine[2:]]
+    assert set(sym) <= {"Si", "Ge"} and 0.25 < sym.count("Ge") / len(sym) < 0.35
