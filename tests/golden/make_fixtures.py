@@ -29,6 +29,9 @@ Fixtures written:
   refwriter/start.dat    start.dat written by the reference's
                          pymulskips.setuprun.run_mulskips (setup_only) for the
                          plain Si(001) process object of mulskips_gb300.setuprun
+  refwriter/{cvd,in_sige,la}.dat
+                         the same writer for the process objects of
+                         process_stubs.py (REF_WRITER_CASES below)
 """
 import gzip
 import os
@@ -133,6 +136,37 @@ def reference_writer():
         d = os.path.join(HERE, "refwriter")
         os.makedirs(d, exist_ok=True)
         shutil.copyfile(os.path.join(tmp, "ref", "start.dat"), os.path.join(d, "start.dat"))
+    # the other layouts of the writer: coverage species (CVD), a SiGe crystal
+    # with a geometry file (IN), and the LA block (file names are written
+    # under $PWD, kept here as PWD/<name>; the tests compare base names)
+    sys.path.insert(0, HERE)
+    import process_stubs as ps
+    for name, kw in REF_WRITER_CASES.items():
+        kw = dict(kw)
+        kw["mp"] = getattr(ps, kw["mp"])()
+        with tempfile.TemporaryDirectory() as tmp:
+            try:
+                ref_setup.run_mulskips(execpath=tmp, runpath=os.path.join(tmp, "ref"), setup_only=True, **kw)
+            finally:
+                os.chdir(cwd)
+            txt = open(os.path.join(tmp, "ref", "start.dat")).read()
+        pwd = os.environ.get("PWD", cwd)
+        with open(os.path.join(HERE, "refwriter", name + ".dat"), "w") as f:
+            f.write(txt.replace(pwd + "/", "PWD/"))
+
+
+# run_mulskips arguments of the extra writer fixtures (mp names a class of
+# process_stubs.py)
+REF_WRITER_CASES = {
+    "cvd": dict(Simulation="FS", mp="CVD", ExitStrategy="Time", TotTime=3.0, OutTime=1.0,
+                Seed_box=[48, 48, 48], RunType="R", IDUM=7),
+    "in_sige": dict(Simulation="IN", mp="PVD", ExitStrategy="Iter", OutMolMol=1000, IterMax=4000,
+                    cadfilename="geo.dat", RunType="T", IDUM=9, SaveFinalState=True, restartfilename="final.dat"),
+    "la": dict(Simulation="LA", mp="PhaseChange", ExitStrategy="Time", TotTime=1e-8, OutTime=1e-9,
+               cadfilename="LattGeo.dat", tempfilename="TempStat.dat", LenVac=10.0, LenNuc=20.0,
+               initialState="inhomogeneous", LenSiGe=0.0, SaveCoo=True, coofilename="LattStat.dat",
+               restartfilename="restart.dat", RunType="R", IDUM=3),
+}
 
 
 if __name__ == "__main__":

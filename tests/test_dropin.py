@@ -54,3 +54,26 @@ def test_setup_src_writes_box_and_make_log(tmp_path):
     assert "Compilation terminated" in open(tmp_path / "make.log").read()
     with pytest.raises(ValueError):
         setup_mulskips_src(str(tmp_path), 100, 240, 480)
+
+
+@pytest.mark.parametrize("name", ["cvd", "in_sige", "la"])
+def test_startdat_layouts_match_reference_writer(tmp_path, name):
+    """The writer's other layouts against the reference's own
+    run_mulskips(setup_only=True) output for the same process objects
+    (tests/golden/refwriter/<name>.dat, tests/golden/make_fixtures.py):
+    coverage rates, a SiGe geometry run with its Ge fraction and checkpoint,
+    the LA block.  File names are compared by base name (the reference writes
+    them under the caller's $PWD)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_fixtures
+    import process_stubs
+    from mulskips_gb300.setuprun import run_mulskips
+    kw = dict(make_fixtures.REF_WRITER_CASES[name])
+    kw["mp"] = getattr(process_stubs, kw["mp"])()
+    run_mulskips(runpath=str(tmp_path / "ours"), setup_only=True, **kw)
+
+    def norm(path):
+        return [[os.path.basename(t) if "/" in t else t for t in toks] for toks in first_tokens(path)]
+
+    assert norm(os.path.join(GOLDEN, "refwriter", name + ".dat")) == norm(tmp_path / "ours" / "start.dat")
