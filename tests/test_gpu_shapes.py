@@ -412,3 +412,36 @@ def test_mulskips_e_cad_sige(oracle_lib, tmp_path):
     assert [l.split()[1:] for l in mine[2:]] == [l.split()[1:] for l in ref[2:]]
     sym = [l.split()[0] for l in mine[2:]]
     assert set(sym) <= {"Si", "Ge"} and 0.25 < sym.count("Ge") / len(sym) < 0.35
+
+
+def test_run_mulskips_la_call(tmp_path, monkeypatch):
+    """The pymulskips-style LA call: mulskips_gb300.setuprun.run_mulskips
+    writes the LA start.dat (energetics, files, LA block, the layout the
+    reference writer gives) and runs mulskips.e on the geometry and
+    temperature files, which writes the phases file."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import process_stubs
+    from mulskips_gb300.setuprun import run_mulskips
+    L = 120
+    layers = np.where(np.arange(L) < 100, 1, 10).astype(np.int8)
+    layers[:4] = 10
+    T = np.where(layers == 10, 10, (1650 + 0.1 * np.arange(L)).astype(np.int64))
+    work = tmp_path / "inputs"
+    work.mkdir()
+    with open(work / "LattGeo.dat", "w") as fg, open(work / "TempStat.dat", "w") as ft:
+        for z in range(L):
+            fg.write(" ".join([str(int(layers[z]))] * (L * L)) + "\n")
+            ft.write(" ".join([str(int(T[z]))] * (L * L)) + "\n")
+    monkeypatch.chdir(work)
+    monkeypatch.setenv("PWD", str(work))
+    monkeypatch.setenv("MULSKIPS_BOX", f"{L} {L} {L}")
+    ok = run_mulskips(execpath=os.path.dirname(EXE), runpath=str(tmp_path / "run"), Simulation="LA",
+                      mp=process_stubs.PhaseChange(), ExitStrategy="Time", TotTime=0.02, OutTime=0.01,
+                      cadfilename="LattGeo.dat", tempfilename="TempStat.dat", LenVac=10.0, LenNuc=20.0,
+                      initialState="inhomogeneous", LenSiGe=0.0, SaveCoo=True, coofilename="LattStat.dat",
+                      restartfilename="restart.dat", RunType="R", IDUM=3)
+    log = open(tmp_path / "run" / "log.txt").read()
+    assert ok, log[-3000:]
+    assert len(open(work / "LattStat.dat").read().splitlines()) == L
+    assert (tmp_path / "run" / "I00000001.xyz").exists()
