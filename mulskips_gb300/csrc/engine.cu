@@ -2543,6 +2543,18 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
 
 int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st);
 
+// A host-built lattice (mks_shapes::Grid, rows of NA bytes) into the padded
+// rows of replica rep, then upload_compact.
+int upload_grid(mks_handle *h, int rep, const mks_shapes::Grid &g)
+{
+    const RepHost &r = h->reps[rep];
+    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
+    for (int z1 = 0; z1 < r.NZ; z1++)
+        for (int b = 0; b < r.NB; b++)
+            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
+    return upload_compact(h, rep, st);
+}
+
 int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
 {
     const RepHost &r = h->reps[rep];
@@ -2758,11 +2770,7 @@ int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const 
     char msg[160];
     if (int e = mks_shapes::build_shape(g, kind, lens, params, temp, msg, sizeof msg))
         return fail(e == 2 ? MKS_ERR_UNSUPPORTED : MKS_ERR_ARG, "%s", msg);
-    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
-    for (int z1 = 0; z1 < r.NZ; z1++)
-        for (int b = 0; b < r.NB; b++)
-            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
-    int rc = upload_compact(h, rep, st);
+    int rc = upload_grid(h, rep, g);
     if (rc) return rc;
     if (kind == "ST")   // the temperatures of SetTrenchSi.f:46-63 as the replica's field
         return set_temperature_impl(h, rep, [&](int, int, int z, int) { return temp[(size_t)z] & 8191; });
@@ -2783,11 +2791,7 @@ int mks_batch_init_cad_la(mks_handle *h, int32_t rep, const int8_t *geo, int32_t
     la.len_nuc = len_nuc;
     la.sf = r.cfg.sf;
     mks_shapes::set_cad(g, geo, la);
-    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
-    for (int z1 = 0; z1 < r.NZ; z1++)
-        for (int b = 0; b < r.NB; b++)
-            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
-    return upload_compact(h, rep, st);
+    return upload_grid(h, rep, g);
 }
 
 int mks_batch_init_cad(mks_handle *h, int32_t rep, const int8_t *geo)
@@ -2803,11 +2807,7 @@ int mks_batch_init_cad_alloy(mks_handle *h, int32_t rep, const int8_t *geo, doub
     if (r.cfg.ncrystal < 2 && x > 0.0) return fail(MKS_ERR_ARG, "an alloy needs NCrystal >= 2");
     mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
     mks_shapes::set_cad(g, geo, mks_shapes::CadLA(), x, seed);
-    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
-    for (int z1 = 0; z1 < r.NZ; z1++)
-        for (int b = 0; b < r.NB; b++)
-            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
-    return upload_compact(h, rep, st);
+    return upload_grid(h, rep, g);
 }
 
 int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const int8_t *species, int64_t n)
@@ -2822,11 +2822,7 @@ int mks_batch_init_points(mks_handle *h, int32_t rep, const int32_t *xyz, const 
     }
     mks_shapes::Grid g(r.cfg.lenx, r.cfg.leny, r.cfg.lenz);
     if (const char *e = mks_shapes::set_points(g, xyz, species, n)) return fail(MKS_ERR_UNSUPPORTED, "SetShape: %s", e);
-    std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
-    for (int z1 = 0; z1 < r.NZ; z1++)
-        for (int b = 0; b < r.NB; b++)
-            memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
-    return upload_compact(h, rep, st);
+    return upload_grid(h, rep, g);
 }
 
 int mks_init_points(mks_handle *h, const int32_t *xyz, const int8_t *species, int64_t n)
