@@ -371,18 +371,27 @@ inline const char *set_points(Grid &g, const int32_t *xyz, const int8_t *sp, int
         if (sp[i] != 1 && sp[i] != 2) return "an atom symbol other than Si, C or Ge";
         *v = mks::mk(mks::sp_of(*v) | sp[i], 0, 0, 0);
     }
-    // an off-site wall point within an atom's |d|^2 = 27 shell would count as
-    // a neighbour the one-byte lattice cannot list
-    for (int64_t i : offsite)
-        for (int k = -5; k <= 5; k++)
-            for (int j = -5; j <= 5; j++)
-                for (int l = -5; l <= 5; l++) {
-                    if (l * l + j * j + k * k != 27) continue;
-                    const int z = xyz[3 * i + 2] + k;
-                    if (z < 4 || z > g.lz - 5) continue;
-                    uint8_t *v = g.at(((xyz[3 * i] + l) % g.lx + g.lx) % g.lx, ((xyz[3 * i + 1] + j) % g.ly + g.ly) % g.ly, z);
-                    if (v && *v != WALL && occupied(*v)) return "an atom next to an off-site wall point";
+    // an off-site wall point within an atom's |d|^2 = 27 shell (the 32
+    // offsets of SetShape.f:87-99) would count as a neighbour the one-byte
+    // lattice cannot list
+    int shell[32][3], ns = 0;
+    for (int k = -5; k <= 5; k++)
+        for (int j = -5; j <= 5; j++)
+            for (int l = -5; l <= 5; l++)
+                if (l * l + j * j + k * k == 27) {
+                    shell[ns][0] = l;
+                    shell[ns][1] = j;
+                    shell[ns][2] = k;
+                    ns++;
                 }
+    for (int64_t i : offsite)
+        for (int q = 0; q < ns; q++) {
+            const int z = xyz[3 * i + 2] + shell[q][2];
+            if (z < 4 || z > g.lz - 5) continue;
+            uint8_t *v = g.at(((xyz[3 * i] + shell[q][0]) % g.lx + g.lx) % g.lx,
+                              ((xyz[3 * i + 1] + shell[q][1]) % g.ly + g.ly) % g.ly, z);
+            if (v && *v != WALL && occupied(*v)) return "an atom next to an off-site wall point";
+        }
     auto is_atom = [](uint8_t v) { return v != WALL && (v & 3) != 0; };
     for (int z1 = 0; z1 < g.NZ; z1++)
         for (int b = 0; b < g.NB; b++)

@@ -197,6 +197,12 @@ def test_undefined_inputs_refused_by_both(helper, tmp_path):
     sic_startdat(str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
     rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
     assert "product: an atom with fewer than two neighbours" in out and "oracle: ok" not in out, out
+    # an off-site wall point in the 32-site shell of the atom at (6, 0, 6): a
+    # fifth neighbour for the reference, refused by the library
+    xyz3 = np.vstack([xyz, [[5, 1, 1]]])
+    write_points(tmp_path / "p.xyz", xyz3, np.append(sym, "Si"))
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    assert "product: an atom next to an off-site wall point" in out and "oracle: ok" not in out, out
     # an atom off the diamond sites: the one-byte lattice refuses it
     xyz2 = np.vstack([xyz, [[1, 1, 30]]])
     write_points(tmp_path / "p.xyz", xyz2, np.append(sym, "Si"))
