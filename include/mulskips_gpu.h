@@ -17,8 +17,16 @@
  *                                absorption.f and desorption.f
  *   mks_init_flat                SetSi / SetSiC3C (SetSi.f:25-221,
  *                                SetSiC3C.f:25-199), main.f:237-239,224-226
+ *   mks_init_shape               the shaped initializers of main.f:224-278
+ *                                (SetNC, SetNCSp(Si), SetInvPOff and its
+ *                                variants, SetTrench(Si), SetSiC3Cww(aperture),
+ *                                SetSiFINFET)
+ *   mks_batch_init_cad(_la,      SetCAD (SetCAD.f:80-341) for InitSt IN, with
+ *     _alloy)                    SetT and the molten nucleus for LA
+ *   mks_init_points              SetShape (SetShape.f:25-436, InitSt SH)
  *   mks_load_lattice             continuation / CAD load of LattCoo
  *                                (SetCAD.f:54-79,301-418)
+ *   mks_write_frame              WriteMolMolXYZFile.f:22-406
  *   mks_get_lattice              LattCoo dump (main.f:385-403)
  *   mks_run                      the KMC loop main.f:304-371 (PickTreeEvent,
  *                                Deposition, Evaporation, Get_Prob, UpdateTree)
