@@ -141,6 +141,9 @@ int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
  * 5-6 first list entry, 7 dummy flag; 0x80 a wall); n >= mks_state_size(). */
 int64_t mks_state_size(mks_handle *h);
 int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
+/* The compact state of replica rep, NZ*NB*NA bytes (NA = LenX/6, NB = LenY/6,
+ * NZ = LenZ/3 + 1), in the layout of mks_get_state.                     */
+int mks_batch_get_state(mks_handle *h, int32_t rep, uint8_t *st, int64_t n);
 /* Upload compact state bytes (same layout); the per-tile bands are rebuilt. */
 int mks_set_state(mks_handle *h, const uint8_t *st, int64_t n);
 /* Double-buffered input: mks_prefetch_state starts copying a compact state

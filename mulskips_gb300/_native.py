@@ -102,6 +102,7 @@ SIGNATURES = {
     "mks_batch_load_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_init_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_char_p, C.c_void_p, C.c_void_p]),
+    "mks_batch_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "mks_init_shape": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p]),
     "mks_batch_init_cad": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "mks_batch_init_cad_alloy": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_uint64]),

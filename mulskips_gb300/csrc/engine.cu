@@ -2453,6 +2453,18 @@ int mks_get_state(mks_handle *h, uint8_t *out, int64_t n)
     return 0;
 }
 
+int mks_batch_get_state(mks_handle *h, int32_t rep, uint8_t *out, int64_t n)
+{
+    if (!h || !out || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    const RepHost &r = h->reps[rep];
+    const int64_t need = (int64_t)r.NZ * r.NB * r.NA;
+    if (n < need) return fail(MKS_ERR_ARG, "buffer of %lld bytes, %lld needed", (long long)n, (long long)need);
+    CK(cudaMemcpy2DAsync(out, r.NA, h->d_st + r.st_off, r.pitch, r.NA, (size_t)r.NZ * r.NB, cudaMemcpyDeviceToHost,
+                         h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
 int mks_prefetch_state(mks_handle *h, const uint8_t *in, int64_t n)
 {
     if (!h || !in || n < mks_state_size(h) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");

@@ -306,6 +306,32 @@ class Batch:
         lc = np.ascontiguousarray(lattcoo, dtype=np.int32)
         N.check(N.lib().mks_batch_load_lattice(self._h, int(rep), N.ptr(lc)))
 
+    def state(self, rep):
+        """The compact one-byte state of replica rep, [z1, b, a]."""
+        lx, ly, lz = self.boxes[rep]
+        a = np.empty((lz // 3 + 1, ly // 6, lx // 6), dtype=np.uint8)
+        N.check(N.lib().mks_batch_get_state(self._h, int(rep), N.ptr(a), a.size))
+        return a
+
+    def init_shape(self, rep, init_st, lens, params=None):
+        """Replica rep by one of the reference's shaped initializers
+        (Lattice.init_shape lists them)."""
+        l = np.zeros(4, dtype=np.int32)
+        l[:len(lens)] = lens
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        N.check(N.lib().mks_batch_init_shape(self._h, int(rep), init_st.encode(), N.ptr(l),
+                                             None if p is None else N.ptr(p)))
+
+    def init_cad(self, rep, geo, alloy=0.0, seed=0):
+        """Replica rep by SetCAD (InitSt IN) from the LattGeo id of every grid
+        point, [z, y, x]; with alloy > 0 species 2 is drawn on each Si site."""
+        g = np.ascontiguousarray(geo, dtype=np.int8)
+        if alloy > 0.0:
+            N.check(N.lib().mks_batch_init_cad_alloy(self._h, int(rep), N.ptr(g), float(alloy),
+                                                     int(seed) & 0xFFFFFFFFFFFFFFFF))
+        else:
+            N.check(N.lib().mks_batch_init_cad(self._h, int(rep), N.ptr(g)))
+
     def init_points(self, rep, xyz, species):
         """Replica rep by SetShape (InitSt SH) from grid points xyz [n, 3] with
         species 1 (Si) or 2 (C / Ge)."""

@@ -445,3 +445,43 @@ def test_run_mulskips_la_call(tmp_path, monkeypatch):
     assert ok, log[-3000:]
     assert len(open(work / "LattStat.dat").read().splitlines()) == L
     assert (tmp_path / "run" / "I00000001.xyz").exists()
+
+
+def test_batch_replicas_of_shapes_match_oracle(oracle_lib, tmp_path):
+    """Replicas of one batch built by different shaped initializers (an
+    antiphase-domain inverted pyramid and a SiC trench) and by SetShape, each
+    byte-identical to the oracle's lattice."""
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.startdat import parse_startdat, read_shape_points, write_startdat
+    from test_shape_points import pyramid_points, sic_startdat, write_points
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1600.0))
+    refs, paths = [], []
+    for k, (kind, lens) in enumerate((("K", (24, 90, 0)), ("T", (30, 40, 90)))):
+        p = tmp_path / f"{kind}.dat"
+        write_startdat(str(p), E, np.full((3, 3), 0.5), ncrystal=2, list_crystal=(14, 6), init_st=kind,
+                       len1=lens[0], lens=lens[1:], run_type="T")
+        o = oracle_lib.Oracle(str(p), 240, 240, 240)
+        o.init()
+        refs.append(oracle_lib.compact_state(o)[0])
+        o.close()
+    xyz, sym, _, _ = pyramid_points(240, 60, 54)
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    sic_startdat(str(tmp_path / "sh.dat"), str(tmp_path / "p.xyz"), 240)
+    o = oracle_lib.Oracle(str(tmp_path / "sh.dat"), 240, 240, 240)
+    o.init()
+    refs.append(oracle_lib.compact_state(o)[0])
+    o.close()
+    d = parse_startdat(str(tmp_path / "K.dat"))
+    b = Batch([(240, 240, 240)] * 3, seeds=[1, 2, 3], ncrystal=2, list_crystal=(14, 6), sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * 3), np.stack([d["ptransD"]] * 3))
+    b.init_shape(0, "K", [24, 90])
+    b.init_shape(1, "T", [30, 40, 90])
+    b.init_points(2, *read_shape_points(str(tmp_path / "p.xyz")))
+    for r in range(3):
+        assert np.array_equal(b.state(r), refs[r]), r
+    b.close()
