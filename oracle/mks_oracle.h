@@ -42,7 +42,9 @@ ora_t *ora_create(const char *startdat_path, const char *numbers_path,
 void ora_destroy(ora_t *o);
 const char *ora_last_error(void);
 
-/* Run the initializer named by InitSt (FS, F, C, S, LA supported).  0 on success. */
+/* Run the initializer named by InitSt (FS, F, Fw, Fa, C, S, SS, I, D, Z, J, K, L,
+ * T, ST, FF, IN, LA, SH; the point-list file of SH is read from the path named
+ * in start.dat).  0 on success. */
 int ora_init(ora_t *o);
 
 /* Input of InitSt 'LA' (SetT + SetCAD, fresh start, NCrystal 1), used by
