@@ -236,3 +236,26 @@ def test_library_shapes_equal_oracle(helper, tmp_path, kind, lens):
     r = subprocess.run([helper, p, NUMBERS, "@" + kind, "240", "240", "240", *[str(v) for v in lens]],
                        stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
     assert r.returncode == 0 and "mismatch 0" in r.stdout, r.stdout
+
+
+def test_oracle_ss_is_the_pinned_sphere_in_si(oracle_lib, tmp_path):
+    """SetNCSpSi (InitSt SS) against the sphere regression case (SetNCSp,
+    pinned byte for byte): the same sites, coordinations and first list
+    entries, every atom Si."""
+    src = os.path.join(GOLDEN, "sphere", "start.dat")
+    lines = open(src).read().splitlines()
+    assert lines[2].split()[0] == "S"
+    lines[2] = "SS ! Initstat"
+    (tmp_path / "ss.dat").write_text("\n".join(lines) + "\n")
+    o = oracle_lib.Oracle(src, 480, 480, 480)
+    o.init()
+    ref, _ = oracle_lib.compact_state(o)
+    o.close()
+    o = oracle_lib.Oracle(str(tmp_path / "ss.dat"), 480, 480, 480)
+    o.init()
+    ss, _ = oracle_lib.compact_state(o)
+    o.close()
+    occ = (ref & 3) != 0
+    assert occ.sum() > 1000
+    assert np.array_equal(ref & 0xFC, ss & 0xFC)
+    assert np.array_equal(occ, (ss & 3) != 0) and ((ss[occ] & 3) == 1).all()
