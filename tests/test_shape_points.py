@@ -259,3 +259,31 @@ def test_oracle_ss_is_the_pinned_sphere_in_si(oracle_lib, tmp_path):
     assert occ.sum() > 1000
     assert np.array_equal(ref & 0xFC, ss & 0xFC)
     assert np.array_equal(occ, (ss & 3) != 0) and ((ss[occ] & 3) == 1).all()
+
+
+def test_oracle_fw_is_the_pinned_setsi_slab_in_sic(oracle_lib, tmp_path):
+    """SetSiC3Cww (InitSt Fw) against SetSi (FS, pinned by the Si-SL case) on
+    the surface case's start.dat: below the wall block the same walls, sites,
+    coordinations and first list entries, the species of the 3C sublattices;
+    from Lenww up to LenZ-7 every diamond site a wall."""
+    src = os.path.join(GOLDEN, "surface", "start.dat")
+    lines = open(src).read().splitlines()
+    out = {}
+    for kind, lens in (("FS", "120 120 120"), ("Fw", "120 240 0")):
+        l2 = list(lines)
+        l2[2], l2[3] = f"{kind} ! Initstat", f"{lens} ! Len1 Len2 Len3"
+        (tmp_path / f"{kind}.dat").write_text("\n".join(l2) + "\n")
+        o = oracle_lib.Oracle(str(tmp_path / f"{kind}.dat"), 480, 480, 480)
+        o.init()
+        out[kind], _ = oracle_lib.compact_state(o)
+        o.close()
+    fs, fw = out["FS"], out["Fw"]
+    below = slice(0, 240 // 3)
+    assert np.array_equal(fs[below] & 0xFC, fw[below] & 0xFC)
+    occ = (fw[below] & 3) != 0
+    assert occ.sum() > 1000 and set(np.unique(fw[below][occ] & 3)) == {1, 2}
+    nz, nb, na = fw.shape
+    z1, b, a = np.meshgrid(np.arange(nz), np.arange(nb), np.arange(na), indexing="ij")
+    site = ((a + b + (z1 >> 1)) & 1) == 0
+    block = site & (3 * z1 >= 240) & (3 * z1 <= 480 - 7)
+    assert (fw[block] == 0x80).all()
