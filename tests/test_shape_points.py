@@ -287,3 +287,33 @@ def test_oracle_fw_is_the_pinned_setsi_slab_in_sic(oracle_lib, tmp_path):
     site = ((a + b + (z1 >> 1)) & 1) == 0
     block = site & (3 * z1 >= 240) & (3 * z1 <= 480 - 7)
     assert (fw[block] == 0x80).all()
+
+
+def test_oracle_variant_species_rules(oracle_lib, tmp_path):
+    """The inverted-pyramid variants share one geometry: SetInvPwOnlyCorSi
+    (L) is SetInvPwOnlySiorC (K) with the two species swapped, SetInvPC (D)
+    is SetInvPSi (Z) with C in place of Si."""
+    from mulskips_gb300.startdat import write_startdat
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    for s in range(2):
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * np.exp(-0.6 * (n1 + n2) / (8.617e-5 * 1600.0))
+    st = {}
+    for kind in "KLDZ":
+        p = str(tmp_path / f"{kind}.dat")
+        write_startdat(p, E, np.full((3, 3), 0.5), ncrystal=2, list_crystal=(14, 6), init_st=kind, len1=24,
+                       lens=(90, 0), run_type="T")
+        o = oracle_lib.Oracle(p, 240, 240, 240)
+        o.init()
+        st[kind], _ = oracle_lib.compact_state(o)
+        o.close()
+    occ = (st["K"] & 3) != 0
+    assert occ.sum() > 1000
+    swapped = st["K"].copy()
+    swapped[occ] = (st["K"][occ] & 0xFC) | (3 - (st["K"][occ] & 3))
+    assert np.array_equal(swapped, st["L"])
+    assert np.array_equal(st["Z"] & 0xFC, st["D"] & 0xFC)
+    assert ((st["Z"][occ] & 3) == 1).all() and ((st["D"][occ] & 3) == 2).all()
+    assert np.array_equal(occ, (st["D"] & 3) != 0)
