@@ -33,6 +33,8 @@
  *   mks_replay                   Deposition.f / Evaporation.f applied to a
  *                                given event sequence (no selection)
  *   mks_class_histogram          the per-class view of the rate tree Tree(:)
+ *   mks_site_rates               the tree leaves: ListAdAtom ProbTrans
+ *                                (Get_Prob.f:54-331, Get_Prob_Ini.f:23-161)
  *   mks_get_observables          the scans of WriteMolMolXYZFile.f:77-119 and
  *                                pymulskips/analyze.py:124-207
  *
@@ -62,7 +64,7 @@ extern "C" {
 #define MKS_ERR_UNSUPPORTED 5  /* feature outside the engine (e.g. PtransZig<1) */
 #define MKS_ERR_TIMEOUT 6      /* a bounded device wait gave up               */
 
-#define MKS_NCLASS 63          /* rate classes, see mks_class_histogram       */
+#define MKS_NCLASS 64          /* rate classes, see mks_class_histogram       */
 
 typedef struct mks_handle mks_handle;
 
@@ -138,7 +140,9 @@ int mks_load_lattice(mks_handle *h, const int32_t *lattcoo);
 int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
 /* Compact state: one byte per diamond site (a, b, z1) at index
  * (z1 * (LenY/6) + b) * (LenX/6) + a (bits 0-1 species, 2-4 coordination,
- * 5-6 first list entry, 7 dummy flag; 0x80 a wall); n >= mks_state_size(). */
+ * 5-6 first list entry, 7 dummy flag; 0x80 a wall; coordination field 5 with
+ * the dummy flag: a coor-1 site still at Get_Prob_Ini's dummy rate 1e-6,
+ * Get_Prob_Ini.f:102-104); n >= mks_state_size().                        */
 int64_t mks_state_size(mks_handle *h);
 int mks_get_state(mks_handle *h, uint8_t *st, int64_t n);
 /* The compact state of replica rep, NZ*NB*NA bytes (NA = LenX/6, NB = LenY/6,
@@ -164,8 +168,10 @@ int mks_replay(mks_handle *h, const mks_event *trace, int64_t n);
  * call (longer traces are rejected with MKS_ERR_ARG; split them).  The array
  * is shared by every call and every handle on a device: calls that overlap on
  * the GPU (several handles or threads at once) race and must be serialized.
- * The first call on a device looks up the array's device address, so make
- * that first call before any CUDA stream capture.                         */
+ * Each call starts by clearing the array's progress counter, and the array
+ * keeps the last call's trace afterwards.  mks_create / mks_batch_create look
+ * up the array's device address once, with the handle's device current, and
+ * keep it in the handle.                                                  */
 #define MKS_REPLAY_NOALLOC_MAX 65536
 int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n);
 /* Synchronous-sublattice KMC: windows of length tau (s); stops after
@@ -173,7 +179,19 @@ int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n);
  * window), or when fewer than 21 surface sites remain (main.f:307-310).    */
 int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events,
             double max_time, int64_t *events_done, double *time_out);
+/* Event sites per rate class (nclass >= MKS_NCLASS): 1 empty coor-1, 2 its
+ * dummy (1e-8, Get_Prob.f:183), 3 coor-2, 4 coor-3, 5 isolated atom, 6..62
+ * atoms by species and census (PTransE key), 63 the dummy an initializer
+ * wrote (1e-6, Get_Prob_Ini.f:104); coverage mode: 6..8 covered sites,
+ * 9..58 atoms by species, census and covered neighbours.                  */
 int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
+/* Rate class and FP32 rate of n sites of replica rep given by grid
+ * coordinates xyz[3n] (AtomXYZ of ListAdAtom, defdertype.f:32-37): the
+ * ProbTrans of the reference's tree leaves (Get_Prob.f:54-331,
+ * Get_Prob_Ini.f:23-161).  Class 0 for a site without an event, -1 for a
+ * grid point that is not a diamond site; isolated atoms (class 5, rate
+ * 1e5 x Tree(1), Get_Prob.f:305) report rate 0.                           */
+int mks_site_rates(mks_handle *h, int32_t rep, const int32_t *xyz, int64_t n, int32_t *cls, float *rate);
 /* Sites listed in an output frame, as compact-state indices in the
  * reference's z, y, x scan order (WriteMolMolXYZFile.f:171-260): kind 0 the
  * atoms with coordination <= 3 and, with a coverage species, the covered
@@ -208,7 +226,7 @@ int mks_batch_init_flat(mks_handle *h, char kind, const int32_t *len1);
 int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows,
                   int64_t max_events_each, double max_time_each, int64_t *events_total);
 int mks_batch_observables(mks_handle *h, mks_observables *obs /* n entries */);
-/* Class histogram of every replica (n * nclass, nclass >= 63), the
+/* Class histogram of every replica (n * nclass, nclass >= 64), the
  * per-replica view of mks_class_histogram.                               */
 int mks_batch_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass);
 int32_t mks_batch_size(mks_handle *h);

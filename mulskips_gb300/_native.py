@@ -10,7 +10,7 @@ import numpy as np
 
 _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmulskips_gpu.so")
 
-MKS_NCLASS = 63
+MKS_NCLASS = 64
 ERRORS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "invariant violated", 4: "tile capacity",
           5: "unsupported", 6: "bounded wait timed out"}
 
@@ -75,6 +75,7 @@ SIGNATURES = {
     "mks_frame_sites": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "mks_write_frame": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, C.c_int64, C.c_void_p]),
     "mks_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "mks_site_rates": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "mks_get_observables": (C.c_int, [C.c_void_p, C.POINTER(MksObservables)]),
     "mks_get_status": (C.c_int, [C.c_void_p, C.POINTER(MksStatus)]),
     "mks_batch_create": (C.c_int, [C.POINTER(MksConfig), C.c_int32, C.POINTER(C.c_void_p)]),

@@ -27,7 +27,6 @@
 #include <string>
 #include <vector>
 #include <algorithm>
-#include <mutex>
 
 #include "lattice.cuh"
 #include "shapes.cuh"
@@ -172,13 +171,13 @@ __device__ __forceinline__ int la_coor(int c) { return c == CLS_C3 ? 3 : (c == C
 // rate of one site of class c at temperature T
 __device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
 {
-    if (A.ntab && c >= CLS_OCC0) {
+    if (A.ntab && c >= CLS_OCC0 && c < CLS_C1I) {
         int i;
         float w;
         la_tab_at(A, T, i, w);
         return la_tab_mix(A, i, w, A.tabE[i][c], w > 0.f ? A.tabE[i + 1][c] : 0.f);
     }
-    if (c >= CLS_OCC0) {
+    if (c >= CLS_OCC0 && c < CLS_C1I) {
         float E = A.E[c];
         return E != 0.f ? A.P0[(c - CLS_OCC0) / NCENSUS] * __expf(-E / (KB_EV_F * T)) : 0.f;
     }
@@ -186,7 +185,8 @@ __device__ __forceinline__ float la_rate(const LADev &A, int c, float T)
         int co = la_coor(c);
         return la_dep(A, 0, co, T) + la_dep(A, 1, co, T) + la_dep(A, 2, co, T);
     }
-    if (c == CLS_C1D) return 1.e-8f;
+    if (c == CLS_C1D) return 1.e-8f;     // Get_Prob.f:183
+    if (c == CLS_C1I) return 1.e-6f;     // Get_Prob_Ini.f:104
     return 0.f;
 }
 // Empty sites above the initial surface are vacuum, not liquid: nothing
@@ -202,7 +202,7 @@ __device__ __forceinline__ void la_drate(const LADev &A, int c, float T, float d
 {
     d[0] = d[1] = d[2] = d[3] = 0.f;
     if (vac) return;
-    if (c >= CLS_OCC0) {
+    if (c >= CLS_OCC0 && c < CLS_C1I) {
         float k = la_rate(A, c, T);
         for (int j = 0; j < 4; j++) d[j] = -k * A.dE[c][j] / (KB_EV_F * T);
     } else if (c == CLS_C1 || c == CLS_C2 || c == CLS_C3) {
@@ -460,6 +460,37 @@ __global__ void k_observables_heights(const int *top, int64_t ncol, int nslab, u
     }
 }
 
+// Rate class and rate of given sites (grid coordinates, as AtomXYZ of the
+// reference's ListAdAtom): the ProbTrans the reference keeps in its tree
+// leaves (Get_Prob / Get_Prob_Ini).  Isolated atoms get rate 0 here (their
+// rate, 1e5 x Tree(1), follows the total); LA replicas take the rate law at
+// the site's temperature at the replica's clock.  A grid point that is not a
+// diamond site of the box gets class -1.
+__global__ void k_site_rates(const RepDev *reps, int rep, const uint8_t *st_all, const LADev *la, const int32_t *xyz,
+                             int64_t n, int32_t *cls, float *rate)
+{
+    const RepDev &R = reps[rep];
+    GLat L{const_cast<uint8_t *>(st_all) + R.st_off, R.NA, R.NB, R.NZ, R.pitch};
+    const LADev *A = (la && la[rep].on) ? &la[rep] : nullptr;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        int x1 = x / 3, y1 = y / 3, z1 = z / 3, a = x1 >> 1, b = y1 >> 1;
+        bool ok = x >= 0 && y >= 0 && z >= 0 && x % 3 == 0 && y % 3 == 0 && z % 3 == 0 && ((x1 & 1) == (z1 & 1)) &&
+                  ((y1 & 1) == (z1 & 1)) && z1 < R.NZ && a < R.NA && b < R.NB && ((a + b + (z1 >> 1)) & 1) == 0;
+        if (!ok) {
+            cls[i] = -1;
+            rate[i] = 0.f;
+            continue;
+        }
+        int c = site_class(L, a, b, z1, R.single != 0, R.cov != 0);
+        float r = 0.f;
+        if (c != CLS_ISO && c != CLS_NONE)
+            r = A ? la_rate(*A, c, la_temp_at(*A, a, b, z1, R.T0)) : R.rate[c];
+        cls[i] = c;
+        rate[i] = r;
+    }
+}
+
 // Apply a given event sequence in order (one thread; the sequence is serial by
 // definition).  Deposition.f / Evaporation.f restated in lattice.cuh.
 __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *ev, int64_t n, DevStatus *status,
@@ -473,14 +504,15 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
         int x1 = e.x / 3, y1 = e.y / 3, z1 = e.z / 3;
         int a = x1 >> 1, b = y1 >> 1;
         bool ok = (e.x % 3 == 0) && (e.y % 3 == 0) && (e.z % 3 == 0) && ((x1 & 1) == (z1 & 1)) &&
-                  ((y1 & 1) == (z1 & 1)) && z1 >= 0 && z1 < R.NZ && a < R.NA && b < R.NB && e.arm == 0;
+                  ((y1 & 1) == (z1 & 1)) && e.x >= 0 && e.y >= 0 && z1 >= 0 && z1 < R.NZ && a < R.NA &&
+                  b < R.NB && e.arm == 0;
         const bool cov = R.cov != 0;
         int c = ok ? site_class(L, a, b, z1, false, cov) : CLS_NONE;
-        bool atom_cls = c == CLS_ISO || (cov ? c >= CLS_COV0 : c >= CLS_OCC0);
+        bool atom_cls = c == CLS_ISO || ((cov ? c >= CLS_COV0 : c >= CLS_OCC0) && c < CLS_C1I);
         Touched tc;
         int err = 1;
         if (ok && c != CLS_NONE) {
-            if (e.itrans >= 1 && e.itrans <= 3 && c >= CLS_C1 && c <= CLS_C3)
+            if (e.itrans >= 1 && e.itrans <= 3 && dep_class(c))
                 err = apply_deposition(L, a, b, z1, e.itrans, tc, cov);
             else if (e.itrans == 4 && atom_cls)
                 err = apply_evaporation(L, a, b, z1, tc, cov);
@@ -825,9 +857,10 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         int covev = 0;                                 // 1 absorption, 2 desorption
         if (R.cov && cls >= CLS_D1 && cls < CLS_COV0) {
             covev = 2;                                 // main.f:346-349
-        } else if (cls == CLS_C1D) {
-            // unsupported coor-1 site: Get_Prob.f:181-184 fixes IndexEvent = 1
-            // (species 1) with its 1e-8 rate, whatever the tables say
+        } else if (dummy_class(cls)) {
+            // unsupported coor-1 site: Get_Prob.f:181-184 (and Get_Prob_Ini.f:
+            // 102-104) fix IndexEvent = 1 (species 1) with the dummy rate,
+            // whatever the tables say
             sp = 1;
         } else if (cls >= CLS_C1 && cls <= CLS_C3) {
             int co = cls == CLS_C3 ? 3 : (cls == CLS_C2 ? 2 : 1);
@@ -850,7 +883,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                     covev = 1;
                 }
             }
-        } else if (A && sc && lane == 0 && cls >= CLS_OCC0) {
+        } else if (A && sc && lane == 0 && cls >= CLS_OCC0 && cls < CLS_C1I) {
             for (int j = 0; j < 4; j++) sc[j] += -(double)A->dE[cls][j] / ((double)KB_EV_F * (double)Tsite);
         }
         int ta = a, tb = b, tz = z;
@@ -1503,6 +1536,7 @@ struct mks_handle {
     int64_t last_kernels = 0, last_graphs = 0, last_phase_launches = 0;
     double last_ms = 0.0;
     double time_acc = 0.0;
+    unsigned char *noalloc_scratch = nullptr;  // device address of the mks_replay_noalloc array (set at creation)
 };
 
 namespace {
@@ -1526,6 +1560,7 @@ void rate_tables(const RepHost &r, RepDev &d)
         if (cov) d.rate[CLS_D1 + co - 1] = (float)r.ptransDes[co - 1];   // Get_Prob.f:114
     }
     d.rate[CLS_C1D] = 1.e-8f;   // Get_Prob.f:183
+    d.rate[CLS_C1I] = 1.e-6f;   // Get_Prob_Ini.f:104
     d.rate[CLS_ISO] = 0.f;      // dynamic: 1e5 x tile rate (Get_Prob.f:305)
     if (cov) {
         // PE(NSiC, n1, n2, 0, c, 0, 0), Get_Prob.f:309-312
@@ -1771,6 +1806,31 @@ int make_tensor_maps(mks_handle *h, uint8_t *base, CUtensorMap **out)
     return 0;
 }
 
+}  // namespace
+
+// ---- mks_replay_noalloc: the replay kernel fed from a library-owned array ----
+// Layout of the array: bytes [0, 8) the kernel's progress counter, bytes
+// [256, 256 + 16 * MKS_REPLAY_NOALLOC_MAX) the staged events.  Every GPU that
+// loads this library holds the array until the process exits.
+static __device__ __align__(256) unsigned char g_replay_scratch[256 + sizeof(mks_event) * MKS_REPLAY_NOALLOC_MAX];
+
+namespace {
+
+// Device address of g_replay_scratch on the current device.  In host code the
+// symbol itself is only a stand-in for the device array, never a device
+// address.  Called by create_impl with the handle's device current, outside
+// any stream capture, so each handle carries the address of the array in its
+// own context (a context created again after a device reset reloads the
+// module, and its handles look the address up afresh).
+int noalloc_lookup(unsigned char **out)
+{
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_replay_scratch);
+    if (e != cudaSuccess) return fail(MKS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    *out = static_cast<unsigned char *>(p);
+    return 0;
+}
+
 int create_impl(const mks_config *cfgs, int n, mks_handle **out)
 {
     if (!cfgs || n <= 0 || !out) return fail(MKS_ERR_ARG, "bad arguments");
@@ -1807,6 +1867,10 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return cleanup_fail("stream", e);
+    if (noalloc_lookup(&h->noalloc_scratch)) {
+        mks_destroy(h);
+        return MKS_ERR_CUDA;
+    }
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return cleanup_fail("event", e);
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return cleanup_fail("event", e);
     if ((e = cudaMalloc(&h->d_st, (size_t)h->st_bytes)) != cudaSuccess) return cleanup_fail("lattice allocation", e);
@@ -2354,13 +2418,13 @@ int mks_batch_set_tabulated(mks_handle *h, int32_t ntemp, const int32_t *temps, 
             RepDev d;
             memset(&d, 0, sizeof d);
             rate_tables(row, d);
-            for (int c = 0; c < 64; c++) A.tabE[k][c] = c >= CLS_OCC0 ? d.rate[c] : 0.f;
+            for (int c = 0; c < 64; c++) A.tabE[k][c] = (c >= CLS_OCC0 && c < CLS_C1I) ? d.rate[c] : 0.f;
             for (int sp = 0; sp < 3; sp++)
                 for (int co = 0; co < 3; co++) A.tabD[k][sp][co] = (float)row.ptransD[sp * 3 + co];
         }
         // the per-tile bound takes the rates at the hottest staged layer
         for (int k = 1; k < ntemp; k++) {
-            for (int c = CLS_OCC0; c < NCLASS; c++)
+            for (int c = CLS_OCC0; c < CLS_C1I; c++)
                 if (A.tabE[k][c] < A.tabE[k - 1][c])
                     return fail(MKS_ERR_UNSUPPORTED, "replica %zu: tabulated rate of class %d decreases with T", i, c);
             for (int co = 0; co < 3; co++) {
@@ -2553,18 +2617,19 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
     return 0;
 }
 
-int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st);
+int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st, bool ini = true);
 
 // A host-built lattice (mks_shapes::Grid, rows of NA bytes) into the padded
-// rows of replica rep, then upload_compact.
-int upload_grid(mks_handle *h, int rep, const mks_shapes::Grid &g)
+// rows of replica rep, then upload_compact (ini: the initializer rates its
+// sites with Get_Prob_Ini).
+int upload_grid(mks_handle *h, int rep, const mks_shapes::Grid &g, bool ini = true)
 {
     const RepHost &r = h->reps[rep];
     std::vector<uint8_t> st((size_t)r.NZ * r.NB * r.pitch, 0);
     for (int z1 = 0; z1 < r.NZ; z1++)
         for (int b = 0; b < r.NB; b++)
             memcpy(&st[((size_t)z1 * r.NB + b) * r.pitch], &g.st[((size_t)z1 * r.NB + b) * r.NA], (size_t)r.NA);
-    return upload_compact(h, rep, st);
+    return upload_compact(h, rep, st, ini);
 }
 
 int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
@@ -2603,8 +2668,11 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
 }
 
 // The first list entry and dummy flag of coor-1 sites, then the upload of the
-// padded compact state st of replica rep and the event-site scan.
-int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st)
+// padded compact state st of replica rep and the event-site scan.  A lattice
+// loaded as LattCoo is an initial lattice: its lists are rebuilt as SetCAD.f:
+// 301-418 does, and its dummies take Get_Prob_Ini's rate (ini), as do those
+// of every initializer but SetSiC3Cww(aperture).
+int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st, bool ini)
 {
     const RepHost &r = h->reps[rep];
     auto at = [&](int a, int b, int z) -> uint8_t & {
@@ -2636,7 +2704,7 @@ int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st)
                     }
                 }
                 if (found < 0) return fail(MKS_ERR_INVARIANT, "coor-1 site without neighbour");
-                at(a, b, z1) = covered ? mk(COVSP, 1, found, 0) : mk(0, 1, found, co_of(ns) < 2 ? 1 : 0);
+                at(a, b, z1) = covered ? mk(COVSP, 1, found, 0) : mk_c1(found, co_of(ns), ini);
             }
     CK(cudaMemcpyAsync(h->d_st + r.st_off, st.data(), st.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -2782,7 +2850,7 @@ int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const 
     char msg[160];
     if (int e = mks_shapes::build_shape(g, kind, lens, params, temp, msg, sizeof msg))
         return fail(e == 2 ? MKS_ERR_UNSUPPORTED : MKS_ERR_ARG, "%s", msg);
-    int rc = upload_grid(h, rep, g);
+    int rc = upload_grid(h, rep, g, mks_shapes::ini_rates(kind));
     if (rc) return rc;
     if (kind == "ST")   // the temperatures of SetTrenchSi.f:46-63 as the replica's field
         return set_temperature_impl(h, rep, [&](int, int, int z, int) { return temp[(size_t)z] & 8191; });
@@ -2902,39 +2970,6 @@ int mks_replay(mks_handle *h, const mks_event *trace, int64_t n)
     return rescan(h);
 }
 
-// ---- mks_replay_noalloc: the replay kernel fed from a library-owned array ----
-// Layout of the array: bytes [0, 8) the kernel's progress counter, bytes
-// [256, 256 + 16 * MKS_REPLAY_NOALLOC_MAX) the staged events.  Every GPU that
-// loads this library holds the array until the process exits.
-static __device__ __align__(256) unsigned char g_replay_scratch[256 + sizeof(mks_event) * MKS_REPLAY_NOALLOC_MAX];
-
-namespace {
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
-
-// Device address of g_replay_scratch on `dev`, looked up once per device with
-// that device current.  In host code the symbol itself is only a stand-in for
-// the device array, never a device address.
-int noalloc_scratch(int dev, unsigned char **out)
-{
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(MKS_ERR_ARG, "device %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        int prev = -1;
-        CK(cudaGetDevice(&prev));
-        if (prev != dev) CK(cudaSetDevice(dev));
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_replay_scratch);
-        if (prev != dev) cudaSetDevice(prev);
-        if (e != cudaSuccess) return fail(MKS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_noalloc_ptr[dev];
-    return 0;
-}
-}  // namespace
-
 int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n)
 {
     if (!h || (n > 0 && !trace) || n < 0 || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
@@ -2942,11 +2977,7 @@ int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n)
         return fail(MKS_ERR_ARG, "mks_replay_noalloc: %lld events exceed the per-call limit of %d; split the trace",
                     (long long)n, MKS_REPLAY_NOALLOC_MAX);
     if (n == 0) return 0;
-    int dev = -1;
-    CK(cudaStreamGetDevice(h->stream, &dev));
-    unsigned char *scratch = nullptr;
-    int rc = noalloc_scratch(dev, &scratch);
-    if (rc) return rc;
+    unsigned char *scratch = h->noalloc_scratch;
     long long *d_done = reinterpret_cast<long long *>(scratch);
     mks_event *d_ev = reinterpret_cast<mks_event *>(scratch + 256);
     // the array keeps the previous call's contents: reset the progress counter
@@ -2958,7 +2989,7 @@ int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n)
     CK(cudaMemcpyAsync(&done, d_done, sizeof done, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     DevStatus s;
-    rc = read_status(h, s);
+    int rc = read_status(h, s);
     if (rc) return rc;
     if (s.error) {
         CK(cudaMemsetAsync(h->d_status, 0, sizeof(DevStatus), h->stream));
@@ -3001,6 +3032,30 @@ int mks_batch_run(mks_handle *h, const double *tau, int64_t max_windows, int64_t
     unsigned long long e1 = 0;
     for (auto &x : d) e1 += x.events;
     if (events_total) *events_total = (int64_t)(e1 - e0);
+    return 0;
+}
+
+int mks_site_rates(mks_handle *h, int32_t rep, const int32_t *xyz, int64_t n, int32_t *cls, float *rate)
+{
+    if (!h || n < 0 || (n && (!xyz || !cls || !rate)) || rep < 0 || rep >= (int)h->reps.size())
+        return fail(MKS_ERR_ARG, "bad arguments");
+    if (n == 0) return 0;
+    int32_t *d_xyz = nullptr, *d_cls = nullptr;
+    float *d_rate = nullptr;
+    CK(cudaMallocAsync(&d_xyz, sizeof(int32_t) * 3 * (size_t)n, h->stream));
+    CK(cudaMallocAsync(&d_cls, sizeof(int32_t) * (size_t)n, h->stream));
+    CK(cudaMallocAsync(&d_rate, sizeof(float) * (size_t)n, h->stream));
+    CK(cudaMemcpyAsync(d_xyz, xyz, sizeof(int32_t) * 3 * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+    int nb = (int)std::min<int64_t>(152 * 8, (n + 255) / 256);
+    k_site_rates<<<nb, 256, 0, h->stream>>>(h->d_reps, rep, h->d_st, h->la_on ? h->d_la : nullptr, d_xyz, n, d_cls,
+                                            d_rate);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cls, d_cls, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(rate, d_rate, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    cudaFreeAsync(d_xyz, h->stream);
+    cudaFreeAsync(d_cls, h->stream);
+    cudaFreeAsync(d_rate, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
 
@@ -3119,7 +3174,7 @@ int mks_suggest_tau(mks_handle *h, double f, double *tau)
     for (size_t i = 0; i < h->reps.size(); i++) {
         double best = 0.0, rstar = 0.0;
         for (int c = 1; c < NCLASS; c++) {
-            if (c == CLS_ISO || c == CLS_C1D) continue;
+            if (c == CLS_ISO || dummy_class(c)) continue;
             double w = (double)hist[i * NCLASS + c] * (double)d[i].rate[c];
             if (w > best) {
                 best = w;

@@ -18,6 +18,14 @@
 //             (Get_Prob.f:181-184); with species 0 and coordination 0 the
 //             value 0x80 marks a wall site (CovInd 113, SetSi.f:38-46)
 //
+// A dummy coor-1 site written by an initializer carries the init-time rate
+// 1e-6 of Get_Prob_Ini.f:102-104 instead of Get_Prob's 1e-8 until the site
+// itself changes (nothing re-rates a coor-1 site before its one neighbour
+// has an event, and that event changes the site): its coordination field
+// holds 5 (bits 2-4 = 101).  co_of() reads it as coordination 1, so only the
+// rate class tells the two dummies apart; every event writes a fresh byte
+// and so drops the mark.
+//
 // Coverage mode (one coverage species, NCrystal <= 2): species value 3 marks
 // an EMPTY site carrying the coverage species (LattCoo Occ = 0 with CovInd =
 // ListCov(1), absorption.f:34-36).  A covered site keeps its coordination and
@@ -43,7 +51,9 @@ namespace mks {
 // ---- state byte ----
 constexpr uint8_t WALL = 0x80;
 MKS_HD int sp_of(uint8_t s) { return s & 3; }
-MKS_HD int co_of(uint8_t s) { return (s >> 2) & 7; }
+// coordination; the field value 5 of an init-time dummy site reads as 1
+MKS_HD int co_of(uint8_t s) { return (s >> 2) & (7 ^ (s & 4)); }
+MKS_HD bool ini_of(uint8_t s) { return (s & 0x1C) == 0x14; }
 MKS_HD int fd_of(uint8_t s) { return (s >> 5) & 3; }
 MKS_HD int dm_of(uint8_t s) { return (s >> 7) & 1; }
 MKS_HD bool is_wall(uint8_t s) { return s == WALL; }
@@ -55,6 +65,13 @@ MKS_HD bool is_cov(uint8_t s, bool cov) { return cov && (s & 3) == COVSP; }
 MKS_HD uint8_t mk(int sp, int co, int fd, int dm)
 {
     return (uint8_t)((sp & 3) | ((co & 7) << 2) | ((fd & 3) << 5) | ((dm & 1) << 7));
+}
+// an empty coor-1 site whose one occupied neighbour (direction fd) has
+// coordination nco: Get_Prob's dummy when nco < 2; from an initializer
+// (ini) the dummy keeps Get_Prob_Ini's rate
+MKS_HD uint8_t mk_c1(int fd, int nco, bool ini)
+{
+    return nco >= 2 ? mk(0, 1, fd, 0) : (uint8_t)(mk(0, 1, fd, 1) | (ini ? 0x10 : 0));
 }
 
 // ---- geometry ----
@@ -75,10 +92,15 @@ MKS_HD int rev_dir(int d) { return (d + 2) & 3; }
 // 0 none (bulk, void, wall, untracked empty), 1 empty coor-1, 2 empty coor-1
 // dummy, 3 empty coor-2, 4 empty coor-3, 5 isolated atom, 6.. occupied
 // species sp with reciprocal-neighbour census (nSi+nWall, nC, nB) summing to
-// 1..3 (the PTransE key of Get_Prob.f:309-321 without coverage).
+// 1..3 (the PTransE key of Get_Prob.f:309-321 without coverage); 63 the
+// empty coor-1 dummy of an initializer (Get_Prob_Ini.f:102-104, rate 1e-6).
 constexpr int CLS_NONE = 0, CLS_C1 = 1, CLS_C1D = 2, CLS_C2 = 3, CLS_C3 = 4, CLS_ISO = 5, CLS_OCC0 = 6;
 constexpr int NCENSUS = 19;
-constexpr int NCLASS = CLS_OCC0 + 3 * NCENSUS;   // 63
+constexpr int CLS_C1I = CLS_OCC0 + 3 * NCENSUS;  // 63
+constexpr int NCLASS = CLS_C1I + 1;              // 64
+// an empty site's deposition class (coordination 1..3, either dummy)
+MKS_HD bool dep_class(int c) { return (c >= CLS_C1 && c <= CLS_C3) || c == CLS_C1I; }
+MKS_HD bool dummy_class(int c) { return c == CLS_C1D || c == CLS_C1I; }
 // Coverage mode: 6..8 covered site of coordination 1..3 (desorption,
 // Get_Prob.f:93-118), 9.. atom of species sp (1..2) with census (nSi+nWall,
 // nC) summing to 1..3 and c covered neighbours, c <= 4 - census (the PTransE
@@ -155,7 +177,7 @@ MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false, bo
         }
     }
     if (sp == 0) {
-        if (co == 1) return dm_of(s) ? CLS_C1D : CLS_C1;
+        if (co == 1) return dm_of(s) ? (ini_of(s) ? CLS_C1I : CLS_C1D) : CLS_C1;
         if (co == 2) return CLS_C2;
         if (co == 3) return CLS_C3;
         return CLS_NONE;

@@ -341,6 +341,32 @@ inline void set_cad(Grid &g, const int8_t *geo, const CadLA &la = CadLA(), doubl
     coor_pass(g, 0, g.lx - 1, 0, g.ly - 1, 0, g.lz - 1, true);
 }
 
+// The first list entry of every coor-1 empty site is its one occupied
+// neighbour that is not a wall (Get_Prob_Ini keeps it as NextN(1)); the site
+// is a dummy when that neighbour has coordination < 2, with the rate of
+// Get_Prob_Ini.f:89-104 (ini) or of Get_Prob.f:156-184 for the initializers
+// that rate their sites with Get_Prob.
+inline void list_heads(Grid &g, bool ini)
+{
+    for (int z1 = 0; z1 < g.NZ; z1++)
+        for (int b = 0; b < g.NB; b++)
+            for (int a = 0; a < g.NA; a++) {
+                if ((a + b + (z1 >> 1)) & 1) continue;
+                uint8_t &v = g.st[((size_t)z1 * g.NB + b) * g.NA + a];
+                if (v == WALL || (v & 3) || mks::co_of(v) != 1) continue;
+                int found = -1;
+                uint8_t ns = 0;
+                for (int d = 0; d < 4; d++) {
+                    uint8_t *w = g.nb(a, b, z1, d);
+                    if (w && *w != WALL && (*w & 3)) {
+                        found = d;
+                        ns = *w;
+                    }
+                }
+                if (found >= 0) v = mks::mk_c1(found, mks::co_of(ns), ini);
+            }
+}
+
 // SetShape (SetShape.f:25-436, InitSt SH): grid points (x, y, z) with
 // species 1 (Si) or 2 (C or Ge), n of them.  A point with z <= 3 or
 // z >= LenZ-4 is a wall (:58-62), any other an atom, which must sit on a
@@ -434,33 +460,14 @@ inline const char *set_points(Grid &g, const int32_t *xyz, const int8_t *sp, int
                     *w = mks::mk(0, c + 1, c == 0 ? mks::rev_dir(d) : mks::fd_of(*w), 0);
                 }
             }
+    list_heads(g, true);     // the ad-voids are rated by Get_Prob_Ini (SetShape.f:378-431)
     return nullptr;
 }
 
-// The first list entry of every coor-1 empty site is its one occupied
-// neighbour that is not a wall (Get_Prob_Ini keeps it as NextN(1)); its
-// dummy flag is set when that neighbour has coordination < 2 (the rate of
-// Get_Prob_Ini.f:89-104).
-inline void list_heads(Grid &g)
-{
-    for (int z1 = 0; z1 < g.NZ; z1++)
-        for (int b = 0; b < g.NB; b++)
-            for (int a = 0; a < g.NA; a++) {
-                if ((a + b + (z1 >> 1)) & 1) continue;
-                uint8_t &v = g.st[((size_t)z1 * g.NB + b) * g.NA + a];
-                if (v == WALL || (v & 3) || mks::co_of(v) != 1) continue;
-                int found = -1;
-                uint8_t ns = 0;
-                for (int d = 0; d < 4; d++) {
-                    uint8_t *w = g.nb(a, b, z1, d);
-                    if (w && *w != WALL && (*w & 3)) {
-                        found = d;
-                        ns = *w;
-                    }
-                }
-                if (found >= 0) v = mks::mk(0, 1, found, mks::co_of(ns) < 2 ? 1 : 0);
-            }
-}
+// Does the shaped initializer rate its sites with Get_Prob_Ini (SetNC,
+// SetNCSp(Si), SetInvP*, SetTrench(Si), SetSiFINFET) rather than Get_Prob
+// (SetSiC3Cww, SetSiC3Cwwaperture)?
+inline bool ini_rates(const std::string &kind) { return kind != "Fw" && kind != "Fa"; }
 
 // The shaped initializers by InitSt (main.f:224-278): lens are Len1..Len4 as
 // start.dat gives them, params the angle, Ttop and Tbottom of "ST" (whose
@@ -512,7 +519,7 @@ inline int build_shape(Grid &g, const std::string &kind, const int32_t *lens, co
     } else {
         return err(2, "InitSt %s has no shape initializer", kind.c_str());
     }
-    list_heads(g);
+    list_heads(g, ini_rates(kind));
     return 0;
 }
 

@@ -14,6 +14,14 @@ from . import _native as N
 KB_EV = 0.00008617330350  # Boltzmann constant in eV/K, mulskips-source/mcevent/Get_Prob.f:70
 
 
+def coordination(st):
+    """Coordination of every site of a compact state (numpy uint8 array in
+    the layout of mks_get_state): bits 2-4, where the value 5 of an
+    initializer's dummy coor-1 site (Get_Prob_Ini's rate) reads as 1."""
+    st = np.asarray(st, dtype=np.uint8)
+    return (st >> 2) & (7 ^ (st & 4))
+
+
 def arrhenius_tables(T, e_bond=0.6, nu=1e13, flux=0.5, ncrystal=1):
     """PTransE / PTransD arrays of the plain Si(001) model: evaporation rate
     nu*exp(-n*e_bond/kT) for an atom with n bonded neighbours (n = 1..3) and a
@@ -39,6 +47,15 @@ def _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed, list_co
     c.sf = float(sf)
     c.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     return c
+
+
+def _site_rates(h, rep, xyz):
+    p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+    n = p.shape[0]
+    cls = np.zeros(max(n, 1), dtype=np.int32)
+    rate = np.zeros(max(n, 1), dtype=np.float32)
+    N.check(N.lib().mks_site_rates(h, int(rep), N.ptr(p), n, N.ptr(cls), N.ptr(rate)))
+    return cls[:n], rate[:n]
 
 
 class Lattice:
@@ -170,6 +187,11 @@ class Lattice:
         N.check(N.lib().mks_class_histogram(self._h, N.ptr(h), N.MKS_NCLASS))
         return h
 
+    def site_rates(self, xyz):
+        """(class, FP32 rate) of the sites at grid points xyz [n, 3] (the
+        tree-leaf rates of the reference's MC particles)."""
+        return _site_rates(self._h, 0, xyz)
+
     def write_frame(self, base, time, it):
         """The frame files <base>.xyz, _d, _v (and _w for SiC) of the
         current lattice; returns the SiC NumAtWrong count (0 otherwise)."""
@@ -296,10 +318,14 @@ class Batch:
                 "phase_launches": p.value}
 
     def class_histogram(self):
-        """(n, 63) event sites per rate class of every replica."""
-        h = np.zeros((self.n, 63), dtype=np.int64)
-        N.check(N.lib().mks_batch_class_histogram(self._h, N.ptr(h), 63))
+        """(n, MKS_NCLASS) event sites per rate class of every replica."""
+        h = np.zeros((self.n, N.MKS_NCLASS), dtype=np.int64)
+        N.check(N.lib().mks_batch_class_histogram(self._h, N.ptr(h), N.MKS_NCLASS))
         return h
+
+    def site_rates(self, rep, xyz):
+        """(class, FP32 rate) of replica rep's sites at grid points xyz [n, 3]."""
+        return _site_rates(self._h, rep, xyz)
 
     def load_lattice(self, rep, lattcoo):
         """Replica rep from a LattCoo(0:LenX-1,0:LenY-1,0:LenZ) array (x fastest)."""

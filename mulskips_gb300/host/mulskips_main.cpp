@@ -16,6 +16,7 @@
 // The loop is the synchronous-sublattice engine: events are counted per
 // window, so the Iter exit and the frame schedule are met at the first window
 // boundary at or after the requested event count.
+#include <ctype.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -291,6 +292,59 @@ void box_size(int &lx, int &ly, int &lz)
     if (e) sscanf(e, "%d %d %d", &lx, &ly, &lz);
 }
 
+// List-directed READ(unit,*) of a large array (SetCAD.f:58-60,162-170): the
+// values are separated by blanks, commas or line breaks and may span several
+// records; once the statement has its values the rest of the current record
+// is skipped.  Streams the file through a fixed buffer.
+struct ListReader {
+    FILE *f;
+    std::vector<char> buf;
+    size_t pos = 0, len = 0;
+    explicit ListReader(FILE *fp) : f(fp), buf(1 << 20) {}
+    int peek()
+    {
+        if (pos == len) {
+            len = fread(buf.data(), 1, buf.size(), f);
+            pos = 0;
+            if (len == 0) return EOF;
+        }
+        return (unsigned char)buf[pos];
+    }
+    // next value as text; false at the end of the file
+    bool token(char *out, size_t cap)
+    {
+        int c;
+        while ((c = peek()) != EOF && (isspace(c) || c == ',')) pos++;
+        if (c == EOF) return false;
+        size_t n = 0;
+        while ((c = peek()) != EOF && !isspace(c) && c != ',') {
+            if (n + 1 < cap) out[n++] = (char)c;
+            pos++;
+        }
+        out[n] = 0;
+        return n > 0;
+    }
+    // the rest of the current record
+    void end_record()
+    {
+        int c;
+        while ((c = peek()) != EOF && c != '\n') pos++;
+        if (c == '\n') pos++;
+    }
+    // one READ statement of n values, each passed to put(k, text)
+    template <class F>
+    bool read(size_t n, F put)
+    {
+        char t[64];
+        for (size_t k = 0; k < n; k++) {
+            if (!token(t, sizeof t)) return false;
+            put(k, t);
+        }
+        end_record();
+        return true;
+    }
+};
+
 void check(int rc)
 {
     if (rc) {
@@ -425,17 +479,16 @@ int main()
         FILE *cf = fopen(in.cad_file.c_str(), "r");
         if (!cf) die("cannot open the checkpoint file");
         std::vector<int32_t> lc((size_t)lx * ly * (lz + 1), 0);
-        std::vector<char> line((size_t)lx * ly * 16 + 4096);
+        ListReader rd(cf);
         for (int z = 0; z < lz; z++) {
-            if (!fgets(line.data(), (int)line.size(), cf)) die("checkpoint file: too few records");
-            char *p = line.data();
-            for (size_t k = 0; k < (size_t)lx * ly; k++) {
+            int32_t *layer = lc.data() + (size_t)lx * ly * z;
+            bool ok = rd.read((size_t)lx * ly, [&](size_t k, const char *t) {
                 char *e;
-                long v = strtol(p, &e, 10);
-                if (e == p) die("checkpoint file: short record");
-                lc[(size_t)lx * ly * z + k] = (int32_t)v;
-                p = e;
-            }
+                long v = strtol(t, &e, 10);
+                if (e == t || *e) die("checkpoint file: not an integer");
+                layer[k] = (int32_t)v;
+            });
+            if (!ok) die("checkpoint file: too few values");
         }
         fclose(cf);
         printf(" Done reading checkpoint file\n");
@@ -445,18 +498,17 @@ int main()
         FILE *gf = fopen(in.cad_file.c_str(), "r");
         if (!gf) die("cannot open the geometry file");
         std::vector<int8_t> geo((size_t)lx * ly * lz, 0);
-        std::vector<char> line((size_t)lx * ly * 24 + 4096);
+        ListReader rd(gf);
         for (int z = 0; z < lz - 4; z++) {          // the last four layers are walls
-            if (!fgets(line.data(), (int)line.size(), gf)) die("geometry file: too few records");
             // list-directed READ of LenX*LenY values: the rest of the record is skipped
-            char *p = line.data();
-            for (size_t k = 0; k < (size_t)lx * ly; k++) {
+            int8_t *layer = geo.data() + (size_t)z * lx * ly;
+            bool ok = rd.read((size_t)lx * ly, [&](size_t k, const char *t) {
                 char *e;
-                double v = strtod(p, &e);
-                if (e == p) die("geometry file: short record");
-                geo[(size_t)z * lx * ly + k] = (int8_t)v;
-                p = e;
-            }
+                double v = strtod(t, &e);
+                if (e == t) die("geometry file: not a number");
+                layer[k] = (int8_t)v;
+            });
+            if (!ok) die("geometry file: too few values");
         }
         fclose(gf);
         printf(" Done reading input geometry file\n");

@@ -145,7 +145,7 @@ def max_rate(theta, mat, T_peak):
 
 
 # rate classes of the engine (mulskips_gb300/csrc/lattice.cuh)
-CLS_C1, CLS_C1D, CLS_C2, CLS_C3, CLS_ISO, CLS_OCC0, NCENSUS, NCLASS = 1, 2, 3, 4, 5, 6, 19, 63
+CLS_C1, CLS_C1D, CLS_C2, CLS_C3, CLS_ISO, CLS_OCC0, NCENSUS, CLS_C1I, NCLASS = 1, 2, 3, 4, 5, 6, 19, 63, 64
 
 
 def census_index(n1, n2, n3):
@@ -186,7 +186,8 @@ def class_rates_tables(E, Ed, mat, T, xliq=(1.0, 1.0, 1.0)):
             if d:
                 r[cls] += 0.5 * mat.P0[sp] * xliq[sp] * math.exp(-d / (KB_EV * mat.Tm[sp])) * \
                     (1.0 + math.erf((T - mat.Tflex[sp]) / mat.A[sp]))
-    r[CLS_C1D] = 1e-8
+    r[CLS_C1D] = 1e-8      # Get_Prob.f:183
+    r[CLS_C1I] = 1e-6      # Get_Prob_Ini.f:104, dummies written by an initializer
     return r
 
 
@@ -196,6 +197,7 @@ def share_rate(hist, rates):
     w = hist.astype(np.float64) * rates[None, :]
     w[:, CLS_ISO] = 0.0
     w[:, CLS_C1D] = 0.0
+    w[:, CLS_C1I] = 0.0
     return rates[np.argmax(w, axis=1)]
 
 

@@ -2825,8 +2825,10 @@ int64_t ora_compact_state(const ora_t *o, uint8_t *out)
                     }
                     if (fd < 0) return -1;
                 }
-                /* the dummy rates of Get_Prob (1e-8) and Get_Prob_Ini (1e-6) share the one flag */
+                /* the dummy rate of Get_Prob (1e-8) is the flag; that of
+                 * Get_Prob_Ini (1e-6) the flag with coordination field 5 */
                 int dm = (!occ && co == 1 && which == 1 && (pr == (double)1.e-8f || pr == (double)1.e-6f)) ? 1 : 0;
+                if (dm && pr == (double)1.e-6f) co = 5;
                 /* an empty site carrying a coverage species is species value 3 */
                 if (!occ && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
                     sp = 3;
@@ -2852,6 +2854,15 @@ static int census_idx(int n1, int n2, int n3)
     return -1;
 }
 
+/* Grid coordinates of the MC particles in list order (ListAdAtom(i) %
+ * AtomXYZ, defdertype.f:32-37), up to n of them; returns NumAdAtom. */
+int64_t ora_mc_sites(const ora_t *o, int32_t *xyz, int64_t n)
+{
+    for (int i = 1; i <= o->num_mc && i <= n; i++)
+        for (int k = 0; k < 3; k++) xyz[3 * (i - 1) + k] = o->mc[i].xyz[k];
+    return o->num_mc;
+}
+
 int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
 {
     ora_t *o = (ora_t *)o_;
@@ -2864,7 +2875,7 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
         if (!occ && o->ncov > 0 && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
             if (co >= 1 && co <= 3) c = 6 + co - 1;      /* covered: desorption */
         } else if (!occ) {
-            if (co == 1) c = (p->prob == (double)1.e-8f) ? 2 : 1;
+            if (co == 1) c = (p->prob == (double)1.e-8f) ? 2 : (p->prob == (double)1.e-6f ? 63 : 1);
             else if (co == 2) c = 3;
             else if (co == 3) c = 4;
         } else if (o->ncov > 0) {

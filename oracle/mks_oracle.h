@@ -92,17 +92,23 @@ int ora_write_frame(ora_t *o, const char *base, double time, int64_t iter);
 
 /* The state as one byte per diamond site, in the GPU engine's layout
  * (mulskips_gb300/csrc/lattice.cuh): out[(z1*LenY/6 + b)*LenX/6 + a] =
- * species | coor<<2 | first-list-entry direction<<5 | dummy<<7, 0x80 wall.
+ * species | coor<<2 | first-list-entry direction<<5 | dummy<<7, 0x80 wall; a
+ * dummy coor-1 site still at Get_Prob_Ini's rate 1e-6 has coordination
+ * field 5 (the engine's init-time dummy).
  * Returns the number of non-wall points off the diamond sub-grid (arm-chair
  * sites, which that layout cannot hold), or -1 if a list entry is not a bond. */
 int64_t ora_compact_state(const ora_t *o, uint8_t *out);
 
 /* Rate class of every listed MC particle, in the GPU engine's enumeration
  * (0 none, 1 empty coor-1, 2 empty coor-1 with the dummy rate, 3 coor-2,
- * 4 coor-3, 5 isolated atom, 6 + (species-1)*19 + census index for atoms),
+ * 4 coor-3, 5 isolated atom, 6 + (species-1)*19 + census index for atoms,
+ * 63 coor-1 dummy at Get_Prob_Ini's rate),
  * derived from the oracle's own lists and reciprocity checks.  Writes up to
  * n (class, rate) pairs and returns NumAdAtom.                              */
 int64_t ora_mc_classes(const ora_t *o, int32_t *cls, double *rate, int64_t n);
+/* Grid coordinates (x, y, z) of the MC particles in the same list order,
+ * up to n of them; returns NumAdAtom.                                      */
+int64_t ora_mc_sites(const ora_t *o, int32_t *xyz, int64_t n);
 
 /* Export the rate tables parsed from start.dat. */
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);

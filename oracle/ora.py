@@ -60,6 +60,8 @@ def lib():
         L.ora_ran3_sequence.argtypes = [C.c_int, C.c_int, C.c_void_p]
         L.ora_mc_classes.restype = C.c_int64
         L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L.ora_mc_sites.restype = C.c_int64
+        L.ora_mc_sites.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_set_la_input.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -255,6 +257,14 @@ def mc_classes(o):
     rate = np.zeros(max(n, 1), dtype=np.float64)
     m = lib().ora_mc_classes(o._h, cls.ctypes.data_as(C.c_void_p), rate.ctypes.data_as(C.c_void_p), n)
     return cls[:m], rate[:m]
+
+
+def mc_sites(o):
+    """Grid coordinates (n, 3) of the MC particles, in the order of mc_classes."""
+    n = o.counts()["mc"]
+    xyz = np.zeros((max(n, 1), 3), dtype=np.int32)
+    m = lib().ora_mc_sites(o._h, xyz.ctypes.data_as(C.c_void_p), n)
+    return xyz[:m]
 
 
 def rate_of_site(o, x, y, z):

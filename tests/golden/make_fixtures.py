@@ -1,8 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the MulSKIPS reference.
 
-Run once in a container that has the reference checkout (default path
-/root/reference, override with MULSKIPS_REF).  The outputs are committed; the
-tests read only the committed files, never the reference itself.
+Run once where the reference checkout is present, with its path given as the
+first argument or in MULSKIPS_REF (python make_fixtures.py <reference dir>).
+The outputs are committed; the tests read only the committed files, never the
+reference itself.
 
 Fixtures written:
   numberslist.txt        the 1000 test-mode uniforms of
@@ -37,10 +38,11 @@ import gzip
 import os
 import re
 import shutil
+import sys
 
-REF = os.environ.get("MULSKIPS_REF", "/root/reference")
+REF = None     # the reference checkout, set by main()
+RT = None
 HERE = os.path.dirname(os.path.abspath(__file__))
-RT = os.path.join(REF, "regression-tests", "input-and-references-files")
 CASES = ["Si-SL", "surface", "cube", "cube-zigzag", "sphere", "inverted-pyramid", "finfet", "CVD-Si-SiH2"]
 
 
@@ -169,9 +171,18 @@ REF_WRITER_CASES = {
 }
 
 
-if __name__ == "__main__":
+def main(argv):
+    global REF, RT
+    REF = argv[1] if len(argv) > 1 else os.environ.get("MULSKIPS_REF")
+    if not REF or not os.path.isdir(os.path.join(REF, "mulskips-source")):
+        raise SystemExit("usage: make_fixtures.py <MulSKIPS reference checkout> (or set MULSKIPS_REF)")
+    RT = os.path.join(REF, "regression-tests", "input-and-references-files")
     numbers_list()
     cases()
     la_case()
     cad_case()
     reference_writer()
+
+
+if __name__ == "__main__":
+    main(sys.argv)

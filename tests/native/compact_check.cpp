@@ -85,6 +85,8 @@ int main(int argc, char **argv)
                 r = pD[co - 1] + pD[3 + co - 1] + pD[6 + co - 1];
             } else if (c == 2) {
                 r = (double)1.e-8f;
+            } else if (c == CLS_C1I) {
+                r = (double)1.e-6f;
             } else if (c >= CLS_OCC0) {
                 int q = c - CLS_OCC0, sp = q / NCENSUS + 1, ci = q % NCENSUS, kk = 0;
                 for (int t = 1; t <= 3; t++)

@@ -3,6 +3,7 @@
 histogram consistent), clock and event accounting, batching."""
 import numpy as np
 import pytest
+from mulskips_gb300.engine import coordination
 
 pytestmark = pytest.mark.gpu
 
@@ -17,7 +18,7 @@ def check_invariants(st):
     nz, nb, na = st.shape
     wall = st == 0x80
     occ = ((st & 3) != 0) & ~wall
-    co = (st >> 2) & 7
+    co = coordination(st)
     z = np.arange(nz)[:, None, None]
     n_occ = np.zeros(st.shape, np.int32)
     n_wall = np.zeros(st.shape, np.int32)

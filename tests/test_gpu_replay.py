@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 def oracle_hist(ora, o):
     cls, _ = ora.mc_classes(o)
-    return np.bincount(cls, minlength=63)[:63]
+    return np.bincount(cls, minlength=64)[:64]
 
 
 def replay_case(ora, startdat, len1, kind, total, chunk, lenxyz=480):
@@ -106,3 +106,58 @@ def test_replay_rejects_inapplicable_event(oracle_lib):
         ev[0] = (0, 0, 300, 1, 0, 0)      # empty, untracked site far above the surface
         with pytest.raises(MksError):
             lat.replay(ev)
+
+
+def site_rates_case(ora, startdat, len1, kind, events):
+    """The engine's rate of every MC particle of the oracle against the
+    oracle's tree leaf (ProbTrans), at the start and after `events` replayed
+    events; returns the number of sites compared at each point."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    d = parse_startdat(startdat)
+    o = ora.Oracle(startdat, 480, 480, 480)
+    o.init()
+    pE, pD = o.rates()
+    lat = Lattice(480, 480, 480, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"],
+                  list_cov=d["list_cov"])
+    counts = []
+    try:
+        lat.set_rates(pE, pD)
+        if d["list_cov"]:
+            lat.set_coverage_rates(*o.cov_rates())
+        if kind:
+            lat.init_flat(kind, len1)
+        else:
+            lat.load_lattcoo(o.lattcoo())
+        o.trace_enable()
+        for step in range(2):
+            if step:
+                o.run(events)
+                lat.replay(o.trace())
+            xyz = ora.mc_sites(o)
+            cls_o, rate_o = ora.mc_classes(o)
+            cls_g, rate_g = lat.site_rates(xyz)
+            assert np.array_equal(cls_g, cls_o), f"step {step}: classes differ at {np.argwhere(cls_g != cls_o)[:3]}"
+            keep = cls_o != 5                      # isolated atoms: 1e5 x Tree(1), dynamic
+            # FP32 class rates of the engine against the FP64 leaves of the reference
+            assert np.array_equal(rate_g[keep], rate_o[keep].astype(np.float32)), f"step {step}: rates differ"
+            counts.append((int(keep.sum()), int(np.count_nonzero(cls_o == 63)), int(np.count_nonzero(cls_o == 2))))
+        return counts
+    finally:
+        lat.close()
+        o.close()
+
+
+@pytest.mark.parametrize("case,len1,kind", [("Si-SL", 360, "S"), ("CVD-Si-SiH2", 48, "S"), ("cube", 0, None)])
+def test_site_rates_match_oracle_leaves(oracle_lib, case, len1, kind):
+    """Per-site rates, not only classes: every MC particle's tree leaf in the
+    oracle (Get_Prob / Get_Prob_Ini's ProbTrans) equals the engine's rate of
+    that site, right after initialization and after 20000 replayed events.
+    The cube's initializer (SetNC) rates its unsupported coor-1 sites with
+    Get_Prob_Ini's 1e-6, which they keep until they change; later dummies
+    take Get_Prob's 1e-8."""
+    counts = site_rates_case(oracle_lib, os.path.join(GOLDEN, case, "start.dat"), len1, kind, 20000)
+    print(case, counts)
+    assert counts[0][0] > 1000
+    if case == "cube":
+        assert counts[0][1] > 0                    # initial dummies at 1e-6

@@ -369,6 +369,22 @@ def test_mulskips_e_continuation_run(tmp_path):
     first = (d2 / "I00000000.xyz").read_text().splitlines()
     assert first[0].split()[0] == last[0].split()[0] and first[1:] == last[1:]
     assert int((d2 / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 4000
+    # a checkpoint written by a Fortran runtime that wraps long list-directed
+    # records across lines (here 37 values per line) reads as the same
+    # LattCoo: each READ takes LenX*LenY values across line breaks and skips
+    # the rest of its last record
+    d3 = tmp_path / "wrapped"
+    d3.mkdir()
+    with open(d3 / "final.dat", "w") as f:
+        for rec in (d1 / "final.dat").read_text().splitlines():
+            vals = rec.split()
+            for i in range(0, len(vals), 37):
+                f.write(" " + " ".join(vals[i:i + 37]) + "\n")
+    (d3 / "start.dat").write_text(startdat("C", str(d3 / "final.dat"), False))
+    r = subprocess.run([EXE], cwd=d3, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d3 / "I00000000.xyz").read_text().splitlines()[1:] == first[1:]
+    assert (d3 / "I00000001.xyz").read_text() == (d2 / "I00000001.xyz").read_text()
 
 
 def test_mulskips_e_cad_sige(oracle_lib, tmp_path):

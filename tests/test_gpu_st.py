@@ -73,11 +73,11 @@ def test_tabulated_rates_match_oracle(oracle_lib, tmp_path):
     # class rates at the hottest temperature: C1, C2, C3 and atoms of coordination 1..3
     w = (TTOP - 1100.0) / 200.0
     hot = lambda lo, hi: (1 - w) * lo + w * hi
-    rate = np.zeros(63)
+    rate = np.zeros(64)
     rate[1], rate[3], rate[4] = (hot(ROWS[1][2][n], ROWS[2][2][n]) for n in range(3))
     rate[6], rate[9], rate[15] = (hot(ROWS[1][1][n], ROWS[2][1][n]) for n in range(3))
     hist = b.class_histogram()[0]
-    rstar = rate[int(np.argmax(hist[:63] * rate))]
+    rstar = rate[int(np.argmax(hist[:64] * rate))]
     nwin = int(math.ceil(T_OBS / (0.3 / rstar)))
     b.run(T_OBS / nwin, nwin)
     g = np.array([x["atoms"] for x in b.observables()], float)

@@ -8,6 +8,7 @@ the reference's integer-weighted interpolation at the site's temperature."""
 import os
 
 import numpy as np
+from mulskips_gb300.engine import coordination
 
 
 def write_st(d, ttop, tbottom, rows, run_type="T", iters=20000, seed=9117116, box=(480, 480, 480),
@@ -72,7 +73,7 @@ def test_site_rates_are_the_interpolated_tables(oracle_lib, tmp_path):
     checked = 0
     for z1, b, a in zip(*np.nonzero((st != 0) & (st != 0x80))):
         s = int(st[z1, b, a])
-        co, sp = (s >> 2) & 7, s & 3
+        co, sp = int(coordination(np.uint8(s))), s & 3
         if (sp and co > 3) or (not sp and (co == 0 or co == 4)):
             continue
         x, y, z = 3 * (2 * a + (z1 & 1)), 3 * (2 * b + (z1 & 1)), 3 * z1

@@ -17,6 +17,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
+from mulskips_gb300.engine import coordination
 
 HELPER_SRC = os.path.join(ROOT, "tests", "native", "shape_check.cpp")
 NUMBERS = os.path.join(GOLDEN, "numberslist.txt")
@@ -181,7 +182,7 @@ def test_library_sh_equals_oracle_pyramid(helper, oracle_lib, tmp_path):
     st, _ = oracle_lib.compact_state(o)
     o.close()
     # the facets hold 2- and 3-coordinated atoms; first entries vary with the scan
-    co = (st >> 2) & 7
+    co = coordination(st)
     occ = (st & 3) != 0
     assert ((co == 2) & occ).sum() > 100 and ((co == 3) & occ).sum() > 100
     assert len(np.unique((st[occ & (co <= 3)] >> 5) & 3)) > 1
