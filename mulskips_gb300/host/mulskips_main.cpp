@@ -570,9 +570,9 @@ int main()
     // the field's hottest temperature (PtransE / PtransD are barriers in eV)
     auto la_tau = [&]() {
         const double kb = 0.00008617330350;           // Get_Prob.f:70
-        int64_t hist[64] = {0};
-        check(mks_class_histogram(h, hist, 63));
-        double rate[64] = {0};
+        int64_t hist[MKS_NCLASS] = {0};
+        check(mks_class_histogram(h, hist, MKS_NCLASS));
+        double rate[MKS_NCLASS] = {0};
         double fe = 0.5 * (1.0 + erf((la_tmax - in.Tflex) / in.sigma));
         const int dep_cls[3] = {1, 3, 4}, occ_cls[3] = {6, 9, 15};   // C1, C2, C3; census 1, 2, 3
         for (int n = 1; n <= 3; n++) {
@@ -581,7 +581,7 @@ int main()
             rate[occ_cls[n - 1]] = e != 0.0 ? in.P0 * exp(-e / (kb * la_tmax)) : 0.0;
         }
         double best = 0.0, rs = 0.0;
-        for (int c = 0; c < 63; c++)
+        for (int c = 0; c < MKS_NCLASS; c++)
             if ((double)hist[c] * rate[c] > best) {
                 best = (double)hist[c] * rate[c];
                 rs = rate[c];

@@ -33,6 +33,13 @@ Fixtures written:
   refwriter/{cvd,in_sige,la}.dat
                          the same writer for the process objects of
                          process_stubs.py (REF_WRITER_CASES below)
+  analysis.json          the reference's post-processing on its own frames:
+                         pymulskips.analyze.get_surface_height of every
+                         golden I0000000{0,1}.xyz (default and a second set
+                         of bin_size / surface_roughness), and
+                         analyze_growth_rate ('finitediff' and 'polyfit',
+                         Nexclude 2) of the synthetic frame series of
+                         growth_series() below
 """
 import gzip
 import os
@@ -171,6 +178,72 @@ REF_WRITER_CASES = {
 }
 
 
+def growth_series(frame_lines, k):
+    """Frame k of a synthetic growth series built from the lines of one
+    golden frame: every z shifted by 0.9 k + 0.3 sin(k) A, at time
+    10 k + k^2 / 7 s.  Returns (time, lines)."""
+    import math
+    t = 10.0 * k + k * k / 7.0
+    dz = 0.9 * k + 0.3 * math.sin(k)
+    out = []
+    for line in frame_lines:
+        sym, x, y, z = line.split()[:4]
+        out.append(f"{sym} {x} {y} {float(z) + dz:.5f}")
+    return t, out
+
+
+def analysis():
+    import glob as globmod
+    import json
+    import tempfile
+    import types
+    import warnings
+    sys.path.insert(0, REF)
+    # analyze_growth_rate imports matplotlib.pyplot before its work even with
+    # plotting=False; this checkout has no matplotlib, so a module without
+    # content stands in (nothing of it is called)
+    mpl = types.ModuleType("matplotlib")
+    mpl.pyplot = types.ModuleType("matplotlib.pyplot")
+    sys.modules.setdefault("matplotlib", mpl)
+    sys.modules.setdefault("matplotlib.pyplot", mpl.pyplot)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import pymulskips.analyze as ref_an
+    out = {"surface_height": {}, "surface_height_b3_r10": {}, "growth": {}}
+    cases = sorted(c for c in os.listdir(HERE) if os.path.exists(os.path.join(HERE, c, "I00000000.xyz.gz")))
+    with tempfile.TemporaryDirectory() as tmp:
+        for case in cases:
+            for fr in ("I00000000", "I00000001"):
+                p = os.path.join(tmp, f"{case}-{fr}.xyz")
+                with gzip.open(os.path.join(HERE, case, fr + ".xyz.gz"), "rb") as fi, open(p, "wb") as fo:
+                    fo.write(fi.read())
+                key = f"{case}/{fr}"
+                out["surface_height"][key] = ref_an.get_surface_height(p)
+                out["surface_height_b3_r10"][key] = ref_an.get_surface_height(p, bin_size=3.0, surface_roughness=10.0)
+        # growth series from the Si-SL final frame; the reference globs the
+        # frames unsorted, so the series is handed over in time order
+        with gzip.open(os.path.join(HERE, "Si-SL", "I00000001.xyz.gz"), "rt") as f:
+            lines = f.read().splitlines()
+        hdr, box, body = lines[0].split(), lines[1], lines[2:]
+        run = os.path.join(tmp, "series")
+        os.makedirs(run)
+        for k in range(9):
+            t, fl = growth_series(body, k)
+            with open(os.path.join(run, f"I{k:08d}.xyz"), "w") as f:
+                f.write(f" {hdr[0]} angstroem KMC-time: {t!r} Iter: {k}\n{box}\n" + "\n".join(fl) + "\n")
+        orig = globmod.glob
+        globmod.glob = lambda pat, *a, **kw: sorted(orig(pat, *a, **kw))
+        try:
+            for m in ("finitediff", "polyfit"):
+                gr, h = ref_an.analyze_growth_rate(run, method=m, plotting=False, return_surf_height=True)
+                out["growth"][m] = {"rate": gr, "heights": [float(v) for v in h]}
+        finally:
+            globmod.glob = orig
+    with open(os.path.join(HERE, "analysis.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+        f.write("\n")
+
+
 def main(argv):
     global REF, RT
     REF = argv[1] if len(argv) > 1 else os.environ.get("MULSKIPS_REF")
@@ -182,6 +255,7 @@ def main(argv):
     la_case()
     cad_case()
     reference_writer()
+    analysis()
 
 
 if __name__ == "__main__":

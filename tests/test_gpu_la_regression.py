@@ -8,7 +8,8 @@ initializer (pinned byte for byte to the reference's frames), the rate law is
 mulskips-source/mcevent/Get_Prob.f:127-149 (no liquid fraction).  Atoms at
 t = 2e-10 s and 4e-10 s: 32 GPU replicas (sublattice windows, exponential
 waiting times) against 32 oracle runs (RunType R, the reference's clock);
-the difference of the means must lie inside the 3-sigma band.
+the difference of the means must lie inside the 95 % family band (Welch t,
+Bonferroni over the two times, tests/stat_bands.py).
 """
 import math
 import multiprocessing as mp
@@ -98,12 +99,9 @@ def test_la_law_matches_oracle_on_regression_input(initial, oracle_runs):
         got.append([o["atoms"] for o in b.observables()])
     b.close()
     got = np.array(got, dtype=float).T
-    print(f"\ninitial atoms {atoms0}, tau {tau:.3e}")
+    from stat_bands import Family
+    fam = Family(f"LA regression lattice, initial atoms {atoms0}, tau {tau:.3e}", len(MARKS))
     for j, m in enumerate(MARKS):
-        g, o = got[:, j], oracle_runs[:, j]
-        d = g.mean() - o.mean()
-        band = 3.0 * math.sqrt(g.var(ddof=1) / N + o.var(ddof=1) / N)
-        print(f"t={m:.1e}: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f} oracle {o.mean():.1f}+-{o.std(ddof=1):.1f} "
-              f"diff {d:.1f} band +-{band:.1f}")
-        assert o.mean() > atoms0 + 100          # the pocket regrows
-        assert abs(d) < band
+        assert oracle_runs[:, j].mean() > atoms0 + 100          # the pocket regrows
+        fam.add(f"atoms at t={m:.1e}", got[:, j], oracle_runs[:, j])
+    fam.check()

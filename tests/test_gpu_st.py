@@ -4,12 +4,12 @@
 A Si trench (SetTrenchSi, 480^3 grid, Len = 60, Len2 = 60, Len3 = 120,
 70 degrees) under a temperature gradient from 1000 K at the bottom to
 1250 K at the top, rates tabulated at 950, 1100 and 1300 K (all rising with
-T; coor-2 evaporation comparable to deposition), RunType R.  Atoms at
-t = 100 s: 16 oracle runs against 16 GPU replicas
-loaded from the oracle's initial LattCoo (lattice and temperatures), window
-0.3 / r* with r* the rate of the class carrying the largest share at the
-hottest temperature.  The difference of the means must lie inside the
-3-sigma band."""
+T; coor-2 evaporation comparable to deposition), RunType R.  Atoms and RMS
+roughness at t = 100 s: 32 oracle runs against 32 GPU replicas loaded from
+the oracle's initial LattCoo (lattice and temperatures), window 0.3 / r*
+with r* the rate of the class carrying the largest share at the hottest
+temperature.  The differences of the means must lie inside the 95 % family
+band (Welch t, Bonferroni over the two observables, tests/stat_bands.py)."""
 import math
 import multiprocessing as mp
 import os
@@ -26,7 +26,7 @@ ROWS = [(950, (3.0e2, 0.15, 0.002), (0.5, 0.5, 0.5)),
         (1300, (9.0e2, 0.6, 0.008), (0.6, 0.6, 0.6))]
 TTOP, TBOTTOM = 1250.0, 1000.0
 T_OBS = 100.0
-N = 16
+N = 32
 
 
 def _oracle_atoms(args):
@@ -37,7 +37,9 @@ def _oracle_atoms(args):
     o = ora.Oracle(path, 480, 480, 480, numbers=None)
     o.init()
     o.run_until(T_OBS)
-    n = o.atoms()
+    from mulskips_gb300 import analyze as an
+    st, _ = ora.compact_state(o)
+    n = (o.atoms(), an.height_stats(st)[1])
     o.close()
     return n
 
@@ -80,11 +82,11 @@ def test_tabulated_rates_match_oracle(oracle_lib, tmp_path):
     rstar = rate[int(np.argmax(hist[:64] * rate))]
     nwin = int(math.ceil(T_OBS / (0.3 / rstar)))
     b.run(T_OBS / nwin, nwin)
-    g = np.array([x["atoms"] for x in b.observables()], float)
+    g = np.array([(x["atoms"], x["rms_roughness"]) for x in b.observables()], float)
     b.close()
-    d = g.mean() - ref.mean()
-    band = 3.0 * math.sqrt(g.var(ddof=1) / N + ref.var(ddof=1) / N)
-    print(f"\nST: atoms0 {atoms0} gpu {g.mean():.1f}+-{g.std(ddof=1):.1f} oracle {ref.mean():.1f}"
-          f"+-{ref.std(ddof=1):.1f} diff {d:.1f} band +-{band:.1f} ({nwin} windows)")
-    assert abs(ref.mean() - atoms0) > 5 * band        # the trench evolves
-    assert abs(d) < band
+    from stat_bands import Family
+    fam = Family(f"ST trench, atoms0 {atoms0} ({nwin} windows)", 2)
+    fam.add("atoms", g[:, 0], ref[:, 0])
+    fam.add("RMS roughness", g[:, 1], ref[:, 1])
+    assert abs(ref[:, 0].mean() - atoms0) > 10 * ref[:, 0].std(ddof=1) / math.sqrt(N)   # the trench evolves
+    fam.check()

@@ -1,261 +1,296 @@
 """Statistical parity of the sublattice KMC with the serial reference.
 
-The plain Si(001) model at T = 1100 K (the benchmark's model, 480^3 box,
-Len1 = 120 slab) etches.  Observable: atoms left at time T_obs (the etch
-rate).  32 seeds of the serial oracle (RunType R, exact reference dynamics,
-deterministic dt = 1/R_tot) against 32 GPU replicas (exponential waiting
-times, synchronous sublattice windows of length tau).  The difference of the
-means must lie inside the 3-sigma band of the difference (99.7 %; several
-statistical checks run together, so a 95 % band would fail by chance too
-often)."""
+The sublattice engine and the serial reference are different samplers of the
+same process: each test runs 32 GPU replicas (exponential waiting times,
+synchronous sublattice windows of length tau, stated per test) and 32 seeds
+of the serial oracle (RunType R: the reference's own dynamics with dt =
+1/R_tot), each replica or seed with its own seed, and compares the means of
+the trajectory observables the reference itself reports:
+
+  atoms        atoms in the box at t_obs (the net grown or etched amount),
+  growth rate  pymulskips' analyze_growth_rate ('finitediff', Nexclude = 2;
+               pymulskips/analyze.py:209-416) of the surface heights
+               (get_surface_height, :124-207) of nine frames at t = 0, t_obs/8,
+               ..., t_obs, in micron/hour (mulskips_gb300.analyze restates
+               both and is pinned to them by tests/test_analysis.py),
+  RMS          RMS roughness of the column heights at t_obs,
+  C atoms / covered sites where the model has them (3C-SiC / CVD coverage).
+
+Band: Welch's two-sample t band of the difference of the means at level
+1 - 0.05/k for each of the k observables of a test (Bonferroni), i.e. 95 %
+confidence for the test as a whole (tests/stat_bands.py).  The window
+length is stated per case as f = tau * r*, r* the rate of the class that
+carries the largest share of the replica's rate (mks_suggest_tau)."""
 import math
+import multiprocessing as mp
 import os
 
 import numpy as np
 import pytest
 
+from conftest import GOLDEN, ROOT
+from stat_bands import Family
+
 pytestmark = pytest.mark.gpu
 
-T_OBS = 4e-7
 NSEEDS = 32
+NFRAMES = 8
+KB = 0.00008617330350
 
 
-def oracle_atoms(ora, tmp_path, seed):
-    from mulskips_gb300.startdat import write_plain_si_startdat
-    p = tmp_path / f"start{seed}.dat"
-    write_plain_si_startdat(str(p), T=1100.0, len1=120, max_iter=10 ** 9, seed=seed)
-    o = ora.Oracle(str(p), 480, 480, 480, numbers=None)
+def k2(T):
+    """Coordination-2 evaporation rate of the plain Si(001) model."""
+    return 1e13 * math.exp(-1.2 / (KB * T))
+
+
+def _oracle_run(args):
+    """One serial oracle run (RunType R): frames at `times`; returns (frame
+    times, surface heights, observables of the last frame)."""
+    import sys
+    path, box, times, sf, cov, root = args
+    sys.path.insert(0, root)
+    from oracle import ora
+    from mulskips_gb300 import analyze as an
+    o = ora.Oracle(path, box[0], box[1], box[2], numbers=None)
     o.init()
-    o.run_until(T_OBS)
-    n = o.atoms()
+    zl = box[2] * sf
+    st, _ = ora.compact_state(o)
+    ts, hs = [0.0], [an.surface_height(an.frame_z(st, sf, cov), zl)]
+    for t in times:
+        o.run_until(t)
+        st, off = ora.compact_state(o)
+        assert off == 0
+        ts.append(o.time)
+        hs.append(an.surface_height(an.frame_z(st, sf, cov), zl))
+    obs = an.state_observables(st, cov)
+    assert obs["atoms"] == o.atoms()
     o.close()
-    return n
+    return ts, hs, obs
 
 
-def gpu_atoms(tau, seeds):
-    from mulskips_gb300 import Batch, arrhenius_tables
-    pE, pD = arrhenius_tables(1100.0)
-    n = len(seeds)
-    b = Batch([(480, 480, 480)] * n, seeds=seeds)
-    b.set_rates(np.stack([pE] * n), np.stack([pD] * n))
-    b.init_flat("S", [120] * n)
-    nwin = int(round(T_OBS / tau))
-    b.run(tau, nwin)
+def oracle_sample(paths, box, t_obs, sf, cov=False):
+    """Serial runs of the start.dat files `paths` in parallel processes."""
+    times = [t_obs * (k + 1) / NFRAMES for k in range(NFRAMES)]
+    with mp.get_context("spawn").Pool(min(len(paths), os.cpu_count() or 1)) as pool:
+        return pool.map(_oracle_run, [(p, box, times, sf, cov, ROOT) for p in paths])
+
+
+def gpu_sample(b, tau, nwin, box, sf, cov=False):
+    """Run batch b for nwin windows of length tau in NFRAMES chunks; returns
+    per replica (frame times, surface heights, observables at the end)."""
+    from mulskips_gb300 import analyze as an
+    assert nwin % NFRAMES == 0
+    zl = box[2] * sf
+    hs = [[an.surface_height(an.frame_z(b.state(r), sf, cov), zl)] for r in range(b.n)]
+    for k in range(NFRAMES):
+        b.run(tau, nwin // NFRAMES)
+        for r in range(b.n):
+            hs[r].append(an.surface_height(an.frame_z(b.state(r), sf, cov), zl))
     obs = b.observables()
+    ts = [tau * nwin * k / NFRAMES for k in range(NFRAMES + 1)]
+    for r in range(b.n):
+        assert abs(obs[r]["time"] - ts[-1]) <= 1e-9 * ts[-1], "a replica stopped early"
+        # the device's column statistics are the host definition's
+        m, rms = an.height_stats(b.state(r))
+        assert abs(obs[r]["mean_height"] - m) < 1e-9 * max(1.0, m) and abs(obs[r]["rms_roughness"] - rms) < 1e-9 * max(1.0, rms)
+    return [(ts, hs[r], obs[r]) for r in range(b.n)]
+
+
+def growth(sample):
+    from mulskips_gb300 import analyze as an
+    return np.array([an.growth_rate(ts, hs)[1] for ts, hs, _ in sample])
+
+
+def column(sample, key, idx=None):
+    return np.array([o[key] if idx is None else o[key][idx] for _, _, o in sample], dtype=float)
+
+
+def windows_for(t_obs, tau):
+    """Window count: a multiple of the frame count, windows no longer than tau."""
+    return NFRAMES * int(math.ceil(t_obs / tau / NFRAMES))
+
+
+def startdats(tmp_path, case, runtype_line, seed0, n, name):
+    txt = open(os.path.join(GOLDEN, case, "start.dat")).read()
+    a, b_ = runtype_line
+    assert a in txt
+    txt = txt.replace(a, b_)
+    paths = []
+    for s in range(n):
+        p = tmp_path / f"{name}{s}.dat"
+        p.write_text(txt.replace("9117116 ! Random seed", f"{seed0 + s} ! Random seed"))
+        paths.append(str(p))
+    return paths
+
+
+# ---------------------------------------------------------------- etch (the benchmark's model)
+_ETCH_REF = {}
+
+
+def etch_oracle(tmp_path_factory, T):
+    """32 serial runs of the plain Si(001) model at T (480^3 box, Len1 = 120),
+    to t_obs = 4e-7 s x k2(1100 K) / k2(T) (the same etched amount at each T)."""
+    if T not in _ETCH_REF:
+        from mulskips_gb300.startdat import write_plain_si_startdat
+        tmp = tmp_path_factory.mktemp(f"etch{int(T)}")
+        paths = []
+        for s in range(NSEEDS):
+            p = tmp / f"start{s}.dat"
+            write_plain_si_startdat(str(p), T=T, len1=120, max_iter=10 ** 9, seed=100 + s)
+            paths.append(str(p))
+        t_obs = 4e-7 * k2(1100.0) / k2(T)
+        _ETCH_REF[T] = (t_obs, oracle_sample(paths, (480, 480, 480), t_obs, 0.4525))
+    return _ETCH_REF[T]
+
+
+# (T, tile width, k2 tau): the benchmark's window rule f = 0.3 and tile width 6
+# at its three temperatures, on the same model in a 480^3 box; and a shorter
+# window at the default width
+@pytest.mark.parametrize("T,width,f", [(1000.0, 6, 0.3), (1100.0, 6, 0.3), (1200.0, 6, 0.3), (1100.0, 8, 0.064)])
+def test_etch_matches_serial_reference(tmp_path_factory, T, width, f):
+    from mulskips_gb300 import Batch, arrhenius_tables
+    t_obs, ref = etch_oracle(tmp_path_factory, T)
+    pE, pD = arrhenius_tables(T)
+    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[1 + s for s in range(NSEEDS)], sf=0.4525)
+    b.set_rates(np.stack([pE] * NSEEDS), np.stack([pD] * NSEEDS))
+    b.init_flat("S", [120] * NSEEDS)
+    b.set_tiling(width)
+    nwin = windows_for(t_obs, f / k2(T))
+    tau = t_obs / nwin
+    g = gpu_sample(b, tau, nwin, (480, 480, 480), 0.4525)
     b.close()
-    assert all(abs(o["time"] - nwin * tau) < 1e-12 for o in obs)
-    return np.array([o["atoms"] for o in obs], dtype=float)
+    fam = Family(f"etch T={T:.0f} K width {width} k2*tau={k2(T) * tau:.3f} ({nwin} windows)", 3)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("growth rate um/h", growth(g), growth(ref))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    assert column(ref, "atoms").mean() < 3200 * 36 - 5000          # etching happened
+    fam.check()
 
 
-def band(x, y):
-    d = x.mean() - y.mean()
-    se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
-    return d, 3.0 * se
-
-
-@pytest.fixture(scope="module")
-def oracle_sample(oracle_lib, tmp_path_factory):
-    tmp = tmp_path_factory.mktemp("stat")
-    return np.array([oracle_atoms(oracle_lib, tmp, 100 + s) for s in range(NSEEDS)], dtype=float)
-
-
-# k2 = 1e13 exp(-1.2 eV / kT) at 1100 K is the coor-2 evaporation rate: 2e-9 s
-# is k2 tau = 0.064; T_OBS / 43 is k2 tau = 0.296, the f = 0.3 window rule of
-# the engine's tau suggestion
-@pytest.mark.parametrize("tau", [2e-9, T_OBS / 43])
-def test_etch_rate_matches_serial_reference(oracle_sample, tau):
-    g = gpu_atoms(tau, [1 + s for s in range(NSEEDS)])
-    d, hw = band(g, oracle_sample)
-    start = 3200 * 36
-    print(f"tau={tau}: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f}  serial {oracle_sample.mean():.1f}"
-          f"+-{oracle_sample.std(ddof=1):.1f}  diff {d:.1f}  3-sigma band +-{hw:.1f}")
-    assert g.mean() < start and oracle_sample.mean() < start       # etching happened
-    assert abs(d) <= hw, f"etch-rate difference {d:.1f} atoms outside the 3-sigma band {hw:.1f}"
-
-
-def test_deposition_evaporation_regime_matches_serial_reference(oracle_lib, tmp_path):
+# ---------------------------------------------------------------- deposition + evaporation
+def test_deposition_evaporation_regime_matches_serial_reference(tmp_path):
     """The Si-SL regression rates with RunType R (deposition 9.3e-4 against
-    coor-2 evaporation 2.0e-3, so both event kinds matter): atoms left at
-    t = 1e4 s, 16 oracle seeds against 16 GPU replicas at the autotuned tau."""
+    coor-2 evaporation 2.0e-3, so both event kinds matter): t_obs = 1e4 s at
+    the single-species window f = 0.3."""
     from mulskips_gb300 import Batch
     from mulskips_gb300.startdat import parse_startdat
-    from conftest import GOLDEN
-    txt = open(os.path.join(GOLDEN, "Si-SL", "start.dat")).read().replace("T   ! R = production run",
-                                                                            "R   ! R = production run")
-    ref = []
-    for s in range(16):
-        p = tmp_path / f"sl{s}.dat"
-        p.write_text(txt.replace("9117116 ! Random seed", f"{200 + s} ! Random seed"))
-        o = oracle_lib.Oracle(str(p), 480, 480, 480, numbers=None)
-        o.init()
-        o.run_until(1e4)
-        ref.append(o.atoms())
-        o.close()
-    ref = np.array(ref, float)
-    d = parse_startdat(str(tmp_path / "sl0.dat"))
-    n = 16
-    b = Batch([(480, 480, 480)] * n, seeds=[31 + s for s in range(n)], sf=d["sf"])
-    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
-    b.init_flat("S", [360] * n)
-    tau = float(b.suggest_tau(0.3)[0])
-    nwin = int(round(1e4 / tau))
-    b.run(1e4 / nwin, nwin)
-    g = np.array([o["atoms"] for o in b.observables()], float)
+    paths = startdats(tmp_path, "Si-SL", ("T   ! R = production run", "R   ! R = production run"), 200, NSEEDS, "sl")
+    d = parse_startdat(paths[0])
+    ref = oracle_sample(paths, (480, 480, 480), 1e4, d["sf"])
+    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[31 + s for s in range(NSEEDS)], sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
+    b.init_flat("S", [360] * NSEEDS)
+    nwin = windows_for(1e4, float(b.suggest_tau(0.3)[0]))
+    g = gpu_sample(b, 1e4 / nwin, nwin, (480, 480, 480), d["sf"])
     b.close()
-    diff, hw = band(g, ref)
-    print(f"Si-SL rates: gpu {g.mean():.1f}+-{g.std(ddof=1):.1f} serial {ref.mean():.1f}+-{ref.std(ddof=1):.1f} "
-          f"diff {diff:.1f} 3-sigma band +-{hw:.1f}")
-    assert abs(diff) <= hw
+    fam = Family(f"Si-SL rates, f = 0.3 ({nwin} windows)", 3)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("growth rate um/h", growth(g), growth(ref))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    fam.check()
 
 
-def test_sic_surface_matches_serial_reference(oracle_lib, tmp_path):
+# ---------------------------------------------------------------- 3C-SiC
+def test_sic_surface_matches_serial_reference(tmp_path):
     """3C-SiC(001), the rates of the reference's `surface` regression case
     (NCrystal 2, Si and C with 18 census-dependent evaporation rates), RunType
-    R: atoms and C atoms at t = 2e5 s, 16 oracle seeds against 16 GPU
-    replicas at the two-species window factor f = 0.03."""
+    R, t_obs = 2e5 s, at the two-species window factor."""
     from mulskips_gb300 import Batch
-    from mulskips_gb300.startdat import parse_startdat
-    from conftest import GOLDEN
-    t_obs = 2e5
-    txt = open(os.path.join(GOLDEN, "surface", "start.dat")).read().replace(
-        "T   ! R = production run", "R   ! R = production run")
-    ref, ref_c = [], []
-    for s in range(16):
-        p = tmp_path / f"sic{s}.dat"
-        p.write_text(txt.replace("9117116 ! Random seed", f"{400 + s} ! Random seed"))
-        o = oracle_lib.Oracle(str(p), 480, 480, 480, numbers=None)
-        o.init()
-        o.run_until(t_obs)
-        st, _ = oracle_lib.compact_state(o)
-        ref.append(int(np.count_nonzero((st & 3) != 0)))
-        ref_c.append(int(np.count_nonzero((st & 3) == 2)))
-        o.close()
-    ref, ref_c = np.array(ref, float), np.array(ref_c, float)
-    d = parse_startdat(str(tmp_path / "sic0.dat"))
-    n = 16
-    b = Batch([(480, 480, 480)] * n, seeds=[51 + s for s in range(n)], ncrystal=2, list_crystal=(14, 6),
-              sf=d["sf"])
-    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
-    b.init_flat("C", [d["len"][0]] * n)
     from mulskips_gb300.autotune import accurate_f
-    tau = float(b.suggest_tau(accurate_f(2))[0])
-    nwin = int(math.ceil(t_obs / tau))
-    b.run(t_obs / nwin, nwin)
-    obs = b.observables()
+    from mulskips_gb300.startdat import parse_startdat
+    paths = startdats(tmp_path, "surface", ("T   ! R = production run", "R   ! R = production run"), 400, NSEEDS,
+                      "sic")
+    d = parse_startdat(paths[0])
+    ref = oracle_sample(paths, (480, 480, 480), 2e5, d["sf"])
+    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[51 + s for s in range(NSEEDS)], ncrystal=2, list_crystal=(14, 6),
+              sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
+    b.init_flat("C", [d["len"][0]] * NSEEDS)
+    f = accurate_f(2)
+    nwin = windows_for(2e5, float(b.suggest_tau(f)[0]))
+    g = gpu_sample(b, 2e5 / nwin, nwin, (480, 480, 480), d["sf"])
     b.close()
-    g = np.array([o["atoms"] for o in obs], float)
-    gc = np.array([o["species"][1] for o in obs], float)
-    for name, x, y in (("atoms", g, ref), ("C atoms", gc, ref_c)):
-        diff, hw = band(x, y)
-        print(f"SiC {name}: gpu {x.mean():.1f}+-{x.std(ddof=1):.1f} serial {y.mean():.1f}+-{y.std(ddof=1):.1f} "
-              f"diff {diff:.1f} 3-sigma band +-{hw:.1f} (tau {tau:.3e})")
-        assert abs(diff) <= hw, name
+    fam = Family(f"3C-SiC(001) surface rates, f = {f} ({nwin} windows)", 4)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("C atoms", column(g, "species", 1), column(ref, "species", 1))
+    fam.add("growth rate um/h", growth(g), growth(ref))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    fam.check()
 
 
-def test_sic_facets_match_serial_reference(oracle_lib, tmp_path):
+def test_sic_facets_match_serial_reference(tmp_path):
     """3C-SiC on {111} facets: a square pyramid with {111} faces on a (001)
     slab (InitSt SH point list, 240^3 box), the rates of the reference's
-    `surface` case, RunType R: atoms and C atoms at t = 2e5 s (about 2.5e5
-    events, the facets filling in), 16 oracle seeds against 16 GPU replicas
-    at the two-species window factor."""
+    `surface` case, RunType R, t_obs = 2e5 s (about 2.5e5 events, the facets
+    filling in), at the two-species window factor."""
     from mulskips_gb300 import Batch
     from mulskips_gb300.autotune import accurate_f
     from mulskips_gb300.startdat import parse_startdat, read_shape_points
-    from conftest import GOLDEN
     from test_shape_points import pyramid_points, sh_startdat, write_points
-    t_obs, n, L = 2e5, 16, 240
+    L, t_obs = 240, 2e5
     xyz, sym, _, _ = pyramid_points(L, 60, 54)
     write_points(tmp_path / "p.xyz", xyz, sym)
     txt = open(os.path.join(GOLDEN, "surface", "start.dat")).read().replace(
         "T   ! R = production run", "R   ! R = production run")
-    ref, ref_c = [], []
-    for s in range(n):
+    paths = []
+    for s in range(NSEEDS):
         p = tmp_path / f"fac{s}.dat"
         sh_startdat(txt.replace("9117116 ! Random seed", f"{600 + s} ! Random seed").splitlines(), p,
                     str(tmp_path / "p.xyz"))
-        o = oracle_lib.Oracle(str(p), L, L, L, numbers=None)
-        o.init()
-        o.run_until(t_obs)
-        st, _ = oracle_lib.compact_state(o)
-        ref.append(int(np.count_nonzero((st & 3) != 0)))
-        ref_c.append(int(np.count_nonzero((st & 3) == 2)))
-        o.close()
-    ref, ref_c = np.array(ref, float), np.array(ref_c, float)
-    d = parse_startdat(str(tmp_path / "fac0.dat"))
+        paths.append(str(p))
+    d = parse_startdat(paths[0])
+    ref = oracle_sample(paths, (L, L, L), t_obs, d["sf"])
     pts, sp = read_shape_points(str(tmp_path / "p.xyz"))
-    b = Batch([(L, L, L)] * n, seeds=[81 + s for s in range(n)], ncrystal=2, list_crystal=(14, 6), sf=d["sf"])
-    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
-    for r in range(n):
+    b = Batch([(L, L, L)] * NSEEDS, seeds=[81 + s for s in range(NSEEDS)], ncrystal=2, list_crystal=(14, 6),
+              sf=d["sf"])
+    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
+    for r in range(NSEEDS):
         b.init_points(r, pts, sp)
     start = np.array([o["atoms"] for o in b.observables()], float)
-    tau = float(b.suggest_tau(accurate_f(2))[0])
-    nwin = int(math.ceil(t_obs / tau))
-    b.run(t_obs / nwin, nwin)
-    obs = b.observables()
+    f = accurate_f(2)
+    nwin = windows_for(t_obs, float(b.suggest_tau(f)[0]))
+    g = gpu_sample(b, t_obs / nwin, nwin, (L, L, L), d["sf"])
     b.close()
-    g = np.array([o["atoms"] for o in obs], float)
-    gc = np.array([o["species"][1] for o in obs], float)
-    assert g.mean() - start.mean() > 1000
-    for name, x, y in (("atoms", g, ref), ("C atoms", gc, ref_c)):
-        diff, hw = band(x, y)
-        print(f"SiC facets {name}: gpu {x.mean():.1f}+-{x.std(ddof=1):.1f} serial {y.mean():.1f}+-{y.std(ddof=1):.1f} "
-              f"diff {diff:.1f} 3-sigma band +-{hw:.1f} (tau {tau:.3e}, {nwin} windows)")
-        assert abs(diff) <= hw, name
+    assert column(g, "atoms").mean() - start.mean() > 1000
+    fam = Family(f"3C-SiC {{111}} facets, f = {f} ({nwin} windows)", 3)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("C atoms", column(g, "species", 1), column(ref, "species", 1))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    fam.check()
 
 
-def _cvd_oracle(args):
-    """One RunType R oracle run of the CVD case to t_obs: (atoms, covered)."""
-    import sys
-    path, t_obs, root = args
-    sys.path.insert(0, root)
-    from oracle import ora
-    o = ora.Oracle(path, 480, 480, 480, numbers=None)
-    o.init()
-    o.run_until(t_obs)
-    st, _ = ora.compact_state(o)
-    out = (o.atoms(), int(np.count_nonzero((st & 3) == 3)))
-    o.close()
-    return out
+# ---------------------------------------------------------------- CVD with hydrogen coverage
+_CVD_REF = {}
 
 
 @pytest.mark.parametrize("f", [0.3, 0.03])
-def test_cvd_hydrogen_coverage_matches_serial_reference(oracle_lib, tmp_path, f):
+def test_cvd_hydrogen_coverage_matches_serial_reference(tmp_path_factory, f):
     """CVD of Si(001) under one coverage species (H), the rates of the
     reference's CVD-Si-SiH2 case (deposition 85/s, absorption 287/s and
     desorption 40/s per site, evaporation keyed by covered neighbours),
-    RunType R: atoms and covered sites at t = 3 s, 16 oracle seeds against 16
-    GPU replicas at the window factors f = 0.3 (the one-crystal-species rule
-    mulskips.e uses) and 0.03."""
-    import multiprocessing as mp
+    RunType R, t_obs = 3 s, at the window factors f = 0.3 (the one-crystal-
+    species rule mulskips.e uses) and 0.03."""
     from mulskips_gb300 import Batch
     from mulskips_gb300.startdat import parse_startdat
-    from conftest import GOLDEN, ROOT
-    t_obs, n = 3.0, 16
-    txt = open(os.path.join(GOLDEN, "CVD-Si-SiH2", "start.dat")).read().replace(
-        "T ! RunType", "R ! RunType")
-    paths = []
-    for s in range(n):
-        p = tmp_path / f"cvd{s}.dat"
-        p.write_text(txt.replace("9117116 ! Random seed", f"{500 + s} ! Random seed"))
-        paths.append(str(p))
-    with mp.get_context("spawn").Pool(min(n, os.cpu_count() or 1)) as pool:
-        ref = np.array(pool.map(_cvd_oracle, [(p, t_obs, ROOT) for p in paths]), float)
-    d = parse_startdat(paths[0])
-    assert d["run_type"] == "R" and d["list_cov"] == [1]
-    b = Batch([(480, 480, 480)] * n, seeds=[71 + s for s in range(n)], sf=d["sf"], list_cov=d["list_cov"])
-    b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
-    b.set_coverage_rates(np.stack([d["ptransAbs"][:, 1:]] * n), np.stack([d["ptransDes"][:, 1:]] * n))
-    b.init_flat("S", [48] * n)
-    tau = float(b.suggest_tau(f)[0])
-    nwin = int(math.ceil(t_obs / tau))
-    b.run(t_obs / nwin, nwin)
-    obs = b.observables()
+    t_obs = 3.0
+    if "ref" not in _CVD_REF:
+        tmp = tmp_path_factory.mktemp("cvd")
+        paths = startdats(tmp, "CVD-Si-SiH2", ("T ! RunType", "R ! RunType"), 500, NSEEDS, "cvd")
+        d = parse_startdat(paths[0])
+        assert d["run_type"] == "R" and d["list_cov"] == [1]
+        _CVD_REF["ref"] = (d, oracle_sample(paths, (480, 480, 480), t_obs, d["sf"], cov=True))
+    d, ref = _CVD_REF["ref"]
+    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[71 + s for s in range(NSEEDS)], sf=d["sf"], list_cov=d["list_cov"])
+    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
+    b.set_coverage_rates(np.stack([d["ptransAbs"][:, 1:]] * NSEEDS), np.stack([d["ptransDes"][:, 1:]] * NSEEDS))
+    b.init_flat("S", [48] * NSEEDS)
+    nwin = windows_for(t_obs, float(b.suggest_tau(f)[0]))
+    g = gpu_sample(b, t_obs / nwin, nwin, (480, 480, 480), d["sf"], cov=True)
     b.close()
-    g = np.array([(o["atoms"], o["covered"]) for o in obs], float)
-    print(f"\nCVD tau {t_obs / nwin:.3e} ({nwin} windows)")
-    for k, name in enumerate(("atoms", "covered")):
-        diff, hw = band(g[:, k], ref[:, k])
-        print(f"{name}: gpu {g[:, k].mean():.1f}+-{g[:, k].std(ddof=1):.1f} serial {ref[:, k].mean():.1f}"
-              f"+-{ref[:, k].std(ddof=1):.1f} diff {diff:.1f} 3-sigma band +-{hw:.1f}")
-        assert abs(diff) <= hw, name
-    assert ref[:, 1].mean() > 1000 and g[:, 0].mean() > 0
+    fam = Family(f"CVD Si(001) + H, f = {f} ({nwin} windows)", 4)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("covered sites", column(g, "covered"), column(ref, "covered"))
+    fam.add("growth rate um/h", growth(g), growth(ref))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    assert column(ref, "covered").mean() > 1000 and column(g, "atoms").mean() > 0
+    fam.check()
