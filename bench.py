@@ -107,22 +107,33 @@ def _oracle_sample(args):
     write_plain_si_startdat(p, T=T, len1=360, max_iter=100000000, seed=seed)
     o = ora.Oracle(p, 480, 480, 480, numbers=None)
     o.init()
+    c0 = o.counts()
     t0 = time.perf_counter()
     o.run(100000000)
     dt = time.perf_counter() - t0
     n = o.iter - 1
     o.close()
     shutil.rmtree(d, ignore_errors=True)
-    return n, dt
+    return n, dt, c0["atoms"], c0["mc"]
+
+
+# the serial reference's selection: a sum tree of 2^20 - 1 nodes (Levels = 20,
+# AllocateArrays.f:30-43), descended with one uniform per level
+# (PickTreeEvent.f:41-55)
+TREE_LEVELS = 20
 
 
 def cpu_baseline(seconds=10.0, cores=1):
+    """Events/s of the oracle on `cores` processes (one seed each), the total
+    events, runs, and the sample's slab state (mean initial atoms and MC sites
+    of a run)."""
     from oracle import ora
     ora.build()
     ctx = mp.get_context("spawn")
     ev = 0
     busy = 0.0
     k = 0
+    atoms0 = mc0 = 0
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
         while time.perf_counter() - t0 < seconds:
@@ -131,7 +142,10 @@ def cpu_baseline(seconds=10.0, cores=1):
             res = pool.map(_oracle_sample, jobs)
             ev += sum(r[0] for r in res)
             busy += max(r[1] for r in res)
-    return ev / busy, ev, k
+            atoms0 += sum(r[2] for r in res)
+            mc0 += sum(r[3] for r in res)
+    return ev / busy, ev, k, {"initial_atoms": atoms0 / k, "initial_mc_sites": mc0 / k,
+                              "tree_levels": TREE_LEVELS, "uniforms_per_pick": TREE_LEVELS - 1}
 
 
 def reduce_over_ranks(dist, wall, count, device="cpu"):
@@ -267,7 +281,13 @@ def gb300(args, rank, world):
     batched = batched_bench(args) if not args.no_batched else None
     la_grad = la_gradient_bench() if not args.no_batched else None
     cvd = cvd_bench() if not args.no_batched else None
-    base_v, base_ev, base_runs = cpu_baseline(seconds=args.cpu_seconds, cores=1)
+    base_v, base_ev, base_runs, base_slab = cpu_baseline(seconds=args.cpu_seconds, cores=1)
+    all_cores = os.cpu_count() or 1
+    all_v, _, _, _ = cpu_baseline(seconds=args.cpu_seconds, cores=all_cores)
+    if batched:
+        batched["batched_over_plain_3072cube"] = batched["value"] / value
+        batched["batched_over_cpu_all_cores"] = batched["value"] / all_v
+    accuracy = bench_accuracy(width)
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
@@ -295,7 +315,11 @@ def gb300(args, rank, world):
         "cpu_baseline": {"value": base_v, "unit": "events/s", "cores": 1, "kind": "port",
                          "sample": f"oracle (serial C restatement) on {base_runs} runs of the same model in a "
                                    f"480^3 box, Len1=360 slab etched to the walls, T cycling 1000/1100/1200 K, "
-                                   f"{base_ev} events"},
+                                   f"{base_ev} events",
+                         "slab": base_slab},
+        "cpu_all_cores": {"value": all_v, "unit": "events/s", "cores": all_cores,
+                          "sample": "the cpu_baseline sample, one oracle process per core"},
+        "accuracy": accuracy,
         "clocks": clocks,
         "wall_s_timed": wall,
         "batched": batched,
@@ -305,6 +329,21 @@ def gb300(args, rank, world):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def bench_accuracy(width):
+    """The growth-rate error at this benchmark's window rule (f = 0.3) and
+    tile width, as the statistical parity test measured it on GB300 on the
+    same model in a 480^3 box at the benchmark's three temperatures (32 GPU
+    replicas against 32 serial seeds, 95 % family band): read from
+    profiles/etch_accuracy_480cube.json, which that test run wrote."""
+    p = os.path.join(ROOT, "profiles", "etch_accuracy_480cube.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    d["bench_tile_width"] = width
+    d["bench_f"] = ACCURATE_F
+    return d
 
 
 def batched_bench(args):
@@ -430,8 +469,9 @@ def reference(args, rank, world):
         pass
     total_ev = 0
     total_t = 0.0
+    slab = None
     for k in range(args.steps):
-        v, ev, runs = cpu_baseline(seconds=args.cpu_seconds, cores=cores)
+        v, ev, runs, slab = cpu_baseline(seconds=args.cpu_seconds, cores=cores)
         samples.append(v)
         total_ev += ev
         total_t += ev / v
@@ -444,7 +484,8 @@ def reference(args, rank, world):
                                "etched to the walls, T cycling 1000/1100/1200 K, one oracle process per core"},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": "port",
                          "sample": "serial C restatement of the reference (no Fortran compiler for the "
-                                   "reference itself), one independent seed per core"},
+                                   "reference itself), one independent seed per core",
+                         "slab": slab},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

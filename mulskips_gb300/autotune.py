@@ -6,16 +6,17 @@ sublattice result inside the serial reference's statistical band depends on
 the model:
   * single species (plain Si(001), 1000/1100/1200 K, 32 seeds each): f = 0.3
     (at f = 1 the etch rate is 0.5 % off, at f = 3 it is 5 % off);
-  * two species (the 3C-SiC(001) rates of the reference's `surface` case,
-    16 seeds): f = 0.03 (f = 0.3 grows 10 % too slowly: fast carbon
-    desorption across tile borders outruns the stabilising depositions, which
-    the dominant-share class does not see at the start).
+  * two species (the 3C-SiC(001) rates of the reference's `surface` case):
+    f = 0.01.  f = 0.3 grows 10 % too slowly (fast carbon desorption across
+    tile borders outruns the stabilising depositions, which the
+    dominant-share class does not see at the start); at f = 0.03 the deficit
+    is 0.1 % of the atoms, at the edge of the 95 % band of 32 seeds.
 
 Tile width: a short timed trial of each candidate width on the lattice
 itself; the plain path restores the lattice afterwards.
 """
 ACCURATE_F = 0.3          # single species
-ACCURATE_F_MULTI = 0.03   # two or three species
+ACCURATE_F_MULTI = 0.01   # two or three species
 
 
 def accurate_f(ncrystal):

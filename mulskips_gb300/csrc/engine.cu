@@ -96,7 +96,8 @@ struct LADev {
     long long init_cnt[3];
     long long cnt[3];
     float xliq[3];
-    int on, score_on, pad0;
+    int on, score_on;
+    int swap_species;        // SiGe (14, 32) with liquid fractions: the species swap of LaserAnnealing main.f:676-681
     float P0[3], Tm[3], Tflex[3], sigma[3];
     float E[64];             // melting barrier of each occupied class
     float dE[64][4];         // d E / d theta
@@ -873,6 +874,17 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                     int s0 = sp - 1;
                     for (int j = 0; j < 4; j++)
                         sc[j] += -(double)A->dEdep[s0][co - 1][j] / ((double)KB_EV_F * (double)A->Tm[s0]);
+                }
+                // LaserAnnealing main.f:676-681: SiGe solidification of a
+                // species whose crystal count has reached its initial count
+                // deposits the other one; the count is the replica's at the
+                // last tile publication plus this tile's own changes (lane 0
+                // reads it once, so every lane takes the same species)
+                if (A->swap_species && sp <= 2) {
+                    int sw = 0;
+                    if (lane == 0)
+                        sw = __ldcg(&A->cnt[sp - 1]) + (long long)S.dcnt[sp - 1] >= A->init_cnt[sp - 1] ? 1 : 0;
+                    if (__shfl_sync(FULL, sw, 0)) sp = 3 - sp;
                 }
             } else {
                 sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
@@ -2331,6 +2343,8 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
         A.zsurf = p[i].zsurf;
         A.sf = (float)r.cfg.sf;
         A.liquid_weighting = p[i].liquid_weighting ? 1 : 0;
+        A.swap_species = A.liquid_weighting && r.cfg.ncrystal == 2 && r.cfg.list_crystal[0] == 14 &&
+                         r.cfg.list_crystal[1] == 32;
         if (r.t_layer_off >= 0) {
             A.tfield = h->d_tfield + r.st_off;
             A.tlayer = h->d_tlayer + r.t_layer_off;

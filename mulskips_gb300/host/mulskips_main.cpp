@@ -601,11 +601,11 @@ int main()
     bool few = false;
     for (long long block = 0;; block++) {
         // window factor validated against the serial reference: 0.3 for one
-        // crystal species (with or without a coverage species), 0.03 for two
+        // crystal species (with or without a coverage species), 0.01 for two
         // or three (fast desorption across tile borders)
         if (block % 4 == 0) {
             if (in.init_st == "LA") tau = la_tau();
-            else check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.03, &tau));
+            else check(mks_suggest_tau(h, in.ncrystal <= 1 ? 0.3 : 0.01, &tau));
         }
         // Iter mode: the chunk ends at the window that reaches the next
         // output multiple or IterMax, so frames land just past each multiple

@@ -2946,8 +2946,8 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
  * fractions are refreshed every `phase` windows and the stop rules (more atoms
  * than at the start, LA/main.f:714-723; <= 20 MC particles, main.f:307-310)
  * are checked at window ends — the schedule of the GPU engine's LA mode.
- * The Ge/Si swap of LA/main.f:676-681 is not applied (a species with no liquid
- * left has zero solidification rate from the next refresh on).            */
+ * A SiGe solidification of a species whose crystal count has reached its
+ * initial count deposits the other species instead (LA/main.f:676-681).   */
 
 static uint64_t la_next(ora_t *o)
 {   /* xoshiro256** (Blackman & Vigna) */
@@ -3192,6 +3192,11 @@ int ora_la_run_until(ora_t *o, double t_end)
             double u = la_u01(o) * (ps[0] + ps[1] + ps[2]);
             int s = u < ps[0] ? 0 : (u < ps[0] + ps[1] ? 1 : 2);
             for (int j = 0; j < 4; j++) o->la_score[j] -= o->dEd[s][coor - 1][j] / (KB * o->lap.Tm[s]);
+            /* LA/main.f:676-681: a SiGe deposition of a species whose crystal
+             * count has reached its initial count deposits the other one */
+            if (o->ncrystal == 2 && o->list_crystal[0] == 14 && o->list_crystal[1] == 32 && s < 2 &&
+                o->la_cnt[s] >= o->la_init[s])
+                s = 1 - s;
             deposition(o, ind, s + 1);
             o->la_cnt[s]++;
             o->count_crystal[s]++;

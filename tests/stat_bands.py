@@ -6,7 +6,9 @@ means must lie inside the two-sided Welch t band at level 1 - 0.05 / k
 (Bonferroni correction over the k observables of the test), so that the test
 as a whole holds with 95 % confidence when both samplers have the same
 distribution.  Seeds are fixed, so each test is deterministic."""
+import json
 import math
+import os
 
 import numpy as np
 
@@ -47,8 +49,22 @@ class Family:
                        f"diff {d:.4g}{rel}  band +-{hw:.4g} (t={q:.3f})")
         return "\n".join(out)
 
+    def record(self):
+        """Append the family's rows to the JSON-lines file named by
+        MKS_STATS_OUT, if set (a record of the measured bands)."""
+        path = os.environ.get("MKS_STATS_OUT")
+        if not path:
+            return
+        rows = [{"observable": r[0], "gpu_mean": float(r[1]), "gpu_sd": float(r[2]), "ref_mean": float(r[3]),
+                 "ref_sd": float(r[4]), "diff": float(r[5]), "band": float(r[6]), "t": float(r[7]),
+                 "n_gpu": int(r[8]), "n_ref": int(r[9])} for r in self.rows]
+        with open(path, "a") as f:
+            f.write(json.dumps({"test": os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0],
+                                "family": self.title, "k": self.k, "rows": rows}) + "\n")
+
     def check(self):
         assert len(self.rows) == self.k, "every observable of the family must be compared"
         print("\n" + self.report())
+        self.record()
         bad = [r[0] for r in self.rows if not abs(r[5]) <= r[6]]
         assert not bad, f"outside the band: {bad}\n{self.report()}"
