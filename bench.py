@@ -107,14 +107,14 @@ def _oracle_sample(args):
     write_plain_si_startdat(p, T=T, len1=360, max_iter=100000000, seed=seed)
     o = ora.Oracle(p, 480, 480, 480, numbers=None)
     o.init()
-    c0 = o.counts()
+    atoms0, mc0 = o.atoms(), o.counts()["mc"]
     t0 = time.perf_counter()
     o.run(100000000)
     dt = time.perf_counter() - t0
     n = o.iter - 1
     o.close()
     shutil.rmtree(d, ignore_errors=True)
-    return n, dt, c0["atoms"], c0["mc"]
+    return n, dt, atoms0, mc0
 
 
 # the serial reference's selection: a sum tree of 2^20 - 1 nodes (Levels = 20,

@@ -236,6 +236,16 @@ int32_t mks_batch_size(mks_handle *h);
  * loop is serial; the tile shape is one of the autotuner's knobs).         */
 int mks_set_tiling(mks_handle *h, int32_t width);
 int32_t mks_get_tiling(mks_handle *h);
+/* Colouring of the sublattice tiles (no counterpart in the reference, whose
+ * loop is serial).  0 (the default): every replica whose tiles can be at
+ * least 6 sites wide at the current width takes the brick tiling -- rows of
+ * tiles with the odd rows shifted by half a tile, three colours, 3 phases
+ * and 6 neighbours per tile per window -- and the others the square grid of
+ * four colours (4 phases, 8 neighbours); 3: the brick tiling for every
+ * replica (MKS_ERR_ARG if one cannot take it); 4: the square grid for all.
+ * mks_get_colours gives the largest colour count in use.                 */
+int mks_set_colours(mks_handle *h, int32_t ncolour);
+int32_t mks_get_colours(mks_handle *h);
 /* Schedule of the sublattice windows: 1 (default) one persistent kernel in
  * which each tile waits only for its eight neighbours, 0 one launch per
  * colour phase.  Both give the same lattice for the same seed.           */
@@ -298,6 +308,18 @@ int mks_batch_la_counts(mks_handle *h, int64_t *crystal, double *xliq);
  * other replicas' f (use_baseline != 0) or 0; se[j] (may be NULL) is its
  * standard error.  No counterpart in the reference.                      */
 int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, double *grad, double *se);
+/* Causal form of the same gradient for an observable that is a sum of
+ * increments over segments of the run, f = sum_k df_k (e.g. crystal atoms
+ * gained per segment): after each segment the host passes df (one value per
+ * replica) and the engine adds (df_i - b_i) S_i to replica i's FP64 sums,
+ * S_i the score of its path so far and b_i the leave-one-out mean of df.
+ * An increment is weighted only by the score of the path before it (the
+ * later score has zero mean given that past), which lowers the variance.
+ * mks_batch_lr_result gives the mean of the sums over the replicas and its
+ * standard error (grad[4], se[4]) and clears the sums with reset != 0, as
+ * mks_batch_set_la does.  No counterpart in the reference.               */
+int mks_batch_lr_accumulate(mks_handle *h, const double *df);
+int mks_batch_lr_result(mks_handle *h, int32_t reset, double *grad, double *se);
 /* Static per-site temperatures for LA mode, from the T bits (9..21) of a
  * LattCoo array (SetT, mulskips-source/initial/SetT.f:25-50), replacing T(z,t)
  * for replica rep.  Call before mks_batch_set_la.                          */

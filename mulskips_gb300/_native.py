@@ -76,6 +76,10 @@ SIGNATURES = {
     "mks_write_frame": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, C.c_int64, C.c_void_p]),
     "mks_class_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "mks_site_rates": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "mks_set_colours": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mks_batch_lr_accumulate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mks_batch_lr_result": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "mks_get_colours": (C.c_int32, [C.c_void_p]),
     "mks_get_observables": (C.c_int, [C.c_void_p, C.POINTER(MksObservables)]),
     "mks_get_status": (C.c_int, [C.c_void_p, C.POINTER(MksStatus)]),
     "mks_batch_create": (C.c_int, [C.POINTER(MksConfig), C.c_int32, C.POINTER(C.c_void_p)]),

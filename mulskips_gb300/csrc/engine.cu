@@ -30,6 +30,7 @@
 
 #include "lattice.cuh"
 #include "shapes.cuh"
+#include "tiling.cuh"
 #include "rng.cuh"
 #include "../../include/mulskips_gpu.h"
 
@@ -38,7 +39,7 @@ using namespace mks;
 namespace {
 
 // ---------------------------------------------------------------- limits
-constexpr int QMAX = 8;                  // max tile width (sites) in a or b
+constexpr int QMAX = mks_tiling::QMAX;   // max tile width (sites) in a or b
 constexpr int HALO = 2;                  // read range of an event, in columns
 constexpr int WB_MAX = QMAX + 2 * HALO;  // 12: staged rows per layer
 constexpr int RS = 32;                   // staged row stride: one aligned 32-byte row segment
@@ -64,7 +65,8 @@ struct RepDev {
     unsigned long long events;
     long long mc_count;
     unsigned int window;
-    int active, stop_reason, pad1;
+    int active, stop_reason;
+    int qshift;              // brick tiling: columns by which the tiles of odd rows are shifted (0: square grid)
     float rate[64];          // per class; CLS_ISO is computed per event
     float spcum[3][3];       // per coordination: cumulative fractions of species 1, 1+2, all deposition
 };
@@ -73,6 +75,7 @@ struct QuadDev {
     int rep, a0, a1, b0, b1;
     int zlo, zhi, mc;        // mutable: band of event sites and their count
     int qa, qb, colour;
+    int ncol;                // colours of the replica's tiling: 4 square grid, 3 brick
     int ev;                  // events of this tile since the last window end (k_window_end folds them)
     int nbr[8];              // the eight neighbouring tiles (periodic)
 };
@@ -311,8 +314,7 @@ __global__ void k_band_scan(const RepDev *reps, int rep, QuadDev *quads, const u
                 continue;
             }
             if (R.single && sp_of(sb) > 1) bad = true;
-            int qa = ((a + 1) * R.nqa - 1) / R.NA;   // the tile column holding a
-            int qq = R.quad_base + qb * R.nqa + qa;
+            int qq = R.quad_base + mks_tiling::tile_of(R.NA, R.NB, R.nqa, R.nqb, R.qshift, a, b);
             if (qq != q) {
                 if (q >= 0) {
                     atomicMin(&quads[q].zlo, lo);
@@ -1212,11 +1214,12 @@ __global__ void __launch_bounds__(32, 16) k_sl_phase(RepDev *reps, QuadDev *quad
     process_tile<LAM, COV>(reps, quads, qid, st_all, status, phase_tag, R.window, R.T0, la, score, tmaps);
 }
 
-// Persistent schedule: phases P = 4*w + colour for windows w = 0..nwin-1.  Warp
+// Persistent schedule: phases P = ncol*w + colour for windows w = 0..nwin-1 (ncol
+// = 4 colours on the square grid of tiles, 3 on the brick tiling).  Warp
 // g owns tile i of each colour list for i = g mod G (so at most one tile per
 // phase when a colour has <= G tiles) and runs them in increasing P.  A tile of colour c
 // may run phase P once each neighbour (all of another colour) has finished
-// its last phase before P, i.e. progress[n] >= P - ((c - colour(n)) & 3); a
+// its last phase before P, i.e. progress[n] >= P - ((c - colour(n)) mod ncol); a
 // neighbour cannot start a later phase before this tile publishes P.  All
 // waits point to strictly earlier phases and all blocks are co-resident
 // (cooperative launch), so the schedule cannot deadlock; every wait is still
@@ -1237,39 +1240,43 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
     // this warp's tiles of colour c: wtiles[woff[4 g + c] .. woff[4 g + c + 1])
     const int o0 = woff[4 * blockIdx.x], o1 = woff[4 * blockIdx.x + 1], o2 = woff[4 * blockIdx.x + 2],
               o3 = woff[4 * blockIdx.x + 3], o4 = woff[4 * blockIdx.x + 4];
-    for (int P = 0; P < 4 * nwin; P++) {
-        int c = P & 3, w = P >> 2;
-        int kb = c == 0 ? o0 : (c == 1 ? o1 : (c == 2 ? o2 : o3));
-        int ke = c == 0 ? o1 : (c == 1 ? o2 : (c == 2 ? o3 : o4));
-        for (int k = kb; k < ke; k++) {
-            int t = wtiles[k];
-            if (lane < 8) {
-                int n = quads[t].nbr[lane];
-                int need = P - ((c - quads[n].colour) & 3);
-                long long t0 = clock64();
-                volatile int *pr = progress + n;
-                volatile int *err = &status->error;
-                // tight poll (one L2 round trip per check; a sleep between
-                // checks oversleeps the flag and lengthens every phase)
-                while (*pr < need) {
-                    if (*err) break;
-                    if (clock64() - t0 > spin_limit) {
-                        set_error(status, DERR_TIMEOUT, t);
-                        break;
+    // windows in order, colours in order within a window: every wait points
+    // to a phase that comes earlier in this order
+    for (int w = 0; w < nwin; w++)
+        for (int c = 0; c < 4; c++) {
+            int kb = c == 0 ? o0 : (c == 1 ? o1 : (c == 2 ? o2 : o3));
+            int ke = c == 0 ? o1 : (c == 1 ? o2 : (c == 2 ? o3 : o4));
+            for (int k = kb; k < ke; k++) {
+                int t = wtiles[k];
+                const int ncol = quads[t].ncol;
+                const int P = ncol * w + c;
+                if (lane < 8) {
+                    int n = quads[t].nbr[lane];
+                    int need = P - ((c - quads[n].colour + ncol) % ncol);
+                    long long t0 = clock64();
+                    volatile int *pr = progress + n;
+                    volatile int *err = &status->error;
+                    // tight poll (one L2 round trip per check; a sleep between
+                    // checks oversleeps the flag and lengthens every phase)
+                    while (*pr < need) {
+                        if (*err) break;
+                        if (clock64() - t0 > spin_limit) {
+                            set_error(status, DERR_TIMEOUT, t);
+                            break;
+                        }
                     }
                 }
+                __syncwarp();
+                __threadfence();                                // acquire: neighbours' writes before their flag
+                if (*(volatile int *)&status->error) return;
+                const RepDev &R = reps[quads[t].rep];
+                process_tile<LAM, COV>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
+                                       R.T0 + (double)w * R.tau, la, score, tmaps);
+                __threadfence();                                // release: each lane's writes reach L2 ...
+                __syncwarp();                                   // ... before lane 0 publishes the flag
+                if (lane == 0 && t != hold_tile) atomicExch(progress + t, P);
             }
-            __syncwarp();
-            __threadfence();                                // acquire: neighbours' writes before their flag
-            if (*(volatile int *)&status->error) return;
-            const RepDev &R = reps[quads[t].rep];
-            process_tile<LAM, COV>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
-                         R.T0 + (double)w * R.tau, la, score, tmaps);
-            __threadfence();                                // release: each lane's writes reach L2 ...
-            __syncwarp();                                   // ... before lane 0 publishes the flag
-            if (lane == 0 && t != hold_tile) atomicExch(progress + t, P);
         }
-    }
 }
 
 // End of a window: advance the replica clock, apply the exit conditions.
@@ -1373,6 +1380,30 @@ __global__ void k_lr_grad(const double *score, const double *f, int n, int use_b
             out[j] = m;
             out[4 + j] = sqrt(var / n);
         }
+    }
+}
+
+// Causal step of the LR gradient: for increments df of the observable over
+// the last segment, acc_i += (df_i - b_i) S_i with S_i the replica's score
+// so far and b_i the leave-one-out mean of df (unbiased: b_i is independent
+// of replica i, and E[S_i] = 0).  One block, FP64.
+__global__ void k_lr_step(const double *score, const double *df, int n, double *acc)
+{
+    __shared__ double sh[256];
+    int tid = threadIdx.x;
+    double fs = 0.0;
+    for (int i = tid; i < n; i += blockDim.x) fs += df[i];
+    sh[tid] = fs;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (tid < o) sh[tid] += sh[tid + o];
+        __syncthreads();
+    }
+    const double tot = sh[0];
+    for (int i = tid; i < n; i += blockDim.x) {
+        double b = n > 1 ? (tot - df[i]) / (double)(n - 1) : 0.0;
+        double w = df[i] - b;
+        for (int j = 0; j < 4; j++) acc[4 * i + j] += w * score[4 * i + j];
     }
 }
 
@@ -1498,6 +1529,7 @@ struct RepHost {
     mks_config cfg;
     int NA, NB, NZ, pitch;
     int nqa, nqb, quad_base;
+    int qshift = 0;             // brick tiling: shift of the odd tile rows (columns)
     int64_t st_off;
     double ptransE[3 * 4096];
     double ptransD[9];
@@ -1540,11 +1572,14 @@ struct mks_handle {
     double *d_score = nullptr;
     int la_on = 0;
     int64_t la_window = 0;
-    double *d_lr = nullptr;  // f values and result of mks_batch_lr_grad   // windows run since mks_batch_set_la (persistent launch alignment)
+    double *d_lr = nullptr;      // f values and result of mks_batch_lr_grad
+    double *d_lr_acc = nullptr;  // causal LR sums per replica (4 each), then ones and the result
     int coop_grid = 0;
     bool any_cov = false;        // a replica has a coverage species: the COV kernels run
     int schedule = 1;            // 1 persistent dataflow kernel, 0 one launch per colour phase
     uint32_t phase_counter = 0;
+    int ncolour = 4;             // most colours of a replica's tiling: 4 square grid, 3 brick
+    int colours_req = 0;         // 0: brick for every replica that admits it; 4: square grid for all
     int64_t last_kernels = 0, last_graphs = 0, last_phase_launches = 0;
     double last_ms = 0.0;
     double time_acc = 0.0;
@@ -1622,14 +1657,6 @@ int check_config(const mks_config &c)
 // even number of tiles along a side of n sites, each about `width` wide
 // (at least 4: the write ring of one tile and the read halo of the next
 // same-colour tile must not meet) and at most QMAX
-int tiles_for(int n, int width)
-{
-    int t = 2 * (n / (2 * width));
-    if (t < 2) t = 2;
-    while ((n + t - 1) / t > QMAX) t += 2;
-    return t;
-}
-
 int upload_reps(mks_handle *h, const std::vector<RepDev> &d)
 {
     CK(cudaMemcpyAsync(h->d_reps, d.data(), sizeof(RepDev) * d.size(), cudaMemcpyHostToDevice, h->stream));
@@ -1684,40 +1711,41 @@ void class_hist(mks_handle *h, int r0, int r1, unsigned long long *hist)
 }
 
 // cut every replica's (a,b) plane into tiles of about `width` sites
+// The tiles of every replica (mks_tiling::layout): the brick tiling of three
+// colours where a replica admits it and colours_req allows, else the square
+// grid of four.
 void partition(mks_handle *h, int width)
 {
     h->quads_h.clear();
     for (int c = 0; c < 4; c++) h->color_list_h[c].clear();
+    h->ncolour = 0;
     for (size_t i = 0; i < h->reps.size(); i++) {
         RepHost &r = h->reps[i];
-        r.nqa = tiles_for(r.NA, width);
-        r.nqb = tiles_for(r.NB, width);
+        const mks_tiling::Layout L = mks_tiling::layout(r.NA, r.NB, width, h->colours_req != 4);
+        h->ncolour = std::max(h->ncolour, L.ncol);
+        r.nqa = L.nqa;
+        r.nqb = L.nqb;
+        r.qshift = L.shift;
         r.quad_base = (int)h->quads_h.size();
-        for (int qb = 0; qb < r.nqb; qb++)
-            for (int qa = 0; qa < r.nqa; qa++) {
-                QuadDev q;
-                q.rep = (int)i;
-                q.a0 = (qa * r.NA) / r.nqa;
-                q.a1 = ((qa + 1) * r.NA) / r.nqa;
-                q.b0 = (qb * r.NB) / r.nqb;
-                q.b1 = ((qb + 1) * r.NB) / r.nqb;
-                q.zlo = 1 << 30;
-                q.zhi = -1;
-                q.mc = 0;
-                q.qa = qa;
-                q.qb = qb;
-                q.colour = (qa & 1) + 2 * (qb & 1);
-                q.ev = 0;
-                int k = 0;
-                for (int db = -1; db <= 1; db++)
-                    for (int da = -1; da <= 1; da++) {
-                        if (!da && !db) continue;
-                        int na = (qa + da + r.nqa) % r.nqa, nb = (qb + db + r.nqb) % r.nqb;
-                        q.nbr[k++] = r.quad_base + nb * r.nqa + na;
-                    }
-                h->color_list_h[q.colour].push_back((int)h->quads_h.size());
-                h->quads_h.push_back(q);
-            }
+        for (const mks_tiling::Tile &t : L.tiles) {
+            QuadDev q;
+            q.rep = (int)i;
+            q.a0 = t.a0;
+            q.a1 = t.a1;
+            q.b0 = t.b0;
+            q.b1 = t.b1;
+            q.zlo = 1 << 30;
+            q.zhi = -1;
+            q.mc = 0;
+            q.qa = t.qa;
+            q.qb = t.qb;
+            q.colour = t.colour;
+            q.ncol = L.ncol;
+            q.ev = 0;
+            for (int k = 0; k < 8; k++) q.nbr[k] = r.quad_base + t.nbr[k];
+            h->color_list_h[q.colour].push_back((int)h->quads_h.size());
+            h->quads_h.push_back(q);
+        }
     }
     h->tile_width = width;
 }
@@ -1914,6 +1942,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         d[i].pitch = r.pitch;
         d[i].nqa = r.nqa;
         d[i].nqb = r.nqb;
+        d[i].qshift = r.qshift;
         d[i].quad_base = r.quad_base;
         d[i].tau = 1e-6;
         d[i].T0 = 0.0;
@@ -1935,7 +1964,8 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     return 0;
 }
 
-// one window = 4 colour phases + window end
+// one window = one phase per colour + window end (a replica on the
+// three-colour tiling has no tiles of colour 3)
 int launch_window(mks_handle *h)
 {
     for (int c = 0; c < 4; c++) {
@@ -2207,6 +2237,7 @@ void mks_destroy(mks_handle *h)
     cudaFree(h->d_tlayer);
     cudaFree(h->d_la);
     if (h->d_lr) cudaFree(h->d_lr);
+    if (h->d_lr_acc) cudaFree(h->d_lr_acc);
     cudaFree(h->d_score);
     for (int c = 0; c < 4; c++) cudaFree(h->d_clist[c]);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -2393,6 +2424,7 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
     }
     CK(cudaMemcpyAsync(h->d_la, la.data(), sizeof(LADev) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream));
+    if (h->d_lr_acc) CK(cudaMemsetAsync(h->d_lr_acc, 0, sizeof(double) * 4 * n, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->la_on = 1;
     return 0;
@@ -2461,6 +2493,7 @@ int mks_batch_set_tabulated(mks_handle *h, int32_t ntemp, const int32_t *temps, 
     }
     CK(cudaMemcpyAsync(h->d_la, la.data(), sizeof(LADev) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->d_score, 0, sizeof(double) * 4 * n, h->stream));
+    if (h->d_lr_acc) CK(cudaMemsetAsync(h->d_lr_acc, 0, sizeof(double) * 4 * n, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->la_on = 1;
     return 0;
@@ -2477,6 +2510,46 @@ int mks_batch_lr_grad(mks_handle *h, const double *f, int32_t use_baseline, doub
     CK(cudaGetLastError());
     double out[8];
     CK(cudaMemcpyAsync(out, h->d_lr + n, sizeof out, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int j = 0; j < 4; j++) {
+        grad[j] = out[j];
+        if (se) se[j] = out[4 + j];
+    }
+    return 0;
+}
+
+int mks_batch_lr_accumulate(mks_handle *h, const double *df)
+{
+    if (!h || !df) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->la_on) return fail(MKS_ERR_ARG, "LA mode is not set (mks_batch_set_la)");
+    int n = (int)h->reps.size();
+    if (!h->d_lr) CK(cudaMalloc(&h->d_lr, sizeof(double) * (size_t)(n + 8)));
+    if (!h->d_lr_acc) {
+        CK(cudaMalloc(&h->d_lr_acc, sizeof(double) * (size_t)(5 * n + 8)));
+        CK(cudaMemsetAsync(h->d_lr_acc, 0, sizeof(double) * 4 * (size_t)n, h->stream));
+    }
+    CK(cudaMemcpyAsync(h->d_lr, df, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    k_lr_step<<<1, 256, 0, h->stream>>>(h->d_score, h->d_lr, n, h->d_lr_acc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int mks_batch_lr_result(mks_handle *h, int32_t reset, double *grad, double *se)
+{
+    if (!h || !grad) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->d_lr_acc) return fail(MKS_ERR_ARG, "no mks_batch_lr_accumulate since the last reset");
+    int n = (int)h->reps.size();
+    // the mean over replicas of the causal sums and its standard error: the
+    // reduction of k_lr_grad with f = 1 and no baseline
+    std::vector<double> ones((size_t)n, 1.0);
+    double *d_one = h->d_lr_acc + 4 * (size_t)n;
+    CK(cudaMemcpyAsync(d_one, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    k_lr_grad<<<1, 256, 0, h->stream>>>(h->d_lr_acc, d_one, n, 0, d_one + n);
+    CK(cudaGetLastError());
+    double out[8];
+    CK(cudaMemcpyAsync(out, d_one + n, sizeof out, cudaMemcpyDeviceToHost, h->stream));
+    if (reset) CK(cudaMemsetAsync(h->d_lr_acc, 0, sizeof(double) * 4 * (size_t)n, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (int j = 0; j < 4; j++) {
         grad[j] = out[j];
@@ -3156,6 +3229,7 @@ int mks_set_tiling(mks_handle *h, int32_t width)
     for (size_t i = 0; i < d.size(); i++) {
         d[i].nqa = h->reps[i].nqa;
         d[i].nqb = h->reps[i].nqb;
+        d[i].qshift = h->reps[i].qshift;
         d[i].quad_base = h->reps[i].quad_base;
     }
     rc = upload_reps(h, d);
@@ -3164,6 +3238,22 @@ int mks_set_tiling(mks_handle *h, int32_t width)
 }
 
 int32_t mks_get_tiling(mks_handle *h) { return h ? h->tile_width : 0; }
+
+int mks_set_colours(mks_handle *h, int32_t ncolour)
+{
+    if (!h || (ncolour != 0 && ncolour != 3 && ncolour != 4)) return fail(MKS_ERR_ARG, "colours must be 0, 3 or 4");
+    if (ncolour == 3)                   // every replica must take the brick tiling
+        for (const RepHost &r : h->reps) {
+            int t, sh;
+            if (!mks_tiling::brick_fits(r.NA, h->tile_width, t, sh))
+                return fail(MKS_ERR_ARG, "a %d-site row cannot take the three-colour tiling at width %d", r.NA,
+                            h->tile_width);
+        }
+    h->colours_req = ncolour == 4 ? 4 : 0;
+    return mks_set_tiling(h, h->tile_width);
+}
+
+int32_t mks_get_colours(mks_handle *h) { return h ? h->ncolour : 0; }
 
 // tau = f / r*, with r* the rate of the class that carries the largest share
 // of the replica's total rate; f = 0.3 keeps the etch rate of the plain

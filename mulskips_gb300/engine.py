@@ -227,6 +227,14 @@ class Lattice:
     def tiling(self):
         return N.lib().mks_get_tiling(self._h)
 
+    def set_colours(self, ncolour):
+        """Tile colouring: 0 brick (3 colours) where it fits, 3 brick for all,
+        4 square grid (4 colours) for all."""
+        N.check(N.lib().mks_set_colours(self._h, int(ncolour)))
+
+    def colours(self):
+        return N.lib().mks_get_colours(self._h)
+
     def set_schedule(self, persistent):
         N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
 
@@ -306,6 +314,14 @@ class Batch:
 
     def tiling(self):
         return N.lib().mks_get_tiling(self._h)
+
+    def set_colours(self, ncolour):
+        """Tile colouring: 0 brick (3 colours) where it fits, 3 brick for all,
+        4 square grid (4 colours) for all."""
+        N.check(N.lib().mks_set_colours(self._h, int(ncolour)))
+
+    def colours(self):
+        return N.lib().mks_get_colours(self._h)
 
     def set_schedule(self, persistent):
         N.check(N.lib().mks_set_schedule(self._h, 1 if persistent else 0))
@@ -442,6 +458,19 @@ class Batch:
         x = np.zeros((self.n, 3))
         N.check(N.lib().mks_batch_la_counts(self._h, N.ptr(c), N.ptr(x)))
         return c, x
+
+    def lr_accumulate(self, df):
+        """Causal LR step: df, one increment of the observable per replica
+        over the segment just run, weighted by the score so far (GPU)."""
+        d = np.ascontiguousarray(df, dtype=np.float64).reshape(-1)
+        assert d.size == self.n
+        N.check(N.lib().mks_batch_lr_accumulate(self._h, N.ptr(d)))
+
+    def lr_result(self, reset=True):
+        """(gradient, standard error) of the causal sums of lr_accumulate."""
+        g, se = np.zeros(4), np.zeros(4)
+        N.check(N.lib().mks_batch_lr_result(self._h, 1 if reset else 0, N.ptr(g), N.ptr(se)))
+        return g, se
 
     def lr_grad(self, f, baseline=True):
         """Likelihood-ratio gradient of E[f] (one f per replica) and its

@@ -105,14 +105,18 @@ def test_unsupported_config_is_rejected():
         Lattice(100, 480, 480)
 
 
-def test_persistent_schedule_equals_per_colour_launches():
-    """The persistent kernel (each tile waits only for its eight neighbours)
-    and one launch per colour phase give the same lattice bit for bit."""
+@pytest.mark.parametrize("colours", [3, 4])
+def test_persistent_schedule_equals_per_colour_launches(colours):
+    """The persistent kernel (each tile waits only for its neighbours: 6 on
+    the three-colour brick tiling, 8 on the four-colour grid) and one launch
+    per colour phase give the same lattice bit for bit."""
     from mulskips_gb300 import Lattice, arrhenius_tables
     pE, pD = arrhenius_tables(1100.0)
     states = []
     for persistent in (0, 1):
         with Lattice(480, 480, 480, seed=21) as lat:
+            lat.set_colours(colours)
+            assert lat.colours() == colours
             lat.set_schedule(persistent)
             lat.set_rates(pE, pD)
             lat.init_flat("S", 240)
@@ -122,12 +126,37 @@ def test_persistent_schedule_equals_per_colour_launches():
     assert np.array_equal(states[0][0], states[1][0])
 
 
-@pytest.mark.parametrize("width", [4, 6, 8])
-def test_tile_widths_keep_invariants(width):
+def test_batch_mixes_tilings():
+    """A batch whose small replicas cannot take the brick tiling runs them on
+    the four-colour grid and the others on the brick; both schedules agree."""
+    from mulskips_gb300 import Batch, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    boxes = [(192, 192, 192), (480, 480, 480), (288, 288, 288)]
+    states = []
+    for persistent in (0, 1):
+        b = Batch(boxes, seeds=[5, 6, 7])
+        b.set_tiling(8)
+        assert b.colours() == 4                    # the 32-site rows take the grid
+        b.set_schedule(persistent)
+        b.set_rates(np.stack([pE] * 3), np.stack([pD] * 3))
+        b.init_flat("S", [96, 240, 144])
+        ev = b.run(1e-8, 24)
+        states.append(([b.state(r) for r in range(3)], ev))
+        b.close()
+    assert states[0][1] == states[1][1] > 0
+    for r in range(3):
+        assert np.array_equal(states[0][0][r], states[1][0][r])
+        check_invariants(states[1][0][r])
+
+
+@pytest.mark.parametrize("width,colours", [(4, 4), (6, 3), (6, 4), (8, 3), (8, 4)])
+def test_tile_widths_keep_invariants(width, colours):
     from mulskips_gb300 import Lattice, arrhenius_tables
     pE, pD = arrhenius_tables(1100.0)
     with Lattice(480, 480, 480, seed=4) as lat:
         lat.set_tiling(width)
+        lat.set_colours(colours)
+        assert lat.colours() == colours
         lat.set_rates(pE, pD)
         lat.init_flat("S", 240)
         ev, _ = lat.run(2e-8, 24)

@@ -91,7 +91,8 @@ def gpu_sample(b, tau, nwin, box, sf, cov=False):
     for r in range(b.n):
         assert abs(obs[r]["time"] - ts[-1]) <= 1e-9 * ts[-1], "a replica stopped early"
         # the device's column statistics are the host definition's
-        m, rms = an.height_stats(b.state(r))
+        so = an.state_observables(b.state(r), cov)
+        m, rms = so["mean_height"], so["rms_roughness"]
         assert abs(obs[r]["mean_height"] - m) < 1e-9 * max(1.0, m) and abs(obs[r]["rms_roughness"] - rms) < 1e-9 * max(1.0, rms)
     return [(ts, hs[r], obs[r]) for r in range(b.n)]
 
@@ -143,11 +144,13 @@ def etch_oracle(tmp_path_factory, T):
     return _ETCH_REF[T]
 
 
-# (T, tile width, k2 tau): the benchmark's window rule f = 0.3 and tile width 6
-# at its three temperatures, on the same model in a 480^3 box; and a shorter
-# window at the default width
-@pytest.mark.parametrize("T,width,f", [(1000.0, 6, 0.3), (1100.0, 6, 0.3), (1200.0, 6, 0.3), (1100.0, 8, 0.064)])
-def test_etch_matches_serial_reference(tmp_path_factory, T, width, f):
+# (T, tile width, k2 tau, colours): the benchmark's window rule f = 0.3 and
+# tile width 6 (brick tiling, three colours) at its three temperatures, on the
+# same model in a 480^3 box; the same on the four-colour grid; a shorter
+# window at width 8
+@pytest.mark.parametrize("T,width,f,colours", [(1000.0, 6, 0.3, 3), (1100.0, 6, 0.3, 3), (1200.0, 6, 0.3, 3),
+                                               (1100.0, 6, 0.3, 4), (1100.0, 8, 0.064, 3)])
+def test_etch_matches_serial_reference(tmp_path_factory, T, width, f, colours):
     from mulskips_gb300 import Batch, arrhenius_tables
     t_obs, ref = etch_oracle(tmp_path_factory, T)
     pE, pD = arrhenius_tables(T)
@@ -155,11 +158,13 @@ def test_etch_matches_serial_reference(tmp_path_factory, T, width, f):
     b.set_rates(np.stack([pE] * NSEEDS), np.stack([pD] * NSEEDS))
     b.init_flat("S", [120] * NSEEDS)
     b.set_tiling(width)
+    b.set_colours(colours)
+    assert b.colours() == colours
     nwin = windows_for(t_obs, f / k2(T))
     tau = t_obs / nwin
     g = gpu_sample(b, tau, nwin, (480, 480, 480), 0.4525)
     b.close()
-    fam = Family(f"etch T={T:.0f} K width {width} k2*tau={k2(T) * tau:.3f} ({nwin} windows)", 3)
+    fam = Family(f"etch T={T:.0f} K width {width} colours {colours} k2*tau={k2(T) * tau:.3f} ({nwin} windows)", 3)
     fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
     fam.add("growth rate um/h", growth(g), growth(ref))
     fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
