@@ -113,7 +113,7 @@ struct LADev {
     // same layout as the lattice, and its maximum per layer
     const uint16_t *tfield;
     const float *tlayer;
-    int tNB, tpitch;
+    int tNA, tNB, tpitch;
     // tabulated rates instead of the law above (InitSt ST, SetProbabilityFromField.f,
     // InterpProbFromField.f): class rates and deposition rates at ntab
     // temperatures, linear in T between them (0: not tabulated)
@@ -136,7 +136,8 @@ __device__ __forceinline__ float la_temp(const LADev &A, int z1, double t)
 // the prescribed T(z, t)
 __device__ __forceinline__ float la_temp_at(const LADev &A, int a, int b, int z1, double t)
 {
-    if (A.tfield) return (float)__ldg(&A.tfield[((int64_t)z1 * A.tNB + b) * A.tpitch + a]);
+    // a tile of a shifted brick row runs over the periodic edge: a may be >= NA
+    if (A.tfield) return (float)__ldg(&A.tfield[((int64_t)z1 * A.tNB + b) * A.tpitch + (a >= A.tNA ? a - A.tNA : a)]);
     return la_temp(A, z1, t);
 }
 // row i and upper weight w of temperature T in the table: T between tabT[i]
@@ -433,6 +434,37 @@ __global__ void k_observables(const RepDev *reps, int rep, uint8_t *st_all, unsi
         unsigned long long x = c[j];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&cnt[j], x);
+    }
+}
+
+// Atoms per species of every replica in one launch: grid (x blocks, replicas),
+// 16-byte units, counts reduced per warp into cnt[3 * rep + species - 1].
+__global__ void k_species_counts(const RepDev *reps, int rep0, const uint8_t *st_all, unsigned long long *cnt)
+{
+    const int rep = rep0 + (int)blockIdx.y;
+    const RepDev &R = reps[rep];
+    const uint4 *st = reinterpret_cast<const uint4 *>(st_all + R.st_off);
+    const int64_t nu = (int64_t)R.NZ * R.NB * (R.pitch / 16);
+    unsigned long long c[3] = {0, 0, 0};
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nu; u += (int64_t)gridDim.x * blockDim.x) {
+        uint4 v = __ldcs(st + u);
+        if ((v.x | v.y | v.z | v.w) == 0u) continue;
+        const uint8_t *by = reinterpret_cast<const uint8_t *>(&v);
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            uint8_t sb = by[k];
+            int sp = sp_of(sb);
+            if (sb == WALL || !sp) continue;
+            c[0] += sp == 1;
+            c[1] += sp == 2;
+            c[2] += sp == 3;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        unsigned long long x = c[j];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&cnt[3 * rep + j], x);
     }
 }
 
@@ -2379,6 +2411,7 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
         if (r.t_layer_off >= 0) {
             A.tfield = h->d_tfield + r.st_off;
             A.tlayer = h->d_tlayer + r.t_layer_off;
+            A.tNA = r.NA;
             A.tNB = r.NB;
             A.tpitch = r.pitch;
         }
@@ -2404,14 +2437,27 @@ int mks_batch_set_la(mks_handle *h, const mks_la_params *p, const double *dptran
     }
     // crystal atoms now: nothing is liquid yet (InitCountCrystal = CountCrystal);
     // the MS law has no liquid fraction (it is 1 for every species)
-    for (size_t i = 0; i < n; i++) {
-        mks_observables o;
-        int rc = obs_impl(h, (int)i, &o);
-        if (rc) return rc;
-        for (int s = 0; s < 3; s++) {
-            la[i].init_cnt[s] = la[i].cnt[s] = o.species[s];
-            if (!la[i].liquid_weighting) la[i].xliq[s] = 1.f;
+    {
+        int64_t umax = 0;
+        for (const RepHost &r : h->reps) umax = std::max<int64_t>(umax, (int64_t)r.NZ * r.NB * (r.pitch / 16));
+        unsigned long long *d_cnt = nullptr;
+        CK(cudaMallocAsync(&d_cnt, sizeof(unsigned long long) * 3 * n, h->stream));
+        CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 3 * n, h->stream));
+        for (size_t r0 = 0; r0 < n; r0 += 65535) {
+            dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>(1024, umax / 4096)),
+                      (unsigned)std::min<size_t>(65535, n - r0));
+            k_species_counts<<<grid, 256, 0, h->stream>>>(h->d_reps, (int)r0, h->d_st, d_cnt);
         }
+        CK(cudaGetLastError());
+        std::vector<unsigned long long> cnt(3 * n);
+        CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned long long) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+        cudaFreeAsync(d_cnt, h->stream);
+        CK(cudaStreamSynchronize(h->stream));
+        for (size_t i = 0; i < n; i++)
+            for (int s = 0; s < 3; s++) {
+                la[i].init_cnt[s] = la[i].cnt[s] = (long long)cnt[3 * i + s];
+                if (!la[i].liquid_weighting) la[i].xliq[s] = 1.f;
+            }
     }
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
@@ -2563,13 +2609,22 @@ int mks_batch_la_counts(mks_handle *h, int64_t *crystal, double *xliq)
     if (!h || !crystal) return fail(MKS_ERR_ARG, "bad arguments");
     if (!h->la_on) return fail(MKS_ERR_ARG, "LA mode is not set (mks_batch_set_la)");
     size_t n = h->reps.size();
-    std::vector<LADev> la(n);
-    CK(cudaMemcpyAsync(la.data(), h->d_la, sizeof(LADev) * n, cudaMemcpyDeviceToHost, h->stream));
+    // the counters lead each replica's LADev: copy that head only
+    struct Head {
+        long long init_cnt[3], cnt[3];
+        float xliq[3];
+    };
+    static_assert(offsetof(LADev, init_cnt) == 0 && offsetof(LADev, cnt) == offsetof(Head, cnt) &&
+                      offsetof(LADev, xliq) == offsetof(Head, xliq),
+                  "LADev starts with its counters");
+    std::vector<Head> hd(n);
+    CK(cudaMemcpy2DAsync(hd.data(), sizeof(Head), h->d_la, sizeof(LADev), offsetof(Head, xliq) + sizeof(float) * 3, n,
+                         cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (size_t i = 0; i < n; i++)
         for (int s = 0; s < 3; s++) {
-            crystal[3 * i + s] = la[i].cnt[s];
-            if (xliq) xliq[3 * i + s] = la[i].xliq[s];
+            crystal[3 * i + s] = hd[i].cnt[s];
+            if (xliq) xliq[3 * i + s] = hd[i].xliq[s];
         }
     return 0;
 }
