@@ -733,6 +733,8 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             dz++;
         }
         unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
+        // lanes holding the same class add their count with one atomic
+        const unsigned peers = __match_any_sync(FULL, cls);
         if (cls != CLS_NONE) {
             uint32_t key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
             int slot = nl + __popc(m & lanemask_lt());
@@ -740,7 +742,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
                 S.list[slot] = (key << 8) | (uint32_t)cls;
                 if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
             }
-            atomicAdd(&S.cnt[cls], 1);
+            if ((peers & lanemask_lt()) == 0) atomicAdd(&S.cnt[cls], __popc(peers));
             if (A) {
                 float d[4];
                 la_drate(*A, cls, la_temp_at(*A, a0 + ia, b0 + ib, z, t_mid), d, la_vacuum(*A, cls, z));
@@ -789,13 +791,17 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
     // time left in the window, FP32 on the critical path; the FP64 clock t is
     // still accumulated event by event
     float rem = (float)(t_end - t);
+    // lane l owns classes 2l and 2l+1 (ISO apart); the class rates stay fixed
+    // while the tile runs
+    const int c0 = 2 * lane, c1 = 2 * lane + 1;
+    const float rate0 = (c0 < NCLASS && c0 != CLS_ISO) ? S.rate[c0] : 0.f;
+    const float rate1 = (c1 < NCLASS && c1 != CLS_ISO) ? S.rate[c1] : 0.f;
     for (;;) {
         int nlist = S.nlist;
         if (nlist > MCCAP - 5) return fresh ? -DERR_CAPACITY : 1;   // compact the list by re-staging
-        // cumulative class weights: lane l owns classes 2l and 2l+1 (ISO apart)
-        int c0 = 2 * lane, c1 = 2 * lane + 1;
-        float w0 = (c0 < NCLASS && c0 != CLS_ISO) ? (float)S.cnt[c0] * S.rate[c0] : 0.f;
-        float w1 = (c1 < NCLASS && c1 != CLS_ISO) ? (float)S.cnt[c1] * S.rate[c1] : 0.f;
+        // cumulative class weights
+        float w0 = (float)S.cnt[c0] * rate0;
+        float w1 = (float)S.cnt[c1] * rate1;
         float s = w0 + w1;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -872,7 +878,12 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         uint32_t key = S.list[slot] >> 8;
         int z = key >> 10;
         int a = Q.a0 + (int)(key & 31) - HALO, b = Q.b0 + (int)((key >> 5) & 31) - HALO;
-        if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return 1;   // needs re-staging
+        // every listed site lies inside the staged layers with its two-layer
+        // read range (the list is built inside them and an event that lists a
+        // site outside re-stages before the next draw, below), so a drawn event
+        // is never set aside: throwing a draw away and drawing again would
+        // under-sample the sites at the band's edges
+        if ((z - 2 < zw0 && zw0 > 0) || (z + 3 > zw1 && zw1 < NZ)) return -DERR_INVARIANT;
         t += (double)dt;
         rem -= dt;
         if (sc && lane == 0)
@@ -1035,6 +1046,9 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         __syncwarp();
         nev++;
         fresh = false;
+        // a site that joined the list beyond the staged layers' safe range:
+        // re-stage now, before any draw can pick it
+        if (__ballot_sync(FULL, append && ((tz - 2 < zw0 && zw0 > 0) || (tz + 3 > zw1 && zw1 < NZ)))) return 1;
     }
 }
 
@@ -2493,6 +2507,7 @@ int mks_batch_set_tabulated(mks_handle *h, int32_t ntemp, const int32_t *temps, 
         A.sf = (float)r.cfg.sf;
         A.tfield = h->d_tfield + r.st_off;
         A.tlayer = h->d_tlayer + r.t_layer_off;
+        A.tNA = r.NA;
         A.tNB = r.NB;
         A.tpitch = r.pitch;
         A.ntab = ntemp;

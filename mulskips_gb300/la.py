@@ -254,16 +254,17 @@ class Anneal:
         r = share_rate(self.batch.class_histogram(), class_rates(self.theta, self.mat, T_max))
         return self.f_tau / float(np.max(r))
 
-    def advance(self, t_end, segment=1e-9):
+    def advance(self, t_end, segment=1e-9, on_segment=None):
         """Run every replica to time t_end in segments, each cut into a
         multiple of 8 windows no longer than its tau (the fixed tau given to
         start, else tau_at of the segment) and ending exactly at the segment
         end.  A segment is `segment` long, or 8 windows when those are
-        longer (cold stretches of the pulse)."""
+        longer (cold stretches of the pulse).  on_segment() is called after
+        each segment."""
         ev = 0
         while self.t < t_end * (1.0 - 1e-12):
             if self.tau_fixed:
-                te, tau0 = t_end, self.tau_fixed
+                te, tau0 = (min(t_end, self.t + segment) if on_segment else t_end), self.tau_fixed
             else:
                 te = min(t_end, self.t + segment)
                 tau0 = self.tau_at(self.t, te)
@@ -275,28 +276,46 @@ class Anneal:
             tau = dt / nw
             ev += self.batch.run(tau, nw, 0, self.t + dt - 0.5 * tau)
             self.t = te
+            if on_segment:
+                on_segment()
         return ev
 
     def crystal(self):
         """Crystal atoms per replica (n,)."""
         return self.batch.la_counts()[0].sum(axis=1)
 
-    def velocity(self, t1, t2):
+    def velocity(self, t1, t2, causal=False):
         """Regrowth velocity (m/s) per replica between t1 and t2: crystal
-        atoms gained / sites per layer x layer thickness / (t2 - t1)."""
+        atoms gained / sites per layer x layer thickness / (t2 - t1).  With
+        causal, each segment's share of it is passed to the engine's causal
+        LR accumulation as the segment ends (batch.lr_result() then gives
+        the gradient of the mean velocity)."""
+        scale = self.layer_nm * 1e-9 / (self.area * (t2 - t1))
         self.advance(t1)
         n1 = self.crystal()
-        self.advance(t2)
+        if causal:                                  # start() cleared the sums
+            last = [n1]
+
+            def step():
+                c = self.crystal()
+                self.batch.lr_accumulate((c - last[0]).astype(np.float64) * scale)
+                last[0] = c
+
+            self.advance(t2, on_segment=step)
+        else:
+            self.advance(t2)
         n2 = self.crystal()
-        self.last_v = (n2 - n1).astype(np.float64) / self.area * self.layer_nm * 1e-9 / (t2 - t1)
+        self.last_v = (n2 - n1).astype(np.float64) * scale
         return self.last_v
 
 
 def regrowth_velocity_lr(sim, theta, t1, t2):
-    """Mean regrowth velocity over the replicas and its LR gradient."""
+    """Mean regrowth velocity over the replicas and its LR gradient (the
+    causal form: each segment's velocity increment weighted by the score of
+    the path before it)."""
     sim.start(theta, score=True)
-    v = sim.velocity(t1, t2)
-    g, se = sim.batch.lr_grad(v)
+    v = sim.velocity(t1, t2, causal=True)
+    g, se = sim.batch.lr_result()
     return v, g, se
 
 
@@ -311,8 +330,9 @@ def _autograd_function():
         def forward(ctx, theta, sim, t1, t2):
             th = theta.detach().cpu().double().numpy()
             sim.start(th, score=True)
-            v = sim.velocity(t1, t2)
-            g, se = sim.batch.lr_grad(v)
+            v = sim.velocity(t1, t2, causal=True)
+            g, se = sim.batch.lr_result()
+            sim.last_grad = (g, se)
             ctx.save_for_backward(torch.as_tensor(g, dtype=theta.dtype, device=theta.device))
             ctx.se = se
             return torch.as_tensor(float(v.mean()), dtype=theta.dtype, device=theta.device)

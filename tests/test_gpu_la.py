@@ -6,13 +6,17 @@ static temperature field (1750 K at the surface, decaying with depth over
 reference's lists, FP64 score, same window schedule) and against
 common-random-number finite differences on the GPU:
 
-* crystal atoms at 10 and 20 ns and Ge atoms at 20 ns: GPU mean within the
-  3-sigma band of the oracle mean;
+* crystal atoms at 10 and 20 ns and Ge atoms at 20 ns: GPU mean inside the
+  95 % family band of the oracle mean (Welch t, Bonferroni over the three);
 * the score has mean zero (E[S] = 0) on both;
 * the LR gradient of f = crystal(20 ns) - crystal(10 ns) on the GPU agrees
-  with the oracle's FP64 LR gradient and with CRN central differences
-  (h = 0.02 eV) within 3 sigma, and the differences resolve a nonzero
-  gradient (so the comparison has power).
+  with the oracle's FP64 LR gradient inside the 95 % family band over the
+  four parameters;
+* at 16384 replicas the causal LR gradient of the crystal atoms gained in
+  0..20 ns (each 1 ns segment's gain weighted by the score of the path
+  before it) is within 5 % of common-random-number central differences
+  (h = 0.02 eV) for Ed2_Si, with both standard errors under 2 %; Ed2_Ge
+  agrees inside the 95 % band, its standard errors reported.
 """
 import math
 import multiprocessing as mp
@@ -74,6 +78,17 @@ def gpu(theta):
     sim.batch.close()
 
 
+def _share_tau_rate(theta):
+    """f = 0.3 over the rate of the class carrying the largest share at the
+    start (the dominant-share window), as a length."""
+    from mulskips_gb300 import la
+    sim = _sim(n=64, seed=8)
+    sim.start(theta, score=False, tau=1.0)
+    r = la.share_rate(sim.batch.class_histogram(), la.class_rates(theta, sim.mat, PULSE["Tb"] + PULSE["Ta"]))
+    sim.batch.close()
+    return 0.3 / float(np.max(r))
+
+
 def _share_tau(theta):
     """Window length of the dominant-share rule at the start of the run,
     rounded so that T1 is a multiple of 8 windows."""
@@ -118,21 +133,20 @@ def oracle(oracle_lib, theta):
     return _oracle_sample(oracle_lib, theta, _tau(theta))
 
 
-def _band(x, y, k=3.0):
-    d = x.mean() - y.mean()
-    se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
-    return d, k * se
+def _family(title, rows):
+    from stat_bands import Family
+    fam = Family(title, len(rows))
+    for name, xg, xo in rows:
+        fam.add(name, np.asarray(xg, float), np.asarray(xo, float))
+    fam.check()
 
 
 def test_la_crystal_matches_oracle(gpu, oracle):
     c0 = gpu["sim"].c0.astype(float)
     print("\ntau", gpu["tau"], "events/replica gpu", gpu["events"].mean(), "oracle", oracle["events"].mean())
-    for name, xg, xo in (("crystal(10ns)", gpu["c1"].sum(1) - c0, oracle["c1"].sum(1) - c0),
-                         ("crystal(20ns)", gpu["c2"].sum(1) - c0, oracle["c2"].sum(1) - c0),
-                         ("Ge(20ns)", gpu["c2"][:, 1], oracle["c2"][:, 1])):
-        d, b = _band(xg.astype(float), xo.astype(float))
-        print(f"{name}: gpu {xg.mean():.2f} oracle {xo.mean():.2f} diff {d:.2f} band +-{b:.2f}")
-        assert abs(d) < b, name
+    _family("LA mode, fastest-class windows", (("crystal(10ns)", gpu["c1"].sum(1) - c0, oracle["c1"].sum(1) - c0),
+                                                ("crystal(20ns)", gpu["c2"].sum(1) - c0, oracle["c2"].sum(1) - c0),
+                                                ("Ge(20ns)", gpu["c2"][:, 1], oracle["c2"][:, 1])))
     # molten material exists and the liquid fractions in use are fractions
     assert (gpu["c2"].sum(1) < c0).mean() > 0.9
     x = gpu["x2"]
@@ -151,12 +165,9 @@ def test_la_share_tau_matches_oracle(oracle_lib, theta):
     sim.batch.close()
     o = _oracle_sample(oracle_lib, theta, tau)
     print(f"\nshare-rule tau {tau:.3e} (fastest-class rule {_tau(theta):.3e})")
-    for name, xg, xo in (("crystal(10ns)", c1.sum(1) - c0, o["c1"].sum(1) - c0),
-                         ("crystal(20ns)", c2.sum(1) - c0, o["c2"].sum(1) - c0),
-                         ("Ge(20ns)", c2[:, 1], o["c2"][:, 1])):
-        d, b = _band(xg.astype(float), xo.astype(float))
-        print(f"{name}: gpu {xg.mean():.2f} oracle {xo.mean():.2f} diff {d:.2f} band +-{b:.2f}")
-        assert abs(d) < b, name
+    _family("LA mode, dominant-share windows", (("crystal(10ns)", c1.sum(1) - c0, o["c1"].sum(1) - c0),
+                                                 ("crystal(20ns)", c2.sum(1) - c0, o["c2"].sum(1) - c0),
+                                                 ("Ge(20ns)", c2[:, 1], o["c2"][:, 1])))
 
 
 def test_la_score_mean_zero(gpu, oracle):
@@ -168,31 +179,69 @@ def test_la_score_mean_zero(gpu, oracle):
         assert np.all(se > 0)
 
 
-def test_la_lr_gradient(gpu, oracle, theta):
-    sim = gpu["sim"]
-    tau = gpu["tau"]
-    fd = np.zeros(4)
-    fd_se = np.zeros(4)
-    for j in range(4):
-        e = np.zeros(4)
-        e[j] = H
-        c1p, c2p, _ = _gpu_run(sim, theta + e, tau, score=False)
-        c1m, c2m, _ = _gpu_run(sim, theta - e, tau, score=False)
-        dp = (c2p.sum(1) - c1p.sum(1)).astype(float)
-        dm = (c2m.sum(1) - c1m.sum(1)).astype(float)
-        q = (dp - dm) / (2 * H)
-        fd[j] = q.mean()
-        fd_se[j] = q.std(ddof=1) / math.sqrt(len(q))
+def test_la_lr_gradient_matches_oracle(gpu, oracle):
+    """The GPU's LR gradient of crystal(20 ns) - crystal(10 ns) against the
+    oracle's FP64 LR gradient of the same observable: each of the four
+    parameters inside the 95 % family band (Bonferroni over the four, normal
+    quantile on the two standard errors)."""
+    from scipy import stats
+    q = float(stats.norm.ppf(1.0 - 0.05 / 8.0))
     print("\nLR gpu   ", gpu["g"], "+-", gpu["se"])
     print("LR oracle", oracle["g"], "+-", oracle["se"])
-    print("CRN FD   ", fd, "+-", fd_se)
     for j in range(4):
-        b1 = 3.0 * math.hypot(gpu["se"][j], oracle["se"][j])
-        b2 = 3.0 * math.hypot(gpu["se"][j], fd_se[j])
-        assert abs(gpu["g"][j] - oracle["g"][j]) < b1, j
-        assert abs(gpu["g"][j] - fd[j]) < b2, j
-    # the test resolves a gradient
-    assert np.max(np.abs(fd) / fd_se) > 4.0
+        assert abs(gpu["g"][j] - oracle["g"][j]) <= q * math.hypot(gpu["se"][j], oracle["se"][j]), j
+    assert abs(gpu["g"][0]) > 4.0 * gpu["se"][0]          # the comparison resolves a gradient
+
+
+NBIG = 16384
+NSEG = 20
+
+
+def _causal_run(theta, n, tau, score, seed=4):
+    """Crystal atoms per species at 0, 1, ..., 20 ns of n replicas; with
+    score, the causal LR sums of the total gained per 1 ns segment."""
+    sim = _sim(n=n, seed=seed)
+    sim.start(theta, score=score, tau=tau)
+    c = [sim.batch.la_counts()[0].astype(np.float64)]
+    for k in range(NSEG):
+        sim.advance(T2 * (k + 1) / NSEG)
+        ck = sim.batch.la_counts()[0].astype(np.float64)
+        if score:
+            sim.batch.lr_accumulate((ck - c[-1]).sum(1))
+        c.append(ck)
+    g = sim.batch.lr_result() if score else None
+    sim.batch.close()
+    return np.array(c), g
+
+
+def test_la_lr_gradient_within_5pct_of_finite_differences(theta):
+    """LR against finite differences at the benchmark spec's bar.  f = crystal
+    atoms gained from 0 to 20 ns (melting makes it negative), 16384
+    replicas, windows of the dominant-share rule (capped at 8 per 1 ns
+    segment).  The causal LR gradient (mks_batch_lr_accumulate after each
+    segment, mks_batch_lr_result) against common-random-number central
+    differences (h = 0.02 eV, the same seeds at theta +- h): for Ed2_Si the
+    two agree within 5 % with both standard errors under 2 % of the
+    gradient; for Ed2_Ge, inside the 95 % band of the two standard errors."""
+    from scipy import stats
+    k = math.ceil(T2 / NSEG / 8.0 / _share_tau_rate(theta))
+    tau = T2 / (NSEG * 8.0 * k)
+    c, (g, se) = _causal_run(theta, NBIG, tau, True)
+    f = (c[-1] - c[0]).sum(1)
+    fd, fd_se = np.zeros(2), np.zeros(2)
+    for j, nfd in ((0, 4096), (1, NBIG)):
+        e = np.zeros(4)
+        e[j] = H
+        cp, _ = _causal_run(theta + e, nfd, tau, False)
+        cm, _ = _causal_run(theta - e, nfd, tau, False)
+        dq = ((cp[-1] - cp[0]).sum(1) - (cm[-1] - cm[0]).sum(1)) / (2 * H)
+        fd[j], fd_se[j] = dq.mean(), dq.std(ddof=1) / math.sqrt(len(dq))
+    rel = np.abs(g[:2] - fd) / np.abs(fd)
+    print(f"\nE f {f.mean():.2f}; causal LR {g} +- {se}; CRN FD (Ed2_Si, Ed2_Ge) {fd} +- {fd_se}; "
+          f"relative difference {rel}, relative SE LR {se[:2] / np.abs(fd)}, FD {fd_se / np.abs(fd)}")
+    assert rel[0] <= 0.05 and se[0] <= 0.02 * abs(fd[0]) and fd_se[0] <= 0.02 * abs(fd[0])
+    q = float(stats.norm.ppf(1.0 - 0.05 / 2.0))
+    assert abs(g[1] - fd[1]) <= q * math.hypot(se[1], fd_se[1]) and fd_se[1] <= 0.02 * abs(fd[1])
 
 
 def test_la_schedules_agree(theta):
@@ -219,7 +268,7 @@ def test_autograd_function(theta):
     v = la.regrowth_velocity(th, sim, T1, T2)
     assert v.dim() == 0 and abs(float(v) - sim.last_v.mean()) < 1e-12 * max(1.0, abs(float(v)))
     v.backward()
-    g, se = sim.batch.lr_grad(sim.last_v)
+    g, se = sim.last_grad                          # the causal LR gradient of the forward pass
     np.testing.assert_allclose(th.grad.numpy(), g, rtol=1e-12, atol=0)
     assert np.all(np.isfinite(g)) and np.all(se > 0)
     sim.batch.close()
