@@ -335,15 +335,18 @@ def bench_accuracy(width):
     """The growth-rate error at this benchmark's window rule (f = 0.3) and
     tile width, as the statistical parity test measured it on GB300 on the
     same model in a 480^3 box at the benchmark's three temperatures (32 GPU
-    replicas against 32 serial seeds, 95 % family band): read from
-    profiles/etch_accuracy_480cube.json, which that test run wrote."""
+    replicas against 32 serial seeds, 95 % family band): the cases of
+    profiles/etch_accuracy_480cube.json (written from that test's record) at
+    this run's width and f."""
     p = os.path.join(ROOT, "profiles", "etch_accuracy_480cube.json")
     if not os.path.exists(p):
         return None
     d = json.load(open(p))
-    d["bench_tile_width"] = width
-    d["bench_f"] = ACCURATE_F
-    return d
+    tag = f"width {width} colours 3 k2*tau=0.265"
+    cases = [f for f in d["families"] if tag in f["case"]]
+    return {"source": d["source"], "band": d["band"], "bench_tile_width": width, "bench_f": ACCURATE_F,
+            "cases": [{"case": f["case"], "growth_rate": f["observables"]["growth rate um/h"],
+                       "atoms": f["observables"]["atoms"]} for f in cases]}
 
 
 def batched_bench(args):

@@ -733,8 +733,6 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             dz++;
         }
         unsigned m = __ballot_sync(FULL, cls != CLS_NONE);
-        // lanes holding the same class add their count with one atomic
-        const unsigned peers = __match_any_sync(FULL, cls);
         if (cls != CLS_NONE) {
             uint32_t key = (uint32_t)key_of(ia + HALO, ib + HALO, z);
             int slot = nl + __popc(m & lanemask_lt());
@@ -742,7 +740,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
                 S.list[slot] = (key << 8) | (uint32_t)cls;
                 if (use_pos) S.pos[pos_index(key, zw0)] = (uint16_t)slot;
             }
-            if ((peers & lanemask_lt()) == 0) atomicAdd(&S.cnt[cls], __popc(peers));
+            atomicAdd(&S.cnt[cls], 1);
             if (A) {
                 float d[4];
                 la_drate(*A, cls, la_temp_at(*A, a0 + ia, b0 + ib, z, t_mid), d, la_vacuum(*A, cls, z));

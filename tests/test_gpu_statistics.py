@@ -144,11 +144,12 @@ def etch_oracle(tmp_path_factory, T):
     return _ETCH_REF[T]
 
 
-# (T, tile width, k2 tau, colours): the benchmark's window rule f = 0.3 and
-# tile width 6 (brick tiling, three colours) at its three temperatures, on the
-# same model in a 480^3 box; the same on the four-colour grid; a shorter
-# window at width 8
+# (T, tile width, k2 tau, colours): the benchmark's window rule f = 0.3 at
+# tile widths 6 and 8 (brick tiling, three colours) at its three
+# temperatures, on the same model in a 480^3 box; width 6 on the four-colour
+# grid; a shorter window at width 8
 @pytest.mark.parametrize("T,width,f,colours", [(1000.0, 6, 0.3, 3), (1100.0, 6, 0.3, 3), (1200.0, 6, 0.3, 3),
+                                               (1000.0, 8, 0.3, 3), (1100.0, 8, 0.3, 3), (1200.0, 8, 0.3, 3),
                                                (1100.0, 6, 0.3, 4), (1100.0, 8, 0.064, 3)])
 def test_etch_matches_serial_reference(tmp_path_factory, T, width, f, colours):
     from mulskips_gb300 import Batch, arrhenius_tables
