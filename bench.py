@@ -187,7 +187,7 @@ def gb300(args, rank, world):
 
     lat.init_flat("S", LEN1)
     lat.set_rates(*tables[1])
-    width = choose_width(lat, lat.suggest_tau(ACCURATE_F))
+    width = choose_width(lat, lat.suggest_tau(ACCURATE_F), widths=(6, 8), windows=64)
     taus = []
 
     def step(k):
