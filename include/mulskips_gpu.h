@@ -47,6 +47,21 @@
  * One handle holds a batch of independent replicas (1 for a plain run) on one
  * GPU, with one CUDA stream.  Handles are not thread-safe; several handles
  * may live in one process.
+ *
+ * Arm-chair stacking.  With PtransZig < 1 (a single-replica handle, NCov = 0)
+ * a deposition on a coor-1 site may take the hexagonal (arm-chair) position
+ * of IF_Arm_Choice.f:21-56, whose atoms lie off the diamond sub-grid
+ * (FIND_SN.f:67).  Such a handle runs the explicit-neighbour engine: one
+ * LattCoo word and one LattInd word per grid point and the NextN list of
+ * every listed site, as the reference stores them (defsystem.f:49,87-91,
+ * defdertype.f:25-45).  The initializers build the lattice as usual; it is
+ * expanded at the first call that runs or reads it.  mks_replay, mks_run,
+ * mks_get_lattice, mks_get_observables (nonepitaxial: the non-epitaxial bulk
+ * atoms of the reference's _d.xyz, WriteMolMolXYZFile.f:120-160),
+ * mks_write_frame, mks_get_status, mks_get_clock and mks_suggest_tau work
+ * on it; the compact-lattice calls (mks_get_state, mks_class_histogram,
+ * mks_site_rates, mks_frame_sites, mks_replay_noalloc, mks_set_clock) return
+ * MKS_ERR_UNSUPPORTED once it is expanded.
  */
 #ifndef MULSKIPS_GPU_H
 #define MULSKIPS_GPU_H
@@ -73,7 +88,7 @@ typedef struct {
     int32_t lenx, leny, lenz;      /* LenX, LenY, LenZ; LenX, LenY multiples of 12, LenZ of 3 */
     int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (0, or 1 with NCrystal <= 2) */
     int32_t list_crystal[3];       /* atomic numbers (ListCrystal)               */
-    double ptrans_zig;             /* PtransZig; the engine requires 1.0         */
+    double ptrans_zig;             /* PtransZig; < 1 selects arm-chair stacking (see below) */
     double sf;                     /* super-lattice parameter in Angstrom        */
     uint64_t seed;                 /* IDUM / replica seed                        */
     int32_t list_cov[3];           /* coverage atomic numbers (ListCov, main.f:91) */
@@ -85,7 +100,7 @@ typedef struct {
     int32_t x, y, z;               /* grid coordinates of the event site         */
     int8_t itrans;                 /* 1..3 deposition of that species, 4 evaporation,
                                       5 desorption, 6 absorption of coverage species 1 */
-    int8_t arm;                    /* arm-chair stacking choice (must be 0)      */
+    int8_t arm;                    /* arm-chair stacking choice of a tie (IF_Arm_Choice.f:44-51) */
     int16_t pad;
 } mks_event;
 
@@ -138,6 +153,24 @@ int mks_init_flat(mks_handle *h, char kind, int32_t len1);
 /* LattCoo(0:LenX-1,0:LenY-1,0:LenZ), x fastest (Fortran order).           */
 int mks_load_lattice(mks_handle *h, const int32_t *lattcoo);
 int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
+/* Arm-chair stacking handles only (PtransZig < 1): load the full reference
+ * state -- LattCoo(0:LenX-1, 0:LenY-1, 0:LenZ) (x fastest) and n list
+ * entries (ListAdAtom, ListAtom and ListVoid; grid point xyz[3i..3i+2] and
+ * NextN nn[12i..12i+11], defdertype.f:25-45) -- and rate every entry with
+ * Get_Prob; ini[i] != 0 (ini may be NULL) keeps an unsupported coor-1 site at
+ * Get_Prob_Ini's dummy rate 1e-6 (Get_Prob_Ini.f:102-104).  Continuation
+ * from a saved state (main.f:385-403 writes LattCoo; the lists follow).   */
+int mks_load_lists(mks_handle *h, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
+                   const uint8_t *ini);
+/* Arm-chair stacking handles only: every listed site, with its grid point
+ * (xyz, 3 per site), NextN (nn, 12 per site), kind (1 with an event, the
+ * ListAdAtom entries; 2 a bulk atom, ListAtom; 3 a void, ListVoid), event
+ * (1 deposition, 2 dummy deposition, 4 evaporation, 5 isolated atom) and FP32
+ * rate (the ProbTrans of the tree leaf; 0 for an isolated atom, whose rate is
+ * 1e5 x the total, Get_Prob.f:305).  *n gets the count; the arrays (all
+ * non-NULL) are written when cap >= *n.                                   */
+int mks_get_lists(mks_handle *h, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *event, float *rate,
+                  int64_t *n);
 /* Compact state: one byte per diamond site (a, b, z1) at index
  * (z1 * (LenY/6) + b) * (LenX/6) + a (bits 0-1 species, 2-4 coordination,
  * 5-6 first list entry, 7 dummy flag; 0x80 a wall; coordination field 5 with

@@ -32,10 +32,16 @@ def _run(cmd):
     return r.stdout
 
 
-def engine_cmd(out):
-    src = os.path.join(PKG, "csrc", "engine.cu")
-    return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-            "-I", os.path.join(ROOT, "include"), src, "-o", out]
+ENGINE_SOURCES = ("engine.cu", "stacking.cu")
+
+
+def object_cmd(src, out):
+    return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+            "-I", os.path.join(ROOT, "include"), os.path.join(PKG, "csrc", src), "-o", out]
+
+
+def link_cmd(objs, out):
+    return [nvcc(), *ARCH, "-shared", *objs, "-o", out]
 
 
 def host_cmd(out, lib):
@@ -52,7 +58,11 @@ def host_only(out=None):
 def build_all(verbose=False):
     os.makedirs(LIB, exist_ok=True)
     lib = os.path.join(LIB, "libmulskips_gpu.so")
-    out = _run(engine_cmd(lib))
+    objs = [os.path.join(LIB, os.path.splitext(src)[0] + ".o") for src in ENGINE_SOURCES]
+    # the translation units compile in parallel, then one link
+    with ThreadPoolExecutor(len(objs)) as ex:
+        outs = list(ex.map(lambda so: _run(object_cmd(*so)), zip(ENGINE_SOURCES, objs)))
+    out = "".join(outs) + _run(link_cmd(objs, lib))
     if verbose:
         print(out)
     host_src = os.path.join(PKG, "host", "mulskips_main.cpp")

@@ -32,6 +32,7 @@
 #include "shapes.cuh"
 #include "tiling.cuh"
 #include "rng.cuh"
+#include "stacking.cuh"
 #include "../../include/mulskips_gpu.h"
 
 using namespace mks;
@@ -1628,6 +1629,11 @@ struct mks_handle {
     double last_ms = 0.0;
     double time_acc = 0.0;
     unsigned char *noalloc_scratch = nullptr;  // device address of the mks_replay_noalloc array (set at creation)
+    // PtransZig < 1: the explicit-neighbour engine (stacking.cu) runs the
+    // lattice; the initializers still build it in compact form, expanded at
+    // the first call that needs the explicit form (stk_dirty)
+    mks_stk::State *stk = nullptr;
+    bool stk_dirty = false;
 };
 
 namespace {
@@ -1692,8 +1698,10 @@ int check_config(const mks_config &c)
         return fail(MKS_ERR_UNSUPPORTED, "a coverage species needs NCrystal <= 2 (species value 3 marks covered sites)");
     if (c.ncov == 1 && (c.list_cov[0] <= 0 || c.list_cov[0] >= 113))
         return fail(MKS_ERR_ARG, "coverage species atomic number %d", c.list_cov[0]);
-    if (c.ptrans_zig != 1.0)
-        return fail(MKS_ERR_UNSUPPORTED, "PtransZig=%g: arm-chair stacking is not in the compact GPU lattice", c.ptrans_zig);
+    if (!(c.ptrans_zig >= 0.0 && c.ptrans_zig <= 1.0)) return fail(MKS_ERR_ARG, "PtransZig=%g outside [0, 1]", c.ptrans_zig);
+    if (c.ptrans_zig != 1.0 && c.ncov)
+        return fail(MKS_ERR_UNSUPPORTED, "PtransZig=%g with a coverage species: arm-chair stacking runs without coverage",
+                    c.ptrans_zig);
     return 0;
 }
 
@@ -1728,6 +1736,7 @@ int read_status(mks_handle *h, DevStatus &s);
 int rescan(mks_handle *h)
 {
     NvtxRange nr("mks_rescan");
+    if (h->stk) h->stk_dirty = true;      // a new compact lattice: expand it before the next stacking call
     int nq = (int)h->quads_h.size();
     k_band_init<<<std::min(1024, (nq + 255) / 256), 256, 0, h->stream>>>(h->d_quads, 0, nq);
     for (size_t i = 0; i < h->reps.size(); i++) {
@@ -1943,6 +1952,11 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         h->reps.push_back(r);
     }
     h->st_bytes = off;
+    for (int i = 0; i < n; i++)
+        if (cfgs[i].ptrans_zig != 1.0 && n != 1) {
+            delete h;
+            return fail(MKS_ERR_UNSUPPORTED, "arm-chair stacking (PtransZig < 1) runs in single-replica handles");
+        }
     partition(h, 8);
     auto cleanup_fail = [&](const char *what, cudaError_t e) {
         fail(MKS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -2004,7 +2018,62 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         mks_destroy(h);
         return rc;
     }
+    if (n == 1 && cfgs[0].ptrans_zig != 1.0) {
+        std::string err;
+        rc = mks_stk::create(&h->stk, cfgs[0], h->stream, err);
+        if (rc) {
+            mks_destroy(h);
+            return fail(rc, "%s", err.c_str());
+        }
+    }
     *out = h;
+    return 0;
+}
+
+// Arm-chair stacking: the explicit-neighbour form of the lattice, expanded
+// from the compact one after an initializer wrote it.
+int stk_sync(mks_handle *h)
+{
+    if (!h->stk || !h->stk_dirty) return 0;
+    const RepHost &r = h->reps[0];
+    std::string err;
+    int rc = mks_stk::from_compact(h->stk, h->d_st + r.st_off, r.NA, r.NB, r.NZ, r.pitch, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    h->stk_dirty = false;
+    return 0;
+}
+
+int stk_unsupported(const char *what)
+{
+    return fail(MKS_ERR_UNSUPPORTED, "%s: not available with arm-chair stacking (PtransZig < 1)", what);
+}
+
+// tau = f / r*, r* the rate carrying the largest share of the total (the
+// rule of mks_suggest_tau), from the explicit lists; dummies and isolated
+// atoms do not count
+int stk_suggest_tau(mks_handle *h, double f, double *tau)
+{
+    std::string err;
+    int64_t n = 0;
+    int rc = mks_stk::get_lists(h->stk, 0, nullptr, nullptr, nullptr, nullptr, nullptr, &n, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    std::vector<int32_t> xyz(3 * (size_t)n + 3), nn(12 * (size_t)n + 12), kind((size_t)n + 1), ev((size_t)n + 1);
+    std::vector<float> rate((size_t)n + 1);
+    rc = mks_stk::get_lists(h->stk, n, xyz.data(), nn.data(), kind.data(), ev.data(), rate.data(), &n, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    std::vector<std::pair<float, double>> share;
+    std::sort(rate.begin(), rate.begin() + n);
+    for (int64_t i = 0; i < n; i++) {
+        if (!(rate[i] > 1.e-6f)) continue;
+        if (!share.empty() && share.back().first == rate[i]) share.back().second += rate[i];
+        else share.push_back({rate[i], rate[i]});
+    }
+    if (share.empty()) return fail(MKS_ERR_ARG, "no event with a rate");
+    auto best = std::max_element(share.begin(), share.end(),
+                                 [](const std::pair<float, double> &a, const std::pair<float, double> &b) {
+                                     return a.second < b.second;
+                                 });
+    *tau = f / (double)best->first;
     return 0;
 }
 
@@ -2264,6 +2333,7 @@ void mks_destroy(mks_handle *h)
     if (!h) return;
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    mks_stk::destroy(h->stk);
     cudaFree(h->d_st);
     cudaFree(h->d_reps);
     cudaFree(h->d_quads);
@@ -2311,7 +2381,11 @@ int mks_batch_set_rates(mks_handle *h, const double *ptransE, const double *ptra
 int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD)
 {
     if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_set_rates needs a single-replica handle");
-    return mks_batch_set_rates(h, ptransE, ptransD);
+    int rc = mks_batch_set_rates(h, ptransE, ptransD);
+    if (rc || !h->stk) return rc;
+    std::string err;
+    rc = mks_stk::set_rates(h->stk, ptransE, ptransD, err);
+    return rc ? fail(rc, "%s", err.c_str()) : 0;
 }
 
 int mks_batch_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes)
@@ -2662,6 +2736,7 @@ int64_t mks_state_size(mks_handle *h)
 int mks_get_state(mks_handle *h, uint8_t *out, int64_t n)
 {
     if (!h || !out || n < mks_state_size(h)) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) return stk_unsupported("mks_get_state (see mks_get_lattice)");
     const RepHost &r = h->reps[0];
     if (r.NA == r.pitch)
         CK(cudaMemcpyAsync(out, h->d_st + r.st_off, (size_t)mks_state_size(h), cudaMemcpyDeviceToHost, h->stream));
@@ -2737,9 +2812,38 @@ int mks_set_state(mks_handle *h, const uint8_t *in, int64_t n)
     return rescan(h);
 }
 
+int mks_load_lists(mks_handle *h, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
+                   const uint8_t *ini)
+{
+    if (!h || !lattcoo || n < 0 || (n && (!xyz || !nn))) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->stk) return fail(MKS_ERR_ARG, "mks_load_lists needs a handle with PtransZig < 1");
+    std::string err;
+    int rc = mks_stk::load_lists(h->stk, lattcoo, n, xyz, nn, ini, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    h->stk_dirty = false;
+    return 0;
+}
+
+int mks_get_lists(mks_handle *h, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *event, float *rate,
+                  int64_t *n)
+{
+    if (!h || !n) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h->stk) return fail(MKS_ERR_ARG, "mks_get_lists needs a handle with PtransZig < 1");
+    int rc = stk_sync(h);
+    if (rc) return rc;
+    std::string err;
+    rc = mks_stk::get_lists(h->stk, cap, xyz, nn, kind, event, rate, n, err);
+    return rc ? fail(rc, "%s", err.c_str()) : 0;
+}
+
 int mks_get_lattice(mks_handle *h, int32_t *lc)
 {
     if (!h || !lc) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) {
+        std::string err;
+        int rc = mks_stk::get_lattice(h->stk, lc, err);
+        return rc ? fail(rc, "%s", err.c_str()) : 0;
+    }
     const RepHost &r = h->reps[0];
     std::vector<uint8_t> st((size_t)mks_state_size(h));
     int rc = mks_get_state(h, st.data(), (int64_t)st.size());
@@ -3103,6 +3207,14 @@ int mks_replay(mks_handle *h, const mks_event *trace, int64_t n)
 {
     if (!h || (n > 0 && !trace) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
     if (n == 0) return 0;
+    if (h->stk) {
+        int rc = stk_sync(h);
+        if (rc) return rc;
+        std::string err;
+        int64_t done = 0;
+        rc = mks_stk::replay(h->stk, trace, n, &done, err);
+        return rc ? fail(rc, "replay, event %lld: %s", (long long)done, err.c_str()) : 0;
+    }
     mks_event *d_ev = nullptr;
     long long *d_done = nullptr;
     CK(cudaMallocAsync(&d_ev, sizeof(mks_event) * (size_t)n, h->stream));
@@ -3132,6 +3244,7 @@ int mks_replay_noalloc(mks_handle *h, const mks_event *trace, int64_t n)
         return fail(MKS_ERR_ARG, "mks_replay_noalloc: %lld events exceed the per-call limit of %d; split the trace",
                     (long long)n, MKS_REPLAY_NOALLOC_MAX);
     if (n == 0) return 0;
+    if (h->stk) return stk_unsupported("mks_replay_noalloc");
     unsigned char *scratch = h->noalloc_scratch;
     long long *d_done = reinterpret_cast<long long *>(scratch);
     mks_event *d_ev = reinterpret_cast<mks_event *>(scratch + 256);
@@ -3158,6 +3271,13 @@ int mks_run(mks_handle *h, double tau, int64_t max_windows, int64_t max_events, 
             int64_t *events_done, double *time_out)
 {
     if (!h || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_run needs a single-replica handle");
+    if (h->stk) {
+        int rc = stk_sync(h);
+        if (rc) return rc;
+        std::string err;
+        rc = mks_stk::run(h->stk, tau, max_windows, max_events, max_time, events_done, time_out, err);
+        return rc ? fail(rc, "%s", err.c_str()) : 0;
+    }
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
     if (rc) return rc;
@@ -3194,6 +3314,7 @@ int mks_site_rates(mks_handle *h, int32_t rep, const int32_t *xyz, int64_t n, in
 {
     if (!h || n < 0 || (n && (!xyz || !cls || !rate)) || rep < 0 || rep >= (int)h->reps.size())
         return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) return stk_unsupported("mks_site_rates (see mks_get_lists)");
     if (n == 0) return 0;
     int32_t *d_xyz = nullptr, *d_cls = nullptr;
     float *d_rate = nullptr;
@@ -3217,6 +3338,7 @@ int mks_site_rates(mks_handle *h, int32_t rep, const int32_t *xyz, int64_t n, in
 int mks_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
 {
     if (!h || !hist || nclass < NCLASS) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) return stk_unsupported("mks_class_histogram (see mks_get_lists)");
     unsigned long long *d_hist = nullptr;
     CK(cudaMallocAsync(&d_hist, sizeof(unsigned long long) * NCLASS, h->stream));
     CK(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * NCLASS, h->stream));
@@ -3251,6 +3373,13 @@ int mks_batch_class_histogram(mks_handle *h, int64_t *hist, int32_t nclass)
 int mks_get_observables(mks_handle *h, mks_observables *obs)
 {
     if (!h || !obs) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk) {
+        int rc = stk_sync(h);
+        if (rc) return rc;
+        std::string err;
+        rc = mks_stk::observables(h->stk, obs, err);
+        return rc ? fail(rc, "%s", err.c_str()) : 0;
+    }
     return obs_impl(h, 0, obs);
 }
 
@@ -3267,6 +3396,7 @@ int mks_batch_observables(mks_handle *h, mks_observables *obs)
 int mks_get_status(mks_handle *h, mks_status *st)
 {
     if (!h || !st) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk) return mks_stk::status(h->stk, st);
     DevStatus s;
     int rc = read_status(h, s);
     if (rc) return rc;
@@ -3330,6 +3460,7 @@ int32_t mks_get_colours(mks_handle *h) { return h ? h->ncolour : 0; }
 int mks_suggest_tau(mks_handle *h, double f, double *tau)
 {
     if (!h || !tau || !(f > 0.0)) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) return stk_suggest_tau(h, f, tau);
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
     if (rc) return rc;
@@ -3361,6 +3492,7 @@ int mks_suggest_tau(mks_handle *h, double f, double *tau)
 int mks_frame_sites(mks_handle *h, int32_t kind, uint32_t *idx, int64_t cap, int64_t *n_out)
 {
     if (!h || !n_out || (kind != 0 && kind != 1) || h->reps.size() != 1) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk && !h->stk_dirty) return stk_unsupported("mks_frame_sites (see mks_get_lists)");
     const RepHost &r = h->reps[0];
     int64_t nunit = (int64_t)r.NZ * r.NB * (r.pitch / 16);
     int nchunk = (int)((nunit + FRAME_UNITS - 1) / FRAME_UNITS);
@@ -3581,6 +3713,7 @@ int mks_write_frame(mks_handle *h, const char *base, double time, int64_t iter, 
 int mks_get_clock(mks_handle *h, int32_t rep, double *time, int64_t *window, int64_t *events)
 {
     if (!h || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk) return mks_stk::clock(h->stk, time, window, events);
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
     if (rc) return rc;
@@ -3594,6 +3727,7 @@ int mks_set_clock(mks_handle *h, int32_t rep, double time, int64_t window, int64
 {
     if (!h || rep < 0 || rep >= (int)h->reps.size() || window < 0 || events < 0 || !(time >= 0.0))
         return fail(MKS_ERR_ARG, "bad arguments");
+    if (h->stk) return stk_unsupported("mks_set_clock");
     std::vector<RepDev> d;
     int rc = download_reps(h, d);
     if (rc) return rc;

@@ -1,0 +1,1628 @@
+// stacking.cu — the MulSKIPS KMC with arm-chair (hexagonal) stacking on
+// GB300 (sm_103a): the reference's explicit-neighbour data model on the
+// device, advanced by the synchronous-sublattice method.
+//
+// Layout in HBM (one replica):
+//   coo[z+ZG][y][x]  uint32 LattCoo word of every grid point (defsystem.f:
+//                    87-91: bits 0-7 CovInd, 113 a wall; 23 Occ; 24-26 Coor;
+//                    27-29 species), z from -ZG to lz+ZG (zero guard planes)
+//   ind[z+ZG][y][x]  int32 record of the site (LattInd), 0 for none
+//   rec[1..]         one 36-byte record per listed site: grid point, the four
+//                    NextN coordinates (int16; defdertype.f:25-45), event
+//                    code and FP32 rate; rec[0] stays zero, the reference's
+//                    zero guard entry of every list
+// The (x, y) plane is cut into an even number of square tiles per side, at
+// least 24 grid units wide, coloured by tile parity (four colours).  An event
+// writes its site and its NextN sites (one bond, <= 6 units after rounding)
+// and reads two bonds away at most (<= 12 units): two tiles of one colour are
+// a tile apart, so one tile's writes never meet another's reads.  In a window
+// of length tau the four colours run in turn, each tile from the window's
+// start to its end with exponential waiting times, one warp per tile:
+// lanes sum the rates of the tile's list and find the drawn entry with a
+// prefix scan, lane 0 applies the event (Deposition.f / Evaporation.f,
+// serial by nature: every step reads what the previous one wrote).
+// Each tile keeps a list of record ids with an event.  An event of tile A may
+// give a site of an idle neighbour tile B its event; B's list then grows by
+// an atomic append.  At the start of its phase a tile compacts its list
+// (drops entries that lost their event, moved to another tile or repeat).
+// Records freed by a tile wait on its pending stack until its next phase, so
+// a record never changes its site while a list entry of the running phase
+// could still select it.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdarg.h>
+#include <string.h>
+#include <math.h>
+#include <vector>
+#include <algorithm>
+#include "stacking.cuh"
+#include "rng.cuh"
+
+namespace mks_stk {
+namespace {
+
+using mks::U4;
+using mks::philox4x32_10;
+using mks::u01;
+
+constexpr int ZG = 8;               // guard planes below z = 0 and above z = lz
+constexpr uint32_t B_OCC = 1u << 23;
+constexpr int WALLIND = 113;        // CovInd of a wall (SetSi.f:38-46)
+constexpr int TWMIN = 24;           // smallest tile side (grid units)
+constexpr int LCAP = 4096;          // list entries per tile
+constexpr int FCAP = 1024;          // free records per tile and stack
+enum : uint8_t { EV_NONE = 0, EV_DEP = 1, EV_DUMMY = 2, EV_EVAP = 4, EV_ISO = 5 };
+enum : uint8_t { F_LISTED = 1, F_SEEN = 2 };
+// device error codes (err[0]); err[1..3] say where
+enum { E_INVARIANT = 3, E_CAPACITY = 4, E_NOTAPPLICABLE = 7, E_BOUNDS = 8, E_NBUFF = 9, E_ARM = 10 };
+
+struct Rec {
+    int16_t x, y, z;
+    int16_t nn[4][3];
+    uint8_t ev, flags;
+    float rate;
+};
+static_assert(sizeof(Rec) == 36, "record layout");
+
+struct P3 {
+    int x, y, z;
+};
+
+struct Dev {
+    uint32_t *coo;
+    int32_t *ind;
+    Rec *rec;
+    int lx, ly, lz;
+    int tw, ntx, nty;
+    int32_t *tl, *tl_n;        // tile lists [tile][LCAP] and their lengths
+    int32_t *fr, *fr_n;        // reusable records per tile [tile][FCAP]
+    int32_t *fp, *fp_n;        // records freed in the tile's current phase
+    int32_t *top;              // records handed out so far (+1: rec[0] is the guard)
+    int rcap;
+    int32_t *err;              // [0] first error code, [1..3] where
+    int32_t *nmc;              // sites with an event (NumAdAtom)
+    unsigned long long *events;
+    int32_t *stop;             // set when fewer than 21 sites keep an event
+    const double *pe;          // [3][4][4][4]: PTransE(s, n1, n2, n3, 0, 0, 0)
+    const double *pd;          // [3][3]: PTransD(s, coor)
+    double cth[2], sth[2];     // FIND_NN: cos, sin of 2 pi irot / 3 (pi in single precision)
+    double shift;              // FIND_SN: arm-chair shift 8.6602254037 (single precision)
+    double pzig;               // PtransZig
+    uint32_t k0, k1;           // seed
+};
+
+// Per-warp event context (lane 0).
+struct Ctx {
+    int tile;                  // running tile; -1 in the replay kernel
+    P3 nbuff;                  // Evaporation.f's NBuff, kept across calls as there
+    int forced_arm;            // replay: the trace's stacking choice
+    uint32_t key2, key3;       // Philox counter words of the stacking ties
+    uint32_t nties;
+    int dmc;                   // change of the count of sites with an event
+};
+
+__device__ __forceinline__ int coor_of(uint32_t v) { return (v >> 24) & 7; }
+__device__ __forceinline__ int occ_of(uint32_t v) { return (v >> 23) & 1; }
+__device__ __forceinline__ int cov_of(uint32_t v) { return v & 255; }
+__device__ __forceinline__ int sp_of(uint32_t v) { return (v >> 27) & 7; }
+__device__ __forceinline__ uint32_t with_coor(uint32_t v, int c) { return (v & ~(7u << 24)) | ((uint32_t)(c & 7) << 24); }
+__device__ __forceinline__ bool same(P3 a, P3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+__device__ __forceinline__ int isign(int a, int b) { return b >= 0 ? abs(a) : -abs(a); }
+// NINT: nearest integer, halves away from zero
+__device__ __forceinline__ int nint(double v) { return (int)round(v); }
+
+__device__ void set_err(const Dev &D, int code, int a = 0, int b = 0, int c = 0)
+{
+    if (atomicCAS(D.err, 0, code) == 0) {
+        D.err[1] = a;
+        D.err[2] = b;
+        D.err[3] = c;
+    }
+}
+
+// grid point -> array index; a point outside the arrays is an error and
+// reads (0, 0, 0) instead, so no access leaves the arrays
+__device__ __forceinline__ int64_t gidx(const Dev &D, P3 p)
+{
+    if (p.x < 0 || p.x >= D.lx || p.y < 0 || p.y >= D.ly || p.z < -ZG || p.z > D.lz + ZG) {
+        set_err(D, E_BOUNDS, p.x, p.y, p.z);
+        return (int64_t)ZG * D.ly * D.lx;
+    }
+    return ((int64_t)(p.z + ZG) * D.ly + p.y) * D.lx + p.x;
+}
+__device__ __forceinline__ uint32_t cw(const Dev &D, P3 p) { return D.coo[gidx(D, p)]; }
+__device__ __forceinline__ int tile_of(const Dev &D, int x, int y) { return (y / D.tw) * D.ntx + x / D.tw; }
+__device__ __forceinline__ P3 nn_at(const Rec &r, int i) { return P3{r.nn[i][0], r.nn[i][1], r.nn[i][2]}; }
+__device__ __forceinline__ void put_nn(Rec &r, int i, P3 p)
+{
+    r.nn[i][0] = (int16_t)p.x;
+    r.nn[i][1] = (int16_t)p.y;
+    r.nn[i][2] = (int16_t)p.z;
+}
+__device__ __forceinline__ bool in_list(const P3 nn[4], P3 s)
+{
+    return same(nn[0], s) || same(nn[1], s) || same(nn[2], s) || same(nn[3], s);
+}
+__device__ __forceinline__ void load_nn(const Rec &r, P3 nn[4])
+{
+    for (int i = 0; i < 4; i++) nn[i] = nn_at(r, i);
+}
+__device__ __forceinline__ bool rec_lists(const Dev &D, int r, P3 s)
+{
+    P3 nn[4];
+    load_nn(D.rec[r], nn);
+    return in_list(nn, s);
+}
+
+__device__ __forceinline__ double pd_of(const Dev &D, int s, int coor) { return D.pd[(s - 1) * 3 + coor - 1]; }
+
+// Get_Prob (Get_Prob.f:54-331) without coverage: the event code and FP32 rate
+// of a site from its LattCoo word and NextN.  An empty site carries the sum
+// of the deposition rates (the species is drawn when the event happens, from
+// the same shares as Get_Prob.f:159-176 draws it); an isolated atom gets code
+// EV_ISO, its rate 1e5 x the total being set at selection (:300-306).
+__device__ void get_prob(const Dev &D, int occ, int nsic, int coor, P3 site, const P3 nn[4], uint8_t &ev, float &rate)
+{
+    if (!occ) {
+        if (coor == 1) {
+            int cnn = coor_of(cw(D, nn[0]));
+            if (cnn >= 2) {
+                ev = EV_DEP;
+                rate = (float)(pd_of(D, 1, 1) + pd_of(D, 2, 1) + pd_of(D, 3, 1));
+            } else {
+                ev = EV_DUMMY;        // Get_Prob.f:181-184
+                rate = 1.e-8f;
+            }
+        } else if (coor == 2 || coor == 3) {
+            ev = EV_DEP;
+            rate = (float)(pd_of(D, 1, coor) + pd_of(D, 2, coor) + pd_of(D, 3, coor));
+        } else {
+            ev = EV_NONE;
+            rate = 0.f;
+        }
+        return;
+    }
+    int nsi = 0, nc = 0, nb = 0, nw = 0;
+    for (int i = 0; i < 4; i++) {
+        uint32_t v = cw(D, nn[i]);
+        if (!occ_of(v)) continue;
+        if (cov_of(v) == WALLIND) {
+            nw++;
+            continue;
+        }
+        if (rec_lists(D, D.ind[gidx(D, nn[i])], site)) {   // reciprocal bonds only (:232-239)
+            int s = sp_of(v);
+            nsi += s == 1;
+            nc += s == 2;
+            nb += s == 3;
+        }
+    }
+    int tot = nsi + nc + nb + nw;
+    if (tot != coor) {                                      // :293-298
+        set_err(D, E_INVARIANT, site.x, site.y, site.z);
+        ev = EV_NONE;
+        rate = 0.f;
+        return;
+    }
+    if (tot > 3) {
+        ev = EV_NONE;
+        rate = 0.f;
+    } else if (tot == 0) {
+        ev = EV_ISO;
+        rate = 0.f;
+    } else {
+        int s = nsic >= 1 && nsic <= 3 ? nsic : 1;
+        ev = EV_EVAP;
+        rate = (float)D.pe[(s - 1) * 64 + (nsi + nw) * 16 + nc * 4 + nb];
+    }
+}
+
+// ---- list bookkeeping (AddMC / EraseMC and friends, Add.f, Erase.f) ----
+__device__ void list_site(const Dev &D, const Ctx &c, int r)
+{
+    if (c.tile < 0) return;               // replay: the lists are rebuilt before a run
+    Rec &R = D.rec[r];
+    if (R.flags & F_LISTED) return;
+    R.flags |= F_LISTED;
+    int t = tile_of(D, R.x, R.y);
+    int k = atomicAdd(&D.tl_n[t], 1);
+    if (k >= LCAP) {
+        set_err(D, E_CAPACITY, t, k, 0);
+        return;
+    }
+    D.tl[(int64_t)t * LCAP + k] = r;
+}
+
+__device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
+{
+    if (r <= 0) {
+        set_err(D, E_INVARIANT, -1, r, 0);
+        return;
+    }
+    Rec &R = D.rec[r];
+    c.dmc += (ev != 0) - (R.ev != 0);
+    R.ev = ev;
+    R.rate = rate;
+    if (ev) list_site(D, c, r);
+}
+
+__device__ int alloc_rec(const Dev &D, const Ctx &c)
+{
+    int t = c.tile < 0 ? 0 : c.tile;
+    int n = D.fr_n[t];
+    if (n > 0) {
+        D.fr_n[t] = n - 1;
+        return D.fr[(int64_t)t * FCAP + n - 1];
+    }
+    int r = atomicAdd(D.top, 1);
+    if (r >= D.rcap) {
+        set_err(D, E_CAPACITY, -2, r, 0);
+        return 0;
+    }
+    return r;
+}
+
+__device__ void free_rec(const Dev &D, const Ctx &c, int r)
+{
+    if (c.tile < 0) {                     // replay: reusable at once (no lists)
+        int n = D.fr_n[0];
+        if (n < FCAP) {
+            D.fr[n] = r;
+            D.fr_n[0] = n + 1;
+        }
+        return;
+    }
+    int n = D.fp_n[c.tile];
+    if (n < FCAP) {
+        D.fp[(int64_t)c.tile * FCAP + n] = r;
+        D.fp_n[c.tile] = n + 1;
+    }
+}
+
+// a new listed site (AddMC of a coor-1 empty site, Add.f:24-52)
+__device__ void new_site(const Dev &D, Ctx &c, P3 p, const P3 nn[4], uint8_t ev, float rate)
+{
+    int r = alloc_rec(D, c);
+    if (r <= 0) return;
+    Rec &R = D.rec[r];
+    R.x = (int16_t)p.x;
+    R.y = (int16_t)p.y;
+    R.z = (int16_t)p.z;
+    for (int i = 0; i < 4; i++) put_nn(R, i, nn[i]);
+    R.ev = EV_NONE;
+    R.flags = 0;
+    R.rate = 0.f;
+    D.ind[gidx(D, p)] = r;
+    set_event(D, c, r, ev, rate);
+}
+
+// the site leaves every list (EraseMC with LattInd = 0, Erase.f:24-76)
+__device__ void drop_site(const Dev &D, Ctx &c, P3 p)
+{
+    int64_t g = gidx(D, p);
+    int r = D.ind[g];
+    if (r <= 0) {
+        set_err(D, E_INVARIANT, p.x, p.y, p.z);
+        return;
+    }
+    D.ind[g] = 0;
+    Rec &R = D.rec[r];
+    c.dmc -= R.ev != 0;
+    R.ev = EV_NONE;
+    R.flags = 0;
+    R.rate = 0.f;
+    R.x = -1;
+    free_rec(D, c, r);
+}
+
+// ---- geometry: FIND_SN.f:26-84, FIND_NN.f:25-77, IF_Arm_Choice.f:21-56 ----
+// FP64 as the reference, each product and sum rounded on its own (no fused
+// multiply-add), NINT to the grid.
+__device__ void find_sn(const Dev &D, P3 site, P3 sitec, const P3 sn_in[3], P3 zig[3], P3 arm[3])
+{
+    const int lx = D.lx, ly = D.ly;
+    P3 sn[3] = {sn_in[0], sn_in[1], sn_in[2]};
+    if (abs(site.x - sitec.x) > lx / 2) sitec.x += isign(lx, site.x - sitec.x);
+    if (abs(site.y - sitec.y) > ly / 2) sitec.y += isign(ly, site.y - sitec.y);
+    for (int i = 0; i < 3; i++) {
+        if (abs(site.x - sn[i].x) > lx / 2) sn[i].x += isign(lx, site.x - sn[i].x);
+        if (abs(site.y - sn[i].y) > ly / 2) sn[i].y += isign(ly, site.y - sn[i].y);
+    }
+    const int s3[3] = {site.x, site.y, site.z}, c3[3] = {sitec.x, sitec.y, sitec.z};
+    double cent[3], ax[3];
+    for (int k = 0; k < 3; k++) {
+        cent[k] = 0.5 * ((double)c3[k] + (double)s3[k]);     // exact
+        ax[k] = (double)s3[k] - (double)c3[k];
+    }
+    double snorm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);   // integer squares: exact sum
+    for (int k = 0; k < 3; k++) ax[k] = __ddiv_rn(ax[k], snorm);
+    for (int i = 0; i < 3; i++) {
+        const int n3[3] = {sn[i].x, sn[i].y, sn[i].z};
+        int z3[3], a3[3];
+        for (int k = 0; k < 3; k++) {
+            z3[k] = nint(2.0 * cent[k] - (double)n3[k]);          // exact
+            a3[k] = nint(__dadd_rn((double)n3[k], __dmul_rn(D.shift, ax[k])));
+        }
+        zig[i] = P3{z3[0], z3[1], z3[2]};
+        arm[i] = P3{a3[0], a3[1], a3[2]};
+        if (zig[i].x >= lx) zig[i].x -= lx;
+        if (zig[i].x < 0) zig[i].x += lx;
+        if (zig[i].y >= ly) zig[i].y -= ly;
+        if (zig[i].y < 0) zig[i].y += ly;
+        if (arm[i].x >= lx) arm[i].x -= lx;
+        if (arm[i].x < 0) arm[i].x += lx;
+        if (arm[i].y >= ly) arm[i].y -= ly;
+        if (arm[i].y < 0) arm[i].y += ly;
+    }
+}
+
+__device__ void find_nn(const Dev &D, P3 s1, P3 s2, P3 sc, P3 out[2])
+{
+    const int lx = D.lx, ly = D.ly;
+    if (abs(sc.x - s1.x) > lx / 2) s1.x += isign(lx, sc.x - s1.x);
+    if (abs(sc.y - s1.y) > ly / 2) s1.y += isign(ly, sc.y - s1.y);
+    if (abs(sc.x - s2.x) > lx / 2) s2.x += isign(lx, sc.x - s2.x);
+    if (abs(sc.y - s2.y) > ly / 2) s2.y += isign(ly, sc.y - s2.y);
+    const int c3[3] = {sc.x, sc.y, sc.z}, t3[3] = {s2.x, s2.y, s2.z};
+    double ax[3] = {(double)(sc.x - s1.x), (double)(sc.y - s1.y), (double)(sc.z - s1.z)};
+    double snorm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    for (int k = 0; k < 3; k++) ax[k] = __ddiv_rn(ax[k], snorm);
+    for (int irot = 0; irot < 2; irot++) {
+        const double cth = D.cth[irot], sth = D.sth[irot];
+        const double omc = __dsub_rn(1.0, cth);
+        double rot[3][3];
+        for (int i = 0; i < 3; i++) rot[i][i] = __dadd_rn(__dmul_rn(__dmul_rn(ax[i], ax[i]), omc), cth);
+        rot[1][0] = __dsub_rn(__dmul_rn(__dmul_rn(ax[0], ax[1]), omc), __dmul_rn(ax[2], sth));
+        rot[0][1] = __dadd_rn(__dmul_rn(__dmul_rn(ax[0], ax[1]), omc), __dmul_rn(ax[2], sth));
+        rot[2][0] = __dadd_rn(__dmul_rn(__dmul_rn(ax[0], ax[2]), omc), __dmul_rn(ax[1], sth));
+        rot[0][2] = __dsub_rn(__dmul_rn(__dmul_rn(ax[0], ax[2]), omc), __dmul_rn(ax[1], sth));
+        rot[2][1] = __dsub_rn(__dmul_rn(__dmul_rn(ax[1], ax[2]), omc), __dmul_rn(ax[0], sth));
+        rot[1][2] = __dadd_rn(__dmul_rn(__dmul_rn(ax[1], ax[2]), omc), __dmul_rn(ax[0], sth));
+        int o3[3];
+        for (int k = 0; k < 3; k++) {
+            double r = 0.0;
+            for (int l = 0; l < 3; l++) r = __dadd_rn(r, __dmul_rn(rot[l][k], (double)(t3[l] - c3[l])));
+            o3[k] = nint(r) + c3[k];
+        }
+        P3 p{o3[0], o3[1], o3[2]};
+        if (p.x >= lx) p.x -= lx;
+        if (p.x < 0) p.x += lx;
+        if (p.y >= ly) p.y -= ly;
+        if (p.y < 0) p.y += ly;
+        out[irot] = p;
+    }
+}
+
+__device__ float tie_uniform(const Dev &D, Ctx &c)
+{
+    U4 r = philox4x32_10(U4{c.nties++, (uint32_t)c.tile, c.key2, c.key3}, D.k0 ^ 0x5bd1e995u, D.k1);
+    return u01(r.x);
+}
+
+// 1 for arm-chair (hexagonal), 0 for zig-zag (cubic)
+__device__ int arm_choice(const Dev &D, Ctx &c, const P3 zig[3], const P3 arm[3])
+{
+    int ca = 0, cz = 0;
+    for (int i = 0; i < 3; i++) {
+        ca += coor_of(cw(D, arm[i]));
+        cz += coor_of(cw(D, zig[i]));
+    }
+    int choice;
+    if (cz > ca) choice = 0;
+    else if (cz == ca) {
+        if (c.tile < 0) return c.forced_arm;
+        choice = (double)tie_uniform(D, c) <= D.pzig ? 0 : 1;
+    } else choice = 1;
+    if (c.tile < 0 && choice != c.forced_arm) set_err(D, E_ARM, ca, cz, c.forced_arm);
+    return choice;
+}
+
+// ---- events ----
+// Deposition of species sp on the empty site (deposition.f:24-251)
+__device__ void deposition(const Dev &D, Ctx &c, P3 site, int sp)
+{
+    const int64_t gs = gidx(D, site);
+    const int rs = D.ind[gs];
+    if (rs <= 0) {
+        set_err(D, E_INVARIANT, site.x, site.y, site.z);
+        return;
+    }
+    uint32_t w = D.coo[gs];
+    int coor = coor_of(w);
+    const int coor_old = coor;
+    w = (w & ~(7u << 27)) | B_OCC | ((uint32_t)sp << 27);
+    D.coo[gs] = w;
+    Rec &R = D.rec[rs];
+    if (coor == 1) {                                       // :49-74
+        P3 sitec = nn_at(R, 0);
+        const Rec &Rc = D.rec[D.ind[gidx(D, sitec)]];
+        P3 sn[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        int j = 0;
+        for (int i = 0; i < 4; i++) {
+            P3 q = nn_at(Rc, i);
+            if (!same(q, site)) {
+                if (j < 3) sn[j] = q;
+                j++;
+            }
+        }
+        P3 zig[3], arm[3];
+        find_sn(D, site, sitec, sn, zig, arm);
+        int a = arm_choice(D, c, zig, arm);
+        for (int i = 0; i < 3; i++) put_nn(R, i + 1, a ? arm[i] : zig[i]);
+    }
+    P3 nextn[4];
+    load_nn(R, nextn);
+    for (int i = 0; i < 4; i++) {                          // :78-235
+        const P3 n = nextn[i];
+        const int64_t gn = gidx(D, n);
+        const uint32_t vn = D.coo[gn];
+        const int rn = D.ind[gn];
+        int coornn = coor_of(vn);
+        const int covind = cov_of(vn);
+        uint8_t ev;
+        float rate;
+        if (!occ_of(vn)) {
+            if (coornn == 0) {                             // :86-99
+                D.coo[gn] = with_coor(vn, 1);
+                P3 nnn[4] = {site, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                get_prob(D, 0, 0, 1, n, nnn, ev, rate);
+                if (ev) new_site(D, c, n, nnn, ev, rate);
+            } else if (coornn == 1) {                      // :100-160
+                if (rn <= 0) {
+                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                    return;
+                }
+                Rec &N = D.rec[rn];
+                P3 nnn[4];
+                load_nn(N, nnn);
+                int dx = abs(nnn[0].x - site.x);
+                if (D.lx - dx < dx) dx = D.lx - dx;
+                int dy = abs(nnn[0].y - site.y);
+                if (D.ly - dy < dy) dy = D.ly - dy;
+                int dz = nnn[0].z - site.z;
+                if (dx * dx + dy * dy + dz * dz == 72) {
+                    coornn = 2;
+                    nnn[1] = site;
+                    P3 ns[2];
+                    find_nn(D, nnn[0], nnn[1], n, ns);
+                    for (int k = 2; k < 4; k++) {
+                        nnn[k] = ns[k - 2];
+                        uint32_t v = cw(D, nnn[k]);
+                        if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND &&
+                            rec_lists(D, D.ind[gidx(D, nnn[k])], n))
+                            coornn++;
+                    }
+                    D.coo[gn] = with_coor(vn, coornn);
+                    for (int k = 0; k < 4; k++) put_nn(N, k, nnn[k]);
+                    get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+                    set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddVoid
+                }
+            } else if (coornn == 2 || coornn == 3) {       // :161-191
+                if (rn <= 0) {
+                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                    return;
+                }
+                P3 nnn[4];
+                load_nn(D.rec[rn], nnn);
+                if (in_list(nnn, site)) {
+                    coornn++;
+                    D.coo[gn] = with_coor(vn, coornn);
+                    get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+                    set_event(D, c, rn, ev, rate);
+                }
+            }
+        } else if (covind != WALLIND) {                    // :192-230
+            if (covind != 0) {
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return;
+            }
+            if (coornn <= 3) {
+                if (rn <= 0) {
+                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                    return;
+                }
+                P3 nnn[4];
+                load_nn(D.rec[rn], nnn);
+                if (in_list(nnn, site)) {
+                    coornn++;
+                    D.coo[gn] = with_coor(vn, coornn);
+                    get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
+                    set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddBulk
+                    if (coor_old == 1 && i >= 1) coor++;
+                }
+            }
+        } else {
+            coor++;
+        }
+    }
+    if (coor != coor_old) D.coo[gs] = with_coor(D.coo[gs], coor);   // :236-250
+    uint8_t ev;
+    float rate;
+    get_prob(D, 1, sp, coor, site, nextn, ev, rate);
+    set_event(D, c, D.ind[gs], ev, rate);
+}
+
+// The neighbour of `site` whose list holds `site`, among the occupied
+// non-wall sites of nn (Evaporation.f:87-104,238-253); NBuff keeps the last.
+__device__ void prune_to_buffer(const Dev &D, Ctx &c, Rec &S, P3 site, bool &got)
+{
+    for (int j = 0; j < 4; j++) {
+        P3 q = nn_at(S, j);
+        uint32_t v = cw(D, q);
+        if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND && rec_lists(D, D.ind[gidx(D, q)], site)) {
+            c.nbuff = q;
+            got = true;
+        }
+        put_nn(S, j, P3{0, 0, 0});
+    }
+    put_nn(S, 0, c.nbuff);
+}
+
+// Evaporation of the atom at site (Evaporation.f:25-262)
+__device__ void evaporation(const Dev &D, Ctx &c, P3 site)
+{
+    const int64_t gs = gidx(D, site);
+    const int rs = D.ind[gs];
+    if (rs <= 0) {
+        set_err(D, E_INVARIANT, site.x, site.y, site.z);
+        return;
+    }
+    uint32_t w = D.coo[gs];
+    int coor = coor_of(w);
+    D.coo[gs] = w & ~(B_OCC | (7u << 27));
+    P3 nextn[4];
+    load_nn(D.rec[rs], nextn);
+    for (int i = 0; i < 4; i++) {
+        const P3 n = nextn[i];
+        const int64_t gn = gidx(D, n);
+        const uint32_t vn = D.coo[gn];
+        const int rn = D.ind[gn];
+        int coornn = coor_of(vn);
+        const int covind = cov_of(vn);
+        uint8_t ev;
+        float rate;
+        if (!occ_of(vn)) {
+            if (coornn < 1 || coornn > 4) continue;
+            if (rn <= 0) {                                 // a coordinated empty site is always listed
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return;
+            }
+            P3 nnn[4];
+            load_nn(D.rec[rn], nnn);
+            if (!in_list(nnn, site)) continue;
+            if (coornn == 1) {                             // :51-68
+                drop_site(D, c, n);
+                D.coo[gn] = 0;
+            } else if (coornn == 2) {                      // :69-123
+                D.coo[gn] = with_coor(vn, 1);
+                bool got = false;
+                prune_to_buffer(D, c, D.rec[rn], n, got);
+                if (!got && c.tile >= 0) set_err(D, E_NBUFF, n.x, n.y, n.z);
+                get_prob(D, 0, 0, 1, n, nnn, ev, rate);   // the list as it was before pruning
+                set_event(D, c, rn, ev, rate);
+            } else {                                       // :124-164 (coor 3 -> 2, void -> MC)
+                coornn--;
+                D.coo[gn] = with_coor(vn, coornn);
+                get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+                set_event(D, c, rn, ev, rate);
+            }
+        } else if (covind != WALLIND) {                    // :166-210
+            if (covind != 0 || rn <= 0) {
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return;
+            }
+            P3 nnn[4];
+            load_nn(D.rec[rn], nnn);
+            if (in_list(nnn, site)) {
+                coornn--;
+                D.coo[gn] = with_coor(vn, coornn);
+                get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
+                set_event(D, c, rn, ev, rate);             // bulk -> MC when coor was 4
+            }
+        } else {
+            coor--;
+        }
+    }
+    D.coo[gs] = with_coor(D.coo[gs], coor);                // :216-261
+    if (coor == 0) {
+        drop_site(D, c, site);
+        return;
+    }
+    uint8_t ev;
+    float rate;
+    get_prob(D, 0, 0, coor, site, nextn, ev, rate);
+    Rec &S = D.rec[D.ind[gs]];
+    if (coor == 1) {
+        bool got = false;
+        prune_to_buffer(D, c, S, site, got);
+        if (!got && c.tile >= 0) set_err(D, E_NBUFF, site.x, site.y, site.z);
+    }
+    set_event(D, c, D.ind[gs], ev, rate);
+}
+
+// Apply event code ev of record r: the deposited species is drawn from the
+// PTransD shares of the site's coordination with u (Get_Prob.f:159-176);
+// an unsupported coor-1 site deposits species 1 (:181-184).
+__device__ void apply(const Dev &D, Ctx &c, int r, float u)
+{
+    const Rec &R = D.rec[r];
+    P3 site{R.x, R.y, R.z};
+    if (R.ev == EV_EVAP || R.ev == EV_ISO) {
+        evaporation(D, c, site);
+        return;
+    }
+    int sp = 1;
+    if (R.ev == EV_DEP) {
+        int co = coor_of(cw(D, site));
+        co = co < 1 ? 1 : (co > 3 ? 3 : co);
+        double p1 = pd_of(D, 1, co), p2 = pd_of(D, 2, co), p3 = pd_of(D, 3, co);
+        double pc = (double)u * (p1 + p2 + p3);
+        sp = pc <= p1 ? 1 : (pc > p1 + p2 ? 3 : 2);
+    }
+    deposition(D, c, site, sp);
+}
+
+// ---- kernels ----
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// One colour phase: every tile of the colour runs from the window's start to
+// its end (one warp per tile).
+__global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
+{
+    const int lane = threadIdx.x & 31;
+    const int wid = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    const int hx = D.ntx / 2, hy = D.nty / 2;
+    if (wid >= hx * hy) return;
+    const int ti = 2 * (wid % hx) + (colour & 1), tj = 2 * (wid / hx) + (colour >> 1);
+    const int t = tj * D.ntx + ti;
+    if (*(volatile int32_t *)D.err || *(volatile int32_t *)D.stop) return;
+    int32_t *list = D.tl + (int64_t)t * LCAP;
+    // records freed in the tile's last phase become reusable
+    if (lane == 0) {
+        int np = D.fp_n[t], nr = D.fr_n[t];
+        for (int k = 0; k < np && nr < FCAP; k++) D.fr[(int64_t)t * FCAP + nr++] = D.fp[(int64_t)t * FCAP + k];
+        D.fr_n[t] = nr;
+        D.fp_n[t] = 0;
+    }
+    // compact the list: keep each record once if it is still in this tile and
+    // still has an event; a dropped record without an event may be listed again
+    int n = min(D.tl_n[t], LCAP);
+    int out = 0;
+    for (int base = 0; base < n; base += 32) {
+        int i = base + lane;
+        int r = i < n ? list[i] : 0;
+        bool keep = false;
+        if (r > 0) {
+            Rec &R = D.rec[r];
+            bool mine = R.x >= 0 && tile_of(D, R.x, R.y) == t;
+            if (mine && R.ev == EV_NONE) R.flags &= (uint8_t)~F_LISTED;
+            keep = mine && R.ev != EV_NONE && !(R.flags & F_SEEN);
+        }
+        unsigned grp = __match_any_sync(FULL, r);
+        keep = keep && lane == __ffs(grp) - 1;
+        unsigned km = __ballot_sync(FULL, keep);
+        __syncwarp();
+        if (keep) {
+            D.rec[r].flags |= F_SEEN;
+            list[out + __popc(km & lanemask_lt())] = r;
+        }
+        out += __popc(km);
+        __syncwarp();
+    }
+    for (int i = lane; i < out; i += 32) D.rec[list[i]].flags &= (uint8_t)~F_SEEN;
+    if (lane == 0) D.tl_n[t] = out;
+    __syncwarp();
+
+    Ctx c;
+    c.tile = t;
+    c.nbuff = P3{0, 0, 0};
+    c.forced_arm = 0;
+    c.key2 = window;
+    c.key3 = 0x7a000000u | (uint32_t)colour;
+    c.nties = 0;
+    c.dmc = 0;
+    float rem = tau;
+    uint32_t nev = 0, ndraw = 0;
+    for (;;) {
+        const int len = min(*(volatile int32_t *)&D.tl_n[t], LCAP);
+        float s = 0.f;
+        int niso = 0;
+        for (int i = lane; i < len; i += 32) {
+            const Rec &R = D.rec[list[i]];
+            if (R.ev == EV_NONE || R.x < 0) continue;
+            if (R.ev == EV_ISO) niso++;
+            else s += R.rate;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s += __shfl_xor_sync(FULL, s, o);
+            niso += __shfl_xor_sync(FULL, niso, o);
+        }
+        // isolated atoms: 1e5 x the total rate (Get_Prob.f:305), the tile's here
+        const float riso = niso ? (float)niso * 1.0e5f * fmaxf(s, 1.0e-30f) : 0.f;
+        const float rtot = s + riso;
+        if (!(rtot > 0.f)) break;
+        U4 rnd = philox4x32_10(U4{ndraw++, (uint32_t)t, window, 0x51000000u | (uint32_t)colour}, D.k0, D.k1);
+        float dt = -__logf(u01(rnd.x)) / rtot;
+        if (dt > rem) break;
+        rem -= dt;
+        float target = u01(rnd.y) * rtot;
+        int pick = -1;
+        if (target >= s && niso > 0) {
+            // the k-th isolated atom of the list
+            int k = min((int)(u01(rnd.z) * (float)niso), niso - 1);
+            for (int base = 0; base < len && pick < 0; base += 32) {
+                int i = base + lane;
+                bool hit = false;
+                if (i < len) {
+                    const Rec &R = D.rec[list[i]];
+                    hit = R.ev == EV_ISO && R.x >= 0;
+                }
+                unsigned m = __ballot_sync(FULL, hit);
+                if (k < __popc(m)) {
+                    unsigned sel = __ballot_sync(FULL, hit && __popc(m & lanemask_lt()) == k);
+                    pick = list[base + __ffs(sel) - 1];
+                }
+                k -= __popc(m);
+            }
+        } else {
+            // cumulative rates in list order: the first entry past the target
+            float run = 0.f;
+            int last = -1;
+            for (int base = 0; base < len && pick < 0; base += 32) {
+                int i = base + lane;
+                float v = 0.f;
+                if (i < len) {
+                    const Rec &R = D.rec[list[i]];
+                    if (R.ev != EV_NONE && R.ev != EV_ISO && R.x >= 0) v = R.rate;
+                }
+                float cum = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    float y = __shfl_up_sync(FULL, cum, o);
+                    if (lane >= o) cum += y;
+                }
+                cum += run;
+                unsigned m = __ballot_sync(FULL, v > 0.f && cum > target);
+                unsigned nz = __ballot_sync(FULL, v > 0.f);
+                if (nz) last = list[base + 31 - __clz(nz)];
+                if (m) pick = list[base + __ffs(m) - 1];
+                run = __shfl_sync(FULL, cum, 31);
+            }
+            if (pick < 0) pick = last;       // rounding at the top end
+        }
+        if (pick <= 0) break;
+        if (lane == 0) apply(D, c, pick, u01(rnd.w));
+        nev++;
+        __syncwarp();
+        if (*(volatile int32_t *)D.err) break;
+    }
+    if (lane == 0) {
+        if (nev) atomicAdd(D.events, (unsigned long long)nev);
+        if (c.dmc) atomicAdd(D.nmc, c.dmc);
+    }
+}
+
+// the replay: events in order on one thread
+__global__ void k_replay(Dev D, const mks_event *ev, long long n, long long *done)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Ctx c;
+    c.tile = -1;
+    c.nbuff = P3{0, 0, 0};
+    c.forced_arm = 0;
+    c.key2 = c.key3 = 0;
+    c.nties = 0;
+    c.dmc = 0;
+    long long k = 0;
+    for (; k < n; k++) {
+        const mks_event e = ev[k];
+        P3 s{e.x, e.y, e.z};
+        if (s.x < 0 || s.x >= D.lx || s.y < 0 || s.y >= D.ly || s.z < 0 || s.z > D.lz) {
+            set_err(D, E_NOTAPPLICABLE, s.x, s.y, s.z);
+            break;
+        }
+        const int64_t g = gidx(D, s);
+        const uint32_t v = D.coo[g];
+        const int r = D.ind[g];
+        const uint8_t code = r > 0 ? D.rec[r].ev : EV_NONE;
+        c.forced_arm = e.arm ? 1 : 0;
+        if (e.itrans >= 1 && e.itrans <= 3) {
+            if (occ_of(v) || (code != EV_DEP && code != EV_DUMMY) || (code == EV_DUMMY && e.itrans != 1)) {
+                set_err(D, E_NOTAPPLICABLE, s.x, s.y, s.z);
+                break;
+            }
+            deposition(D, c, s, e.itrans);
+        } else if (e.itrans == 4) {
+            if (!occ_of(v) || cov_of(v) == WALLIND || (code != EV_EVAP && code != EV_ISO)) {
+                set_err(D, E_NOTAPPLICABLE, s.x, s.y, s.z);
+                break;
+            }
+            evaporation(D, c, s);
+        } else {
+            set_err(D, E_NOTAPPLICABLE, s.x, s.y, s.z);
+            break;
+        }
+        if (*(volatile int32_t *)D.err) {
+            k++;
+            break;
+        }
+    }
+    *done = k;
+    atomicAdd(D.nmc, c.dmc);
+}
+
+// rates of every record from the current lattice (Get_Prob_Ini.f:23-161: an
+// empty coor-1 site marked ini keeps the init-time dummy rate 1e-6, :102-104)
+__global__ void k_rate_all(Dev D, const uint8_t *ini, int first, int last)
+{
+    for (int r = first + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
+        Rec &R = D.rec[r];
+        if (R.x < 0) continue;
+        P3 s{R.x, R.y, R.z};
+        uint32_t v = cw(D, s);
+        P3 nn[4];
+        load_nn(R, nn);
+        uint8_t ev;
+        float rate;
+        get_prob(D, occ_of(v), sp_of(v), coor_of(v), s, nn, ev, rate);
+        if (ev == EV_DUMMY && ini && ini[r]) rate = 1.e-6f;
+        R.ev = ev;
+        R.rate = rate;
+        R.flags = 0;
+    }
+}
+
+// tile lists from scratch, and the count of sites with an event
+__global__ void k_rebuild(Dev D, int last)
+{
+    for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
+        Rec &R = D.rec[r];
+        R.flags = 0;
+        if (R.x < 0 || R.ev == EV_NONE) continue;
+        atomicAdd(D.nmc, 1);
+        R.flags = F_LISTED;
+        int t = tile_of(D, R.x, R.y);
+        int k = atomicAdd(&D.tl_n[t], 1);
+        if (k >= LCAP) {
+            set_err(D, E_CAPACITY, t, k, 1);
+            continue;
+        }
+        D.tl[(int64_t)t * LCAP + k] = r;
+    }
+}
+
+__global__ void k_stop_check(Dev D)
+{
+    if (threadIdx.x == 0 && *D.nmc <= 20) *D.stop = 1;      // main.f:307-310
+}
+
+// compact lattice -> LattCoo words and records.  Pass 1 counts the listed
+// sites of each (z1, b) row; pass 2 writes them with ids from the row offsets.
+__device__ __forceinline__ bool compact_site(int a, int b, int z1) { return ((a + b + (z1 >> 1)) & 1) == 0; }
+__device__ __forceinline__ bool listed_byte(uint8_t s) { return s != 0 && s != 0x80 && ((s & 3) || ((s >> 2) & 7)); }
+
+__global__ void k_count_rows(const uint8_t *st, int NA, int NB, int NZ, int pitch, int lz, int32_t *rowcnt)
+{
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= NZ * NB) return;
+    int z1 = row / NB, b = row % NB, k = 0;
+    if (3 * z1 <= lz)
+        for (int a = 0; a < NA; a++)
+            if (compact_site(a, b, z1) && listed_byte(st[(int64_t)row * pitch + a])) k++;
+    rowcnt[row] = k;
+}
+
+__global__ void k_expand(Dev D, const uint8_t *st, int NA, int NB, int NZ, int pitch, const int32_t *rowoff,
+                         uint8_t *ini)
+{
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= NZ * NB) return;
+    const int z1 = row / NB, b = row % NB;
+    const int z = 3 * z1;
+    if (z > D.lz) return;
+    int r = rowoff[row];
+    const int zp = z1 & 1;
+    for (int a = 0; a < NA; a++) {
+        if (!compact_site(a, b, z1)) continue;
+        uint8_t s = st[(int64_t)row * pitch + a];
+        if (s == 0 || s == 0x80) continue;
+        P3 p{3 * (2 * a + zp), 3 * (2 * b + zp), z};
+        int sp = s & 3;
+        int co = (s >> 2) & (7 ^ (s & 4));              // field 5 of an init-time dummy reads 1
+        D.coo[gidx(D, p)] = ((uint32_t)co << 24) | (sp ? B_OCC : 0u) | ((uint32_t)sp << 27);
+        if (!listed_byte(s)) continue;
+        const int fd = (s >> 5) & 3;
+        Rec &R = D.rec[r];
+        R.x = (int16_t)p.x;
+        R.y = (int16_t)p.y;
+        R.z = (int16_t)p.z;
+        // NextN: the four bonds (JumpDia order, defsystem.f:104-105) from the
+        // first list entry on, as the initializers list them (SetSi.f:52-57)
+        for (int i = 0; i < 4; i++) {
+            int d = (fd + i) & 3;
+            int da = zp - (d >> 1), db = zp - ((d ^ (d >> 1)) & 1), dz = ((d ^ zp) & 1) ? -1 : 1;
+            int aa = a + da, bb = b + db, kk = z1 + dz;
+            P3 q{3 * (2 * aa + (kk & 1)), 3 * (2 * bb + (kk & 1)), 3 * kk};
+            if (q.x < 0) q.x += D.lx;
+            if (q.x >= D.lx) q.x -= D.lx;
+            if (q.y < 0) q.y += D.ly;
+            if (q.y >= D.ly) q.y -= D.ly;
+            put_nn(R, i, q);
+        }
+        R.ev = EV_NONE;
+        R.flags = 0;
+        R.rate = 0.f;
+        ini[r] = (s & 0x9C) == 0x94;                    // dummy flag with coordination field 5
+        D.ind[gidx(D, p)] = r;
+        r++;
+    }
+}
+
+__global__ void k_wall_planes(Dev D, const int32_t *wall_plane)
+{
+    int64_t plane = (int64_t)D.lx * D.ly;
+    int64_t nplanes = D.lz + 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < plane * nplanes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int z = (int)(i / plane);
+        if (wall_plane[z]) D.coo[(int64_t)(z + ZG) * plane + (i % plane)] = B_OCC | WALLIND;
+    }
+}
+
+// per compact layer: sites, wall sites
+__global__ void k_layer_walls(const uint8_t *st, int NA, int NB, int NZ, int pitch, int32_t *cnt)
+{
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= NZ * NB) return;
+    int z1 = row / NB, b = row % NB, ns = 0, nw = 0;
+    for (int a = 0; a < NA; a++)
+        if (compact_site(a, b, z1)) {
+            ns++;
+            nw += st[(int64_t)row * pitch + a] == 0x80;
+        }
+    atomicAdd(&cnt[2 * z1], ns);
+    atomicAdd(&cnt[2 * z1 + 1], nw);
+}
+
+__global__ void k_load_records(Dev D, const int32_t *xyz, const int32_t *nn, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        Rec &R = D.rec[i + 1];
+        P3 p{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+        R.x = (int16_t)p.x;
+        R.y = (int16_t)p.y;
+        R.z = (int16_t)p.z;
+        for (int k = 0; k < 4; k++) put_nn(R, k, P3{nn[12 * i + 3 * k], nn[12 * i + 3 * k + 1], nn[12 * i + 3 * k + 2]});
+        R.ev = EV_NONE;
+        R.flags = 0;
+        R.rate = 0.f;
+        D.ind[gidx(D, p)] = (int32_t)(i + 1);
+    }
+}
+
+__global__ void k_gather(Dev D, int last, int32_t *word)
+{
+    for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
+        const Rec &R = D.rec[r];
+        word[r] = R.x >= 0 ? (int32_t)cw(D, P3{R.x, R.y, R.z}) : 0;
+    }
+}
+
+// the reference's diamond-site test (SetSi.f:52-57)
+__device__ __forceinline__ bool dia_site(int x, int y, int z)
+{
+    if (x % 3 || y % 3 || z % 3) return false;
+    int x1 = x / 3, y1 = y / 3, z1 = z / 3;
+    if ((x1 & 1) != (y1 & 1) || (x1 & 1) != (z1 & 1)) return false;
+    int m = (x1 + y1 + z1) & 3;
+    return m == 0 || m == 3;
+}
+
+// counters: 0 atoms, 1 undercoordinated, 2 with an event, 3 voids, 4..6
+// species, 7 non-epitaxial bulk; rate sums [0] non-isolated, [1] isolated
+// count; column tops (6 x 6 grid-unit columns)
+__global__ void k_observe(Dev D, int last, unsigned long long *cnt, double *rsum, int32_t *coltop)
+{
+    __shared__ unsigned long long sc[8];
+    __shared__ double sr[2];
+    if (threadIdx.x < 8) sc[threadIdx.x] = 0;
+    if (threadIdx.x < 2) sr[threadIdx.x] = 0.0;
+    __syncthreads();
+    const int ncx = D.lx / 6;
+    for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
+        const Rec &R = D.rec[r];
+        if (R.x < 0) continue;
+        uint32_t v = cw(D, P3{R.x, R.y, R.z});
+        if (R.ev != EV_NONE) {
+            atomicAdd(&sc[2], 1ull);
+            if (R.ev == EV_ISO) atomicAdd(&sr[1], 1.0);
+            else atomicAdd(&sr[0], (double)R.rate);
+        }
+        if (occ_of(v) && cov_of(v) != WALLIND) {
+            atomicAdd(&sc[0], 1ull);
+            int co = coor_of(v), s = sp_of(v);
+            if (co <= 3) atomicAdd(&sc[1], 1ull);
+            if (s >= 1 && s <= 3) atomicAdd(&sc[3 + s], 1ull);
+            if (co == 4 && R.z >= 0 && R.z < D.lz && !dia_site(R.x, R.y, R.z)) atomicAdd(&sc[7], 1ull);
+            atomicMax(&coltop[(R.y / 6) * ncx + R.x / 6], (int)R.z);
+        } else if (!occ_of(v) && coor_of(v) == 4) {
+            atomicAdd(&sc[3], 1ull);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) atomicAdd(&cnt[threadIdx.x], sc[threadIdx.x]);
+    if (threadIdx.x < 2) atomicAdd(&rsum[threadIdx.x], sr[threadIdx.x]);
+}
+
+int grid_for(int64_t n, int block = 256) { return (int)std::max<int64_t>(1, std::min<int64_t>(152 * 32, (n + block - 1) / block)); }
+
+}  // namespace
+
+struct State {
+    mks_config cfg{};
+    cudaStream_t stream = nullptr;
+    Dev D{};
+    int64_t ngrid = 0;
+    int nrec = 0;                 // records in use at load (ids 1..nrec)
+    double ptransE[3 * 4096] = {0}, ptransD[9] = {0};
+    bool rates = false, ready = false, lists_ok = false;
+    double time = 0.0;
+    int64_t window = 0, events = 0;
+    int32_t *d_scratch = nullptr;
+    double *d_tab = nullptr;
+    int stop_reason = 0;
+    int last_error = 0;
+};
+
+namespace {
+
+int ferr(std::string &err, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+}
+
+#define SK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return ferr(err, MKS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+int upload_tables(State *s, std::string &err)
+{
+    double tab[192 + 9];
+    for (int sp = 0; sp < 3; sp++)
+        for (int n1 = 0; n1 < 4; n1++)
+            for (int n2 = 0; n2 < 4; n2++)
+                for (int n3 = 0; n3 < 4; n3++)
+                    tab[sp * 64 + n1 * 16 + n2 * 4 + n3] = s->ptransE[sp * 4096 + n1 * 1024 + n2 * 256 + n3 * 64];
+    for (int k = 0; k < 9; k++) tab[192 + k] = s->ptransD[k];
+    SK(cudaMemcpyAsync(s->d_tab, tab, sizeof tab, cudaMemcpyHostToDevice, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+const char *derr_name(int code)
+{
+    switch (code) {
+    case E_INVARIANT: return "lattice state contradicts the model";
+    case E_CAPACITY: return "a tile list or the record pool is full";
+    case E_NOTAPPLICABLE: return "event not applicable to the lattice state";
+    case E_BOUNDS: return "grid point outside the box";
+    case E_NBUFF: return "no occupied neighbour lists the site (stale NBuff)";
+    case E_ARM: return "stacking choice differs from the trace";
+    default: return "device error";
+    }
+}
+
+int check_device(State *s, std::string &err, const char *what)
+{
+    int32_t e[4];
+    SK(cudaMemcpyAsync(e, s->D.err, sizeof e, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    if (!e[0]) return 0;
+    SK(cudaMemsetAsync(s->D.err, 0, 4 * sizeof(int32_t), s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    s->last_error = e[0];
+    int code = e[0] == E_CAPACITY ? MKS_ERR_CAPACITY : (e[0] == E_NOTAPPLICABLE || e[0] == E_ARM ? MKS_ERR_ARG
+                                                                                                 : MKS_ERR_INVARIANT);
+    return ferr(err, code, "%s: %s at (%d, %d, %d)", what, derr_name(e[0]), e[1], e[2], e[3]);
+}
+
+int rates_and_lists(State *s, const uint8_t *d_ini, std::string &err)
+{
+    int top = s->nrec + 1;
+    SK(cudaMemcpyAsync(s->D.top, &top, sizeof top, cudaMemcpyHostToDevice, s->stream));
+    if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, d_ini, 1, top);
+    SK(cudaGetLastError());
+    int ntiles = s->D.ntx * s->D.nty;
+    SK(cudaMemsetAsync(s->D.fr_n, 0, sizeof(int32_t) * ntiles, s->stream));
+    SK(cudaMemsetAsync(s->D.fp_n, 0, sizeof(int32_t) * ntiles, s->stream));
+    s->lists_ok = false;
+    s->ready = true;
+    return check_device(s, err, "rates");
+}
+
+int rebuild(State *s, std::string &err)
+{
+    int top = 0;
+    SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    int ntiles = s->D.ntx * s->D.nty;
+    SK(cudaMemsetAsync(s->D.tl_n, 0, sizeof(int32_t) * ntiles, s->stream));
+    SK(cudaMemsetAsync(s->D.nmc, 0, sizeof(int32_t), s->stream));
+    if (top > 1) k_rebuild<<<grid_for(top), 256, 0, s->stream>>>(s->D, top);
+    SK(cudaGetLastError());
+    s->lists_ok = true;
+    return check_device(s, err, "list build");
+}
+
+}  // namespace
+
+int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string &err)
+{
+    *out = nullptr;
+    const int lx = cfg.lenx, ly = cfg.leny, lz = cfg.lenz;
+    if (lx > 30000 || ly > 30000 || lz + ZG > 30000)
+        return ferr(err, MKS_ERR_ARG, "box %dx%dx%d: sides up to 30000 grid units with arm-chair stacking", lx, ly, lz);
+    if (cfg.ncov != 0) return ferr(err, MKS_ERR_UNSUPPORTED, "arm-chair stacking with a coverage species");
+    if (!(cfg.ptrans_zig >= 0.0 && cfg.ptrans_zig <= 1.0))
+        return ferr(err, MKS_ERR_ARG, "PtransZig=%g outside [0, 1]", cfg.ptrans_zig);
+    // an even number of tiles per side, each at least TWMIN wide
+    auto tiles = [](int L) {
+        for (int n = L / TWMIN; n >= 2; n--)
+            if (n % 2 == 0 && L % n == 0) return n;
+        return 0;
+    };
+    int ntx = tiles(lx), nty = tiles(ly);
+    if (!ntx || !nty)
+        return ferr(err, MKS_ERR_ARG, "box %dx%d cannot be cut into an even number of tiles >= %d grid units wide",
+                    lx, ly, TWMIN);
+    if (lx / ntx != ly / nty)
+        return ferr(err, MKS_ERR_ARG, "box %dx%d: square tiles need LenX/ntiles = LenY/ntiles", lx, ly);
+    State *s = new State;
+    s->cfg = cfg;
+    s->stream = stream;
+    Dev &D = s->D;
+    D.lx = lx;
+    D.ly = ly;
+    D.lz = lz;
+    D.ntx = ntx;
+    D.nty = nty;
+    D.tw = lx / ntx;
+    s->ngrid = (int64_t)(lz + 1 + 2 * ZG) * ly * lx;
+    int ntiles = ntx * nty;
+    // records: every diamond site of the box could be listed, and growth
+    // adds sites beyond them; 25 % headroom above the site count
+    int64_t sites = (int64_t)lx * ly * (lz + 1) / 216 * 8 / 4 + 1;
+    int64_t rcap = std::min<int64_t>(INT32_MAX - 1, sites + sites / 4 + (1 << 20));
+    D.rcap = (int)rcap;
+    const double pi = (double)3.14159265358979323f;   // FIND_NN.f:37: default-REAL literal
+    for (int irot = 1; irot <= 2; irot++) {
+        D.cth[irot - 1] = cos((double)(2 * irot) * pi / 3.0);
+        D.sth[irot - 1] = sin((double)(2 * irot) * pi / 3.0);
+    }
+    D.shift = (double)8.6602254037f;                  // FIND_SN.f:67
+    D.pzig = cfg.ptrans_zig;
+    D.k0 = (uint32_t)cfg.seed;
+    D.k1 = (uint32_t)(cfg.seed >> 32) ^ 0xa511e9b3u;
+    auto fail_free = [&](int rc) {
+        destroy(s);
+        return rc;
+    };
+#define SA(p, bytes)                                                                         \
+    do {                                                                                     \
+        cudaError_t e_ = cudaMalloc((void **)&(p), (bytes));                                 \
+        if (e_ != cudaSuccess) {                                                             \
+            ferr(err, MKS_ERR_CUDA, "cudaMalloc %lld bytes: %s", (long long)(bytes), cudaGetErrorString(e_)); \
+            return fail_free(MKS_ERR_CUDA);                                                  \
+        }                                                                                    \
+    } while (0)
+    SA(D.coo, sizeof(uint32_t) * s->ngrid);
+    SA(D.ind, sizeof(int32_t) * s->ngrid);
+    SA(D.rec, sizeof(Rec) * (size_t)rcap);
+    SA(D.tl, sizeof(int32_t) * (size_t)ntiles * LCAP);
+    SA(D.tl_n, sizeof(int32_t) * ntiles);
+    SA(D.fr, sizeof(int32_t) * (size_t)ntiles * FCAP);
+    SA(D.fr_n, sizeof(int32_t) * ntiles);
+    SA(D.fp, sizeof(int32_t) * (size_t)ntiles * FCAP);
+    SA(D.fp_n, sizeof(int32_t) * ntiles);
+    SA(s->d_scratch, sizeof(int32_t) * 16 + sizeof(unsigned long long) * 2);
+    SA(s->d_tab, sizeof(double) * (192 + 9));
+#undef SA
+    int32_t *sc = s->d_scratch;
+    D.err = sc;                 // 4
+    D.nmc = sc + 4;
+    D.stop = sc + 5;
+    D.top = sc + 6;
+    D.events = reinterpret_cast<unsigned long long *>(sc + 8);
+    D.pe = s->d_tab;
+    D.pd = s->d_tab + 192;
+    cudaError_t e = cudaMemsetAsync(s->d_scratch, 0, sizeof(int32_t) * 16 + sizeof(unsigned long long) * 2, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.coo, 0, sizeof(uint32_t) * s->ngrid, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.ind, 0, sizeof(int32_t) * s->ngrid, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.rec, 0, sizeof(Rec), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_tab, 0, sizeof(double) * (192 + 9), stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        ferr(err, MKS_ERR_CUDA, "clearing the lattice: %s", cudaGetErrorString(e));
+        return fail_free(MKS_ERR_CUDA);
+    }
+    *out = s;
+    return 0;
+}
+
+void destroy(State *s)
+{
+    if (!s) return;
+    Dev &D = s->D;
+    cudaFree(D.coo);
+    cudaFree(D.ind);
+    cudaFree(D.rec);
+    cudaFree(D.tl);
+    cudaFree(D.tl_n);
+    cudaFree(D.fr);
+    cudaFree(D.fr_n);
+    cudaFree(D.fp);
+    cudaFree(D.fp_n);
+    cudaFree(s->d_scratch);
+    cudaFree(s->d_tab);
+    delete s;
+}
+
+bool loaded(const State *s) { return s && s->ready; }
+
+int set_rates(State *s, const double *ptransE, const double *ptransD, std::string &err)
+{
+    memcpy(s->ptransE, ptransE, sizeof s->ptransE);
+    memcpy(s->ptransD, ptransD, sizeof s->ptransD);
+    s->rates = true;
+    int rc = upload_tables(s, err);
+    if (rc) return rc;
+    if (s->ready) {   // re-rate the current lattice (SetProbability then Get_Prob of every site)
+        int top = 0;
+        SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
+        SK(cudaStreamSynchronize(s->stream));
+        if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, nullptr, 1, top);
+        SK(cudaGetLastError());
+        s->lists_ok = false;
+        return check_device(s, err, "rates");
+    }
+    return 0;
+}
+
+int from_compact(State *s, const uint8_t *d_st, int NA, int NB, int NZ, int pitch, std::string &err)
+{
+    Dev &D = s->D;
+    if (NA * 6 != D.lx || NB * 6 != D.ly) return ferr(err, MKS_ERR_ARG, "compact lattice does not match the box");
+    const int rows = NZ * NB;
+    SK(cudaMemsetAsync(D.coo, 0, sizeof(uint32_t) * s->ngrid, s->stream));
+    SK(cudaMemsetAsync(D.ind, 0, sizeof(int32_t) * s->ngrid, s->stream));
+    int32_t *d_rows = nullptr, *d_lw = nullptr;
+    uint8_t *d_ini = nullptr;
+    SK(cudaMallocAsync(&d_rows, sizeof(int32_t) * rows, s->stream));
+    SK(cudaMallocAsync(&d_lw, sizeof(int32_t) * 2 * NZ, s->stream));
+    SK(cudaMemsetAsync(d_lw, 0, sizeof(int32_t) * 2 * NZ, s->stream));
+    k_count_rows<<<(rows + 127) / 128, 128, 0, s->stream>>>(d_st, NA, NB, NZ, pitch, D.lz, d_rows);
+    k_layer_walls<<<(rows + 127) / 128, 128, 0, s->stream>>>(d_st, NA, NB, NZ, pitch, d_lw);
+    SK(cudaGetLastError());
+    std::vector<int32_t> rc(rows), lw(2 * NZ);
+    SK(cudaMemcpyAsync(rc.data(), d_rows, sizeof(int32_t) * rows, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaMemcpyAsync(lw.data(), d_lw, sizeof(int32_t) * 2 * NZ, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    // walls: a layer of wall sites stands for its three grid planes, every
+    // grid point of them a wall (SetSi.f:38-46,212-220); a layer with only
+    // some wall sites has wall points off the diamond sub-grid that the
+    // compact lattice does not record
+    std::vector<int32_t> wp(D.lz + 1, 0);
+    for (int z1 = 0; z1 < NZ; z1++) {
+        if (lw[2 * z1 + 1] == 0) continue;
+        if (lw[2 * z1 + 1] != lw[2 * z1]) {
+            cudaFreeAsync(d_rows, s->stream);
+            cudaFreeAsync(d_lw, s->stream);
+            return ferr(err, MKS_ERR_UNSUPPORTED,
+                        "layer z=%d holds a partial wall block: its points off the diamond sites are not in the "
+                        "compact lattice (arm-chair stacking needs them)", 3 * z1);
+        }
+        for (int zz = 3 * z1; zz < 3 * z1 + 3 && zz <= D.lz; zz++) wp[zz] = 1;
+    }
+    std::vector<int32_t> off(rows);
+    int64_t tot = 0;
+    for (int i = 0; i < rows; i++) {
+        off[i] = (int32_t)(tot + 1);
+        tot += rc[i];
+    }
+    if (tot + 1 > D.rcap) {
+        cudaFreeAsync(d_rows, s->stream);
+        cudaFreeAsync(d_lw, s->stream);
+        return ferr(err, MKS_ERR_CAPACITY, "%lld listed sites exceed the record pool", (long long)tot);
+    }
+    SK(cudaMemcpyAsync(d_rows, off.data(), sizeof(int32_t) * rows, cudaMemcpyHostToDevice, s->stream));
+    SK(cudaMallocAsync(&d_ini, (size_t)tot + 2, s->stream));
+    SK(cudaMemsetAsync(d_ini, 0, (size_t)tot + 2, s->stream));
+    int32_t *d_wplanes = nullptr;
+    SK(cudaMallocAsync(&d_wplanes, sizeof(int32_t) * (D.lz + 1), s->stream));
+    SK(cudaMemcpyAsync(d_wplanes, wp.data(), sizeof(int32_t) * (D.lz + 1), cudaMemcpyHostToDevice, s->stream));
+    k_wall_planes<<<grid_for((int64_t)D.lx * D.ly * (D.lz + 1)), 256, 0, s->stream>>>(D, d_wplanes);
+    k_expand<<<(rows + 127) / 128, 128, 0, s->stream>>>(D, d_st, NA, NB, NZ, pitch, d_rows, d_ini);
+    SK(cudaGetLastError());
+    s->nrec = (int)tot;
+    int r = rates_and_lists(s, d_ini, err);
+    cudaFreeAsync(d_rows, s->stream);
+    cudaFreeAsync(d_lw, s->stream);
+    cudaFreeAsync(d_ini, s->stream);
+    cudaFreeAsync(d_wplanes, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
+    s->time = 0.0;
+    s->window = 0;
+    s->events = 0;
+    s->stop_reason = 0;
+    return r;
+}
+
+int load_lists(State *s, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
+               const uint8_t *ini, std::string &err)
+{
+    Dev &D = s->D;
+    if (n + 1 > D.rcap) return ferr(err, MKS_ERR_CAPACITY, "%lld list entries exceed the record pool", (long long)n);
+    for (int64_t i = 0; i < n; i++) {
+        const int32_t *p = xyz + 3 * i;
+        if (p[0] < 0 || p[0] >= D.lx || p[1] < 0 || p[1] >= D.ly || p[2] < 0 || p[2] > D.lz)
+            return ferr(err, MKS_ERR_ARG, "list entry %lld at (%d, %d, %d) is outside the box", (long long)i, p[0], p[1],
+                        p[2]);
+        for (int k = 0; k < 4; k++) {
+            const int32_t *q = nn + 12 * i + 3 * k;
+            if (q[0] < 0 || q[0] >= D.lx || q[1] < 0 || q[1] >= D.ly || q[2] < -ZG || q[2] > D.lz + ZG)
+                return ferr(err, MKS_ERR_ARG, "NextN %d of list entry %lld is outside the box", k, (long long)i);
+        }
+    }
+    const int64_t plane = (int64_t)D.lx * D.ly;
+    SK(cudaMemsetAsync(D.coo, 0, sizeof(uint32_t) * s->ngrid, s->stream));
+    SK(cudaMemsetAsync(D.ind, 0, sizeof(int32_t) * s->ngrid, s->stream));
+    SK(cudaMemcpyAsync(D.coo + ZG * plane, lattcoo, sizeof(int32_t) * plane * (D.lz + 1), cudaMemcpyHostToDevice,
+                       s->stream));
+    int32_t *d_xyz = nullptr, *d_nn = nullptr;
+    uint8_t *d_ini = nullptr;
+    size_t nb = (size_t)std::max<int64_t>(n, 1);
+    SK(cudaMallocAsync(&d_xyz, sizeof(int32_t) * 3 * nb, s->stream));
+    SK(cudaMallocAsync(&d_nn, sizeof(int32_t) * 12 * nb, s->stream));
+    SK(cudaMallocAsync(&d_ini, nb + 2, s->stream));
+    SK(cudaMemsetAsync(d_ini, 0, nb + 2, s->stream));
+    if (n) {
+        SK(cudaMemcpyAsync(d_xyz, xyz, sizeof(int32_t) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+        SK(cudaMemcpyAsync(d_nn, nn, sizeof(int32_t) * 12 * n, cudaMemcpyHostToDevice, s->stream));
+        if (ini) SK(cudaMemcpyAsync(d_ini + 1, ini, (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        k_load_records<<<grid_for(n), 256, 0, s->stream>>>(D, d_xyz, d_nn, (long long)n);
+        SK(cudaGetLastError());
+    }
+    s->nrec = (int)n;
+    int r = rates_and_lists(s, d_ini, err);
+    cudaFreeAsync(d_xyz, s->stream);
+    cudaFreeAsync(d_nn, s->stream);
+    cudaFreeAsync(d_ini, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
+    s->time = 0.0;
+    s->window = 0;
+    s->events = 0;
+    s->stop_reason = 0;
+    return r;
+}
+
+int replay(State *s, const mks_event *trace, int64_t n, int64_t *done, std::string &err)
+{
+    if (!s->ready) return ferr(err, MKS_ERR_ARG, "no lattice loaded");
+    if (done) *done = 0;
+    if (n <= 0) return 0;
+    mks_event *d_ev = nullptr;
+    long long *d_done = nullptr;
+    SK(cudaMallocAsync(&d_ev, sizeof(mks_event) * (size_t)n, s->stream));
+    SK(cudaMallocAsync(&d_done, sizeof(long long), s->stream));
+    SK(cudaMemcpyAsync(d_ev, trace, sizeof(mks_event) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    SK(cudaMemsetAsync(s->D.fr_n, 0, sizeof(int32_t), s->stream));
+    k_replay<<<1, 32, 0, s->stream>>>(s->D, d_ev, (long long)n, d_done);
+    SK(cudaGetLastError());
+    long long k = 0;
+    SK(cudaMemcpyAsync(&k, d_done, sizeof k, cudaMemcpyDeviceToHost, s->stream));
+    cudaFreeAsync(d_ev, s->stream);
+    cudaFreeAsync(d_done, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
+    SK(cudaMemsetAsync(s->D.fr_n, 0, sizeof(int32_t), s->stream));
+    if (done) *done = k;
+    s->events += k;
+    s->lists_ok = false;
+    return check_device(s, err, "replay");
+}
+
+int run(State *s, double tau, int64_t max_windows, int64_t max_events, double max_time, int64_t *events,
+        double *time, std::string &err)
+{
+    if (!s->ready) return ferr(err, MKS_ERR_ARG, "no lattice loaded");
+    if (!s->rates) return ferr(err, MKS_ERR_ARG, "rates not set");
+    if (!(tau > 0.0)) return ferr(err, MKS_ERR_ARG, "tau must be positive");
+    if (!s->lists_ok) {
+        int rc = rebuild(s, err);
+        if (rc) return rc;
+    }
+    Dev &D = s->D;
+    unsigned long long e0 = 0;
+    SK(cudaMemcpyAsync(&e0, D.events, sizeof e0, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaMemsetAsync(D.stop, 0, sizeof(int32_t), s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    s->stop_reason = 0;
+    const int warps = D.ntx * D.nty / 4;
+    const int blocks = (warps * 32 + 127) / 128;
+    int64_t w = 0;
+    const int64_t batch = 8;
+    unsigned long long ev = e0;
+    while (max_windows <= 0 || w < max_windows) {
+        int64_t nb = max_windows > 0 ? std::min<int64_t>(batch, max_windows - w) : batch;
+        if (max_time > 0.0) {
+            int64_t left = (int64_t)ceil((max_time - s->time) / tau - 1e-9);
+            if (left <= 0) {
+                s->stop_reason = 3;
+                break;
+            }
+            nb = std::min(nb, left);
+        }
+        for (int64_t k = 0; k < nb; k++) {
+            k_stop_check<<<1, 32, 0, s->stream>>>(D);
+            for (int colour = 0; colour < 4; colour++)
+                k_phase<<<blocks, 128, 0, s->stream>>>(D, colour, (uint32_t)(s->window + k), (float)tau);
+        }
+        SK(cudaGetLastError());
+        int rc = check_device(s, err, "run");
+        if (rc) {
+            s->lists_ok = false;
+            return rc;
+        }
+        int32_t stop = 0;
+        SK(cudaMemcpyAsync(&ev, D.events, sizeof ev, cudaMemcpyDeviceToHost, s->stream));
+        SK(cudaMemcpyAsync(&stop, D.stop, sizeof stop, cudaMemcpyDeviceToHost, s->stream));
+        SK(cudaStreamSynchronize(s->stream));
+        s->window += nb;
+        s->time += (double)nb * tau;
+        w += nb;
+        if (stop) {
+            s->stop_reason = 1;
+            break;
+        }
+        if (max_events > 0 && (int64_t)(ev - e0) >= max_events) {
+            s->stop_reason = 2;
+            break;
+        }
+    }
+    s->events += (int64_t)(ev - e0);
+    if (events) *events = (int64_t)(ev - e0);
+    if (time) *time = s->time;
+    return 0;
+}
+
+int get_lattice(State *s, int32_t *lattcoo, std::string &err)
+{
+    const int64_t plane = (int64_t)s->D.lx * s->D.ly;
+    SK(cudaMemcpyAsync(lattcoo, s->D.coo + ZG * plane, sizeof(int32_t) * plane * (s->D.lz + 1), cudaMemcpyDeviceToHost,
+                       s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int get_lists(State *s, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *evc, float *rate,
+              int64_t *n, std::string &err)
+{
+    int top = 0;
+    SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    std::vector<Rec> rec((size_t)std::max(top, 1));
+    std::vector<int32_t> word((size_t)std::max(top, 1));
+    int32_t *d_word = nullptr;
+    SK(cudaMallocAsync(&d_word, sizeof(int32_t) * (size_t)std::max(top, 1), s->stream));
+    if (top > 1) k_gather<<<grid_for(top), 256, 0, s->stream>>>(s->D, top, d_word);
+    SK(cudaGetLastError());
+    SK(cudaMemcpyAsync(rec.data(), s->D.rec, sizeof(Rec) * (size_t)top, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaMemcpyAsync(word.data(), d_word, sizeof(int32_t) * (size_t)top, cudaMemcpyDeviceToHost, s->stream));
+    cudaFreeAsync(d_word, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
+    int64_t k = 0;
+    bool write = xyz && nn && kind && evc && rate;
+    for (int r = 1; r < top; r++) {
+        const Rec &R = rec[r];
+        if (R.x < 0) continue;
+        if (write && k < cap) {
+            uint32_t v = (uint32_t)word[r];
+            int kd = R.ev ? 1 : (((v >> 23) & 1) && ((v >> 24) & 7) == 4 ? 2 : (((v >> 24) & 7) == 4 ? 3 : 0));
+            xyz[3 * k] = R.x;
+            xyz[3 * k + 1] = R.y;
+            xyz[3 * k + 2] = R.z;
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 3; j++) nn[12 * k + 3 * i + j] = R.nn[i][j];
+            kind[k] = kd;
+            evc[k] = R.ev;
+            rate[k] = R.rate;
+        }
+        k++;
+    }
+    *n = k;
+    return 0;
+}
+
+int observables(State *s, mks_observables *o, std::string &err)
+{
+    memset(o, 0, sizeof *o);
+    int top = 0;
+    SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    const int ncol = (s->D.lx / 6) * (s->D.ly / 6);
+    unsigned long long *d_cnt = nullptr;
+    double *d_rs = nullptr;
+    int32_t *d_col = nullptr;
+    SK(cudaMallocAsync(&d_cnt, sizeof(unsigned long long) * 8, s->stream));
+    SK(cudaMallocAsync(&d_rs, sizeof(double) * 2, s->stream));
+    SK(cudaMallocAsync(&d_col, sizeof(int32_t) * ncol, s->stream));
+    SK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long) * 8, s->stream));
+    SK(cudaMemsetAsync(d_rs, 0, sizeof(double) * 2, s->stream));
+    SK(cudaMemsetAsync(d_col, 0xff, sizeof(int32_t) * ncol, s->stream));
+    if (top > 1) k_observe<<<grid_for(top), 256, 0, s->stream>>>(s->D, top, d_cnt, d_rs, d_col);
+    SK(cudaGetLastError());
+    unsigned long long cnt[8];
+    double rs[2];
+    std::vector<int32_t> col(ncol);
+    SK(cudaMemcpyAsync(cnt, d_cnt, sizeof cnt, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaMemcpyAsync(rs, d_rs, sizeof rs, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaMemcpyAsync(col.data(), d_col, sizeof(int32_t) * ncol, cudaMemcpyDeviceToHost, s->stream));
+    cudaFreeAsync(d_cnt, s->stream);
+    cudaFreeAsync(d_rs, s->stream);
+    cudaFreeAsync(d_col, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
+    o->events = s->events;
+    o->time = s->time;
+    o->atoms = (int64_t)cnt[0];
+    o->undercoord = (int64_t)cnt[1];
+    o->mc_sites = (int64_t)cnt[2];
+    o->voids = (int64_t)cnt[3];
+    for (int k = 0; k < 3; k++) o->species[k] = (int64_t)cnt[4 + k];
+    o->nonepitaxial = (int64_t)cnt[7];
+    o->total_rate = rs[0] + rs[1] * 1.0e5 * rs[0];
+    double sh = 0.0, sh2 = 0.0;
+    int64_t m = 0;
+    for (int32_t h : col)
+        if (h >= 0) {
+            sh += h;
+            sh2 += (double)h * h;
+            m++;
+        }
+    if (m) {
+        o->mean_height = sh / (double)m;
+        double var = sh2 / (double)m - o->mean_height * o->mean_height;
+        o->rms_roughness = sqrt(var > 0.0 ? var : 0.0);
+    }
+    return 0;
+}
+
+int clock(State *s, double *time, int64_t *window, int64_t *events)
+{
+    if (time) *time = s->time;
+    if (window) *window = s->window;
+    if (events) *events = s->events;
+    return 0;
+}
+
+int status(State *s, mks_status *st)
+{
+    memset(st, 0, sizeof *st);
+    st->error = s->last_error;
+    st->windows = s->window;
+    st->active = s->stop_reason == 0;
+    st->stop_reason = s->stop_reason;
+    return 0;
+}
+
+}  // namespace mks_stk

@@ -221,6 +221,33 @@ class Lattice:
         assert a.size == lx * ly * (lz + 1)
         N.check(N.lib().mks_load_lattice(self._h, N.ptr(a)))
 
+    def load_lists(self, lattcoo, xyz, nn, ini=None):
+        """Arm-chair stacking (ptrans_zig < 1): the full reference state, LattCoo
+        [z, y, x] and the list entries (grid points xyz (n, 3), NextN nn
+        (n, 4, 3); ini marks unsupported coor-1 sites at the init-time rate)."""
+        a = np.ascontiguousarray(lattcoo, dtype=np.int32)
+        lx, ly, lz = self.dims
+        assert a.size == lx * ly * (lz + 1)
+        p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        q = np.ascontiguousarray(nn, dtype=np.int32).reshape(-1, 4, 3)
+        assert len(p) == len(q)
+        f = None if ini is None else np.ascontiguousarray(ini, dtype=np.uint8).reshape(-1)
+        N.check(N.lib().mks_load_lists(self._h, N.ptr(a), len(p), N.ptr(p), N.ptr(q),
+                                       None if f is None else N.ptr(f)))
+
+    def lists(self):
+        """Arm-chair stacking: every listed site as a dict of xyz (n, 3), nn
+        (n, 4, 3), kind (1 with an event, 2 bulk atom, 3 void), event (1
+        deposition, 2 dummy, 4 evaporation, 5 isolated atom) and rate."""
+        n = C.c_int64()
+        N.check(N.lib().mks_get_lists(self._h, 0, None, None, None, None, None, C.byref(n)))
+        m = max(n.value, 1)
+        out = {"xyz": np.zeros((m, 3), np.int32), "nn": np.zeros((m, 4, 3), np.int32),
+               "kind": np.zeros(m, np.int32), "event": np.zeros(m, np.int32), "rate": np.zeros(m, np.float32)}
+        N.check(N.lib().mks_get_lists(self._h, m, *(N.ptr(out[k]) for k in ("xyz", "nn", "kind", "event", "rate")),
+                                      C.byref(n)))
+        return {k: v[:n.value] for k, v in out.items()}
+
     def set_tiling(self, width):
         N.check(N.lib().mks_set_tiling(self._h, int(width)))
 

@@ -2863,6 +2863,32 @@ int64_t ora_mc_sites(const ora_t *o, int32_t *xyz, int64_t n)
     return o->num_mc;
 }
 
+/* Every list entry: the MC particles (kind 1, ListAdAtom), the bulk atoms
+ * (kind 2, ListAtom) and the voids (kind 3, ListVoid), each list in its
+ * order, with the grid point, the four NextN entries, and for MC particles
+ * Ind_Event and ProbTrans (defdertype.f:25-45).  Writes up to n entries;
+ * returns the total count. */
+int64_t ora_list_entries(const ora_t *o, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *ind_event,
+                         double *prob, int64_t n)
+{
+    int64_t k = 0;
+    for (int pass = 1; pass <= 3; pass++) {
+        int64_t m = pass == 1 ? o->num_mc : (pass == 2 ? o->num_bulk : o->num_void);
+        for (int64_t i = 1; i <= m; i++, k++) {
+            if (k >= n) continue;
+            const int *p = pass == 1 ? o->mc[i].xyz : (pass == 2 ? o->bulk[i].xyz : o->voids[i].xyz);
+            const int(*q)[3] = pass == 1 ? o->mc[i].nn : (pass == 2 ? o->bulk[i].nn : o->voids[i].nn);
+            for (int c = 0; c < 3; c++) xyz[3 * k + c] = p[c];
+            for (int j = 0; j < 4; j++)
+                for (int c = 0; c < 3; c++) nn[12 * k + 3 * j + c] = q[j][c];
+            kind[k] = pass;
+            ind_event[k] = pass == 1 ? o->mc[i].ind_event : 0;
+            prob[k] = pass == 1 ? o->mc[i].prob : 0.0;
+        }
+    }
+    return k;
+}
+
 int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
 {
     ora_t *o = (ora_t *)o_;

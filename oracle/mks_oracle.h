@@ -109,6 +109,8 @@ int64_t ora_mc_classes(const ora_t *o, int32_t *cls, double *rate, int64_t n);
 /* Grid coordinates (x, y, z) of the MC particles in the same list order,
  * up to n of them; returns NumAdAtom.                                      */
 int64_t ora_mc_sites(const ora_t *o, int32_t *xyz, int64_t n);
+int64_t ora_list_entries(const ora_t *o, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *ind_event,
+                         double *prob, int64_t n);
 
 /* Export the rate tables parsed from start.dat. */
 void ora_get_rates(const ora_t *o, double ptransE[3 * 4096], double ptransD[9]);

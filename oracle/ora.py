@@ -62,6 +62,8 @@ def lib():
         L.ora_mc_classes.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.ora_mc_sites.restype = C.c_int64
         L.ora_mc_sites.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        L.ora_list_entries.restype = C.c_int64
+        L.ora_list_entries.argtypes = [C.c_void_p] * 7 + [C.c_int64]
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_set_la_input.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -265,6 +267,22 @@ def mc_sites(o):
     xyz = np.zeros((max(n, 1), 3), dtype=np.int32)
     m = lib().ora_mc_sites(o._h, xyz.ctypes.data_as(C.c_void_p), n)
     return xyz[:m]
+
+
+def list_entries(o):
+    """Every list entry of the oracle (ListAdAtom, ListAtom, ListVoid, each in
+    its order): dict of xyz (n, 3), nn (n, 4, 3), kind (1 MC, 2 bulk, 3 void),
+    ind_event and prob (MC particles only)."""
+    c = o.counts()
+    n = c["bulk"] + c["voids"] + c["mc"]
+    xyz = np.zeros((max(n, 1), 3), dtype=np.int32)
+    nn = np.zeros((max(n, 1), 4, 3), dtype=np.int32)
+    kind = np.zeros(max(n, 1), dtype=np.int32)
+    ie = np.zeros(max(n, 1), dtype=np.int32)
+    pr = np.zeros(max(n, 1), dtype=np.float64)
+    m = lib().ora_list_entries(o._h, *(a.ctypes.data_as(C.c_void_p) for a in (xyz, nn, kind, ie, pr)), n)
+    assert m == n
+    return {"xyz": xyz[:n], "nn": nn[:n], "kind": kind[:n], "ind_event": ie[:n], "prob": pr[:n]}
 
 
 def rate_of_site(o, x, y, z):
