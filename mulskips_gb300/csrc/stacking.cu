@@ -941,8 +941,15 @@ __global__ void k_expand(Dev D, const uint8_t *st, int NA, int NB, int NZ, int p
         R.y = (int16_t)p.y;
         R.z = (int16_t)p.z;
         // NextN: the four bonds (JumpDia order, defsystem.f:104-105) from the
-        // first list entry on, as the initializers list them (SetSi.f:52-57)
+        // first list entry on, as the initializers list them (SetSi.f:52-57);
+        // an empty coor-1 site lists its one neighbour and zeros, as the
+        // initializers' ad-void passes and deposition.f:86-99 write it
+        const bool one = !sp && co == 1;
         for (int i = 0; i < 4; i++) {
+            if (one && i > 0) {
+                put_nn(R, i, P3{0, 0, 0});
+                continue;
+            }
             int d = (fd + i) & 3;
             int da = zp - (d >> 1), db = zp - ((d ^ (d >> 1)) & 1), dz = ((d ^ zp) & 1) ? -1 : 1;
             int aa = a + da, bb = b + db, kk = z1 + dz;

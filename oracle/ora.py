@@ -63,7 +63,7 @@ def lib():
         L.ora_mc_sites.restype = C.c_int64
         L.ora_mc_sites.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         L.ora_list_entries.restype = C.c_int64
-        L.ora_list_entries.argtypes = [C.c_void_p] * 7 + [C.c_int64]
+        L.ora_list_entries.argtypes = [C.c_void_p] * 6 + [C.c_int64]
         L.ora_compact_state.restype = C.c_int64
         L.ora_compact_state.argtypes = [C.c_void_p, C.c_void_p]
         L.ora_set_la_input.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
