@@ -156,12 +156,17 @@ int mks_get_lattice(mks_handle *h, int32_t *lattcoo);
 /* Arm-chair stacking handles only (PtransZig < 1): load the full reference
  * state -- LattCoo(0:LenX-1, 0:LenY-1, 0:LenZ) (x fastest) and n list
  * entries (ListAdAtom, ListAtom and ListVoid; grid point xyz[3i..3i+2] and
- * NextN nn[12i..12i+11], defdertype.f:25-45) -- and rate every entry with
- * Get_Prob; ini[i] != 0 (ini may be NULL) keeps an unsupported coor-1 site at
- * Get_Prob_Ini's dummy rate 1e-6 (Get_Prob_Ini.f:102-104).  Continuation
- * from a saved state (main.f:385-403 writes LattCoo; the lists follow).   */
+ * NextN nn[12i..12i+11], defdertype.f:25-45).  With event and rate NULL
+ * every entry is rated as Get_Prob_Ini does (an unsupported coor-1 site at
+ * 1e-6, Get_Prob_Ini.f:102-104); with both given, entry i keeps event code
+ * event[i] (0 none, 1 deposition, 2 dummy deposition, 4 evaporation) and
+ * rate[i] -- the ProbTrans of a saved ListAdAtom, which the reference does
+ * not recompute when only a site's second neighbours change -- except that
+ * an atom without reciprocal neighbours is the isolated atom of
+ * Get_Prob.f:300-306.  Continuation from a saved state (main.f:385-403
+ * writes LattCoo; the lists follow).                                       */
 int mks_load_lists(mks_handle *h, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
-                   const uint8_t *ini);
+                   const int32_t *event, const float *rate);
 /* Arm-chair stacking handles only: every listed site, with its grid point
  * (xyz, 3 per site), NextN (nn, 12 per site), kind (1 with an event, the
  * ListAdAtom entries; 2 a bulk atom, ListAtom; 3 a void, ListVoid), event

@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <unordered_map>
 
 #include "lattice.cuh"
 #include "shapes.cuh"
@@ -2813,12 +2814,12 @@ int mks_set_state(mks_handle *h, const uint8_t *in, int64_t n)
 }
 
 int mks_load_lists(mks_handle *h, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
-                   const uint8_t *ini)
+                   const int32_t *event, const float *rate)
 {
-    if (!h || !lattcoo || n < 0 || (n && (!xyz || !nn))) return fail(MKS_ERR_ARG, "bad arguments");
+    if (!h || !lattcoo || n < 0 || (n && (!xyz || !nn)) || (!event) != (!rate)) return fail(MKS_ERR_ARG, "bad arguments");
     if (!h->stk) return fail(MKS_ERR_ARG, "mks_load_lists needs a handle with PtransZig < 1");
     std::string err;
-    int rc = mks_stk::load_lists(h->stk, lattcoo, n, xyz, nn, ini, err);
+    int rc = mks_stk::load_lists(h->stk, lattcoo, n, xyz, nn, event, rate, err);
     if (rc) return fail(rc, "%s", err.c_str());
     h->stk_dirty = false;
     return 0;
@@ -3563,6 +3564,156 @@ const char *crystal_symbol(const mks_config &c, int sp)
     return z == 6 ? "C" : (z == 32 ? "Ge" : (z == 5 ? "B" : nullptr));
 }
 
+// The frame files of WriteMolMolXYZFile.f:22-406 for an arm-chair stacking
+// handle, from its listed sites (every atom and void is listed; walls are
+// not written).  Sites follow the reference's z, y, x scan; voids too (the
+// reference lists them in ListVoid order).  The SiC wrong-site analysis works
+// on a copy, as the compact writer's does.
+int stk_write_frame(mks_handle *h, const char *base, double time, int64_t iter, int64_t *num_at_wrong)
+{
+    const mks_config &c = h->reps[0].cfg;
+    std::string err;
+    std::vector<mks_stk::Site> all;
+    int rc = mks_stk::sites(h->stk, all, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    const int64_t lx = c.lenx, ly = c.leny;
+    auto key = [&](int64_t x, int64_t y, int64_t z) { return x + lx * (y + ly * z); };
+    std::sort(all.begin(), all.end(), [&](const mks_stk::Site &a, const mks_stk::Site &b) {
+        return key(a.x, a.y, a.z) < key(b.x, b.y, b.z);
+    });
+    auto occ = [](uint32_t v) { return (v >> 23) & 1; };
+    auto coor = [](uint32_t v) { return (int)((v >> 24) & 7); };
+    auto spv = [](uint32_t v) { return (int)((v >> 27) & 7); };
+    auto dia = [](int x, int y, int z) {   // SetSi.f:52-57
+        if (x % 3 || y % 3 || z % 3) return false;
+        int x1 = x / 3, y1 = y / 3, z1 = z / 3;
+        if ((x1 & 1) != (y1 & 1) || (x1 & 1) != (z1 & 1)) return false;
+        int m = (x1 + y1 + z1) & 3;
+        return m == 0 || m == 3;
+    };
+    const int lz = c.lenz;
+    int64_t num_at = 0, noepi = 0, nvoid = 0;
+    for (const auto &t : all) {
+        uint32_t v = t.word;
+        if (t.z >= 1 && t.z <= lz - 1 && occ(v) && coor(v) <= 3) num_at++;
+        if (t.z >= 0 && t.z <= lz - 1 && occ(v) && coor(v) == 4 && !dia(t.x, t.y, t.z)) noepi++;
+        if (!occ(v) && coor(v) == 4) nvoid++;
+    }
+    const std::string per = " periodic " + fortran_e(c.sf * c.lenx, 15, 8) + " " + fortran_e(c.sf * c.leny, 15, 8) +
+                            " " + fortran_e(c.sf * c.lenz, 15, 8) + "\n";
+    auto header = [&](FILE *f, int64_t n) {
+        fprintf(f, " %8lld angstroem KMC-time: %s Iter: %12lld\n", (long long)n, fortran_e(time, 15, 8).c_str(),
+                (long long)iter);
+        fputs(per.c_str(), f);
+    };
+    auto line = [&](FILE *f, const char *sym, const mks_stk::Site &t) {
+        fprintf(f, "%s %10.5f %10.5f %10.5f  \n", sym, c.sf * t.x, c.sf * t.y, c.sf * t.z);
+    };
+    std::string b(base);
+    FILE *f = fopen((b + "_d.xyz").c_str(), "w");          // :96-160, the non-epitaxial bulk
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_d.xyz", base);
+    header(f, noepi);
+    for (const auto &t : all) {
+        uint32_t v = t.word;
+        if (t.z < 0 || t.z > lz - 1 || !occ(v) || coor(v) != 4 || dia(t.x, t.y, t.z)) continue;
+        int s = spv(v);
+        if (s == 1) line(f, "Ge", t);
+        if (s == 2) line(f, "B", t);
+        if (s == 3) line(f, "Cl", t);
+    }
+    fclose(f);
+    f = fopen((b + ".xyz").c_str(), "w");
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s.xyz", base);
+    header(f, num_at + nvoid);
+    for (const auto &t : all) {
+        uint32_t v = t.word;
+        int s = spv(v);
+        if (t.z < 0 || t.z > lz - 1 || s < 1 || s > 3 || coor(v) > 3) continue;
+        const char *sym = crystal_symbol(c, s);
+        if (!sym || s > c.ncrystal) {
+            fclose(f);
+            return fail(MKS_ERR_INVARIANT, "ERROR: 2nd crystal specie can only be C/Ge/B");
+        }
+        line(f, sym, t);
+    }
+    for (const auto &t : all)
+        if (!occ(t.word) && coor(t.word) == 4) line(f, "O", t);
+    fclose(f);
+    std::unordered_map<int64_t, uint32_t> word;
+    word.reserve(all.size() * 2);
+    for (const auto &t : all) word[key(t.x, t.y, t.z)] = t.word;
+    auto word_at = [&](const int32_t *p) -> uint32_t {
+        auto it = word.find(key(p[0], p[1], p[2]));
+        return it == word.end() ? 0u : it->second;
+    };
+    const bool sic = c.ncrystal == 2 && (c.list_crystal[0] == 6 || c.list_crystal[1] == 6 || c.list_crystal[2] == 6);
+    f = fopen((b + "_v.xyz").c_str(), "w");                 // :216-260
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_v.xyz", base);
+    fprintf(f, " %8lld angstroem\n", (long long)nvoid);
+    fputs(per.c_str(), f);
+    for (const auto &t : all) {
+        if (occ(t.word) || coor(t.word) != 4) continue;
+        if (sic) {
+            int sum = 0;
+            for (int j = 0; j < 4; j++) sum += spv(word_at(t.nn[j]));
+            const char *lbl = sum == 4 ? "Mg %10.5f %10.5f %10.5f # CV (C vacancy)\n"
+                            : sum == 8 ? "He %10.5f %10.5f %10.5f # SV (Si vacancy)\n"
+                            : sum == 7 ? "Ne %10.5f %10.5f %10.5f # SAV (Si antisite vac)\n"
+                            : sum == 5 ? "Be %10.5f %10.5f %10.5f # CAV (C antisite vac)\n"
+                            : sum == 6 ? "Ar %10.5f %10.5f %10.5f # XV (near 2C and 2Si)\n" : nullptr;
+            if (!lbl) {
+                fclose(f);
+                return fail(MKS_ERR_INVARIANT, "ERROR: Weird Defect type was formed");
+            }
+            fprintf(f, lbl, c.sf * t.x, c.sf * t.y, c.sf * t.z);
+        } else {
+            line(f, "O", t);
+        }
+    }
+    fclose(f);
+    if (num_at_wrong) *num_at_wrong = 0;
+    if (!sic) return 0;
+    // :264-398: bulk atoms (z >= 1) with no neighbour of the other species
+    // count as swapped (Si bit 27, C bit 28), then bulk atoms with three are
+    // listed
+    auto bulk = [&](const mks_stk::Site &t) {
+        return t.z >= 1 && t.z <= lz - 1 && occ(t.word) && coor(t.word) == 4 && (t.word & 255) != 113;
+    };
+    auto other = [&](uint32_t own, uint32_t w) {
+        int s = spv(own);
+        return s == 1 ? (int)((w >> 28) & 1) : (s == 2 ? (int)((w >> 27) & 1) : 0);
+    };
+    std::unordered_map<int64_t, uint32_t> sw(word);
+    for (const auto &t : all) {
+        if (!bulk(t)) continue;
+        int nc = 0;
+        for (int j = 0; j < 4; j++) nc += other(t.word, word_at(t.nn[j]));
+        int s = spv(t.word);
+        if (nc == 0 && (s == 1 || s == 2))
+            sw[key(t.x, t.y, t.z)] = (t.word & ~(7u << 27)) | ((uint32_t)(s == 1 ? 2 : 1) << 27);
+    }
+    auto sw_at = [&](const int32_t *p) -> uint32_t {
+        auto it = sw.find(key(p[0], p[1], p[2]));
+        return it == sw.end() ? 0u : it->second;
+    };
+    std::vector<std::pair<const mks_stk::Site *, uint32_t>> wrong;
+    for (const auto &t : all) {
+        if (!bulk(t)) continue;
+        uint32_t own = sw[key(t.x, t.y, t.z)];
+        int nc = 0;
+        for (int j = 0; j < 4; j++) nc += other(own, sw_at(t.nn[j]));
+        if (nc == 3) wrong.push_back({&t, own});
+    }
+    if (num_at_wrong) *num_at_wrong = (int64_t)wrong.size();
+    f = fopen((b + "_w.xyz").c_str(), "w");
+    if (!f) return fail(MKS_ERR_ARG, "cannot write %s_w.xyz", base);
+    fprintf(f, " %8lld angstroem\n", (long long)wrong.size());
+    fputs(per.c_str(), f);
+    for (const auto &w : wrong) line(f, spv(w.second) == 1 ? "Si" : "C", *w.first);
+    fclose(f);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -3571,6 +3722,10 @@ int mks_write_frame(mks_handle *h, const char *base, double time, int64_t iter, 
 {
     if (num_at_wrong) *num_at_wrong = 0;
     if (!h || !base || h->reps.size() != 1) return fail(MKS_ERR_ARG, "mks_write_frame needs a single-replica handle");
+    if (h->stk) {
+        int rc = stk_sync(h);
+        return rc ? rc : stk_write_frame(h, base, time, iter, num_at_wrong);
+    }
     const RepHost &r = h->reps[0];
     const mks_config &c = r.cfg;
     const bool cov = c.ncov > 0;

@@ -856,8 +856,13 @@ __global__ void k_replay(Dev D, const mks_event *ev, long long n, long long *don
 }
 
 // rates of every record from the current lattice (Get_Prob_Ini.f:23-161: an
-// empty coor-1 site marked ini keeps the init-time dummy rate 1e-6, :102-104)
-__global__ void k_rate_all(Dev D, const uint8_t *ini, int first, int last)
+// empty coor-1 site marked ini keeps the init-time dummy rate 1e-6, :102-104),
+// or, with gev / grate, the given event codes and rates kept as they are (the
+// reference does not re-rate a site when only its neighbours' neighbours
+// change, so a saved state's rates are not all what Get_Prob would give now);
+// an evaporation whose site has no reciprocal neighbour is the isolated atom
+// of Get_Prob.f:300-306 either way
+__global__ void k_rate_all(Dev D, const uint8_t *ini, const int32_t *gev, const float *grate, int first, int last)
 {
     for (int r = first + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
         Rec &R = D.rec[r];
@@ -870,6 +875,10 @@ __global__ void k_rate_all(Dev D, const uint8_t *ini, int first, int last)
         float rate;
         get_prob(D, occ_of(v), sp_of(v), coor_of(v), s, nn, ev, rate);
         if (ev == EV_DUMMY && ini && ini[r]) rate = 1.e-6f;
+        if (gev && ev != EV_ISO) {
+            ev = (uint8_t)gev[r];
+            rate = grate[r];
+        }
         R.ev = ev;
         R.rate = rate;
         R.flags = 0;
@@ -1145,11 +1154,12 @@ int check_device(State *s, std::string &err, const char *what)
     return ferr(err, code, "%s: %s at (%d, %d, %d)", what, derr_name(e[0]), e[1], e[2], e[3]);
 }
 
-int rates_and_lists(State *s, const uint8_t *d_ini, std::string &err)
+int rates_and_lists(State *s, const uint8_t *d_ini, std::string &err, const int32_t *d_ev = nullptr,
+                    const float *d_rate = nullptr)
 {
     int top = s->nrec + 1;
     SK(cudaMemcpyAsync(s->D.top, &top, sizeof top, cudaMemcpyHostToDevice, s->stream));
-    if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, d_ini, 1, top);
+    if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, d_ini, d_ev, d_rate, 1, top);
     SK(cudaGetLastError());
     int ntiles = s->D.ntx * s->D.nty;
     SK(cudaMemsetAsync(s->D.fr_n, 0, sizeof(int32_t) * ntiles, s->stream));
@@ -1299,7 +1309,7 @@ int set_rates(State *s, const double *ptransE, const double *ptransD, std::strin
         int top = 0;
         SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
         SK(cudaStreamSynchronize(s->stream));
-        if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, nullptr, 1, top);
+        if (top > 1) k_rate_all<<<grid_for(top), 256, 0, s->stream>>>(s->D, nullptr, nullptr, nullptr, 1, top);
         SK(cudaGetLastError());
         s->lists_ok = false;
         return check_device(s, err, "rates");
@@ -1377,7 +1387,7 @@ int from_compact(State *s, const uint8_t *d_st, int NA, int NB, int NZ, int pitc
 }
 
 int load_lists(State *s, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
-               const uint8_t *ini, std::string &err)
+               const int32_t *event, const float *rate, std::string &err)
 {
     Dev &D = s->D;
     if (n + 1 > D.rcap) return ferr(err, MKS_ERR_CAPACITY, "%lld list entries exceed the record pool", (long long)n);
@@ -1397,25 +1407,40 @@ int load_lists(State *s, const int32_t *lattcoo, int64_t n, const int32_t *xyz, 
     SK(cudaMemsetAsync(D.ind, 0, sizeof(int32_t) * s->ngrid, s->stream));
     SK(cudaMemcpyAsync(D.coo + ZG * plane, lattcoo, sizeof(int32_t) * plane * (D.lz + 1), cudaMemcpyHostToDevice,
                        s->stream));
-    int32_t *d_xyz = nullptr, *d_nn = nullptr;
+    if (event)
+        for (int64_t i = 0; i < n; i++)
+            if (event[i] != EV_NONE && event[i] != EV_DEP && event[i] != EV_DUMMY && event[i] != EV_EVAP &&
+                event[i] != EV_ISO)
+                return ferr(err, MKS_ERR_ARG, "event code %d of list entry %lld", event[i], (long long)i);
+    int32_t *d_xyz = nullptr, *d_nn = nullptr, *d_ev = nullptr;
+    float *d_rate = nullptr;
     uint8_t *d_ini = nullptr;
     size_t nb = (size_t)std::max<int64_t>(n, 1);
     SK(cudaMallocAsync(&d_xyz, sizeof(int32_t) * 3 * nb, s->stream));
     SK(cudaMallocAsync(&d_nn, sizeof(int32_t) * 12 * nb, s->stream));
     SK(cudaMallocAsync(&d_ini, nb + 2, s->stream));
-    SK(cudaMemsetAsync(d_ini, 0, nb + 2, s->stream));
+    SK(cudaMemsetAsync(d_ini, 1, nb + 2, s->stream));   // loading is an initialization: Get_Prob_Ini's dummy rate
+    if (event && rate) {
+        SK(cudaMallocAsync(&d_ev, sizeof(int32_t) * (nb + 1), s->stream));
+        SK(cudaMallocAsync(&d_rate, sizeof(float) * (nb + 1), s->stream));
+    }
     if (n) {
         SK(cudaMemcpyAsync(d_xyz, xyz, sizeof(int32_t) * 3 * n, cudaMemcpyHostToDevice, s->stream));
         SK(cudaMemcpyAsync(d_nn, nn, sizeof(int32_t) * 12 * n, cudaMemcpyHostToDevice, s->stream));
-        if (ini) SK(cudaMemcpyAsync(d_ini + 1, ini, (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        if (d_ev) {
+            SK(cudaMemcpyAsync(d_ev + 1, event, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
+            SK(cudaMemcpyAsync(d_rate + 1, rate, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+        }
         k_load_records<<<grid_for(n), 256, 0, s->stream>>>(D, d_xyz, d_nn, (long long)n);
         SK(cudaGetLastError());
     }
     s->nrec = (int)n;
-    int r = rates_and_lists(s, d_ini, err);
+    int r = rates_and_lists(s, d_ini, err, d_ev, d_rate);
     cudaFreeAsync(d_xyz, s->stream);
     cudaFreeAsync(d_nn, s->stream);
     cudaFreeAsync(d_ini, s->stream);
+    if (d_ev) cudaFreeAsync(d_ev, s->stream);
+    if (d_rate) cudaFreeAsync(d_rate, s->stream);
     SK(cudaStreamSynchronize(s->stream));
     s->time = 0.0;
     s->window = 0;
@@ -1473,7 +1498,7 @@ int run(State *s, double tau, int64_t max_windows, int64_t max_events, double ma
     while (max_windows <= 0 || w < max_windows) {
         int64_t nb = max_windows > 0 ? std::min<int64_t>(batch, max_windows - w) : batch;
         if (max_time > 0.0) {
-            int64_t left = (int64_t)ceil((max_time - s->time) / tau - 1e-9);
+            int64_t left = s->time < max_time ? std::max<int64_t>(1, (int64_t)ceil((max_time - s->time) / tau)) : 0;
             if (left <= 0) {
                 s->stop_reason = 3;
                 break;
@@ -1522,9 +1547,9 @@ int get_lattice(State *s, int32_t *lattcoo, std::string &err)
     return 0;
 }
 
-int get_lists(State *s, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *evc, float *rate,
-              int64_t *n, std::string &err)
+int sites(State *s, std::vector<Site> &out, std::string &err)
 {
+    out.clear();
     int top = 0;
     SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
     SK(cudaStreamSynchronize(s->stream));
@@ -1538,26 +1563,44 @@ int get_lists(State *s, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, i
     SK(cudaMemcpyAsync(word.data(), d_word, sizeof(int32_t) * (size_t)top, cudaMemcpyDeviceToHost, s->stream));
     cudaFreeAsync(d_word, s->stream);
     SK(cudaStreamSynchronize(s->stream));
-    int64_t k = 0;
-    bool write = xyz && nn && kind && evc && rate;
     for (int r = 1; r < top; r++) {
         const Rec &R = rec[r];
         if (R.x < 0) continue;
-        if (write && k < cap) {
-            uint32_t v = (uint32_t)word[r];
-            int kd = R.ev ? 1 : (((v >> 23) & 1) && ((v >> 24) & 7) == 4 ? 2 : (((v >> 24) & 7) == 4 ? 3 : 0));
-            xyz[3 * k] = R.x;
-            xyz[3 * k + 1] = R.y;
-            xyz[3 * k + 2] = R.z;
-            for (int i = 0; i < 4; i++)
-                for (int j = 0; j < 3; j++) nn[12 * k + 3 * i + j] = R.nn[i][j];
-            kind[k] = kd;
-            evc[k] = R.ev;
-            rate[k] = R.rate;
-        }
-        k++;
+        Site t;
+        t.x = R.x;
+        t.y = R.y;
+        t.z = R.z;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) t.nn[i][j] = R.nn[i][j];
+        t.word = (uint32_t)word[r];
+        t.ev = R.ev;
+        t.rate = R.rate;
+        out.push_back(t);
     }
-    *n = k;
+    return 0;
+}
+
+int get_lists(State *s, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *evc, float *rate,
+              int64_t *n, std::string &err)
+{
+    std::vector<Site> all;
+    int rc = sites(s, all, err);
+    if (rc) return rc;
+    *n = (int64_t)all.size();
+    if (!(xyz && nn && kind && evc && rate) || cap < *n) return 0;
+    for (size_t k = 0; k < all.size(); k++) {
+        const Site &t = all[k];
+        uint32_t v = t.word;
+        int kd = t.ev ? 1 : (((v >> 23) & 1) && ((v >> 24) & 7) == 4 ? 2 : (((v >> 24) & 7) == 4 ? 3 : 0));
+        xyz[3 * k] = t.x;
+        xyz[3 * k + 1] = t.y;
+        xyz[3 * k + 2] = t.z;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) nn[12 * k + 3 * i + j] = t.nn[i][j];
+        kind[k] = kd;
+        evc[k] = t.ev;
+        rate[k] = t.rate;
+    }
     return 0;
 }
 

@@ -14,6 +14,7 @@
 #pragma once
 #include <stdint.h>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include "../../include/mulskips_gpu.h"
 
@@ -34,10 +35,10 @@ int set_rates(State *s, const double *ptransE, const double *ptransD, std::strin
 // keeps 1e-6).
 int from_compact(State *s, const uint8_t *d_st, int NA, int NB, int NZ, int pitch, std::string &err);
 // The full reference state: LattCoo(0:lx-1, 0:ly-1, 0:lz) (x fastest) and
-// n list entries (grid point xyz[3i..], NextN nn[12i..]); ini[i] != 0 marks
-// an empty coor-1 site at Get_Prob_Ini's dummy rate (may be NULL).
+// n list entries (grid point xyz[3i..], NextN nn[12i..]), rated by
+// Get_Prob_Ini, or with the given event codes and rates (both non-NULL).
 int load_lists(State *s, const int32_t *lattcoo, int64_t n, const int32_t *xyz, const int32_t *nn,
-               const uint8_t *ini, std::string &err);
+               const int32_t *event, const float *rate, std::string &err);
 // Deposition.f / Evaporation.f applied to the events in order; a
 // deposition of coordination 1 takes its stacking from IF_Arm_Choice, the
 // trace's arm flag deciding a tie.  *done gets the events applied.
@@ -52,6 +53,15 @@ int get_lattice(State *s, int32_t *lattcoo, std::string &err);
 // and FP32 rate.  *n gets the count; arrays are written when cap >= *n.
 int get_lists(State *s, int64_t cap, int32_t *xyz, int32_t *nn, int32_t *kind, int32_t *ev, float *rate,
               int64_t *n, std::string &err);
+// Every listed site with its LattCoo word, for the host-side writers.
+struct Site {
+    int32_t x, y, z;
+    int32_t nn[4][3];
+    uint32_t word;
+    int32_t ev;
+    float rate;
+};
+int sites(State *s, std::vector<Site> &out, std::string &err);
 int observables(State *s, mks_observables *o, std::string &err);
 int clock(State *s, double *time, int64_t *window, int64_t *events);
 int status(State *s, mks_status *st);

@@ -221,19 +221,24 @@ class Lattice:
         assert a.size == lx * ly * (lz + 1)
         N.check(N.lib().mks_load_lattice(self._h, N.ptr(a)))
 
-    def load_lists(self, lattcoo, xyz, nn, ini=None):
+    def load_lists(self, lattcoo, xyz, nn, event=None, rate=None):
         """Arm-chair stacking (ptrans_zig < 1): the full reference state, LattCoo
         [z, y, x] and the list entries (grid points xyz (n, 3), NextN nn
-        (n, 4, 3); ini marks unsupported coor-1 sites at the init-time rate)."""
+        (n, 4, 3)), rated as an initializer rates them, or with the given
+        event codes (0 none, 1 deposition, 2 dummy, 4 evaporation) and rates."""
         a = np.ascontiguousarray(lattcoo, dtype=np.int32)
         lx, ly, lz = self.dims
         assert a.size == lx * ly * (lz + 1)
         p = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
         q = np.ascontiguousarray(nn, dtype=np.int32).reshape(-1, 4, 3)
         assert len(p) == len(q)
-        f = None if ini is None else np.ascontiguousarray(ini, dtype=np.uint8).reshape(-1)
+        e = r = None
+        if event is not None:
+            e = np.ascontiguousarray(event, dtype=np.int32).reshape(-1)
+            r = np.ascontiguousarray(rate, dtype=np.float32).reshape(-1)
+            assert e.size == len(p) and r.size == len(p)
         N.check(N.lib().mks_load_lists(self._h, N.ptr(a), len(p), N.ptr(p), N.ptr(q),
-                                       None if f is None else N.ptr(f)))
+                                       None if e is None else N.ptr(e), None if r is None else N.ptr(r)))
 
     def lists(self):
         """Arm-chair stacking: every listed site as a dict of xyz (n, 3), nn

@@ -36,9 +36,16 @@ def gpu_lists(lat):
     return key[order], {k: v[order] for k, v in e.items()}
 
 
-def ini_flags(e):
-    """Unsupported coor-1 sites still at Get_Prob_Ini's dummy rate 1e-6."""
-    return ((e["kind"] == 1) & (e["prob"] == float(np.float32(1e-6)))).astype(np.uint8)
+def oracle_events(e):
+    """The engine's event codes and FP32 rates of the oracle's list entries:
+    1 deposition, 2 the dummy of an unsupported coor-1 site (1e-8 or, still
+    from the initializer, 1e-6), 4 evaporation, 0 bulk atoms and voids."""
+    mc = e["kind"] == 1
+    dummy = mc & (e["ind_event"] <= 3) & ((e["prob"] == float(np.float32(1e-8))) |
+                                         (e["prob"] == float(np.float32(1e-6))))
+    ev = np.where(mc, np.where(e["ind_event"] <= 3, 1, 4), 0)
+    ev[dummy] = 2
+    return ev.astype(np.int32), np.where(mc, e["prob"], 0.0).astype(np.float32)
 
 
 def compare_state(ora, o, lat, where):
@@ -65,7 +72,8 @@ def compare_state(ora, o, lat, where):
 
 def load_from_oracle(ora, o, lat):
     e = ora.list_entries(o)
-    lat.load_lists(o.lattcoo(), e["xyz"], e["nn"], ini_flags(e))
+    ev, rate = oracle_events(e)
+    lat.load_lists(o.lattcoo(), e["xyz"], e["nn"], ev, rate)
 
 
 def stacking_replay(ora, startdat, warm, total, chunk, box=480):
@@ -110,15 +118,15 @@ def test_stacking_replay_from_start(oracle_lib):
     done, arm, off = stacking_replay(oracle_lib, CUBE_ZZ, 0, 600000, 150000)
     assert done == 600000
     assert arm > 1000, "the trace should hold arm-chair depositions"
-    assert off > 100, "atoms should sit off the diamond sub-grid"
 
 
 def test_stacking_replay_twinned_lattice(oracle_lib):
-    """From the oracle's state after 3e6 events (about 5 % of the atoms off
-    the diamond sub-grid): evaporation and growth around twinned atoms,
-    FIND_NN's rotations about non-<111> bonds and their rounding, replay
-    exactly."""
-    done, arm, off = stacking_replay(oracle_lib, CUBE_ZZ, 3000000, 500000, 250000)
+    """From the oracle's state after 8e6 events (atoms off the diamond
+    sub-grid in the thousands: 440 at 3e6 events, 2657 at 1e7), loaded with
+    its list entries and their saved rates: evaporation and growth around
+    twinned atoms, FIND_NN's rotations about non-<111> bonds and their
+    rounding, replay exactly."""
+    done, arm, off = stacking_replay(oracle_lib, CUBE_ZZ, 8000000, 500000, 250000)
     assert done == 500000
     assert off > 1000
 
@@ -155,36 +163,126 @@ def test_stacking_expands_initializer_lattice(oracle_lib):
     o.close()
 
 
-def test_stacking_run_grows_hexagonal_sites(oracle_lib):
-    """The synchronous-sublattice run with PtransZig = 0.8 on the cube
-    case: events happen, the lattice stays consistent (the engine checks the
-    census of every re-rated atom against its coordination, Get_Prob.f:
-    293-298), and atoms grow off the diamond sub-grid."""
+def test_stacking_frames_match_oracle_writer(oracle_lib, tmp_path):
+    """The frame files of an arm-chair stacking handle (WriteMolMolXYZFile.f:
+    22-406) against the oracle's writer on the same twinned state (the
+    oracle's cube-zigzag lattice after 3e6 events, loaded with its lists):
+    _d.xyz -- the non-epitaxial bulk atoms off the diamond sites, the
+    reference's own stacking-fault output -- and _w.xyz byte for byte; the
+    atom lines of .xyz in order and its voids, and the labelled voids of
+    _v.xyz, as sets (the reference lists voids in ListVoid order)."""
     from mulskips_gb300 import Lattice
     from mulskips_gb300.startdat import parse_startdat
     ora = oracle_lib
     d = parse_startdat(CUBE_ZZ)
     o = ora.Oracle(CUBE_ZZ, 480, 480, 480)
     o.init()
+    o.run(8000000)
     pE, pD = o.rates()
-    o.close()
     with Lattice(480, 480, 480, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"],
-                 ptrans_zig=d["ptrans_zig"], seed=7) as lat:
+                 ptrans_zig=d["ptrans_zig"]) as lat:
         lat.set_rates(pE, pD)
+        load_from_oracle(ora, o, lat)
+        lat.write_frame(str(tmp_path / "g"), 1.5, 8000000)
+    o.write_frame(str(tmp_path / "o"), 1.5, 8000000)
+    o.close()
+
+    def read(name):
+        return (tmp_path / name).read_text().splitlines()
+
+    assert read("g_d.xyz") == read("o_d.xyz")
+    assert int(read("g_d.xyz")[0].split()[0]) > 200, "the twinned lattice holds non-epitaxial bulk atoms"
+    assert read("g_w.xyz") == read("o_w.xyz")
+    g, r = read("g.xyz"), read("o.xyz")
+    assert g[:2] == r[:2]
+    ga = [x for x in g[2:] if not x.startswith("O ")]
+    ra = [x for x in r[2:] if not x.startswith("O ")]
+    assert ga == ra
+    assert sorted(x for x in g[2:] if x.startswith("O ")) == sorted(x for x in r[2:] if x.startswith("O "))
+    gv, rv = read("g_v.xyz"), read("o_v.xyz")
+    assert gv[:2] == rv[:2] and sorted(gv[2:]) == sorted(rv[2:])
+
+
+# ---------------------------------------------------------------- statistics
+NSEEDS = 32
+T_OBS = 1.2e6          # s: about 3e6 events of the serial reference
+
+
+def stacking_observables(lg):
+    """From LattCoo [z, y, x] (z < LenZ): atoms, C atoms, atoms off the
+    diamond sub-grid, and the non-epitaxial bulk atoms of _d.xyz
+    (WriteMolMolXYZFile.f:120-160: coordination 4 on a grid point that is not
+    a diamond site)."""
+    z, y, x = np.nonzero(lg)
+    v = lg[z, y, x]
+    atom = (((v >> 23) & 1) == 1) & ((v & 255) != 113)
+    dia = (x % 3 == 0) & (y % 3 == 0) & (z % 3 == 0)
+    x1, y1, z1 = x // 3, y // 3, z // 3
+    dia &= ((x1 & 1) == (y1 & 1)) & ((x1 & 1) == (z1 & 1)) & (((x1 + y1 + z1) & 3) % 3 == 0)
+    co4 = ((v >> 24) & 7) == 4
+    return {"atoms": int(atom.sum()), "C": int((atom & (((v >> 27) & 7) == 2)).sum()),
+            "off-grid atoms": int((atom & ~dia).sum()), "non-epitaxial bulk": int((atom & co4 & ~dia).sum())}
+
+
+def _oracle_seed(args):
+    path, t_obs = args
+    from oracle import ora
+    o = ora.Oracle(path, 480, 480, 480)
+    o.init()
+    o.run_until(t_obs)
+    out = stacking_observables(o.lattcoo()[:480])
+    out["events"] = o.iter
+    o.close()
+    return out
+
+
+def _gpu_seed(args):
+    seed, d, t_obs, f = args
+    from mulskips_gb300 import Lattice
+    with Lattice(480, 480, 480, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"],
+                 ptrans_zig=d["ptrans_zig"], seed=seed) as lat:
+        lat.set_rates(d["ptransE"], d["ptransD"])
         lat.init_shape("C", d["len"])
-        tau = lat.suggest_tau(0.03)
-        n, t = lat.run(tau, 200)
-        assert n > 100000
-        ob = lat.observables()
-        lg = lat.lattcoo()
-        z, y, x = np.nonzero(lg[:480])
-        v = lg[:480][z, y, x]
-        occ = ((v >> 23) & 1) == 1
-        off = occ & ((x % 3 != 0) | (y % 3 != 0) | (z % 3 != 0))
-        assert np.count_nonzero(off) > 50
-        assert ob["atoms"] == int(np.count_nonzero(occ & ((v & 255) != 113)))
-        # lists are consistent with the lattice: every atom and every
-        # coordinated empty site is listed once
-        e = lat.lists()
-        assert len(np.unique(e["xyz"], axis=0)) == len(e["xyz"])
-        assert np.all(e["kind"] > 0)
+        t, events, windows = 0.0, 0, 0
+        while t < t_obs:
+            tau = lat.suggest_tau(f)        # the window follows the state, as mulskips.e re-suggests it
+            n, t1 = lat.run(tau, 64, 0, t_obs)
+            assert t1 > t
+            t = t1
+            events += n
+            windows += 64
+        out = stacking_observables(lat.lattcoo()[:480])
+        out["events"] = events
+        return out
+
+
+def test_stacking_statistics_match_serial_reference(tmp_path):
+    """The sublattice KMC with arm-chair stacking against the serial
+    reference: the cube-zigzag case (SiC rates of its start.dat, PtransZig =
+    0.8), RunType R, 32 oracle seeds and 32 GPU replicas observed at t =
+    1.2e6 s (about 3e6 events): atoms, C atoms, atoms off the diamond
+    sub-grid and non-epitaxial bulk atoms -- the stacking-fault density --
+    each inside its 95 % family band (Welch t, Bonferroni over the four)."""
+    import multiprocessing as mp
+    from concurrent.futures import ThreadPoolExecutor
+    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.startdat import parse_startdat
+    from stat_bands import Family
+    txt = open(CUBE_ZZ).read().replace("T   ! R = production run", "R   ! R = production run")
+    paths = []
+    for s in range(NSEEDS):
+        p = tmp_path / f"zz{s}.dat"
+        p.write_text(txt.replace("9117116 ! Random seed", f"{900 + s} ! Random seed"))
+        paths.append(str(p))
+    d = parse_startdat(paths[0])
+    assert d["run_type"] == "R" and d["ptrans_zig"] == 0.8
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        ref = pool.map(_oracle_seed, [(p, T_OBS) for p in paths])
+    f = accurate_f(2)
+    with ThreadPoolExecutor(8) as ex:
+        gpu = list(ex.map(_gpu_seed, [(31 + s, d, T_OBS, f) for s in range(NSEEDS)]))
+    fam = Family(f"cube-zigzag, PtransZig = 0.8, t = {T_OBS:g} s, f = {f}", 4)
+    for k in ("atoms", "C", "off-grid atoms", "non-epitaxial bulk"):
+        fam.add(k, np.array([g[k] for g in gpu], float), np.array([r[k] for r in ref], float))
+    assert np.mean([r["off-grid atoms"] for r in ref]) > 100
+    fam.check()
