@@ -16,8 +16,10 @@ host buffers, timed on the host: the lattice uploaded from pinned memory,
 the windows, then the step's result as the reference writes it (the frame's
 site list and the observables) read back.
 Side lines (not the headline): `batched` (512 small replicas), `la_gradient`
-(the SiGe laser-anneal gradient) and `cvd` (Si(001) + H, one coverage
-species, with the serial oracle's events/s on the reference's 480^3 case).
+(the SiGe laser-anneal gradient), `cvd` (Si(001) + H, one coverage
+species, with the serial oracle's events/s on the reference's 480^3 case) and
+`stacking` (3C-SiC with arm-chair stacking, PtransZig < 1, on the
+explicit-neighbour engine).
 `--impl reference`: the reference CPU path (the oracle restatement; the
 Fortran reference has no compiler here) on all host cores.
 """
@@ -281,6 +283,7 @@ def gb300(args, rank, world):
     batched = batched_bench(args) if not args.no_batched else None
     la_grad = la_gradient_bench() if not args.no_batched else None
     cvd = cvd_bench() if not args.no_batched else None
+    stacking = stacking_bench() if not args.no_batched else None
     base_v, base_ev, base_runs, base_slab = cpu_baseline(seconds=args.cpu_seconds, cores=1)
     all_cores = os.cpu_count() or 1
     all_v, _, _, _ = cpu_baseline(seconds=args.cpu_seconds, cores=all_cores)
@@ -325,6 +328,7 @@ def gb300(args, rank, world):
         "batched": batched,
         "la_gradient": la_grad,
         "cvd": cvd,
+        "stacking": stacking,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -440,6 +444,66 @@ def cvd_bench(windows=4096, oracle_events=3000000):
             "oracle_events_per_s": n / cdt, "oracle_events": int(n),
             "workload": "Si(001) + H CVD, rates of the reference's CVD-Si-SiH2 case, 3072x3072x240 grid, "
                         "Len1=48, f=0.3; oracle: the reference's 480^3 case, serial, 1 core"}
+
+
+PZIG_1600K = 1.0 / (1.0 + math.exp(-0.02 / (0.00008617330350 * 1600.0)))   # 0.5362
+
+
+def stacking_bench(side=1536, cube=960, warm_blocks=24, windows=1024, oracle_events=2000000):
+    """Config 2 (3C-SiC with stacking faults): arm-chair stacking on the
+    explicit-neighbour engine.  A 3C-SiC parallelepiped (SetNC, `cube` grid
+    units a side, 80 cells) in a 128^3-cell box (1536^3 grid), the SiC rates
+    of the reference's cube-zigzag case, PtransZig = 1 / (1 + exp(-0.02 eV /
+    kT)) at 1600 K (a 0.02 eV preference for cubic stacking on ties).  The
+    config's own rates (barriers U(0.4, 0.9) eV at 1600 K) evaporate every
+    atom far faster than a flux of 1 ML/s deposits, so nothing would grow or
+    stack; the cube-zigzag rates grow the crystal and form stacking faults.
+    Window factor f = 0.01 (two species), re-suggested for each of the
+    warm-up's blocks of 64 windows while the fast C adatoms of the initial
+    faces evaporate; then events/s over `windows` windows at the median of
+    the last warm-up suggestions (a single fast site can make one suggestion
+    tiny for a moment), wall time of the synchronous call, with the
+    non-epitaxial bulk count (_d.xyz); against the serial oracle on the
+    reference's 480^3 cube-zigzag case (RunType R, one core)."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.startdat import parse_startdat
+    from oracle import ora
+    path = os.path.join(ROOT, "tests", "golden", "cube-zigzag", "start.dat")
+    d = parse_startdat(path)
+    f = accurate_f(2)
+    lat = Lattice(side, side, side, ncrystal=2, list_crystal=d["list_crystal"], sf=d["sf"], ptrans_zig=PZIG_1600K,
+                  seed=11)
+    lat.set_rates(d["ptransE"], d["ptransD"])
+    lat.init_shape("C", [cube, cube, cube])
+    taus = []
+    for _ in range(warm_blocks):
+        taus.append(lat.suggest_tau(f))
+        lat.run(taus[-1], 64)
+    tau = float(sorted(taus[warm_blocks // 2:])[len(taus[warm_blocks // 2:]) // 2])
+    t0 = time.perf_counter()
+    n, tsim = lat.run(tau, windows)
+    wall = time.perf_counter() - t0
+    obs = lat.observables()
+    lat.close()
+    txt = open(path).read().replace("T   ! R = production run", "R   ! R = production run")
+    tmp = tempfile.mkdtemp()
+    p = os.path.join(tmp, "start.dat")
+    open(p, "w").write(txt)
+    o = ora.Oracle(p, 480, 480, 480, numbers=None)
+    o.init()
+    c0 = time.perf_counter()
+    o.run(oracle_events)
+    cdt = time.perf_counter() - c0
+    m = o.iter - 1
+    o.close()
+    shutil.rmtree(tmp, ignore_errors=True)
+    return {"value": n / wall, "unit": "events/s", "events": int(n), "windows": windows, "tau_s": tau,
+            "sim_time_s": tsim, "atoms": int(obs["atoms"]), "nonepitaxial_bulk": int(obs["nonepitaxial"]),
+            "ptrans_zig": PZIG_1600K, "oracle_events_per_s": m / cdt, "oracle_events": int(m),
+            "workload": f"3C-SiC parallelepiped (SetNC, {cube} grid units a side) in a {side}^3 grid (128^3 cells), "
+                        "rates of the reference's cube-zigzag case, PtransZig 0.5362 (0.02 eV at 1600 K), f = 0.01; "
+                        "oracle: the reference's 480^3 cube-zigzag case, serial, 1 core"}
 
 
 def la_gradient_bench():

@@ -2055,16 +2055,12 @@ int stk_unsupported(const char *what)
 int stk_suggest_tau(mks_handle *h, double f, double *tau)
 {
     std::string err;
-    int64_t n = 0;
-    int rc = mks_stk::get_lists(h->stk, 0, nullptr, nullptr, nullptr, nullptr, nullptr, &n, err);
-    if (rc) return fail(rc, "%s", err.c_str());
-    std::vector<int32_t> xyz(3 * (size_t)n + 3), nn(12 * (size_t)n + 12), kind((size_t)n + 1), ev((size_t)n + 1);
-    std::vector<float> rate((size_t)n + 1);
-    rc = mks_stk::get_lists(h->stk, n, xyz.data(), nn.data(), kind.data(), ev.data(), rate.data(), &n, err);
+    std::vector<float> rate;
+    int rc = mks_stk::event_rates(h->stk, rate, err);
     if (rc) return fail(rc, "%s", err.c_str());
     std::vector<std::pair<float, double>> share;
-    std::sort(rate.begin(), rate.begin() + n);
-    for (int64_t i = 0; i < n; i++) {
+    std::sort(rate.begin(), rate.end());
+    for (size_t i = 0; i < rate.size(); i++) {
         if (!(rate[i] > 1.e-6f)) continue;
         if (!share.empty() && share.back().first == rate[i]) share.back().second += rate[i];
         else share.push_back({rate[i], rate[i]});

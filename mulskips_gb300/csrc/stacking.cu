@@ -21,10 +21,12 @@
 // lanes sum the rates of the tile's list and find the drawn entry with a
 // prefix scan, lane 0 applies the event (Deposition.f / Evaporation.f,
 // serial by nature: every step reads what the previous one wrote).
-// Each tile keeps a list of record ids with an event.  An event of tile A may
-// give a site of an idle neighbour tile B its event; B's list then grows by
-// an atomic append.  At the start of its phase a tile compacts its list
-// (drops entries that lost their event, moved to another tile or repeat).
+// Each tile keeps a list of record ids with an event and, beside it, their
+// rates (contiguous floats for the selection scans; every rate change writes
+// the record's list slot).  An event of tile A may give a site of an idle
+// neighbour tile B its event; B's list then grows by an atomic append.  At
+// the start of its phase a tile compacts its list once a quarter of its
+// entries are dead.
 // Records freed by a tile wait on its pending stack until its next phase, so
 // a record never changes its site while a list entry of the running phase
 // could still select it.
@@ -53,7 +55,7 @@ constexpr int TWMIN = 24;           // smallest tile side (grid units)
 constexpr int LCAP = 4096;          // list entries per tile
 constexpr int FCAP = 1024;          // free records per tile and stack
 enum : uint8_t { EV_NONE = 0, EV_DEP = 1, EV_DUMMY = 2, EV_EVAP = 4, EV_ISO = 5 };
-enum : uint8_t { F_LISTED = 1, F_SEEN = 2 };
+enum : uint8_t { F_LISTED = 1 };
 // device error codes (err[0]); err[1..3] say where
 enum { E_INVARIANT = 3, E_CAPACITY = 4, E_NOTAPPLICABLE = 7, E_BOUNDS = 8, E_NBUFF = 9, E_ARM = 10 };
 
@@ -62,8 +64,9 @@ struct Rec {
     int16_t nn[4][3];
     uint8_t ev, flags;
     float rate;
+    int32_t slot;          // position in its tile's list while F_LISTED
 };
-static_assert(sizeof(Rec) == 36, "record layout");
+static_assert(sizeof(Rec) == 40, "record layout");
 
 struct P3 {
     int x, y, z;
@@ -76,6 +79,7 @@ struct Dev {
     int lx, ly, lz;
     int tw, ntx, nty;
     int32_t *tl, *tl_n;        // tile lists [tile][LCAP] and their lengths
+    float *tr;                 // the listed sites' rates beside tl: > 0 a rate, -1 an isolated atom, 0 none
     int32_t *fr, *fr_n;        // reusable records per tile [tile][FCAP]
     int32_t *fp, *fp_n;        // records freed in the tile's current phase
     int32_t *top;              // records handed out so far (+1: rec[0] is the guard)
@@ -155,6 +159,12 @@ __device__ __forceinline__ bool rec_lists(const Dev &D, int r, P3 s)
     return in_list(nn, s);
 }
 
+// the selection weight of a record in its tile list
+__device__ __forceinline__ float list_rate(const Rec &R)
+{
+    return R.ev == EV_NONE ? 0.f : (R.ev == EV_ISO ? -1.f : R.rate);
+}
+
 __device__ __forceinline__ double pd_of(const Dev &D, int s, int coor) { return D.pd[(s - 1) * 3 + coor - 1]; }
 
 // Get_Prob (Get_Prob.f:54-331) without coverage: the event code and FP32 rate
@@ -224,14 +234,16 @@ __device__ void list_site(const Dev &D, const Ctx &c, int r)
     if (c.tile < 0) return;               // replay: the lists are rebuilt before a run
     Rec &R = D.rec[r];
     if (R.flags & F_LISTED) return;
-    R.flags |= F_LISTED;
     int t = tile_of(D, R.x, R.y);
     int k = atomicAdd(&D.tl_n[t], 1);
     if (k >= LCAP) {
         set_err(D, E_CAPACITY, t, k, 0);
         return;
     }
+    R.flags |= F_LISTED;
+    R.slot = k;
     D.tl[(int64_t)t * LCAP + k] = r;
+    D.tr[(int64_t)t * LCAP + k] = list_rate(R);
 }
 
 __device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
@@ -244,7 +256,9 @@ __device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
     c.dmc += (ev != 0) - (R.ev != 0);
     R.ev = ev;
     R.rate = rate;
-    if (ev) list_site(D, c, r);
+    if (c.tile < 0) return;               // replay: the lists are rebuilt before a run
+    if (R.flags & F_LISTED) D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = list_rate(R);
+    else if (ev) list_site(D, c, r);
 }
 
 __device__ int alloc_rec(const Dev &D, const Ctx &c)
@@ -309,6 +323,7 @@ __device__ void drop_site(const Dev &D, Ctx &c, P3 p)
     D.ind[g] = 0;
     Rec &R = D.rec[r];
     c.dmc -= R.ev != 0;
+    if (c.tile >= 0 && (R.flags & F_LISTED)) D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = 0.f;
     R.ev = EV_NONE;
     R.flags = 0;
     R.rate = 0.f;
@@ -680,6 +695,7 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
     const int t = tj * D.ntx + ti;
     if (*(volatile int32_t *)D.err || *(volatile int32_t *)D.stop) return;
     int32_t *list = D.tl + (int64_t)t * LCAP;
+    float *rates = D.tr + (int64_t)t * LCAP;
     // records freed in the tile's last phase become reusable
     if (lane == 0) {
         int np = D.fp_n[t], nr = D.fr_n[t];
@@ -687,33 +703,52 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
         D.fr_n[t] = nr;
         D.fp_n[t] = 0;
     }
-    // compact the list: keep each record once if it is still in this tile and
-    // still has an event; a dropped record without an event may be listed again
-    int n = min(D.tl_n[t], LCAP);
-    int out = 0;
-    for (int base = 0; base < n; base += 32) {
-        int i = base + lane;
-        int r = i < n ? list[i] : 0;
-        bool keep = false;
-        if (r > 0) {
-            Rec &R = D.rec[r];
-            bool mine = R.x >= 0 && tile_of(D, R.x, R.y) == t;
-            if (mine && R.ev == EV_NONE) R.flags &= (uint8_t)~F_LISTED;
-            keep = mine && R.ev != EV_NONE && !(R.flags & F_SEEN);
+    // compact the list once a quarter of it is dead.  An entry with a nonzero
+    // rate is its record's current entry (a freed record's entry is zeroed,
+    // and a record is appended again only after its entry was dropped); an
+    // entry with rate 0 is kept only if it is the current entry (slot) of a
+    // live record of this tile whose event has a zero rate, otherwise
+    // dropped, and a record of this tile without an event whose current entry
+    // it was may be listed again
+    const int n = min(D.tl_n[t], LCAP);
+    int dead = 0;
+    for (int i = lane; i < n; i += 32) dead += rates[i] == 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dead += __shfl_xor_sync(FULL, dead, o);
+    if (dead && (4 * dead > n || n > 3 * LCAP / 4)) {
+        int out = 0;
+        for (int base = 0; base < n; base += 32) {
+            const int i = base + lane;
+            int r = 0;
+            float v = 0.f;
+            bool keep = false;
+            if (i < n) {
+                r = list[i];
+                v = rates[i];
+                if (v != 0.f) {
+                    keep = true;
+                } else if (r > 0) {
+                    Rec &R = D.rec[r];
+                    const bool cur = R.x >= 0 && (R.flags & F_LISTED) && R.slot == i && tile_of(D, R.x, R.y) == t;
+                    if (cur && R.ev != EV_NONE) keep = true;
+                    else if (cur) R.flags &= (uint8_t)~F_LISTED;
+                }
+            }
+            const unsigned km = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (keep) {
+                const int pos = out + __popc(km & lanemask_lt());
+                if (pos != i) {
+                    list[pos] = r;
+                    rates[pos] = v;
+                    D.rec[r].slot = pos;
+                }
+            }
+            out += __popc(km);
+            __syncwarp();
         }
-        unsigned grp = __match_any_sync(FULL, r);
-        keep = keep && lane == __ffs(grp) - 1;
-        unsigned km = __ballot_sync(FULL, keep);
-        __syncwarp();
-        if (keep) {
-            D.rec[r].flags |= F_SEEN;
-            list[out + __popc(km & lanemask_lt())] = r;
-        }
-        out += __popc(km);
-        __syncwarp();
+        if (lane == 0) D.tl_n[t] = out;
     }
-    for (int i = lane; i < out; i += 32) D.rec[list[i]].flags &= (uint8_t)~F_SEEN;
-    if (lane == 0) D.tl_n[t] = out;
     __syncwarp();
 
     Ctx c;
@@ -731,10 +766,9 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
         float s = 0.f;
         int niso = 0;
         for (int i = lane; i < len; i += 32) {
-            const Rec &R = D.rec[list[i]];
-            if (R.ev == EV_NONE || R.x < 0) continue;
-            if (R.ev == EV_ISO) niso++;
-            else s += R.rate;
+            const float v = rates[i];
+            if (v > 0.f) s += v;
+            else if (v < 0.f) niso++;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -756,11 +790,7 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
             int k = min((int)(u01(rnd.z) * (float)niso), niso - 1);
             for (int base = 0; base < len && pick < 0; base += 32) {
                 int i = base + lane;
-                bool hit = false;
-                if (i < len) {
-                    const Rec &R = D.rec[list[i]];
-                    hit = R.ev == EV_ISO && R.x >= 0;
-                }
+                const bool hit = i < len && rates[i] < 0.f;
                 unsigned m = __ballot_sync(FULL, hit);
                 if (k < __popc(m)) {
                     unsigned sel = __ballot_sync(FULL, hit && __popc(m & lanemask_lt()) == k);
@@ -774,11 +804,7 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
             int last = -1;
             for (int base = 0; base < len && pick < 0; base += 32) {
                 int i = base + lane;
-                float v = 0.f;
-                if (i < len) {
-                    const Rec &R = D.rec[list[i]];
-                    if (R.ev != EV_NONE && R.ev != EV_ISO && R.x >= 0) v = R.rate;
-                }
+                float v = i < len ? fmaxf(rates[i], 0.f) : 0.f;
                 float cum = v;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -893,14 +919,16 @@ __global__ void k_rebuild(Dev D, int last)
         R.flags = 0;
         if (R.x < 0 || R.ev == EV_NONE) continue;
         atomicAdd(D.nmc, 1);
-        R.flags = F_LISTED;
         int t = tile_of(D, R.x, R.y);
         int k = atomicAdd(&D.tl_n[t], 1);
         if (k >= LCAP) {
             set_err(D, E_CAPACITY, t, k, 1);
             continue;
         }
+        R.flags = F_LISTED;
+        R.slot = k;
         D.tl[(int64_t)t * LCAP + k] = r;
+        D.tr[(int64_t)t * LCAP + k] = list_rate(R);
     }
 }
 
@@ -1025,6 +1053,17 @@ __global__ void k_gather(Dev D, int last, int32_t *word)
     for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
         const Rec &R = D.rec[r];
         word[r] = R.x >= 0 ? (int32_t)cw(D, P3{R.x, R.y, R.z}) : 0;
+    }
+}
+
+// FP32 rates of the sites whose event has a table rate (no dummy, no
+// isolated atom), compacted into out
+__global__ void k_event_rates(Dev D, int last, float *out, int32_t *cnt)
+{
+    for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
+        const Rec &R = D.rec[r];
+        if (R.x < 0 || (R.ev != EV_DEP && R.ev != EV_EVAP) || !(R.rate > 0.f)) continue;
+        out[atomicAdd(cnt, 1)] = R.rate;
     }
 }
 
@@ -1248,6 +1287,7 @@ int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string 
     SA(D.ind, sizeof(int32_t) * s->ngrid);
     SA(D.rec, sizeof(Rec) * (size_t)rcap);
     SA(D.tl, sizeof(int32_t) * (size_t)ntiles * LCAP);
+    SA(D.tr, sizeof(float) * (size_t)ntiles * LCAP);
     SA(D.tl_n, sizeof(int32_t) * ntiles);
     SA(D.fr, sizeof(int32_t) * (size_t)ntiles * FCAP);
     SA(D.fr_n, sizeof(int32_t) * ntiles);
@@ -1286,6 +1326,7 @@ void destroy(State *s)
     cudaFree(D.ind);
     cudaFree(D.rec);
     cudaFree(D.tl);
+    cudaFree(D.tr);
     cudaFree(D.tl_n);
     cudaFree(D.fr);
     cudaFree(D.fr_n);
@@ -1577,6 +1618,31 @@ int sites(State *s, std::vector<Site> &out, std::string &err)
         t.rate = R.rate;
         out.push_back(t);
     }
+    return 0;
+}
+
+int event_rates(State *s, std::vector<float> &out, std::string &err)
+{
+    out.clear();
+    int top = 0;
+    SK(cudaMemcpyAsync(&top, s->D.top, sizeof top, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    if (top <= 1) return 0;
+    float *d_out = nullptr;
+    int32_t *d_cnt = nullptr;
+    SK(cudaMallocAsync(&d_out, sizeof(float) * (size_t)top, s->stream));
+    SK(cudaMallocAsync(&d_cnt, sizeof(int32_t), s->stream));
+    SK(cudaMemsetAsync(d_cnt, 0, sizeof(int32_t), s->stream));
+    k_event_rates<<<grid_for(top), 256, 0, s->stream>>>(s->D, top, d_out, d_cnt);
+    SK(cudaGetLastError());
+    int32_t n = 0;
+    SK(cudaMemcpyAsync(&n, d_cnt, sizeof n, cudaMemcpyDeviceToHost, s->stream));
+    SK(cudaStreamSynchronize(s->stream));
+    out.resize((size_t)n);
+    if (n) SK(cudaMemcpyAsync(out.data(), d_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    cudaFreeAsync(d_out, s->stream);
+    cudaFreeAsync(d_cnt, s->stream);
+    SK(cudaStreamSynchronize(s->stream));
     return 0;
 }
 

@@ -62,6 +62,9 @@ struct Site {
     float rate;
 };
 int sites(State *s, std::vector<Site> &out, std::string &err);
+// FP32 rates of the sites with a deposition or evaporation (dummies and
+// isolated atoms left out), in no particular order.
+int event_rates(State *s, std::vector<float> &out, std::string &err);
 int observables(State *s, mks_observables *o, std::string &err);
 int clock(State *s, double *time, int64_t *window, int64_t *events);
 int status(State *s, mks_status *st);

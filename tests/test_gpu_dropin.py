@@ -85,3 +85,30 @@ def test_cvd_start_dat_runs_with_coverage(tmp_path):
     lines = (d / "I00000001.xyz").read_text().splitlines()
     nh = sum(1 for ln in lines[2:] if ln.startswith("H "))
     assert int(lines[0].split()[0]) == len(lines) - 2 and nh > 500
+
+
+def test_arm_chair_start_dat_runs(tmp_path):
+    """The reference's cube-zigzag start.dat (3C-SiC parallelepiped, SetNC,
+    PtransZig = 0.8: arm-chair stacking on ties, IF_Arm_Choice.f:44-51) cut
+    to 1e6 events: mulskips.e runs it on the explicit-neighbour engine, its
+    initial frame equals the reference's byte for byte, and every frame file
+    (.xyz, the non-epitaxial bulk of _d.xyz, _v, and _w for SiC) is written
+    with a header count that matches its lines."""
+    d = tmp_path / "zz"
+    d.mkdir()
+    txt = open(os.path.join(GOLDEN, "cube-zigzag", "start.dat")).read()
+    txt = txt.replace("10000000 ! IterMax", "1000000 ! IterMax").replace("10000000  ! OutMolMol",
+                                                                          "1000000  ! OutMolMol")
+    assert "1000000 ! IterMax" in txt
+    (d / "start.dat").write_text(txt)
+    r = run_exe(d)
+    assert r.returncode == 0, r.stdout[-3000:]
+    with gzip.open(os.path.join(GOLDEN, "cube-zigzag", "I00000000.xyz.gz"), "rb") as f:
+        gold = f.read()
+    assert (d / "I00000000.xyz").read_bytes() == gold
+    for name in ("I00000001.xyz", "I00000001_d.xyz", "I00000001_v.xyz", "I00000001_w.xyz"):
+        lines = (d / name).read_text().splitlines()
+        assert int(lines[0].split()[0]) == len(lines) - 2, name
+    hdr = (d / "I00000001.xyz").read_text().splitlines()[0].split()
+    assert int(hdr[-1]) >= 1000000
+    assert "NatNvoidNad" in r.stdout
