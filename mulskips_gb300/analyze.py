@@ -124,7 +124,8 @@ def height_stats(st):
 
 def state_observables(st, cov=False):
     """Counts and column statistics of compact state st as mks_get_observables
-    defines them: atoms, atoms per species, covered sites (coverage mode),
+    defines them: atoms, atoms per species, covered sites (coverage mode;
+    covered2 those of the second coverage species, bit 7 of a covered byte),
     mean height and RMS roughness of the columns (grid units)."""
     st = np.asarray(st, dtype=np.uint8)
     sp = st & 3
@@ -133,4 +134,5 @@ def state_observables(st, cov=False):
     atom = (sp != 0) & notwall & ~covered
     m, r = height_stats(np.where(covered, 0, st).astype(np.uint8))
     return {"atoms": int(atom.sum()), "species": [int(((sp == s) & atom).sum()) for s in (1, 2, 3)],
-            "covered": int(covered.sum()), "mean_height": m, "rms_roughness": r}
+            "covered": int(covered.sum()), "covered2": int((covered & ((st & 0x80) != 0)).sum()),
+            "mean_height": m, "rms_roughness": r}

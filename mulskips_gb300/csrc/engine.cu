@@ -60,7 +60,7 @@ struct RepDev {
     int NA, NB, NZ, pitch;
     int nqa, nqb, quad_base;
     int single;              // NCrystal = 1: only species 1 on the lattice
-    int cov;                 // one coverage species: species value 3 is a covered empty site
+    int cov;                 // coverage species (0..2): species value 3 is a covered empty site, bit 7 which
     double tau, T0, t_max;
     long long ev_max;
     unsigned long long seed;
@@ -70,7 +70,8 @@ struct RepDev {
     int active, stop_reason;
     int qshift;              // brick tiling: columns by which the tiles of odd rows are shifted (0: square grid)
     float rate[64];          // per class; CLS_ISO is computed per event
-    float spcum[3][3];       // per coordination: cumulative fractions of species 1, 1+2, all deposition
+    float spcum[3][4];       // per coordination: cumulative fractions of species 1, 1+2, all deposition,
+                             // deposition + absorption of coverage species 1
 };
 
 struct QuadDev {
@@ -360,7 +361,7 @@ __global__ void k_class_hist(const RepDev *reps, const QuadDev *quads, int q0, i
             int a = Q.a0 + ia, b = Q.b0 + ib;
             if ((a + b + (z >> 1)) & 1) continue;
             if (!event_byte(L.get(a, b, z))) continue;
-            atomicAdd(&sh[site_class(L, a, b, z, false, R.cov != 0)], 1u);
+            atomicAdd(&sh[site_class(L, a, b, z, false, R.cov != 0, R.cov == 2)], 1u);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < NCLASS; i += blockDim.x)
@@ -519,7 +520,7 @@ __global__ void k_site_rates(const RepDev *reps, int rep, const uint8_t *st_all,
             rate[i] = 0.f;
             continue;
         }
-        int c = site_class(L, a, b, z1, R.single != 0, R.cov != 0);
+        int c = site_class(L, a, b, z1, R.single != 0, R.cov != 0, R.cov == 2);
         float r = 0.f;
         if (c != CLS_ISO && c != CLS_NONE)
             r = A ? la_rate(*A, c, la_temp_at(*A, a, b, z1, R.T0)) : R.rate[c];
@@ -544,7 +545,7 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
                   ((y1 & 1) == (z1 & 1)) && e.x >= 0 && e.y >= 0 && z1 >= 0 && z1 < R.NZ && a < R.NA &&
                   b < R.NB && e.arm == 0;
         const bool cov = R.cov != 0;
-        int c = ok ? site_class(L, a, b, z1, false, cov) : CLS_NONE;
+        int c = ok ? site_class(L, a, b, z1, false, cov, R.cov == 2) : CLS_NONE;
         bool atom_cls = c == CLS_ISO || ((cov ? c >= CLS_COV0 : c >= CLS_OCC0) && c < CLS_C1I);
         Touched tc;
         int err = 1;
@@ -553,10 +554,11 @@ __global__ void k_replay(const RepDev *reps, uint8_t *st_all, const mks_event *e
                 err = apply_deposition(L, a, b, z1, e.itrans, tc, cov);
             else if (e.itrans == 4 && atom_cls)
                 err = apply_evaporation(L, a, b, z1, tc, cov);
-            else if (cov && e.itrans == 5 && c >= CLS_D1 && c < CLS_COV0)   // desorption, main.f:346-349
-                err = apply_coverage(L, a, b, z1, false, tc);
-            else if (cov && e.itrans == 6 && c >= CLS_C1 && c <= CLS_C3 && c != CLS_C1D)   // absorption, :350-356
-                err = apply_coverage(L, a, b, z1, true, tc);
+            else if (cov && e.itrans == 5 &&
+                     ((c >= CLS_D1 && c < CLS_COV0) || (R.cov == 2 && c >= CLS_D2 && c < CLS_D2 + 3)))
+                err = apply_coverage(L, a, b, z1, false, tc);    // desorption, main.f:346-349
+            else if (cov && e.itrans >= 6 && e.itrans - 5 <= R.cov && c >= CLS_C1 && c <= CLS_C3 && c != CLS_C1D)
+                err = apply_coverage(L, a, b, z1, true, tc, e.itrans - 5);   // absorption of ListCov(Itrans-5), :350-356
         }
         if (err) {
             set_error(status, DERR_INVARIANT, (int)i);
@@ -574,7 +576,7 @@ struct __align__(128) TileShared {
     uint16_t pos[QMAX * QMAX * WMAX];          // list slot of each listed tile site (others stale: checked against list)
     int cnt[64];
     float rate[64];
-    float spcum[3][3];
+    float spcum[3][4];
     float G[4];                                // LA: sum over event sites of d(rate)/d(theta)
     int dcnt[3];                               // LA: net crystal atoms per species added by this tile
     int nlist;
@@ -699,7 +701,7 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 // match_any).  pos covers the wz staged layers from zw0 (smem path only).
 template <class Lat>
 __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa, int wb, int zl, int zh,
-                                           bool use_pos, int zw0, int wz, bool single, bool cov,
+                                           bool use_pos, int zw0, int wz, bool single, bool cov, bool cov2,
                                            const LADev *A = nullptr, double t_mid = 0.0)
 {
     TileShared &S = g_tile;
@@ -727,7 +729,7 @@ __device__ __forceinline__ bool build_list(const Lat &L, int a0, int b0, int wa,
             z = zl + dz;
             ib = (int)(((unsigned)k * hmul) >> 16);
             ia = 2 * (k - ib * hw) + ((a0 + b0 + ib + (z >> 1)) & 1);
-            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single, cov);
+            if (ia < wa) cls = site_class(L, a0 + ia, b0 + ib, z, single, cov, cov2);
         }
         k += 32;
         while (k >= per) {
@@ -900,8 +902,8 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                 if (!(uacc * S.rate[cls] < r_true)) continue;   // null event: time only
             }
         }
-        int covev = 0;                                 // 1 absorption, 2 desorption
-        if (R.cov && cls >= CLS_D1 && cls < CLS_COV0) {
+        int covev = 0;                                 // 1 absorption of ListCov(1), 2 desorption, 3 absorption of ListCov(2)
+        if (R.cov && ((cls >= CLS_D1 && cls < CLS_COV0) || (R.cov == 2 && cls >= CLS_D2 && cls < CLS_D2 + 3))) {
             covev = 2;                                 // main.f:346-349
         } else if (dummy_class(cls)) {
             // unsupported coor-1 site: Get_Prob.f:181-184 (and Get_Prob_Ini.f:
@@ -933,11 +935,12 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
                 }
             } else {
                 sp = u < S.spcum[co - 1][0] ? 1 : (u < S.spcum[co - 1][1] ? 2 : 3);
-                // past the deposition share: absorption of the coverage
-                // species (Get_Prob.f:155-204)
+                // past the deposition share: absorption of a coverage
+                // species, the first up to its cumulative share
+                // (Get_Prob.f:155-204, IndexEvent_Abs :22-52)
                 if (R.cov && !(u < S.spcum[co - 1][2])) {
                     sp = 0;
-                    covev = 1;
+                    covev = (R.cov == 2 && !(u < S.spcum[co - 1][3])) ? 3 : 1;
                 }
             }
         } else if (A && sc && lane == 0 && cls >= CLS_OCC0 && cls < CLS_C1I) {
@@ -947,7 +950,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
         if (covev) {
             // absorption.f / desorption.f: only the site byte changes; lanes
             // 1..4 take its neighbours for re-classification
-            int v = lane == 0 ? cov_event_state(L, a, b, z, covev == 1) : 0;
+            int v = lane == 0 ? cov_event_state(L, a, b, z, covev != 2, covev == 3 ? 2 : 1) : 0;
             if (__shfl_sync(FULL, v, 0) < 0) return -DERR_INVARIANT;
             __syncwarp();
             if (lane == 0) L.put(a, b, z, (uint8_t)v);
@@ -990,7 +993,7 @@ __device__ __forceinline__ int run_events(Lat &L, const RepLocal &R, const QuadD
             hz_lo = min(hz_lo, tz);
             hz_hi = max(hz_hi, tz);
         }
-        int ncls = interior ? site_class(L, ta, tb, tz, R.single != 0, R.cov != 0) : CLS_NONE;
+        int ncls = interior ? site_class(L, ta, tb, tz, R.single != 0, R.cov != 0, R.cov == 2) : CLS_NONE;
         uint32_t tkey = interior ? (uint32_t)key_of(ia + HALO, ib + HALO, tz) : 0u;
         // old list slot of each touched site
         int my_slot = -1;
@@ -1082,7 +1085,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
     // the class rates as bounds, so LA tiles reload it
     if (LAM || S.rate_rep != Q.rep) {
         for (int c = lane; c < 64; c += 32) S.rate[c] = Rg.rate[c];
-        if (lane < 9) S.spcum[lane / 3][lane % 3] = Rg.spcum[lane / 3][lane % 3];
+        if (lane < 12) S.spcum[lane / 4][lane % 4] = Rg.spcum[lane / 4][lane % 4];
         __syncwarp();
         if (lane == 0) S.rate_rep = LAM ? -1 : Q.rep;
     }
@@ -1170,7 +1173,7 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             SLat L{ax0, bx0, zw0, R.NZ, st, R.NA, R.NB, R.pitch};
             if (A) la_bounds(zw0, zw1 - 1);
             if (!build_list(L, Q.a0, Q.b0, wa, wb, max(zlo, zw0), min(zhi, zw1 - 1), true, zw0, WZ, R.single != 0, R.cov != 0,
-                            scp ? A : nullptr, t_mid)) {
+                            R.cov == 2, scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -1184,8 +1187,8 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
             // events here may walk the band upwards without re-staging: bound
             // the rates by the top layer (T rises with z)
             if (A) la_bounds(max(0, zlo - 2), R.NZ - 1);
-            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, R.single != 0, R.cov != 0, scp ? A : nullptr,
-                            t_mid)) {
+            if (!build_list(G, Q.a0, Q.b0, wa, wb, zlo, zhi, false, 0, 0, R.single != 0, R.cov != 0, R.cov == 2,
+                            scp ? A : nullptr, t_mid)) {
                 if (lane == 0) set_error(status, DERR_CAPACITY, qid);
                 return;
             }
@@ -1647,19 +1650,32 @@ void rate_tables(const RepHost &r, RepDev &d)
     for (int co = 1; co <= 3; co++) {
         double p1 = pD[co - 1], p2 = pD[3 + co - 1], p3 = pD[6 + co - 1];
         double dep = p1 + p2 + p3;
-        // empty site: deposition of any species or absorption of the coverage
-        // species, one rate (Get_Prob.f:155-204)
-        double tot = dep + (cov ? r.ptransAbs[co - 1] : 0.0);
+        // empty site: deposition of any species or absorption of a coverage
+        // species, one rate (Get_Prob.f:155-204; the absorption sum runs over
+        // the species in order, as SUM(PtransAbs(:,Coor)) does)
+        const double a1 = r.ptransAbs[co - 1], a2 = r.ptransAbs[3 + co - 1];
+        double tot = dep + (cov ? (a1 + a2) + r.ptransAbs[6 + co - 1] : 0.0);
         int cls = co == 1 ? CLS_C1 : (co == 2 ? CLS_C2 : CLS_C3);
         d.rate[cls] = (float)tot;
         d.spcum[co - 1][0] = tot > 0 ? (float)(p1 / tot) : 1.f;
         d.spcum[co - 1][1] = tot > 0 ? (float)((p1 + p2) / tot) : 1.f;
         d.spcum[co - 1][2] = (tot > 0 && cov) ? (float)(dep / tot) : 1.f;
+        d.spcum[co - 1][3] = (tot > 0 && cov) ? (float)((dep + a1) / tot) : 1.f;
         if (cov) d.rate[CLS_D1 + co - 1] = (float)r.ptransDes[co - 1];   // Get_Prob.f:114
+        if (r.cfg.ncov == 2) d.rate[CLS_D2 + co - 1] = (float)r.ptransDes[3 + co - 1];
     }
     d.rate[CLS_C1D] = 1.e-8f;   // Get_Prob.f:183
     d.rate[CLS_C1I] = 1.e-6f;   // Get_Prob_Ini.f:104
     d.rate[CLS_ISO] = 0.f;      // dynamic: 1e5 x tile rate (Get_Prob.f:305)
+    if (r.cfg.ncov == 2) {
+        // PE(1, n1, 0, 0, c1, c2, 0), Get_Prob.f:309-312
+        for (int n1 = 1; n1 <= 3; n1++)
+            for (int c1 = 0; c1 <= 4 - n1; c1++)
+                for (int c2 = 0; c1 + c2 <= 4 - n1; c2++)
+                    d.rate[CLS_COV0 + cov2_census_index(n1, c1, c2)] =
+                        (float)r.ptransE[n1 * 1024 + c1 * 16 + c2 * 4];
+        return;
+    }
     if (cov) {
         // PE(NSiC, n1, n2, 0, c, 0, 0), Get_Prob.f:309-312
         for (int sp = 1; sp <= 2; sp++)
@@ -1693,8 +1709,12 @@ int check_config(const mks_config &c)
     if (c.lenx / 6 < 16 || c.leny / 6 < 16)
         return fail(MKS_ERR_ARG, "box side %d/%d too small (needs >= 96 grid units)", c.lenx, c.leny);
     if (c.ncrystal < 1 || c.ncrystal > 3) return fail(MKS_ERR_ARG, "NCrystal must be 1..3");
-    if (c.ncov < 0 || c.ncov > 1)
-        return fail(MKS_ERR_UNSUPPORTED, "NCov=%d: the GPU engine holds one coverage species at most", c.ncov);
+    if (c.ncov < 0 || c.ncov > 2)
+        return fail(MKS_ERR_UNSUPPORTED, "NCov=%d: the GPU engine holds two coverage species at most", c.ncov);
+    if (c.ncov == 2 && c.ncrystal != 1)
+        return fail(MKS_ERR_UNSUPPORTED, "two coverage species need NCrystal = 1 (the rate classes of their census)");
+    if (c.ncov == 2 && (c.list_cov[1] <= 0 || c.list_cov[1] >= 113 || c.list_cov[1] == c.list_cov[0]))
+        return fail(MKS_ERR_ARG, "second coverage species atomic number %d", c.list_cov[1]);
     if (c.ncov == 1 && c.ncrystal > 2)
         return fail(MKS_ERR_UNSUPPORTED, "a coverage species needs NCrystal <= 2 (species value 3 marks covered sites)");
     if (c.ncov == 1 && (c.list_cov[0] <= 0 || c.list_cov[0] >= 113))
@@ -2010,7 +2030,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         d[i].seed = r.cfg.seed;
         d[i].active = 1;
         d[i].single = r.cfg.ncrystal == 1 && r.cfg.ncov == 0;
-        d[i].cov = r.cfg.ncov == 1;
+        d[i].cov = r.cfg.ncov;
         if (d[i].cov) h->any_cov = true;
         rate_tables(r, d[i]);
     }
@@ -2397,8 +2417,9 @@ int mks_batch_set_coverage_rates(mks_handle *h, const double *ptransAbs, const d
         for (int k = 0; k < 9; k++) {
             double a = ptransAbs[i * 9 + k], b = ptransDes[i * 9 + k];
             if (!(a >= 0.0) || !(b >= 0.0)) return fail(MKS_ERR_ARG, "negative or NaN coverage rate");
-            if (k >= 3 && (a != 0.0 || b != 0.0))
-                return fail(MKS_ERR_UNSUPPORTED, "rates for a second or third coverage species");
+            if (k >= 3 * r.cfg.ncov && (a != 0.0 || b != 0.0))
+                return fail(MKS_ERR_ARG, "replica %zu: rates for coverage species %d of NCov = %d", i, k / 3 + 1,
+                            r.cfg.ncov);
         }
         memcpy(r.ptransAbs, ptransAbs + i * 9, sizeof(double) * 9);
         memcpy(r.ptransDes, ptransDes + i * 9, sizeof(double) * 9);
@@ -2864,8 +2885,8 @@ int mks_get_lattice(mks_handle *h, int32_t *lc)
                 int32_t v;
                 if (s == WALL) continue;
                 int sp = sp_of(s), co = co_of(s);
-                if (r.cfg.ncov && sp == COVSP)      // covered empty site: CovInd = ListCov(1), absorption.f:34-36
-                    v = (co << 24) | r.cfg.list_cov[0];
+                if (r.cfg.ncov && sp == COVSP)      // covered empty site: CovInd = ListCov(i), absorption.f:34-36
+                    v = (co << 24) | r.cfg.list_cov[(s & COV2) ? 1 : 0];
                 else
                     v = (co << 24) | (sp ? (1 << 23) : 0) | (sp << 27);
                 lc[(size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z)] = v;
@@ -2910,10 +2931,10 @@ int load_lattice_impl(mks_handle *h, int rep, const int32_t *lc)
                 }
                 int occ = (v >> 23) & 1, co = (v >> 24) & 7, sp = (v >> 27) & 7;
                 if ((v & 255) != 0) {
-                    if (!r.cfg.ncov || (v & 255) != r.cfg.list_cov[0])
-                        return fail(MKS_ERR_UNSUPPORTED, "coverage index %d in LattCoo", v & 255);
+                    const int ci = (v & 255) == r.cfg.list_cov[0] ? 1 : ((r.cfg.ncov == 2 && (v & 255) == r.cfg.list_cov[1]) ? 2 : 0);
+                    if (!r.cfg.ncov || !ci) return fail(MKS_ERR_UNSUPPORTED, "coverage index %d in LattCoo", v & 255);
                     if (occ || sp || co < 1 || co > 4) return fail(MKS_ERR_INVARIANT, "bad covered LattCoo word %d", v);
-                    at(a, b, z1) = mk(COVSP, co, 0, 0);
+                    at(a, b, z1) = (uint8_t)(mk(COVSP, co, 0, 0) | (ci == 2 ? COV2 : 0));
                     continue;
                 }
                 if (sp > (r.cfg.ncov ? 2 : 3) || (occ && !sp) || (!occ && sp))
@@ -2960,7 +2981,7 @@ int upload_compact(mks_handle *h, int rep, std::vector<uint8_t> &st, bool ini)
                     }
                 }
                 if (found < 0) return fail(MKS_ERR_INVARIANT, "coor-1 site without neighbour");
-                at(a, b, z1) = covered ? mk(COVSP, 1, found, 0) : mk_c1(found, co_of(ns), ini);
+                at(a, b, z1) = covered ? (uint8_t)(mk(COVSP, 1, found, 0) | (s & COV2)) : mk_c1(found, co_of(ns), ini);
             }
     CK(cudaMemcpyAsync(h->d_st + r.st_off, st.data(), st.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -3776,7 +3797,8 @@ int mks_write_frame(mks_handle *h, const char *base, double time, int64_t iter, 
         double x, y, z;
         site_xyz(i, x, y, z);
         int sp = st[i] & 3;
-        const char *sym = (cov && sp == COVSP) ? (c.list_cov[0] == 17 ? "Cl" : "H") : crystal_symbol(c, sp);
+        const int cz = (cov && sp == COVSP) ? c.list_cov[(st[i] & COV2) ? 1 : 0] : 0;
+        const char *sym = (cov && sp == COVSP) ? (cz == 17 ? "Cl" : "H") : crystal_symbol(c, sp);
         if (!sym) {
             fclose(f);
             return fail(MKS_ERR_INVARIANT, "ERROR: 2nd crystal specie can only be C/Ge/B");

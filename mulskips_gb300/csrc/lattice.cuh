@@ -26,12 +26,15 @@
 // rate class tells the two dummies apart; every event writes a fresh byte
 // and so drops the mark.
 //
-// Coverage mode (one coverage species, NCrystal <= 2): species value 3 marks
-// an EMPTY site carrying the coverage species (LattCoo Occ = 0 with CovInd =
-// ListCov(1), absorption.f:34-36).  A covered site keeps its coordination and
-// list head; the reference clears the whole word when its last neighbour
-// leaves (Evaporation.f:60-67), so a covered site always has coordination
-// 1..4.
+// Coverage mode (one coverage species with NCrystal <= 2, or two with
+// NCrystal = 1): species value 3 marks an EMPTY site carrying a coverage
+// species (LattCoo Occ = 0 with CovInd = ListCov(i), absorption.f:34-36);
+// bit 7, the dummy flag of an uncovered empty site, says which: 0 ListCov(1),
+// 1 ListCov(2) (a covered site has no dummy rate: Get_Prob takes its
+// desorption branch first, Get_Prob.f:91-119).  A covered site keeps its
+// coordination and list head; the reference clears the whole word when its
+// last neighbour leaves (Evaporation.f:60-67), so a covered site always has
+// coordination 1..4.
 //
 // Site (a, b, z1) sits at grid point x = 3(2a + (z1&1)), y = 3(2b + (z1&1)),
 // z = 3 z1 and exists when (a + b + (z1 >> 1)) is even.  Even layers hold the
@@ -59,6 +62,7 @@ MKS_HD int dm_of(uint8_t s) { return (s >> 7) & 1; }
 MKS_HD bool is_wall(uint8_t s) { return s == WALL; }
 MKS_HD bool is_occ(uint8_t s) { return s == WALL || (s & 3) != 0; }
 constexpr int COVSP = 3;                       // species value of a covered empty site
+constexpr uint8_t COV2 = 0x80;                 // with COVSP: the second coverage species
 // species of an atom, 0 for an empty (or covered) site; cov selects coverage mode
 MKS_HD int atom_sp(uint8_t s, bool cov) { int sp = s & 3; return (cov && sp == COVSP) ? 0 : sp; }
 MKS_HD bool is_cov(uint8_t s, bool cov) { return cov && (s & 3) == COVSP; }
@@ -108,6 +112,18 @@ MKS_HD bool dummy_class(int c) { return c == CLS_C1D || c == CLS_C1I; }
 // deposition + absorption (Get_Prob.f:155-204).
 constexpr int CLS_D1 = 6, CLS_COV0 = 9;
 constexpr int NCOVCENSUS = 25;
+// Two coverage species (NCrystal = 1): 6..8 and 59..61 the sites covered by
+// species 1 and 2 (desorption), 9..27 atoms with (nSi+nWall) = n1 and c1, c2
+// covered neighbours of each species, c1 + c2 <= 4 - n1 (the PTransE key
+// PE(1, n1, 0, 0, c1, c2, 0) of Get_Prob.f:309-312).
+constexpr int CLS_D2 = 59;
+constexpr int NCOV2CENSUS = 19;
+MKS_HD int cov2_census_index(int n1, int c1, int c2)
+{
+    int m = 4 - n1;                                     // c1 + c2 <= m
+    int base = n1 == 1 ? 0 : (n1 == 2 ? 10 : 16);
+    return base + c1 * (m + 1) - c1 * (c1 - 1) / 2 + c2;
+}
 
 MKS_HD int cov_census_index(int n1, int n2, int c)
 {
@@ -147,18 +163,20 @@ MKS_HD bool event_byte(uint8_t s)
 // single: the lattice holds species 1 only, so an atom's census is
 // (coordination, 0, 0) — walls count with species 1 and reciprocity holds —
 // and the neighbours need not be read.
-// cov: coverage mode (then single is ignored: the census reads the neighbours).
+// cov: coverage mode (then single is ignored: the census reads the neighbours);
+// cov2: two coverage species.
 template <class L>
-MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false, bool cov = false)
+MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false, bool cov = false, bool cov2 = false)
 {
     uint8_t s = lat.get(a, b, z);
     if (s == 0 || s == WALL) return CLS_NONE;
     int sp = sp_of(s), co = co_of(s);
     if (cov) {
-        if (sp == COVSP) return (co >= 1 && co <= 3) ? CLS_D1 + co - 1 : CLS_NONE;
+        if (sp == COVSP)
+            return (co >= 1 && co <= 3) ? ((cov2 && (s & COV2)) ? CLS_D2 : CLS_D1) + co - 1 : CLS_NONE;
         if (sp != 0) {
             if (co >= 4) return CLS_NONE;
-            int n1 = 0, n2 = 0, nc = 0;
+            int n1 = 0, n2 = 0, nc = 0, nc2 = 0;
             int zp = z & 1;
 #pragma unroll
             for (int d = 0; d < 4; d++) {
@@ -168,11 +186,13 @@ MKS_HD int site_class(const L &lat, int a, int b, int z, bool single = false, bo
                 int st = sp_of(t);
                 n1 += (t == WALL || st == 1) ? 1 : 0;
                 n2 += st == 2 ? 1 : 0;
-                nc += st == COVSP ? 1 : 0;
+                nc += (st == COVSP && !(t & COV2)) ? 1 : 0;
+                nc2 += (st == COVSP && (t & COV2)) ? 1 : 0;
             }
             int tot = n1 + n2;
             if (tot == 0) return CLS_ISO;
             if (tot > 3) return CLS_NONE;
+            if (cov2) return CLS_COV0 + cov2_census_index(n1, nc, nc2);
             return CLS_COV0 + (sp - 1) * NCOVCENSUS + cov_census_index(n1, n2, nc);
         }
     }
@@ -276,6 +296,7 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
     int cy = co_of(sy);
     int ay = atom_sp(sy, e.cov);               // species of an atom, 0 if empty
     int cv = sp_of(sy) - ay;                   // COVSP on a covered site, else 0
+    const uint8_t hi = cv ? (uint8_t)(sy & COV2) : (uint8_t)0;   // which coverage species
     if (e.sp) {                                // deposition.f:78-235
         if (ay != 0) {                         // occupied neighbour, :192-230
             if (cy <= 3) lat.put(ya, yb, yz, mk(ay, cy + 1, fd_of(sy), 0));
@@ -293,9 +314,9 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
                 if (t != WALL && atom_sp(t, e.cov) != 0) cnt++;
             }
             if (cnt < 2) return -2;
-            lat.put(ya, yb, yz, mk(cv, cnt, fd_of(sy), 0));
+            lat.put(ya, yb, yz, (uint8_t)(mk(cv, cnt, fd_of(sy), 0) | hi));
         } else if (cy == 2 || cy == 3) {       // :161-191
-            lat.put(ya, yb, yz, mk(cv, cy + 1, fd_of(sy), 0));
+            lat.put(ya, yb, yz, (uint8_t)(mk(cv, cy + 1, fd_of(sy), 0) | hi));
         }
     } else {                                   // Evaporation.f:46-215
         if (ay != 0) {                         // :166-210
@@ -310,11 +331,11 @@ MKS_HD int ev_neighbour(L &lat, const EvCtx &e, int d, int &ya, int &yb, int &yz
             uint8_t sf = lat.get(ya + fa, yb + fb, yz + fz);
             int w = occupied_dir(lat, ya, yb, yz, e.cov);
             if (w < 0) return -4;
-            lat.put(ya, yb, yz, mk(cv, 1, w, (!cv && co_of(sf) < 2) ? 1 : 0));
+            lat.put(ya, yb, yz, (uint8_t)(mk(cv, 1, w, (!cv && co_of(sf) < 2) ? 1 : 0) | hi));
         } else if (cy == 3) {                  // :124-141
-            lat.put(ya, yb, yz, mk(cv, 2, fd_of(sy), 0));
+            lat.put(ya, yb, yz, (uint8_t)(mk(cv, 2, fd_of(sy), 0) | hi));
         } else if (cy == 4) {                  // void -> MC, :142-164
-            lat.put(ya, yb, yz, mk(cv, 3, fd_of(sy), 0));
+            lat.put(ya, yb, yz, (uint8_t)(mk(cv, 3, fd_of(sy), 0) | hi));
         }
     }
     return 0;
@@ -378,18 +399,19 @@ MKS_HD int apply_evaporation(L &lat, int a, int b, int z, Touched &tc, bool cov 
 }
 
 // Coverage events: the new state of the event site, or -1 if the event does
-// not apply.  Absorption (absorption.f:24-78) covers an empty site of
-// coordination 1..3 keeping its coordination and list; desorption
-// (desorption.f:24-117) uncovers it, and Get_Prob then recomputes the dummy
-// flag of a coor-1 site from its list head's coordination (Get_Prob.f:156-158).
-// Only the site byte changes; its four neighbours' classes follow from it.
+// not apply.  Absorption (absorption.f:24-78) of coverage species `which`
+// (1 or 2) covers an empty site of coordination 1..3 keeping its coordination
+// and list; desorption (desorption.f:24-117) uncovers it, and Get_Prob then
+// recomputes the dummy flag of a coor-1 site from its list head's
+// coordination (Get_Prob.f:156-158).  Only the site byte changes; its four
+// neighbours' classes follow from it.
 template <class L>
-MKS_HD int cov_event_state(const L &lat, int a, int b, int z, bool absorb)
+MKS_HD int cov_event_state(const L &lat, int a, int b, int z, bool absorb, int which = 1)
 {
     uint8_t s = lat.get(a, b, z);
     int co = co_of(s);
     if (s == WALL || co < 1 || co > 3) return -1;
-    if (absorb) return sp_of(s) == 0 ? mk(COVSP, co, fd_of(s), 0) : -1;
+    if (absorb) return sp_of(s) == 0 ? (int)(mk(COVSP, co, fd_of(s), 0) | (which == 2 ? COV2 : 0)) : -1;
     if (sp_of(s) != COVSP) return -1;
     int dm = 0;
     if (co == 1) {
@@ -401,9 +423,9 @@ MKS_HD int cov_event_state(const L &lat, int a, int b, int z, bool absorb)
 }
 
 template <class L>
-MKS_HD int apply_coverage(L &lat, int a, int b, int z, bool absorb, Touched &tc)
+MKS_HD int apply_coverage(L &lat, int a, int b, int z, bool absorb, Touched &tc, int which = 1)
 {
-    int v = cov_event_state(lat, a, b, z, absorb);
+    int v = cov_event_state(lat, a, b, z, absorb, which);
     if (v < 0) return 1;
     lat.put(a, b, z, (uint8_t)v);
     tc.n = 5;

@@ -417,7 +417,8 @@ int main()
     if (in.ncov > 0) {
         printf(" Coverage species (NCov= %d ) --> Z: %d %d %d\n", in.ncov, in.list_cov[0], in.list_cov[1],
                in.list_cov[2]);
-        if (in.ncov > 1) die("ERR NOT IMPLEMENTED: the GPU engine holds one coverage species");
+        if (in.ncov > 2 || (in.ncov == 2 && in.ncrystal != 1))
+            die("ERR NOT IMPLEMENTED: the GPU engine holds two coverage species with NCrystal = 1, or one");
     }
     const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "SS" || in.init_st == "I" ||
                         in.init_st == "D" || in.init_st == "Z" || in.init_st == "J" || in.init_st == "K" ||

@@ -2829,10 +2829,11 @@ int64_t ora_compact_state(const ora_t *o, uint8_t *out)
                  * Get_Prob_Ini (1e-6) the flag with coordination field 5 */
                 int dm = (!occ && co == 1 && which == 1 && (pr == (double)1.e-8f || pr == (double)1.e-6f)) ? 1 : 0;
                 if (dm && pr == (double)1.e-6f) co = 5;
-                /* an empty site carrying a coverage species is species value 3 */
+                /* an empty site carrying a coverage species is species value
+                 * 3, with bit 7 set for the second coverage species */
                 if (!occ && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
                     sp = 3;
-                    dm = 0;
+                    dm = (o->ncov >= 2 && ibits(v, POS_INDEX, LEN_INDEX) == o->list_cov[1]) ? 1 : 0;
                 }
                 *d = (uint8_t)((sp & 3) | ((co & 7) << 2) | (fd << 5) | (dm << 7));
             }
@@ -2899,7 +2900,9 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
         int sp = ibits(v, POS_SIC, LEN_SIC);
         int c = 0;
         if (!occ && o->ncov > 0 && ibits(v, POS_INDEX, LEN_INDEX) != 0) {
-            if (co >= 1 && co <= 3) c = 6 + co - 1;      /* covered: desorption */
+            /* covered: desorption, 6..8 for ListCov(1), 59..61 for ListCov(2) */
+            int second = o->ncov >= 2 && ibits(v, POS_INDEX, LEN_INDEX) == o->list_cov[1];
+            if (co >= 1 && co <= 3) c = (second ? 59 : 6) + co - 1;
         } else if (!occ) {
             if (co == 1) c = (p->prob == (double)1.e-8f) ? 2 : (p->prob == (double)1.e-6f ? 63 : 1);
             else if (co == 2) c = 3;
@@ -2907,7 +2910,7 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
         } else if (o->ncov > 0) {
             /* census (nSi+nWall, nC) and covered neighbours as Get_Prob.f:
              * 215-291 counts them, reciprocity through each neighbour's list */
-            int n_si = 0, n_c = 0, n_w = 0, n_cov = 0;
+            int n_si = 0, n_c = 0, n_w = 0, n_cov = 0, n_cov2 = 0;
             for (int k = 0; k < 4; k++) {
                 int32_t w = *LC(o, p->nn[k]);
                 int cn = ibits(w, POS_COOR, LEN_COOR), ind = *LI(o, p->nn[k]);
@@ -2915,7 +2918,10 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
                 if (!ibits(w, POS_OCC, LEN_OCC)) {
                     if (ibits(w, POS_INDEX, LEN_INDEX) == 0) continue;
                     get_nn_list(o, ind, 1, nnn);
-                    if (in_list(nnn, p->xyz)) n_cov++;
+                    if (in_list(nnn, p->xyz)) {
+                        if (o->ncov >= 2 && ibits(w, POS_INDEX, LEN_INDEX) == o->list_cov[1]) n_cov2++;
+                        else n_cov++;
+                    }
                     continue;
                 }
                 if (ibits(w, POS_INDEX, LEN_INDEX) == WALL) { n_w++; continue; }
@@ -2927,7 +2933,11 @@ int64_t ora_mc_classes(const ora_t *o_, int32_t *cls, double *rate, int64_t n)
             }
             int t = n_si + n_c + n_w;
             if (t == 0) c = 5;
-            else if (t <= 3) {
+            else if (t <= 3 && o->ncov >= 2) {
+                /* (n1, c1, c2), c1 + c2 <= 4 - n1: 19 classes from 9 */
+                int n1 = n_si + n_w, m = 4 - n1, base = n1 == 1 ? 0 : (n1 == 2 ? 10 : 16);
+                c = 9 + base + n_cov * (m + 1) - n_cov * (n_cov - 1) / 2 + n_cov2;
+            } else if (t <= 3) {
                 int n1 = n_si + n_w, base = t == 1 ? 0 : (t == 2 ? 8 : 17);
                 c = 9 + (sp - 1) * 25 + base + (t - n1) * (5 - t) + n_cov;
             }

@@ -97,12 +97,28 @@ def test_batch_uneven_replicas():
 
 
 def test_unsupported_config_is_rejected():
+    """Configurations outside the engine fail at creation with an error code:
+    arm-chair stacking in a batch or with a coverage species, three coverage
+    species, two with NCrystal = 2, a box side that is not a multiple of 12."""
+    import ctypes as C
     from mulskips_gb300 import Lattice
+    from mulskips_gb300 import _native as N
     from mulskips_gb300._native import MksError
-    with pytest.raises(MksError):
-        Lattice(480, 480, 480, ptrans_zig=0.8)
+    from mulskips_gb300.engine import _cfg
     with pytest.raises(MksError):
         Lattice(100, 480, 480)
+    with pytest.raises(MksError):
+        Lattice(480, 480, 480, ptrans_zig=0.8, list_cov=(1,))
+    with pytest.raises(MksError):
+        Lattice(480, 480, 480, list_cov=(1, 17, 9))
+    with pytest.raises(MksError):
+        Lattice(480, 480, 480, ncrystal=2, list_crystal=(14, 6), list_cov=(1, 17))
+    cfgs = (N.MksConfig * 2)(*[_cfg(480, 480, 480, 1, (14,), 0.8, 5.43 / 12, s) for s in (1, 2)])
+    h = C.c_void_p()
+    with pytest.raises(MksError):
+        N.check(N.lib().mks_batch_create(cfgs, 2, C.byref(h)))
+    with Lattice(480, 480, 480, ptrans_zig=0.8) as lat:      # arm-chair stacking: a supported mode
+        assert lat.dims == (480, 480, 480)
 
 
 @pytest.mark.parametrize("colours", [3, 4])

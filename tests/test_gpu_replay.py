@@ -77,6 +77,18 @@ def test_replay_cvd_si001_hydrogen(oracle_lib):
     assert n == 400000
 
 
+def test_replay_cvd_two_coverage_species(oracle_lib, tmp_path):
+    """CVD of Si(001) under two coverage species (H and Cl, the input of
+    tests/cvd2.py): depositions, evaporations, desorptions and absorptions of
+    either species (itrans 6 and 7, IndexEvent_Abs of Get_Prob.f:22-52)
+    replay exactly, covered sites of each species and the 19 atom classes
+    keyed by their covered neighbours (PE(1, n1, 0, 0, c1, c2, 0)) included."""
+    from cvd2 import two_coverage_startdat
+    p = two_coverage_startdat(str(tmp_path / "start.dat"))
+    n = replay_case(oracle_lib, p, 48, "S", 400000, 100000)
+    assert n == 400000
+
+
 def test_replay_sic_cube(oracle_lib):
     """The free-standing 3C-SiC parallelepiped of the reference's `cube` case
     (SetNC, no walls), loaded from the oracle's LattCoo through

@@ -265,6 +265,38 @@ def test_sic_facets_match_serial_reference(tmp_path):
     fam.check()
 
 
+# ---------------------------------------------------------------- CVD with two coverage species
+def test_cvd_two_coverage_species_match_serial_reference(tmp_path):
+    """CVD of Si(001) under H and Cl (tests/cvd2.py: two coverage species,
+    absorption split by IndexEvent_Abs, Get_Prob.f:22-52, atom rates keyed by
+    covered neighbours of each species), RunType R, t_obs = 3 s, f = 0.3:
+    atoms, H- and Cl-covered sites, growth rate and RMS roughness."""
+    from cvd2 import two_coverage_startdat
+    from mulskips_gb300 import Batch
+    from mulskips_gb300.startdat import parse_startdat
+    t_obs, f = 3.0, 0.3
+    paths = [two_coverage_startdat(str(tmp_path / f"c2_{s}.dat"), "R", 700 + s, 100.0) for s in range(NSEEDS)]
+    d = parse_startdat(paths[0])
+    assert d["run_type"] == "R" and d["list_cov"] == [1, 17]
+    ref = oracle_sample(paths, (480, 480, 480), t_obs, d["sf"], cov=True)
+    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[171 + s for s in range(NSEEDS)], sf=d["sf"], list_cov=d["list_cov"])
+    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
+    b.set_coverage_rates(np.stack([d["ptransAbs"][:, 1:]] * NSEEDS), np.stack([d["ptransDes"][:, 1:]] * NSEEDS))
+    b.init_flat("S", [48] * NSEEDS)
+    nwin = windows_for(t_obs, float(b.suggest_tau(f)[0]))
+    g = gpu_sample(b, t_obs / nwin, nwin, (480, 480, 480), d["sf"], cov=True)
+    b.close()
+    fam = Family(f"CVD Si(001) + H + Cl, f = {f} ({nwin} windows)", 5)
+    fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
+    fam.add("H-covered sites", column(g, "covered") - column(g, "covered2"),
+            column(ref, "covered") - column(ref, "covered2"))
+    fam.add("Cl-covered sites", column(g, "covered2"), column(ref, "covered2"))
+    fam.add("growth rate um/h", growth(g), growth(ref))
+    fam.add("RMS roughness", column(g, "rms_roughness"), column(ref, "rms_roughness"))
+    assert column(ref, "covered2").mean() > 100
+    fam.check()
+
+
 # ---------------------------------------------------------------- CVD with hydrogen coverage
 _CVD_REF = {}
 
