@@ -356,12 +356,14 @@ def bench_accuracy(width):
 def batched_bench(args):
     """Config 3: 512 independent Si(001) replicas, box side ~U{16..96} cells,
     T ~ U(900, 1300) K, F ~ logU(0.05, 5) ML/s, seed 1000+i, in one persistent
-    launch per block of windows; tau per replica and tile width autotuned.
+    launch per block of windows; tau per replica and tile width autotuned
+    (one width for the batch by a timed trial, then one per group of box
+    sizes by coordinate descent).
     Also one replica of the median size run alone (the plain single-replica
     path) for the batched/plain ratio."""
     import numpy as np
     from mulskips_gb300 import Batch, Lattice, arrhenius_tables
-    from mulskips_gb300.autotune import choose_width
+    from mulskips_gb300.autotune import choose_width, choose_widths, size_groups
     rng = np.random.default_rng(3)
     n = 512
     sides = rng.integers(16, 97, n)
@@ -375,6 +377,11 @@ def batched_bench(args):
     b.init_flat("S", len1)
     tau = b.suggest_tau(ACCURATE_F)
     width = choose_width(b, tau, restore=False)
+    # then one width per group of box sizes, starting from the batch's best
+    groups = size_groups(sides)
+    widths, trials = choose_widths(b, b.suggest_tau(ACCURATE_F), groups)
+    by_group = [{"side_cells": [int(sides[g].min()), int(sides[g].max())], "replicas": int(len(g)),
+                 "tile_width": int(widths[g[0]])} for g in groups]
     tau = b.suggest_tau(ACCURATE_F)
     b.run(tau, 8)
     ev = 0
@@ -396,7 +403,8 @@ def batched_bench(args):
     v = ev / (ms / 1e3)
     v1 = ev1 / (ms1 / 1e3)
     return {"value": v, "unit": "events/s", "replicas": n, "events": ev, "windows": BATCH_WINDOWS_PER_STEP * args.steps,
-            "tile_width": width, "single_replica_value": v1, "single_replica_side_cells": med,
+            "tile_width": width, "tile_width_by_size_group": by_group, "width_trials": trials,
+            "single_replica_value": v1, "single_replica_side_cells": med,
             "batched_over_single": v / v1,
             "workload": "512 Si(001) replicas, side ~U{16..96} cells, T~U(900,1300) K, F~logU(0.05,5), "
                         "seed 1000+i, tau = 0.3/r* per replica"}

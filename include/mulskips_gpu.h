@@ -274,6 +274,11 @@ int32_t mks_batch_size(mks_handle *h);
  * loop is serial; the tile shape is one of the autotuner's knobs).         */
 int mks_set_tiling(mks_handle *h, int32_t width);
 int32_t mks_get_tiling(mks_handle *h);
+/* Tile width per replica (n entries, 4..8 each): replicas of a batch may be
+ * cut at different widths (the autotuner picks one per group of replica
+ * sizes); mks_get_tiling then gives the largest.                          */
+int mks_batch_set_tiling(mks_handle *h, const int32_t *widths);
+int mks_batch_get_tiling(mks_handle *h, int32_t *widths);
 /* Colouring of the sublattice tiles (no counterpart in the reference, whose
  * loop is serial).  0 (the default): every replica whose tiles can be at
  * least 6 sites wide at the current width takes the brick tiling -- rows of

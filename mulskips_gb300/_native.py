@@ -65,6 +65,8 @@ SIGNATURES = {
     "mks_init_flat": (C.c_int, [C.c_void_p, C.c_char, C.c_int32]),
     "mks_load_lattice": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mks_get_lattice": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mks_batch_set_tiling": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mks_batch_get_tiling": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mks_load_lists": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
     "mks_get_lists": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

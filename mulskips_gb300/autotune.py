@@ -13,8 +13,12 @@ the model:
     is 0.1 % of the atoms, at the edge of the 95 % band of 32 seeds.
 
 Tile width: a short timed trial of each candidate width on the lattice
-itself; the plain path restores the lattice afterwards.
+itself; the plain path restores the lattice afterwards.  A batch of uneven
+replicas takes one width per group of box sizes (choose_widths), found by
+coordinate descent over the groups.
 """
+import numpy as np
+
 ACCURATE_F = 0.3          # single species
 ACCURATE_F_MULTI = 0.01   # two or three species
 
@@ -42,6 +46,40 @@ def choose_width(sim, tau, widths=(4, 6, 8), windows=16, restore=True):
     if saved is not None:
         sim.set_state(saved)
     return best
+
+
+def size_groups(sides, edges=(40, 72)):
+    """Replica indices grouped by box side in cells: below edges[0], up to
+    edges[1], above (empty groups dropped)."""
+    sides = np.asarray(sides)
+    bins = np.digitize(sides, edges)
+    return [np.flatnonzero(bins == k) for k in range(len(edges) + 1) if np.any(bins == k)]
+
+
+def choose_widths(batch, tau, groups, widths=(4, 6, 8), windows=16):
+    """Tile width per group of replicas (mks_batch_set_tiling), by coordinate
+    descent: one group at a time, each candidate width timed over `windows`
+    windows with the other groups at their current widths, keeping the width
+    that gives the whole batch the most events per device ms.  The trial
+    windows advance the batch (they are part of its warm-up).  Returns the
+    widths per replica and a record of the trials."""
+    cur = np.array(batch.tilings(), dtype=np.int32)
+    trials = []
+    for g in groups:
+        best, best_rate = None, -1.0
+        for w in widths:
+            trial = cur.copy()
+            trial[g] = w
+            batch.set_tilings(trial)
+            ev = batch.run(tau, windows)
+            ms = batch.run_stats()["kernel_ms"]
+            rate = ev / max(ms, 1e-6)
+            trials.append({"group_size": int(len(g)), "width": int(w), "events_per_ms": rate})
+            if rate > best_rate:
+                best, best_rate = w, rate
+        cur[g] = best
+    batch.set_tilings(cur)
+    return cur, trials
 
 
 def tune(sim, f=ACCURATE_F, widths=(4, 6, 8), windows=16):

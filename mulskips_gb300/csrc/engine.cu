@@ -1579,6 +1579,7 @@ struct RepHost {
     int NA, NB, NZ, pitch;
     int nqa, nqb, quad_base;
     int qshift = 0;             // brick tiling: shift of the odd tile rows (columns)
+    int width = 8;              // tile width (sites) of this replica's tiling
     int64_t st_off;
     double ptransE[3 * 4096];
     double ptransD[9];
@@ -1788,14 +1789,14 @@ void class_hist(mks_handle *h, int r0, int r1, unsigned long long *hist)
 // The tiles of every replica (mks_tiling::layout): the brick tiling of three
 // colours where a replica admits it and colours_req allows, else the square
 // grid of four.
-void partition(mks_handle *h, int width)
+void partition(mks_handle *h)
 {
     h->quads_h.clear();
     for (int c = 0; c < 4; c++) h->color_list_h[c].clear();
     h->ncolour = 0;
     for (size_t i = 0; i < h->reps.size(); i++) {
         RepHost &r = h->reps[i];
-        const mks_tiling::Layout L = mks_tiling::layout(r.NA, r.NB, width, h->colours_req != 4);
+        const mks_tiling::Layout L = mks_tiling::layout(r.NA, r.NB, r.width, h->colours_req != 4);
         h->ncolour = std::max(h->ncolour, L.ncol);
         r.nqa = L.nqa;
         r.nqb = L.nqb;
@@ -1821,7 +1822,6 @@ void partition(mks_handle *h, int width)
             h->quads_h.push_back(q);
         }
     }
-    h->tile_width = width;
 }
 
 int upload_tiles(mks_handle *h)
@@ -1978,7 +1978,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
             delete h;
             return fail(MKS_ERR_UNSUPPORTED, "arm-chair stacking (PtransZig < 1) runs in single-replica handles");
         }
-    partition(h, 8);
+    partition(h);
     auto cleanup_fail = [&](const char *what, cudaError_t e) {
         fail(MKS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
         mks_destroy(h);
@@ -3430,13 +3430,13 @@ int mks_get_status(mks_handle *h, mks_status *st)
     return 0;
 }
 
-int mks_set_tiling(mks_handle *h, int32_t width)
+// re-partition every replica with its own width and rescan
+int retile(mks_handle *h)
 {
-    if (!h || width < 4 || width > QMAX) return fail(MKS_ERR_ARG, "tile width must be 4..%d", QMAX);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
     h->graph_windows = 0;
-    partition(h, width);
+    partition(h);
     int rc = upload_tiles(h);
     if (rc) return rc;
     std::vector<RepDev> d;
@@ -3453,7 +3453,36 @@ int mks_set_tiling(mks_handle *h, int32_t width)
     return rescan(h);
 }
 
+int mks_set_tiling(mks_handle *h, int32_t width)
+{
+    if (!h || width < 4 || width > QMAX) return fail(MKS_ERR_ARG, "tile width must be 4..%d", QMAX);
+    for (RepHost &r : h->reps) r.width = width;
+    h->tile_width = width;
+    return retile(h);
+}
+
 int32_t mks_get_tiling(mks_handle *h) { return h ? h->tile_width : 0; }
+
+int mks_batch_set_tiling(mks_handle *h, const int32_t *widths)
+{
+    if (!h || !widths) return fail(MKS_ERR_ARG, "bad arguments");
+    for (size_t i = 0; i < h->reps.size(); i++)
+        if (widths[i] < 4 || widths[i] > QMAX) return fail(MKS_ERR_ARG, "replica %zu: tile width must be 4..%d", i, QMAX);
+    int wmax = 0;
+    for (size_t i = 0; i < h->reps.size(); i++) {
+        h->reps[i].width = widths[i];
+        wmax = std::max(wmax, (int)widths[i]);
+    }
+    h->tile_width = wmax;
+    return retile(h);
+}
+
+int mks_batch_get_tiling(mks_handle *h, int32_t *widths)
+{
+    if (!h || !widths) return fail(MKS_ERR_ARG, "bad arguments");
+    for (size_t i = 0; i < h->reps.size(); i++) widths[i] = h->reps[i].width;
+    return 0;
+}
 
 int mks_set_colours(mks_handle *h, int32_t ncolour)
 {
@@ -3461,12 +3490,12 @@ int mks_set_colours(mks_handle *h, int32_t ncolour)
     if (ncolour == 3)                   // every replica must take the brick tiling
         for (const RepHost &r : h->reps) {
             int t, sh;
-            if (!mks_tiling::brick_fits(r.NA, h->tile_width, t, sh))
+            if (!mks_tiling::brick_fits(r.NA, r.width, t, sh))
                 return fail(MKS_ERR_ARG, "a %d-site row cannot take the three-colour tiling at width %d", r.NA,
-                            h->tile_width);
+                            r.width);
         }
     h->colours_req = ncolour == 4 ? 4 : 0;
-    return mks_set_tiling(h, h->tile_width);
+    return retile(h);
 }
 
 int32_t mks_get_colours(mks_handle *h) { return h ? h->ncolour : 0; }

@@ -347,6 +347,17 @@ class Batch:
     def tiling(self):
         return N.lib().mks_get_tiling(self._h)
 
+    def set_tilings(self, widths):
+        """Tile width of each replica (mks_batch_set_tiling)."""
+        w = np.ascontiguousarray(widths, dtype=np.int32).reshape(-1)
+        assert w.size == self.n
+        N.check(N.lib().mks_batch_set_tiling(self._h, N.ptr(w)))
+
+    def tilings(self):
+        w = np.zeros(self.n, dtype=np.int32)
+        N.check(N.lib().mks_batch_get_tiling(self._h, N.ptr(w)))
+        return w
+
     def set_colours(self, ncolour):
         """Tile colouring: 0 brick (3 colours) where it fits, 3 brick for all,
         4 square grid (4 colours) for all."""

@@ -165,6 +165,30 @@ def test_batch_mixes_tilings():
         check_invariants(states[1][0][r])
 
 
+def test_batch_widths_per_replica():
+    """mks_batch_set_tiling: each replica of a batch cut at its own width;
+    the persistent and per-colour schedules agree and the lattices stay
+    consistent."""
+    from mulskips_gb300 import Batch, arrhenius_tables
+    pE, pD = arrhenius_tables(1100.0)
+    boxes = [(288, 288, 288), (480, 480, 480), (384, 384, 384)]
+    states = []
+    for persistent in (0, 1):
+        b = Batch(boxes, seeds=[15, 16, 17])
+        b.set_tilings([4, 8, 6])
+        assert list(b.tilings()) == [4, 8, 6] and b.tiling() == 8
+        b.set_schedule(persistent)
+        b.set_rates(np.stack([pE] * 3), np.stack([pD] * 3))
+        b.init_flat("S", [144, 240, 192])
+        ev = b.run(1e-8, 24)
+        states.append(([b.state(r) for r in range(3)], ev, [o["events"] for o in b.observables()]))
+        b.close()
+    assert states[0][1] == states[1][1] > 0 and min(states[1][2]) > 0
+    for r in range(3):
+        assert np.array_equal(states[0][0][r], states[1][0][r])
+        check_invariants(states[1][0][r])
+
+
 @pytest.mark.parametrize("width,colours", [(4, 4), (6, 3), (6, 4), (8, 3), (8, 4)])
 def test_tile_widths_keep_invariants(width, colours):
     from mulskips_gb300 import Lattice, arrhenius_tables
