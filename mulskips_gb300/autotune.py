@@ -16,7 +16,13 @@ Tile width: a short timed trial of each candidate width on the lattice
 itself; the plain path restores the lattice afterwards.  A batch of uneven
 replicas takes one width per group of box sizes (choose_widths), found by
 coordinate descent over the groups.
+
+choose_f picks f per model from pilot runs (an equivalence test of the
+growth against the shortest window of a ladder); the constants above are the
+validated defaults it is checked against.
 """
+import math
+
 import numpy as np
 
 ACCURATE_F = 0.3          # single species
@@ -80,6 +86,46 @@ def choose_widths(batch, tau, groups, widths=(4, 6, 8), windows=16):
         cur[g] = best
     batch.set_tilings(cur)
     return cur, trials
+
+
+def choose_f(make, t_pilot, ladder=(0.3, 0.1, 0.03, 0.01), tol=0.02, z=1.96):
+    """Window factor f for a model, from pilot runs instead of a lookup.
+
+    make(f) builds a fresh pilot batch (several replicas of one model, each
+    with its own seed) and returns it; each pilot runs for t_pilot simulated
+    seconds in windows of tau = f / r* and gives the atoms gained per replica.
+    The smallest f of the ladder is the reference: the sublattice error
+    vanishes as tau -> 0.  The largest f whose mean gain agrees with the
+    reference's by an equivalence test -- the 95 % interval of the
+    difference inside +-tol of the reference's mean -- is returned, so a noisy
+    pilot errs towards a shorter window, never towards a biased one.
+    Returns (f, record of the pilots)."""
+    ladder = sorted(ladder, reverse=True)
+
+    def pilot(f):
+        b = make(f)
+        try:
+            a0 = np.array([o["atoms"] for o in b.observables()], float)
+            tau = np.asarray(b.suggest_tau(f), float)
+            nwin = int(math.ceil(t_pilot / float(tau.min())))
+            b.run(np.full(b.n, t_pilot / nwin), nwin)
+            a1 = np.array([o["atoms"] for o in b.observables()], float)
+        finally:
+            b.close()
+        g = a1 - a0
+        return {"f": f, "windows": nwin, "gain": float(g.mean()), "se": float(g.std(ddof=1) / math.sqrt(len(g)))}
+
+    ref = pilot(ladder[-1])
+    record = [ref]
+    for f in ladder[:-1]:
+        p = pilot(f)
+        d = p["gain"] - ref["gain"]
+        sd = math.hypot(p["se"], ref["se"])
+        p["accepted"] = abs(d) + z * sd <= tol * abs(ref["gain"])
+        record.append(p)
+        if p["accepted"]:
+            return f, record
+    return ladder[-1], record
 
 
 def tune(sim, f=ACCURATE_F, widths=(4, 6, 8), windows=16):
