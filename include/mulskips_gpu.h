@@ -86,7 +86,7 @@ typedef struct mks_handle mks_handle;
 /* One replica's setup (the scalar part of start.dat, main.f:83-212). */
 typedef struct {
     int32_t lenx, leny, lenz;      /* LenX, LenY, LenZ; LenX, LenY multiples of 12, LenZ of 3 */
-    int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (0, or 1 with NCrystal <= 2) */
+    int32_t ncrystal, ncov;        /* NCrystal (1..3), NCov (0; 1 with NCrystal <= 2; 2 with NCrystal = 1) */
     int32_t list_crystal[3];       /* atomic numbers (ListCrystal)               */
     double ptrans_zig;             /* PtransZig; < 1 selects arm-chair stacking (see below) */
     double sf;                     /* super-lattice parameter in Angstrom        */
@@ -99,7 +99,7 @@ typedef struct {
 typedef struct {
     int32_t x, y, z;               /* grid coordinates of the event site         */
     int8_t itrans;                 /* 1..3 deposition of that species, 4 evaporation,
-                                      5 desorption, 6 absorption of coverage species 1 */
+                                      5 desorption, 6 / 7 absorption of coverage species 1 / 2 */
     int8_t arm;                    /* arm-chair stacking choice of a tie (IF_Arm_Choice.f:44-51) */
     int16_t pad;
 } mks_event;
@@ -138,14 +138,18 @@ int mks_last_error(char *buf, int32_t len);
 /* ptransE: 3*4^6 doubles indexed [s][n1][n2][n3][c1][c2][c3] (the PTransE
  * array of defsystem.f:63-64); ptransD: 3x3 doubles [s][coor-1].          */
 int mks_set_rates(mks_handle *h, const double *ptransE, const double *ptransD);
-/* Coverage species (NCov = 1): ptransAbs, ptransDes are 3x3 doubles
- * [coverage species][coor-1] (PtransAbs / PtransDes, SetProbability.f:
- * 121-140; only the first species' row may be nonzero).  An empty site of
- * coordination n then carries deposition + absorption at
- * sum_s PtransD(s,n) + PtransAbs(1,n) (Get_Prob.f:155-204), a covered site
- * desorbs at PtransDes(1,n) (:93-118), and an atom's evaporation key counts
- * its covered neighbours (PE(NSiC,n1,n2,0,c,0,0), :309-312).  Replaces
- * IndexEvent_Abs / absorption.f / desorption.f.                            */
+/* Coverage species (NCov = 1 with NCrystal <= 2, or NCov = 2 with NCrystal
+ * = 1): ptransAbs, ptransDes are 3x3 doubles [coverage species][coor-1]
+ * (PtransAbs / PtransDes, SetProbability.f:121-140; rows past NCov must be
+ * zero).  An empty site of coordination n then carries deposition +
+ * absorption at sum_s PtransD(s,n) + sum_i PtransAbs(i,n) (Get_Prob.f:
+ * 155-204), the species absorbed drawn past the deposition share by the
+ * cumulative PtransAbs (IndexEvent_Abs, :22-52); a site covered by species i
+ * desorbs at PtransDes(i,n) (:93-118); an atom's evaporation key counts its
+ * covered neighbours of each species (PE(NSiC,n1,n2,0,c1,c2,0), :309-312).
+ * mks_replay takes itrans 5 for a desorption and 5+i for an absorption of
+ * species i (main.f:346-356).  Replaces IndexEvent_Abs / absorption.f /
+ * desorption.f.                                                           */
 int mks_set_coverage_rates(mks_handle *h, const double *ptransAbs, const double *ptransDes);
 /* kind 'S' = SetSi (InitSt FS), 'C' = SetSiC3C (InitSt F); len1 is the slab
  * height, rounded down to a multiple of 24 as main.f:226,238 does.         */

@@ -681,6 +681,46 @@ __device__ void apply(const Dev &D, Ctx &c, int r, float u)
 // ---- kernels ----
 constexpr unsigned FULL = 0xffffffffu;
 
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+__device__ __forceinline__ bool in_arrays(const Dev &D, P3 p)
+{
+    return p.x >= 0 && p.x < D.lx && p.y >= 0 && p.y < D.ly && p.z >= -ZG && p.z <= D.lz + ZG;
+}
+__device__ __forceinline__ void prefetch_site(const Dev &D, P3 p)
+{
+    if (!in_arrays(D, p)) return;
+    const int64_t g = ((int64_t)(p.z + ZG) * D.ly + p.y) * D.lx + p.x;
+    prefetch_l1(&D.coo[g]);
+    const int r = D.ind[g];
+    if (r > 0) {
+        prefetch_l1(&D.rec[r]);
+        prefetch_l1(reinterpret_cast<const char *>(&D.rec[r]) + sizeof(Rec) - 1);
+    }
+}
+
+// Before lane 0 applies the event of record r, the warp brings the words it
+// will read into L1: the site, its four NextN sites and their sixteen NextN
+// sites (LattCoo word, LattInd and record each; lane 0 + lanes 1..4 + lanes
+// 5..20).  The event then runs on L1 hits instead of a chain of L2 round
+// trips.  Reads only: a point outside the arrays is skipped.
+__device__ void prefetch_event(const Dev &D, int r, int lane)
+{
+    const Rec &R = D.rec[r];
+    if (lane == 0) {
+        prefetch_site(D, P3{R.x, R.y, R.z});
+    } else if (lane <= 4) {
+        prefetch_site(D, nn_at(R, lane - 1));
+    } else if (lane <= 20) {
+        const P3 q = nn_at(R, (lane - 5) >> 2);
+        if (!in_arrays(D, q)) return;
+        const int rq = D.ind[((int64_t)(q.z + ZG) * D.ly + q.y) * D.lx + q.x];
+        if (rq > 0) prefetch_site(D, nn_at(D.rec[rq], (lane - 5) & 3));
+    }
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
 
 // One colour phase: every tile of the colour runs from the window's start to
@@ -821,6 +861,8 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
             if (pick < 0) pick = last;       // rounding at the top end
         }
         if (pick <= 0) break;
+        prefetch_event(D, pick, lane);
+        __syncwarp();
         if (lane == 0) apply(D, c, pick, u01(rnd.w));
         nev++;
         __syncwarp();
