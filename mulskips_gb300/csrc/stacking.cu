@@ -803,21 +803,33 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
     uint32_t nev = 0, ndraw = 0;
     for (;;) {
         const int len = min(*(volatile int32_t *)&D.tl_n[t], LCAP);
+        // lane l owns the contiguous chunk [l C, l C + C) of the list: one
+        // pass of independent loads gives each lane its partial sum, a warp
+        // scan the prefix of every chunk
+        const int C = (len + 31) >> 5;
+        const int i0 = min(len, lane * C), i1 = min(len, i0 + C);
         float s = 0.f;
         int niso = 0;
-        for (int i = lane; i < len; i += 32) {
+        for (int i = i0; i < i1; i++) {
             const float v = rates[i];
             if (v > 0.f) s += v;
             else if (v < 0.f) niso++;
         }
+        float inc = s;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s += __shfl_xor_sync(FULL, s, o);
-            niso += __shfl_xor_sync(FULL, niso, o);
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += y;
         }
+        float excl = __shfl_up_sync(FULL, inc, 1);
+        if (lane == 0) excl = 0.f;
+        const float tot = __shfl_sync(FULL, inc, 31);
+        int nisot = niso;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nisot += __shfl_xor_sync(FULL, nisot, o);
         // isolated atoms: 1e5 x the total rate (Get_Prob.f:305), the tile's here
-        const float riso = niso ? (float)niso * 1.0e5f * fmaxf(s, 1.0e-30f) : 0.f;
-        const float rtot = s + riso;
+        const float riso = nisot ? (float)nisot * 1.0e5f * fmaxf(tot, 1.0e-30f) : 0.f;
+        const float rtot = tot + riso;
         if (!(rtot > 0.f)) break;
         U4 rnd = philox4x32_10(U4{ndraw++, (uint32_t)t, window, 0x51000000u | (uint32_t)colour}, D.k0, D.k1);
         float dt = -__logf(u01(rnd.x)) / rtot;
@@ -825,9 +837,9 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
         rem -= dt;
         float target = u01(rnd.y) * rtot;
         int pick = -1;
-        if (target >= s && niso > 0) {
+        if (target >= tot && nisot > 0) {
             // the k-th isolated atom of the list
-            int k = min((int)(u01(rnd.z) * (float)niso), niso - 1);
+            int k = min((int)(u01(rnd.z) * (float)nisot), nisot - 1);
             for (int base = 0; base < len && pick < 0; base += 32) {
                 int i = base + lane;
                 const bool hit = i < len && rates[i] < 0.f;
@@ -839,26 +851,27 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
                 k -= __popc(m);
             }
         } else {
-            // cumulative rates in list order: the first entry past the target
-            float run = 0.f;
-            int last = -1;
-            for (int base = 0; base < len && pick < 0; base += 32) {
-                int i = base + lane;
-                float v = i < len ? fmaxf(rates[i], 0.f) : 0.f;
-                float cum = v;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    float y = __shfl_up_sync(FULL, cum, o);
-                    if (lane >= o) cum += y;
+            // the chunk whose prefix range holds the target, then its entry
+            // (rounding at the top end: the last entry with a rate)
+            const unsigned m = __ballot_sync(FULL, s > 0.f && inc > target);
+            const unsigned nz = __ballot_sync(FULL, s > 0.f);
+            if (nz) {
+                const int L = m ? __ffs(m) - 1 : 31 - __clz(nz);
+                int p = -1;
+                if (lane == L) {
+                    float acc = excl;
+                    int lastnz = -1;
+                    for (int i = i0; i < i1; i++) {
+                        const float v = rates[i];
+                        if (!(v > 0.f)) continue;
+                        lastnz = i;
+                        acc += v;
+                        if (acc > target) break;
+                    }
+                    p = lastnz >= 0 ? list[lastnz] : -1;
                 }
-                cum += run;
-                unsigned m = __ballot_sync(FULL, v > 0.f && cum > target);
-                unsigned nz = __ballot_sync(FULL, v > 0.f);
-                if (nz) last = list[base + 31 - __clz(nz)];
-                if (m) pick = list[base + __ffs(m) - 1];
-                run = __shfl_sync(FULL, cum, 31);
+                pick = __shfl_sync(FULL, p, L);
             }
-            if (pick < 0) pick = last;       // rounding at the top end
         }
         if (pick <= 0) break;
         prefetch_event(D, pick, lane);

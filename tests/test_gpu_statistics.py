@@ -94,6 +94,8 @@ def gpu_sample(b, tau, nwin, box, sf, cov=False):
         so = an.state_observables(b.state(r), cov)
         m, rms = so["mean_height"], so["rms_roughness"]
         assert abs(obs[r]["mean_height"] - m) < 1e-9 * max(1.0, m) and abs(obs[r]["rms_roughness"] - rms) < 1e-9 * max(1.0, rms)
+        assert obs[r]["covered"] == so["covered"]
+        obs[r]["covered2"] = so["covered2"]        # the device's count holds both coverage species
     return [(ts, hs[r], obs[r]) for r in range(b.n)]
 
 
