@@ -57,7 +57,7 @@ constexpr int FCAP = 1024;          // free records per tile and stack
 enum : uint8_t { EV_NONE = 0, EV_DEP = 1, EV_DUMMY = 2, EV_EVAP = 4, EV_ISO = 5 };
 enum : uint8_t { F_LISTED = 1 };
 // device error codes (err[0]); err[1..3] say where
-enum { E_INVARIANT = 3, E_CAPACITY = 4, E_NOTAPPLICABLE = 7, E_BOUNDS = 8, E_NBUFF = 9, E_ARM = 10 };
+enum { E_INVARIANT = 3, E_CAPACITY = 4, E_TIMEOUT = 6, E_NOTAPPLICABLE = 7, E_BOUNDS = 8, E_NBUFF = 9, E_ARM = 10 };
 
 struct Rec {
     int16_t x, y, z;
@@ -88,6 +88,7 @@ struct Dev {
     int32_t *nmc;              // sites with an event (NumAdAtom)
     unsigned long long *events;
     int32_t *stop;             // set when fewer than 21 sites keep an event
+    unsigned *windows_done;    // windows completed by the persistent kernel
     const double *pe;          // [3][4][4][4]: PTransE(s, n1, n2, n3, 0, 0, 0)
     const double *pd;          // [3][3]: PTransD(s, coor)
     double cth[2], sth[2];     // FIND_NN: cos, sin of 2 pi irot / 3 (pi in single precision)
@@ -725,15 +726,14 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 
 // One colour phase: every tile of the colour runs from the window's start to
 // its end (one warp per tile).
-__global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
+// tile k of colour `colour` runs from the window's start to its end (one
+// warp; every lane of the warp calls this)
+__device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float tau)
 {
     const int lane = threadIdx.x & 31;
-    const int wid = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    const int hx = D.ntx / 2, hy = D.nty / 2;
-    if (wid >= hx * hy) return;
-    const int ti = 2 * (wid % hx) + (colour & 1), tj = 2 * (wid / hx) + (colour >> 1);
+    const int hx = D.ntx / 2;
+    const int ti = 2 * (k % hx) + (colour & 1), tj = 2 * (k / hx) + (colour >> 1);
     const int t = tj * D.ntx + ti;
-    if (*(volatile int32_t *)D.err || *(volatile int32_t *)D.stop) return;
     int32_t *list = D.tl + (int64_t)t * LCAP;
     float *rates = D.tr + (int64_t)t * LCAP;
     // records freed in the tile's last phase become reusable
@@ -887,6 +887,61 @@ __global__ void k_phase(Dev D, int colour, uint32_t window, float tau)
     }
 }
 
+// Grid-wide barrier of a cooperative launch (generation counter; all blocks
+// are resident).  The wait is bounded: after `limit` cycles the block sets
+// E_TIMEOUT and leaves, and every block sees the error after its own wait.
+__device__ void grid_barrier(const Dev &D, unsigned *bar, long long limit)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                if (clock64() - t0 > limit) {
+                    set_err(D, E_TIMEOUT, (int)blockIdx.x, 0, 0);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Persistent form: `nwin` windows from `w0`, the four colour phases of each
+// separated by grid barriers; every warp takes the tiles wid, wid + W, ...
+// of the colour.  At each window's start the replica stops once fewer than
+// 21 sites keep an event (main.f:307-310) or `ev_limit` events are done.
+__global__ void k_windows(Dev D, uint32_t w0, int nwin, float tau, unsigned long long ev_limit, unsigned *bar,
+                          long long limit)
+{
+    const int wid = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const int per = (D.ntx / 2) * (D.nty / 2);
+    for (int w = 0; w < nwin; w++) {
+        if (*(volatile int32_t *)D.err || *(volatile int32_t *)D.stop) return;
+        if (*(volatile int32_t *)D.nmc <= 20 || (ev_limit && *(volatile unsigned long long *)D.events >= ev_limit)) {
+            grid_barrier(D, bar, limit);            // every block reads the counters before any sets stop
+            if (blockIdx.x == 0 && threadIdx.x == 0) *D.stop = *(volatile int32_t *)D.nmc <= 20 ? 1 : 2;
+            return;
+        }
+        for (int colour = 0; colour < 4; colour++) {
+            for (int k = wid; k < per; k += nw) run_tile(D, colour, k, w0 + (uint32_t)w, tau);
+            grid_barrier(D, bar, limit);
+            if (*(volatile int32_t *)D.err) return;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(D.windows_done, 1u);
+    }
+}
+
 // the replay: events in order on one thread
 __global__ void k_replay(Dev D, const mks_event *ev, long long n, long long *done)
 {
@@ -987,10 +1042,6 @@ __global__ void k_rebuild(Dev D, int last)
     }
 }
 
-__global__ void k_stop_check(Dev D)
-{
-    if (threadIdx.x == 0 && *D.nmc <= 20) *D.stop = 1;      // main.f:307-310
-}
 
 // compact lattice -> LattCoo words and records.  Pass 1 counts the listed
 // sites of each (z1, b) row; pass 2 writes them with ids from the row offsets.
@@ -1183,6 +1234,7 @@ struct State {
     double time = 0.0;
     int64_t window = 0, events = 0;
     int32_t *d_scratch = nullptr;
+    unsigned *d_bar = nullptr;   // grid barrier of the persistent kernel (count, generation)
     double *d_tab = nullptr;
     int stop_reason = 0;
     int last_error = 0;
@@ -1230,6 +1282,7 @@ const char *derr_name(int code)
     case E_BOUNDS: return "grid point outside the box";
     case E_NBUFF: return "no occupied neighbour lists the site (stale NBuff)";
     case E_ARM: return "stacking choice differs from the trace";
+    case E_TIMEOUT: return "a block waited too long at the grid barrier";
     default: return "device error";
     }
 }
@@ -1243,8 +1296,9 @@ int check_device(State *s, std::string &err, const char *what)
     SK(cudaMemsetAsync(s->D.err, 0, 4 * sizeof(int32_t), s->stream));
     SK(cudaStreamSynchronize(s->stream));
     s->last_error = e[0];
-    int code = e[0] == E_CAPACITY ? MKS_ERR_CAPACITY : (e[0] == E_NOTAPPLICABLE || e[0] == E_ARM ? MKS_ERR_ARG
-                                                                                                 : MKS_ERR_INVARIANT);
+    int code = e[0] == E_CAPACITY ? MKS_ERR_CAPACITY
+             : e[0] == E_TIMEOUT ? MKS_ERR_TIMEOUT
+             : (e[0] == E_NOTAPPLICABLE || e[0] == E_ARM) ? MKS_ERR_ARG : MKS_ERR_INVARIANT;
     return ferr(err, code, "%s: %s at (%d, %d, %d)", what, derr_name(e[0]), e[1], e[2], e[3]);
 }
 
@@ -1357,6 +1411,8 @@ int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string 
     D.stop = sc + 5;
     D.top = sc + 6;
     D.events = reinterpret_cast<unsigned long long *>(sc + 8);
+    D.windows_done = reinterpret_cast<unsigned *>(sc + 12);
+    s->d_bar = reinterpret_cast<unsigned *>(sc + 13);     // 2 words
     D.pe = s->d_tab;
     D.pd = s->d_tab + 192;
     cudaError_t e = cudaMemsetAsync(s->d_scratch, 0, sizeof(int32_t) * 16 + sizeof(unsigned long long) * 2, stream);
@@ -1586,10 +1642,18 @@ int run(State *s, double tau, int64_t max_windows, int64_t max_events, double ma
     SK(cudaMemsetAsync(D.stop, 0, sizeof(int32_t), s->stream));
     SK(cudaStreamSynchronize(s->stream));
     s->stop_reason = 0;
-    const int warps = D.ntx * D.nty / 4;
-    const int blocks = (warps * 32 + 127) / 128;
+    // one cooperative launch per block of windows: every block resident, the
+    // warps striding over the tiles of each colour
+    const int per = (D.ntx / 2) * (D.nty / 2);
+    int dev = 0, nsm = 0, per_sm = 0;
+    SK(cudaGetDevice(&dev));
+    SK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    SK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_windows, 128, 0));
+    if (per_sm < 1) return ferr(err, MKS_ERR_CUDA, "the window kernel cannot be resident");
+    const int blocks = (int)std::min<int64_t>((int64_t)(per * 32 + 127) / 128, (int64_t)nsm * per_sm);
+    const long long limit = 4000000000LL;        // cycles a block waits at a barrier (about 2 s)
     int64_t w = 0;
-    const int64_t batch = 8;
+    const int64_t batch = 64;
     unsigned long long ev = e0;
     while (max_windows <= 0 || w < max_windows) {
         int64_t nb = max_windows > 0 ? std::min<int64_t>(batch, max_windows - w) : batch;
@@ -1601,30 +1665,32 @@ int run(State *s, double tau, int64_t max_windows, int64_t max_events, double ma
             }
             nb = std::min(nb, left);
         }
-        for (int64_t k = 0; k < nb; k++) {
-            k_stop_check<<<1, 32, 0, s->stream>>>(D);
-            for (int colour = 0; colour < 4; colour++)
-                k_phase<<<blocks, 128, 0, s->stream>>>(D, colour, (uint32_t)(s->window + k), (float)tau);
-        }
-        SK(cudaGetLastError());
+        SK(cudaMemsetAsync(s->d_bar, 0, 2 * sizeof(unsigned), s->stream));
+        SK(cudaMemsetAsync(D.windows_done, 0, sizeof(unsigned), s->stream));
+        uint32_t w0 = (uint32_t)s->window;
+        int nwin = (int)nb;
+        float ftau = (float)tau;
+        unsigned long long ev_limit = max_events > 0 ? e0 + (unsigned long long)max_events : 0ull;
+        unsigned *bar = s->d_bar;
+        long long lim = limit;
+        void *args[] = {&D, &w0, &nwin, &ftau, &ev_limit, &bar, &lim};
+        SK(cudaLaunchCooperativeKernel((const void *)k_windows, dim3(blocks), dim3(128), args, 0, s->stream));
         int rc = check_device(s, err, "run");
         if (rc) {
             s->lists_ok = false;
             return rc;
         }
         int32_t stop = 0;
+        unsigned done = 0;
         SK(cudaMemcpyAsync(&ev, D.events, sizeof ev, cudaMemcpyDeviceToHost, s->stream));
         SK(cudaMemcpyAsync(&stop, D.stop, sizeof stop, cudaMemcpyDeviceToHost, s->stream));
+        SK(cudaMemcpyAsync(&done, D.windows_done, sizeof done, cudaMemcpyDeviceToHost, s->stream));
         SK(cudaStreamSynchronize(s->stream));
-        s->window += nb;
-        s->time += (double)nb * tau;
-        w += nb;
+        s->window += done;
+        s->time += (double)done * tau;
+        w += done;
         if (stop) {
-            s->stop_reason = 1;
-            break;
-        }
-        if (max_events > 0 && (int64_t)(ev - e0) >= max_events) {
-            s->stop_reason = 2;
+            s->stop_reason = stop == 1 ? 1 : 2;
             break;
         }
     }
