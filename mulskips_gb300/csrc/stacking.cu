@@ -91,6 +91,8 @@ struct Dev {
     unsigned *windows_done;    // windows completed by the persistent kernel
     const double *pe;          // [3][4][4][4]: PTransE(s, n1, n2, n3, 0, 0, 0)
     const double *pd;          // [3][3]: PTransD(s, coor)
+    const float *pef;          // the same PTransE entries in FP32
+    const float *pds;          // [3] FP32 of the FP64 sum of PTransD(s, coor) over s; [3..8] species shares
     double cth[2], sth[2];     // FIND_NN: cos, sin of 2 pi irot / 3 (pi in single precision)
     double shift;              // FIND_SN: arm-chair shift 8.6602254037 (single precision)
     double pzig;               // PtransZig
@@ -180,14 +182,14 @@ __device__ void get_prob(const Dev &D, int occ, int nsic, int coor, P3 site, con
             int cnn = coor_of(cw(D, nn[0]));
             if (cnn >= 2) {
                 ev = EV_DEP;
-                rate = (float)(pd_of(D, 1, 1) + pd_of(D, 2, 1) + pd_of(D, 3, 1));
+                rate = D.pds[0];
             } else {
                 ev = EV_DUMMY;        // Get_Prob.f:181-184
                 rate = 1.e-8f;
             }
         } else if (coor == 2 || coor == 3) {
             ev = EV_DEP;
-            rate = (float)(pd_of(D, 1, coor) + pd_of(D, 2, coor) + pd_of(D, 3, coor));
+            rate = D.pds[coor - 1];
         } else {
             ev = EV_NONE;
             rate = 0.f;
@@ -225,7 +227,7 @@ __device__ void get_prob(const Dev &D, int occ, int nsic, int coor, P3 site, con
     } else {
         int s = nsic >= 1 && nsic <= 3 ? nsic : 1;
         ev = EV_EVAP;
-        rate = (float)D.pe[(s - 1) * 64 + (nsi + nw) * 16 + nc * 4 + nb];
+        rate = D.pef[(s - 1) * 64 + (nsi + nw) * 16 + nc * 4 + nb];
     }
 }
 
@@ -335,7 +337,58 @@ __device__ void drop_site(const Dev &D, Ctx &c, P3 p)
 // ---- geometry: FIND_SN.f:26-84, FIND_NN.f:25-77, IF_Arm_Choice.f:21-56 ----
 // FP64 as the reference, each product and sum rounded on its own (no fused
 // multiply-add), NINT to the grid.
+// NINT of v when the FP32 value v32 (within 1e-3 of v) is not near a
+// rounding half: the two round alike; -2^30 otherwise (take the FP64 form)
+__device__ __forceinline__ int nint_safe(float v32)
+{
+    const float f = fabsf(v32 - truncf(v32));
+    return fabsf(f - 0.5f) < 1.0e-3f ? -(1 << 30) : (int)rintf(v32);
+}
+
+__device__ void find_sn_fp64(const Dev &D, P3 site, P3 sitec, const P3 sn_in[3], P3 zig[3], P3 arm[3]);
+
+// FIND_SN in FP32 where that gives the FP64 result: the zig-zag sites are
+// integer arithmetic (2 cent - sn = site + sitec - sn); an arm-chair
+// coordinate sn + shift ax rounds as in FP64 unless the FP32 value lies
+// within 1e-3 of a half (FP32's error here is below 1e-4), and then the FP64
+// form runs.  GB300's FP64 rate is a small fraction of its FP32 rate.
 __device__ void find_sn(const Dev &D, P3 site, P3 sitec, const P3 sn_in[3], P3 zig[3], P3 arm[3])
+{
+    const int lx = D.lx, ly = D.ly;
+    P3 sn[3] = {sn_in[0], sn_in[1], sn_in[2]};
+    P3 c = sitec;
+    if (abs(site.x - c.x) > lx / 2) c.x += isign(lx, site.x - c.x);
+    if (abs(site.y - c.y) > ly / 2) c.y += isign(ly, site.y - c.y);
+    for (int i = 0; i < 3; i++) {
+        if (abs(site.x - sn[i].x) > lx / 2) sn[i].x += isign(lx, site.x - sn[i].x);
+        if (abs(site.y - sn[i].y) > ly / 2) sn[i].y += isign(ly, site.y - sn[i].y);
+    }
+    const int d3[3] = {site.x - c.x, site.y - c.y, site.z - c.z};
+    const float inv = 1.0f / sqrtf((float)(d3[0] * d3[0] + d3[1] * d3[1] + d3[2] * d3[2]));
+    const float sh = (float)D.shift;
+    int off[3];
+    for (int k = 0; k < 3; k++) {
+        off[k] = nint_safe(sh * ((float)d3[k] * inv));
+        if (off[k] == -(1 << 30)) {
+            find_sn_fp64(D, site, sitec, sn_in, zig, arm);
+            return;
+        }
+    }
+    for (int i = 0; i < 3; i++) {
+        zig[i] = P3{site.x + c.x - sn[i].x, site.y + c.y - sn[i].y, site.z + c.z - sn[i].z};
+        arm[i] = P3{sn[i].x + off[0], sn[i].y + off[1], sn[i].z + off[2]};
+        if (zig[i].x >= lx) zig[i].x -= lx;
+        if (zig[i].x < 0) zig[i].x += lx;
+        if (zig[i].y >= ly) zig[i].y -= ly;
+        if (zig[i].y < 0) zig[i].y += ly;
+        if (arm[i].x >= lx) arm[i].x -= lx;
+        if (arm[i].x < 0) arm[i].x += lx;
+        if (arm[i].y >= ly) arm[i].y -= ly;
+        if (arm[i].y < 0) arm[i].y += ly;
+    }
+}
+
+__device__ void find_sn_fp64(const Dev &D, P3 site, P3 sitec, const P3 sn_in[3], P3 zig[3], P3 arm[3])
 {
     const int lx = D.lx, ly = D.ly;
     P3 sn[3] = {sn_in[0], sn_in[1], sn_in[2]};
@@ -373,7 +426,52 @@ __device__ void find_sn(const Dev &D, P3 site, P3 sitec, const P3 sn_in[3], P3 z
     }
 }
 
+__device__ void find_nn_fp64(const Dev &D, P3 s1, P3 s2, P3 sc, P3 out[2]);
+
+// FIND_NN in FP32 where that gives the FP64 result (see find_sn); the
+// rotated coordinates are at most a bond long, FP32's error below 1e-5
 __device__ void find_nn(const Dev &D, P3 s1, P3 s2, P3 sc, P3 out[2])
+{
+    const int lx = D.lx, ly = D.ly;
+    P3 a = s1, b = s2;
+    if (abs(sc.x - a.x) > lx / 2) a.x += isign(lx, sc.x - a.x);
+    if (abs(sc.y - a.y) > ly / 2) a.y += isign(ly, sc.y - a.y);
+    if (abs(sc.x - b.x) > lx / 2) b.x += isign(lx, sc.x - b.x);
+    if (abs(sc.y - b.y) > ly / 2) b.y += isign(ly, sc.y - b.y);
+    const int d3[3] = {sc.x - a.x, sc.y - a.y, sc.z - a.z};
+    const float t3[3] = {(float)(b.x - sc.x), (float)(b.y - sc.y), (float)(b.z - sc.z)};
+    const float inv = 1.0f / sqrtf((float)(d3[0] * d3[0] + d3[1] * d3[1] + d3[2] * d3[2]));
+    const float ax[3] = {(float)d3[0] * inv, (float)d3[1] * inv, (float)d3[2] * inv};
+    const int c3[3] = {sc.x, sc.y, sc.z};
+    for (int irot = 0; irot < 2; irot++) {
+        const float cth = (float)D.cth[irot], sth = (float)D.sth[irot], omc = 1.0f - cth;
+        float rot[3][3];
+        for (int i = 0; i < 3; i++) rot[i][i] = ax[i] * ax[i] * omc + cth;
+        rot[1][0] = ax[0] * ax[1] * omc - ax[2] * sth;
+        rot[0][1] = ax[0] * ax[1] * omc + ax[2] * sth;
+        rot[2][0] = ax[0] * ax[2] * omc + ax[1] * sth;
+        rot[0][2] = ax[0] * ax[2] * omc - ax[1] * sth;
+        rot[2][1] = ax[1] * ax[2] * omc - ax[0] * sth;
+        rot[1][2] = ax[1] * ax[2] * omc + ax[0] * sth;
+        int o3[3];
+        for (int k = 0; k < 3; k++) {
+            const int q = nint_safe(rot[0][k] * t3[0] + rot[1][k] * t3[1] + rot[2][k] * t3[2]);
+            if (q == -(1 << 30)) {
+                find_nn_fp64(D, s1, s2, sc, out);
+                return;
+            }
+            o3[k] = q + c3[k];
+        }
+        P3 p{o3[0], o3[1], o3[2]};
+        if (p.x >= lx) p.x -= lx;
+        if (p.x < 0) p.x += lx;
+        if (p.y >= ly) p.y -= ly;
+        if (p.y < 0) p.y += ly;
+        out[irot] = p;
+    }
+}
+
+__device__ void find_nn_fp64(const Dev &D, P3 s1, P3 s2, P3 sc, P3 out[2])
 {
     const int lx = D.lx, ly = D.ly;
     if (abs(sc.x - s1.x) > lx / 2) s1.x += isign(lx, sc.x - s1.x);
@@ -672,9 +770,7 @@ __device__ void apply(const Dev &D, Ctx &c, int r, float u)
     if (R.ev == EV_DEP) {
         int co = coor_of(cw(D, site));
         co = co < 1 ? 1 : (co > 3 ? 3 : co);
-        double p1 = pd_of(D, 1, co), p2 = pd_of(D, 2, co), p3 = pd_of(D, 3, co);
-        double pc = (double)u * (p1 + p2 + p3);
-        sp = pc <= p1 ? 1 : (pc > p1 + p2 ? 3 : 2);
+        sp = u < D.pds[3 + 2 * (co - 1)] ? 1 : (u < D.pds[4 + 2 * (co - 1)] ? 2 : 3);
     }
     deposition(D, c, site, sp);
 }
@@ -1236,6 +1332,7 @@ struct State {
     int32_t *d_scratch = nullptr;
     unsigned *d_bar = nullptr;   // grid barrier of the persistent kernel (count, generation)
     double *d_tab = nullptr;
+    float *d_tabf = nullptr;
     int stop_reason = 0;
     int last_error = 0;
 };
@@ -1262,13 +1359,24 @@ int ferr(std::string &err, int code, const char *fmt, ...)
 int upload_tables(State *s, std::string &err)
 {
     double tab[192 + 9];
+    float tf[192 + 9];
     for (int sp = 0; sp < 3; sp++)
         for (int n1 = 0; n1 < 4; n1++)
             for (int n2 = 0; n2 < 4; n2++)
                 for (int n3 = 0; n3 < 4; n3++)
                     tab[sp * 64 + n1 * 16 + n2 * 4 + n3] = s->ptransE[sp * 4096 + n1 * 1024 + n2 * 256 + n3 * 64];
     for (int k = 0; k < 9; k++) tab[192 + k] = s->ptransD[k];
+    for (int k = 0; k < 192; k++) tf[k] = (float)tab[k];
+    for (int co = 1; co <= 3; co++) {
+        // Get_Prob.f:159-176: the deposition rate is the FP64 sum over species
+        const double p1 = s->ptransD[co - 1], p2 = s->ptransD[3 + co - 1], p3 = s->ptransD[6 + co - 1];
+        const double tot = p1 + p2 + p3;
+        tf[192 + co - 1] = (float)tot;
+        tf[195 + 2 * (co - 1)] = tot > 0 ? (float)(p1 / tot) : 1.f;
+        tf[196 + 2 * (co - 1)] = tot > 0 ? (float)((p1 + p2) / tot) : 1.f;
+    }
     SK(cudaMemcpyAsync(s->d_tab, tab, sizeof tab, cudaMemcpyHostToDevice, s->stream));
+    SK(cudaMemcpyAsync(s->d_tabf, tf, sizeof tf, cudaMemcpyHostToDevice, s->stream));
     SK(cudaStreamSynchronize(s->stream));
     return 0;
 }
@@ -1404,6 +1512,7 @@ int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string 
     SA(D.fp_n, sizeof(int32_t) * ntiles);
     SA(s->d_scratch, sizeof(int32_t) * 16 + sizeof(unsigned long long) * 2);
     SA(s->d_tab, sizeof(double) * (192 + 9));
+    SA(s->d_tabf, sizeof(float) * (192 + 9));
 #undef SA
     int32_t *sc = s->d_scratch;
     D.err = sc;                 // 4
@@ -1415,11 +1524,14 @@ int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string 
     s->d_bar = reinterpret_cast<unsigned *>(sc + 13);     // 2 words
     D.pe = s->d_tab;
     D.pd = s->d_tab + 192;
+    D.pef = s->d_tabf;
+    D.pds = s->d_tabf + 192;
     cudaError_t e = cudaMemsetAsync(s->d_scratch, 0, sizeof(int32_t) * 16 + sizeof(unsigned long long) * 2, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(D.coo, 0, sizeof(uint32_t) * s->ngrid, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(D.ind, 0, sizeof(int32_t) * s->ngrid, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(D.rec, 0, sizeof(Rec), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_tab, 0, sizeof(double) * (192 + 9), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_tabf, 0, sizeof(float) * (192 + 9), stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
         ferr(err, MKS_ERR_CUDA, "clearing the lattice: %s", cudaGetErrorString(e));
@@ -1445,6 +1557,7 @@ void destroy(State *s)
     cudaFree(D.fp_n);
     cudaFree(s->d_scratch);
     cudaFree(s->d_tab);
+    cudaFree(s->d_tabf);
     delete s;
 }
 
