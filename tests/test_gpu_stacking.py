@@ -131,6 +131,24 @@ def test_stacking_replay_twinned_lattice(oracle_lib):
     assert off > 1000
 
 
+def test_stacking_replay_sic_facets(oracle_lib, tmp_path):
+    """Config 2's stacking preference (PtransZig = 0.5362, a 0.02 eV
+    preference for cubic stacking at 1600 K) on {111} facets: a 3C-SiC
+    square pyramid with {111} faces on a (001) slab (InitSt SH point list,
+    240^3 box), the reference's SiC `surface` rates.  About one coor-1
+    deposition in five takes the hexagonal position here; 300k events of
+    the oracle's trace replay exactly."""
+    from test_shape_points import pyramid_points, sh_startdat, write_points
+    xyz, sym, _, _ = pyramid_points(240, 60, 54)
+    write_points(tmp_path / "p.xyz", xyz, sym)
+    lines = [("0.5362 ! PtransZig" if "PtransZig" in ln else ln)
+             for ln in open(os.path.join(GOLDEN, "surface", "start.dat")).read().splitlines()]
+    p = tmp_path / "start.dat"
+    sh_startdat(lines, p, str(tmp_path / "p.xyz"))
+    done, arm, off = stacking_replay(oracle_lib, str(p), 0, 300000, 100000, box=240)
+    assert done == 300000 and arm > 1000
+
+
 def test_stacking_expands_initializer_lattice(oracle_lib):
     """The compact lattice of an initializer (SetNC, InitSt 'C') expanded to
     the explicit form equals the oracle's SetNC lattice: every LattCoo word,
