@@ -168,7 +168,6 @@ __device__ __forceinline__ float list_rate(const Rec &R)
     return R.ev == EV_NONE ? 0.f : (R.ev == EV_ISO ? -1.f : R.rate);
 }
 
-__device__ __forceinline__ double pd_of(const Dev &D, int s, int coor) { return D.pd[(s - 1) * 3 + coor - 1]; }
 
 // Get_Prob (Get_Prob.f:54-331) without coverage: the event code and FP32 rate
 // of a site from its LattCoo word and NextN.  An empty site carries the sum
@@ -264,14 +263,16 @@ __device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
     else if (ev) list_site(D, c, r);
 }
 
+// A record from the running tile's reusable stack, else a new one.  The
+// lanes of a warp may allocate at once (the neighbour updates of one event
+// run on four lanes): the stack is popped atomically, and nothing pushes to
+// it during a phase.
 __device__ int alloc_rec(const Dev &D, const Ctx &c)
 {
     int t = c.tile < 0 ? 0 : c.tile;
-    int n = D.fr_n[t];
-    if (n > 0) {
-        D.fr_n[t] = n - 1;
-        return D.fr[(int64_t)t * FCAP + n - 1];
-    }
+    int n = atomicSub(&D.fr_n[t], 1);
+    if (n > 0) return D.fr[(int64_t)t * FCAP + n - 1];
+    atomicAdd(&D.fr_n[t], 1);
     int r = atomicAdd(D.top, 1);
     if (r >= D.rcap) {
         set_err(D, E_CAPACITY, -2, r, 0);
@@ -290,11 +291,8 @@ __device__ void free_rec(const Dev &D, const Ctx &c, int r)
         }
         return;
     }
-    int n = D.fp_n[c.tile];
-    if (n < FCAP) {
-        D.fp[(int64_t)c.tile * FCAP + n] = r;
-        D.fp_n[c.tile] = n + 1;
-    }
+    int n = atomicAdd(&D.fp_n[c.tile], 1);   // a full stack drops the record (counted past FCAP)
+    if (n < FCAP) D.fp[(int64_t)c.tile * FCAP + n] = r;
 }
 
 // a new listed site (AddMC of a coor-1 empty site, Add.f:24-52)
@@ -533,6 +531,98 @@ __device__ int arm_choice(const Dev &D, Ctx &c, const P3 zig[3], const P3 arm[3]
 }
 
 // ---- events ----
+// Neighbour i (NextN entry n) of a deposition at `site`, deposition.f:
+// 78-235.  Returns the change of the site's own coordination that this
+// neighbour makes: a wall, or an atom that lists the site when the site had
+// coordination 1 (then only for i >= 1).  It reads and writes n, n's record
+// and n's own neighbours' words only: two neighbours of a site are never
+// bonded, so the four calls of one event are independent of one another.
+__device__ int dep_neighbour(const Dev &D, Ctx &c, P3 site, int coor_old, int i, P3 n)
+{
+    int inc = 0;
+    const int64_t gn = gidx(D, n);
+    const uint32_t vn = D.coo[gn];
+    const int rn = D.ind[gn];
+    int coornn = coor_of(vn);
+    const int covind = cov_of(vn);
+    uint8_t ev;
+    float rate;
+    if (!occ_of(vn)) {
+        if (coornn == 0) {                             // :86-99
+            D.coo[gn] = with_coor(vn, 1);
+            P3 nnn[4] = {site, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            get_prob(D, 0, 0, 1, n, nnn, ev, rate);
+            if (ev) new_site(D, c, n, nnn, ev, rate);
+        } else if (coornn == 1) {                      // :100-160
+            if (rn <= 0) {
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return 0;
+            }
+            Rec &N = D.rec[rn];
+            P3 nnn[4];
+            load_nn(N, nnn);
+            int dx = abs(nnn[0].x - site.x);
+            if (D.lx - dx < dx) dx = D.lx - dx;
+            int dy = abs(nnn[0].y - site.y);
+            if (D.ly - dy < dy) dy = D.ly - dy;
+            int dz = nnn[0].z - site.z;
+            if (dx * dx + dy * dy + dz * dz == 72) {
+                coornn = 2;
+                nnn[1] = site;
+                P3 ns[2];
+                find_nn(D, nnn[0], nnn[1], n, ns);
+                for (int k = 2; k < 4; k++) {
+                    nnn[k] = ns[k - 2];
+                    uint32_t v = cw(D, nnn[k]);
+                    if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND &&
+                        rec_lists(D, D.ind[gidx(D, nnn[k])], n))
+                        coornn++;
+                }
+                D.coo[gn] = with_coor(vn, coornn);
+                for (int k = 0; k < 4; k++) put_nn(N, k, nnn[k]);
+                get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+                set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddVoid
+            }
+        } else if (coornn == 2 || coornn == 3) {       // :161-191
+            if (rn <= 0) {
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return 0;
+            }
+            P3 nnn[4];
+            load_nn(D.rec[rn], nnn);
+            if (in_list(nnn, site)) {
+                coornn++;
+                D.coo[gn] = with_coor(vn, coornn);
+                get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+                set_event(D, c, rn, ev, rate);
+            }
+        }
+    } else if (covind != WALLIND) {                    // :192-230
+        if (covind != 0) {
+            set_err(D, E_INVARIANT, n.x, n.y, n.z);
+            return 0;
+        }
+        if (coornn <= 3) {
+            if (rn <= 0) {
+                set_err(D, E_INVARIANT, n.x, n.y, n.z);
+                return 0;
+            }
+            P3 nnn[4];
+            load_nn(D.rec[rn], nnn);
+            if (in_list(nnn, site)) {
+                coornn++;
+                D.coo[gn] = with_coor(vn, coornn);
+                get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
+                set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddBulk
+                if (coor_old == 1 && i >= 1) inc = 1;
+            }
+        }
+    } else {
+        inc = 1;                                       // a wall
+    }
+    return inc;
+}
+
 // Deposition of species sp on the empty site (deposition.f:24-251)
 __device__ void deposition(const Dev &D, Ctx &c, P3 site, int sp)
 {
@@ -568,87 +658,8 @@ __device__ void deposition(const Dev &D, Ctx &c, P3 site, int sp)
     P3 nextn[4];
     load_nn(R, nextn);
     for (int i = 0; i < 4; i++) {                          // :78-235
-        const P3 n = nextn[i];
-        const int64_t gn = gidx(D, n);
-        const uint32_t vn = D.coo[gn];
-        const int rn = D.ind[gn];
-        int coornn = coor_of(vn);
-        const int covind = cov_of(vn);
-        uint8_t ev;
-        float rate;
-        if (!occ_of(vn)) {
-            if (coornn == 0) {                             // :86-99
-                D.coo[gn] = with_coor(vn, 1);
-                P3 nnn[4] = {site, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-                get_prob(D, 0, 0, 1, n, nnn, ev, rate);
-                if (ev) new_site(D, c, n, nnn, ev, rate);
-            } else if (coornn == 1) {                      // :100-160
-                if (rn <= 0) {
-                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                    return;
-                }
-                Rec &N = D.rec[rn];
-                P3 nnn[4];
-                load_nn(N, nnn);
-                int dx = abs(nnn[0].x - site.x);
-                if (D.lx - dx < dx) dx = D.lx - dx;
-                int dy = abs(nnn[0].y - site.y);
-                if (D.ly - dy < dy) dy = D.ly - dy;
-                int dz = nnn[0].z - site.z;
-                if (dx * dx + dy * dy + dz * dz == 72) {
-                    coornn = 2;
-                    nnn[1] = site;
-                    P3 ns[2];
-                    find_nn(D, nnn[0], nnn[1], n, ns);
-                    for (int k = 2; k < 4; k++) {
-                        nnn[k] = ns[k - 2];
-                        uint32_t v = cw(D, nnn[k]);
-                        if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND &&
-                            rec_lists(D, D.ind[gidx(D, nnn[k])], n))
-                            coornn++;
-                    }
-                    D.coo[gn] = with_coor(vn, coornn);
-                    for (int k = 0; k < 4; k++) put_nn(N, k, nnn[k]);
-                    get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
-                    set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddVoid
-                }
-            } else if (coornn == 2 || coornn == 3) {       // :161-191
-                if (rn <= 0) {
-                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                    return;
-                }
-                P3 nnn[4];
-                load_nn(D.rec[rn], nnn);
-                if (in_list(nnn, site)) {
-                    coornn++;
-                    D.coo[gn] = with_coor(vn, coornn);
-                    get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
-                    set_event(D, c, rn, ev, rate);
-                }
-            }
-        } else if (covind != WALLIND) {                    // :192-230
-            if (covind != 0) {
-                set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                return;
-            }
-            if (coornn <= 3) {
-                if (rn <= 0) {
-                    set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                    return;
-                }
-                P3 nnn[4];
-                load_nn(D.rec[rn], nnn);
-                if (in_list(nnn, site)) {
-                    coornn++;
-                    D.coo[gn] = with_coor(vn, coornn);
-                    get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
-                    set_event(D, c, rn, ev, rate);         // no event: EraseMC + AddBulk
-                    if (coor_old == 1 && i >= 1) coor++;
-                }
-            }
-        } else {
-            coor++;
-        }
+        coor += dep_neighbour(D, c, site, coor_old, i, nextn[i]);
+        if (*(volatile int32_t *)D.err) return;
     }
     if (coor != coor_old) D.coo[gs] = with_coor(D.coo[gs], coor);   // :236-250
     uint8_t ev;
@@ -673,6 +684,65 @@ __device__ void prune_to_buffer(const Dev &D, Ctx &c, Rec &S, P3 site, bool &got
     put_nn(S, 0, c.nbuff);
 }
 
+// NextN entry n of an evaporating atom at `site`, Evaporation.f:46-215.
+// Returns -1 for a wall (the site's coordination drops), else 0.  Touches n,
+// n's record and reads n's neighbours only (independent of the other three,
+// as in deposition); the NBuff of a pruned coor-1 site is this call's (the
+// run treats a stale NBuff as an error, the replay carries it as the
+// reference does).
+__device__ int evap_neighbour(const Dev &D, Ctx &c, P3 site, P3 n)
+{
+    const int64_t gn = gidx(D, n);
+    const uint32_t vn = D.coo[gn];
+    const int rn = D.ind[gn];
+    int coornn = coor_of(vn);
+    const int covind = cov_of(vn);
+    uint8_t ev;
+    float rate;
+    if (!occ_of(vn)) {
+        if (coornn < 1 || coornn > 4) return 0;
+        if (rn <= 0) {                                 // a coordinated empty site is always listed
+            set_err(D, E_INVARIANT, n.x, n.y, n.z);
+            return 0;
+        }
+        P3 nnn[4];
+        load_nn(D.rec[rn], nnn);
+        if (!in_list(nnn, site)) return 0;
+        if (coornn == 1) {                             // :51-68
+            drop_site(D, c, n);
+            D.coo[gn] = 0;
+        } else if (coornn == 2) {                      // :69-123
+            D.coo[gn] = with_coor(vn, 1);
+            bool got = false;
+            prune_to_buffer(D, c, D.rec[rn], n, got);
+            if (!got && c.tile >= 0) set_err(D, E_NBUFF, n.x, n.y, n.z);
+            get_prob(D, 0, 0, 1, n, nnn, ev, rate);   // the list as it was before pruning
+            set_event(D, c, rn, ev, rate);
+        } else {                                       // :124-164 (coor 3 -> 2, void -> MC)
+            coornn--;
+            D.coo[gn] = with_coor(vn, coornn);
+            get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
+            set_event(D, c, rn, ev, rate);
+        }
+    } else if (covind != WALLIND) {                    // :166-210
+        if (covind != 0 || rn <= 0) {
+            set_err(D, E_INVARIANT, n.x, n.y, n.z);
+            return 0;
+        }
+        P3 nnn[4];
+        load_nn(D.rec[rn], nnn);
+        if (in_list(nnn, site)) {
+            coornn--;
+            D.coo[gn] = with_coor(vn, coornn);
+            get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
+            set_event(D, c, rn, ev, rate);             // bulk -> MC when coor was 4
+        }
+    } else {
+        return -1;                                     // a wall
+    }
+    return 0;
+}
+
 // Evaporation of the atom at site (Evaporation.f:25-262)
 __device__ void evaporation(const Dev &D, Ctx &c, P3 site)
 {
@@ -688,55 +758,8 @@ __device__ void evaporation(const Dev &D, Ctx &c, P3 site)
     P3 nextn[4];
     load_nn(D.rec[rs], nextn);
     for (int i = 0; i < 4; i++) {
-        const P3 n = nextn[i];
-        const int64_t gn = gidx(D, n);
-        const uint32_t vn = D.coo[gn];
-        const int rn = D.ind[gn];
-        int coornn = coor_of(vn);
-        const int covind = cov_of(vn);
-        uint8_t ev;
-        float rate;
-        if (!occ_of(vn)) {
-            if (coornn < 1 || coornn > 4) continue;
-            if (rn <= 0) {                                 // a coordinated empty site is always listed
-                set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                return;
-            }
-            P3 nnn[4];
-            load_nn(D.rec[rn], nnn);
-            if (!in_list(nnn, site)) continue;
-            if (coornn == 1) {                             // :51-68
-                drop_site(D, c, n);
-                D.coo[gn] = 0;
-            } else if (coornn == 2) {                      // :69-123
-                D.coo[gn] = with_coor(vn, 1);
-                bool got = false;
-                prune_to_buffer(D, c, D.rec[rn], n, got);
-                if (!got && c.tile >= 0) set_err(D, E_NBUFF, n.x, n.y, n.z);
-                get_prob(D, 0, 0, 1, n, nnn, ev, rate);   // the list as it was before pruning
-                set_event(D, c, rn, ev, rate);
-            } else {                                       // :124-164 (coor 3 -> 2, void -> MC)
-                coornn--;
-                D.coo[gn] = with_coor(vn, coornn);
-                get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
-                set_event(D, c, rn, ev, rate);
-            }
-        } else if (covind != WALLIND) {                    // :166-210
-            if (covind != 0 || rn <= 0) {
-                set_err(D, E_INVARIANT, n.x, n.y, n.z);
-                return;
-            }
-            P3 nnn[4];
-            load_nn(D.rec[rn], nnn);
-            if (in_list(nnn, site)) {
-                coornn--;
-                D.coo[gn] = with_coor(vn, coornn);
-                get_prob(D, 1, sp_of(vn), coornn, n, nnn, ev, rate);
-                set_event(D, c, rn, ev, rate);             // bulk -> MC when coor was 4
-            }
-        } else {
-            coor--;
-        }
+        coor += evap_neighbour(D, c, site, nextn[i]);
+        if (*(volatile int32_t *)D.err) return;
     }
     D.coo[gs] = with_coor(D.coo[gs], coor);                // :216-261
     if (coor == 0) {
@@ -755,28 +778,160 @@ __device__ void evaporation(const Dev &D, Ctx &c, P3 site)
     set_event(D, c, D.ind[gs], ev, rate);
 }
 
+// ---- kernels ----
+constexpr unsigned FULL = 0xffffffffu;
+
+// The same events with the four neighbour updates on lanes 1..4 at once
+// (all lanes of the warp call these).  Lane 0 updates the event site first
+// (deposition.f:43-74: occupancy, species and the stacking of a coor-1
+// site) and last (:236-250, Evaporation.f:216-261), the lanes between: their
+// updates touch disjoint words (two NextN sites of a site are never bonded),
+// and their changes of the site's coordination are summed.  A site whose
+// NextN list repeats a grid point (left by the reference's rounding only in
+// contrived geometry) takes the serial order.
+__device__ bool nn_distinct(const P3 nn[4])
+{
+    for (int i = 0; i < 4; i++)
+        for (int j = i + 1; j < 4; j++)
+            if (same(nn[i], nn[j])) return false;
+    return true;
+}
+
+__device__ void deposition_warp(const Dev &D, Ctx &c, P3 site, int sp, int lane)
+{
+    const int64_t gs = gidx(D, site);
+    int coor_old = 0, go = 0;
+    if (lane == 0) {
+        const int rs = D.ind[gs];
+        if (rs <= 0) {
+            set_err(D, E_INVARIANT, site.x, site.y, site.z);
+        } else {
+            uint32_t w = D.coo[gs];
+            coor_old = coor_of(w);
+            D.coo[gs] = (w & ~(7u << 27)) | B_OCC | ((uint32_t)sp << 27);
+            Rec &R = D.rec[rs];
+            if (coor_old == 1) {                           // :49-74
+                P3 sitec = nn_at(R, 0);
+                const Rec &Rc = D.rec[D.ind[gidx(D, sitec)]];
+                P3 sn[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                int j = 0;
+                for (int i = 0; i < 4; i++) {
+                    P3 q = nn_at(Rc, i);
+                    if (!same(q, site)) {
+                        if (j < 3) sn[j] = q;
+                        j++;
+                    }
+                }
+                P3 zig[3], arm[3];
+                find_sn(D, site, sitec, sn, zig, arm);
+                int a = arm_choice(D, c, zig, arm);
+                for (int i = 0; i < 3; i++) put_nn(R, i + 1, a ? arm[i] : zig[i]);
+            }
+            P3 nn[4];
+            load_nn(R, nn);
+            go = nn_distinct(nn) ? 1 : 2;
+        }
+    }
+    go = __shfl_sync(FULL, go, 0);
+    coor_old = __shfl_sync(FULL, coor_old, 0);
+    __syncwarp();
+    if (!go) return;
+    P3 nextn[4];
+    load_nn(D.rec[D.ind[gs]], nextn);
+    int inc = 0;
+    if (go == 1) {
+        if (lane >= 1 && lane <= 4) inc = dep_neighbour(D, c, site, coor_old, lane - 1, nextn[lane - 1]);
+    } else if (lane == 0) {
+        for (int i = 0; i < 4; i++) inc += dep_neighbour(D, c, site, coor_old, i, nextn[i]);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) inc += __shfl_xor_sync(FULL, inc, o);   // lanes 0..7 hold the sum
+    __syncwarp();
+    if (lane == 0 && !*(volatile int32_t *)D.err) {
+        const int coor = coor_old + inc;
+        if (coor != coor_old) D.coo[gs] = with_coor(D.coo[gs], coor);    // :236-250
+        uint8_t ev;
+        float rate;
+        get_prob(D, 1, sp, coor, site, nextn, ev, rate);
+        set_event(D, c, D.ind[gs], ev, rate);
+    }
+    __syncwarp();
+}
+
+__device__ void evaporation_warp(const Dev &D, Ctx &c, P3 site, int lane)
+{
+    const int64_t gs = gidx(D, site);
+    int coor_old = 0, go = 0;
+    if (lane == 0) {
+        const int rs = D.ind[gs];
+        if (rs <= 0) {
+            set_err(D, E_INVARIANT, site.x, site.y, site.z);
+        } else {
+            uint32_t w = D.coo[gs];
+            coor_old = coor_of(w);
+            D.coo[gs] = w & ~(B_OCC | (7u << 27));
+            P3 nn[4];
+            load_nn(D.rec[rs], nn);
+            go = nn_distinct(nn) ? 1 : 2;
+        }
+    }
+    go = __shfl_sync(FULL, go, 0);
+    coor_old = __shfl_sync(FULL, coor_old, 0);
+    __syncwarp();
+    if (!go) return;
+    P3 nextn[4];
+    load_nn(D.rec[D.ind[gs]], nextn);
+    int dec = 0;
+    if (go == 1) {
+        if (lane >= 1 && lane <= 4) dec = evap_neighbour(D, c, site, nextn[lane - 1]);
+    } else if (lane == 0) {
+        for (int i = 0; i < 4; i++) dec += evap_neighbour(D, c, site, nextn[i]);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) dec += __shfl_xor_sync(FULL, dec, o);
+    __syncwarp();
+    if (lane == 0 && !*(volatile int32_t *)D.err) {
+        const int coor = coor_old + dec;
+        D.coo[gs] = with_coor(D.coo[gs], coor);                          // :216-261
+        if (coor == 0) {
+            drop_site(D, c, site);
+        } else {
+            uint8_t ev;
+            float rate;
+            get_prob(D, 0, 0, coor, site, nextn, ev, rate);
+            Rec &S = D.rec[D.ind[gs]];
+            if (coor == 1) {
+                bool got = false;
+                prune_to_buffer(D, c, S, site, got);
+                if (!got) set_err(D, E_NBUFF, site.x, site.y, site.z);
+            }
+            set_event(D, c, D.ind[gs], ev, rate);
+        }
+    }
+    __syncwarp();
+}
+
 // Apply event code ev of record r: the deposited species is drawn from the
 // PTransD shares of the site's coordination with u (Get_Prob.f:159-176);
 // an unsupported coor-1 site deposits species 1 (:181-184).
-__device__ void apply(const Dev &D, Ctx &c, int r, float u)
+__device__ void apply_warp(const Dev &D, Ctx &c, int r, float u, int lane)
 {
     const Rec &R = D.rec[r];
-    P3 site{R.x, R.y, R.z};
-    if (R.ev == EV_EVAP || R.ev == EV_ISO) {
-        evaporation(D, c, site);
+    const P3 site{R.x, R.y, R.z};
+    const uint8_t ev = R.ev;
+    __syncwarp();
+    if (ev == EV_EVAP || ev == EV_ISO) {
+        evaporation_warp(D, c, site, lane);
         return;
     }
     int sp = 1;
-    if (R.ev == EV_DEP) {
+    if (ev == EV_DEP) {
         int co = coor_of(cw(D, site));
         co = co < 1 ? 1 : (co > 3 ? 3 : co);
         sp = u < D.pds[3 + 2 * (co - 1)] ? 1 : (u < D.pds[4 + 2 * (co - 1)] ? 2 : 3);
     }
-    deposition(D, c, site, sp);
+    deposition_warp(D, c, site, sp, lane);
 }
-
-// ---- kernels ----
-constexpr unsigned FULL = 0xffffffffu;
 
 __device__ __forceinline__ void prefetch_l1(const void *p)
 {
@@ -834,7 +989,7 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
     float *rates = D.tr + (int64_t)t * LCAP;
     // records freed in the tile's last phase become reusable
     if (lane == 0) {
-        int np = D.fp_n[t], nr = D.fr_n[t];
+        int np = min(D.fp_n[t], FCAP), nr = D.fr_n[t];
         for (int k = 0; k < np && nr < FCAP; k++) D.fr[(int64_t)t * FCAP + nr++] = D.fp[(int64_t)t * FCAP + k];
         D.fr_n[t] = nr;
         D.fp_n[t] = 0;
@@ -972,15 +1127,15 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
         if (pick <= 0) break;
         prefetch_event(D, pick, lane);
         __syncwarp();
-        if (lane == 0) apply(D, c, pick, u01(rnd.w));
+        apply_warp(D, c, pick, u01(rnd.w), lane);
         nev++;
         __syncwarp();
         if (*(volatile int32_t *)D.err) break;
     }
     if (lane == 0) {
         if (nev) atomicAdd(D.events, (unsigned long long)nev);
-        if (c.dmc) atomicAdd(D.nmc, c.dmc);
     }
+    if (c.dmc) atomicAdd(D.nmc, c.dmc);          // every lane's own changes
 }
 
 // Grid-wide barrier of a cooperative launch (generation counter; all blocks
