@@ -216,34 +216,52 @@ def _causal_run(theta, n, tau, score, seed=4):
     return np.array(c), g
 
 
+LR_SEEDS = 16          # x NBIG replicas: 262144 for the LR gradient
+FD_SEEDS = (1, 4)      # x NBIG replicas at theta +- h: Ed2_Si, Ed2_Ge
+
+
+def _causal_many(theta, tau, seeds):
+    """The causal LR gradient over len(seeds) independent batches of NBIG
+    replicas: the mean of the batch gradients and its standard error."""
+    gs, ses = [], []
+    for sd in seeds:
+        _, (g, se) = _causal_run(theta, NBIG, tau, True, seed=sd)
+        gs.append(g)
+        ses.append(se)
+    return np.mean(gs, axis=0), np.sqrt(np.sum(np.square(ses), axis=0)) / len(seeds)
+
+
 def test_la_lr_gradient_within_5pct_of_finite_differences(theta):
-    """LR against finite differences at the benchmark spec's bar.  f = crystal
-    atoms gained from 0 to 20 ns (melting makes it negative), 16384
-    replicas, windows of the dominant-share rule (capped at 8 per 1 ns
-    segment).  The causal LR gradient (mks_batch_lr_accumulate after each
-    segment, mks_batch_lr_result) against common-random-number central
-    differences (h = 0.02 eV, the same seeds at theta +- h): for Ed2_Si the
-    two agree within 5 % with both standard errors under 2 % of the
-    gradient; for Ed2_Ge, inside the 95 % band of the two standard errors."""
-    from scipy import stats
+    """LR against finite differences at the benchmark spec's bar, for both
+    barriers Ed2_Si and Ed2_Ge.  f = crystal atoms gained from 0 to 20 ns
+    (melting makes it negative); windows of the dominant-share rule (capped
+    at 8 per 1 ns segment).  The causal LR gradient (mks_batch_lr_accumulate
+    after each segment, mks_batch_lr_result) over 16 x 16384 replicas against
+    common-random-number central differences (h = 0.02 eV, the same seeds at
+    theta +- h; 16384 replicas for Ed2_Si, 4 x 16384 for Ed2_Ge, whose
+    gradient is 7x smaller): the two agree within 5 % and both standard errors
+    are under 2 % of the gradient.  The LR gradients of the two delta
+    parameters are printed with their standard errors."""
     k = math.ceil(T2 / NSEG / 8.0 / _share_tau_rate(theta))
     tau = T2 / (NSEG * 8.0 * k)
-    c, (g, se) = _causal_run(theta, NBIG, tau, True)
-    f = (c[-1] - c[0]).sum(1)
+    g, se = _causal_many(theta, tau, range(4, 4 + LR_SEEDS))
     fd, fd_se = np.zeros(2), np.zeros(2)
-    for j, nfd in ((0, 4096), (1, NBIG)):
+    for j in (0, 1):
         e = np.zeros(4)
         e[j] = H
-        cp, _ = _causal_run(theta + e, nfd, tau, False)
-        cm, _ = _causal_run(theta - e, nfd, tau, False)
-        dq = ((cp[-1] - cp[0]).sum(1) - (cm[-1] - cm[0]).sum(1)) / (2 * H)
+        dq = []
+        for sd in range(4, 4 + FD_SEEDS[j]):
+            cp, _ = _causal_run(theta + e, NBIG, tau, False, seed=sd)
+            cm, _ = _causal_run(theta - e, NBIG, tau, False, seed=sd)
+            dq.append(((cp[-1] - cp[0]).sum(1) - (cm[-1] - cm[0]).sum(1)) / (2 * H))
+        dq = np.concatenate(dq)
         fd[j], fd_se[j] = dq.mean(), dq.std(ddof=1) / math.sqrt(len(dq))
     rel = np.abs(g[:2] - fd) / np.abs(fd)
-    print(f"\nE f {f.mean():.2f}; causal LR {g} +- {se}; CRN FD (Ed2_Si, Ed2_Ge) {fd} +- {fd_se}; "
+    print(f"\ncausal LR (Ed2_Si, Ed2_Ge, delta_Si, delta_Ge) {g} +- {se}; CRN FD (Ed2_Si, Ed2_Ge) {fd} +- {fd_se}; "
           f"relative difference {rel}, relative SE LR {se[:2] / np.abs(fd)}, FD {fd_se / np.abs(fd)}")
-    assert rel[0] <= 0.05 and se[0] <= 0.02 * abs(fd[0]) and fd_se[0] <= 0.02 * abs(fd[0])
-    q = float(stats.norm.ppf(1.0 - 0.05 / 2.0))
-    assert abs(g[1] - fd[1]) <= q * math.hypot(se[1], fd_se[1]) and fd_se[1] <= 0.02 * abs(fd[1])
+    for j in (0, 1):
+        assert rel[j] <= 0.05, f"theta {j}: LR {g[j]} vs FD {fd[j]}"
+        assert se[j] <= 0.02 * abs(fd[j]) and fd_se[j] <= 0.02 * abs(fd[j])
 
 
 def test_la_schedules_agree(theta):
