@@ -576,7 +576,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--only", choices=["stacking"], default=None,
+    ap.add_argument("--only", choices=["stacking", "batched", "cvd", "la"], default=None,
                     help="run one side line alone and print it (e.g. for a profile of its kernel)")
     ap.add_argument("--stacking-side", type=int, default=1536)
     ap.add_argument("--stacking-cube", type=int, default=960)
@@ -585,6 +585,11 @@ def main():
     if args.only == "stacking":
         print(json.dumps(stacking_bench(side=args.stacking_side, cube=args.stacking_cube,
                                         windows=args.stacking_windows, oracle_events=200000)))
+        return
+    if args.only:
+        line = {"batched": lambda: batched_bench(args), "cvd": lambda: cvd_bench(oracle_events=200000),
+                "la": la_gradient_bench}[args.only]()
+        print(json.dumps(line))
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
