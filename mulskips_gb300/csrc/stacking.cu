@@ -54,8 +54,12 @@ constexpr int WALLIND = 113;        // CovInd of a wall (SetSi.f:38-46)
 constexpr int TWMIN = 24;           // smallest tile side (grid units)
 constexpr int LCAP = 4096;          // list entries per tile
 constexpr int FCAP = 1024;          // free records per tile and stack
+constexpr int ICAP = 1024;          // inbox entries per tile (sites given an event by a neighbour tile)
 enum : uint8_t { EV_NONE = 0, EV_DEP = 1, EV_DUMMY = 2, EV_EVAP = 4, EV_ISO = 5 };
-enum : uint8_t { F_LISTED = 1 };
+// F_LISTED: in its tile's list (slot valid unless F_PEND / F_INBOX);
+// F_PEND: appended to the running tile's list at the end of the event;
+// F_INBOX: waiting in its tile's inbox for the tile's next phase
+enum : uint8_t { F_LISTED = 1, F_PEND = 2, F_INBOX = 4 };
 // device error codes (err[0]); err[1..3] say where
 enum { E_INVARIANT = 3, E_CAPACITY = 4, E_TIMEOUT = 6, E_NOTAPPLICABLE = 7, E_BOUNDS = 8, E_NBUFF = 9, E_ARM = 10 };
 
@@ -79,6 +83,7 @@ struct Dev {
     int lx, ly, lz;
     int tw, ntx, nty;
     int32_t *tl, *tl_n;        // tile lists [tile][LCAP] and their lengths
+    int32_t *ib, *ib_n;        // tile inboxes [tile][ICAP] and their lengths
     float *tr;                 // the listed sites' rates beside tl: > 0 a rate, -1 an isolated atom, 0 none
     int32_t *fr, *fr_n;        // reusable records per tile [tile][FCAP]
     int32_t *fp, *fp_n;        // records freed in the tile's current phase
@@ -107,6 +112,8 @@ struct Ctx {
     uint32_t key2, key3;       // Philox counter words of the stacking ties
     uint32_t nties;
     int dmc;                   // change of the count of sites with an event
+    int npend;                 // records of the running tile to append after this event
+    int pend[4];
 };
 
 __device__ __forceinline__ int coor_of(uint32_t v) { return (v >> 24) & 7; }
@@ -231,21 +238,33 @@ __device__ void get_prob(const Dev &D, int occ, int nsic, int coor, P3 site, con
 }
 
 // ---- list bookkeeping (AddMC / EraseMC and friends, Add.f, Erase.f) ----
-__device__ void list_site(const Dev &D, const Ctx &c, int r)
+// A site that gets an event joins its tile's list in an order that does not
+// depend on the scheduling of warps or lanes, so a run is reproducible for
+// its seed: a site of the running tile is appended after the event, in lane
+// order (flush_pending); a site of an idle neighbour tile goes to that tile's
+// inbox, which the tile drains at its next phase in grid-point order.
+__device__ void list_site(const Dev &D, Ctx &c, int r)
 {
     if (c.tile < 0) return;               // replay: the lists are rebuilt before a run
     Rec &R = D.rec[r];
     if (R.flags & F_LISTED) return;
     int t = tile_of(D, R.x, R.y);
-    int k = atomicAdd(&D.tl_n[t], 1);
-    if (k >= LCAP) {
-        set_err(D, E_CAPACITY, t, k, 0);
+    if (t == c.tile) {
+        if (c.npend >= 4) {
+            set_err(D, E_INVARIANT, R.x, R.y, R.z);
+            return;
+        }
+        c.pend[c.npend++] = r;
+        R.flags |= F_LISTED | F_PEND;
         return;
     }
-    R.flags |= F_LISTED;
-    R.slot = k;
-    D.tl[(int64_t)t * LCAP + k] = r;
-    D.tr[(int64_t)t * LCAP + k] = list_rate(R);
+    int k = atomicAdd(&D.ib_n[t], 1);
+    if (k >= ICAP) {
+        set_err(D, E_CAPACITY, t, k, 2);
+        return;
+    }
+    D.ib[(int64_t)t * ICAP + k] = r;
+    R.flags |= F_LISTED | F_INBOX;
 }
 
 __device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
@@ -259,8 +278,11 @@ __device__ void set_event(const Dev &D, Ctx &c, int r, uint8_t ev, float rate)
     R.ev = ev;
     R.rate = rate;
     if (c.tile < 0) return;               // replay: the lists are rebuilt before a run
-    if (R.flags & F_LISTED) D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = list_rate(R);
-    else if (ev) list_site(D, c, r);
+    if (R.flags & F_LISTED) {
+        if (!(R.flags & (F_PEND | F_INBOX))) D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = list_rate(R);
+    } else if (ev) {
+        list_site(D, c, r);
+    }
 }
 
 // A record from the running tile's reusable stack, else a new one.  The
@@ -324,7 +346,8 @@ __device__ void drop_site(const Dev &D, Ctx &c, P3 p)
     D.ind[g] = 0;
     Rec &R = D.rec[r];
     c.dmc -= R.ev != 0;
-    if (c.tile >= 0 && (R.flags & F_LISTED)) D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = 0.f;
+    if (c.tile >= 0 && (R.flags & F_LISTED) && !(R.flags & (F_PEND | F_INBOX)))
+        D.tr[(int64_t)tile_of(D, R.x, R.y) * LCAP + R.slot] = 0.f;
     R.ev = EV_NONE;
     R.flags = 0;
     R.rate = 0.f;
@@ -977,6 +1000,106 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x &
 
 // One colour phase: every tile of the colour runs from the window's start to
 // its end (one warp per tile).
+__device__ __forceinline__ long long site_key(const Dev &D, const Rec &R)
+{
+    return ((long long)(R.z + ZG) * D.ly + R.y) * D.lx + R.x;
+}
+
+// The running tile's sites that got an event in this event, appended in
+// lane order (every lane calls this after the event).  A record dropped or
+// left without an event in the meantime is appended as a dead entry (rate 0)
+// for the next compaction.
+__device__ void flush_pending(const Dev &D, Ctx &c, int t, int lane)
+{
+    int inc = c.npend;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const int tot = __shfl_sync(FULL, inc, 31);
+    if (!tot) return;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&D.tl_n[t], tot);
+    base = __shfl_sync(FULL, base, 0);
+    const int excl = inc - c.npend;
+    for (int i = 0; i < c.npend; i++) {
+        const int r = c.pend[i];
+        const int k = base + excl + i;
+        if (k >= LCAP) {
+            set_err(D, E_CAPACITY, t, k, 3);
+            continue;
+        }
+        Rec &R = D.rec[r];
+        D.tl[(int64_t)t * LCAP + k] = r;
+        if (R.x >= 0 && (R.flags & F_PEND)) {
+            R.flags = F_LISTED;
+            R.slot = k;
+            D.tr[(int64_t)t * LCAP + k] = list_rate(R);
+        } else {
+            D.tr[(int64_t)t * LCAP + k] = 0.f;
+        }
+    }
+    c.npend = 0;
+    __syncwarp();
+}
+
+// Sites that neighbour tiles gave an event while this tile was idle join
+// its list in grid-point order (a repeated record once); the inbox empties.
+__device__ void drain_inbox(const Dev &D, int t, int lane, long long *key)
+{
+    const int m = min(D.ib_n[t], ICAP);
+    if (m <= 0) return;
+    const int32_t *in = D.ib + (int64_t)t * ICAP;
+    const long long NONE = 0x7fffffffffffffffLL;
+    for (int i = lane; i < m; i += 32) {
+        const Rec &R = D.rec[in[i]];
+        const bool ok = R.x >= 0 && tile_of(D, R.x, R.y) == t && (R.flags & F_INBOX) && R.ev != EV_NONE;
+        key[i] = ok ? site_key(D, R) : NONE;
+    }
+    __syncwarp();
+    // a repeated key keeps its first entry
+    for (int i = lane; i < m; i += 32) {
+        if (key[i] == NONE) continue;
+        bool dup = false;
+        for (int j = 0; j < i && !dup; j++) dup = key[j] == key[i];
+        if (dup) key[i] = NONE - 1;
+    }
+    __syncwarp();
+    int nv = 0;
+    for (int i = lane; i < m; i += 32) nv += key[i] < NONE - 1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nv += __shfl_xor_sync(FULL, nv, o);
+    const int base = D.tl_n[t];
+    if (base + nv > LCAP) {
+        if (lane == 0) set_err(D, E_CAPACITY, t, base + nv, 4);
+        return;
+    }
+    for (int i = lane; i < m; i += 32) {
+        const int r = in[i];
+        Rec &R = D.rec[r];
+        if (key[i] == NONE) {
+            // lost its event (or moved, or freed) while waiting
+            if (R.x >= 0 && tile_of(D, R.x, R.y) == t && (R.flags & F_INBOX)) R.flags = 0;
+            continue;
+        }
+        if (key[i] == NONE - 1) continue;
+        int rank = 0;
+        for (int j = 0; j < m; j++) rank += key[j] < key[i];
+        const int k = base + rank;
+        R.flags = F_LISTED;
+        R.slot = k;
+        D.tl[(int64_t)t * LCAP + k] = r;
+        D.tr[(int64_t)t * LCAP + k] = list_rate(R);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        D.tl_n[t] = base + nv;
+        D.ib_n[t] = 0;
+    }
+    __syncwarp();
+}
+
 // tile k of colour `colour` runs from the window's start to its end (one
 // warp; every lane of the warp calls this)
 __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float tau)
@@ -993,6 +1116,11 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
         for (int k = 0; k < np && nr < FCAP; k++) D.fr[(int64_t)t * FCAP + nr++] = D.fp[(int64_t)t * FCAP + k];
         D.fr_n[t] = nr;
         D.fp_n[t] = 0;
+    }
+    __syncwarp();
+    {
+        __shared__ long long inbox_key[4][ICAP];          // k_windows runs 4 warps per block
+        drain_inbox(D, t, lane, inbox_key[(threadIdx.x >> 5) & 3]);
     }
     // compact the list once a quarter of it is dead.  An entry with a nonzero
     // rate is its record's current entry (a freed record's entry is zeroed,
@@ -1050,6 +1178,7 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
     c.key3 = 0x7a000000u | (uint32_t)colour;
     c.nties = 0;
     c.dmc = 0;
+    c.npend = 0;
     float rem = tau;
     uint32_t nev = 0, ndraw = 0;
     for (;;) {
@@ -1128,6 +1257,7 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
         prefetch_event(D, pick, lane);
         __syncwarp();
         apply_warp(D, c, pick, u01(rnd.w), lane);
+        flush_pending(D, c, t, lane);
         nev++;
         __syncwarp();
         if (*(volatile int32_t *)D.err) break;
@@ -1204,6 +1334,7 @@ __global__ void k_replay(Dev D, const mks_event *ev, long long n, long long *don
     c.key2 = c.key3 = 0;
     c.nties = 0;
     c.dmc = 0;
+    c.npend = 0;
     long long k = 0;
     for (; k < n; k++) {
         const mks_event e = ev[k];
@@ -1273,6 +1404,54 @@ __global__ void k_rate_all(Dev D, const uint8_t *ini, const int32_t *gev, const 
 }
 
 // tile lists from scratch, and the count of sites with an event
+// Each tile's list in grid-point order after a rebuild (whose appends come
+// in any order): a bitonic sort in shared memory, one block per tile.
+__global__ void __launch_bounds__(256) k_sort_lists(Dev D)
+{
+    __shared__ long long key[LCAP];
+    __shared__ int32_t id[LCAP];
+    const int t = blockIdx.x;
+    const int n = min(D.tl_n[t], LCAP);
+    if (n < 2) return;
+    int m = 1;
+    while (m < n) m <<= 1;
+    int32_t *list = D.tl + (int64_t)t * LCAP;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        if (i < n) {
+            id[i] = list[i];
+            key[i] = site_key(D, D.rec[id[i]]);
+        } else {
+            id[i] = 0;
+            key[i] = 0x7fffffffffffffffLL;
+        }
+    }
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const bool up = (i & k) == 0;
+                    if ((key[i] > key[p]) == up) {
+                        const long long tk = key[i];
+                        key[i] = key[p];
+                        key[p] = tk;
+                        const int32_t ti = id[i];
+                        id[i] = id[p];
+                        id[p] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        Rec &R = D.rec[id[i]];
+        R.slot = i;
+        list[i] = id[i];
+        D.tr[(int64_t)t * LCAP + i] = list_rate(R);
+    }
+}
+
 __global__ void k_rebuild(Dev D, int last)
 {
     for (int r = 1 + blockIdx.x * blockDim.x + threadIdx.x; r < last; r += gridDim.x * blockDim.x) {
@@ -1588,7 +1767,9 @@ int rebuild(State *s, std::string &err)
     int ntiles = s->D.ntx * s->D.nty;
     SK(cudaMemsetAsync(s->D.tl_n, 0, sizeof(int32_t) * ntiles, s->stream));
     SK(cudaMemsetAsync(s->D.nmc, 0, sizeof(int32_t), s->stream));
+    SK(cudaMemsetAsync(s->D.ib_n, 0, sizeof(int32_t) * ntiles, s->stream));
     if (top > 1) k_rebuild<<<grid_for(top), 256, 0, s->stream>>>(s->D, top);
+    k_sort_lists<<<ntiles, 256, 0, s->stream>>>(s->D);
     SK(cudaGetLastError());
     s->lists_ok = true;
     return check_device(s, err, "list build");
@@ -1660,6 +1841,8 @@ int create(State **out, const mks_config &cfg, cudaStream_t stream, std::string 
     SA(D.rec, sizeof(Rec) * (size_t)rcap);
     SA(D.tl, sizeof(int32_t) * (size_t)ntiles * LCAP);
     SA(D.tr, sizeof(float) * (size_t)ntiles * LCAP);
+    SA(D.ib, sizeof(int32_t) * (size_t)ntiles * ICAP);
+    SA(D.ib_n, sizeof(int32_t) * ntiles);
     SA(D.tl_n, sizeof(int32_t) * ntiles);
     SA(D.fr, sizeof(int32_t) * (size_t)ntiles * FCAP);
     SA(D.fr_n, sizeof(int32_t) * ntiles);
@@ -1705,6 +1888,8 @@ void destroy(State *s)
     cudaFree(D.rec);
     cudaFree(D.tl);
     cudaFree(D.tr);
+    cudaFree(D.ib);
+    cudaFree(D.ib_n);
     cudaFree(D.tl_n);
     cudaFree(D.fr);
     cudaFree(D.fr_n);

@@ -149,6 +149,29 @@ def test_stacking_replay_sic_facets(oracle_lib, tmp_path):
     assert done == 300000 and arm > 1000
 
 
+def test_stacking_run_is_reproducible(oracle_lib):
+    """Two runs with the same seed give the same lattice: list order never
+    depends on the scheduling of warps or lanes (inbox drained in grid-point
+    order, a tile's own new sites appended in lane order, lists sorted after
+    a rebuild)."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    d = parse_startdat(CUBE_ZZ)
+    out = []
+    for _ in range(2):
+        with Lattice(480, 480, 480, ncrystal=d["ncrystal"], list_crystal=d["list_crystal"], sf=d["sf"],
+                     ptrans_zig=d["ptrans_zig"], seed=23) as lat:
+            lat.set_rates(d["ptransE"], d["ptransD"])
+            lat.init_shape("C", d["len"])
+            n = 0
+            for _ in range(12):
+                m, _t = lat.run(lat.suggest_tau(0.01), 64)
+                n += m
+            out.append((n, lat.lattcoo()))
+    assert out[0][0] == out[1][0] > 10000
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_stacking_expands_initializer_lattice(oracle_lib):
     """The compact lattice of an initializer (SetNC, InitSt 'C') expanded to
     the explicit form equals the oracle's SetNC lattice: every LattCoo word,
