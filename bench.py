@@ -356,14 +356,25 @@ def bench_accuracy(width):
 def batched_bench(args):
     """Config 3: 512 independent Si(001) replicas, box side ~U{16..96} cells,
     T ~ U(900, 1300) K, F ~ logU(0.05, 5) ML/s, seed 1000+i, in one persistent
-    launch per block of windows; tau per replica and tile width autotuned
-    (one width for the batch by a timed trial, then one per group of box
-    sizes by coordinate descent).
+    launch per block of windows; tau per replica and tile width autotuned:
+    the window factor f by the pilot tuner (autotune.choose_f: 16 replicas
+    of the model at 1100 K, 0.5 ML/s in 480^3 boxes, each f of the ladder
+    against the shortest), one width for the batch by a timed trial, then one
+    per group of box sizes by coordinate descent.
     Also one replica of the median size run alone (the plain single-replica
     path) for the batched/plain ratio."""
     import numpy as np
     from mulskips_gb300 import Batch, Lattice, arrhenius_tables
-    from mulskips_gb300.autotune import choose_width, choose_widths, size_groups
+    from mulskips_gb300.autotune import choose_f, choose_width, choose_widths, size_groups
+    pE, pD = arrhenius_tables(1100.0, flux=0.5)
+
+    def pilot(f):
+        p = Batch([(480, 480, 480)] * 16, seeds=[300 + s for s in range(16)])
+        p.set_rates(np.stack([pE] * 16), np.stack([pD] * 16))
+        p.init_flat("S", [120] * 16)
+        return p
+
+    f, pilots = choose_f(pilot, 4e-7)
     rng = np.random.default_rng(3)
     n = 512
     sides = rng.integers(16, 97, n)
@@ -375,14 +386,14 @@ def batched_bench(args):
     b = Batch(boxes, seeds=[1000 + i for i in range(n)])
     b.set_rates(np.stack([t[0] for t in tabs]), np.stack([t[1] for t in tabs]))
     b.init_flat("S", len1)
-    tau = b.suggest_tau(ACCURATE_F)
+    tau = b.suggest_tau(f)
     width = choose_width(b, tau, restore=False)
     # then one width per group of box sizes, starting from the batch's best
     groups = size_groups(sides)
-    widths, trials = choose_widths(b, b.suggest_tau(ACCURATE_F), groups)
+    widths, trials = choose_widths(b, b.suggest_tau(f), groups)
     by_group = [{"side_cells": [int(sides[g].min()), int(sides[g].max())], "replicas": int(len(g)),
                  "tile_width": int(widths[g[0]])} for g in groups]
-    tau = b.suggest_tau(ACCURATE_F)
+    tau = b.suggest_tau(f)
     b.run(tau, 8)
     ev = 0
     ms = 0.0
@@ -394,7 +405,7 @@ def batched_bench(args):
     one = Lattice(12 * med, 12 * med, 12 * med, seed=7)
     one.set_rates(*arrhenius_tables(1100.0, flux=0.5))
     one.init_flat("S", max(48, (6 * med) // 24 * 24))
-    t1 = one.suggest_tau(ACCURATE_F)
+    t1 = one.suggest_tau(f)
     one.set_tiling(width)
     one.run(t1, 8)
     ev1, _ = one.run(t1, BATCH_WINDOWS_PER_STEP * args.steps)
@@ -406,8 +417,9 @@ def batched_bench(args):
             "tile_width": width, "tile_width_by_size_group": by_group, "width_trials": trials,
             "single_replica_value": v1, "single_replica_side_cells": med,
             "batched_over_single": v / v1,
+            "f": f, "f_pilots": pilots,
             "workload": "512 Si(001) replicas, side ~U{16..96} cells, T~U(900,1300) K, F~logU(0.05,5), "
-                        "seed 1000+i, tau = 0.3/r* per replica"}
+                        f"seed 1000+i, tau = {f}/r* per replica (f from the pilot tuner)"}
 
 
 def cvd_bench(windows=4096, oracle_events=3000000):

@@ -33,8 +33,8 @@ def welch_band(x, y, k=1, alpha=FAMILY_ALPHA):
 class Family:
     """The k observables of one test: add() each, then check() them all."""
 
-    def __init__(self, title, k):
-        self.title, self.k, self.rows = title, k, []
+    def __init__(self, title, k, extra=None):
+        self.title, self.k, self.rows, self.extra = title, k, [], extra
 
     def add(self, name, gpu, ref):
         d, hw, q = welch_band(gpu, ref, self.k)
@@ -58,9 +58,12 @@ class Family:
         rows = [{"observable": r[0], "gpu_mean": float(r[1]), "gpu_sd": float(r[2]), "ref_mean": float(r[3]),
                  "ref_sd": float(r[4]), "diff": float(r[5]), "band": float(r[6]), "t": float(r[7]),
                  "n_gpu": int(r[8]), "n_ref": int(r[9])} for r in self.rows]
+        rec = {"test": os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], "family": self.title, "k": self.k,
+               "rows": rows}
+        if self.extra:
+            rec.update(self.extra)
         with open(path, "a") as f:
-            f.write(json.dumps({"test": os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0],
-                                "family": self.title, "k": self.k, "rows": rows}) + "\n")
+            f.write(json.dumps(rec) + "\n")
 
     def check(self):
         assert len(self.rows) == self.k, "every observable of the family must be compared"

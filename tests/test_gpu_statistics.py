@@ -199,26 +199,44 @@ def test_deposition_evaporation_regime_matches_serial_reference(tmp_path):
 
 
 # ---------------------------------------------------------------- 3C-SiC
-def test_sic_surface_matches_serial_reference(tmp_path):
+_SURFACE_REF = {}
+
+
+@pytest.mark.parametrize("window", ["fixed", "tuned"])
+def test_sic_surface_matches_serial_reference(tmp_path_factory, window):
     """3C-SiC(001), the rates of the reference's `surface` regression case
     (NCrystal 2, Si and C with 18 census-dependent evaporation rates), RunType
-    R, t_obs = 2e5 s, at the two-species window factor."""
+    R, t_obs = 2e5 s, at the two-species window factor ("fixed",
+    autotune.accurate_f) and at the factor the pilot tuner picks for these
+    rates ("tuned", autotune.choose_f on 16 pilot replicas of its own seeds)."""
     from mulskips_gb300 import Batch
-    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.autotune import accurate_f, choose_f
     from mulskips_gb300.startdat import parse_startdat
-    paths = startdats(tmp_path, "surface", ("T   ! R = production run", "R   ! R = production run"), 400, NSEEDS,
-                      "sic")
-    d = parse_startdat(paths[0])
-    ref = oracle_sample(paths, (480, 480, 480), 2e5, d["sf"])
-    b = Batch([(480, 480, 480)] * NSEEDS, seeds=[51 + s for s in range(NSEEDS)], ncrystal=2, list_crystal=(14, 6),
-              sf=d["sf"])
-    b.set_rates(np.stack([d["ptransE"]] * NSEEDS), np.stack([d["ptransD"]] * NSEEDS))
-    b.init_flat("C", [d["len"][0]] * NSEEDS)
-    f = accurate_f(2)
+    if "ref" not in _SURFACE_REF:
+        tmp = tmp_path_factory.mktemp("sic")
+        paths = startdats(tmp, "surface", ("T   ! R = production run", "R   ! R = production run"), 400, NSEEDS,
+                          "sic")
+        d = parse_startdat(paths[0])
+        _SURFACE_REF["ref"] = (d, oracle_sample(paths, (480, 480, 480), 2e5, d["sf"]))
+    d, ref = _SURFACE_REF["ref"]
+
+    def make(n, seed0):
+        b = Batch([(480, 480, 480)] * n, seeds=[seed0 + s for s in range(n)], ncrystal=2, list_crystal=(14, 6),
+                  sf=d["sf"])
+        b.set_rates(np.stack([d["ptransE"]] * n), np.stack([d["ptransD"]] * n))
+        b.init_flat("C", [d["len"][0]] * n)
+        return b
+
+    pilots = None
+    if window == "fixed":
+        f = accurate_f(2)
+    else:
+        f, pilots = choose_f(lambda f_: make(16, 900), 2e5)
+    b = make(NSEEDS, 51)
     nwin = windows_for(2e5, float(b.suggest_tau(f)[0]))
     g = gpu_sample(b, 2e5 / nwin, nwin, (480, 480, 480), d["sf"])
     b.close()
-    fam = Family(f"3C-SiC(001) surface rates, f = {f} ({nwin} windows)", 4)
+    fam = Family(f"3C-SiC(001) surface rates, {window} f = {f} ({nwin} windows)", 4, extra={"pilots": pilots})
     fam.add("atoms", column(g, "atoms"), column(ref, "atoms"))
     fam.add("C atoms", column(g, "species", 1), column(ref, "species", 1))
     fam.add("growth rate um/h", growth(g), growth(ref))
