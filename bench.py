@@ -284,6 +284,7 @@ def gb300(args, rank, world):
     la_grad = la_gradient_bench() if not args.no_batched else None
     cvd = cvd_bench() if not args.no_batched else None
     stacking = stacking_bench() if not args.no_batched else None
+    config2 = config2_bench() if not args.no_batched else None
     base_v, base_ev, base_runs, base_slab = cpu_baseline(seconds=args.cpu_seconds, cores=1)
     all_cores = os.cpu_count() or 1
     all_v, _, _, _ = cpu_baseline(seconds=args.cpu_seconds, cores=all_cores)
@@ -329,6 +330,7 @@ def gb300(args, rank, world):
         "la_gradient": la_grad,
         "cvd": cvd,
         "stacking": stacking,
+        "config2": config2,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -528,6 +530,112 @@ def stacking_bench(side=1536, cube=960, warm_blocks=24, windows=1024, oracle_eve
                         "oracle: the reference's 480^3 cube-zigzag case, serial, 1 core"}
 
 
+def config2_tables(seed=2, T=1600.0):
+    """Config 2's rate tables: per-species flux F_s ~ U(0.1, 1.0) ML/s as
+    PtransD(s, n) for n = 1..3, and the 18 evaporation entries of
+    SetProbability.f:49-50 (species Si, C x the neighbour census (n_Si, n_C),
+    1 <= n_Si + n_C <= 3) with barriers E ~ U(0.4, 0.9) eV and prefactor 1e13
+    s^-1 at T, drawn from numpy's PCG64 with `seed`.  Returns (PtransE,
+    PtransD, F, barriers)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    F = rng.uniform(0.1, 1.0, 2)
+    Eb = rng.uniform(0.4, 0.9, (2, 9))
+    E = np.zeros((3, 4, 4, 4, 4, 4, 4))
+    D = np.zeros((3, 3))
+    for s in range(2):
+        D[s, :] = F[s]
+        j = 0
+        for n1 in range(4):
+            for n2 in range(4 - n1):
+                if n1 + n2:
+                    E[s, n1, n2] = 1e13 * math.exp(-Eb[s, j] / (0.00008617330350 * T))
+                    j += 1
+    return E, D, F, Eb
+
+
+def config2_oracle(E, D, sf, events, side=480, h_slab=400, period=96):
+    """The serial oracle (RunType R, one core) on config 2's model in a 480^3
+    box: the same rates and PtransZig on a {111}-faceted slab of the same
+    form, `events` events (fewer than half its atoms, so the etch front stays
+    clear of the bottom wall).  Returns (events/s, events)."""
+    from mulskips_gb300.shapes import faceted_slab_points
+    from mulskips_gb300.startdat import write_startdat
+    from oracle import ora
+    xyz, sp = faceted_slab_points(side, h_slab, period)
+    assert events < 0.5 * int(((xyz[:, 2] > 3) & (xyz[:, 2] < side - 4)).sum())
+    tmp = tempfile.mkdtemp()
+    try:
+        pts = os.path.join(tmp, "slab.xyz")
+        with open(pts, "w") as fh:
+            fh.write(f"{len(xyz)}\nslab\n")
+            fh.write("".join(f"{'Si' if s == 1 else 'C'} {x} {y} {z}\n" for (x, y, z), s in zip(xyz.tolist(), sp)))
+        p = os.path.join(tmp, "start.dat")
+        write_startdat(p, E, D, ncrystal=2, list_crystal=(14, 6), init_st="SH", points=pts, run_type="R",
+                       seed=7, sf=sf, ptrans_zig=PZIG_1600K, max_iter=10 ** 9)
+        o = ora.Oracle(p, side, side, side, numbers=None)
+        o.init()
+        c0 = time.perf_counter()
+        o.run(events)
+        cdt = time.perf_counter() - c0
+        m = o.iter - 1
+        o.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return m / cdt, m
+
+
+def config2_bench(side=1536, h_slab=768, period=192, warm_blocks=8, windows=1024, oracle_events=200000):
+    """Config 2 as stated: 3C-SiC (Si, C) in a 128^3-cell box (1536^3 grid)
+    on a slab whose surface is {111} facets only (an SH point list of square
+    pyramids of period 192 grid units, mulskips_gb300.shapes), per-species
+    fluxes U(0.1, 1.0) ML/s and 18 evaporation barriers U(0.4, 0.9) eV with
+    a 1e13 prefactor at 1600 K (table seed 2), PtransZig = 0.5362, on the
+    explicit-neighbour engine.  These rates evaporate a surface atom at
+    1e10-1e11 s^-1 against a deposition of at most 1 s^-1 per site, so the
+    slab etches (the atoms lost and the etch rate are in the line); an
+    arm-chair choice needs a deposition next to a single bond and is rare.
+    Window factor f = 0.01 (two species), re-suggested per block of 64
+    warm-up windows; then events/s over `windows` windows at the largest
+    suggestion of the warm-up's second half, wall time of the synchronous
+    call."""
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.shapes import faceted_slab_points
+    from mulskips_gb300.startdat import parse_startdat
+    sf = parse_startdat(os.path.join(ROOT, "tests", "golden", "cube-zigzag", "start.dat"))["sf"]
+    E, D, F, Eb = config2_tables()
+    xyz, sp = faceted_slab_points(side, h_slab, period)
+    f = accurate_f(2)
+    lat = Lattice(side, side, side, ncrystal=2, list_crystal=(14, 6), sf=sf, ptrans_zig=PZIG_1600K, seed=13)
+    lat.set_rates(E, D)
+    lat.init_points(xyz, sp)
+    a0 = lat.observables()["atoms"]
+    taus = []
+    for _ in range(warm_blocks):
+        taus.append(lat.suggest_tau(f))
+        lat.run(taus[-1], 64)
+    tau = float(max(taus[warm_blocks // 2:]))
+    a1 = lat.observables()["atoms"]
+    t0 = time.perf_counter()
+    n, tsim = lat.run(tau, windows)
+    wall = time.perf_counter() - t0
+    obs = lat.observables()
+    lat.close()
+    ov, om = config2_oracle(E, D, sf, oracle_events)
+    return {"value": n / wall, "unit": "events/s", "events": int(n), "windows": windows, "tau_s": tau,
+            "oracle_events_per_s": ov, "oracle_events": int(om),
+            "atoms_initial": int(a0), "atoms_before": int(a1), "atoms_after": int(obs["atoms"]),
+            "etch_atoms_per_s": (int(a1) - int(obs["atoms"])) / (windows * tau),
+            "nonepitaxial_bulk": int(obs["nonepitaxial"]), "ptrans_zig": PZIG_1600K,
+            "flux_ml_per_s": [float(v) for v in F], "barriers_eV": Eb.round(4).tolist(),
+            "workload": f"3C-SiC slab with {{111}} facets only (SH point list, pyramids of period {period}, valleys "
+                        f"at z = {h_slab - period // 2}, apexes at {h_slab + period // 2}) in a {side}^3 grid, "
+                        "fluxes U(0.1,1) ML/s, 18 barriers U(0.4,0.9) eV, nu 1e13, 1600 K, table seed 2, "
+                        "PtransZig 0.5362, f = 0.01; oracle: the same model on a slab of the same form in a "
+                        "480^3 box, serial, 1 core"}
+
+
 def la_gradient_bench():
     """Config 4: 128 SiGe replicas (64x64x256 cells, Ge 0.2) under the laser
     pulse T = 300 + 1500 exp(-((t-100 ns)/40 ns)^2) exp(-z/200 nm) K, melting
@@ -588,7 +696,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--only", choices=["stacking", "batched", "cvd", "la"], default=None,
+    ap.add_argument("--only", choices=["stacking", "config2", "batched", "cvd", "la"], default=None,
                     help="run one side line alone and print it (e.g. for a profile of its kernel)")
     ap.add_argument("--stacking-side", type=int, default=1536)
     ap.add_argument("--stacking-cube", type=int, default=960)
@@ -600,6 +708,7 @@ def main():
         return
     if args.only:
         line = {"batched": lambda: batched_bench(args), "cvd": lambda: cvd_bench(oracle_events=200000),
+                "config2": config2_bench,
                 "la": la_gradient_bench}[args.only]()
         print(json.dumps(line))
         return

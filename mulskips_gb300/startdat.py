@@ -168,21 +168,25 @@ def write_plain_si_startdat(path, T=1100.0, e_bond=0.6, nu=1e13, flux=0.5, len1=
 
 def write_startdat(path, ptransE, ptransD, ncrystal=1, list_crystal=(14,), init_st="FS", len1=120,
                    max_iter=1000000, out_molmol=None, run_type="R", seed=1, sf=5.43 / 12, lens=(120, 120),
-                   alloy_fraction=0.0):
+                   alloy_fraction=0.0, ptrans_zig=1.0, points=None):
     """start.dat for NCrystal 1..3 species without coverage (main.f:83-212
     grammar): every PTransE(s, n_1..n_NCrystal) entry with 1 <= sum n <= 3 and
     the 3 PTransD entries of each species, from arrays in the engine layout
     (ptransE (3,4,4,4,4,4,4), ptransD (3,3)).  Si/Ge lists carry the alloy
-    fraction record that main.f reads after the box sizes."""
+    fraction record that main.f reads after the box sizes.  InitSt SH takes
+    the point file's path (`points`) on the line where the others read the
+    box sizes (main.f:224-278)."""
     E = np.asarray(ptransE, dtype=np.float64).reshape(3, 4, 4, 4, 4, 4, 4)
     D = np.asarray(ptransD, dtype=np.float64).reshape(3, 3)
     out_molmol = out_molmol or max_iter
     lc = " ".join(str(int(z)) for z in list_crystal[:ncrystal])
+    if (init_st == "SH") != (points is not None):
+        raise ValueError("InitSt SH needs a point file, and only SH takes one")
     lines = [f"{ncrystal} 0 ! NCrystal, NCov", f"{lc} ! Atomic numbers of crystal species",
-             f"{init_st} ! Initstat", f"{len1} {lens[0]} {lens[1]} ! Len1 Len2 Len3"]
+             f"{init_st} ! Initstat", points if points is not None else f"{len1} {lens[0]} {lens[1]} ! Len1 Len2 Len3"]
     if ncrystal >= 2 and tuple(list_crystal[:2]) == (14, 32):
         lines.append(f"{float(alloy_fraction)!r} ! alloy fraction")
-    lines += ["1.0 ! PtransZig", f"{sf:.15f} ! KMC_sf", "Iter ! ExitStrategy", f"{max_iter} ! IterMax",
+    lines += [f"{float(ptrans_zig)!r} ! PtransZig", f"{sf:.15f} ! KMC_sf", "Iter ! ExitStrategy", f"{max_iter} ! IterMax",
               f"{out_molmol} ! OutMolMol", f"{run_type} ! RunType", f"{seed} ! Random seed",
               "F ! Save final state", "F ! Save final Coor"]
     for s in range(ncrystal):

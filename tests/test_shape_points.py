@@ -188,6 +188,34 @@ def test_library_sh_equals_oracle_pyramid(helper, oracle_lib, tmp_path):
     assert len(np.unique((st[occ & (co <= 3)] >> 5) & 3)) > 1
 
 
+def test_faceted_slab_points_equal_oracle(helper, oracle_lib, tmp_path):
+    """mulskips_gb300.shapes.faceted_slab_points (the {111}-faceted 3C-SiC
+    slab of the config-2 bench line): the library's SetShape equals the
+    oracle's, and the surface is {111} facets: its atoms hold three bonds
+    (one dangling bond each, as on a {111} plane), two only on the pyramid
+    apexes and ridges, none one."""
+    from mulskips_gb300.shapes import faceted_slab_points
+    L, h, P = 240, 120, 60
+    xyz, sp = faceted_slab_points(L, h, P)
+    write_points(tmp_path / "p.xyz", xyz, np.where(sp == 1, "Si", "C"))
+    sic_startdat(str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    rc, out = run_helper(helper, str(tmp_path / "start.dat"), str(tmp_path / "p.xyz"), L)
+    assert rc == 0 and "mismatch 0" in out, out
+    o = oracle_lib.Oracle(str(tmp_path / "start.dat"), L, L, L)
+    o.init()
+    st, _ = oracle_lib.compact_state(o)
+    o.close()
+    co = coordination(st)
+    occ = (st & 3) != 0
+    assert occ.sum() == ((xyz[:, 2] > 3) & (xyz[:, 2] < L - 4)).sum()
+    # periodic pyramids: 16 apexes at h + P/2, valleys at h - P/2
+    z = xyz[(xyz[:, 2] > 3) & (xyz[:, 2] < L - 4), 2]
+    assert h + P // 2 - 6 <= z.max() <= h + P // 2
+    n2, n3 = ((co == 2) & occ).sum(), ((co == 3) & occ).sum()
+    assert n3 > 1000 and n2 < n3 / 20, (n2, n3)
+    assert not (occ & (co == 1)).any()
+
+
 def test_undefined_inputs_refused_by_both(helper, tmp_path):
     L = 240
     xyz, sym, lone, lone_kind = pyramid_points(L, 60, 30)
