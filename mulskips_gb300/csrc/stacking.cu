@@ -126,8 +126,15 @@ __device__ __forceinline__ int isign(int a, int b) { return b >= 0 ? abs(a) : -a
 // NINT: nearest integer, halves away from zero
 __device__ __forceinline__ int nint(double v) { return (int)round(v); }
 
+// Set by set_err for the block that raised an error: the window kernel's
+// warps test it after each event (a shared-memory read) instead of reading
+// the grid's error word from L2; errors of other blocks stop them at the
+// next grid barrier.  Kernels that do not read it leave it unset.
+__shared__ int s_block_err;
+
 __device__ void set_err(const Dev &D, int code, int a = 0, int b = 0, int c = 0)
 {
+    s_block_err = 1;
     if (atomicCAS(D.err, 0, code) == 0) {
         D.err[1] = a;
         D.err[2] = b;
@@ -137,6 +144,8 @@ __device__ void set_err(const Dev &D, int code, int a = 0, int b = 0, int c = 0)
 
 // grid point -> array index; a point outside the arrays is an error and
 // reads (0, 0, 0) instead, so no access leaves the arrays
+__device__ __forceinline__ bool block_err() { return *(volatile int *)&s_block_err != 0; }
+
 __device__ __forceinline__ int64_t gidx(const Dev &D, P3 p)
 {
     if (p.x < 0 || p.x >= D.lx || p.y < 0 || p.y >= D.ly || p.z < -ZG || p.z > D.lz + ZG) {
@@ -162,12 +171,33 @@ __device__ __forceinline__ void load_nn(const Rec &r, P3 nn[4])
 {
     for (int i = 0; i < 4; i++) nn[i] = nn_at(r, i);
 }
-__device__ __forceinline__ bool rec_lists(const Dev &D, int r, P3 s)
+// The first 32 bytes of record r (x, y, z, the NextN list, ev, flags) as
+// four 8-byte words: the pool is 256-byte aligned and records sit at 40-byte
+// strides, so every word is aligned.  The heads of several records can be
+// read at once; r <= 0 reads the zero guard record.
+struct RecHead {
+    unsigned long long w[4];
+};
+__device__ __forceinline__ RecHead rec_head(const Dev &D, int r)
 {
-    P3 nn[4];
-    load_nn(D.rec[r], nn);
-    return in_list(nn, s);
+    const unsigned long long *p = reinterpret_cast<const unsigned long long *>(D.rec + (r > 0 ? r : 0));
+    return RecHead{{p[0], p[1], p[2], p[3]}};
 }
+// the k-th int16 of the head (little-endian: bytes 2k, 2k + 1)
+__device__ __forceinline__ int head16(const RecHead &h, int k)
+{
+    return (int)(int16_t)(unsigned short)(h.w[k >> 2] >> (16 * (k & 3)));
+}
+// whether the head's NextN list (int16 3..14) holds s
+__device__ __forceinline__ bool head_lists(const RecHead &h, P3 s)
+{
+    bool hit = false;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        hit |= head16(h, 3 + 3 * i) == s.x && head16(h, 4 + 3 * i) == s.y && head16(h, 5 + 3 * i) == s.z;
+    return hit;
+}
+__device__ __forceinline__ bool rec_lists(const Dev &D, int r, P3 s) { return head_lists(rec_head(D, r), s); }
 
 // the selection weight of a record in its tile list
 __device__ __forceinline__ float list_rate(const Rec &R)
@@ -202,16 +232,34 @@ __device__ void get_prob(const Dev &D, int occ, int nsic, int coor, P3 site, con
         }
         return;
     }
-    int nsi = 0, nc = 0, nb = 0, nw = 0;
+    // the four NextN words and records are read first, all in flight at once,
+    // then tested: a chain of two memory round trips instead of three per
+    // neighbour one after the other
+    uint32_t v[4];
+    int rn[4];
+#pragma unroll
     for (int i = 0; i < 4; i++) {
-        uint32_t v = cw(D, nn[i]);
-        if (!occ_of(v)) continue;
-        if (cov_of(v) == WALLIND) {
+        const int64_t g = gidx(D, nn[i]);
+        v[i] = D.coo[g];
+        rn[i] = D.ind[g];
+    }
+    RecHead h[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = rec_head(D, rn[i]);
+    bool bond[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)                              // reciprocal bonds only (:232-239)
+        bond[i] = occ_of(v[i]) && cov_of(v[i]) != WALLIND && head_lists(h[i], site);
+    int nsi = 0, nc = 0, nb = 0, nw = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (!occ_of(v[i])) continue;
+        if (cov_of(v[i]) == WALLIND) {
             nw++;
             continue;
         }
-        if (rec_lists(D, D.ind[gidx(D, nn[i])], site)) {   // reciprocal bonds only (:232-239)
-            int s = sp_of(v);
+        if (bond[i]) {
+            int s = sp_of(v[i]);
             nsi += s == 1;
             nc += s == 2;
             nb += s == 3;
@@ -594,13 +642,19 @@ __device__ int dep_neighbour(const Dev &D, Ctx &c, P3 site, int coor_old, int i,
                 nnn[1] = site;
                 P3 ns[2];
                 find_nn(D, nnn[0], nnn[1], n, ns);
-                for (int k = 2; k < 4; k++) {
-                    nnn[k] = ns[k - 2];
-                    uint32_t v = cw(D, nnn[k]);
-                    if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND &&
-                        rec_lists(D, D.ind[gidx(D, nnn[k])], n))
-                        coornn++;
+                // both candidates' words and records in flight at once
+                uint32_t v[2];
+                int rk[2];
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    nnn[k + 2] = ns[k];
+                    const int64_t g = gidx(D, ns[k]);
+                    v[k] = D.coo[g];
+                    rk[k] = D.ind[g];
                 }
+                const RecHead h0 = rec_head(D, rk[0]), h1 = rec_head(D, rk[1]);
+                if (occ_of(v[0]) && coor_of(v[0]) <= 3 && cov_of(v[0]) != WALLIND && head_lists(h0, n)) coornn++;
+                if (occ_of(v[1]) && coor_of(v[1]) <= 3 && cov_of(v[1]) != WALLIND && head_lists(h1, n)) coornn++;
                 D.coo[gn] = with_coor(vn, coornn);
                 for (int k = 0; k < 4; k++) put_nn(N, k, nnn[k]);
                 get_prob(D, 0, 0, coornn, n, nnn, ev, rate);
@@ -695,11 +749,28 @@ __device__ void deposition(const Dev &D, Ctx &c, P3 site, int sp)
 // non-wall sites of nn (Evaporation.f:87-104,238-253); NBuff keeps the last.
 __device__ void prune_to_buffer(const Dev &D, Ctx &c, Rec &S, P3 site, bool &got)
 {
+    // the neighbours' words and records are read before S changes (none of
+    // them is S: a site is not its own neighbour), all in flight at once
+    P3 q[4];
+    uint32_t v[4];
+    int rq[4];
+#pragma unroll
     for (int j = 0; j < 4; j++) {
-        P3 q = nn_at(S, j);
-        uint32_t v = cw(D, q);
-        if (occ_of(v) && coor_of(v) <= 3 && cov_of(v) != WALLIND && rec_lists(D, D.ind[gidx(D, q)], site)) {
-            c.nbuff = q;
+        q[j] = nn_at(S, j);
+        const int64_t g = gidx(D, q[j]);
+        v[j] = D.coo[g];
+        rq[j] = D.ind[g];
+    }
+    RecHead h[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) h[j] = rec_head(D, rq[j]);
+    bool hit[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        hit[j] = occ_of(v[j]) && coor_of(v[j]) <= 3 && cov_of(v[j]) != WALLIND && head_lists(h[j], site);
+    for (int j = 0; j < 4; j++) {
+        if (hit[j]) {
+            c.nbuff = q[j];
             got = true;
         }
         put_nn(S, j, P3{0, 0, 0});
@@ -870,7 +941,7 @@ __device__ void deposition_warp(const Dev &D, Ctx &c, P3 site, int sp, int lane)
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) inc += __shfl_xor_sync(FULL, inc, o);   // lanes 0..7 hold the sum
     __syncwarp();
-    if (lane == 0 && !*(volatile int32_t *)D.err) {
+    if (lane == 0 && !block_err()) {
         const int coor = coor_old + inc;
         if (coor != coor_old) D.coo[gs] = with_coor(D.coo[gs], coor);    // :236-250
         uint8_t ev;
@@ -913,7 +984,7 @@ __device__ void evaporation_warp(const Dev &D, Ctx &c, P3 site, int lane)
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) dec += __shfl_xor_sync(FULL, dec, o);
     __syncwarp();
-    if (lane == 0 && !*(volatile int32_t *)D.err) {
+    if (lane == 0 && !block_err()) {
         const int coor = coor_old + dec;
         D.coo[gs] = with_coor(D.coo[gs], coor);                          // :216-261
         if (coor == 0) {
@@ -956,46 +1027,6 @@ __device__ void apply_warp(const Dev &D, Ctx &c, int r, float u, int lane)
     deposition_warp(D, c, site, sp, lane);
 }
 
-__device__ __forceinline__ void prefetch_l1(const void *p)
-{
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-__device__ __forceinline__ bool in_arrays(const Dev &D, P3 p)
-{
-    return p.x >= 0 && p.x < D.lx && p.y >= 0 && p.y < D.ly && p.z >= -ZG && p.z <= D.lz + ZG;
-}
-__device__ __forceinline__ void prefetch_site(const Dev &D, P3 p)
-{
-    if (!in_arrays(D, p)) return;
-    const int64_t g = ((int64_t)(p.z + ZG) * D.ly + p.y) * D.lx + p.x;
-    prefetch_l1(&D.coo[g]);
-    const int r = D.ind[g];
-    if (r > 0) {
-        prefetch_l1(&D.rec[r]);
-        prefetch_l1(reinterpret_cast<const char *>(&D.rec[r]) + sizeof(Rec) - 1);
-    }
-}
-
-// Before lane 0 applies the event of record r, the warp brings the words it
-// will read into L1: the site, its four NextN sites and their sixteen NextN
-// sites (LattCoo word, LattInd and record each; lane 0 + lanes 1..4 + lanes
-// 5..20).  The event then runs on L1 hits instead of a chain of L2 round
-// trips.  Reads only: a point outside the arrays is skipped.
-__device__ void prefetch_event(const Dev &D, int r, int lane)
-{
-    const Rec &R = D.rec[r];
-    if (lane == 0) {
-        prefetch_site(D, P3{R.x, R.y, R.z});
-    } else if (lane <= 4) {
-        prefetch_site(D, nn_at(R, lane - 1));
-    } else if (lane <= 20) {
-        const P3 q = nn_at(R, (lane - 5) >> 2);
-        if (!in_arrays(D, q)) return;
-        const int rq = D.ind[((int64_t)(q.z + ZG) * D.ly + q.y) * D.lx + q.x];
-        if (rq > 0) prefetch_site(D, nn_at(D.rec[rq], (lane - 5) & 3));
-    }
-}
-
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
 
 // One colour phase: every tile of the colour runs from the window's start to
@@ -1008,8 +1039,10 @@ __device__ __forceinline__ long long site_key(const Dev &D, const Rec &R)
 // The running tile's sites that got an event in this event, appended in
 // lane order (every lane calls this after the event).  A record dropped or
 // left without an event in the meantime is appended as a dead entry (rate 0)
-// for the next compaction.
-__device__ void flush_pending(const Dev &D, Ctx &c, int t, int lane)
+// for the next compaction.  ntl is the list's length, held by the warp: only
+// the tile's own warp appends to its list during a phase (other tiles' warps
+// write its inbox), so the length needs no atomic; lane 0 stores it back.
+__device__ void flush_pending(const Dev &D, Ctx &c, int t, int lane, int &ntl)
 {
     int inc = c.npend;
 #pragma unroll
@@ -1019,9 +1052,9 @@ __device__ void flush_pending(const Dev &D, Ctx &c, int t, int lane)
     }
     const int tot = __shfl_sync(FULL, inc, 31);
     if (!tot) return;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&D.tl_n[t], tot);
-    base = __shfl_sync(FULL, base, 0);
+    const int base = ntl;
+    ntl = base + tot;
+    if (lane == 0) D.tl_n[t] = ntl;
     const int excl = inc - c.npend;
     for (int i = 0; i < c.npend; i++) {
         const int r = c.pend[i];
@@ -1181,8 +1214,9 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
     c.npend = 0;
     float rem = tau;
     uint32_t nev = 0, ndraw = 0;
+    int ntl = D.tl_n[t];                      // after drain and compaction (lane 0 wrote it before a __syncwarp)
     for (;;) {
-        const int len = min(*(volatile int32_t *)&D.tl_n[t], LCAP);
+        const int len = min(ntl, LCAP);
         // lane l owns the contiguous chunk [l C, l C + C) of the list: one
         // pass of independent loads gives each lane its partial sum, a warp
         // scan the prefix of every chunk
@@ -1254,13 +1288,12 @@ __device__ void run_tile(const Dev &D, int colour, int k, uint32_t window, float
             }
         }
         if (pick <= 0) break;
-        prefetch_event(D, pick, lane);
         __syncwarp();
         apply_warp(D, c, pick, u01(rnd.w), lane);
-        flush_pending(D, c, t, lane);
+        flush_pending(D, c, t, lane, ntl);
         nev++;
         __syncwarp();
-        if (*(volatile int32_t *)D.err) break;
+        if (block_err()) break;
     }
     if (lane == 0) {
         if (nev) atomicAdd(D.events, (unsigned long long)nev);
@@ -1307,6 +1340,8 @@ __global__ void k_windows(Dev D, uint32_t w0, int nwin, float tau, unsigned long
     const int wid = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const int per = (D.ntx / 2) * (D.nty / 2);
+    if (threadIdx.x == 0) s_block_err = 0;
+    __syncthreads();
     for (int w = 0; w < nwin; w++) {
         if (*(volatile int32_t *)D.err || *(volatile int32_t *)D.stop) return;
         if (*(volatile int32_t *)D.nmc <= 20 || (ev_limit && *(volatile unsigned long long *)D.events >= ev_limit)) {
