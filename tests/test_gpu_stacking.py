@@ -327,3 +327,92 @@ def test_stacking_statistics_match_serial_reference(tmp_path):
         fam.add(k, np.array([g[k] for g in gpu], float), np.array([r[k] for r in ref], float))
     assert np.mean([r["off-grid atoms"] for r in ref]) > 100
     fam.check()
+
+
+# ---------------------------------------------------------------- config 2 as stated: an etching {111}-faceted slab
+C2_SIDE, C2_T_OBS = 240, 2e-11      # s: about 8.4e3 events of the serial reference (a third of the atoms)
+
+
+def slab_observables(lg):
+    """From LattCoo [z, y, x]: atoms, C atoms, and the mean and RMS of the
+    top atom's height over the (x, y) columns holding atoms."""
+    z, y, x = np.nonzero(lg)
+    v = lg[z, y, x]
+    atom = (((v >> 23) & 1) == 1) & ((v & 255) != 113)
+    top = np.full(lg.shape[1:], -1, np.int64)
+    np.maximum.at(top, (y[atom], x[atom]), z[atom])
+    h = top[top >= 0].astype(float)
+    return {"atoms": int(atom.sum()), "C": int((atom & (((v >> 27) & 7) == 2)).sum()),
+            "mean top height": float(h.mean()), "RMS roughness": float(h.std())}
+
+
+def _config2_oracle(args):
+    path, t_obs = args
+    from oracle import ora
+    o = ora.Oracle(path, C2_SIDE, C2_SIDE, C2_SIDE, numbers=None)
+    o.init()
+    o.run_until(t_obs)
+    out = slab_observables(o.lattcoo()[:C2_SIDE])
+    out["events"] = o.iter
+    o.close()
+    return out
+
+
+def _config2_gpu(args):
+    seed, E, D, sf, pzig, xyz, sp, t_obs, f = args
+    from mulskips_gb300 import Lattice
+    with Lattice(C2_SIDE, C2_SIDE, C2_SIDE, ncrystal=2, list_crystal=(14, 6), sf=sf, ptrans_zig=pzig,
+                 seed=seed) as lat:
+        lat.set_rates(E, D)
+        lat.init_points(xyz, sp)
+        t, events = 0.0, 0
+        while t < t_obs:
+            n, t1 = lat.run(lat.suggest_tau(f), 64, 0, t_obs)
+            assert t1 > t
+            t = t1
+            events += n
+        out = slab_observables(lat.lattcoo()[:C2_SIDE])
+        out["events"] = events
+        return out
+
+
+def test_config2_faceted_etch_matches_serial_reference(tmp_path):
+    """Config 2 as stated, on a small box: a 3C-SiC slab with {111} facets
+    only (mulskips_gb300.shapes, square pyramids of period 60 in a 240^3
+    box), per-species fluxes U(0.1, 1) ML/s and 18 evaporation barriers
+    U(0.4, 0.9) eV with a 1e13 prefactor at 1600 K (table seed 2), PtransZig
+    = 0.5362, on the explicit-neighbour engine.  The slab etches; 32 oracle
+    seeds (RunType R) and 32 GPU runs observed at t = 2e-11 s: atoms, C
+    atoms, mean top height and RMS roughness of the etched surface, each
+    inside its 95 % family band (Welch t, Bonferroni over the four)."""
+    import multiprocessing as mp
+    from concurrent.futures import ThreadPoolExecutor
+    from bench import PZIG_1600K, config2_tables
+    from mulskips_gb300.autotune import accurate_f
+    from mulskips_gb300.shapes import faceted_slab_points
+    from mulskips_gb300.startdat import parse_startdat, write_startdat
+    from stat_bands import Family
+    E, D, _, _ = config2_tables()
+    sf = parse_startdat(CUBE_ZZ)["sf"]
+    xyz, sp = faceted_slab_points(C2_SIDE, 120, 60)
+    pts = tmp_path / "slab.xyz"
+    with open(pts, "w") as fh:
+        fh.write(f"{len(xyz)}\nslab\n")
+        fh.write("".join(f"{'Si' if s == 1 else 'C'} {x} {y} {z}\n" for (x, y, z), s in zip(xyz.tolist(), sp)))
+    paths = []
+    for s in range(NSEEDS):
+        p = tmp_path / f"c2_{s}.dat"
+        write_startdat(str(p), E, D, ncrystal=2, list_crystal=(14, 6), init_st="SH", points=str(pts), run_type="R",
+                       seed=1300 + s, sf=sf, ptrans_zig=PZIG_1600K, max_iter=10 ** 9)
+        paths.append(str(p))
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        ref = pool.map(_config2_oracle, [(p, C2_T_OBS) for p in paths])
+    f = accurate_f(2)
+    with ThreadPoolExecutor(8) as ex:
+        gpu = list(ex.map(_config2_gpu, [(71 + s, E, D, sf, PZIG_1600K, xyz, sp, C2_T_OBS, f) for s in range(NSEEDS)]))
+    fam = Family(f"config 2 faceted etch, PtransZig = {PZIG_1600K:.4f}, t = {C2_T_OBS:g} s, f = {f}", 4)
+    for k in ("atoms", "C", "mean top height", "RMS roughness"):
+        fam.add(k, np.array([g[k] for g in gpu], float), np.array([r[k] for r in ref], float))
+    atoms0 = int(((xyz[:, 2] > 3) & (xyz[:, 2] < C2_SIDE - 4)).sum())
+    assert 0.1 * atoms0 < atoms0 - np.mean([r["atoms"] for r in ref]) < 0.6 * atoms0
+    fam.check()
