@@ -583,6 +583,12 @@ struct __align__(128) TileShared {
     int rate_rep;                              // replica whose rate table is in rate/spcum (-1 none)
     unsigned long long mbar;                   // TMA staging barrier
     unsigned int tma_phase;                    // its parity
+    // persistent schedule, a colour with exactly one tile of this warp: the
+    // tile's colour count (0 otherwise) and, per neighbour k, (tile << 2) |
+    // phase lag -- fixed for the launch, so the flag polls start without
+    // global reads
+    int one_ncol[4];
+    int one_nb[4][8];
 };
 
 // The one tile a warp works on (one warp per block).  Declared at file scope so
@@ -1232,20 +1238,23 @@ __device__ __forceinline__ void process_tile(RepDev *reps, QuadDev *quads, int q
         quads[qid].zlo = zlo;
         quads[qid].zhi = zhi;
         quads[qid].mc = live;
-        if (nev) quads[qid].ev += (int)nev;      // only this tile writes its count
+        // only this tile adds to its count during a launch: a reduction, so
+        // the lane does not wait for a read of the old value
+        if (nev) atomicAdd(&quads[qid].ev, (int)nev);
         if (scp)
             for (int j = 0; j < 4; j++) atomicAdd(&score_all[4 * Q.rep + j], sc[j]);
         if (A)
             for (int s2 = 0; s2 < 3; s2++)
                 if (S.dcnt[s2]) atomicAdd((unsigned long long *)&la_all[Q.rep].cnt[s2], (unsigned long long)(long long)S.dcnt[s2]);
-        if (hz_hi >= 0) {
-            // widen the z bands of the neighbouring tiles whose sites changed
-            for (int k = 0; k < 8; k++) {
-                QuadDev *N = &quads[quads[qid].nbr[k]];
-                atomicMin(&N->zlo, hz_lo);
-                atomicMax(&N->zhi, hz_hi);
-            }
-        }
+    }
+    if (hz_hi >= 0 && lane < 8) {
+        // widen the z bands of the neighbouring tiles whose sites changed:
+        // lane k takes neighbour k (hz_lo, hz_hi are uniform over the warp),
+        // so the eight lookups and reductions are in flight together before
+        // the tile publishes its progress
+        QuadDev *N = &quads[quads[qid].nbr[lane]];
+        atomicMin(&N->zlo, hz_lo);
+        atomicMax(&N->zhi, hz_hi);
     }
 }
 
@@ -1289,35 +1298,66 @@ __global__ void __launch_bounds__(32, 16) k_sl_persistent(RepDev *reps, QuadDev 
     // this warp's tiles of colour c: wtiles[woff[4 g + c] .. woff[4 g + c + 1])
     const int o0 = woff[4 * blockIdx.x], o1 = woff[4 * blockIdx.x + 1], o2 = woff[4 * blockIdx.x + 2],
               o3 = woff[4 * blockIdx.x + 3], o4 = woff[4 * blockIdx.x + 4];
+    for (int c = 0; c < 4; c++) {
+        const int kb = c == 0 ? o0 : (c == 1 ? o1 : (c == 2 ? o2 : o3));
+        const int ke = c == 0 ? o1 : (c == 1 ? o2 : (c == 2 ? o3 : o4));
+        if (ke - kb == 1) {
+            const int t = wtiles[kb];
+            const int nc = quads[t].ncol;
+            if (lane == 0) g_tile.one_ncol[c] = nc;
+            if (lane < 8) {
+                const int n = quads[t].nbr[lane];
+                g_tile.one_nb[c][lane] = (n << 2) | ((c - quads[n].colour + nc) % nc);
+            }
+        } else if (lane == 0) {
+            g_tile.one_ncol[c] = 0;
+        }
+    }
+    __syncwarp();
     // windows in order, colours in order within a window: every wait points
     // to a phase that comes earlier in this order
     for (int w = 0; w < nwin; w++)
         for (int c = 0; c < 4; c++) {
             int kb = c == 0 ? o0 : (c == 1 ? o1 : (c == 2 ? o2 : o3));
             int ke = c == 0 ? o1 : (c == 1 ? o2 : (c == 2 ? o3 : o4));
+            const int one_nc = g_tile.one_ncol[c];
             for (int k = kb; k < ke; k++) {
                 int t = wtiles[k];
-                const int ncol = quads[t].ncol;
+                const int ncol = one_nc ? one_nc : quads[t].ncol;
                 const int P = ncol * w + c;
+                // lane 8 reads the error word while lanes 0..7 poll, so a
+                // phase whose flags are already set costs one round trip
+                int bad = lane == 8 ? *(volatile int *)&status->error : 0;
                 if (lane < 8) {
-                    int n = quads[t].nbr[lane];
-                    int need = P - ((c - quads[n].colour + ncol) % ncol);
+                    int n, need;
+                    if (one_nc) {
+                        const int v = g_tile.one_nb[c][lane];
+                        n = v >> 2;
+                        need = P - (v & 3);
+                    } else {
+                        n = quads[t].nbr[lane];
+                        need = P - (c - quads[n].colour + ncol) % ncol;
+                    }
                     long long t0 = clock64();
                     volatile int *pr = progress + n;
                     volatile int *err = &status->error;
                     // tight poll (one L2 round trip per check; a sleep between
                     // checks oversleeps the flag and lengthens every phase)
                     while (*pr < need) {
-                        if (*err) break;
+                        if (*err) {
+                            bad = 1;
+                            break;
+                        }
                         if (clock64() - t0 > spin_limit) {
                             set_error(status, DERR_TIMEOUT, t);
+                            bad = 1;
                             break;
                         }
                     }
                 }
                 __syncwarp();
                 __threadfence();                                // acquire: neighbours' writes before their flag
-                if (*(volatile int *)&status->error) return;
+                if (__any_sync(0xffffffffu, bad != 0)) return;
                 const RepDev &R = reps[quads[t].rep];
                 process_tile<LAM, COV>(reps, quads, t, st_all, status, (uint32_t)c, R.window + (unsigned)w,
                                        R.T0 + (double)w * R.tau, la, score, tmaps);
