@@ -447,24 +447,24 @@ int main()
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
     if (in.ncov) check(mks_set_coverage_rates(h, in.pAbs.data(), in.pDes.data()));
     double la_tmax = 0.0;
-    if (in.init_st == "LA") {                         // SetT (SetT.f:25-50): TempStat, one record per layer
+    if (in.init_st == "LA") {                         // SetT (SetT.f:50-66): TempStat, one READ per layer
         FILE *tf = fopen(in.temp_file.c_str(), "r");
         if (!tf) die("cannot open the temperature file");
         std::vector<int32_t> field((size_t)lx * ly * lz, 10);
-        std::vector<char> line((size_t)lx * ly * 32 + 4096);
+        ListReader rd(tf);
         for (int z = 0; z < lz; z++) {
-            if (!fgets(line.data(), (int)line.size(), tf)) die("temperature file: too few records");
-            char *p = line.data();
-            for (int y = 0; y < ly; y++)
-                for (int x = 0; x < lx; x++) {
-                    char *e;
-                    double v = strtod(p, &e);
-                    if (e == p) die("temperature file: short record");
-                    p = e;
-                    int t = (int)v;                   // INT(LenIn)
-                    field[(size_t)z + (size_t)lz * ((size_t)x + (size_t)lx * y)] = t;
-                    if (t != 10) la_tmax = std::max(la_tmax, (double)t);
-                }
+            // list-directed READ of LenX*LenY values (they may span records;
+            // the rest of the last record is skipped), x fastest
+            bool ok = rd.read((size_t)lx * ly, [&](size_t k, const char *tok) {
+                char *e;
+                double v = strtod(tok, &e);
+                if (e == tok) die("temperature file: not a number");
+                const int t = (int)v;                 // INT(LenIn)
+                const size_t x = k % (size_t)lx, y = k / (size_t)lx;
+                field[(size_t)z + (size_t)lz * (x + (size_t)lx * y)] = t;
+                if (t != 10) la_tmax = std::max(la_tmax, (double)t);
+            });
+            if (!ok) die("temperature file: too few values");
         }
         fclose(tf);
         check(mks_batch_set_field(h, 0, field.data()));

@@ -160,17 +160,23 @@ def test_mulskips_e_la(oracle_lib, tmp_path):
     frame equals the oracle's, and the run writes the LA phases file.  The
     run is capped at 4000 events: the nucleus solidifies to the upper wall
     within about 13000, after which the reference stops on too few MC sites
-    and its final frame (index 0) would overwrite I00000000."""
+    and its final frame (index 0) would overwrite I00000000.  Each layer of
+    both files is wrapped over records of 997 values, as a Fortran runtime may
+    write a list-directed record: SetT's and SetCAD's READ(*) read across
+    them."""
     L = 120
     d = tmp_path / "la"
     d.mkdir()
     layers = np.where(np.arange(L) < 100, 1, 10).astype(np.int8)
     layers[:4] = 10
     T = np.where(layers == 10, 10, (1650 + 0.1 * np.arange(L)).astype(np.int64))
+    def wrapped(vals, n=997):
+        return "".join(" ".join(vals[i:i + n]) + "\n" for i in range(0, len(vals), n))
+
     with open(d / "LattGeo.dat", "w") as fg, open(d / "TempStat.dat", "w") as ft:
         for z in range(L):
-            fg.write(" ".join([str(int(layers[z]))] * (L * L)) + "\n")
-            ft.write(" ".join([str(int(T[z]))] * (L * L)) + "\n")
+            fg.write(wrapped([str(int(layers[z]))] * (L * L)))
+            ft.write(wrapped([str(int(T[z]))] * (L * L)))
     out, skip = [], False
     for line in open(os.path.join(GOLDEN, "LA", "start.dat")).read().splitlines():
         if skip:
