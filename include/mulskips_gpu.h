@@ -92,7 +92,9 @@ typedef struct {
     double sf;                     /* super-lattice parameter in Angstrom        */
     uint64_t seed;                 /* IDUM / replica seed                        */
     int32_t list_cov[3];           /* coverage atomic numbers (ListCov, main.f:91) */
-    int32_t pad;
+    int32_t explicit_nn;           /* 1: the explicit-neighbour engine even at PtransZig = 1,
+                                      for lattices with atoms off the diamond sites (InitSt E);
+                                      0 (the default): that engine only when PtransZig < 1 */
 } mks_config;
 
 /* One applied event (the trace format of the oracle and of mks_replay). */
@@ -395,7 +397,12 @@ int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field);
  * "Fa" SetSiC3Cwwaperture (Len1, Len2, Len3; these two and "FF" round each
  * length down to a multiple of 24), "FF" SetSiFINFET (Len1..Len4), "ST"
  * SetTrenchSi (Len1, Len2, Len3; params = angle in degrees, Ttop, Tbottom in
- * K; also loads the temperature field T(z) for mks_batch_set_tabulated).
+ * K; also loads the temperature field T(z) for mks_batch_set_tabulated), "E"
+ * SetSiCSF (Len1, Len2, Len3: a 3C-SiC slab up to Len1 with a triangular
+ * triple stacking fault whose vertex is (Len2, Len3, Len1 - Len2), as
+ * main.f:267-272 passes it; its atoms lie off the diamond sites, so only a
+ * handle on the explicit-neighbour engine takes it -- PtransZig < 1 or
+ * mks_config.explicit_nn = 1 -- and the rates must be set first).
  * Same result as the reference's routines including their closing
  * coordination passes.                                                      */
 int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const int32_t *lens, const double *params);

@@ -19,7 +19,7 @@ class MksConfig(C.Structure):
     _fields_ = [("lenx", C.c_int32), ("leny", C.c_int32), ("lenz", C.c_int32),
                 ("ncrystal", C.c_int32), ("ncov", C.c_int32), ("list_crystal", C.c_int32 * 3),
                 ("ptrans_zig", C.c_double), ("sf", C.c_double), ("seed", C.c_uint64),
-                ("list_cov", C.c_int32 * 3), ("pad", C.c_int32)]
+                ("list_cov", C.c_int32 * 3), ("explicit_nn", C.c_int32)]
 
 
 class MksEvent(C.Structure):

@@ -34,6 +34,7 @@
 #include "tiling.cuh"
 #include "rng.cuh"
 #include "stacking.cuh"
+#include "sicsf.h"
 #include "../../include/mulskips_gpu.h"
 
 using namespace mks;
@@ -1764,6 +1765,9 @@ int check_config(const mks_config &c)
     if (c.ptrans_zig != 1.0 && c.ncov)
         return fail(MKS_ERR_UNSUPPORTED, "PtransZig=%g with a coverage species: arm-chair stacking runs without coverage",
                     c.ptrans_zig);
+    if (c.explicit_nn != 0 && c.explicit_nn != 1) return fail(MKS_ERR_ARG, "explicit_nn=%d is not 0 or 1", c.explicit_nn);
+    if (c.explicit_nn && c.ncov)
+        return fail(MKS_ERR_UNSUPPORTED, "the explicit-neighbour engine runs without coverage species");
     return 0;
 }
 
@@ -2014,9 +2018,10 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
     }
     h->st_bytes = off;
     for (int i = 0; i < n; i++)
-        if (cfgs[i].ptrans_zig != 1.0 && n != 1) {
+        if ((cfgs[i].ptrans_zig != 1.0 || cfgs[i].explicit_nn) && n != 1) {
             delete h;
-            return fail(MKS_ERR_UNSUPPORTED, "arm-chair stacking (PtransZig < 1) runs in single-replica handles");
+            return fail(MKS_ERR_UNSUPPORTED,
+                        "the explicit-neighbour engine (PtransZig < 1, explicit_nn) runs in single-replica handles");
         }
     partition(h);
     auto cleanup_fail = [&](const char *what, cudaError_t e) {
@@ -2079,7 +2084,7 @@ int create_impl(const mks_config *cfgs, int n, mks_handle **out)
         mks_destroy(h);
         return rc;
     }
-    if (n == 1 && cfgs[0].ptrans_zig != 1.0) {
+    if (n == 1 && (cfgs[0].ptrans_zig != 1.0 || cfgs[0].explicit_nn)) {
         std::string err;
         rc = mks_stk::create(&h->stk, cfgs[0], h->stream, err);
         if (rc) {
@@ -3156,13 +3161,42 @@ int mks_batch_set_field(mks_handle *h, int32_t rep, const int32_t *field)
     });
 }
 
+// InitSt E, SetSiCSF (main.f:267-272 passes Len1 and the vertex (Len2,
+// Len3, Len1 - Len2)): built on the host (sicsf.h) as LattCoo and the
+// reference's lists, loaded into the explicit-neighbour engine, which rates
+// every entry from that state.  The fault's atoms lie off the diamond sites,
+// which the compact lattice cannot hold.
+static int init_sicsf(mks_handle *h, const int32_t *lens)
+{
+    if (!h->stk)
+        return fail(MKS_ERR_UNSUPPORTED, "InitSt E (SetSiCSF) places atoms off the diamond sites: it needs the "
+                                         "explicit-neighbour engine (PtransZig < 1 or mks_config.explicit_nn = 1)");
+    const mks_config &c = h->reps[0].cfg;
+    mks_sicsf::Result R;
+    const int vsf[3] = {lens[1], lens[2], lens[0] - lens[1]};
+    const std::string e = mks_sicsf::build(c.lenx, c.leny, c.lenz, lens[0], vsf, R);
+    if (!e.empty()) return fail(MKS_ERR_ARG, "SetSiCSF: %s", e.c_str());
+    const int64_t n = (int64_t)(R.mc.size() + R.bulk.size());
+    std::vector<int32_t> xyz((size_t)n * 3), nn((size_t)n * 12);
+    int64_t k = 0;
+    for (const auto *list : {&R.mc, &R.bulk})
+        for (const auto &en : *list) {
+            for (int q = 0; q < 3; q++) xyz[(size_t)(3 * k + q)] = en.xyz[q];
+            for (int j = 0; j < 4; j++)
+                for (int q = 0; q < 3; q++) nn[(size_t)(12 * k + 3 * j + q)] = en.nn[j][q];
+            k++;
+        }
+    return mks_load_lists(h, R.lattcoo.data(), n, xyz.data(), nn.data(), nullptr, nullptr);
+}
+
 int mks_batch_init_shape(mks_handle *h, int32_t rep, const char *init_st, const int32_t *lens, const double *params)
 {
     if (!h || !init_st || !lens || rep < 0 || rep >= (int)h->reps.size()) return fail(MKS_ERR_ARG, "bad arguments");
     const RepHost &r = h->reps[rep];
     const int lx = r.cfg.lenx, ly = r.cfg.leny, lz = r.cfg.lenz;
-    mks_shapes::Grid g(lx, ly, lz);
     std::string kind(init_st);
+    if (kind == "E") return init_sicsf(h, lens);
+    mks_shapes::Grid g(lx, ly, lz);
     std::vector<int> temp;
     char msg[160];
     if (int e = mks_shapes::build_shape(g, kind, lens, params, temp, msg, sizeof msg))

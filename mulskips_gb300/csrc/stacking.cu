@@ -1424,9 +1424,12 @@ __global__ void k_rate_all(Dev D, const uint8_t *ini, const int32_t *gev, const 
         uint32_t v = cw(D, s);
         P3 nn[4];
         load_nn(R, nn);
-        uint8_t ev;
-        float rate;
-        get_prob(D, occ_of(v), sp_of(v), coor_of(v), s, nn, ev, rate);
+        uint8_t ev = EV_NONE;
+        float rate = 0.f;
+        // a bulk atom (coordination 4) has no event and the reference never
+        // asks Get_Prob about it: a slab without walls (SetSiCSF) leaves its
+        // bottom layer at coordination 4 over empty sites
+        if (!(occ_of(v) && coor_of(v) == 4)) get_prob(D, occ_of(v), sp_of(v), coor_of(v), s, nn, ev, rate);
         if (ev == EV_DUMMY && ini && ini[r]) rate = 1.e-6f;
         if (gev && ev != EV_ISO) {
             ev = (uint8_t)gev[r];

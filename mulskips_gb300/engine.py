@@ -63,12 +63,16 @@ class Lattice:
     species (at most one; e.g. (1,) for H in CVD)."""
 
     def __init__(self, lenx, leny, lenz, ncrystal=1, list_crystal=(14,), ptrans_zig=1.0, sf=5.43 / 12,
-                 seed=1, list_cov=()):
+                 seed=1, list_cov=(), explicit_nn=False):
+        """explicit_nn: run the explicit-neighbour engine even at PtransZig = 1
+        (the engine of PtransZig < 1; needed for atoms off the diamond sites,
+        InitSt 'E')."""
         self.dims = (int(lenx), int(leny), int(lenz))
         self.na, self.nb, self.nz = lenx // 6, leny // 6, lenz // 3 + 1
         h = C.c_void_p()
-        N.check(N.lib().mks_create(C.byref(_cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf,
-                                                 seed, list_cov)), C.byref(h)))
+        cfg = _cfg(lenx, leny, lenz, ncrystal, list_crystal, ptrans_zig, sf, seed, list_cov)
+        cfg.explicit_nn = 1 if explicit_nn else 0
+        N.check(N.lib().mks_create(C.byref(cfg), C.byref(h)))
         self._h = h
 
     def close(self):
@@ -108,7 +112,9 @@ class Lattice:
         """The reference's shaped lattices: 'C' (SetNC), 'S' (SetNCSp), 'SS'
         (SetNCSpSi), 'I' (SetInvPOff) and its variants 'D', 'Z', 'J', 'K', 'L',
         'T' (SetTrench), 'Fw' / 'Fa' (SetSiC3Cww / SetSiC3Cwwaperture), 'FF'
-        (SetSiFINFET), 'ST' (SetTrenchSi, params = angle, Ttop, Tbottom)."""
+        (SetSiFINFET), 'ST' (SetTrenchSi, params = angle, Ttop, Tbottom), 'E'
+        (SetSiCSF, a stacking fault off the diamond sites: a handle made with
+        ptrans_zig < 1 or explicit_nn=True, rates set first)."""
         l = np.zeros(4, dtype=np.int32)
         l[:len(lens)] = lens
         p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)

@@ -423,11 +423,11 @@ int main()
     const bool shaped = in.init_st == "C" || in.init_st == "S" || in.init_st == "SS" || in.init_st == "I" ||
                         in.init_st == "D" || in.init_st == "Z" || in.init_st == "J" || in.init_st == "K" ||
                         in.init_st == "L" || in.init_st == "T" || in.init_st == "Fw" || in.init_st == "Fa" ||
-                        in.init_st == "FF" || in.init_st == "ST";
+                        in.init_st == "FF" || in.init_st == "ST" || in.init_st == "E";
     if (in.init_st != "FS" && in.init_st != "F" && in.init_st != "SG" && in.init_st != "IN" && in.init_st != "LA" &&
         in.init_st != "SH" && !shaped)
-        die("initialization not_implemented in the GPU engine (A and E are not: FS, F, Fw, Fa, SG, C, S, SS, I, D, Z, "
-            "J, K, L, T, FF, ST, IN, SH and LA are)");
+        die("initialization not_implemented in the GPU engine (A is not: FS, F, Fw, Fa, SG, C, S, SS, I, D, Z, J, K, "
+            "L, T, FF, ST, E, IN, SH and LA are)");
     if (in.alloy > 0.0 && in.init_st == "LA")   // SetCAD.f:142,161 read LenSiGe, which nothing sets
         die("ERR: InitSt LA with an alloy fraction > 0 is not built (SetCAD reads an unset LenSiGe there)");
     mks_config cfg;
@@ -442,6 +442,9 @@ int main()
     cfg.ptrans_zig = in.ptrans_zig;
     cfg.sf = in.sf;
     cfg.seed = (uint64_t)in.idum;
+    // SetSiCSF places atoms off the diamond sites: the explicit-neighbour
+    // engine holds them, whatever PtransZig is
+    cfg.explicit_nn = in.init_st == "E" ? 1 : 0;
     mks_handle *h = nullptr;
     check(mks_create(&cfg, &h));
     check(mks_set_rates(h, in.pE.data(), in.pD.data()));
@@ -544,6 +547,8 @@ int main()
         check(mks_batch_init_alloy(h, &len1, &in.alloy, (uint64_t)in.idum));
     } else if (shaped) {                              // main.f:240-278
         int32_t lens[4] = {in.len[0], in.len[1], in.len[2], in.len[3]};
+        if (in.init_st == "E")                        // main.f:268-271
+            printf(" %d %d %d %d\n", lens[0], lens[1], lens[2], lens[0] - lens[1]);
         check(mks_init_shape(h, in.init_st.c_str(), lens, in.st_par));
     } else {
         int len1 = in.len[0] - in.len[0] % 24;

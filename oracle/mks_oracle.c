@@ -2514,6 +2514,228 @@ static void set_shape(ora_t *o)
     }
 }
 
+/* SetSiCSF, MS/initial/SetSiCSF.f:7-473 (InitSt 'E', MS/main.f:267-272:
+ * called with Len1 and the vertex VSF = (Len2, Len3, Len1 - Len2)): a 3C-SiC
+ * (001) slab up to z = Len - 1 holding a triangular triple stacking fault.
+ * In the region x >= VSF(1), y >= VSF(2), z >= VSF(3) the atoms of two
+ * {111} planes per sublattice (Si: (x-Vx)+(y-Vy)-(z-Vz) = 12 and 24, C: 3
+ * and 15) are shifted by (+2, +2, +4) and (-2, -2, -4), off the diamond
+ * sites.  Then two passes over z = 13..Len+6 in scan order: the first
+ * empties atoms with fewer than two neighbours (diamond bonds, or the
+ * 32-site |d|^2 = 27 shell when they have fewer than two diamond bonds);
+ * the second sets coordinations and builds the lists, an off-grid atom's
+ * NextN being its shell neighbours completed by FIND_NN, rates by
+ * Get_Prob_Ini.  Then the coordinations are cut to reciprocal bonds, MC
+ * atoms first, then bulk atoms of z >= 13 (re-rated by Get_Prob; a bulk atom
+ * that changes becomes MC: EraseBulk, AddMC -- over the bulk count at the
+ * loop's start, as the Fortran DO evaluates it once), and last the ad-voids
+ * of every MC atom's NextN (:432-471). */
+static void set_sicsf(ora_t *o, int len, const int vsf[3])
+{
+    const int lx = o->lx, ly = o->ly;
+    const int box_sf = len - vsf[2];
+    int shell[32][3], ns = 0;                       /* ListNN, :24-35: k outer, i inner */
+    for (int k = -6; k <= 6; k++)
+        for (int j = -6; j <= 6; j++)
+            for (int i = -6; i <= 6; i++)
+                if (i * i + j * j + k * k == 27) {
+                    shell[ns][0] = i;
+                    shell[ns][1] = j;
+                    shell[ns][2] = k;
+                    ns++;
+                }
+    if (vsf[0] + box_sf > lx || vsf[1] + box_sf > ly || box_sf <= 0)
+        ora_fail(o, "error SF dimension is not correctly set");
+    if (dia_kind(vsf[0], vsf[1], vsf[2]) != 1)
+        ora_fail(o, "SF Vertex position in wrong Site %d %d %d %d", vsf[0], vsf[1], vsf[2], len);
+    if (len + 9 > o->lz) ora_fail(o, "SetSiCSF reads up to z = Len + 9: LenZ too small");
+    int site[3], nextn[4][3];
+    /* :56-107: bulk 3C for z = 0..12 */
+    for (int z = 0; z <= 12; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                int32_t *v = &o->latt[lidx(o, x, y, z)];
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+                mvbits(4, LEN_COOR, v, POS_COOR);
+                site[0] = x; site[1] = y; site[2] = z;
+                std_neighbours(o, site, k == 1 ? 0 : 4, nextn);
+                add_bulk(o, site, nextn);
+            }
+    /* :109-163: z = 13..Len-1 with the shifted planes (bits only: IBSET) */
+    for (int z = 13; z <= len - 1; z++)
+        for (int y = 0; y < ly; y++)
+            for (int x = 0; x < lx; x++) {
+                int k = dia_kind(x, y, z);
+                if (!k) continue;
+                const int inside = x >= vsf[0] && y >= vsf[1] && z >= vsf[2];
+                const int d = (x - vsf[0]) + (y - vsf[1]) - (z - vsf[2]);
+                const int p1 = inside ? d - (k == 1 ? 12 : 3) : -1;
+                const int p2 = inside ? d - (k == 1 ? 24 : 15) : -1;
+                int tx = x, ty = y, tz = z;
+                if (p1 == 0) {
+                    if (!(x + 2 < lx && y + 2 < ly && z + 4 < len)) continue;
+                    tx = x + 2; ty = y + 2; tz = z + 4;
+                } else if (p2 == 0) {
+                    if (!(x - 2 > 0 && y - 2 > 0 && z - 4 > 0)) continue;
+                    tx = x - 2; ty = y - 2; tz = z - 4;
+                }
+                int32_t *v = &o->latt[lidx(o, tx, ty, tz)];
+                *v = (int32_t)((uint32_t)*v | (1u << (k == 1 ? POS_SI : POS_C)) | (1u << POS_OCC));
+            }
+    /* the diamond bonds and the shell neighbours of an occupied site (:172-208) */
+    int nd[32][3];
+    for (int pass = 0; pass < 2; pass++)
+        for (int z = 13; z <= len + 6; z++)
+            for (int y = 0; y < ly; y++)
+                for (int x = 0; x < lx; x++) {
+                    int32_t *v = &o->latt[lidx(o, x, y, z)];
+                    if (!ibits(*v, POS_OCC, LEN_OCC)) continue;
+                    site[0] = x; site[1] = y; site[2] = z;
+                    const int sic = ((x / 3 + y / 3 + z / 3) % 4 == 3) ? 4 : 0;
+                    std_neighbours(o, site, sic, nextn);
+                    int coor = 0, coord = 0, j = 0;
+                    for (int i = 0; i < 4; i++)
+                        if (ibits(*LC(o, nextn[i]), POS_OCC, LEN_OCC)) coor++;
+                    if (coor < 2) {
+                        for (int i = 0; i < ns; i++) {
+                            int q[3] = {x + shell[i][0], y + shell[i][1], z + shell[i][2]};
+                            if (q[0] >= lx) q[0] -= lx;
+                            if (q[0] < 0) q[0] += lx;
+                            if (q[1] >= ly) q[1] -= ly;
+                            if (q[1] < 0) q[1] += ly;
+                            if (ibits(*LC(o, q), POS_OCC, LEN_OCC)) {
+                                coord++;
+                                cp3(nd[j++], q);
+                            }
+                        }
+                        if (j > 4) ora_fail(o, "SetSiCSF: more than four shell neighbours at %d %d %d", x, y, z);
+                    }
+                    if (pass == 0) {                /* :209-220 */
+                        if (coord > coor) {
+                            if (coord <= 1) *v = 0;
+                        } else if (coor <= 1) {
+                            *v = 0;
+                        }
+                        continue;
+                    }
+                    int ev;
+                    double prob;
+                    const int iat = ibits(*v, POS_SIC, LEN_SIC);
+                    if (coord > coor) {             /* :284-317 */
+                        mvbits(coord, LEN_COOR, v, POS_COOR);
+                        int nn4[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                        for (int i = 0; i < j && i < 4; i++) cp3(nn4[i], nd[i]);
+                        if (coord <= 3) {
+                            int ns2[2][3];
+                            find_nn(nn4[0], nn4[1], site, ns2, lx, ly);
+                            cp3(nn4[2], ns2[0]);
+                            cp3(nn4[3], ns2[1]);
+                            get_prob_ini(o, 1, iat, coord, site, nn4, &ev, &prob);
+                            add_mc(o, site, nn4, ev, prob);
+                        } else {
+                            add_bulk(o, site, nn4);
+                        }
+                    } else {                        /* :318-330 */
+                        mvbits(coor, LEN_COOR, v, POS_COOR);
+                        if (coor <= 3) {
+                            get_prob_ini(o, 1, iat, coor, site, nextn, &ev, &prob);
+                            add_mc(o, site, nextn, ev, prob);
+                        } else {
+                            add_bulk(o, site, nextn);
+                        }
+                    }
+                }
+    /* :336-377 (MC atoms) and :380-427 (bulk atoms of z >= 13): reciprocal bonds only */
+    for (int kind = 0; kind < 2; kind++) {
+        const int64_t n0 = kind == 0 ? o->num_mc : o->num_bulk;
+        for (int64_t i = 1; i <= n0; i++) {
+            int nn4[4][3];
+            if (kind == 0) {
+                cp3(site, o->mc[i].xyz);
+                memcpy(nn4, o->mc[i].nn, sizeof nn4);
+            } else {
+                cp3(site, o->bulk[i].xyz);
+                if (site[2] < 13) continue;
+                memcpy(nn4, o->bulk[i].nn, sizeof nn4);
+            }
+            int32_t *v = LC(o, site);
+            int coor = ibits(*v, POS_COOR, LEN_COOR);
+            const int coor_old = coor;
+            for (int jn = 0; jn < 4; jn++) {
+                const int32_t w = *LC(o, nn4[jn]);
+                if (!ibits(w, POS_OCC, LEN_OCC)) continue;
+                const int ind_nn = *LI(o, nn4[jn]);
+                const int(*back)[3] = ibits(w, POS_COOR, LEN_COOR) == 4 ? o->bulk[ind_nn].nn : o->mc[ind_nn].nn;
+                int recip = 0;
+                for (int kk = 0; kk < 4; kk++) recip |= same3(back[kk], site);
+                if (!recip) coor--;
+            }
+            if (coor == coor_old) continue;
+            const int inds = *LI(o, site);
+            const int iat = ibits(*v, POS_SIC, LEN_SIC);
+            mvbits(coor, LEN_COOR, v, POS_COOR);
+            int ev;
+            double prob;
+            get_prob(o, 1, iat, 0, coor, site, nn4, &ev, &prob);
+            if (kind == 0) {
+                o->mc[inds].ind_event = ev;
+                o->mc[inds].prob = prob;
+                update_tree(o, inds, prob);
+            } else {
+                erase_bulk(o, site);
+                add_mc(o, site, nn4, ev, prob);
+            }
+        }
+    }
+    /* :429-471: the ad-voids of every MC atom's NextN */
+    const int nmc_old = o->num_mc;
+    for (int i = 1; i <= nmc_old; i++) {
+        int nns[3];
+        cp3(nns, o->mc[i].xyz);
+        for (int jn = 0; jn < 4; jn++) {
+            cp3(site, o->mc[i].nn[jn]);
+            int32_t *v = LC(o, site);
+            if (ibits(*v, POS_OCC, LEN_OCC)) continue;
+            int nn4[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            const int coor = ibits(*v, POS_COOR, LEN_COOR) + 1;
+            int ev;
+            double prob;
+            if (coor == 1) {
+                cp3(nn4[0], nns);
+                mvbits(coor, LEN_COOR, v, POS_COOR);
+                get_prob_ini(o, 0, 0, coor, site, nn4, &ev, &prob);
+                add_mc(o, site, nn4, ev, prob);
+            } else if (coor == 2) {
+                const int inds = *LI(o, site);
+                memcpy(nn4, o->mc[inds].nn, sizeof nn4);
+                cp3(nn4[1], nns);
+                int ns2[2][3];
+                find_nn(nn4[0], nn4[1], site, ns2, lx, ly);
+                cp3(nn4[2], ns2[0]);
+                cp3(nn4[3], ns2[1]);
+                mvbits(coor, LEN_COOR, v, POS_COOR);
+                get_prob_ini(o, 0, 0, coor, site, nn4, &ev, &prob);
+                memcpy(o->mc[inds].nn, nn4, sizeof nn4);
+                o->mc[inds].ind_event = ev;
+                o->mc[inds].prob = prob;
+                update_tree(o, inds, prob);
+            } else if (coor == 3) {
+                const int inds = *LI(o, site);
+                memcpy(nn4, o->mc[inds].nn, sizeof nn4);
+                mvbits(coor, LEN_COOR, v, POS_COOR);
+                get_prob_ini(o, 0, 0, coor, site, nn4, &ev, &prob);
+                o->mc[inds].ind_event = ev;
+                o->mc[inds].prob = prob;
+                update_tree(o, inds, prob);
+            } else {
+                ora_fail(o, "Vacancy in the SF setting");
+            }
+        }
+    }
+}
+
 int ora_init(ora_t *o)
 {
     if (setjmp(o->jb)) return -1;
@@ -2555,6 +2777,10 @@ int ora_init(ora_t *o)
         set_cad(o, 0);
     } else if (!strcmp(o->init_st, "SH")) {      /* MS/main.f:281-286 */
         set_shape(o);
+    } else if (!strcmp(o->init_st, "E")) {       /* MS/main.f:267-272 */
+        const int vsf[3] = {o->len2, o->len3, o->len1 - o->len2};
+        lg(o, " %d %d %d %d\n", o->len1, vsf[0], vsf[1], vsf[2]);
+        set_sicsf(o, o->len1, vsf);
     } else {
         ora_fail(o, "initialization not_implemented in the oracle: %s", o->init_st);
     }

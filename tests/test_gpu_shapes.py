@@ -507,3 +507,32 @@ def test_batch_replicas_of_shapes_match_oracle(oracle_lib, tmp_path):
     for r in range(3):
         assert np.array_equal(b.state(r), refs[r]), r
     b.close()
+
+
+def test_mulskips_e_sicsf(oracle_lib, tmp_path):
+    """mulskips.e with InitSt E (SetSiCSF, a stacking fault off the diamond
+    sites, run on the explicit-neighbour engine at the start.dat's
+    PtransZig = 1): the initial frame equals the oracle's, and the run of
+    4000 events writes its second frame."""
+    from test_shape_points import sicsf_startdat
+    L = 120
+    d = tmp_path / "sicsf"
+    d.mkdir()
+    sicsf_startdat(d / "start.dat", 60, 24, 24)
+    out = []
+    for line in (d / "start.dat").read_text().splitlines():
+        if "! IterMax" in line:
+            line = "4000 ! IterMax"
+        elif "! OutMolMol" in line:
+            line = "4000 ! OutMolMol"
+        out.append(line)
+    (d / "start.dat").write_text("\n".join(out) + "\n")
+    o = oracle_lib.Oracle(str(d / "start.dat"), L, L, L)
+    o.init()
+    o.write_frame(str(tmp_path / "ora"), 0.0, 0)
+    o.close()
+    r = subprocess.run([EXE], cwd=d, env=dict(os.environ, MULSKIPS_BOX=f"{L} {L} {L}"), stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:]
+    assert (d / "I00000000.xyz").read_text() == (tmp_path / "ora.xyz").read_text()
+    assert int((d / "I00000001.xyz").read_text().splitlines()[0].split()[-1]) >= 4000

@@ -416,3 +416,55 @@ def test_config2_faceted_etch_matches_serial_reference(tmp_path):
     atoms0 = int(((xyz[:, 2] > 3) & (xyz[:, 2] < C2_SIDE - 4)).sum())
     assert 0.1 * atoms0 < atoms0 - np.mean([r["atoms"] for r in ref]) < 0.6 * atoms0
     fam.check()
+
+
+# ---------------------------------------------------------------- InitSt E: SetSiCSF
+@pytest.mark.parametrize("pzig", ["1.0", "0.5362"])
+def test_sicsf_matches_oracle_and_replays(oracle_lib, tmp_path, pzig):
+    """InitSt E (SetSiCSF.f: a 3C-SiC slab holding a triangular triple
+    stacking fault, its atoms off the diamond sites) on the explicit-neighbour
+    engine, at PtransZig = 1 (explicit_nn) and 0.5362: after the initializer
+    the engine holds the oracle's LattCoo word for word and its list entries
+    (NextN in order, event codes, FP32 rates); the oracle's event trace from
+    there then replays exactly, chunk by chunk (a 120^3 box, vertex (24, 24,
+    36), the cube-zigzag SiC rates, RunType T)."""
+    from test_shape_points import sicsf_startdat
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300.startdat import parse_startdat
+    L = 120
+    p = tmp_path / "start.dat"
+    sicsf_startdat(p, 60, 24, 24, pzig)
+    d = parse_startdat(str(p))
+    o = oracle_lib.Oracle(str(p), L, L, L)
+    o.init()
+    pE, pD = o.rates()
+    lat = Lattice(L, L, L, ncrystal=2, list_crystal=d["list_crystal"], sf=d["sf"], ptrans_zig=d["ptrans_zig"],
+                  explicit_nn=True)
+    try:
+        lat.set_rates(pE, pD)
+        lat.init_shape("E", [60, 24, 24])
+        nmc, lg = compare_state(oracle_lib, o, lat, "after SetSiCSF")
+        z, y, x = np.nonzero(((lg >> 23) & 1) == 1)
+        assert nmc > 100 and ((x % 3 != 0) | (y % 3 != 0) | (z % 3 != 0)).sum() > 10
+        o.trace_enable()
+        done = 0
+        while done < 40000:
+            r = o.run(10000)
+            tr = o.trace()
+            lat.replay(tr)
+            done += len(tr)
+            compare_state(oracle_lib, o, lat, f"after {done} events")
+            if r:
+                break
+        assert done >= 40000
+    finally:
+        lat.close()
+        o.close()
+
+
+def test_sicsf_needs_the_explicit_engine():
+    from mulskips_gb300 import Lattice
+    from mulskips_gb300._native import MksError
+    with Lattice(120, 120, 120, ncrystal=2, list_crystal=(14, 6)) as lat:
+        with pytest.raises(MksError, match="explicit-neighbour"):
+            lat.init_shape("E", [60, 24, 24])

@@ -346,3 +346,75 @@ def test_oracle_variant_species_rules(oracle_lib, tmp_path):
     assert np.array_equal(st["Z"] & 0xFC, st["D"] & 0xFC)
     assert ((st["Z"][occ] & 3) == 1).all() and ((st["D"][occ] & 3) == 2).all()
     assert np.array_equal(occ, (st["D"] & 3) != 0)
+
+
+@pytest.fixture(scope="module")
+def sicsf_lib(tmp_path_factory):
+    import ctypes
+    so = str(tmp_path_factory.mktemp("native") / "sicsf_check.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                    os.path.join(ROOT, "tests", "native", "sicsf_check.cpp")], check=True)
+    L = ctypes.CDLL(so)
+    L.sicsf_build.restype = ctypes.c_longlong
+    return L
+
+
+def sicsf_startdat(path, len1, len2, len3, pzig="1.0"):
+    """The cube-zigzag start.dat with InitSt E and the given Len1 Len2 Len3
+    (SetSiCSF's slab height and the fault's vertex (Len2, Len3, Len1 -
+    Len2), main.f:267-272)."""
+    lines = open(os.path.join(GOLDEN, "cube-zigzag", "start.dat")).read().splitlines()
+    lines[2] = "E ! Initstat"
+    lines[3] = f"{len1} {len2} {len3} ! Len1 Len2 Len3"
+    lines = [l.replace("0.8 ! PtransZig", f"{pzig} ! PtransZig") for l in lines]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def sicsf_library(lib, L, len1, len2, len3):
+    import ctypes
+    cap = 4 * L * L * L // 27 + 1024
+    lc = np.zeros((L + 1, L, L), np.int32)
+    xyz = np.zeros((cap, 3), np.int32)
+    nn = np.zeros((cap, 4, 3), np.int32)
+    kind = np.zeros(cap, np.int32)
+    msg = ctypes.create_string_buffer(256)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    n = lib.sicsf_build(L, L, L, len1, len2, len3, len1 - len2, p(lc), p(xyz), p(nn), p(kind), ctypes.c_longlong(cap),
+                        msg, 256)
+    return n, msg.value.decode(), lc, xyz[:max(n, 0)], nn[:max(n, 0)], kind[:max(n, 0)]
+
+
+@pytest.mark.parametrize("lens", [(60, 24, 24), (96, 36, 12), (84, 24, 48)])
+def test_sicsf_equals_oracle(sicsf_lib, oracle_lib, tmp_path, lens):
+    """InitSt E (SetSiCSF, a triangular triple stacking fault in 3C-SiC):
+    the library's host builder (mulskips_gb300/csrc/sicsf.h) gives the
+    oracle's LattCoo word for word and its ListAdAtom and ListAtom entry for
+    entry, in order, NextN order included (a 120^3 box, three vertices)."""
+    L = 120
+    sicsf_startdat(tmp_path / "start.dat", *lens)
+    o = oracle_lib.Oracle(str(tmp_path / "start.dat"), L, L, L)
+    o.init()
+    ref_lc = o.lattcoo()
+    ref = oracle_lib.list_entries(o)
+    o.close()
+    n, msg, lc, xyz, nn, kind = sicsf_library(sicsf_lib, L, *lens)
+    assert n >= 0, msg
+    assert np.array_equal(lc, ref_lc[:L + 1])
+    assert (ref["kind"] == 3).sum() == 0
+    assert n == len(ref["kind"])
+    assert np.array_equal(kind, ref["kind"]) and np.array_equal(xyz, ref["xyz"]) and np.array_equal(nn, ref["nn"])
+    z, y, x = np.nonzero(((lc >> 23) & 1) == 1)
+    assert ((x % 3 != 0) | (y % 3 != 0) | (z % 3 != 0)).sum() > 10      # the fault's atoms are off the sub-grid
+
+
+def test_sicsf_refuses_what_the_reference_stops_on(sicsf_lib, oracle_lib, tmp_path):
+    L = 120
+    for lens, text in (((60, 27, 24), "wrong Site"), ((60, 108, 24), "SF dimension")):
+        n, msg, *_ = sicsf_library(sicsf_lib, L, *lens)
+        assert n < 0 and text in msg, msg
+        sicsf_startdat(tmp_path / "start.dat", *lens)
+        o = oracle_lib.Oracle(str(tmp_path / "start.dat"), L, L, L)
+        with pytest.raises(Exception):
+            o.init()
+        o.close()
